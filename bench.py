@@ -1,0 +1,269 @@
+"""Benchmark of the twin's rendering hot path on GB300.
+
+Metric (one JSON line): path Msamples/s of the plain FP32 path tracer on the seeded synthetic dome
+(640 x 480 KB4 camera, 16 spp, depth 4, ~12.4k triangles), with the node-radiosity solve times beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours: K frames rendered by libvtwin's persistent path-tracing kernel, each timed with CUDA events on the library's
+stream, L2 flushed (a 256 MB write) between frames, clocks sampled during the timed region. `e2e` repeats the
+frames through the public API with the pose upload (host -> device) and the radiance copy back (device -> host)
+inside the timed region. reference: the reference's CPU path restated in C++ (oracle/, FP32, all host threads) on a
+bounded sample of the same frame; the reference itself is JavaScript + WebGPU and runs on neither machine.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "veridien-twin_gb300"))
+
+METRIC = "path Msamples/s and radiosity solve ms at 1e-4 rel err vs FP64, plain vs mixed"
+W_, H_, SPP, DEPTH, NL = 640, 480, 16, 4, 1
+WORKLOAD = "C0 synthetic dome path tracer: 640x480 KB4 camera, 16 spp, depth 4, 1 light sample, ~12.4k tris"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    Q = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.rows, self.index, self.p = [], index, None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+        return self
+
+    def _read(self):
+        for line in self.p.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if "Active" in r[3 + k] and "Not" not in r[3 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def cpu_baseline(threads=None, rows=96, fp64=False):
+    """The reference's CPU path (restated in C++: oracle/) on a bounded sample: `rows` image rows spread over the
+    frame, all host threads. Returns (Msamples/s, info, counters)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from vtwin import _abi as A
+    from vtwin import dome
+
+    scene = dome.make_dome_scene(seed=1)
+    S = O.Scene(scene)
+    S.set_poses(A.identity_poses(1))
+    q = A.vt_render_req(camera=0, spp=SPP, light_samples=NL, seed=0, options=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
+    q.shutter[:] = [0.0, 1.0]
+    q.scale = 1.0
+    threads = threads or os.cpu_count() or 1
+    step = max(1, H_ // rows)
+    t0 = time.perf_counter()
+    n = 0
+    for y in range(0, H_, step):
+        S.render(q, y0=y, y1=y + 1, fp64=fp64, threads=threads)
+        n += W_ * SPP
+    dt = time.perf_counter() - t0
+    return n / dt / 1e6, {"rows": len(range(0, H_, step)), "samples": n, "seconds": dt, "threads": threads}
+
+
+def traffic_per_sample():
+    """Algorithmic bytes per camera sample, counted on the oracle's traversal of a sample of the same frame:
+    64 B per BVH node visited, 48 B (v0, e1, e2) per triangle tested, plus 256 B of shading fetches per hit
+    (triangle record, three vertex normals, material, two albedo-table bins)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from vtwin import _abi as A
+    from vtwin import dome
+
+    scene = dome.make_dome_scene(seed=1)
+    S = O.Scene(scene)
+    S.set_poses(A.identity_poses(1))
+    q = A.vt_render_req(camera=0, spp=SPP, light_samples=NL, seed=0, options=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
+    q.shutter[:] = [0.0, 1.0]
+    q.scale = 1.0
+    visits = tests = hits = 0
+    n = 0
+    for y in range(0, H_, 40):
+        _, dbg = S.render(q, y0=y, y1=y + 1, fp64=False, threads=os.cpu_count() or 1)
+        visits += int(dbg[8]); tests += int(dbg[9]); hits += int(dbg[10])
+        n += W_ * SPP
+    return (64 * visits + 48 * tests + 256 * hits) / n, {"node_visits_per_sample": visits / n, "tri_tests_per_sample": tests / n,
+                                                         "hits_per_sample": hits / n}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, info = cpu_baseline()
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": info["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dome, mulberry32)",
+            "config": {"workload": WORKLOAD, "spp": SPP, "depth": DEPTH, "width": W_, "height": H_},
+            "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": info["threads"], "kind": "port",
+                             "sample": f"{info['rows']} of {H_} rows x {W_} px x {SPP} spp per step ({info['samples']} samples)"},
+            "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-radiosity", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from vtwin import _abi as A
+    from vtwin import dome
+    from vtwin.renderer import TwinRenderer, solve_radiosity, form_factors
+
+    # replicas: every rank renders its own frame of the same workload (views shard with no exchange)
+    scene = dome.make_dome_scene(seed=1)
+    r = TwinRenderer.create(scene, device=local)
+    poses = A.identity_poses(1)
+    r.set_pose_array(poses)
+    stream = torch.cuda.ExternalStream(r.lib.vt_stream(r._ctx))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    kw = dict(spp=SPP, lightSamples=NL, seed=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
+    for _ in range(args.warmup):
+        r.renderCamera(0, **kw)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches0 = r.timings()["launches"]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.fill_(float(k))                 # L2 flush between timed frames (not timed)
+            torch.cuda.synchronize()
+            evs[k][0].record(stream)
+            r.renderCamera(0, **kw)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    launches = r.timings()["launches"] - launches0
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    samples = W_ * H_ * SPP * args.steps * world
+    value = samples / (ms / 1e3) / 1e6
+    # end to end through the public API: pose upload + render + radiance copy to pinned host memory
+    host = torch.empty((H_, W_, 4), dtype=torch.float32).pin_memory()
+    hnp = host.numpy()
+    T0 = np.ascontiguousarray(poses)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        r.set_pose_array(T0)
+        r.renderCamera(0, out=hnp, **kw)
+    e2e_s = time.perf_counter() - t0
+    e2e = W_ * H_ * SPP * args.steps * world / e2e_s / 1e6
+    line = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded dome, mulberry32)",
+            "config": {"workload": WORKLOAD, "width": W_, "height": H_, "spp": SPP, "depth": DEPTH, "light_samples": NL,
+                       "l2": "flushed between timed frames (256 MB write)", "parallelism": "replicas" if world > 1 else "single"},
+            "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 24 * 4 + 48 * 4 * 24 + 16 * 8,
+                    "d2h_bytes_per_step": W_ * H_ * 16},
+            "gpu_launches": int(launches), "clocks": clk.summary()}
+    if rank == 0:
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except (OSError, ValueError):
+            pass
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        if not args.no_cpu_baseline:
+            bps, cnt = traffic_per_sample()
+            per_launch = bps * W_ * H_ * SPP
+            ach = per_launch / (ms / args.steps / 1e3) / 1e9
+            line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                                "kernel": "render_kernel", "bytes_per_sample": bps, "note": "algorithmic bytes (BVH nodes, triangles, "
+                                "shading fetches) counted by the oracle on the same frame; the scene is L2-resident",
+                                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", **cnt}
+            cv, info = cpu_baseline()
+            line["cpu_baseline"] = {"value": cv, "unit": "Msamples/s", "cores": info["threads"], "kind": "port",
+                                    "sample": f"{info['rows']} of {H_} rows x {W_} px x {SPP} spp ({info['samples']} samples, {info['seconds']:.1f} s)"}
+        if not args.no_radiosity:
+            line["radiosity"] = radiosity_bench(solve_radiosity, form_factors, torch)
+        print(json.dumps(line))
+    r.destroy()
+    if dist:
+        dist.destroy_process_group()
+
+
+def radiosity_bench(solve, ff, torch):
+    """C1: N = 4096 patches, 1 right-hand side, plain FP32 Jacobi to 1e-6 relative residual (device time)."""
+    from vtwin import dome
+
+    out = {}
+    P = dome.dome_patches(4096, seed=2)
+    F = torch.empty((4096, 4096), dtype=torch.float32, device="cuda")
+    ff(P["centres"], P["normals"], P["areas"], out=F)
+    E = dome.radiosity_rhs(4096, P["lamps"], 1)
+    solve(F, P["rho"], E, tol=1e-6)                      # warm
+    B, info = solve(F, P["rho"], E, tol=1e-6)
+    out["c1_fp32_ms"] = info["ms"]
+    out["c1_iters"] = info["iters"]
+    out["c1_residual"] = info["residual"]
+    return out
+
+
+if __name__ == "__main__":
+    main()

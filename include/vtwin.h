@@ -1,0 +1,284 @@
+/*
+ * vtwin.h - C ABI of the GB300 (sm_103a) rendering hot path of the veridien dome twin.
+ *
+ * The reference is a WebGPU/JavaScript renderer. Each entry point below replaces one JavaScript interface of it
+ * (cited as file:line of the reference project). Rules for every call:
+ *   - return a vt_status (no exceptions cross the ABI); vt_last_error(ctx) describes the last failure;
+ *   - caller-owned host buffers, library-owned device buffers; a pointer argument documented as "host or device"
+ *     is classified by the CUDA runtime (cudaPointerGetAttributes);
+ *   - one CUDA stream per context; a context is not thread-safe;
+ *   - every device-side loop is bounded: a loop cap that is hit is counted (vt_debug_flags) and a bounded wait that
+ *     runs out returns VT_ERR_TIMEOUT, never a hang.
+ */
+#ifndef VTWIN_H
+#define VTWIN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t vt_status;
+enum {
+  VT_OK = 0,
+  VT_ERR_ARG = 1,            /* bad argument (null pointer, size out of range) */
+  VT_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+  VT_ERR_OOM = 3,            /* device allocation failed */
+  VT_ERR_TIMEOUT = 4,        /* a bounded device wait ran out */
+  VT_ERR_STATE = 5,          /* call out of order (e.g. readback before render) */
+  VT_ERR_UNKNOWN_CAMERA = 6, /* gpu/renderer.js:857 "unknown camera" */
+  VT_ERR_TOO_MANY_BODIES = 7,/* gpu/renderer.js:655 "too many bodies" */
+  VT_ERR_NO_DEVICE = 8,      /* no CUDA device: the library has no CPU fallback */
+  VT_ERR_NOT_CONVERGED = 9   /* a solve stopped at max_iters above its tolerance (results are still written) */
+};
+
+#define VT_MAX_INST 24          /* gpu/wgsl/common.wgsl.js:5 MAX_INST */
+#define VT_NODE_WORDS 16        /* gpu/bvh.js:11 NODE_WORDS */
+#define VT_ALBEDO_BINS 32       /* gpu/scene_gpu.js:15 ALBEDO_BINS */
+#define VT_MISS 0xffffffffu     /* gpu/wgsl/common.wgsl.js:32 MISS */
+
+/* mesh flags, gpu/scene_gpu.js:14 MESH_FLAG */
+enum { VT_F_STATIC = 1, VT_F_EMITTER = 2, VT_F_LAYER = 4, VT_F_BOARD = 8, VT_F_INSTRUMENT = 16, VT_F_SCOPE = 32,
+       VT_F_BENCH = 64, VT_F_TEXTURED = 128 };
+
+/* camera option bits, gpu/renderer.js:26 OPTION_BITS (the cache bits 2048/4096/8192 are accepted and ignored:
+ * the first-hit and static-occlusion caches are a WebGPU-era device; see the render request) */
+enum { VT_O_CUT = 1, VT_O_AID = 2, VT_O_NO_INDIRECT = 4, VT_O_DIRECT_ONLY = 8, VT_O_LAYER = 16, VT_O_NO_CAPSULE = 32,
+       VT_O_NORMALS = 64, VT_O_NO_MIS = 128, VT_O_SPEC_STATIC = 256, VT_O_PACKET = 512, VT_O_REFINE_SHADOW = 1024 };
+
+/* body kinds (gpu/scene_gpu.js:218-235 bodyOfPart) */
+enum { VT_BODY_INSTRUMENT = 0, VT_BODY_SCOPE = 1, VT_BODY_BOARD = 2, VT_BODY_FIXED = 3, VT_BODY_FIXTURE = 4 };
+
+typedef struct vt_ctx vt_ctx;
+
+/* ---------------------------------------------------------------------------------------------- scene input */
+
+/* One row of the mesh table (gpu/scene_gpu.js:252-255; packed as at gpu/renderer.js:279-285). */
+typedef struct {
+  uint32_t mat;          /* material index */
+  uint32_t flags;        /* VT_F_* */
+  float build_dir[3];    /* FDM build direction (layer lines) */
+  float layer_period;    /* m, 0 = no layer lines */
+  float layer_depth;     /* m */
+} vt_mesh;
+
+/* A material as gpu/bsdf.js:68 prepareMaterial receives it (values unwrapped from physics.yaml). */
+typedef struct {
+  int32_t metallic;       /* 0 dielectric, 1 conductor */
+  int32_t coated;         /* 1 coated conductor (metallic 2) */
+  int32_t emitter;        /* 1 the emitter material */
+  int32_t no_table;       /* 1 no directional-albedo table (the emitter body's own material, scene_gpu.js:323) */
+  float rho[3];           /* rho_d (dielectric) */
+  float f0[3];            /* conductor / coated-conductor F0 */
+  float roughness;        /* clamped to >= 0.02 as prepareMaterial does */
+  float ior;              /* dielectric IOR */
+  float fbar;             /* NaN: computed by fresnelAverage (gpu/bsdf.js:35) */
+  float coat_ior, coat_roughness;
+  float tau[3];           /* coat transmittance per normal pass */
+  int32_t textured;       /* charuco print: ink values below (the print mask itself is a 1x1 white texture) */
+  float ink_rho[3];
+  float ink_roughness;
+} vt_material;
+
+/* A posed body: one BLAS built in the body frame (gpu/scene_gpu.js:316-349). */
+typedef struct {
+  const float* P;          /* n_verts x 3 */
+  const float* N;          /* n_verts x 3 */
+  const uint32_t* I;       /* n_tris x 3, indices into this body's vertices */
+  const uint32_t* tri_mesh;/* n_tris mesh ids */
+  const float* UV;         /* n_verts x 2, may be NULL */
+  uint32_t n_verts, n_tris;
+  int32_t kind;            /* VT_BODY_* */
+  int32_t owner_camera;    /* camera index whose own rays skip this body (a lens front), -1 none */
+} vt_body_desc;
+
+/* A KB4 camera (scene.json cameras[]: lens {model 'kb4', K, D, size}, T_D_C), gpu/lens.js:8 lensParams. */
+typedef struct {
+  uint32_t width, height;
+  double fx, fy, cx, cy, alpha;   /* alpha = K[0][1] / fx */
+  double k[4];
+  double T_D_C[16];               /* row-major 4x4: camera-to-dome */
+} vt_camera_desc;
+
+/* The welded scene (gpu/scene_gpu.js:241 prepareScene input after weld + subdivide of the static meshes). */
+typedef struct {
+  const float* static_P;          /* n_static_verts x 3; every static vertex is a radiosity node */
+  const float* static_N;
+  const uint32_t* static_I;       /* n_static_tris x 3 */
+  const uint32_t* static_tri_mesh;
+  const uint32_t* static_vert_mesh;
+  uint32_t n_static_verts, n_static_tris;
+  const vt_body_desc* bodies; uint32_t n_bodies;
+  const vt_mesh* meshes; uint32_t n_meshes;
+  const vt_material* materials; uint32_t n_materials;
+  float L0[3];                    /* emitter radiance scale */
+  const float* profile_theta;     /* radians, ascending */
+  const float* profile_p;
+  uint32_t n_profile;
+  float axis_deg;                 /* emission axis angle from the scope shaft, NaN: the emitter's mean normal */
+  const vt_camera_desc* cameras; uint32_t n_cameras;
+} vt_scene_desc;
+
+typedef struct {
+  uint32_t leaf_size;    /* BVH leaf size (gpu/renderer.js:51 DEFAULTS.leafSize = 4) */
+  uint32_t albedo_samples; /* VNDF samples per albedo-table bin (gpu/scene_gpu.js:197 uses 1024) */
+  int32_t device;        /* CUDA device ordinal */
+} vt_options;
+
+/* gpu/renderer.js:202 TwinRenderer.create (+ gpu/scene_gpu.js:241 prepareScene without weld/subdivide). */
+vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx** out);
+/* gpu/renderer.js:1278 destroy */
+vt_status vt_destroy(vt_ctx* ctx);
+/* last error message of this context (static text if ctx is NULL) */
+const char* vt_last_error(const vt_ctx* ctx);
+
+/* Sizes of the packed scene: nodes (x16 words), triangles (x16 words), vertices (x8 words), params (x4 words),
+ * static vertices, bodies. gpu/scene_gpu.js:461-469 (prepareScene's return value). */
+typedef struct {
+  uint32_t node_count, tri_count, vert_count, param_vec4s, static_verts, static_tris, n_bodies, n_materials,
+           n_meshes, emit_tris;
+  uint32_t mesh_off, mat_off, alb_off, prof_off, prof_n, emit_off;
+  float emit_area, emit_axis[3], emit_normal[3], emit_centroid[3], emit_radius;
+  int32_t shadow_skips_scope, scope_index;
+} vt_scene_info;
+vt_status vt_scene_info_get(const vt_ctx* ctx, vt_scene_info* out);
+/* Copy the packed scene arrays to host buffers (any may be NULL): nodes, tris, verts, params. */
+vt_status vt_scene_export(const vt_ctx* ctx, uint32_t* nodes, uint32_t* tris, uint32_t* verts, float* params);
+/* Per-body BLAS record: root node, first triangle, triangle count, local bounds, capsules, rho_eff. */
+typedef struct { uint32_t root, tri_off, tri_count; float bmin[3], bmax[3]; float cap_a[3], cap_b[3], cap_r;
+                 float occ_a[3], occ_b[3], occ_r; float rho_eff; int32_t kind; } vt_blas_info;
+vt_status vt_blas_info_get(const vt_ctx* ctx, uint32_t body, vt_blas_info* out);
+
+/* --------------------------------------------------------------------------------------------------- poses */
+
+/* gpu/renderer.js:620 setPoses(poses0, poses1). T0/T1: n_bodies column-major 4x4 (doubles), body order of the
+ * scene; a NaN in T0[16*i] hides body i (no pose). T1 may be NULL (= T0). Writes the scene uniform
+ * (gpu/renderer.js:642 _writeSceneU). */
+vt_status vt_set_poses(vt_ctx* ctx, const double* T0, const double* T1, uint32_t n_bodies);
+/* Mean dome irradiance eAvg (rgb) read by a posed body's second bounce (gpu/renderer.js:848-850). */
+vt_status vt_set_eavg(vt_ctx* ctx, const float eavg[3]);
+/* Copy the packed scene uniform (96 + 24 x 192 bytes, gpu/renderer.js:28) to the host. */
+vt_status vt_scene_uniform_get(const vt_ctx* ctx, void* out, size_t bytes);
+
+/* Node radiosity state (16 floats per static vertex: E_free|V, Ls slot 1, Ls slot 2, B_dir|vis; gpu/renderer.js
+ * :316-326) and the latest slot (scene uniform info.z). state: host or device, n_static_verts x 16 floats. */
+vt_status vt_set_node_state(vt_ctx* ctx, const float* state, uint32_t slot);
+
+/* -------------------------------------------------------------------------------------------- ray queries */
+
+/* gpu/wgsl/kernels.wgsl.js:535 traceTest / gpu/wgsl/trace.wgsl.js:297 traceScene: n rays, o4 = (x, y, z, time),
+ * d4 = (dx, dy, dz, -); mask 1 static, 2 posed bodies, 3 both; out4 = (t, tri bits, inst bits, u) and out_v = v.
+ * Buffers are host or device. root: static BVH root (0 = full). Miss: t = 1e30, tri = inst = VT_MISS. */
+vt_status vt_trace_rays(vt_ctx* ctx, const float* o4, const float* d4, uint32_t n, uint32_t mask, uint32_t any_hit,
+                        uint32_t root, float* out4, float* out_v);
+
+/* gpu/renderer.js:1238 visible(name, pointsD, {tol, time}): occlusion from the camera centre to each point.
+ * pts: n x 3 doubles (host); out: n bytes (1 visible). Traced on the device. */
+vt_status vt_visible(vt_ctx* ctx, uint32_t camera, const double* pts, uint32_t n, double tol, double time,
+                     uint8_t* out);
+
+/* gpu/renderer.js:1261 project(name, pointsD): KB4 projection in float64 (gpu/lens.js:43). uv: n x 2. */
+vt_status vt_project(vt_ctx* ctx, uint32_t camera, const double* pts, uint32_t n, double* uv);
+
+/* ----------------------------------------------------------------------------------------------- rendering */
+
+enum { VT_SHADE_TWIN = 0,   /* gpu/wgsl/shade.wgsl.js:250 shadeHit: direct light + node radiosity (depth 2) */
+       VT_SHADE_PATH = 1 }; /* unidirectional path tracing to max_depth: NEE + BSDF continuation, power-heuristic MIS */
+
+/* gpu/renderer.js:975 renderCamera(name, {spp, refine, lightSamples, seed, shutter, exactShadows, ...}). */
+typedef struct {
+  uint32_t camera;         /* camera index */
+  uint32_t spp;            /* sub-samples per pixel (1..4096) */
+  uint32_t light_samples;  /* emitter samples per sub-sample (1..16) */
+  uint32_t seed;
+  uint32_t options;        /* VT_O_* */
+  uint32_t mode;           /* VT_SHADE_* */
+  uint32_t max_depth;      /* path vertices (VT_SHADE_PATH); 2 for VT_SHADE_TWIN */
+  uint32_t root;           /* static BVH root (0 = full) */
+  uint32_t frame;          /* frame counter (scene uniform info.w) */
+  float shutter[2];        /* exposure open/close in [0, 1] between poses0 and poses1 */
+  float scale;             /* output scale (gpu/renderer.js:888 _packCam expo.z; 1) */
+} vt_render_req;
+
+/* Render one camera into its device radiance image (rgba32f, w x h; alpha 0 where every sub-sample missed).
+ * out_rgba: NULL (stay on the device) or a host/device buffer of w*h*4 floats receiving a copy. */
+vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* req, float* out_rgba);
+
+/* gpu/renderer.js:1191 readback(name, 'linear'|'raw'): copy a camera's last radiance (rgba32f) or raw DN image
+ * (f32) into a host buffer of `bytes`. */
+enum { VT_READ_LINEAR = 0, VT_READ_RAW = 1 };
+vt_status vt_readback(vt_ctx* ctx, uint32_t camera, uint32_t kind, void* out, size_t bytes);
+
+/* ------------------------------------------------------------------------------------------------- sensor */
+
+/* The sensor uniform, gpu/sensor.js:158 packSensorUniform (the 256-byte SensU of gpu/wgsl/sensor.wgsl.js:20-32). */
+typedef struct { uint32_t words[64]; } vt_sensor_uniform;
+
+/* gpu/wgsl/sensor.wgsl.js:177 sensorExpose: irradiance image (rgba32f, host or device, w x h as the uniform says)
+ * -> raw DN (f32, host or device). Vertical optics blur, CFA site, Poisson shot + Gaussian read noise, full well,
+ * gain, black level, ADC. Veiling glare is off (fraction must be 0). */
+vt_status vt_sensor_expose(vt_ctx* ctx, const vt_sensor_uniform* su, const float* irradiance, float* raw);
+/* gpu/renderer.js:1092 sensor(name, opts) for the expose stage: the camera's last radiance (scaled by
+ * `optics_scale`, the pi T / (4 N^2) x RI factor, 1 for the configs' unit-radiance sensor) -> its raw DN image. */
+vt_status vt_sensor_camera(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, float optics_scale);
+
+/* -------------------------------------------------------------------------------------- node radiosity */
+
+enum { VT_PREC_FP32 = 0, VT_PREC_BF16 = 1, VT_PREC_FP8 = 2 };
+
+/* Dense node radiosity B = E + diag(rho) F B (the lite_nodes / TwinRenderer Jacobi, gpu/wgsl/kernels.wgsl.js
+ * :416-461 jacobiGather + jacobiUpdate with Lambertian nodes, gpu/renderer.js:729 _submitJacobi, :804 converge).
+ * FP32: plain Jacobi sweeps on CUDA cores. BF16 / FP8 (E4M3, per-row scales): tcgen05 GEMM sweeps with FP32
+ * accumulation, recovered by iterative refinement on an accurate residual r = E + rho F B - B (FP64 epilogue). */
+typedef struct {
+  uint32_t n;              /* nodes */
+  uint32_t n_rhs;          /* right-hand sides (columns of E and B) */
+  const float* F;          /* n x n row-major, host or device */
+  const float* rho;        /* n */
+  const float* E;          /* n x n_rhs row-major */
+  float* B;                /* n x n_rhs row-major out (in: warm start when warm_start = 1) */
+  uint32_t precision;      /* VT_PREC_* */
+  uint32_t max_iters;      /* total sweeps */
+  uint32_t warm_start;
+  uint32_t check_every;    /* sweeps between convergence checks (0 = 8) */
+  double tol;              /* relative residual ||r|| / ||B|| (Frobenius over all right-hand sides) */
+  /* outputs */
+  uint32_t iters;          /* sweeps done */
+  uint32_t refinements;    /* accurate residuals evaluated */
+  double residual;         /* final relative residual (accurate) */
+  double ms;               /* device time of the solve (CUDA events) */
+} vt_solve_req;
+vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* req);
+
+/* Dense form factors of n patches (centres, normals, areas; host or device, float32): the disk approximation
+ * F_ij = A_j max(0, n_i.w) max(0, -n_j.w) / (pi r^2 + A_j), F_ii = 0, rows scaled to sum <= 1. F: device or host
+ * n x n row-major. Unoccluded (the scene's visibility is not applied). */
+vt_status vt_form_factors(vt_ctx* ctx, uint32_t n, const float* centres, const float* normals, const float* areas,
+                          float* F);
+
+/* ---------------------------------------------------------------------------------------- bvh (pure) */
+
+/* gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}): binned SAH BVH2 on the host. nodes_out must hold
+ * vt_bvh_capacity(n_tris, leaf) * 16 words (= max(4, n_tris) nodes); order_out n_tris. Returns node count etc. */
+typedef struct { uint32_t node_count, max_depth; float bmin[3], bmax[3]; } vt_bvh_result;
+uint32_t vt_bvh_capacity(uint32_t n_tris, uint32_t leaf_size);
+vt_status vt_bvh_build(const float* pos, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris, uint32_t leaf_size,
+                       uint32_t* nodes_out, uint32_t* order_out, vt_bvh_result* res);
+
+/* -------------------------------------------------------------------------------------------- diagnostics */
+
+/* gpu/renderer.js:447 debugFlags(): loop-cap counters {traversalCap, leafCap, refined, refinedBody,
+ * refinedShadow, refinedSubsample, corruptTree, packetCap, ...} (16 words). reset = 1 clears them. */
+vt_status vt_debug_flags(vt_ctx* ctx, uint32_t out[16], int reset);
+/* gpu/renderer.js:1271 timings(): device ms of the last render, sensor and solve calls, and kernel launches. */
+typedef struct { double render_ms, sensor_ms, solve_ms, trace_ms; uint64_t launches; } vt_timings;
+vt_status vt_timings_get(const vt_ctx* ctx, vt_timings* out);
+/* The context's CUDA stream (cudaStream_t), for callers that order their own device work after ours. */
+void* vt_stream(vt_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VTWIN_H */

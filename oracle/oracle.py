@@ -1,0 +1,274 @@
+"""ORACLE loader - test infrastructure only (tests/, __graft_entry__.smoke(), bench.py's CPU-baseline leg).
+
+ctypes front of oracle/libvtoracle.so, the CPU restatement of the reference's rendering hot path
+(see vt_oracle.cpp for what it restates and why its parity is unpinned). Nothing in the product imports this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "veridien-twin_gb300"))
+from vtwin import _abi as A  # noqa: E402  (struct layouts of include/vtwin.h)
+
+LIB = os.path.join(HERE, "libvtoracle.so")
+_lib = None
+
+
+def build(force=False):
+    src = os.path.join(HERE, "vt_oracle.cpp")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+        _lib.or_scene_create.restype = C.c_void_p
+        _lib.or_scene_create.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        for nm in ("or_scene_destroy", "or_scene_sizes", "or_scene_arrays", "or_scene_emitter", "or_scene_blas",
+                   "or_scene_set_poses", "or_scene_set_eavg", "or_scene_uniform", "or_scene_set_node_state",
+                   "or_trace_wgsl", "or_render"):
+            getattr(_lib, nm).restype = None
+        _lib.or_fresnel_average.restype = C.c_double
+        _lib.or_disc_irradiance.restype = C.c_double
+        _lib.or_profile.restype = C.c_double
+        _lib.or_capsule_occ.restype = C.c_double
+        _lib.or_jacobi64.restype = C.c_int
+        _lib.or_bvh_build.restype = C.c_int
+    return _lib
+
+
+def _p(a, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def mulberry32(seed, n):
+    out = np.zeros(n, np.float64)
+    lib().or_mulberry32(C.c_uint32(seed), n, _p(out))
+    return out
+
+
+def unproject(lens, uv):
+    uv = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+    out = np.zeros((len(uv), 3))
+    lib().or_unproject(_p(np.ascontiguousarray(lens, np.float64)), len(uv), _p(uv), _p(out))
+    return out
+
+
+def project(lens, X):
+    X = np.ascontiguousarray(X, np.float64).reshape(-1, 3)
+    out = np.zeros((len(X), 2))
+    lib().or_project(_p(np.ascontiguousarray(lens, np.float64)), len(X), _p(X), _p(out))
+    return out
+
+
+def bvh_build(pos, idx, leaf=4):
+    pos = np.ascontiguousarray(pos, np.float32).ravel()
+    idx = np.ascontiguousarray(idx, np.uint32).ravel()
+    n = len(idx) // 3
+    cap = max(4, -(-n // max(1, leaf)) * 2) * 4 + 16
+    nodes = np.zeros(cap * 16, np.uint32)
+    order = np.zeros(max(1, n), np.uint32)
+    info = np.zeros(7)
+    cnt = lib().or_bvh_build(_p(pos, C.c_float), _p(idx, C.c_uint32), C.c_uint32(n), leaf, _p(nodes, C.c_uint32), cap,
+                             _p(order, C.c_uint32), _p(info))
+    assert cnt > 0, cnt
+    return {"nodes": nodes[: cnt * 16].copy(), "node_count": cnt, "order": order[:n].copy(), "max_depth": int(info[0]),
+            "bmin": info[1:4].copy(), "bmax": info[4:7].copy()}
+
+
+def pack_triangles(pos, idx, order):
+    pos = np.ascontiguousarray(pos, np.float32).ravel()
+    idx = np.ascontiguousarray(idx, np.uint32).ravel()
+    order = np.ascontiguousarray(order, np.uint32)
+    T = np.zeros(len(order) * 16, np.float32)
+    lib().or_pack_triangles(_p(pos, C.c_float), _p(idx, C.c_uint32), _p(order, C.c_uint32), C.c_uint32(len(order)), _p(T, C.c_float))
+    return T
+
+
+def traverse_js(nodes, T, o, d, tmin=0.0, tmax=np.inf, any_hit=False, root=0):
+    """gpu/bvh.js:224 traverse in float64: returns (t, u, v, tri) arrays."""
+    o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(d, np.float32).reshape(-1, 3)
+    out = np.zeros((len(o), 4))
+    lib().or_traverse_js(_p(np.ascontiguousarray(nodes, np.uint32), C.c_uint32), _p(np.ascontiguousarray(T, np.float32), C.c_float),
+                         len(o), _p(o, C.c_float), _p(d, C.c_float), C.c_double(tmin), C.c_double(tmax), int(any_hit),
+                         C.c_uint32(root), _p(out))
+    return out[:, 0], out[:, 1], out[:, 2], out[:, 3].astype(np.int64)
+
+
+def brute_force(T, count, o, d, tmin=0.0, tmax=np.inf):
+    o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(d, np.float32).reshape(-1, 3)
+    out = np.zeros((len(o), 4))
+    lib().or_brute_force(_p(np.ascontiguousarray(T, np.float32), C.c_float), C.c_uint32(count), len(o), _p(o, C.c_float),
+                         _p(d, C.c_float), C.c_double(tmin), C.c_double(tmax), _p(out))
+    return out[:, 0], out[:, 1], out[:, 2], out[:, 3].astype(np.int64)
+
+
+def fresnel_average(eta):
+    return lib().or_fresnel_average(C.c_double(eta))
+
+
+def disc_irradiance(x, n, c, m, a, L, nr=48, nphi=96):
+    f = lambda v: _p(np.ascontiguousarray(v, np.float64))
+    return lib().or_disc_irradiance(f(x), f(n), f(c), f(m), C.c_double(a), C.c_double(L), nr, nphi)
+
+
+def profile(theta, knots, p):
+    knots = np.ascontiguousarray(knots, np.float64)
+    p = np.ascontiguousarray(p, np.float64)
+    return lib().or_profile(C.c_double(theta), _p(knots), _p(p), len(knots))
+
+
+def capsule_occ(p, n, a, b, r):
+    f = lambda v: _p(np.ascontiguousarray(v, np.float64))
+    return lib().or_capsule_occ(f(p), f(n), f(a), f(b), C.c_double(r))
+
+
+def bsdf_eval(material: dict, cases):
+    m = A.material_struct(material)
+    cases = np.ascontiguousarray(cases, np.float64).reshape(-1, 12)
+    out = np.zeros((len(cases), 8))
+    lib().or_bsdf_eval(C.byref(m), len(cases), _p(cases), _p(out))
+    return out
+
+
+def albedo_table(material: dict, samples=1024):
+    m = A.material_struct(material)
+    out = np.zeros(32 * 6 + 6)
+    lib().or_albedo_table(C.byref(m), samples, _p(out))
+    return {"spec": out[:96].reshape(32, 3), "diff": out[96:192].reshape(32, 3), "hh": out[192:195], "hhSpec": out[195:198]}
+
+
+class Scene:
+    """prepareScene restated (gpu/scene_gpu.js:241) + poses (gpu/renderer.js:620) + the estimator."""
+
+    def __init__(self, scene: dict, leaf=4, albedo_samples=1024):
+        self.sd = A.SceneDesc(scene)
+        self.h = C.c_void_p(lib().or_scene_create(self.sd.ref, leaf, albedo_samples))
+        self.scene = scene
+        sz = np.zeros(12, np.uint32)
+        lib().or_scene_sizes(self.h, _p(sz, C.c_uint32))
+        (self.node_count, self.tri_count, self.vert_count, self.param_vec4s, self.static_verts, self.mesh_off,
+         self.mat_off, self.alb_off, self.prof_off, self.prof_n, self.emit_off, self.emit_n) = [int(x) for x in sz]
+        self.n_bodies = len(scene.get("bodies", []))
+        self.slot, self.frame = 1, 0
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.or_scene_destroy(self.h)
+            self.h = None
+
+    def arrays(self):
+        nodes = np.zeros(self.node_count * 16, np.uint32)
+        tris = np.zeros(self.tri_count * 16, np.uint32)
+        verts = np.zeros(self.vert_count * 8, np.uint32)
+        params = np.zeros(self.param_vec4s * 4, np.float32)
+        lib().or_scene_arrays(self.h, _p(nodes, C.c_uint32), _p(tris, C.c_uint32), _p(verts, C.c_uint32), _p(params, C.c_float))
+        return {"nodes": nodes, "tris": tris, "verts": verts, "params": params}
+
+    def emitter(self):
+        out = np.zeros(13)
+        lib().or_scene_emitter(self.h, _p(out))
+        return {"area": out[0], "axis": out[1:4], "normal": out[4:7], "centroid": out[7:10], "radius": out[10],
+                "shadow_skips_scope": bool(out[11]), "scope_index": int(out[12])}
+
+    def blas(self, i):
+        out = np.zeros(17)
+        lib().or_scene_blas(self.h, i, _p(out))
+        return {"root": int(out[0]), "tri_off": int(out[1]), "tri_count": int(out[2]), "bmin": out[3:6], "bmax": out[6:9],
+                "cap_a": out[9:12], "cap_b": out[12:15], "cap_r": out[15], "rho_eff": out[16]}
+
+    def set_poses(self, T0=None, T1=None):
+        T0 = A.identity_poses(self.n_bodies) if T0 is None else np.ascontiguousarray(T0, np.float64).reshape(-1, 16)
+        T1p = None if T1 is None else _p(np.ascontiguousarray(T1, np.float64).reshape(-1, 16))
+        self._T = (T0, T1)
+        lib().or_scene_set_poses(self.h, _p(T0), T1p, C.c_uint32(len(T0)), C.c_uint32(self.slot), C.c_uint32(self.frame))
+
+    def set_eavg(self, e):
+        e = np.ascontiguousarray(e, np.float32)
+        lib().or_scene_set_eavg(self.h, _p(e, C.c_float), C.c_uint32(self.slot), C.c_uint32(self.frame))
+
+    def set_node_state(self, st, slot=1):
+        st = np.ascontiguousarray(st, np.float32)
+        self.slot = slot
+        lib().or_scene_set_node_state(self.h, _p(st, C.c_float), C.c_uint32(slot), C.c_uint32(self.frame))
+
+    def uniform(self):
+        out = np.zeros(24 + 48 * 24, np.float32)
+        lib().or_scene_uniform(self.h, _p(out, C.c_float))
+        return out
+
+    def trace(self, o4, d4, mask=3, any_hit=False, root=0, fp64=True):
+        o4 = np.ascontiguousarray(o4, np.float32).reshape(-1, 4)
+        d4 = np.ascontiguousarray(d4, np.float32).reshape(-1, 4)
+        out = np.zeros((len(o4), 5))
+        dbg = np.zeros(16, np.uint64)
+        lib().or_trace_wgsl(self.h, len(o4), _p(o4, C.c_float), _p(d4, C.c_float), C.c_uint32(mask), int(any_hit),
+                            C.c_uint32(root), int(fp64), _p(out), _p(dbg, C.c_uint64))
+        return out, dbg
+
+    def render(self, req: "A.vt_render_req", y0=0, y1=None, x0=0, x1=None, fp64=True, threads=1):
+        cam = self.scene["cameras"][req.camera]
+        W, H = cam["size"]
+        y1 = H if y1 is None else y1
+        x1 = W if x1 is None else x1
+        out = np.zeros((y1 - y0, x1 - x0, 4))
+        dbg = np.zeros(16, np.uint64)
+        lib().or_render(self.h, C.byref(req), C.c_uint32(y0), C.c_uint32(y1), C.c_uint32(x0), C.c_uint32(x1), int(fp64),
+                        int(threads), _p(out), _p(dbg, C.c_uint64))
+        return out, dbg
+
+
+def sensor_expose(su_words, E4):
+    su = np.ascontiguousarray(su_words, np.uint32)
+    E4 = np.ascontiguousarray(E4, np.float32)
+    W, H = int(su[0]), int(su[1])
+    raw = np.zeros((H, W), np.float32)
+    lib().or_sensor_expose(_p(su, C.c_uint32), _p(E4, C.c_float), _p(raw, C.c_float))
+    return raw
+
+
+def vt_math(name, x):
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    getattr(lib(), "or_vt_" + name)(_p(x, C.c_float), len(x), _p(out, C.c_float))
+    return out
+
+
+def solve_dense(F, rho, E):
+    F = np.ascontiguousarray(F, np.float32)
+    n = F.shape[0]
+    E = np.ascontiguousarray(E, np.float32).reshape(n, -1)
+    B = np.zeros(E.shape, np.float64)
+    lib().or_solve_dense(n, _p(F, C.c_float), _p(np.ascontiguousarray(rho, np.float32), C.c_float), _p(E, C.c_float),
+                         E.shape[1], _p(B))
+    return B
+
+
+def jacobi64(F, rho, E, tol=1e-12, max_it=10000, threads=None):
+    F = np.ascontiguousarray(F, np.float32)
+    n = F.shape[0]
+    E = np.ascontiguousarray(E, np.float32).reshape(n, -1)
+    B = np.zeros(E.shape, np.float64)
+    it = lib().or_jacobi64(n, _p(F, C.c_float), _p(np.ascontiguousarray(rho, np.float32), C.c_float), _p(E, C.c_float),
+                           E.shape[1], _p(B), C.c_double(tol), max_it, threads or os.cpu_count() or 1)
+    return B, it
+
+
+def form_factors(C_, N_, A_):
+    C_ = np.ascontiguousarray(C_, np.float32)
+    n = len(C_)
+    F = np.zeros((n, n), np.float32)
+    lib().or_form_factors(n, _p(C_, C.c_float), _p(np.ascontiguousarray(N_, np.float32), C.c_float),
+                          _p(np.ascontiguousarray(A_, np.float32), C.c_float), _p(F, C.c_float))
+    return F

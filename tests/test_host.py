@@ -1,0 +1,95 @@
+"""Host logic of the product on CPU: the C-ABI library loads and exports every symbol include/vtwin.h declares,
+its host BVH builder reproduces gpu/bvh.js's node array word for word (checked against the oracle), the sensor
+uniform packing follows gpu/sensor.js:158, and without a GPU the library fails loudly (no CPU fallback)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import ROOT, has_gpu
+from vtwin import _abi as A
+from vtwin import _lib, dome
+from vtwin import sensor as S
+from vtwin.renderer import build_bvh
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "vtwin.h")).read()
+    # function declarations: a return type at the start of a line, then the vt_ name and its parameter list
+    return sorted(set(re.findall(r"^(?:vt_status|uint32_t|const char\*|void\*)\s+(vt_[a-z0-9_]+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) == set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize("leaf", [1, 2, 4, 8])
+def test_bvh_builder_matches_oracle_on_dome(dome_small, leaf):
+    st = dome_small["static"]
+    a = build_bvh(st["P"], st["I"], leaf)
+    b = O.bvh_build(st["P"], st["I"], leaf)
+    assert a["nodeCount"] == b["node_count"] and a["maxDepth"] == b["max_depth"]
+    assert np.array_equal(a["nodes"], b["nodes"]) and np.array_equal(a["order"], b["order"])
+
+
+def test_bvh_builder_matches_oracle_on_random_and_degenerate_meshes():
+    rng = np.random.default_rng(11)
+    for n in [0, 1, 2, 3, 5, 17, 100, 1000]:
+        P = rng.normal(size=(3 * max(n, 1), 3)).astype(np.float32)
+        I = np.arange(3 * n, dtype=np.uint32).reshape(-1, 3)
+        a, b = build_bvh(P, I), O.bvh_build(P, I)
+        assert np.array_equal(a["nodes"], b["nodes"]) and np.array_equal(a["order"], b["order"]), n
+    # coincident centroids, axis-aligned slivers, duplicated triangles
+    P = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 0], [0, 0, 0], [0, 0, 0]], np.float32)
+    for I in (np.tile([[0, 1, 2]], (50, 1)), np.tile([[3, 4, 5]], (9, 1)), np.array([[0, 1, 2], [0, 2, 1]])):
+        I = I.astype(np.uint32)
+        a, b = build_bvh(P, I), O.bvh_build(P, I)
+        assert np.array_equal(a["nodes"], b["nodes"]) and np.array_equal(a["order"], b["order"])
+
+
+def test_bvh_builder_rejects_bad_indices():
+    lib = _lib.load()
+    P = np.zeros((3, 3), np.float32)
+    I = np.array([[0, 1, 7]], np.uint32)
+    nodes = np.zeros(64, np.uint32)
+    order = np.zeros(1, np.uint32)
+    r = A.vt_bvh_result()
+    st = lib.vt_bvh_build(P.ctypes.data_as(C.c_void_p), 3, I.ctypes.data_as(C.c_void_p), 1, 4,
+                          nodes.ctypes.data_as(C.c_void_p), order.ctypes.data_as(C.c_void_p), C.byref(r))
+    assert st == A.VT_ERR_ARG
+
+
+def test_sensor_uniform_layout():
+    p = S.sensor_params({"cfa": "RGGB", "readNoise": 2.0, "adcBits": 12, "esfSigmaPx": 0.3})
+    u = S.pack_sensor_uniform(p, 640, 480, frame=3, seed=7, exposure=0.01, gain=2.0, cam_index=2)
+    f = u.view(np.float32)
+    assert list(u[:4]) == [640, 480, 0, 3] and u[26] == 7 and u[49] == 2
+    assert f[5] == pytest.approx(np.sqrt(0.3 ** 2 - 1 / 12), rel=1e-6)   # optics blur minus the pixel aperture
+    assert f[6] == pytest.approx(0.01) and f[7] == 2.0 and f[20] == 2.0 and f[24] == 4095.0 and f[27] == 1.0
+    assert f[4] == pytest.approx(np.pi * 0.9 / 16)
+
+
+def test_scene_descriptor_round_trip(dome_small):
+    d = A.SceneDesc(dome_small)
+    assert d.desc.n_static_tris == len(dome_small["static"]["I"]) and d.desc.n_bodies == 1
+    assert d.desc.n_materials == len(dome_small["materials"]) and d.desc.bodies[0].kind == A.BODY_KIND["scope"]
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-device path")
+def test_no_gpu_fails_loudly(dome_small):
+    lib = _lib.load()
+    d = A.SceneDesc(dome_small)
+    ctx = C.c_void_p()
+    assert lib.vt_create(d.ref, None, C.byref(ctx)) == A.VT_ERR_NO_DEVICE
+    from vtwin.renderer import TwinRenderer, VtError
+
+    with pytest.raises(VtError):
+        TwinRenderer.create(dome_small)

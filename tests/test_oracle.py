@@ -1,0 +1,233 @@
+"""The oracle pinned against the reference's known answers (CPU only).
+
+Golden vectors from the reference's own configuration (tests/golden/physics_kat.json, made by make_golden.py),
+and the known-answer methods the reference's source states: brute force judges the BVH (gpu/bvh.js:3),
+the KB4 round trip (gpu/lens.js:43-62), the Gauss-Legendre disc irradiance (gpu/shade_ref.js:40-62), the
+furnace (tools/gpu_bench.py:7), reciprocity, and the direct FP64 solve of the radiosity.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from vtwin import dome
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "physics_kat.json")))
+
+
+def test_fresnel_average_matches_reference_config():
+    # physics.yaml lists fresnel_avg "derived from ior" for 12 materials, rounded to 4 decimals
+    for p in GOLD["fresnel_avg"]:
+        assert round(O.fresnel_average(p["ior"]), 4) == pytest.approx(p["fresnel_avg"], abs=1e-12), p
+
+
+def test_profile_projected_solid_angle_matches_reference_config():
+    pr = GOLD["profile"]
+    th, pp = np.radians(pr["theta_deg"]), np.array(pr["p"], float)
+    x = np.linspace(0.0, math.pi / 2, 4001)
+    y = np.array([O.profile(t, th, pp) for t in x])
+    psa = 2 * math.pi * np.trapezoid(y * np.cos(x) * np.sin(x), x)
+    assert psa == pytest.approx(pr["projected_solid_angle"], abs=2e-6)
+    # p = 0 past the last knot, p(last) exactly at it (gpu/shade_ref.js:7)
+    assert O.profile(th[-1] + 1e-9, th, pp) == 0.0 and O.profile(th[-1], th, pp) == pp[-1]
+
+
+def test_mulberry32_two_restatements_agree():
+    a = O.mulberry32(12345, 1000)
+    g = dome.mulberry32(12345)
+    b = np.array([g() for _ in range(1000)])
+    assert np.array_equal(a, b)
+    assert (a >= 0).all() and (a < 1).all() and abs(a.mean() - 0.5) < 0.03
+
+
+def test_kb4_round_trip():
+    lens = np.array([300.0, 301.0, 319.5, 239.5, 0.001, 0.05, -0.01, 0.002, -0.0003])
+    rng = np.random.default_rng(0)
+    uv = np.stack([rng.uniform(-0.5, 639.5, 500), rng.uniform(-0.5, 479.5, 500)], 1)
+    rays = O.unproject(lens, uv)
+    assert np.allclose(np.linalg.norm(rays, axis=1), 1.0, atol=1e-12)
+    back = O.project(lens, rays * 2.5)
+    assert np.abs(back - uv).max() < 1e-9
+    # the principal point maps to the optical axis
+    assert np.allclose(O.unproject(lens, [[319.5, 239.5]]), [[0, 0, 1]])
+
+
+def test_disc_irradiance_on_axis_closed_form():
+    # a point on the axis of a Lambertian disc (radius a, distance d), normal facing it: E = pi L a^2 / (a^2 + d^2)
+    for a, d in [(0.1, 0.5), (0.3, 0.2), (1.0, 1.0)]:
+        E = O.disc_irradiance([0, 0, 0], [0, 0, 1], [0, 0, d], [0, 0, -1], a, 2.0)
+        assert E == pytest.approx(math.pi * 2.0 * a * a / (a * a + d * d), rel=1e-9)
+
+
+def _cylinder_occ_quadrature(p, n, a, b, r, m=20000):
+    # the thin-cylinder integral the closed form evaluates: (1/pi) int (2r/h) cos(phi) max(0, n.omega(phi)) dphi
+    ab = np.subtract(b, a)
+    L = np.linalg.norm(ab)
+    e = ab / L
+    ap = np.subtract(p, a)
+    s0 = ap @ e
+    perp = ap - s0 * e
+    h = math.sqrt(perp @ perp + r * r)
+    ep = -perp / max(np.linalg.norm(perp), 1e-12)
+    f1, f2 = math.atan(-s0 / h), math.atan((L - s0) / h)
+    phi = np.linspace(f1, f2, m)
+    om = np.cos(phi)[:, None] * ep + np.sin(phi)[:, None] * e
+    g = np.cos(phi) * np.maximum(0.0, om @ n)
+    return min(1.0, max(0.0, (2 * r / h) * np.trapezoid(g, phi) / math.pi))
+
+
+def test_capsule_occlusion_matches_quadrature():
+    rng = np.random.default_rng(3)
+    for _ in range(40):
+        p = rng.normal(size=3) * 0.05
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        a, b = rng.normal(size=3) * 0.1, rng.normal(size=3) * 0.1
+        r = rng.uniform(0.001, 0.01)
+        assert O.capsule_occ(p, n, a, b, r) == pytest.approx(_cylinder_occ_quadrature(p, n, a, b, r), abs=2e-5)
+
+
+def test_bsdf_reciprocity_and_sampling_pdf():
+    mats = [dome.lambertian("l", [0.6, 0.4, 0.2]),
+            {**dome.lambertian("d", [0.6, 0.4, 0.2]), "ior": 1.5, "roughness": 0.3},
+            {**dome.lambertian("m", [0, 0, 0]), "metallic": 1, "f0": [0.9, 0.6, 0.3], "roughness": 0.4},
+            {**dome.lambertian("c", [0, 0, 0]), "coated": 1, "f0": [0.56, 0.57, 0.58], "roughness": 0.3,
+             "coat_ior": 1.5, "coat_roughness": 0.1, "tau": [0.9, 0.8, 0.7]}]
+    rng = np.random.default_rng(5)
+    for m in mats:
+        cases = []
+        for _ in range(200):
+            n = np.array([0, 0, 1.0])
+            l, v = rng.normal(size=3), rng.normal(size=3)
+            l[2], v[2] = abs(l[2]), abs(v[2])
+            cases.append(np.concatenate([n, l / np.linalg.norm(l), v / np.linalg.norm(v), rng.uniform(size=3)]))
+        cases = np.array(cases)
+        f_lv = O.bsdf_eval(m, cases)
+        swapped = cases.copy()
+        swapped[:, 3:6], swapped[:, 6:9] = cases[:, 6:9], cases[:, 3:6]
+        f_vl = O.bsdf_eval(m, swapped)
+        assert np.allclose(f_lv[:, :3], f_vl[:, :3], rtol=1e-10, atol=1e-14)  # reciprocity
+        # a sampled direction's pdf is pdfBSDF at that direction
+        ok = f_lv[:, 7] > 0
+        again = cases[ok].copy()
+        again[:, 3:6] = f_lv[ok, 4:7]
+        assert np.allclose(O.bsdf_eval(m, again)[:, 3], f_lv[ok, 7], rtol=1e-9)
+
+
+def test_albedo_table_furnace():
+    # Lambertian with ior 1: spec = 0, diffuse = rho in every bin, hemispherical albedo = rho (no energy lost)
+    t = O.albedo_table(dome.lambertian("l", [0.3, 0.5, 0.7]))
+    assert np.abs(t["spec"]).max() < 1e-15
+    assert np.allclose(t["diff"], [0.3, 0.5, 0.7]) and np.allclose(t["hh"], [0.3, 0.5, 0.7])
+    # a white conductor never creates energy, and near normal incidence at low roughness keeps almost all of it
+    c = O.albedo_table({**dome.lambertian("m", [0, 0, 0]), "metallic": 1, "f0": [1, 1, 1], "roughness": 0.1})
+    assert c["spec"].max() <= 1.0 + 1e-9 and c["spec"][-1].min() > 0.98
+
+
+def test_bvh_traverse_equals_brute_force(dome_small):
+    st = dome_small["static"]
+    b = O.bvh_build(st["P"], st["I"])
+    T = O.pack_triangles(st["P"], st["I"], b["order"])
+    rng = np.random.default_rng(7)
+    n = 3000
+    o = rng.uniform([-3, -3, 0.05], [3, 3, 3.5], (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    t1, _, _, k1 = O.traverse_js(b["nodes"], T, o, d)
+    t2, _, _, k2 = O.brute_force(T, len(st["I"]), o, d)
+    same = k1 == k2
+    # a tie is two triangles at the same t (shared edges): brute force keeps the first in slot order
+    assert (same | (np.abs(t1 - t2) <= 1e-9)).all()
+    assert np.array_equal(t1, t2)
+    # any-hit finds a hit exactly when closest-hit does
+    ta, _, _, ka = O.traverse_js(b["nodes"], T, o, d, any_hit=True)
+    assert np.array_equal(ka >= 0, k1 >= 0)
+
+
+def test_bvh_structure(dome_small):
+    st = dome_small["static"]
+    b = O.bvh_build(st["P"], st["I"])
+    W = b["nodes"].reshape(-1, 16)
+    F = W.view(np.float32)
+    seen = np.zeros(len(st["I"]), int)
+    for i, w in enumerate(W):
+        for c in (0, 1):
+            ref, cnt = w[8 * c + 3], w[8 * c + 7]
+            if cnt == 0:
+                assert ref > i  # children after the parent (gpu/wgsl/trace.wgsl.js:99)
+            else:
+                seen[ref:ref + cnt] += 1
+                lo, hi = F[i, 8 * c:8 * c + 3], F[i, 8 * c + 4:8 * c + 7]
+                tri = st["P"][st["I"][b["order"][ref:ref + cnt]]].reshape(-1, 3)
+                assert (tri >= lo).all() and (tri <= hi).all()
+    assert (seen == 1).all()  # every triangle in exactly one leaf
+    assert sorted(b["order"]) == list(range(len(st["I"])))
+
+
+def test_bvh_edge_cases():
+    P = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    one = O.bvh_build(P, np.array([[0, 1, 2]], np.uint32))
+    W = one["nodes"].reshape(-1, 16)
+    assert one["node_count"] == 1 and W[0, 7] == 1 and W[0, 15] == 1   # a single triangle: both children the same leaf
+    zero = O.bvh_build(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    assert zero["node_count"] == 1 and zero["nodes"].view(np.float32)[0] == np.float32(1e30)
+    # many triangles with one centroid: split in the middle when too big for a leaf (gpu/bvh.js:101-104)
+    I = np.tile(np.array([[0, 1, 2]], np.uint32), (40, 1))
+    same = O.bvh_build(P, I)
+    W = same["nodes"].reshape(-1, 16)
+    assert same["node_count"] > 1 and (W[:, [7, 15]] <= 16).all()
+
+
+def test_sensor_math_accuracy():
+    x = np.linspace(1e-7, 1.0, 20001, dtype=np.float32)
+    assert np.max(np.abs(O.vt_math("logf", x) - np.log(x.astype(np.float64))) / np.maximum(1e-30, np.abs(np.log(x.astype(np.float64))))) < 2e-6
+    y = np.linspace(-80.0, 0.0, 20001, dtype=np.float32)
+    assert np.max(np.abs(O.vt_math("expf", y) - np.exp(y.astype(np.float64))) / np.exp(y.astype(np.float64))) < 1e-6
+    u = np.linspace(0.0, 1.0, 20001, dtype=np.float32)
+    assert np.max(np.abs(O.vt_math("cos2pi", u) - np.cos(2 * np.pi * u.astype(np.float64)))) < 1e-6
+
+
+def test_sensor_expose_statistics():
+    from vtwin import sensor as S
+
+    W, H = 256, 256
+    p = S.unit_radiance_sensor()
+    su = S.pack_sensor_uniform(p, W, H, seed=9)
+    E = np.zeros((H, W, 4), np.float32)
+    E[..., :3] = 25.0  # 100 e- per pixel: the normal branch; and a dim half in the inversion branch
+    E[H // 2:, :, :3] = 2.5
+    raw = O.sensor_expose(su, E)
+    hi, lo = raw[: H // 2], raw[H // 2:]
+    assert abs(hi.mean() - 100.0) < 0.5 and abs(hi.var() - (100.0 + 4.0)) < 6.0
+    assert abs(lo.mean() - 10.0) < 0.2 and abs(lo.var() - (10.0 + 4.0)) < 1.2
+    assert np.array_equal(raw, O.sensor_expose(su, E))   # deterministic per seed / frame / camera
+    su2 = S.pack_sensor_uniform(p, W, H, seed=10)
+    assert not np.array_equal(raw, O.sensor_expose(su2, E))
+
+
+def test_radiosity_direct_and_jacobi_agree():
+    P = dome.dome_patches(300, seed=2)
+    F = O.form_factors(P["centres"], P["normals"], P["areas"])
+    assert (F >= 0).all() and F.sum(1).max() <= 1 + 1e-6 and np.all(np.diag(F) == 0)
+    E = dome.radiosity_rhs(300, P["lamps"], 4)
+    Bd = O.solve_dense(F, P["rho"], E)
+    Bj, it = O.jacobi64(F, P["rho"], E, tol=1e-13, max_it=5000, threads=2)
+    assert np.abs(Bj - Bd).max() / np.abs(Bd).max() < 1e-11
+    # the solution satisfies B = E + rho F B
+    r = E + P["rho"][:, None] * (F.astype(np.float64) @ Bd) - Bd
+    assert np.abs(r).max() < 1e-9 * np.abs(Bd).max()
+
+
+def test_form_factor_reciprocity_before_scaling():
+    P = dome.dome_patches(200, seed=4)
+    F = O.form_factors(P["centres"], P["normals"], P["areas"]).astype(np.float64)
+    s = F.sum(1)
+    unscaled = np.where(s[:, None] > 1, F * s[:, None], F)   # undo the row scaling
+    A = P["areas"].astype(np.float64)
+    lhs, rhs = A[:, None] * unscaled, (A[:, None] * unscaled).T
+    # the disk approximation is reciprocal up to its A_j in the denominator
+    big = lhs > 1e-6
+    assert np.median(np.abs(lhs[big] - rhs[big]) / lhs[big]) < 0.05

@@ -1,0 +1,542 @@
+// The C ABI of include/vtwin.h: contexts, device-resident scene, poses, rendering, ray queries, sensor and the
+// node-radiosity solve. One CUDA stream per context. There is no CPU fallback: without a device every entry
+// point that needs one returns VT_ERR_NO_DEVICE.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "vt_host.h"
+#include "vt_kernels.cuh"
+
+struct vt_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  vt::Prepared S;
+  std::vector<vt::InstPose> inst;
+  float eavg[3] = {0, 0, 0};
+  uint32_t slot = 1, frame = 0;
+  float su_host[vt::SU_WORDS];
+  // device scene
+  float4 *d_nodes = nullptr, *d_tris = nullptr, *d_verts = nullptr, *d_params = nullptr, *d_nstate = nullptr;
+  float* d_su = nullptr;
+  uint32_t* d_dbg = nullptr;
+  uint32_t* d_work = nullptr;   // tile counter of the persistent render kernel
+  int render_blocks = 0;
+  struct Cam { float4* radiance = nullptr; float* raw = nullptr; bool rendered = false, exposed = false; };
+  std::vector<Cam> cams;
+  // scratch for ray queries and the solver (grown on demand)
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  vt_timings tim{};
+};
+
+namespace {
+
+const char* g_static_err = "no context";
+
+#define VT_CK(call)                                                                  \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) return fail(ctx, VT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+vt_status fail(vt_ctx* ctx, vt_status s, const std::string& m) {
+  if (ctx) ctx->err = m;
+  return s;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+vt_status upload(vt_ctx* ctx, T** dst, const void* src, size_t bytes) {
+  VT_CK(cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(bytes, 16)));
+  if (bytes) VT_CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return VT_OK;
+}
+
+vt_status ensure_scratch(vt_ctx* ctx, size_t bytes) {
+  if (ctx->scratch_bytes >= bytes) return VT_OK;
+  if (ctx->d_scratch) { VT_CK(cudaStreamSynchronize(ctx->stream)); VT_CK(cudaFree(ctx->d_scratch)); ctx->d_scratch = nullptr; ctx->scratch_bytes = 0; }
+  cudaError_t e = cudaMalloc(&ctx->d_scratch, bytes);
+  if (e != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "scratch allocation of " + std::to_string(bytes) + " bytes failed"); }
+  ctx->scratch_bytes = bytes;
+  return VT_OK;
+}
+
+vtd::Scene dev_scene(vt_ctx* ctx) {
+  vtd::Scene S;
+  S.nodes = ctx->d_nodes; S.tris = ctx->d_tris; S.verts = ctx->d_verts; S.params = ctx->d_params;
+  S.su = ctx->d_su; S.nstate = ctx->d_nstate; S.dbg = ctx->d_dbg;
+  S.mesh_off = ctx->S.mesh_off; S.mat_off = ctx->S.mat_off; S.alb_off = ctx->S.alb_off; S.prof_off = ctx->S.prof_off;
+  S.prof_n = ctx->S.prof_n; S.emit_off = ctx->S.emit_off; S.emit_n = ctx->S.emit_n;
+  return S;
+}
+
+vt_status write_su(vt_ctx* ctx) {
+  vt::scene_uniform(ctx->S, ctx->inst, ctx->eavg, ctx->slot, ctx->frame, ctx->su_host);
+  VT_CK(cudaMemcpyAsync(ctx->d_su, ctx->su_host, sizeof(ctx->su_host), cudaMemcpyHostToDevice, ctx->stream));
+  return VT_OK;
+}
+
+uint32_t skip_mask(const vt_ctx* ctx, uint32_t cam) {
+  uint32_t m = 0;
+  for (size_t i = 0; i < ctx->S.bodies.size(); i++) if (ctx->S.bodies[i].owner == int(cam)) m |= 1u << i;
+  return m;
+}
+
+// copy `bytes` from a host or device source into device memory `dst`
+vt_status to_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
+  return VT_OK;
+}
+vt_status from_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+  return VT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* vt_last_error(const vt_ctx* ctx) { return ctx ? ctx->err.c_str() : g_static_err; }
+void* vt_stream(vt_ctx* ctx) { return ctx ? reinterpret_cast<void*>(ctx->stream) : nullptr; }
+
+uint32_t vt_bvh_capacity(uint32_t n_tris, uint32_t leaf_size) {
+  // every node is interior and holds two children, every leaf at least one triangle: at most n_tris - 1 nodes
+  (void)leaf_size;
+  return std::max<uint32_t>(4, n_tris);
+}
+
+vt_status vt_bvh_build(const float* pos, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris, uint32_t leaf_size, uint32_t* nodes_out,
+                       uint32_t* order_out, vt_bvh_result* res) {
+  if ((n_tris && (!pos || !idx)) || !nodes_out || !res || (n_tris && !order_out)) return VT_ERR_ARG;
+  for (uint64_t i = 0; i < uint64_t(n_tris) * 3; i++) if (idx[i] >= n_verts) return VT_ERR_ARG;
+  vt::Bvh b = vt::sah_build(pos, idx, n_tris, leaf_size);
+  if (b.node_count > vt_bvh_capacity(n_tris, leaf_size)) return VT_ERR_ARG;
+  std::copy(b.words.begin(), b.words.end(), nodes_out);
+  std::copy(b.order.begin(), b.order.end(), order_out);
+  res->node_count = b.node_count;
+  res->max_depth = b.max_depth;
+  for (int k = 0; k < 3; k++) { res->bmin[k] = b.lo[k]; res->bmax[k] = b.hi[k]; }
+  return VT_OK;
+}
+
+vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx** out) {
+  if (!scene || !out) return VT_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return VT_ERR_NO_DEVICE; }
+  vt_ctx* ctx = new vt_ctx();
+  const uint32_t leaf = opts && opts->leaf_size ? opts->leaf_size : 4;
+  const uint32_t albs = opts && opts->albedo_samples ? opts->albedo_samples : 1024;
+  ctx->device = opts ? opts->device : 0;
+  try {
+    ctx->S = vt::prepare_scene(*scene, leaf, albs);
+  } catch (const std::exception& e) {
+    const std::string m = e.what();
+    delete ctx;
+    g_static_err = "scene preparation failed";
+    return m.find("too many bodies") != std::string::npos ? VT_ERR_TOO_MANY_BODIES : VT_ERR_ARG;
+  }
+  auto bail = [&](vt_status s) { vt_destroy(ctx); return s; };
+  if (cudaSetDevice(ctx->device) != cudaSuccess) { cudaGetLastError(); delete ctx; return VT_ERR_NO_DEVICE; }
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(VT_ERR_CUDA);
+  if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) return bail(VT_ERR_CUDA);
+  const vt::Prepared& S = ctx->S;
+  vt_status s;
+  if ((s = upload(ctx, &ctx->d_nodes, S.nodes.data(), S.nodes.size() * 4)) != VT_OK) return bail(s);
+  if ((s = upload(ctx, &ctx->d_tris, S.tris.data(), S.tris.size() * 4)) != VT_OK) return bail(s);
+  if ((s = upload(ctx, &ctx->d_verts, S.verts.data(), S.verts.size() * 4)) != VT_OK) return bail(s);
+  if ((s = upload(ctx, &ctx->d_params, S.params.data(), S.params.size() * 4)) != VT_OK) return bail(s);
+  // node state: E_free|V = (0,0,0,1), slots 0, B_dir|vis = (0,0,0,-1) (gpu/renderer.js:323-327)
+  std::vector<float> st(std::max<size_t>(16, size_t(S.static_verts) * 16), 0.0f);
+  for (uint32_t i = 0; i < S.static_verts; i++) { st[16 * i + 3] = 1; st[16 * i + 15] = -1; }
+  if ((s = upload(ctx, &ctx->d_nstate, st.data(), st.size() * 4)) != VT_OK) return bail(s);
+  if (cudaMalloc(&ctx->d_su, sizeof(ctx->su_host)) != cudaSuccess) return bail(VT_ERR_OOM);
+  if (cudaMalloc(&ctx->d_dbg, 64) != cudaSuccess || cudaMemsetAsync(ctx->d_dbg, 0, 64, ctx->stream) != cudaSuccess) return bail(VT_ERR_OOM);
+  if (cudaMalloc(&ctx->d_work, 256) != cudaSuccess) return bail(VT_ERR_OOM);
+  ctx->cams.resize(S.cams.size());
+  for (size_t c = 0; c < S.cams.size(); c++) {
+    const size_t px = size_t(S.cams[c].width) * S.cams[c].height;
+    if (cudaMalloc(&ctx->cams[c].radiance, std::max<size_t>(px, 1) * 16) != cudaSuccess) return bail(VT_ERR_OOM);
+    if (cudaMalloc(&ctx->cams[c].raw, std::max<size_t>(px, 1) * 4) != cudaSuccess) return bail(VT_ERR_OOM);
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  ctx->render_blocks = std::max(1, sms) * vtk::render_blocks_per_sm();
+  // no poses yet: bodies of kind 'fixed' at identity, the rest hidden (gpu/renderer.js:259 setPoses({bodies: {}}))
+  ctx->inst = vt::poses_from(S, nullptr, nullptr, 0);
+  if ((s = write_su(ctx)) != VT_OK) return bail(s);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return bail(VT_ERR_CUDA);
+  *out = ctx;
+  return VT_OK;
+}
+
+vt_status vt_destroy(vt_ctx* ctx) {
+  if (!ctx) return VT_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); }
+  cudaFree(ctx->d_nodes); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
+  cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return VT_OK;
+}
+
+vt_status vt_scene_info_get(const vt_ctx* ctx, vt_scene_info* o) {
+  if (!ctx || !o) return VT_ERR_ARG;
+  const vt::Prepared& S = ctx->S;
+  o->node_count = S.node_count; o->tri_count = S.tri_count; o->vert_count = S.vert_count;
+  o->param_vec4s = uint32_t(S.params.size() / 4); o->static_verts = S.static_verts; o->static_tris = S.static_tris;
+  o->n_bodies = uint32_t(S.bodies.size()); o->n_materials = uint32_t(S.mats.size()); o->n_meshes = uint32_t(S.meshes.size());
+  o->emit_tris = S.emit_tris; o->mesh_off = S.mesh_off; o->mat_off = S.mat_off; o->alb_off = S.alb_off; o->prof_off = S.prof_off;
+  o->prof_n = S.prof_n; o->emit_off = S.emit_off;
+  o->emit_area = float(S.emit_area); o->emit_radius = float(S.emit_radius);
+  for (int k = 0; k < 3; k++) { o->emit_axis[k] = float(S.emit_axis[k]); o->emit_normal[k] = float(S.emit_normal[k]); o->emit_centroid[k] = float(S.emit_centroid[k]); }
+  o->shadow_skips_scope = S.shadow_skips_scope; o->scope_index = S.scope_index;
+  return VT_OK;
+}
+
+vt_status vt_scene_export(const vt_ctx* ctx, uint32_t* nodes, uint32_t* tris, uint32_t* verts, float* params) {
+  if (!ctx) return VT_ERR_ARG;
+  const vt::Prepared& S = ctx->S;
+  if (nodes) std::copy(S.nodes.begin(), S.nodes.end(), nodes);
+  if (tris) std::copy(S.tris.begin(), S.tris.end(), tris);
+  if (verts) std::copy(S.verts.begin(), S.verts.end(), verts);
+  if (params) std::copy(S.params.begin(), S.params.end(), params);
+  return VT_OK;
+}
+
+vt_status vt_blas_info_get(const vt_ctx* ctx, uint32_t body, vt_blas_info* o) {
+  if (!ctx || !o || body >= ctx->S.bodies.size()) return VT_ERR_ARG;
+  const vt::BodyRec& b = ctx->S.bodies[body];
+  o->root = b.root; o->tri_off = b.tri_off; o->tri_count = b.tri_count; o->kind = b.kind;
+  for (int k = 0; k < 3; k++) {
+    o->bmin[k] = b.lo[k]; o->bmax[k] = b.hi[k]; o->cap_a[k] = float(b.cap_a[k]); o->cap_b[k] = float(b.cap_b[k]);
+    o->occ_a[k] = float(b.occ_a[k]); o->occ_b[k] = float(b.occ_b[k]);
+  }
+  o->cap_r = float(b.cap_r); o->occ_r = float(b.occ_r); o->rho_eff = float(b.rho_eff);
+  return VT_OK;
+}
+
+vt_status vt_set_poses(vt_ctx* ctx, const double* T0, const double* T1, uint32_t n_bodies) {
+  if (!ctx) return VT_ERR_ARG;
+  if (n_bodies && !T0) return fail(ctx, VT_ERR_ARG, "poses: T0 is null");
+  ctx->inst = vt::poses_from(ctx->S, T0, T1, n_bodies);
+  return write_su(ctx);
+}
+
+vt_status vt_set_eavg(vt_ctx* ctx, const float e[3]) {
+  if (!ctx || !e) return VT_ERR_ARG;
+  for (int k = 0; k < 3; k++) ctx->eavg[k] = e[k];
+  return write_su(ctx);
+}
+
+vt_status vt_scene_uniform_get(const vt_ctx* ctx, void* out, size_t bytes) {
+  if (!ctx || !out || bytes < sizeof(ctx->su_host)) return VT_ERR_ARG;
+  std::memcpy(out, ctx->su_host, sizeof(ctx->su_host));
+  return VT_OK;
+}
+
+vt_status vt_set_node_state(vt_ctx* ctx, const float* state, uint32_t slot) {
+  if (!ctx || !state || slot < 1 || slot > 2) return VT_ERR_ARG;
+  vt_status s = to_device(ctx, ctx->d_nstate, state, size_t(ctx->S.static_verts) * 64);
+  if (s != VT_OK) return s;
+  ctx->slot = slot;
+  return write_su(ctx);
+}
+
+vt_status vt_trace_rays(vt_ctx* ctx, const float* o4, const float* d4, uint32_t n, uint32_t mask, uint32_t any_hit, uint32_t root,
+                        float* out4, float* out_v) {
+  if (!ctx || (n && (!o4 || !d4 || !out4))) return VT_ERR_ARG;
+  if (root >= ctx->S.node_count) return fail(ctx, VT_ERR_ARG, "trace: root out of range");
+  if (!n) return VT_OK;
+  const size_t b16 = size_t(n) * 16, b4 = size_t(n) * 4;
+  vt_status s = ensure_scratch(ctx, 3 * b16 + b4 + 256);
+  if (s != VT_OK) return s;
+  char* base = static_cast<char*>(ctx->d_scratch);
+  float4 *dO = reinterpret_cast<float4*>(base), *dD = reinterpret_cast<float4*>(base + b16), *dOut = reinterpret_cast<float4*>(base + 2 * b16);
+  float* dV = reinterpret_cast<float*>(base + 3 * b16);
+  if ((s = to_device(ctx, dO, o4, b16)) != VT_OK) return s;
+  if ((s = to_device(ctx, dD, d4, b16)) != VT_OK) return s;
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  vtk::launch_trace(dev_scene(ctx), dO, dD, n, mask, any_hit, root, dOut, dV, ctx->stream);
+  VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  ctx->tim.launches++;
+  if ((s = from_device(ctx, out4, dOut, b16)) != VT_OK) return s;
+  if (out_v && (s = from_device(ctx, out_v, dV, b4)) != VT_OK) return s;
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->tim.trace_ms = ms;
+  return VT_OK;
+}
+
+vt_status vt_visible(vt_ctx* ctx, uint32_t camera, const double* pts, uint32_t n, double tol, double time, uint8_t* out) {
+  if (!ctx || (n && (!pts || !out))) return VT_ERR_ARG;
+  if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
+  if (!n) return VT_OK;
+  std::vector<float3> p(n);
+  for (uint32_t i = 0; i < n; i++) p[i] = make_float3(float(pts[3 * i]), float(pts[3 * i + 1]), float(pts[3 * i + 2]));
+  vt_status s = ensure_scratch(ctx, size_t(n) * 12 + n + 256);
+  if (s != VT_OK) return s;
+  float3* dp = static_cast<float3*>(ctx->d_scratch);
+  uint8_t* dout = reinterpret_cast<uint8_t*>(static_cast<char*>(ctx->d_scratch) + size_t(n) * 12);
+  VT_CK(cudaMemcpyAsync(dp, p.data(), size_t(n) * 12, cudaMemcpyHostToDevice, ctx->stream));
+  const double* T = ctx->S.cams[camera].T_D_C;
+  vtk::launch_visible(dev_scene(ctx), make_float3(float(T[3]), float(T[7]), float(T[11])), dp, n, float(tol), float(time),
+                      skip_mask(ctx, camera), dout, ctx->stream);
+  VT_CK(cudaGetLastError());
+  ctx->tim.launches++;
+  VT_CK(cudaMemcpyAsync(out, dout, n, cudaMemcpyDeviceToHost, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  return VT_OK;
+}
+
+vt_status vt_project(vt_ctx* ctx, uint32_t camera, const double* pts, uint32_t n, double* uv) {
+  if (!ctx || (n && (!pts || !uv))) return VT_ERR_ARG;
+  if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
+  const vt_camera_desc& c = ctx->S.cams[camera];
+  const double* T = c.T_D_C;
+  for (uint32_t i = 0; i < n; i++) {
+    // camera-frame point R^T (p - c), then KB4 in float64 (gpu/lens.js:43 project)
+    const double d[3] = {pts[3 * i] - T[3], pts[3 * i + 1] - T[7], pts[3 * i + 2] - T[11]};
+    const double x = T[0] * d[0] + T[4] * d[1] + T[8] * d[2];
+    const double y = T[1] * d[0] + T[5] * d[1] + T[9] * d[2];
+    const double z = T[2] * d[0] + T[6] * d[1] + T[10] * d[2];
+    const double rho = std::hypot(x, y);
+    if (rho < 1e-300) { uv[2 * i] = c.cx; uv[2 * i + 1] = c.cy; continue; }
+    const double th = std::atan2(rho, z), t2 = th * th;
+    const double thd = th * (1 + t2 * (c.k[0] + t2 * (c.k[1] + t2 * (c.k[2] + t2 * c.k[3]))));
+    const double s = thd / rho, xd = x * s, yd = y * s;
+    uv[2 * i] = c.fx * (xd + c.alpha * yd) + c.cx;
+    uv[2 * i + 1] = c.fy * yd + c.cy;
+  }
+  return VT_OK;
+}
+
+vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba) {
+  if (!ctx || !q) return VT_ERR_ARG;
+  if (q->camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(q->camera));
+  if (q->root >= ctx->S.node_count) return fail(ctx, VT_ERR_ARG, "render: root out of range");
+  if (q->mode != VT_SHADE_TWIN && q->mode != VT_SHADE_PATH) return fail(ctx, VT_ERR_ARG, "render: unknown mode");
+  const vt_camera_desc& c = ctx->S.cams[q->camera];
+  vtk::CamParams cp{};
+  const double* T = c.T_D_C;
+  for (int k = 0; k < 3; k++) {
+    cp.rx[k] = float(T[4 * k]); cp.ry[k] = float(T[4 * k + 1]); cp.rz[k] = float(T[4 * k + 2]); cp.pos[k] = float(T[4 * k + 3]);
+  }
+  cp.lens = {float(c.fx), float(c.fy), float(c.cx), float(c.cy), float(c.alpha), float(c.k[0]), float(c.k[1]), float(c.k[2]), float(c.k[3])};
+  cp.w = c.width; cp.h = c.height;
+  cp.spp = std::min(std::max(q->spp, 1u), q->mode == VT_SHADE_TWIN ? 64u : 4096u);   // kernels.wgsl.js:169 clamps to 64
+  cp.seed = q->seed; cp.cam_index = q->camera; cp.options = q->options; cp.skip = skip_mask(ctx, q->camera);
+  cp.n_light = q->light_samples; cp.mode = q->mode; cp.max_depth = std::max(1u, std::min(q->max_depth, 64u)); cp.root = q->root;
+  cp.t0 = q->shutter[0]; cp.t1 = q->shutter[1]; cp.scale = q->scale;
+  if (q->frame != ctx->frame) { ctx->frame = q->frame; vt_status s = write_su(ctx); if (s != VT_OK) return s; }
+  VT_CK(cudaMemsetAsync(ctx->d_work, 0, 4, ctx->stream));
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  vtk::launch_render(dev_scene(ctx), cp, ctx->cams[q->camera].radiance, ctx->d_work, ctx->render_blocks, ctx->stream);
+  VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  ctx->tim.launches++;
+  ctx->cams[q->camera].rendered = true;
+  if (out_rgba) {
+    vt_status s = from_device(ctx, out_rgba, ctx->cams[q->camera].radiance, size_t(c.width) * c.height * 16);
+    if (s != VT_OK) return s;
+  }
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->tim.render_ms = ms;
+  return VT_OK;
+}
+
+vt_status vt_readback(vt_ctx* ctx, uint32_t camera, uint32_t kind, void* out, size_t bytes) {
+  if (!ctx || !out) return VT_ERR_ARG;
+  if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
+  const size_t px = size_t(ctx->S.cams[camera].width) * ctx->S.cams[camera].height;
+  const auto& C = ctx->cams[camera];
+  if (kind == VT_READ_LINEAR) {
+    if (!C.rendered) return fail(ctx, VT_ERR_STATE, "readback before renderCamera");
+    if (bytes < px * 16) return VT_ERR_ARG;
+    vt_status s = from_device(ctx, out, C.radiance, px * 16);
+    if (s != VT_OK) return s;
+  } else if (kind == VT_READ_RAW) {
+    if (!C.exposed) return fail(ctx, VT_ERR_STATE, "raw readback before sensor");
+    if (bytes < px * 4) return VT_ERR_ARG;
+    vt_status s = from_device(ctx, out, C.raw, px * 4);
+    if (s != VT_OK) return s;
+  } else {
+    return fail(ctx, VT_ERR_ARG, "readback kind");
+  }
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  return VT_OK;
+}
+
+vt_status vt_sensor_expose(vt_ctx* ctx, const vt_sensor_uniform* su, const float* irradiance, float* raw) {
+  if (!ctx || !su || !irradiance || !raw) return VT_ERR_ARG;
+  const uint32_t W = su->words[0], H = su->words[1];
+  float glare;
+  std::memcpy(&glare, &su->words[52], 4);
+  if (!W || !H) return fail(ctx, VT_ERR_ARG, "sensor: empty image");
+  if (glare != 0.0f) return fail(ctx, VT_ERR_ARG, "sensor: veiling glare is not supported by the expose stage (fraction must be 0)");
+  const size_t px = size_t(W) * H;
+  const bool din = is_device_ptr(irradiance), dout = is_device_ptr(raw);
+  vt_status s = ensure_scratch(ctx, (din ? 0 : px * 16) + (dout ? 0 : px * 4) + 256);
+  if (s != VT_OK) return s;
+  const float4* dE = reinterpret_cast<const float4*>(irradiance);
+  char* base = static_cast<char*>(ctx->d_scratch);
+  if (!din) { VT_CK(cudaMemcpyAsync(base, irradiance, px * 16, cudaMemcpyHostToDevice, ctx->stream)); dE = reinterpret_cast<float4*>(base); base += px * 16; }
+  float* dR = dout ? raw : reinterpret_cast<float*>(base);
+  vtk::SensorParams sp;
+  std::memcpy(sp.w, su->words, sizeof(sp.w));
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  vtk::launch_sensor_expose(sp, dE, 1.0f, dR, ctx->stream);
+  VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  ctx->tim.launches++;
+  if (!dout) VT_CK(cudaMemcpyAsync(raw, dR, px * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->tim.sensor_ms = ms;
+  return VT_OK;
+}
+
+vt_status vt_sensor_camera(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, float optics_scale) {
+  if (!ctx || !su) return VT_ERR_ARG;
+  if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
+  auto& C = ctx->cams[camera];
+  if (!C.rendered) return fail(ctx, VT_ERR_STATE, "sensor before renderCamera");
+  if (su->words[0] != ctx->S.cams[camera].width || su->words[1] != ctx->S.cams[camera].height) return fail(ctx, VT_ERR_ARG, "sensor: size mismatch");
+  float glare;
+  std::memcpy(&glare, &su->words[52], 4);
+  if (glare != 0.0f) return fail(ctx, VT_ERR_ARG, "sensor: veiling glare is not supported by the expose stage (fraction must be 0)");
+  vtk::SensorParams sp;
+  std::memcpy(sp.w, su->words, sizeof(sp.w));
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  vtk::launch_sensor_expose(sp, C.radiance, optics_scale, C.raw, ctx->stream);
+  VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  ctx->tim.launches++;
+  C.exposed = true;
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->tim.sensor_ms = ms;
+  return VT_OK;
+}
+
+vt_status vt_form_factors(vt_ctx* ctx, uint32_t n, const float* centres, const float* normals, const float* areas, float* F) {
+  if (!ctx || !n || !centres || !normals || !areas || !F) return VT_ERR_ARG;
+  const size_t nn = size_t(n) * n * 4;
+  const bool dF = is_device_ptr(F);
+  vt_status s = ensure_scratch(ctx, size_t(n) * 28 + (dF ? 0 : nn) + 256);
+  if (s != VT_OK) return s;
+  char* base = static_cast<char*>(ctx->d_scratch);
+  float *dC = reinterpret_cast<float*>(base), *dN = dC + 3 * size_t(n), *dA = dN + 3 * size_t(n);
+  if ((s = to_device(ctx, dC, centres, size_t(n) * 12)) != VT_OK) return s;
+  if ((s = to_device(ctx, dN, normals, size_t(n) * 12)) != VT_OK) return s;
+  if ((s = to_device(ctx, dA, areas, size_t(n) * 4)) != VT_OK) return s;
+  float* dOut = dF ? F : reinterpret_cast<float*>(base + ((size_t(n) * 28 + 255) / 256) * 256);
+  vtk::launch_form_factors(n, dC, dN, dA, dOut, ctx->stream);
+  VT_CK(cudaGetLastError());
+  ctx->tim.launches++;
+  if (!dF) VT_CK(cudaMemcpyAsync(F, dOut, nn, cudaMemcpyDeviceToHost, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  return VT_OK;
+}
+
+vt_status vt_debug_flags(vt_ctx* ctx, uint32_t out[16], int reset) {
+  if (!ctx || !out) return VT_ERR_ARG;
+  VT_CK(cudaMemcpyAsync(out, ctx->d_dbg, 64, cudaMemcpyDeviceToHost, ctx->stream));
+  if (reset) VT_CK(cudaMemsetAsync(ctx->d_dbg, 0, 64, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  return VT_OK;
+}
+
+vt_status vt_timings_get(const vt_ctx* ctx, vt_timings* out) {
+  if (!ctx || !out) return VT_ERR_ARG;
+  *out = ctx->tim;
+  return VT_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------------ radiosity solve
+// Plain FP32: Jacobi sweeps B <- E + rho F B on CUDA cores (the matvec for one right-hand side, the FP32 GEMM
+// for several), the relative update checked every `check_every` sweeps. BF16 / FP8: see vt_tc.cu.
+vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
+  if (!ctx || !q || !q->n || !q->n_rhs || !q->F || !q->rho || !q->E || !q->B) return VT_ERR_ARG;
+  if (q->n_rhs > 64) return fail(ctx, VT_ERR_ARG, "solve: at most 64 right-hand sides");
+  if (q->n_rhs > 1 && (q->n_rhs % 4)) return fail(ctx, VT_ERR_ARG, "solve: several right-hand sides must be a multiple of 4");
+  if (q->precision != VT_PREC_FP32) return fail(ctx, VT_ERR_ARG, "solve: only VT_PREC_FP32 is built in this library");
+  const uint32_t n = q->n, R = q->n_rhs;
+  const size_t nb = size_t(n) * R * 4, nf = size_t(n) * n * 4;
+  const bool dF = is_device_ptr(q->F);
+  const uint32_t max_blocks = (n + 7) / 8 + 8;
+  const size_t need = (dF ? 0 : nf) + 3 * nb + size_t(n) * 4 + size_t(max_blocks) * 16 + 64 + 1024;
+  vt_status s = ensure_scratch(ctx, need);
+  if (s != VT_OK) return s;
+  char* base = static_cast<char*>(ctx->d_scratch);
+  auto take = [&](size_t bytes) { char* p = base; base += (bytes + 255) / 256 * 256; return p; };
+  const float* Fd = dF ? q->F : reinterpret_cast<float*>(take(nf));
+  float* E = reinterpret_cast<float*>(take(nb));
+  float* B0 = reinterpret_cast<float*>(take(nb));
+  float* B1 = reinterpret_cast<float*>(take(nb));
+  float* rho = reinterpret_cast<float*>(take(size_t(n) * 4));
+  double* partials = reinterpret_cast<double*>(take(size_t(max_blocks) * 16));
+  double* norms = reinterpret_cast<double*>(take(64));
+  if (!dF && (s = to_device(ctx, const_cast<float*>(Fd), q->F, nf)) != VT_OK) return s;
+  if ((s = to_device(ctx, E, q->E, nb)) != VT_OK) return s;
+  if ((s = to_device(ctx, rho, q->rho, size_t(n) * 4)) != VT_OK) return s;
+  if (q->warm_start) { if ((s = to_device(ctx, B0, q->B, nb)) != VT_OK) return s; }
+  else VT_CK(cudaMemcpyAsync(B0, E, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+  const uint32_t check = q->check_every ? q->check_every : 8;
+  const uint32_t max_it = q->max_iters ? q->max_iters : 1000;
+  float* cur = B0;
+  float* nxt = B1;
+  uint32_t it = 0, np = 0;
+  double resid = INFINITY;
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  while (it < max_it) {
+    const uint32_t k = std::min(check, max_it - it);
+    for (uint32_t j = 0; j < k; j++) {
+      if (R == 1) vtk::launch_jacobi_matvec(Fd, rho, E, cur, nxt, n, partials, &np, ctx->stream);
+      else vtk::launch_jacobi_gemm_fp32(Fd, rho, E, cur, nxt, n, R, partials, &np, ctx->stream);
+      std::swap(cur, nxt);
+    }
+    ctx->tim.launches += k + 1;
+    it += k;
+    vtk::launch_reduce_partials(partials, np, norms, ctx->stream);
+    VT_CK(cudaGetLastError());
+    double h[2];
+    VT_CK(cudaMemcpyAsync(h, norms, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+    resid = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+    if (resid <= q->tol) break;
+  }
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if ((s = from_device(ctx, q->B, cur, nb)) != VT_OK) return s;
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  q->iters = it; q->refinements = 0; q->residual = resid; q->ms = ms;
+  ctx->tim.solve_ms = ms;
+  return resid <= q->tol ? VT_OK : VT_ERR_NOT_CONVERGED;
+}

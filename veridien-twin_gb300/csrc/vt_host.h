@@ -1,0 +1,72 @@
+// Host side of libvtwin: scene preparation (the part of gpu/scene_gpu.js:prepareScene after welding), the BVH
+// builder of gpu/bvh.js, material preparation with directional-albedo tables (gpu/bsdf.js) and the scene uniform
+// written from poses (gpu/renderer.js:620-705). Everything here runs once per scene or once per pose change.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/vtwin.h"
+
+namespace vt {
+
+// Scene uniform layout in 32-bit words (gpu/wgsl/common.wgsl.js:60-77 SceneU / Inst): 24 header words, then
+// 48 words per instance.
+constexpr int SU_WORDS = 24 + 48 * VT_MAX_INST;
+constexpr int SU_INST = 24;
+
+struct Bvh {
+  std::vector<uint32_t> words;   // 16 per node
+  std::vector<uint32_t> order;   // input triangle of each slot
+  uint32_t node_count = 0, max_depth = 1;
+  float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+Bvh sah_build(const float* P, const uint32_t* I, uint32_t n_tris, uint32_t leaf_size);
+
+struct Material {
+  int kind = 0;                  // 0 dielectric, 1 conductor, 2 coated conductor
+  bool emitter = false, table = true, textured = false;
+  double rho[3] = {0, 0, 0}, f0[3] = {0, 0, 0}, tau[3] = {1, 1, 1}, ink[3] = {0, 0, 0};
+  double roughness = 0.5, alpha = 0.25, ior = 1.5, fbar = 0, fbar_exact = 0, alpha_coat = 0, rough_ink = 0.4;
+  double spec[VT_ALBEDO_BINS][3] = {}, diff[VT_ALBEDO_BINS][3] = {};
+  double hh[3] = {0, 0, 0}, hh_spec[3] = {0, 0, 0};
+};
+Material make_material(const vt_material& m, uint32_t albedo_samples);
+double fresnel_mean(double eta);
+
+struct BodyRec {
+  uint32_t root = 0, tri_off = 0, tri_count = 0;
+  int32_t kind = 0, owner = -1;
+  float lo[3], hi[3];
+  double cap_a[3], cap_b[3], cap_r = 0, occ_a[3], occ_b[3], occ_r = 0, rho_eff = 0;
+};
+
+struct Prepared {
+  std::vector<uint32_t> nodes, tris, verts;   // 16, 16, 8 words per item
+  std::vector<float> params;                  // vec4 array
+  std::vector<float> node_area;
+  uint32_t node_count = 0, tri_count = 0, vert_count = 0, static_verts = 0, static_tris = 0;
+  uint32_t mesh_off = 0, mat_off = 0, alb_off = 0, prof_off = 0, prof_n = 0, emit_off = 0, emit_n = 0, emit_tris = 0;
+  std::vector<BodyRec> bodies;
+  std::vector<Material> mats;
+  std::vector<vt_mesh> meshes;
+  std::vector<vt_camera_desc> cams;
+  double emit_area = 0, emit_axis[3] = {0, 0, 1}, emit_normal[3] = {0, 0, 1}, emit_centroid[3] = {0, 0, 0}, emit_radius = 0;
+  bool shadow_skips_scope = false;
+  int scope_index = -1;
+  float L0[3] = {1, 1, 1};
+};
+// gpu/scene_gpu.js:241-472 + gpu/renderer.js:271-306; throws std::runtime_error on bad input
+Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf_size, uint32_t albedo_samples);
+
+struct InstPose { bool valid = false; double q0[4], q1[4], p0[3], p1[3]; };
+// gpu/renderer.js:620 setPoses: quaternion + translation per body (T column-major 4x4; NaN hides a body)
+std::vector<InstPose> poses_from(const Prepared& S, const double* T0, const double* T1, uint32_t n);
+// gpu/renderer.js:642-705 _writeSceneU
+void scene_uniform(const Prepared& S, const std::vector<InstPose>& inst, const float eavg[3], uint32_t slot, uint32_t frame,
+                   float* out /* SU_WORDS */);
+// gpu/renderer.js:635 _poseAt
+bool pose_at(const InstPose& I, double t, double R[3][3], double p[3]);
+
+}  // namespace vt

@@ -1,0 +1,46 @@
+// Kernel entry points and their launch parameters (shared by the .cu files and vt_api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "vt_device.cuh"
+
+namespace vtk {
+
+// one camera dispatch (the fields of gpu/renderer.js:888 _packCam that the estimators read)
+struct CamParams {
+  float rx[3], ry[3], rz[3], pos[3];   // camera axes in the dome frame (columns of R_D_C) and centre
+  vtd::Kb4 lens;
+  uint32_t w, h, spp, seed, cam_index, options, skip, n_light, mode, max_depth, root;
+  float t0, t1, scale;
+};
+
+// persistent tile scheduler: warps pull 8x4 pixel tiles from a device counter
+constexpr int TILE_W = 8, TILE_H = 4;
+constexpr int RENDER_THREADS = 128;
+
+void launch_render(const vtd::Scene& S, const CamParams& cp, float4* out, uint32_t* work_counter, int blocks, cudaStream_t st);
+int render_blocks_per_sm();
+void launch_trace(const vtd::Scene& S, const float4* o4, const float4* d4, uint32_t n, uint32_t mask, uint32_t any_hit, uint32_t root,
+                  float4* out4, float* out_v, cudaStream_t st);
+void launch_visible(const vtd::Scene& S, float3 c, const float3* pts, uint32_t n, float tol, float time, uint32_t skip, uint8_t* out,
+                    cudaStream_t st);
+
+// sensor (gpu/wgsl/sensor.wgsl.js:177 sensorExpose)
+struct SensorParams { uint32_t w[64]; };
+void launch_sensor_expose(const SensorParams& su, const float4* E, float scale, float* raw, cudaStream_t st);
+
+// radiosity
+// B_out = E + rho (F B_in), n x 1, and per-block partial sums of |B_out - B_in|^2 and |B_out|^2 (doubles)
+void launch_jacobi_matvec(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n,
+                          double* partials, uint32_t* n_partials, cudaStream_t st);
+// B_out = E + rho (F B_in), n x R row-major (R <= 64, multiple of 4), CUDA-core FP32 GEMM
+void launch_jacobi_gemm_fp32(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n, uint32_t R,
+                             double* partials, uint32_t* n_partials, cudaStream_t st);
+// sum the partials into out[0..1] (deterministic order)
+void launch_reduce_partials(const double* partials, uint32_t n, double* out, cudaStream_t st);
+void launch_form_factors(uint32_t n, const float* C, const float* N, const float* A, float* F, cudaStream_t st);
+
+}  // namespace vtk

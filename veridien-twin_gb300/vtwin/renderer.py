@@ -1,0 +1,321 @@
+"""TwinRenderer: the host-side mirror of gpu/renderer.js's TwinRenderer over libvtwin's C ABI.
+
+Same method names and argument meanings as the reference (gpu/renderer.js:3-10): create, setPoses, renderCamera,
+renderFrame, sensor, readback, visible, project, timings, debugFlags, destroy; snake_case aliases are provided.
+Errors raise VtError (the reference throws Error: unknown camera, too many bodies, ...).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._lib import VtError, check, load
+from . import sensor as sensor_mod
+
+DEFAULTS = {"spp": 1, "refine": 0, "lightSamples": 4, "leafSize": 4, "albedoSamples": 1024}
+PRESETS = {"judge": {}, "balanced": {"spp": 1, "lightSamples": 2}, "live": {"spp": 1, "lightSamples": 1}}
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class TwinRenderer:
+    """gpu/renderer.js:200 TwinRenderer (the WebGPU device replaced by one CUDA context)."""
+
+    def __init__(self):
+        self._ctx = None
+
+    # ------------------------------------------------------------------------------------------- lifecycle
+    @classmethod
+    def create(cls, scene: dict, physics: dict | None = None, preset: str | None = None, device: int = 0, **opts):
+        """gpu/renderer.js:202 create({scene, physics, preset, ...DEFAULTS}); `scene` is a dict of welded arrays
+        (vtwin.dome), physics is accepted for the API's sake (materials already resolved in `scene`)."""
+        r = cls()
+        r.opts = {**DEFAULTS, **PRESETS.get(preset or "", {}), **opts}
+        r.lib = load()
+        r.scene = scene
+        r._desc = A.SceneDesc(scene)
+        o = A.vt_options(leaf_size=int(r.opts["leafSize"]), albedo_samples=int(r.opts["albedoSamples"]), device=device)
+        ctx = C.c_void_p()
+        st = r.lib.vt_create(r._desc.ref, C.byref(o), C.byref(ctx))
+        if st != A.VT_OK:
+            raise VtError(st, r.lib.vt_last_error(None).decode())
+        r._ctx = ctx
+        r.cameras = {c.get("name", f"CAM{i + 1}"): i for i, c in enumerate(scene.get("cameras", []))}
+        r.bodies = [b["key"] for b in scene.get("bodies", [])]
+        r.frame = 0
+        r.sensor_p = sensor_mod.sensor_params((opts or {}).get("sensor"))
+        r.set_poses({"bodies": {}})
+        return r
+
+    def destroy(self):
+        if self._ctx is not None:
+            self.lib.vt_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def _cam(self, name) -> int:
+        if isinstance(name, int):
+            if 0 <= name < len(self.cameras):
+                return name
+        elif name in self.cameras:
+            return self.cameras[name]
+        raise VtError(A.VT_ERR_UNKNOWN_CAMERA, f"unknown camera {name}")
+
+    # ------------------------------------------------------------------------------------------- scene
+    def info(self) -> A.vt_scene_info:
+        i = A.vt_scene_info()
+        check(self.lib.vt_scene_info_get(self._ctx, C.byref(i)), self._ctx)
+        return i
+
+    def export(self) -> dict:
+        i = self.info()
+        nodes = np.zeros(i.node_count * 16, np.uint32)
+        tris = np.zeros(i.tri_count * 16, np.uint32)
+        verts = np.zeros(i.vert_count * 8, np.uint32)
+        params = np.zeros(i.param_vec4s * 4, np.float32)
+        check(self.lib.vt_scene_export(self._ctx, _p(nodes), _p(tris), _p(verts), _p(params)), self._ctx)
+        return {"nodes": nodes, "tris": tris, "verts": verts, "params": params}
+
+    def blas(self, body: int) -> A.vt_blas_info:
+        b = A.vt_blas_info()
+        check(self.lib.vt_blas_info_get(self._ctx, body, C.byref(b)), self._ctx)
+        return b
+
+    # ------------------------------------------------------------------------------------------- poses
+    def _pose_array(self, poses):
+        out = np.full((len(self.bodies), 16), np.nan)
+        bodies = (poses or {}).get("bodies", {}) if isinstance(poses, dict) else {}
+        for i, key in enumerate(self.bodies):
+            T = bodies.get(key)
+            if T is not None:
+                out[i] = np.asarray(T, np.float64).ravel()
+        # bodies the caller never posed: the emitter body stays where it was built (identity), as a scene
+        # without a light makes no image; everything else is hidden (gpu/renderer.js:626)
+        for i, b in enumerate(self.scene.get("bodies", [])):
+            if np.isnan(out[i, 0]) and b["kind"] == "scope" and key_missing(bodies, b["key"]):
+                out[i] = np.eye(4).T.ravel()
+        return np.ascontiguousarray(out)
+
+    def setPoses(self, poses0, poses1=None):
+        """gpu/renderer.js:620 setPoses(poses0, poses1?): poses.bodies[key] = column-major 4x4."""
+        T0 = self._pose_array(poses0)
+        T1 = self._pose_array(poses1) if poses1 is not None else None
+        check(self.lib.vt_set_poses(self._ctx, _p(T0), _p(T1) if T1 is not None else None, len(T0)), self._ctx)
+
+    set_poses = setPoses
+
+    def set_pose_array(self, T0, T1=None):
+        T0 = np.ascontiguousarray(T0, np.float64).reshape(-1, 16)
+        T1 = None if T1 is None else np.ascontiguousarray(T1, np.float64).reshape(-1, 16)
+        check(self.lib.vt_set_poses(self._ctx, _p(T0), _p(T1) if T1 is not None else None, len(T0)), self._ctx)
+
+    def set_eavg(self, e):
+        e = np.ascontiguousarray(e, np.float32)
+        check(self.lib.vt_set_eavg(self._ctx, _p(e)), self._ctx)
+
+    def scene_uniform(self) -> np.ndarray:
+        out = np.zeros(24 + 48 * 24, np.float32)
+        check(self.lib.vt_scene_uniform_get(self._ctx, _p(out), out.nbytes), self._ctx)
+        return out
+
+    def set_node_state(self, state, slot=1):
+        state = np.ascontiguousarray(state, np.float32)
+        check(self.lib.vt_set_node_state(self._ctx, _p(state), slot), self._ctx)
+
+    # ------------------------------------------------------------------------------------------- rendering
+    def request(self, name, spp=None, lightSamples=None, seed=0, options=0, mode=A.VT_SHADE_TWIN, max_depth=2,
+                shutter=(0.0, 1.0), scale=1.0, root=0, frame=None) -> A.vt_render_req:
+        q = A.vt_render_req(camera=self._cam(name), spp=int(spp if spp is not None else self.opts["spp"]),
+                            light_samples=int(lightSamples if lightSamples is not None else self.opts["lightSamples"]),
+                            seed=int(seed), options=int(options), mode=int(mode), max_depth=int(max_depth), root=int(root),
+                            frame=int(self.frame if frame is None else frame))
+        q.shutter[:] = [float(shutter[0]), float(shutter[1])]
+        q.scale = float(scale)
+        return q
+
+    def renderCamera(self, name, out=None, **o):
+        """gpu/renderer.js:975 renderCamera(name, {spp, lightSamples, seed, shutter, ...}). Radiance stays on the
+        device; `out` (a float32 array of w*h*4, host or device pointer-holder) receives a copy when given."""
+        q = self.request(name, **o)
+        check(self.lib.vt_render_camera(self._ctx, C.byref(q), _p(out) if isinstance(out, np.ndarray) else out), self._ctx)
+        return q
+
+    render_camera = renderCamera
+
+    def renderFrame(self, cameras=None, sensor=False, sensorOpts=None, **o):
+        """gpu/renderer.js:986 renderFrame({cameras, sensor}): every listed camera, then its sensor stage."""
+        names = cameras or list(self.cameras)
+        for n in names:
+            self.renderCamera(n, **o)
+        if sensor:
+            for n in names:
+                self.sensor(n, **(sensorOpts or {}))
+        self.frame += 1
+        return {n: {"linear": n} for n in names}
+
+    render_frame = renderFrame
+
+    def readback(self, name, kind="linear"):
+        """gpu/renderer.js:1191 readback(name, 'linear'|'raw') -> Float32Array copy."""
+        c = self._cam(name)
+        w, h = self.scene["cameras"][c]["size"]
+        if kind == "linear":
+            out = np.zeros((h, w, 4), np.float32)
+            check(self.lib.vt_readback(self._ctx, c, A.VT_READ_LINEAR, _p(out), out.nbytes), self._ctx)
+        elif kind == "raw":
+            out = np.zeros((h, w), np.float32)
+            check(self.lib.vt_readback(self._ctx, c, A.VT_READ_RAW, _p(out), out.nbytes), self._ctx)
+        else:
+            raise VtError(A.VT_ERR_ARG, f"readback kind {kind} is not produced by this library (linear, raw)")
+        return out
+
+    def sensor(self, name, seed=0, frame=None, noise=True, exposure_s=1.0, gain=1.0, params=None, optics_scale=1.0):
+        """gpu/renderer.js:1092 sensor(name, {seed, frame, noise, exposure_s, gain, params}): the expose stage
+        (CFA, shot + read noise, ADC) of the camera's last radiance into its raw DN image."""
+        c = self._cam(name)
+        w, h = self.scene["cameras"][c]["size"]
+        p = {**self.sensor_p, **(params or {})}
+        if noise is False:
+            p["noise"] = False
+        su = A.vt_sensor_uniform()
+        su.words[:] = [int(x) for x in sensor_mod.pack_sensor_uniform(
+            p, w, h, frame=self.frame if frame is None else frame, seed=seed, exposure=exposure_s, gain=gain, cam_index=c)]
+        check(self.lib.vt_sensor_camera(self._ctx, c, C.byref(su), float(optics_scale)), self._ctx)
+
+    # ------------------------------------------------------------------------------------------- queries
+    def trace(self, o4, d4, mask=3, any_hit=False, root=0):
+        """gpu/wgsl/kernels.wgsl.js:535 traceTest: rays (o.xyz, time), (d.xyz, -) -> (t, tri, inst, u), v."""
+        o4 = np.ascontiguousarray(o4, np.float32).reshape(-1, 4)
+        d4 = np.ascontiguousarray(d4, np.float32).reshape(-1, 4)
+        out = np.zeros((len(o4), 4), np.float32)
+        v = np.zeros(len(o4), np.float32)
+        check(self.lib.vt_trace_rays(self._ctx, _p(o4), _p(d4), len(o4), mask, int(any_hit), root, _p(out), _p(v)), self._ctx)
+        t = out[:, 0].copy()
+        tri = out[:, 1].view(np.uint32).copy()
+        inst = out[:, 2].view(np.uint32).copy()
+        return t, tri, inst, out[:, 3].copy(), v
+
+    def visible(self, name, pointsD, tol=2e-4, time=0.5):
+        pts = np.ascontiguousarray(pointsD, np.float64).reshape(-1, 3)
+        out = np.zeros(len(pts), np.uint8)
+        check(self.lib.vt_visible(self._ctx, self._cam(name), _p(pts), len(pts), tol, time, _p(out)), self._ctx)
+        return out.astype(bool)
+
+    def project(self, name, pointsD):
+        pts = np.ascontiguousarray(pointsD, np.float64).reshape(-1, 3)
+        uv = np.zeros((len(pts), 2), np.float64)
+        check(self.lib.vt_project(self._ctx, self._cam(name), _p(pts), len(pts), _p(uv)), self._ctx)
+        return uv
+
+    # ------------------------------------------------------------------------------------------- diagnostics
+    def debugFlags(self, reset=False) -> dict:
+        v = np.zeros(16, np.uint32)
+        check(self.lib.vt_debug_flags(self._ctx, _p(v), int(reset)), self._ctx)
+        return {"traversalCap": int(v[0]), "leafCap": int(v[1]), "refined": int(v[2]), "refinedBody": int(v[3]),
+                "refinedShadow": int(v[4]), "refinedSubsample": int(v[5]), "corruptTree": int(v[6]), "packetCap": int(v[7])}
+
+    debug_flags = debugFlags
+
+    def timings(self) -> dict:
+        t = A.vt_timings()
+        check(self.lib.vt_timings_get(self._ctx, C.byref(t)), self._ctx)
+        return {"render_ms": t.render_ms, "sensor_ms": t.sensor_ms, "solve_ms": t.solve_ms, "trace_ms": t.trace_ms,
+                "launches": int(t.launches)}
+
+    # ------------------------------------------------------------------------------------------- radiosity
+    def solve_radiosity(self, F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=1000, check_every=8, B0=None):
+        return solve_radiosity(F, rho, E, precision, tol, max_iters, check_every, B0, ctx=self._ctx)
+
+    def form_factors(self, centres, normals, areas, out=None):
+        return form_factors(centres, normals, areas, out, ctx=self._ctx)
+
+
+def key_missing(bodies: dict, key: str) -> bool:
+    return key not in bodies
+
+
+class _Ctx:
+    """A context without a scene, for the radiosity solve and the form-factor builder."""
+    _ctx = None
+
+    @classmethod
+    def get(cls):
+        if cls._ctx is None:
+            lib = load()
+            desc = A.vt_scene_desc()
+            m = (A.vt_mesh * 1)()
+            mt = (A.vt_material * 1)()
+            mt[0] = A.material_struct({"rho": [0.5, 0.5, 0.5], "ior": 1.0, "no_table": 1})
+            desc.meshes, desc.n_meshes, desc.materials, desc.n_materials = m, 1, mt, 1
+            desc.L0[:] = [1, 1, 1]
+            cls._keep = (desc, m, mt)
+            ctx = C.c_void_p()
+            st = lib.vt_create(C.byref(desc), None, C.byref(ctx))
+            if st != A.VT_OK:
+                raise VtError(st, lib.vt_last_error(None).decode())
+            cls._ctx = ctx
+        return cls._ctx
+
+
+def solve_radiosity(F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=1000, check_every=8, B0=None, ctx=None):
+    """B = E + diag(rho) F B on the device (gpu/renderer.js:804 converge, the lite_nodes Jacobi). F, rho, E are
+    numpy arrays (host) or objects exposing an integer device pointer via `.data_ptr()` (device). Returns
+    (B, info) with info = {iters, refinements, residual, ms, status}."""
+    lib = load()
+    ctx = ctx or _Ctx.get()
+    n = int(rho.shape[0])
+    E2 = E.reshape(n, -1) if hasattr(E, "reshape") else E
+    R = int(E2.shape[1])
+
+    def ptr(a):
+        if hasattr(a, "data_ptr"):
+            return C.cast(C.c_void_p(a.data_ptr()), C.POINTER(C.c_float))
+        return np.ascontiguousarray(a, np.float32).ctypes.data_as(C.POINTER(C.c_float))
+
+    keep = [np.ascontiguousarray(x, np.float32) if isinstance(x, np.ndarray) else x for x in (F, rho, E2)]
+    B = np.ascontiguousarray(B0, np.float32).copy() if B0 is not None else np.zeros((n, R), np.float32)
+    q = A.vt_solve_req(n=n, n_rhs=R, F=ptr(keep[0]), rho=ptr(keep[1]), E=ptr(keep[2]), B=B.ctypes.data_as(C.POINTER(C.c_float)),
+                       precision=int(precision), max_iters=int(max_iters), warm_start=int(B0 is not None),
+                       check_every=int(check_every), tol=float(tol))
+    st = lib.vt_radiosity_solve(ctx, C.byref(q))
+    if st not in (A.VT_OK, A.VT_ERR_NOT_CONVERGED):
+        check(st, ctx)
+    return B, {"iters": q.iters, "refinements": q.refinements, "residual": q.residual, "ms": q.ms, "status": st}
+
+
+def form_factors(centres, normals, areas, out=None, ctx=None):
+    lib = load()
+    ctx = ctx or _Ctx.get()
+    C_ = np.ascontiguousarray(centres, np.float32)
+    n = len(C_)
+    N_ = np.ascontiguousarray(normals, np.float32)
+    A_ = np.ascontiguousarray(areas, np.float32)
+    if out is None:
+        out = np.zeros((n, n), np.float32)
+    optr = C.c_void_p(out.data_ptr()) if hasattr(out, "data_ptr") else out.ctypes.data_as(C.c_void_p)
+    check(lib.vt_form_factors(ctx, n, _p(C_), _p(N_), _p(A_), optr), ctx)
+    return out
+
+
+def build_bvh(pos, idx, leaf_size=4) -> dict:
+    """gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}) -> {nodes (uint32 words), nodeCount, order, bmin, bmax, maxDepth}."""
+    lib = load()
+    pos = np.ascontiguousarray(pos, np.float32).ravel()
+    idx = np.ascontiguousarray(idx, np.uint32).ravel()
+    n = len(idx) // 3
+    cap = lib.vt_bvh_capacity(n, leaf_size)
+    nodes = np.zeros(cap * 16, np.uint32)
+    order = np.zeros(max(1, n), np.uint32)
+    res = A.vt_bvh_result()
+    check(lib.vt_bvh_build(_p(pos), len(pos) // 3, _p(idx), n, leaf_size, _p(nodes), _p(order), C.byref(res)))
+    return {"nodes": nodes[: res.node_count * 16].copy(), "nodeCount": res.node_count, "order": order[:n].copy(),
+            "bmin": np.array(res.bmin[:]), "bmax": np.array(res.bmax[:]), "maxDepth": res.max_depth}
