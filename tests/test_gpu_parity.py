@@ -175,7 +175,7 @@ def test_sensor_expose_bit_exact():
     E[..., :3] = rng.gamma(2.0, 8.0, (H, W, 3)).astype(np.float32)
     E[: H // 4] *= 20.0
     for p, seed in ((S.unit_radiance_sensor(), 5), (S.sensor_params({"cfa": "GRBG", "esfSigmaPx": 0.7, "fullWell": 150.0}), 6)):
-        su = S.pack_sensor_uniform(p, W, H, seed=seed, frame=2, cam_index=1, exposure=1.0 if p["conversionGain"] == 1.0 else 2e-11)
+        su = S.pack_sensor_uniform(p, W, H, seed=seed, frame=2, cam_index=1, exposure=1.0 if p["conversionGain"] == 1.0 else 3e-7)
         ref = O.sensor_expose(su, E)
         r = TwinRenderer.create(dome.make_dome_scene(seed=1, width=32, height=24, level=1))
         sw = A.vt_sensor_uniform()

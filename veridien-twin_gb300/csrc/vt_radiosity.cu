@@ -96,10 +96,11 @@ __global__ void __launch_bounds__(G_THREADS) jacobi_gemm_fp32_kernel(const float
       const uint32_t gr = row0 + r, gk = k0 + c4 * 4;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (gr < n) {
-        if (gk + 3 < n) v = __ldcs(reinterpret_cast<const float4*>(F + size_t(gr) * n + gk));
+        const float* p = F + size_t(gr) * n;
+        if ((n & 3u) == 0u && gk + 3 < n) v = __ldcs(reinterpret_cast<const float4*>(p + gk));   // 16-byte aligned rows
         else {
-          const float* p = F + size_t(gr) * n;
           v.x = gk < n ? p[gk] : 0.f; v.y = gk + 1 < n ? p[gk + 1] : 0.f; v.z = gk + 2 < n ? p[gk + 2] : 0.f;
+          v.w = gk + 3 < n ? p[gk + 3] : 0.f;
         }
       }
       As[c4 * 4 + 0][r] = v.x; As[c4 * 4 + 1][r] = v.y; As[c4 * 4 + 2][r] = v.z; As[c4 * 4 + 3][r] = v.w;
