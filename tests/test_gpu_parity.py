@@ -92,8 +92,12 @@ def test_random_rays_with_posed_bodies(inst_scene, inst_poses):
     ref.set_poses(inst_poses)
     rng = np.random.default_rng(2)
     n = 20000
-    # rays aimed at the instruments and the lamps (posed bodies), and scattered ones
-    tgt = np.concatenate([rng.normal([0, 0, 1.15], 0.3, (n // 2, 3)), rng.uniform([-3, -3, 0], [3, 3, 3], (n // 2, 3))])
+    # half the rays aimed at points on the instruments' axes (posed capsules, r = 6 mm), half scattered
+    T = inst_poses[1:].reshape(-1, 4, 4).transpose(0, 2, 1)            # row-major body-to-dome
+    k = rng.integers(0, len(T), n // 2)
+    s = rng.uniform(0.0, 0.25, n // 2)
+    on_axis = T[k, :3, 3] + T[k, :3, 2] * s[:, None] + rng.normal(0, 0.003, (n // 2, 3))
+    tgt = np.concatenate([on_axis, rng.uniform([-3, -3, 0], [3, 3, 3], (n // 2, 3))])
     org = rng.uniform([-2.5, -2.5, 0.2], [2.5, 2.5, 3.0], (n, 3))
     d = tgt - org
     d /= np.linalg.norm(d, axis=1, keepdims=True)

@@ -12,6 +12,7 @@
 
 #include "vt_host.h"
 #include "vt_kernels.cuh"
+#include "vt_wave.cuh"
 
 struct vt_ctx {
   int device = 0;
@@ -27,8 +28,10 @@ struct vt_ctx {
   float4 *d_nodes = nullptr, *d_tris = nullptr, *d_verts = nullptr, *d_params = nullptr, *d_nstate = nullptr;
   float* d_su = nullptr;
   uint32_t* d_dbg = nullptr;
-  uint32_t* d_work = nullptr;   // tile counter of the persistent render kernel
-  int render_blocks = 0;
+  uint32_t* d_work = nullptr;   // queue counters of the wavefront path tracer
+  int wave_blocks = 0;
+  void* d_wave = nullptr;       // wavefront path state (grown on demand)
+  size_t wave_cap = 0;
   struct Cam { float4* radiance = nullptr; float* raw = nullptr; bool rendered = false, exposed = false; };
   std::vector<Cam> cams;
   // scratch for ray queries and the solver (grown on demand)
@@ -175,7 +178,7 @@ vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx**
   }
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  ctx->render_blocks = std::max(1, sms) * vtk::render_blocks_per_sm();
+  ctx->wave_blocks = std::max(1, sms) * vtk::wave_blocks_per_sm();
   // no poses yet: bodies of kind 'fixed' at identity, the rest hidden (gpu/renderer.js:259 setPoses({bodies: {}}))
   ctx->inst = vt::poses_from(S, nullptr, nullptr, 0);
   if ((s = write_su(ctx)) != VT_OK) return bail(s);
@@ -189,7 +192,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); }
   cudaFree(ctx->d_nodes); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
-  cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch);
+  cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -345,15 +348,30 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   cp.w = c.width; cp.h = c.height;
   cp.spp = std::min(std::max(q->spp, 1u), q->mode == VT_SHADE_TWIN ? 64u : 4096u);   // kernels.wgsl.js:169 clamps to 64
   cp.seed = q->seed; cp.cam_index = q->camera; cp.options = q->options; cp.skip = skip_mask(ctx, q->camera);
-  cp.n_light = q->light_samples; cp.mode = q->mode; cp.max_depth = std::max(1u, std::min(q->max_depth, 64u)); cp.root = q->root;
+  cp.n_light = std::min(std::max(q->light_samples, 1u), 16u);   // shade.wgsl.js:270 clamps to 16
+  cp.mode = q->mode;
+  cp.max_depth = std::max(1u, std::min(q->max_depth, 64u));
+  cp.root = q->root;
   cp.t0 = q->shutter[0]; cp.t1 = q->shutter[1]; cp.scale = q->scale;
   if (q->frame != ctx->frame) { ctx->frame = q->frame; vt_status s = write_su(ctx); if (s != VT_OK) return s; }
-  VT_CK(cudaMemsetAsync(ctx->d_work, 0, 4, ctx->stream));
+  // wave of up to 8 M paths (whole sub-sample indices): ~1.4 GB of path state at one light sample
+  const uint32_t n_pix = ((c.width + vtk::TILE_W - 1) / vtk::TILE_W) * ((c.height + vtk::TILE_H - 1) / vtk::TILE_H) * vtk::TILE_W * vtk::TILE_H;
+  const uint32_t per_wave = std::max(1u, std::min(cp.spp, (8u << 20) / std::max(1u, n_pix)));
+  const uint32_t paths = per_wave * n_pix;
+  const size_t need = vtk::wave_bytes(paths, cp.n_light, n_pix);
+  if (ctx->wave_cap < need) {
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->d_wave);
+    ctx->d_wave = nullptr;
+    ctx->wave_cap = 0;
+    if (cudaMalloc(&ctx->d_wave, need) != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "wavefront state allocation failed"); }
+    ctx->wave_cap = need;
+  }
+  const vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, paths, cp.n_light, n_pix, ctx->d_work);
   VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  vtk::launch_render(dev_scene(ctx), cp, ctx->cams[q->camera].radiance, ctx->d_work, ctx->render_blocks, ctx->stream);
+  vtk::wave_render(dev_scene(ctx), cp, wb, paths, ctx->cams[q->camera].radiance, ctx->wave_blocks, ctx->stream, &ctx->tim.launches);
   VT_CK(cudaGetLastError());
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
-  ctx->tim.launches++;
   ctx->cams[q->camera].rendered = true;
   if (out_rgba) {
     vt_status s = from_device(ctx, out_rgba, ctx->cams[q->camera].radiance, size_t(c.width) * c.height * 16);

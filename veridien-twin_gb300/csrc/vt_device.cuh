@@ -410,27 +410,31 @@ __device__ __forceinline__ bool seg_near_capsule(float3 o, float3 d, float t0, f
   return dot(q, q) <= r * r;
 }
 // the static BVH (mask 1) and every posed body's BLAS in its own frame at the ray's time (mask 2); skip: bodies
-// this ray ignores (gpu/wgsl/trace.wgsl.js:302 traceSceneSkip)
+// this ray ignores (gpu/wgsl/trace.wgsl.js:302 traceSceneSkip). The static BVH is visited first, then the
+// instances in order, through a single traversal call site (k = -1 is the static BVH).
 template <bool ANY>
 __device__ __forceinline__ Hit trace_scene(const Scene& S, uint32_t root, float3 o, float3 d, float tmin, float tmax, float time,
                                            uint32_t mask, uint32_t skip) {
   Hit best{tmax, 0.0f, 0.0f, MISS, MISS};
-  if (mask & 1u) {
-    if (traverse<ANY>(S, root, o, d, tmin, best, MISS)) return best;
-  }
-  if (mask & 2u) {
-    const float3 inv = safe_inv(d);
-    const uint32_t n = min(ldu(S.su + 16), uint32_t(VT_MAX_INST));
-    for (uint32_t i = 0; i < n; i++) {
-      const float* I = inst_rec(S, i);
-      if ((ldu(I + 15) & 2u) || ((skip >> i) & 1u)) continue;
+  const int n_inst = (mask & 2u) ? int(min(ldu(S.su + 16), uint32_t(VT_MAX_INST))) : 0;
+  const float3 inv = safe_inv(d);
+  for (int k = (mask & 1u) ? -1 : 0; k < n_inst; k++) {
+    uint32_t r = root, id = MISS;
+    float3 ol = o, dl = d;
+    if (k >= 0) {
+      const float* I = inst_rec(S, uint32_t(k));
+      if ((ldu(I + 15) & 2u) || ((skip >> k) & 1u)) continue;
       if (slab(ld3(I + 16), ld3(I + 20), o, inv, tmin, best.t) >= best.t) continue;
       if (!seg_near_capsule(o, d, tmin, fminf(best.t, 1e3f), ld3(I + 32), ld3(I + 36), __ldg(I + 35))) continue;
       Rot R;
       float3 p;
-      inst_pose(S, i, time, R, p);
-      if (traverse<ANY>(S, ldu(I + 11), rtmul(R, o - p), rtmul(R, d), tmin, best, i)) return best;
+      inst_pose(S, uint32_t(k), time, R, p);
+      ol = rtmul(R, o - p);
+      dl = rtmul(R, d);
+      r = ldu(I + 11);
+      id = uint32_t(k);
     }
+    if (traverse<ANY>(S, r, ol, dl, tmin, best, id)) return best;
   }
   return best;
 }
@@ -580,148 +584,37 @@ __device__ __forceinline__ float3 node_slot(const Scene& S, const Surf& s, uint3
 }
 
 // ------------------------------------------------------------------------------------------------ estimators
-// one emitter sample with its shadow ray, MIS-weighted (power heuristic, nL light samples : 1 BSDF sample)
-// against BSDF sampling when `mis` (gpu/wgsl/shade.wgsl.js:160 directLight, exact shadows)
-__device__ __forceinline__ float3 direct_light(const Scene& S, uint32_t root, const Surf& s, float3 n, const Mat& M, float3 wo, float time,
-                                               float3 u, bool mis, float nL) {
+// One emitter sample: its contribution before the shadow test, MIS-weighted (power heuristic, nL light samples : 1
+// BSDF sample) against BSDF sampling when `mis`, and the shadow segment to test (gpu/wgsl/shade.wgsl.js:135
+// lightEval / :160 directLight). Returns false when the sample contributes nothing whatever the visibility.
+__device__ __forceinline__ bool light_sample(const Scene& S, const Surf& s, float3 n, const Mat& M, float3 wo, float time, float3 u, bool mis,
+                                             float nL, float3& c, float3& so, float3& wi, float& tmax) {
   float3 lp, ln, la;
   sample_emitter(S, u, time, lp, ln, la);
-  float3 wi = lp - s.p;
+  wi = lp - s.p;
   const float d2 = dot(wi, wi), dist = sqrtf(d2);
   wi = wi / dist;
+  c = f3(0, 0, 0);
+  so = s.p;
+  tmax = 0.0f;
   const float cosE = dot(-wi, ln);
-  if (cosE <= 0.0f) return f3(0, 0, 0);
+  if (cosE <= 0.0f) return false;
   const float cosS = dot(n, wi);
-  if (cosS <= 0.0f || dot(s.ng, wi) <= 0.0f) return f3(0, 0, 0);
+  if (cosS <= 0.0f || dot(s.ng, wi) <= 0.0f) return false;
   const float3 Le = emitted(S, ln, la, -wi);
-  if (maxc(Le) <= 0.0f) return f3(0, 0, 0);
+  if (maxc(Le) <= 0.0f) return false;
   const float3 f = eval_bsdf(M, n, wi, wo);
-  if (maxc(f) <= 0.0f) return f3(0, 0, 0);
-  const Hit sh = trace_scene<true>(S, root, offset_ray(s.p, s.ng, wi), wi, 0.0f, dist - 2e-5f, time, 3u, ldu(S.su + 7));
-  if (sh.tri != MISS) return f3(0, 0, 0);
+  if (maxc(f) <= 0.0f) return false;
   const float pdfW = d2 / (cosE * __ldg(S.su + 3));
   float w = 1.0f;
   if (mis) {
     const float pb = pdf_bsdf(M, n, wo, wi);
     w = nL * nL * pdfW * pdfW / (nL * nL * pdfW * pdfW + pb * pb);
   }
-  return f * Le * (cosS * w / pdfW);
-}
-
-// radiance along a BSDF-sampled ray from a posed body (gpu/wgsl/shade.wgsl.js:224 secondary)
-__device__ __forceinline__ float3 secondary(const Scene& S, uint32_t root, float3 o, float3 l, float time, float pdfB, uint32_t opts, float nL) {
-  const Hit h = trace_scene<false>(S, root, o, l, 0.0f, BIG, time, 3u, 0u);
-  if (h.tri == MISS) return f3(0, 0, 0);
-  const Surf s = surface(S, h, o, l, time);
-  if (s.flags & VT_F_EMITTER) {
-    if (opts & VT_O_NO_MIS) return f3(0, 0, 0);
-    const float3 nE = emitter_normal(S, h, s, time);
-    const float cosE = dot(-l, nE);
-    if (cosE <= 0.0f) return f3(0, 0, 0);
-    const float3 Le = emitted(S, nE, emitter_axis_at(S, time), -l);
-    const float pdfL = h.t * h.t / (cosE * __ldg(S.su + 3));
-    return Le * (pdfB * pdfB / (pdfB * pdfB + nL * nL * pdfL * pdfL));
-  }
-  if (opts & (VT_O_DIRECT_ONLY | VT_O_NO_INDIRECT)) return f3(0, 0, 0);
-  if (s.flags & VT_F_STATIC) {
-    const uint32_t slot = ldu(S.su + 18);
-    return albedo(S, s.mat, clampf(dot(s.ns, -l), 0.0f, 1.0f)) * node_slot(S, s, slot, slot);
-  }
-  const Mat M2 = load_mat(S, s.mat);
-  return M2.hh * ld3(S.su + 8) * INV_PI_F;
-}
-
-// gpu/wgsl/shade.wgsl.js:250 shadeHit: emitter, nL light samples, and for static surfaces the node radiosity
-// (E_free x capsule visibility x directional albedo / pi), for posed bodies one BSDF bounce into `secondary`.
-// Exact shadows (no shadow culling or occlusion caches); the board print mask is a 1x1 white texture.
-__device__ __forceinline__ float3 shade_twin(const Scene& S, uint32_t root, const Hit& h, float3 o, float3 d, float time, float3 ul, float3 ub,
-                                             uint32_t opts, uint32_t light_index, const Seeds& sd, uint32_t n_light, uint32_t& key) {
-  if (h.tri == MISS) { key = 0xfffeu; return f3(0, 0, 0); }
-  const Surf s = surface(S, h, o, d, time);
-  key = s.mesh | ((h.inst == MISS || (s.flags & VT_F_STATIC)) ? 0u : 0x10000u);
-  const float3 wo = -d;
-  if (opts & VT_O_NORMALS) return s.ns * 0.5f + f3(0.5f, 0.5f, 0.5f);
-  if (s.flags & VT_F_EMITTER) return emitted(S, emitter_normal(S, h, s, time), emitter_axis_at(S, time), wo);
-  const Mat M = load_mat(S, s.mat);
-  const float3 n = shading_normal(S, s, opts);
-  const bool is_static = (s.flags & VT_F_STATIC) != 0u;
-  const bool mis = !is_static && !(opts & VT_O_NO_MIS);
-  const uint32_t nl = min(max(n_light, 1u), 16u);
-  float3 L = direct_light(S, root, s, n, M, wo, time, ul, mis, float(nl));
-  for (uint32_t j = 1; j < nl; j++) {
-    const float3 uj = f3(kr(light_index + j, KL0, sd.s[3]), kr(light_index + j, KL1, sd.s[4]), kr(light_index + j, KL2, sd.s[5]));
-    L = L + direct_light(S, root, s, n, M, wo, time, uj, mis, float(nl));
-  }
-  L = L / float(nl);
-  if (is_static) {
-    if (!(opts & (VT_O_NO_INDIRECT | VT_O_DIRECT_ONLY))) {
-      float3 E = node_slot(S, s, 0u, ldu(S.su + 18));
-      if (!(opts & VT_O_NO_CAPSULE)) E = E * capsule_vis(S, s.p, n);
-      L = L + E * INV_PI_F * albedo(S, s.mat, fmaxf(dot(n, wo), 0.0f));
-    }
-  } else {
-    float3 l;
-    const float pdf = sample_bsdf(M, n, wo, ub, l);
-    if (pdf > 0.0f && dot(s.ng, l) > 0.0f) {
-      const float3 thr = eval_bsdf(M, n, l, wo) * (dot(n, l) / pdf);
-      L = L + thr * secondary(S, root, offset_ray(s.p, s.ng, l), l, time, pdf, opts, float(nl));
-    }
-  }
-  return L;
-}
-
-// Depth-N unidirectional path tracer: at each vertex the emitter (MIS against the previous BSDF sample), nL light
-// samples with MIS, then a BSDF sample continues the path (bounce 1 with the reference's own sample numbers,
-// bounce b >= 2 with further shifts from the pixel hash).
-__device__ __forceinline__ float3 shade_path(const Scene& S, uint32_t root, Hit h, float3 o, float3 d, float time, float3 ul0, float3 ub0,
-                                             uint32_t opts, uint32_t i, const Seeds& sd, uint32_t n_light, uint32_t max_depth, uint32_t& key) {
-  const uint32_t nl = min(max(n_light, 1u), 16u);
-  const bool mis = !(opts & VT_O_NO_MIS);
-  float3 L = f3(0, 0, 0), thr = f3(1, 1, 1);
-  float pdf_prev = 0.0f;
-  key = 0xfffeu;
-  for (uint32_t b = 1; b <= max_depth; b++) {
-    if (b > 1) h = trace_scene<false>(S, root, o, d, 0.0f, BIG, time, 3u, 0u);
-    if (h.tri == MISS) break;
-    const Surf s = surface(S, h, o, d, time);
-    if (b == 1) key = s.mesh | ((h.inst == MISS || (s.flags & VT_F_STATIC)) ? 0u : 0x10000u);
-    const float3 wo = -d;
-    if (s.flags & VT_F_EMITTER) {
-      const float3 nE = emitter_normal(S, h, s, time);
-      const float3 Le = emitted(S, nE, emitter_axis_at(S, time), wo);
-      if (b == 1) {
-        L = L + thr * Le;
-      } else if (mis) {
-        const float cosE = dot(-d, nE);
-        if (cosE > 0.0f) {
-          const float pdfL = h.t * h.t / (cosE * __ldg(S.su + 3));
-          L = L + thr * Le * (pdf_prev * pdf_prev / (pdf_prev * pdf_prev + float(nl) * float(nl) * pdfL * pdfL));
-        }
-      }
-      break;
-    }
-    const Mat M = load_mat(S, s.mat);
-    const float3 n = shading_normal(S, s, opts);
-    float3 Ld = f3(0, 0, 0);
-    const float sh0 = b == 1 ? sd.s[3] : bounce_shift(sd.hs, b, 0);
-    const float sh1 = b == 1 ? sd.s[4] : bounce_shift(sd.hs, b, 1);
-    const float sh2 = b == 1 ? sd.s[5] : bounce_shift(sd.hs, b, 2);
-    for (uint32_t j = 0; j < nl; j++) {
-      const float3 uj = (b == 1 && j == 0) ? ul0 : f3(kr(i * nl + j, KL0, sh0), kr(i * nl + j, KL1, sh1), kr(i * nl + j, KL2, sh2));
-      Ld = Ld + direct_light(S, root, s, n, M, wo, time, uj, mis, float(nl));
-    }
-    L = L + thr * (Ld / float(nl));
-    if (b == max_depth) break;
-    const float3 ub = b == 1 ? ub0 : f3(kr(i, KB0, bounce_shift(sd.hs, b, 3)), kr(i, KB1, bounce_shift(sd.hs, b, 4)), kr(i, KB2, bounce_shift(sd.hs, b, 5)));
-    float3 l;
-    const float pdf = sample_bsdf(M, n, wo, ub, l);
-    if (!(pdf > 0.0f) || dot(s.ng, l) <= 0.0f) break;
-    thr = thr * eval_bsdf(M, n, l, wo) * (dot(n, l) / pdf);
-    pdf_prev = pdf;
-    o = offset_ray(s.p, s.ng, l);
-    d = l;
-  }
-  return L;
+  c = f * Le * (cosS * w / pdfW);
+  so = offset_ray(s.p, s.ng, wi);
+  tmax = dist - 2e-5f;
+  return true;
 }
 
 }  // namespace vtd

@@ -17,12 +17,8 @@ struct CamParams {
   float t0, t1, scale;
 };
 
-// persistent tile scheduler: warps pull 8x4 pixel tiles from a device counter
+// pixels are enumerated in 8 x 4 tiles, so consecutive paths are neighbouring pixels
 constexpr int TILE_W = 8, TILE_H = 4;
-constexpr int RENDER_THREADS = 128;
-
-void launch_render(const vtd::Scene& S, const CamParams& cp, float4* out, uint32_t* work_counter, int blocks, cudaStream_t st);
-int render_blocks_per_sm();
 void launch_trace(const vtd::Scene& S, const float4* o4, const float4* d4, uint32_t n, uint32_t mask, uint32_t any_hit, uint32_t root,
                   float4* out4, float* out_v, cudaStream_t st);
 void launch_visible(const vtd::Scene& S, float3 c, const float3* pts, uint32_t n, float tol, float time, uint32_t skip, uint8_t* out,

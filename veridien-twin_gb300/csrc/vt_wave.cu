@@ -1,0 +1,318 @@
+// Wavefront path tracing on sm_103a: the camera estimators of the twin (shadeHit, gpu/wgsl/shade.wgsl.js:250,
+// and the depth-N path tracer) split into small kernels that each run one kind of work over compacted queues:
+//
+//   wave_gen       camera rays of a wave of sub-samples (KB4, gpu/wgsl/kernels.wgsl.js:177-185)
+//   wave_extend    closest hit of every queued ray (static BVH + posed bodies)
+//   wave_shade     one path vertex: emitter term, light-sample records (shadow-ray queue), BSDF continuation (next
+//                  ray queue); queues are appended with one atomic per warp
+//   wave_shadow    any-hit test of a path's light samples, then L += thr (sum_j visible c_j) / nL in sample order
+//   wave_finalize  per pixel, the sub-samples' radiance summed in sample order (deterministic), the pixel key
+//
+// Path state lives in structure-of-arrays buffers in HBM (~200 B per path per bounce of traffic); the traversal
+// kernels read only the ray and write only the hit, so their code and register footprint stay small and every lane
+// of a warp runs the same kind of ray. The per-path arithmetic is the megakernel's: results do not depend on the
+// order in which paths sit in a queue.
+#include <algorithm>
+
+#include "vt_wave.cuh"
+
+namespace vtk {
+using namespace vtd;
+
+constexpr int WAVE_THREADS = 256;
+
+// append `want` lanes' items to a queue with one atomic per warp; returns the slot of this lane (if want)
+__device__ __forceinline__ uint32_t warp_append(uint32_t* count, bool want) {
+  const uint32_t act = __activemask();
+  const uint32_t mask = __ballot_sync(act, want);
+  if (!mask) return 0;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, uint32_t(__popc(mask)));
+  base = __shfl_sync(act, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// pixel id (tiled 8 x 4 order, so consecutive paths are neighbouring pixels) -> x, y
+__device__ __forceinline__ bool pixel_xy(const CamParams& cp, uint32_t id, uint32_t& x, uint32_t& y) {
+  const uint32_t tiles_x = (cp.w + TILE_W - 1) / TILE_W;
+  const uint32_t tile = id / (TILE_W * TILE_H), within = id % (TILE_W * TILE_H);
+  x = (tile % tiles_x) * TILE_W + within % TILE_W;
+  y = (tile / tiles_x) * TILE_H + within / TILE_W;
+  return x < cp.w && y < cp.h;
+}
+
+// paths of the wave: sub-sample index i in [i0, i0 + n_i), pixel id in [0, n_pix); path p = (i - i0) * n_pix + id
+__global__ void __launch_bounds__(WAVE_THREADS) wave_gen(const CamParams cp, WaveBufs wb, uint32_t i0, uint32_t n_i, uint32_t n_pix) {
+  const uint32_t total = n_i * n_pix;
+  const float3 rx = f3(cp.rx[0], cp.rx[1], cp.rx[2]), ry = f3(cp.ry[0], cp.ry[1], cp.ry[2]), rz = f3(cp.rz[0], cp.rz[1], cp.rz[2]);
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const uint32_t id = p % n_pix, i = i0 + p / n_pix;
+    uint32_t x, y;
+    const bool valid = pixel_xy(cp, id, x, y);
+    const uint32_t hs = hash3(x, y, cp.seed * 64u + cp.cam_index);   // kernels.wgsl.js:35 pixSeeds
+    float3 d = f3(0, 0, 1);
+    float tt = 0.0f;
+    if (valid) {
+      const float u = __fsub_rn(__fadd_rn(float(x), kr(i, R2A, u01(pcg(hs)))), 0.5f);
+      const float v = __fsub_rn(__fadd_rn(float(y), kr(i, R2B, u01(pcg(hs + 1u)))), 0.5f);
+      tt = mixr(cp.t0, cp.t1, kr(i, GOLD, u01(pcg(hs + 2u))));
+      const float3 dc = kb4_unproject(cp.lens, u, v);
+      d = normalize(rx * dc.x + ry * dc.y + rz * dc.z);
+    }
+    wb.o[p] = make_float4(cp.pos[0], cp.pos[1], cp.pos[2], tt);
+    wb.d[p] = make_float4(d.x, d.y, d.z, 0.0f);
+    wb.thr[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    wb.L[p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xfffeu));
+    wb.meta[p] = make_uint4(id, i, hs, valid ? 1u : 0u);      // bounce 1 (0: no pixel)
+    const uint32_t slot = warp_append(wb.count_in, valid);
+    if (valid) wb.q_in[slot] = p;
+  }
+}
+
+__global__ void __launch_bounds__(WAVE_THREADS) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
+  const uint32_t n = *wb.count_in;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = wb.q_in[k];
+    const float4 o = wb.o[p], d = wb.d[p];
+    const uint32_t b = wb.meta[p].w;
+    const Hit h = trace_scene<false>(S, cp.root, xyz(o), xyz(d), 0.0f, BIG, o.w, 3u, b == 1 ? cp.skip : 0u);
+    wb.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+    wb.hinst[p] = h.inst;
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S, const CamParams cp, WaveBufs wb) {
+  const uint32_t n = *wb.count_in;
+  const uint32_t nl = cp.n_light;
+  const bool no_mis = (cp.options & VT_O_NO_MIS) != 0u;
+  const float emit_area = __ldg(S.su + 3);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = wb.q_in[k];
+    const uint4 meta = wb.meta[p];
+    const uint32_t i = meta.y, hs = meta.z, b = meta.w;
+    const float4 o4 = wb.o[p], d4 = wb.d[p], hv = wb.hit[p];
+    float4 L4 = wb.L[p];
+    float3 L = xyz(L4), thr = xyz(wb.thr[p]);
+    const float3 o = xyz(o4), d = xyz(d4);
+    const float tt = o4.w, pdf_prev = d4.w;
+    Hit h{hv.x, hv.y, hv.z, __float_as_uint(hv.w), wb.hinst[p]};
+    bool cont = false, shadow = false;
+    if (h.tri != MISS) {
+      const Surf s = surface(S, h, o, d, tt);
+      const float3 wo = -d;
+      const bool is_static = (s.flags & VT_F_STATIC) != 0u;
+      if (b == 1) L4.w = __uint_as_float(s.mesh | ((h.inst == MISS || is_static) ? 0u : 0x10000u));
+      if (MODE == VT_SHADE_TWIN && b == 2) {
+        // gpu/wgsl/shade.wgsl.js:224 secondary
+        if (s.flags & VT_F_EMITTER) {
+          if (!no_mis) {
+            const float3 nE = emitter_normal(S, h, s, tt);
+            const float cosE = dot(-d, nE);
+            if (cosE > 0.0f) {
+              const float3 Le = emitted(S, nE, emitter_axis_at(S, tt), -d);
+              const float pdfL = h.t * h.t / (cosE * emit_area);
+              L = L + thr * (Le * (pdf_prev * pdf_prev / (pdf_prev * pdf_prev + float(nl) * float(nl) * pdfL * pdfL)));
+            }
+          }
+        } else if (!(cp.options & (VT_O_DIRECT_ONLY | VT_O_NO_INDIRECT))) {
+          if (is_static) {
+            const uint32_t slot = ldu(S.su + 18);
+            L = L + thr * (albedo(S, s.mat, clampf(dot(s.ns, -d), 0.0f, 1.0f)) * node_slot(S, s, slot, slot));
+          } else {
+            const Mat M2 = load_mat(S, s.mat);
+            L = L + thr * (M2.hh * ld3(S.su + 8) * INV_PI_F);
+          }
+        }
+      } else if (MODE == VT_SHADE_TWIN && (cp.options & VT_O_NORMALS)) {
+        L = s.ns * 0.5f + f3(0.5f, 0.5f, 0.5f);
+      } else if (s.flags & VT_F_EMITTER) {
+        const float3 nE = emitter_normal(S, h, s, tt);
+        const float3 Le = emitted(S, nE, emitter_axis_at(S, tt), wo);
+        if (b == 1) {
+          L = L + thr * Le;
+        } else if (!no_mis) {
+          const float cosE = dot(-d, nE);
+          if (cosE > 0.0f) {
+            const float pdfL = h.t * h.t / (cosE * emit_area);
+            L = L + thr * Le * (pdf_prev * pdf_prev / (pdf_prev * pdf_prev + float(nl) * float(nl) * pdfL * pdfL));
+          }
+        }
+      } else {
+        const Mat M = load_mat(S, s.mat);
+        const float3 n = shading_normal(S, s, cp.options);
+        const bool mis = !no_mis && (MODE == VT_SHADE_PATH || !is_static);
+        const float sh0 = b == 1 ? u01(pcg(hs + 3u)) : bounce_shift(hs, b, 0);
+        const float sh1 = b == 1 ? u01(pcg(hs + 4u)) : bounce_shift(hs, b, 1);
+        const float sh2 = b == 1 ? u01(pcg(hs + 5u)) : bounce_shift(hs, b, 2);
+        // nL emitter samples: the unshadowed contribution and the shadow segment of each (shade.wgsl.js:135 lightEval)
+        float4* rec = wb.sh + size_t(p) * nl * 3;
+        for (uint32_t j = 0; j < nl; j++) {
+          const float3 u = f3(kr(i * nl + j, KL0, sh0), kr(i * nl + j, KL1, sh1), kr(i * nl + j, KL2, sh2));
+          float3 c, so, wi;
+          float tmax;
+          const bool ok = light_sample(S, s, n, M, wo, tt, u, mis, float(nl), c, so, wi, tmax);
+          rec[3 * j] = make_float4(so.x, so.y, so.z, tmax);
+          rec[3 * j + 1] = make_float4(wi.x, wi.y, wi.z, ok ? 1.0f : 0.0f);
+          rec[3 * j + 2] = make_float4(c.x, c.y, c.z, 0.0f);
+          shadow |= ok;
+        }
+        if (shadow) wb.nee[p] = make_float4(thr.x, thr.y, thr.z, tt);
+        bool bounce;
+        if (MODE == VT_SHADE_TWIN) {
+          bounce = !is_static;
+          if (is_static && !(cp.options & (VT_O_NO_INDIRECT | VT_O_DIRECT_ONLY))) {
+            float3 E = node_slot(S, s, 0u, ldu(S.su + 18));
+            if (!(cp.options & VT_O_NO_CAPSULE)) E = E * capsule_vis(S, s.p, n);
+            L = L + E * INV_PI_F * albedo(S, s.mat, fmaxf(dot(n, wo), 0.0f));
+          }
+        } else {
+          bounce = b < cp.max_depth;
+        }
+        if (bounce) {
+          const float3 ub = b == 1 ? f3(kr(i, KB0, u01(pcg(hs + 6u))), kr(i, KB1, u01(pcg(hs + 7u))), kr(i, KB2, u01(pcg(hs + 8u))))
+                                   : f3(kr(i, KB0, bounce_shift(hs, b, 3)), kr(i, KB1, bounce_shift(hs, b, 4)), kr(i, KB2, bounce_shift(hs, b, 5)));
+          float3 l;
+          const float pdf = sample_bsdf(M, n, wo, ub, l);
+          if (pdf > 0.0f && dot(s.ng, l) > 0.0f) {
+            thr = thr * eval_bsdf(M, n, l, wo) * (dot(n, l) / pdf);
+            const float3 no = offset_ray(s.p, s.ng, l);
+            wb.o[p] = make_float4(no.x, no.y, no.z, tt);
+            wb.d[p] = make_float4(l.x, l.y, l.z, pdf);
+            wb.thr[p] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+            wb.meta[p] = make_uint4(meta.x, meta.y, meta.z, b + 1u);
+            cont = true;
+          }
+        }
+      }
+    }
+    wb.L[p] = make_float4(L.x, L.y, L.z, L4.w);
+    const uint32_t qs = warp_append(wb.count_out, cont);
+    if (cont) wb.q_out[qs] = p;
+    const uint32_t ss = warp_append(wb.count_sh, shadow);
+    if (shadow) wb.q_sh[ss] = p;
+  }
+}
+
+__global__ void __launch_bounds__(WAVE_THREADS) wave_shadow(const Scene S, const CamParams cp, WaveBufs wb) {
+  const uint32_t n = *wb.count_sh;
+  const uint32_t nl = cp.n_light;
+  const uint32_t skip = ldu(S.su + 7);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = wb.q_sh[k];
+    const float4 nee = wb.nee[p];
+    const float4* rec = wb.sh + size_t(p) * nl * 3;
+    float3 Ld = f3(0, 0, 0);
+    for (uint32_t j = 0; j < nl; j++) {
+      const float4 a = rec[3 * j], w = rec[3 * j + 1];
+      if (w.w == 0.0f) continue;
+      const Hit sh = trace_scene<true>(S, cp.root, xyz(a), xyz(w), 0.0f, a.w, nee.w, 3u, skip);
+      if (sh.tri == MISS) Ld = Ld + xyz(rec[3 * j + 2]);
+    }
+    const float4 L = wb.L[p];
+    const float3 v = xyz(L) + xyz(nee) * (Ld / float(nl));
+    wb.L[p] = make_float4(v.x, v.y, v.z, L.w);
+  }
+}
+
+// per pixel, the wave's sub-samples in order i0..i0+n_i-1 added to the running sum; the last wave writes the pixel
+__global__ void __launch_bounds__(WAVE_THREADS) wave_finalize(const CamParams cp, WaveBufs wb, uint32_t i0, uint32_t n_i, uint32_t n_pix,
+                                                             float4* __restrict__ acc, float4* __restrict__ out, int last) {
+  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n_pix; id += gridDim.x * blockDim.x) {
+    uint32_t x, y;
+    if (!pixel_xy(cp, id, x, y)) continue;
+    float4 a = i0 == 0 ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[id];
+    float3 s = xyz(a);
+    uint32_t key = __float_as_uint(a.w);
+    for (uint32_t k = 0; k < n_i; k++) {
+      const float4 L = wb.L[size_t(k) * n_pix + id];
+      s = s + xyz(L);
+      const uint32_t gk = __float_as_uint(L.w);
+      if (i0 + k == 0) key = gk;
+      else if ((gk & 0xffffu) != (key & 0xffffu)) key |= 0x40000u;
+      key |= gk & 0x30000u;
+    }
+    if (last) {
+      const float sc = cp.scale / float(cp.spp);
+      out[size_t(y) * cp.w + x] = make_float4(s.x * sc, s.y * sc, s.z * sc, key == 0xfffeu ? 0.0f : 1.0f);
+    } else {
+      acc[id] = make_float4(s.x, s.y, s.z, __uint_as_float(key));
+    }
+  }
+}
+
+size_t wave_bytes(uint32_t paths, uint32_t n_light, uint32_t n_pix) {
+  const size_t P = paths;
+  return P * (16 * 7 + 4 * 4) + P * size_t(n_light) * 48 + size_t(n_pix) * 16 + 16 * 256;
+}
+
+WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix, uint32_t* counts) {
+  char* c = static_cast<char*>(base);
+  auto take = [&](size_t bytes) { char* r = c; c += (bytes + 255) / 256 * 256; return r; };
+  const size_t P = paths;
+  WaveBufs w{};
+  w.o = reinterpret_cast<float4*>(take(P * 16));
+  w.d = reinterpret_cast<float4*>(take(P * 16));
+  w.thr = reinterpret_cast<float4*>(take(P * 16));
+  w.L = reinterpret_cast<float4*>(take(P * 16));
+  w.hit = reinterpret_cast<float4*>(take(P * 16));
+  w.nee = reinterpret_cast<float4*>(take(P * 16));
+  w.meta = reinterpret_cast<uint4*>(take(P * 16));
+  w.hinst = reinterpret_cast<uint32_t*>(take(P * 4));
+  w.qa = reinterpret_cast<uint32_t*>(take(P * 4));
+  w.qb = reinterpret_cast<uint32_t*>(take(P * 4));
+  w.q_sh = reinterpret_cast<uint32_t*>(take(P * 4));
+  w.sh = reinterpret_cast<float4*>(take(P * size_t(n_light) * 48));
+  w.acc = reinterpret_cast<float4*>(take(size_t(n_pix) * 16));
+  w.counts = counts;
+  return w;
+}
+
+// one camera: waves of whole sub-sample indices, each bounce extend -> shade -> shadow over compacted queues
+void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave_paths, float4* out, int blocks, cudaStream_t st,
+                 uint64_t* launches) {
+  const uint32_t tiles = ((cp.w + TILE_W - 1) / TILE_W) * ((cp.h + TILE_H - 1) / TILE_H);
+  const uint32_t n_pix = tiles * TILE_W * TILE_H;
+  const uint32_t per_wave = std::max(1u, std::min(cp.spp, wave_paths / n_pix));
+  const uint32_t depth = cp.mode == VT_SHADE_TWIN ? 2u : cp.max_depth;
+  uint64_t nlaunch = 0;
+  for (uint32_t i0 = 0; i0 < cp.spp; i0 += per_wave) {
+    const uint32_t n_i = std::min(per_wave, cp.spp - i0);
+    cudaMemsetAsync(wb.counts, 0, 16, st);
+    WaveBufs w = wb;
+    w.q_in = wb.qa; w.count_in = wb.counts + 0;
+    wave_gen<<<blocks, WAVE_THREADS, 0, st>>>(cp, w, i0, n_i, n_pix);
+    nlaunch++;
+    for (uint32_t b = 1; b <= depth; b++) {
+      // queue of this bounce in (qa | qb), next bounce's in the other; counters 0/1 alternate, 2 + b is the shadow count
+      w.q_in = (b & 1) ? wb.qa : wb.qb;
+      w.q_out = (b & 1) ? wb.qb : wb.qa;
+      w.count_in = wb.counts + ((b & 1) ? 0 : 1);
+      w.count_out = wb.counts + ((b & 1) ? 1 : 0);
+      w.count_sh = wb.counts + 2;
+      cudaMemsetAsync(w.count_out, 0, 4, st);
+      cudaMemsetAsync(w.count_sh, 0, 4, st);
+      wave_extend<<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+      if (cp.mode == VT_SHADE_TWIN) wave_shade<VT_SHADE_TWIN><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+      else wave_shade<VT_SHADE_PATH><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+      wave_shadow<<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+      nlaunch += 3;
+    }
+    const int last = i0 + n_i >= cp.spp;
+    wave_finalize<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb, i0, n_i, n_pix, wb.acc, out, last);
+    nlaunch++;
+  }
+  if (launches) *launches += nlaunch;
+}
+
+int wave_blocks_per_sm() {
+  int a = 0, b = 0, c = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, wave_extend, WAVE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_shade<VT_SHADE_PATH>, WAVE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, wave_shadow, WAVE_THREADS, 0);
+  return std::max(1, std::max(a, std::max(b, c)));
+}
+
+}  // namespace vtk

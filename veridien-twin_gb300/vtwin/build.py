@@ -16,7 +16,10 @@ CSRC = os.path.join(ROOT, "csrc")
 OBJ = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libvtwin.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math", "--expt-relaxed-constexpr"]
+# host code: no FMA contraction (aarch64 gcc contracts a*b+c by default), so the host scene preparation gives the
+# same bits on x86 and Arm
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math", "-Xcompiler", "-ffp-contract=off",
+          "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:
