@@ -258,6 +258,18 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* req);
 vt_status vt_form_factors(vt_ctx* ctx, uint32_t n, const float* centres, const float* normals, const float* areas,
                           float* F);
 
+/* One-right-hand-side node radiosity (B = E + diag(rho) F B, plain FP32 Jacobi as vt_radiosity_solve) that allocates
+ * no device memory. No counterpart in the reference. For callers that cannot allocate while they run: a per-frame
+ * loop with a fixed time budget (cudaMalloc/cudaFree may synchronise the device) or a host that sizes all its device
+ * memory up front. F (n x n), rho (n), E (n) and B (n, out) are device pointers the caller owns; scratch is a static
+ * device array of VT_STATIC_SOLVE_MAX_N nodes (about 160 KB) that every GPU loading the library holds until exit.
+ * n > VT_STATIC_SOLVE_MAX_N or a host pointer returns VT_ERR_ARG. The first call on a device looks up the array's
+ * device address (make that first call before any stream capture). All calls share the array: calls that overlap on
+ * the GPU race. stream: a cudaStream_t (NULL = legacy default stream). iters / residual may be NULL. */
+#define VT_STATIC_SOLVE_MAX_N 16384
+vt_status vt_radiosity_solve_static(const float* F, const float* rho, const float* E, float* B, uint32_t n, uint32_t max_iters,
+                                    uint32_t check_every, double tol, void* stream, uint32_t* iters, double* residual);
+
 /* ---------------------------------------------------------------------------------------- bvh (pure) */
 
 /* gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}): binned SAH BVH2 on the host. nodes_out must hold

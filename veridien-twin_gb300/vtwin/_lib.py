@@ -32,6 +32,8 @@ SIGNATURES = {
     "vt_sensor_camera": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_float]),
     "vt_radiosity_solve": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_solve_req)]),
     "vt_form_factors": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_radiosity_solve_static": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                              C.c_double, C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
     "vt_bvh_capacity": (C.c_uint32, [C.c_uint32, C.c_uint32]),
     "vt_bvh_build": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                  C.POINTER(A.vt_bvh_result)]),

@@ -292,6 +292,21 @@ def solve_radiosity(F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=100
     return B, {"iters": q.iters, "refinements": q.refinements, "residual": q.residual, "ms": q.ms, "status": st}
 
 
+def solve_radiosity_static(F, rho, E, B, tol=1e-6, max_iters=1000, check_every=8, stream=None):
+    """One right-hand side, no device allocation (vt_radiosity_solve_static): F, rho, E, B are device tensors
+    (objects with .data_ptr()), B receives the solution. Returns {iters, residual, status}."""
+    lib = load()
+    n = int(rho.shape[0])
+    it = C.c_uint32(0)
+    res = C.c_double(0.0)
+    dp = lambda t: C.c_void_p(t.data_ptr())
+    st = lib.vt_radiosity_solve_static(dp(F), dp(rho), dp(E), dp(B), n, int(max_iters), int(check_every), float(tol),
+                                       C.c_void_p(stream) if stream else None, C.byref(it), C.byref(res))
+    if st not in (A.VT_OK, A.VT_ERR_NOT_CONVERGED):
+        raise VtError(st, "vt_radiosity_solve_static failed")
+    return {"iters": it.value, "residual": res.value, "status": st}
+
+
 def form_factors(centres, normals, areas, out=None, ctx=None):
     lib = load()
     ctx = ctx or _Ctx.get()
