@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_gen(const CamParams cp, Wav
   }
 }
 
-__global__ void __launch_bounds__(WAVE_THREADS) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
+__global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t p = wb.q_in[k];
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S, const 
   }
 }
 
-__global__ void __launch_bounds__(WAVE_THREADS) wave_shadow(const Scene S, const CamParams cp, WaveBufs wb) {
+__global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_sh;
   const uint32_t nl = cp.n_light;
   const uint32_t skip = ldu(S.su + 7);
