@@ -230,8 +230,11 @@ enum { VT_PREC_FP32 = 0, VT_PREC_BF16 = 1, VT_PREC_FP8 = 2 };
 
 /* Dense node radiosity B = E + diag(rho) F B (the lite_nodes / TwinRenderer Jacobi, gpu/wgsl/kernels.wgsl.js
  * :416-461 jacobiGather + jacobiUpdate with Lambertian nodes, gpu/renderer.js:729 _submitJacobi, :804 converge).
- * FP32: plain Jacobi sweeps on CUDA cores. BF16 / FP8 (E4M3, per-row scales): tcgen05 GEMM sweeps with FP32
- * accumulation, recovered by iterative refinement on an accurate residual r = E + rho F B - B (FP64 epilogue). */
+ * FP32: plain Jacobi sweeps on CUDA cores. BF16 / FP8 (E4M3, per-row scales of F, per-column scales of the iterate):
+ * tcgen05 GEMM sweeps with FP32 accumulation solve for a correction, recovered by iterative refinement on an accurate
+ * residual r = E + rho F B - B (F and B split into bf16 high and low parts, FP64 epilogue). BF16/FP8 need n % 16 == 0
+ * and keep converted copies of F in the context (2 x n^2 x 2 B, plus n^2 B for FP8). `iters` counts low-precision
+ * sweeps and `refinements` accurate residuals. */
 typedef struct {
   uint32_t n;              /* nodes */
   uint32_t n_rhs;          /* right-hand sides (columns of E and B) */
@@ -243,6 +246,7 @@ typedef struct {
   uint32_t max_iters;      /* total sweeps */
   uint32_t warm_start;
   uint32_t check_every;    /* sweeps between convergence checks (0 = 8) */
+  uint32_t reuse_f;        /* 1: F is the matrix of this context's previous BF16/FP8 solve: reuse its converted copies */
   double tol;              /* relative residual ||r|| / ||B|| (Frobenius over all right-hand sides) */
   /* outputs */
   uint32_t iters;          /* sweeps done */

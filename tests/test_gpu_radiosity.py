@@ -1,0 +1,47 @@
+"""Mixed-precision node radiosity (tcgen05 BF16 / FP8 sweeps + iterative refinement) against a direct FP64 solve.
+
+The bar (the benchmark spec): at most 1e-4 relative error against FP64, for one and for many right-hand sides.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from vtwin import _abi as A
+from vtwin import dome
+from vtwin.renderer import form_factors, solve_radiosity
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def system():
+    n = 1024
+    P = dome.dome_patches(n, seed=2)
+    F = form_factors(P["centres"], P["normals"], P["areas"])
+    return n, P, F
+
+
+@pytest.mark.parametrize("prec", [A.VT_PREC_BF16, A.VT_PREC_FP8])
+@pytest.mark.parametrize("R", [64, 8])
+def test_mixed_precision_matches_fp64(system, prec, R):
+    n, P, F = system
+    E = dome.radiosity_rhs(n, P["lamps"], R, seed=5)
+    Bd = O.solve_dense(F, P["rho"], E)
+    B, info = solve_radiosity(F, P["rho"], E, precision=prec, tol=1e-6, max_iters=400)
+    err = np.linalg.norm(B - Bd) / np.linalg.norm(Bd)
+    col = np.max(np.linalg.norm(B - Bd, axis=0) / np.linalg.norm(Bd, axis=0))
+    print(f"\nprecision {prec} R={R}: sweeps {info['iters']} refinements {info['refinements']} residual {info['residual']:.2e} "
+          f"rel err {err:.2e} (worst column {col:.2e})")
+    assert info["status"] == A.VT_OK
+    assert err <= 1e-4 and col <= 1e-4
+
+
+def test_reuse_of_converted_f(system):
+    n, P, F = system
+    E = dome.radiosity_rhs(n, P["lamps"], 16, seed=7)
+    from vtwin.renderer import TwinRenderer
+    r = TwinRenderer.create(dome.make_dome_scene(seed=1, width=32, height=24, level=1))
+    B1, i1 = r.solve_radiosity(F, P["rho"], E, precision=A.VT_PREC_BF16, tol=1e-6)
+    B2, i2 = r.solve_radiosity(F, P["rho"], E, precision=A.VT_PREC_BF16, tol=1e-6, reuse_f=True)
+    assert np.array_equal(B1, B2) and i1["iters"] == i2["iters"]
+    r.destroy()

@@ -13,6 +13,7 @@
 #include "vt_host.h"
 #include "vt_kernels.cuh"
 #include "vt_wave.cuh"
+#include "vt_tc.cuh"
 
 struct vt_ctx {
   int device = 0;
@@ -38,6 +39,14 @@ struct vt_ctx {
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
   vt_timings tim{};
+  // mixed-precision radiosity: converted copies of F and the solver's work buffers
+  struct Tc {
+    void* mem = nullptr;
+    size_t bytes = 0;
+    const float* f_src = nullptr;   // F whose copies are held
+    uint32_t n = 0, R = 0, prec = 0;
+    bool have_hi_lo = false, have_q = false;
+  } tc;
 };
 
 namespace {
@@ -192,7 +201,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); }
   cudaFree(ctx->d_nodes); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
-  cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave);
+  cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave); cudaFree(ctx->tc.mem);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -496,6 +505,157 @@ vt_status vt_timings_get(const vt_ctx* ctx, vt_timings* out) {
 
 }  // extern "C"
 
+// ------------------------------------------------------------------------------------------------ mixed precision
+// Iterative refinement (outer, accurate) around low-precision Jacobi (inner, tensor cores):
+//   r = E + rho F B - B            F = F_hi + F_lo and B = B_hi + B_lo in bf16, three tcgen05 products, FP64 epilogue
+//   d <- r + rho F_lp d            BF16 or FP8 (per-row / per-column scales) sweeps until the update stalls
+//   B <- B + d
+// Splits of K are chosen so the grid of 128-row tiles x splits fills whole waves of the SMs.
+namespace {
+uint32_t choose_splits(uint32_t mtiles, uint32_t ktiles, int sms) {
+  uint32_t best = 1;
+  double best_eff = 0;
+  for (uint32_t s = 1; s <= 8 && s <= ktiles; s++) {
+    const double ctas = double(mtiles) * s, waves = std::ceil(ctas / sms);
+    const double eff = ctas / (waves * sms);
+    if (eff > best_eff + 0.02) { best_eff = eff; best = s; }
+  }
+  return best;
+}
+}  // namespace
+
+static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
+  const uint32_t n = q->n, R = q->n_rhs;
+  if (n % 16) return fail(ctx, VT_ERR_ARG, "solve: BF16/FP8 need n % 16 == 0");
+  const bool fp8 = q->precision == VT_PREC_FP8;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const uint32_t mtiles = (n + 127) / 128;
+  const uint32_t kt_bf = (n + 63) / 64, kt_q = (n + 127) / 128;
+  const uint32_t sp_bf = choose_splits(mtiles, kt_bf, sms), sp_q = choose_splits(mtiles, kt_q, sms);
+  const uint32_t sp_max = std::max(sp_bf, sp_q);
+  const size_t nn = size_t(n) * n, nr = size_t(n) * R;
+  const bool dF = is_device_ptr(q->F);
+  // layout of the context's mixed-precision block (each piece 256-byte aligned)
+  size_t off = 0;
+  auto place = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+  const size_t o_f32 = dF ? 0 : place(nn * 4), o_hi = place(nn * 2), o_lo = place(nn * 2), o_q = fp8 ? place(nn) : 0;
+  const size_t o_rs = place(size_t(n) * 4), o_bhi = place(size_t(64) * n * 2), o_blo = place(size_t(64) * n * 2),
+               o_bq = place(size_t(64) * n), o_cs = place(256), o_cm = place(256), o_part = place(size_t(sp_max) * n * 64 * 4),
+               o_E = place(nr * 4), o_rho = place(size_t(n) * 4), o_B = place(nr * 4), o_r = place(nr * 4), o_d = place(nr * 4),
+               o_d2 = place(nr * 4), o_np = place((nr / 256 + 2) * 16), o_err = place(64);
+  auto& T = ctx->tc;
+  const bool same_f = q->reuse_f && T.f_src == q->F && T.n == n && T.mem;
+  if (T.bytes < off) {
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(T.mem);
+    T = vt_ctx::Tc{};
+    if (cudaMalloc(&T.mem, off) != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "solve: mixed-precision buffers"); }
+    T.bytes = off;
+  }
+  char* m = static_cast<char*>(T.mem);
+  const float* F32 = dF ? q->F : reinterpret_cast<float*>(m + o_f32);
+  uint16_t* Fhi = reinterpret_cast<uint16_t*>(m + o_hi);
+  uint16_t* Flo = reinterpret_cast<uint16_t*>(m + o_lo);
+  uint8_t* Fq = fp8 ? reinterpret_cast<uint8_t*>(m + o_q) : nullptr;
+  float* rs = reinterpret_cast<float*>(m + o_rs);
+  uint16_t* Bhi = reinterpret_cast<uint16_t*>(m + o_bhi);
+  uint16_t* Blo = reinterpret_cast<uint16_t*>(m + o_blo);
+  uint8_t* Bq = reinterpret_cast<uint8_t*>(m + o_bq);
+  float* cs = reinterpret_cast<float*>(m + o_cs);
+  uint32_t* cm = reinterpret_cast<uint32_t*>(m + o_cm);
+  float* part = reinterpret_cast<float*>(m + o_part);
+  float* E = reinterpret_cast<float*>(m + o_E);
+  float* rho = reinterpret_cast<float*>(m + o_rho);
+  float* B = reinterpret_cast<float*>(m + o_B);
+  float* r = reinterpret_cast<float*>(m + o_r);
+  float* d = reinterpret_cast<float*>(m + o_d);
+  float* d2 = reinterpret_cast<float*>(m + o_d2);
+  double* np = reinterpret_cast<double*>(m + o_np);
+  uint32_t* err = reinterpret_cast<uint32_t*>(m + o_err);
+  double* norms = reinterpret_cast<double*>(m + o_err + 16);
+  vt_status s;
+  float conv_ms = 0;
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (!(same_f && T.have_hi_lo && (!fp8 || T.have_q))) {
+    if (!dF && (s = to_device(ctx, const_cast<float*>(F32), q->F, nn * 4)) != VT_OK) return s;
+    vtk::tc_split_bf16(F32, Fhi, Flo, nn, ctx->stream);
+    if (fp8) vtk::tc_quant_rows_fp8(F32, Fq, rs, n, ctx->stream);
+    VT_CK(cudaGetLastError());
+    T.f_src = q->F; T.n = n; T.have_hi_lo = true; T.have_q = fp8;
+  }
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  VT_CK(cudaEventSynchronize(ctx->ev1));
+  cudaEventElapsedTime(&conv_ms, ctx->ev0, ctx->ev1);
+  vtk::TcMap mhi, mlo, mq, mbhi, mblo, mbq;
+  int code = 0;
+  if (!vtk::tc_encode(&mhi, Fhi, n, n, 2, 128, &code) || !vtk::tc_encode(&mlo, Flo, n, n, 2, 128, &code) ||
+      !vtk::tc_encode(&mbhi, Bhi, n, 64, 2, 64, &code) || !vtk::tc_encode(&mblo, Blo, n, 64, 2, 64, &code) ||
+      (fp8 && (!vtk::tc_encode(&mq, Fq, n, n, 1, 128, &code) || !vtk::tc_encode(&mbq, Bq, n, 64, 1, 64, &code))))
+    return fail(ctx, VT_ERR_CUDA, "solve: tensor map encoding failed (" + std::to_string(code) + ")");
+  if ((s = to_device(ctx, E, q->E, nr * 4)) != VT_OK) return s;
+  if ((s = to_device(ctx, rho, q->rho, size_t(n) * 4)) != VT_OK) return s;
+  if (q->warm_start) { if ((s = to_device(ctx, B, q->B, nr * 4)) != VT_OK) return s; }
+  else VT_CK(cudaMemcpyAsync(B, E, nr * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  VT_CK(cudaMemsetAsync(err, 0, 64, ctx->stream));
+  const uint32_t max_it = q->max_iters ? q->max_iters : 1000;
+  const double inner_tol = fp8 ? 2e-3 : 1e-3;
+  const uint32_t inner_max = 24;
+  uint32_t sweeps = 0, refinements = 0, npart = 0;
+  double resid = INFINITY;
+  auto read_norms = [&](double* h) -> vt_status {
+    vtk::launch_reduce_partials(np, npart, norms, ctx->stream);
+    VT_CK(cudaGetLastError());
+    VT_CK(cudaMemcpyAsync(h, norms, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+    return VT_OK;
+  };
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (;;) {
+    // accurate residual of the current iterate
+    vtk::tc_pack_b(vtk::TC_BF16X3, B, n, R, Bhi, Blo, nullptr, nullptr, nullptr, ctx->stream);
+    vtk::tc_gemm(vtk::TC_BF16X3, &mhi, &mlo, &mbhi, &mblo, n, sp_bf, (kt_bf + sp_bf - 1) / sp_bf, part, err, ctx->stream);
+    vtk::tc_combine_residual(part, sp_bf, n, R, rho, E, B, r, np, &npart, ctx->stream);
+    ctx->tim.launches += 3;
+    double h[2];
+    if ((s = read_norms(h)) != VT_OK) return s;
+    refinements++;
+    resid = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+    if (resid <= q->tol || sweeps >= max_it) break;
+    // correction: (I - diag(rho) F_lp) d = r by Jacobi sweeps from d = r
+    VT_CK(cudaMemcpyAsync(d, r, nr * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    for (uint32_t k = 0; k < inner_max && sweeps < max_it; k++) {
+      if (fp8) {
+        vtk::tc_pack_b(vtk::TC_FP8, d, n, R, nullptr, nullptr, Bq, cs, cm, ctx->stream);
+        vtk::tc_gemm(vtk::TC_FP8, &mq, nullptr, &mbq, nullptr, n, sp_q, (kt_q + sp_q - 1) / sp_q, part, err, ctx->stream);
+        vtk::tc_combine_sweep(part, sp_q, n, R, rho, r, d, d2, rs, cs, np, &npart, ctx->stream);
+      } else {
+        vtk::tc_pack_b(vtk::TC_BF16, d, n, R, Bhi, nullptr, nullptr, nullptr, nullptr, ctx->stream);
+        vtk::tc_gemm(vtk::TC_BF16, &mhi, nullptr, &mbhi, nullptr, n, sp_bf, (kt_bf + sp_bf - 1) / sp_bf, part, err, ctx->stream);
+        vtk::tc_combine_sweep(part, sp_bf, n, R, rho, r, d, d2, nullptr, nullptr, np, &npart, ctx->stream);
+      }
+      ctx->tim.launches += 3;
+      std::swap(d, d2);
+      sweeps++;
+      if ((s = read_norms(h)) != VT_OK) return s;
+      if (!(h[1] > 0) || std::sqrt(h[0] / h[1]) <= inner_tol) break;
+    }
+    vtk::tc_axpy(B, d, nr, ctx->stream);
+  }
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  uint32_t herr = 0;
+  VT_CK(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if ((s = from_device(ctx, q->B, B, nr * 4)) != VT_OK) return s;
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  q->iters = sweeps; q->refinements = refinements; q->residual = resid; q->ms = ms;
+  ctx->tim.solve_ms = ms;
+  (void)conv_ms;
+  if (herr) return fail(ctx, VT_ERR_TIMEOUT, "solve: a tensor-core pipeline wait ran out");
+  return resid <= q->tol ? VT_OK : VT_ERR_NOT_CONVERGED;
+}
+
 // ------------------------------------------------------------------------------------------------ radiosity solve
 // Plain FP32: Jacobi sweeps B <- E + rho F B on CUDA cores (the matvec for one right-hand side, the FP32 GEMM
 // for several), the relative update checked every `check_every` sweeps. BF16 / FP8: see vt_tc.cu.
@@ -503,7 +663,8 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   if (!ctx || !q || !q->n || !q->n_rhs || !q->F || !q->rho || !q->E || !q->B) return VT_ERR_ARG;
   if (q->n_rhs > 64) return fail(ctx, VT_ERR_ARG, "solve: at most 64 right-hand sides");
   if (q->n_rhs > 1 && (q->n_rhs % 4)) return fail(ctx, VT_ERR_ARG, "solve: several right-hand sides must be a multiple of 4");
-  if (q->precision != VT_PREC_FP32) return fail(ctx, VT_ERR_ARG, "solve: only VT_PREC_FP32 is built in this library");
+  if (q->precision == VT_PREC_BF16 || q->precision == VT_PREC_FP8) return tc_solve(ctx, q);
+  if (q->precision != VT_PREC_FP32) return fail(ctx, VT_ERR_ARG, "solve: unknown precision");
   const uint32_t n = q->n, R = q->n_rhs;
   const size_t nb = size_t(n) * R * 4, nf = size_t(n) * n * 4;
   const bool dF = is_device_ptr(q->F);

@@ -232,8 +232,8 @@ class TwinRenderer:
                 "launches": int(t.launches)}
 
     # ------------------------------------------------------------------------------------------- radiosity
-    def solve_radiosity(self, F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=1000, check_every=8, B0=None):
-        return solve_radiosity(F, rho, E, precision, tol, max_iters, check_every, B0, ctx=self._ctx)
+    def solve_radiosity(self, F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=1000, check_every=8, B0=None, reuse_f=False):
+        return solve_radiosity(F, rho, E, precision, tol, max_iters, check_every, B0, ctx=self._ctx, reuse_f=reuse_f)
 
     def form_factors(self, centres, normals, areas, out=None):
         return form_factors(centres, normals, areas, out, ctx=self._ctx)
@@ -266,7 +266,7 @@ class _Ctx:
         return cls._ctx
 
 
-def solve_radiosity(F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=1000, check_every=8, B0=None, ctx=None):
+def solve_radiosity(F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=1000, check_every=8, B0=None, ctx=None, reuse_f=False):
     """B = E + diag(rho) F B on the device (gpu/renderer.js:804 converge, the lite_nodes Jacobi). F, rho, E are
     numpy arrays (host) or objects exposing an integer device pointer via `.data_ptr()` (device). Returns
     (B, info) with info = {iters, refinements, residual, ms, status}."""
@@ -285,7 +285,7 @@ def solve_radiosity(F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=100
     B = np.ascontiguousarray(B0, np.float32).copy() if B0 is not None else np.zeros((n, R), np.float32)
     q = A.vt_solve_req(n=n, n_rhs=R, F=ptr(keep[0]), rho=ptr(keep[1]), E=ptr(keep[2]), B=B.ctypes.data_as(C.POINTER(C.c_float)),
                        precision=int(precision), max_iters=int(max_iters), warm_start=int(B0 is not None),
-                       check_every=int(check_every), tol=float(tol))
+                       check_every=int(check_every), reuse_f=int(bool(reuse_f)), tol=float(tol))
     st = lib.vt_radiosity_solve(ctx, C.byref(q))
     if st not in (A.VT_OK, A.VT_ERR_NOT_CONVERGED):
         check(st, ctx)
