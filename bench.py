@@ -169,7 +169,7 @@ def main():
     torch.cuda.set_device(local)
     from vtwin import _abi as A
     from vtwin import dome
-    from vtwin.renderer import TwinRenderer, solve_radiosity, form_factors
+    from vtwin.renderer import TwinRenderer
 
     # replicas: every rank renders its own frame of the same workload (views shard with no exchange)
     scene = dome.make_dome_scene(seed=1)
@@ -241,28 +241,71 @@ def main():
             line["cpu_baseline"] = {"value": cv, "unit": "Msamples/s", "cores": info["threads"], "kind": "port",
                                     "sample": f"{info['rows']} of {H_} rows x {W_} px x {SPP} spp ({info['samples']} samples, {info['seconds']:.1f} s)"}
         if not args.no_radiosity:
-            line["radiosity"] = radiosity_bench(solve_radiosity, form_factors, torch)
+            line["radiosity"] = radiosity_bench(torch, cpu_check=not args.no_cpu_baseline)
         print(json.dumps(line))
     r.destroy()
     if dist:
         dist.destroy_process_group()
 
 
-def radiosity_bench(solve, ff, torch):
-    """C1: N = 4096 patches, 1 right-hand side, plain FP32 Jacobi to 1e-6 relative residual (device time)."""
+def radiosity_bench(torch, cpu_check=True):
+    """Node radiosity B = E + diag(rho) F B on the seeded dome patches, plain FP32 against the mixed-precision solves.
+    C1: N = 4096, one right-hand side, to relative residual 1e-6. C2: N = 32768, 64 right-hand sides (random lamp
+    masks, intensities U[10, 100]), to 1e-4 relative error against FP64 (residual tolerance 1e-5). Device times."""
+    from vtwin import _abi as A
     from vtwin import dome
+    from vtwin.renderer import form_factors, solve_radiosity
 
     out = {}
-    P = dome.dome_patches(4096, seed=2)
-    F = torch.empty((4096, 4096), dtype=torch.float32, device="cuda")
-    ff(P["centres"], P["normals"], P["areas"], out=F)
-    E = dome.radiosity_rhs(4096, P["lamps"], 1)
-    solve(F, P["rho"], E, tol=1e-6)                      # warm
-    B, info = solve(F, P["rho"], E, tol=1e-6)
-    out["c1_fp32_ms"] = info["ms"]
-    out["c1_iters"] = info["iters"]
-    out["c1_residual"] = info["residual"]
+    precs = (("fp32", A.VT_PREC_FP32), ("bf16", A.VT_PREC_BF16), ("fp8", A.VT_PREC_FP8))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    for key, n, R, tol in (("c1", 4096, 1, 1e-6), ("c2", 32768, 64, 1e-5)):
+        P = dome.dome_patches(n, seed=2)
+        F = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        form_factors(P["centres"], P["normals"], P["areas"], out=F)
+        E = dome.radiosity_rhs(n, P["lamps"], R, seed=5)
+        res = {"n": n, "rhs": R, "tol": tol}
+        sols = {}
+        for name, prec in precs:
+            solve_radiosity(F, P["rho"], E, precision=prec, tol=tol, max_iters=400)          # warm; converts F once
+            B, info = solve_radiosity(F, P["rho"], E, precision=prec, tol=tol, max_iters=400, reuse_f=True)
+            sols[name] = B
+            sb = {"fp32": 4, "bf16": 2, "fp8": 1}[name]
+            alg = n * n * sb + n * R * 8 + n * 8                     # bytes of one sweep: F, B in and out, rho and E
+            res[name] = {"ms": info["ms"], "sweeps": info["iters"], "refinements": info["refinements"], "residual": info["residual"],
+                         "sweep_ms": info["sweep_ms"], "sweep_gbs": alg / (info["sweep_ms"] / 1e3) / 1e9 if info["sweep_ms"] else None,
+                         "status": info["status"]}
+        for name in ("bf16", "fp8"):
+            res[name]["speedup_vs_fp32"] = res["fp32"]["ms"] / res[name]["ms"]
+        res["roofline_bf16_sweep"] = {"bound": "hbm", "achieved": res["bf16"]["sweep_gbs"], "peak": hbm, "unit": "GB/s",
+                                      "frac": (res["bf16"]["sweep_gbs"] or 0) / hbm, "kernel": "tc_gemm_kernel<BF16>"}
+        if cpu_check:
+            res["cpu_fp64"] = radiosity_cpu_fp64(F, P, E, R, sols)
+        out[key] = res
+        del F
+        torch.cuda.empty_cache()
     return out
+
+
+def radiosity_cpu_fp64(F, P, E, R, sols, cols=8):
+    """CPU baseline of the radiosity and the FP64 check: FP64 Jacobi (the oracle, all host threads) on `cols` of the
+    right-hand-side columns (columns are independent), timed per sweep; the GPU solutions' relative error on them."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    Fh = F.cpu().numpy()
+    pick = np.unique(np.linspace(0, R - 1, min(cols, R)).astype(int))
+    t0 = time.perf_counter()
+    B64, it = O.jacobi64(Fh, P["rho"], np.ascontiguousarray(E[:, pick]), tol=1e-12, max_it=400, threads=os.cpu_count() or 1)
+    dt = time.perf_counter() - t0
+    err = {k: float(np.linalg.norm(v[:, pick] - B64) / np.linalg.norm(B64)) for k, v in sols.items()}
+    return {"columns": [int(c) for c in pick], "sweeps": it, "ms_per_sweep": dt / it * 1e3, "cores": os.cpu_count(),
+            "rel_err_vs_fp64": err}
 
 
 if __name__ == "__main__":

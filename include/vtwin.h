@@ -253,6 +253,7 @@ typedef struct {
   uint32_t refinements;    /* accurate residuals evaluated */
   double residual;         /* final relative residual (accurate) */
   double ms;               /* device time of the solve (CUDA events) */
+  double sweep_ms;         /* mean device time of one GEMM launch of a sweep (BF16/FP8: the tcgen05 kernel) */
 } vt_solve_req;
 vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* req);
 

@@ -1810,28 +1810,37 @@ static void solve_dense(int n, const float* F, const float* rho, const float* E,
   std::copy(X.begin(), X.end(), B);
 }
 
-// FP64 Jacobi B <- E + rho (F B) to a relative update below tol (threads over rows), for large n.
+// FP64 Jacobi B <- E + rho (F B) to a relative update below tol, for large n: threads over blocks of 8 rows, each
+// block streaming the rows of B once (B stays in the caches; the per-row sums over j run in order).
 static int jacobi64(int n, const float* F, const float* rho, const float* E, int R, double* B, double tol, int maxIt, int threads) {
   std::vector<double> Bn(size_t(n) * R);
   for (size_t i = 0; i < size_t(n) * R; i++) B[i] = E[i];
   int it = 0;
+  const int RB = 8;
   for (; it < maxIt; it++) {
-    auto work = [&](int t) {
-      std::vector<double> acc(R);
-      for (int i = t; i < n; i += threads) {
+    std::atomic<int> next(0);
+    auto work = [&]() {
+      std::vector<double> acc(size_t(RB) * R);
+      for (;;) {
+        const int i0 = next.fetch_add(RB);
+        if (i0 >= n) break;
+        const int rows = std::min(RB, n - i0);
         std::fill(acc.begin(), acc.end(), 0.0);
-        const float* Fr = F + size_t(i) * n;
         for (int j = 0; j < n; j++) {
-          double f = Fr[j];
-          if (f == 0) continue;
           const double* Bj = B + size_t(j) * R;
-          for (int r = 0; r < R; r++) acc[r] += f * Bj[r];
+          for (int k = 0; k < rows; k++) {
+            const double f = F[size_t(i0 + k) * n + j];
+            if (f == 0) continue;
+            double* a = acc.data() + size_t(k) * R;
+            for (int r = 0; r < R; r++) a[r] += f * Bj[r];
+          }
         }
-        for (int r = 0; r < R; r++) Bn[size_t(i) * R + r] = double(E[size_t(i) * R + r]) + double(rho[i]) * acc[r];
+        for (int k = 0; k < rows; k++)
+          for (int r = 0; r < R; r++) Bn[size_t(i0 + k) * R + r] = double(E[size_t(i0 + k) * R + r]) + double(rho[i0 + k]) * acc[size_t(k) * R + r];
       }
     };
     std::vector<std::thread> th;
-    for (int t = 0; t < threads; t++) th.emplace_back(work, t);
+    for (int t = 0; t < threads; t++) th.emplace_back(work);
     for (auto& x : th) x.join();
     double num = 0, den = 0;
     for (size_t i = 0; i < size_t(n) * R; i++) { double d = Bn[i] - B[i]; num += d * d; den += Bn[i] * Bn[i]; }

@@ -18,7 +18,7 @@
 struct vt_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   std::string err;
   vt::Prepared S;
   std::vector<vt::InstPose> inst;
@@ -165,7 +165,9 @@ vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx**
   auto bail = [&](vt_status s) { vt_destroy(ctx); return s; };
   if (cudaSetDevice(ctx->device) != cudaSuccess) { cudaGetLastError(); delete ctx; return VT_ERR_NO_DEVICE; }
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(VT_ERR_CUDA);
-  if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) return bail(VT_ERR_CUDA);
+  if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess || cudaEventCreate(&ctx->ev2) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev3) != cudaSuccess)
+    return bail(VT_ERR_CUDA);
   const vt::Prepared& S = ctx->S;
   vt_status s;
   if ((s = upload(ctx, &ctx->d_nodes, S.nodes.data(), S.nodes.size() * 4)) != VT_OK) return bail(s);
@@ -204,6 +206,8 @@ vt_status vt_destroy(vt_ctx* ctx) {
   cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave); cudaFree(ctx->tc.mem);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+  if (ctx->ev3) cudaEventDestroy(ctx->ev3);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -602,7 +606,7 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
   const double inner_tol = fp8 ? 2e-3 : 1e-3;
   const uint32_t inner_max = 24;
   uint32_t sweeps = 0, refinements = 0, npart = 0;
-  double resid = INFINITY;
+  double resid = INFINITY, gemm_ms = 0;
   auto read_norms = [&](double* h) -> vt_status {
     vtk::launch_reduce_partials(np, npart, norms, ctx->stream);
     VT_CK(cudaGetLastError());
@@ -627,17 +631,24 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
     for (uint32_t k = 0; k < inner_max && sweeps < max_it; k++) {
       if (fp8) {
         vtk::tc_pack_b(vtk::TC_FP8, d, n, R, nullptr, nullptr, Bq, cs, cm, ctx->stream);
+        VT_CK(cudaEventRecord(ctx->ev2, ctx->stream));
         vtk::tc_gemm(vtk::TC_FP8, &mq, nullptr, &mbq, nullptr, n, sp_q, (kt_q + sp_q - 1) / sp_q, part, err, ctx->stream);
+        VT_CK(cudaEventRecord(ctx->ev3, ctx->stream));
         vtk::tc_combine_sweep(part, sp_q, n, R, rho, r, d, d2, rs, cs, np, &npart, ctx->stream);
       } else {
         vtk::tc_pack_b(vtk::TC_BF16, d, n, R, Bhi, nullptr, nullptr, nullptr, nullptr, ctx->stream);
+        VT_CK(cudaEventRecord(ctx->ev2, ctx->stream));
         vtk::tc_gemm(vtk::TC_BF16, &mhi, nullptr, &mbhi, nullptr, n, sp_bf, (kt_bf + sp_bf - 1) / sp_bf, part, err, ctx->stream);
+        VT_CK(cudaEventRecord(ctx->ev3, ctx->stream));
         vtk::tc_combine_sweep(part, sp_bf, n, R, rho, r, d, d2, nullptr, nullptr, np, &npart, ctx->stream);
       }
       ctx->tim.launches += 3;
       std::swap(d, d2);
       sweeps++;
       if ((s = read_norms(h)) != VT_OK) return s;
+      float gms = 0;
+      cudaEventElapsedTime(&gms, ctx->ev2, ctx->ev3);
+      gemm_ms += gms;
       if (!(h[1] > 0) || std::sqrt(h[0] / h[1]) <= inner_tol) break;
     }
     vtk::tc_axpy(B, d, nr, ctx->stream);
@@ -650,6 +661,7 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   q->iters = sweeps; q->refinements = refinements; q->residual = resid; q->ms = ms;
+  q->sweep_ms = sweeps ? gemm_ms / sweeps : 0.0;
   ctx->tim.solve_ms = ms;
   (void)conv_ms;
   if (herr) return fail(ctx, VT_ERR_TIMEOUT, "solve: a tensor-core pipeline wait ran out");
@@ -690,14 +702,16 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   const uint32_t max_it = q->max_iters ? q->max_iters : 1000;
   float* cur = B0;
   float* nxt = B1;
-  uint32_t it = 0, np = 0;
-  double resid = INFINITY;
+  uint32_t it = 0, np = 0, sweep_n = 0;
+  double resid = INFINITY, sweep_sum = 0;
   VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
   while (it < max_it) {
     const uint32_t k = std::min(check, max_it - it);
     for (uint32_t j = 0; j < k; j++) {
+      if (j == 0) VT_CK(cudaEventRecord(ctx->ev2, ctx->stream));
       if (R == 1) vtk::launch_jacobi_matvec(Fd, rho, E, cur, nxt, n, partials, &np, ctx->stream);
       else vtk::launch_jacobi_gemm_fp32(Fd, rho, E, cur, nxt, n, R, partials, &np, ctx->stream);
+      if (j == 0) VT_CK(cudaEventRecord(ctx->ev3, ctx->stream));
       std::swap(cur, nxt);
     }
     ctx->tim.launches += k + 1;
@@ -708,6 +722,10 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
     VT_CK(cudaMemcpyAsync(h, norms, 16, cudaMemcpyDeviceToHost, ctx->stream));
     VT_CK(cudaStreamSynchronize(ctx->stream));
     resid = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+    float gms = 0;
+    cudaEventElapsedTime(&gms, ctx->ev2, ctx->ev3);
+    sweep_sum += gms;
+    sweep_n++;
     if (resid <= q->tol) break;
   }
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -716,6 +734,7 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   q->iters = it; q->refinements = 0; q->residual = resid; q->ms = ms;
+  q->sweep_ms = sweep_n ? sweep_sum / sweep_n : 0.0;
   ctx->tim.solve_ms = ms;
   return resid <= q->tol ? VT_OK : VT_ERR_NOT_CONVERGED;
 }
