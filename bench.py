@@ -5,11 +5,15 @@ Metric (one JSON line): path Msamples/s of the plain FP32 path tracer on the see
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-ours: K frames rendered by libvtwin's persistent path-tracing kernel, each timed with CUDA events on the library's
+ours: K frames rendered by libvtwin's wavefront path tracer (ray generation, then per bounce closest-hit extension,
+shading and any-hit shadow kernels, then an in-order per-pixel sum), each timed with CUDA events on the library's
 stream, L2 flushed (a 256 MB write) between frames, clocks sampled during the timed region. `e2e` repeats the
 frames through the public API with the pose upload (host -> device) and the radiance copy back (device -> host)
 inside the timed region. reference: the reference's CPU path restated in C++ (oracle/, FP32, all host threads) on a
 bounded sample of the same frame; the reference itself is JavaScript + WebGPU and runs on neither machine.
+
+  python bench.py --case render:W:H:SPP            one small path-traced frame (two renders), for profilers
+  python bench.py --case radiosity:N:PREC:SWEEPS   one 64-RHS radiosity solve capped at SWEEPS sweeps (fp32|bf16|fp8)
 """
 import argparse
 import json
@@ -155,7 +159,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-radiosity", action="store_true")
+    ap.add_argument("--case", default=None, help="render:W:H:SPP or radiosity:N:PREC:SWEEPS (a small profiling case)")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case)
     if args.impl == "reference":
         return run_reference(args)
     rank, world, local = dist_env()
@@ -246,6 +253,38 @@ def main():
     r.destroy()
     if dist:
         dist.destroy_process_group()
+
+
+def run_case(spec):
+    """A small case of one hot kernel family for profilers; prints its device time as one JSON line."""
+    import torch
+    from vtwin import _abi as A
+    from vtwin import dome
+
+    kind, *a = spec.split(":")
+    if kind == "render":
+        from vtwin.renderer import TwinRenderer
+
+        w, h, spp = (int(x) for x in a)
+        r = TwinRenderer.create(dome.make_dome_scene(seed=1, width=w, height=h))
+        r.set_pose_array(A.identity_poses(1))
+        for _ in range(2):
+            r.renderCamera(0, spp=spp, lightSamples=NL, seed=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
+        ms = r.timings()["render_ms"]
+        print(json.dumps({"case": spec, "render_ms": ms, "msamples_per_s": w * h * spp / ms / 1e3}))
+        r.destroy()
+    elif kind == "radiosity":
+        from vtwin.renderer import form_factors, solve_radiosity
+
+        n, prec, sweeps = int(a[0]), {"fp32": A.VT_PREC_FP32, "bf16": A.VT_PREC_BF16, "fp8": A.VT_PREC_FP8}[a[1]], int(a[2])
+        P = dome.dome_patches(n, seed=2)
+        F = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        form_factors(P["centres"], P["normals"], P["areas"], out=F)
+        E = dome.radiosity_rhs(n, P["lamps"], 64, seed=5)
+        _, info = solve_radiosity(F, P["rho"], E, precision=prec, tol=1e-5, max_iters=sweeps)
+        print(json.dumps({"case": spec, **{k: v for k, v in info.items() if isinstance(v, (int, float))}}))
+    else:
+        raise SystemExit(f"unknown case {spec!r}")
 
 
 def radiosity_bench(torch, cpu_check=True):
