@@ -224,6 +224,56 @@ vt_status vt_sensor_expose(vt_ctx* ctx, const vt_sensor_uniform* su, const float
  * `optics_scale`, the pi T / (4 N^2) x RI factor, 1 for the configs' unit-radiance sensor) -> its raw DN image. */
 vt_status vt_sensor_camera(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, float optics_scale);
 
+/* -------------------------------------------------------------------------------------- batched rendering */
+
+/* Many cameras x many kinematic poses of one scene in one call: the twin's renderFrame (gpu/renderer.js:986) over
+ * a sweep of setPoses (gpu/renderer.js:620), with the sensor's expose stage (gpu/wgsl/sensor.wgsl.js:177) applied
+ * to every frame. Frame (camera c, pose q) is identical to vt_set_poses(poses0[q], poses1[q]), vt_render_camera
+ * (mode VT_SHADE_PATH, the request's spp / light_samples / seed / max_depth / shutter / scale) and, with a sensor,
+ * vt_sensor_camera with the uniform's frame word set to frame0 + q (DN stored as uint16).
+ * The common part of the scene is traced once per path for all poses; the (path, pose) pairs that may reach a
+ * body whose pose varies across the batch are re-traced under their own pose. The body that carries the emitter
+ * must keep one pose across the batch. Launches are captured in a CUDA graph and replayed while the request's
+ * shapes repeat (use_graph = 1). */
+#define VT_BATCH_MAX_POSES 64
+typedef struct {
+  const uint32_t* cameras;        /* n_cameras camera indices */
+  uint32_t n_cameras;
+  uint32_t n_poses;               /* pose sets, 1..VT_BATCH_MAX_POSES */
+  uint32_t n_bodies;              /* bodies per pose set (as vt_set_poses) */
+  const double* poses0;           /* n_poses x n_bodies x 16: column-major body transforms at exposure open */
+  const double* poses1;           /* the same at exposure close, or NULL (= poses0) */
+  uint32_t spp;                   /* sub-samples per pixel (1..4096) */
+  uint32_t light_samples;         /* 1..16 */
+  uint32_t seed;
+  uint32_t options;               /* VT_O_* */
+  uint32_t max_depth;             /* path vertices (1..64) */
+  float shutter[2];
+  float scale;                    /* output scale (1) */
+  const vt_sensor_uniform* sensor;/* n_cameras uniforms (sizes as the cameras), or NULL: no raw frames */
+  uint32_t frame0;                /* pose q exposes sensor frame frame0 + q */
+  float optics_scale;             /* as vt_sensor_camera (1 for a unit-radiance sensor) */
+  uint32_t use_graph;             /* 1: capture / replay the launch sequence as a CUDA graph */
+  uint32_t wave_paths;            /* shared paths per wave (0: the tuned or default size) */
+} vt_batch_req;
+typedef struct {
+  double ms;                      /* device time of the batch */
+  uint64_t shared_paths;          /* camera paths traced for all poses at once */
+  uint64_t pair_paths;            /* (path, pose) pairs re-traced under their own pose */
+  uint64_t samples;               /* camera samples delivered: n_cameras x n_poses x w x h x spp */
+  uint32_t waves, graph_replayed, reruns, vary_mask;
+} vt_batch_stats;
+/* raw_out: NULL, or host/device uint16 frames [camera][pose][h][w] (needs req->sensor); radiance_out: NULL, or
+ * host/device rgba32f frames [camera][pose][h][w]. stats may be NULL. */
+vt_status vt_render_batch(vt_ctx* ctx, const vt_batch_req* req, uint16_t* raw_out, float* radiance_out, vt_batch_stats* stats);
+
+/* Autotuner of the batched renderer: times each candidate (wave size x pixel tile) on the request at
+ * min(spp, 8) sub-samples and keeps the fastest in the context for later batches with wave_paths = 0.
+ * table (may be NULL): up to max_rows rows of (wave_paths, tile_w, tile_h, ms per million shared paths). */
+typedef struct { uint32_t wave_paths, tile_w, tile_h; float ms_per_mpath; } vt_tune_row;
+vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* table, uint32_t max_rows, uint32_t* n_rows,
+                            vt_tune_row* best);
+
 /* -------------------------------------------------------------------------------------- node radiosity */
 
 enum { VT_PREC_FP32 = 0, VT_PREC_BF16 = 1, VT_PREC_FP8 = 2 };

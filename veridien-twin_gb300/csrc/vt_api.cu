@@ -10,115 +10,11 @@
 #include <string>
 #include <vector>
 
-#include "vt_host.h"
-#include "vt_kernels.cuh"
-#include "vt_wave.cuh"
 #include "vt_tc.cuh"
 
-struct vt_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
-  std::string err;
-  vt::Prepared S;
-  std::vector<vt::InstPose> inst;
-  float eavg[3] = {0, 0, 0};
-  uint32_t slot = 1, frame = 0;
-  float su_host[vt::SU_WORDS];
-  // device scene
-  float4 *d_nodes = nullptr, *d_tris = nullptr, *d_verts = nullptr, *d_params = nullptr, *d_nstate = nullptr;
-  float* d_su = nullptr;
-  uint32_t* d_dbg = nullptr;
-  uint32_t* d_work = nullptr;   // queue counters of the wavefront path tracer
-  int wave_blocks = 0;
-  void* d_wave = nullptr;       // wavefront path state (grown on demand)
-  size_t wave_cap = 0;
-  struct Cam { float4* radiance = nullptr; float* raw = nullptr; bool rendered = false, exposed = false; };
-  std::vector<Cam> cams;
-  // scratch for ray queries and the solver (grown on demand)
-  void* d_scratch = nullptr;
-  size_t scratch_bytes = 0;
-  vt_timings tim{};
-  // mixed-precision radiosity: converted copies of F and the solver's work buffers
-  struct Tc {
-    void* mem = nullptr;
-    size_t bytes = 0;
-    const float* f_src = nullptr;   // F whose copies are held
-    uint32_t n = 0, R = 0, prec = 0;
-    bool have_hi_lo = false, have_q = false;
-  } tc;
-};
+#include "vt_ctx.cuh"
 
-namespace {
-
-const char* g_static_err = "no context";
-
-#define VT_CK(call)                                                                  \
-  do {                                                                               \
-    cudaError_t e_ = (call);                                                         \
-    if (e_ != cudaSuccess) return fail(ctx, VT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-vt_status fail(vt_ctx* ctx, vt_status s, const std::string& m) {
-  if (ctx) ctx->err = m;
-  return s;
-}
-
-bool is_device_ptr(const void* p) {
-  if (!p) return false;
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
-}
-
-template <typename T>
-vt_status upload(vt_ctx* ctx, T** dst, const void* src, size_t bytes) {
-  VT_CK(cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(bytes, 16)));
-  if (bytes) VT_CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  return VT_OK;
-}
-
-vt_status ensure_scratch(vt_ctx* ctx, size_t bytes) {
-  if (ctx->scratch_bytes >= bytes) return VT_OK;
-  if (ctx->d_scratch) { VT_CK(cudaStreamSynchronize(ctx->stream)); VT_CK(cudaFree(ctx->d_scratch)); ctx->d_scratch = nullptr; ctx->scratch_bytes = 0; }
-  cudaError_t e = cudaMalloc(&ctx->d_scratch, bytes);
-  if (e != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "scratch allocation of " + std::to_string(bytes) + " bytes failed"); }
-  ctx->scratch_bytes = bytes;
-  return VT_OK;
-}
-
-vtd::Scene dev_scene(vt_ctx* ctx) {
-  vtd::Scene S;
-  S.nodes = ctx->d_nodes; S.tris = ctx->d_tris; S.verts = ctx->d_verts; S.params = ctx->d_params;
-  S.su = ctx->d_su; S.nstate = ctx->d_nstate; S.dbg = ctx->d_dbg;
-  S.mesh_off = ctx->S.mesh_off; S.mat_off = ctx->S.mat_off; S.alb_off = ctx->S.alb_off; S.prof_off = ctx->S.prof_off;
-  S.prof_n = ctx->S.prof_n; S.emit_off = ctx->S.emit_off; S.emit_n = ctx->S.emit_n;
-  return S;
-}
-
-vt_status write_su(vt_ctx* ctx) {
-  vt::scene_uniform(ctx->S, ctx->inst, ctx->eavg, ctx->slot, ctx->frame, ctx->su_host);
-  VT_CK(cudaMemcpyAsync(ctx->d_su, ctx->su_host, sizeof(ctx->su_host), cudaMemcpyHostToDevice, ctx->stream));
-  return VT_OK;
-}
-
-uint32_t skip_mask(const vt_ctx* ctx, uint32_t cam) {
-  uint32_t m = 0;
-  for (size_t i = 0; i < ctx->S.bodies.size(); i++) if (ctx->S.bodies[i].owner == int(cam)) m |= 1u << i;
-  return m;
-}
-
-// copy `bytes` from a host or device source into device memory `dst`
-vt_status to_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
-  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
-  return VT_OK;
-}
-vt_status from_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
-  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
-  return VT_OK;
-}
-
-}  // namespace
+using namespace vtapi;
 
 extern "C" {
 
@@ -204,6 +100,9 @@ vt_status vt_destroy(vt_ctx* ctx) {
   for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); }
   cudaFree(ctx->d_nodes); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
   cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave); cudaFree(ctx->tc.mem);
+  cudaFree(ctx->batch.su); cudaFree(ctx->batch.cull); cudaFree(ctx->batch.ctr); cudaFree(ctx->batch.sensor); cudaFree(ctx->batch.mem);
+  cudaFree(ctx->batch.rad); cudaFree(ctx->batch.raw);
+  if (ctx->batch.exec) cudaGraphExecDestroy(ctx->batch.exec);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->ev2) cudaEventDestroy(ctx->ev2);
@@ -352,23 +251,11 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   if (q->root >= ctx->S.node_count) return fail(ctx, VT_ERR_ARG, "render: root out of range");
   if (q->mode != VT_SHADE_TWIN && q->mode != VT_SHADE_PATH) return fail(ctx, VT_ERR_ARG, "render: unknown mode");
   const vt_camera_desc& c = ctx->S.cams[q->camera];
-  vtk::CamParams cp{};
-  const double* T = c.T_D_C;
-  for (int k = 0; k < 3; k++) {
-    cp.rx[k] = float(T[4 * k]); cp.ry[k] = float(T[4 * k + 1]); cp.rz[k] = float(T[4 * k + 2]); cp.pos[k] = float(T[4 * k + 3]);
-  }
-  cp.lens = {float(c.fx), float(c.fy), float(c.cx), float(c.cy), float(c.alpha), float(c.k[0]), float(c.k[1]), float(c.k[2]), float(c.k[3])};
-  cp.w = c.width; cp.h = c.height;
-  cp.spp = std::min(std::max(q->spp, 1u), q->mode == VT_SHADE_TWIN ? 64u : 4096u);   // kernels.wgsl.js:169 clamps to 64
-  cp.seed = q->seed; cp.cam_index = q->camera; cp.options = q->options; cp.skip = skip_mask(ctx, q->camera);
-  cp.n_light = std::min(std::max(q->light_samples, 1u), 16u);   // shade.wgsl.js:270 clamps to 16
-  cp.mode = q->mode;
-  cp.max_depth = std::max(1u, std::min(q->max_depth, 64u));
-  cp.root = q->root;
-  cp.t0 = q->shutter[0]; cp.t1 = q->shutter[1]; cp.scale = q->scale;
+  const vtk::CamParams cp = make_cam(ctx, q->camera, q->spp, q->light_samples, q->seed, q->options, q->mode, q->max_depth, q->root, q->shutter,
+                                     q->scale);
   if (q->frame != ctx->frame) { ctx->frame = q->frame; vt_status s = write_su(ctx); if (s != VT_OK) return s; }
   // wave of up to 8 M paths (whole sub-sample indices): ~1.4 GB of path state at one light sample
-  const uint32_t n_pix = ((c.width + vtk::TILE_W - 1) / vtk::TILE_W) * ((c.height + vtk::TILE_H - 1) / vtk::TILE_H) * vtk::TILE_W * vtk::TILE_H;
+  const uint32_t n_pix = vtk::tiled_pixels(c.width, c.height, cp.tile_w, cp.tile_h);
   const uint32_t per_wave = std::max(1u, std::min(cp.spp, (8u << 20) / std::max(1u, n_pix)));
   const uint32_t paths = per_wave * n_pix;
   const size_t need = vtk::wave_bytes(paths, cp.n_light, n_pix);

@@ -1,0 +1,161 @@
+// The context behind the C ABI (include/vtwin.h) and the helpers its entry points share (vt_api.cu, vt_api_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "vt_host.h"
+#include "vt_kernels.cuh"
+#include "vt_wave.cuh"
+
+struct vt_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  std::string err;
+  vt::Prepared S;
+  std::vector<vt::InstPose> inst;
+  float eavg[3] = {0, 0, 0};
+  uint32_t slot = 1, frame = 0;
+  float su_host[vt::SU_WORDS];
+  // device scene
+  float4 *d_nodes = nullptr, *d_tris = nullptr, *d_verts = nullptr, *d_params = nullptr, *d_nstate = nullptr;
+  float* d_su = nullptr;
+  uint32_t* d_dbg = nullptr;
+  uint32_t* d_work = nullptr;   // queue counters of the wavefront path tracer
+  int wave_blocks = 0;
+  void* d_wave = nullptr;       // wavefront path state (grown on demand)
+  size_t wave_cap = 0;
+  struct Cam { float4* radiance = nullptr; float* raw = nullptr; bool rendered = false, exposed = false; };
+  std::vector<Cam> cams;
+  // scratch for ray queries and the solver (grown on demand)
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  vt_timings tim{};
+  // mixed-precision radiosity: converted copies of F and the solver's work buffers
+  struct Tc {
+    void* mem = nullptr;
+    size_t bytes = 0;
+    const float* f_src = nullptr;   // F whose copies are held
+    uint32_t n = 0, R = 0, prec = 0;
+    bool have_hi_lo = false, have_q = false;
+  } tc;
+  // batched multi-pose rendering: per-pose uniforms, the (pose, body) cull BVH, wave buffers, staging, graph
+  struct Batch {
+    float* su = nullptr;            // VT_BATCH_MAX_POSES scene uniforms
+    float4* cull = nullptr;         // nodes, then items
+    uint32_t* ctr = nullptr;        // queue counters [0..7], status [8], stats (u64) at [16]
+    uint32_t* sensor = nullptr;     // 64 words per camera
+    void* mem = nullptr;            // wave buffers
+    size_t mem_bytes = 0;
+    float4* rad = nullptr;          // radiance frames (staging)
+    size_t rad_bytes = 0;
+    uint16_t* raw = nullptr;        // raw frames (staging)
+    size_t raw_bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    std::string key;
+    uint64_t graph_launches = 0;   // kernels in the captured graph
+    uint32_t cap = 0;               // pair capacity of a wave
+    // tuned configuration (0: defaults)
+    uint32_t wave_paths = 0, tile_w = 0, tile_h = 0;
+  } batch;
+};
+
+namespace vtapi {
+
+inline const char* g_static_err = "no context";
+
+#define VT_CK(call)                                                                  \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) return fail(ctx, VT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+inline vt_status fail(vt_ctx* ctx, vt_status s, const std::string& m) {
+  if (ctx) ctx->err = m;
+  return s;
+}
+
+inline bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+inline vt_status upload(vt_ctx* ctx, T** dst, const void* src, size_t bytes) {
+  VT_CK(cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(bytes, 16)));
+  if (bytes) VT_CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return VT_OK;
+}
+
+inline vt_status ensure_scratch(vt_ctx* ctx, size_t bytes) {
+  if (ctx->scratch_bytes >= bytes) return VT_OK;
+  if (ctx->d_scratch) { VT_CK(cudaStreamSynchronize(ctx->stream)); VT_CK(cudaFree(ctx->d_scratch)); ctx->d_scratch = nullptr; ctx->scratch_bytes = 0; }
+  cudaError_t e = cudaMalloc(&ctx->d_scratch, bytes);
+  if (e != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "scratch allocation of " + std::to_string(bytes) + " bytes failed"); }
+  ctx->scratch_bytes = bytes;
+  return VT_OK;
+}
+
+inline vtd::Scene dev_scene(vt_ctx* ctx) {
+  vtd::Scene S;
+  S.nodes = ctx->d_nodes; S.tris = ctx->d_tris; S.verts = ctx->d_verts; S.params = ctx->d_params;
+  S.su = ctx->d_su; S.nstate = ctx->d_nstate; S.dbg = ctx->d_dbg;
+  S.mesh_off = ctx->S.mesh_off; S.mat_off = ctx->S.mat_off; S.alb_off = ctx->S.alb_off; S.prof_off = ctx->S.prof_off;
+  S.prof_n = ctx->S.prof_n; S.emit_off = ctx->S.emit_off; S.emit_n = ctx->S.emit_n;
+  return S;
+}
+
+inline vt_status write_su(vt_ctx* ctx) {
+  vt::scene_uniform(ctx->S, ctx->inst, ctx->eavg, ctx->slot, ctx->frame, ctx->su_host);
+  VT_CK(cudaMemcpyAsync(ctx->d_su, ctx->su_host, sizeof(ctx->su_host), cudaMemcpyHostToDevice, ctx->stream));
+  return VT_OK;
+}
+
+inline uint32_t skip_mask(const vt_ctx* ctx, uint32_t cam) {
+  uint32_t m = 0;
+  for (size_t i = 0; i < ctx->S.bodies.size(); i++) if (ctx->S.bodies[i].owner == int(cam)) m |= 1u << i;
+  return m;
+}
+
+// copy `bytes` from a host or device source into device memory `dst`
+inline vt_status to_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
+  return VT_OK;
+}
+inline vt_status from_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+  return VT_OK;
+}
+
+// launch parameters of one camera dispatch (gpu/renderer.js:888 _packCam)
+inline vtk::CamParams make_cam(const vt_ctx* ctx, uint32_t camera, uint32_t spp, uint32_t n_light, uint32_t seed, uint32_t options, uint32_t mode,
+                               uint32_t max_depth, uint32_t root, const float shutter[2], float scale) {
+  const vt_camera_desc& c = ctx->S.cams[camera];
+  vtk::CamParams cp{};
+  const double* T = c.T_D_C;
+  for (int k = 0; k < 3; k++) {
+    cp.rx[k] = float(T[4 * k]); cp.ry[k] = float(T[4 * k + 1]); cp.rz[k] = float(T[4 * k + 2]); cp.pos[k] = float(T[4 * k + 3]);
+  }
+  cp.lens = {float(c.fx), float(c.fy), float(c.cx), float(c.cy), float(c.alpha), float(c.k[0]), float(c.k[1]), float(c.k[2]), float(c.k[3])};
+  cp.w = c.width; cp.h = c.height;
+  cp.spp = std::min(std::max(spp, 1u), mode == VT_SHADE_TWIN ? 64u : 4096u);   // kernels.wgsl.js:169 clamps to 64
+  cp.seed = seed; cp.cam_index = camera; cp.options = options; cp.skip = skip_mask(ctx, camera);
+  cp.n_light = std::min(std::max(n_light, 1u), 16u);   // shade.wgsl.js:270 clamps to 16
+  cp.mode = mode;
+  cp.max_depth = std::max(1u, std::min(max_depth, 64u));
+  cp.root = root;
+  cp.t0 = shutter[0]; cp.t1 = shutter[1]; cp.scale = scale;
+  cp.tile_w = vtk::TILE_W; cp.tile_h = vtk::TILE_H;
+  return cp;
+}
+
+}  // namespace vtapi
+

@@ -15,10 +15,13 @@ struct CamParams {
   vtd::Kb4 lens;
   uint32_t w, h, spp, seed, cam_index, options, skip, n_light, mode, max_depth, root;
   float t0, t1, scale;
+  uint32_t tile_w, tile_h;             // pixel enumeration order: tiles of tile_w x tile_h (product 32)
 };
 
-// pixels are enumerated in 8 x 4 tiles, so consecutive paths are neighbouring pixels
+// default pixel tile: consecutive paths are neighbouring pixels of an 8 x 4 tile
 constexpr int TILE_W = 8, TILE_H = 4;
+// padded pixel count of a w x h image in tile_w x tile_h tiles
+inline uint32_t tiled_pixels(uint32_t w, uint32_t h, uint32_t tw, uint32_t th) { return ((w + tw - 1) / tw) * ((h + th - 1) / th) * tw * th; }
 void launch_trace(const vtd::Scene& S, const float4* o4, const float4* d4, uint32_t n, uint32_t mask, uint32_t any_hit, uint32_t root,
                   float4* out4, float* out_v, cudaStream_t st);
 void launch_visible(const vtd::Scene& S, float3 c, const float3* pts, uint32_t n, float tol, float time, uint32_t skip, uint8_t* out,
@@ -27,6 +30,8 @@ void launch_visible(const vtd::Scene& S, float3 c, const float3* pts, uint32_t n
 // sensor (gpu/wgsl/sensor.wgsl.js:177 sensorExpose)
 struct SensorParams { uint32_t w[64]; };
 void launch_sensor_expose(const SensorParams& su, const float4* E, float scale, float* raw, cudaStream_t st);
+// the same with raw DN stored as uint16 (ADC depth <= 16 bits)
+void launch_sensor_expose_u16(const SensorParams& su, const float4* E, float scale, uint16_t* raw, cudaStream_t st);
 
 // radiosity
 // B_out = E + rho (F B_in), n x 1, and per-block partial sums of |B_out - B_in|^2 and |B_out|^2 (doubles)

@@ -34,63 +34,168 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* count, bool want) {
   return base + __popc(mask & ((1u << lane) - 1u));
 }
 
-// pixel id (tiled 8 x 4 order, so consecutive paths are neighbouring pixels) -> x, y
+// pixel id (tiled order, so consecutive paths are neighbouring pixels) -> x, y
 __device__ __forceinline__ bool pixel_xy(const CamParams& cp, uint32_t id, uint32_t& x, uint32_t& y) {
-  const uint32_t tiles_x = (cp.w + TILE_W - 1) / TILE_W;
-  const uint32_t tile = id / (TILE_W * TILE_H), within = id % (TILE_W * TILE_H);
-  x = (tile % tiles_x) * TILE_W + within % TILE_W;
-  y = (tile / tiles_x) * TILE_H + within / TILE_W;
+  const uint32_t tw = cp.tile_w, th = cp.tile_h;
+  const uint32_t tiles_x = (cp.w + tw - 1) / tw;
+  const uint32_t tile = id / (tw * th), within = id % (tw * th);
+  x = (tile % tiles_x) * tw + within % tw;
+  y = (tile / tiles_x) * th + within / tw;
   return x < cp.w && y < cp.h;
+}
+
+// the camera sub-sample (pixel id, index i): KB4 ray, exposure time and pixel hash (gpu/wgsl/kernels.wgsl.js:35
+// pixSeeds, :177-185 camMain sub-samples)
+__device__ __forceinline__ bool camera_path(const CamParams& cp, uint32_t id, uint32_t i, float4& o4, float4& d4, uint32_t& hs) {
+  uint32_t x, y;
+  const bool valid = pixel_xy(cp, id, x, y);
+  hs = hash3(x, y, cp.seed * 64u + cp.cam_index);
+  float3 d = f3(0, 0, 1);
+  float tt = 0.0f;
+  if (valid) {
+    const float u = __fsub_rn(__fadd_rn(float(x), kr(i, R2A, u01(pcg(hs)))), 0.5f);
+    const float v = __fsub_rn(__fadd_rn(float(y), kr(i, R2B, u01(pcg(hs + 1u)))), 0.5f);
+    tt = mixr(cp.t0, cp.t1, kr(i, GOLD, u01(pcg(hs + 2u))));
+    const float3 rx = f3(cp.rx[0], cp.rx[1], cp.rx[2]), ry = f3(cp.ry[0], cp.ry[1], cp.ry[2]), rz = f3(cp.rz[0], cp.rz[1], cp.rz[2]);
+    const float3 dc = kb4_unproject(cp.lens, u, v);
+    d = normalize(rx * dc.x + ry * dc.y + rz * dc.z);
+  }
+  o4 = make_float4(cp.pos[0], cp.pos[1], cp.pos[2], tt);
+  d4 = make_float4(d.x, d.y, d.z, 0.0f);
+  return valid;
+}
+
+__device__ __forceinline__ void init_path(const WaveBufs& wb, uint32_t p, float4 o4, float4 d4, uint32_t id, uint32_t i, uint32_t hs, bool valid) {
+  wb.o[p] = o4;
+  wb.d[p] = d4;
+  wb.thr[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+  wb.L[p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xfffeu));
+  wb.meta[p] = make_uint4(id, i, hs, valid ? 1u : 0u);      // bounce 1 (0: no pixel)
+}
+
+// the scene a path sees: its pose's uniform for a pair path, the shared one otherwise
+template <int VAR>
+__device__ __forceinline__ Scene path_scene(const Scene& S, const WaveBufs& wb, uint32_t p) {
+  if (VAR != WAVE_PAIRS) return S;
+  Scene s = S;
+  s.su = wb.bc.su_base + size_t(__ldg(wb.bc.pair_pose + p)) * wb.bc.su_stride;
+  return s;
+}
+
+// The poses of a batch whose copy of a varying body the segment o + t d, t in [0, t1], may reach: the world-box and
+// capsule culls that trace_scene applies to a body before traversing it (gpu/wgsl/trace.wgsl.js:302), with a relative
+// margin, over the batch's BVH of (pose, body) items. A pose not returned cannot change the segment's result, so
+// the returned set is a superset of the poses whose traced result differs from the shared one; on any overflow
+// every pose is returned.
+__device__ __forceinline__ uint64_t cull_bits(const BatchCull& C, float3 o, float3 d, float t1, uint32_t skip, uint64_t have) {
+  if (!C.n_nodes) return 0ull;
+  const float te = t1 < BIG ? t1 + fabsf(t1) * 1e-5f + 1e-6f : BIG;
+  const float tc = fminf(te, 1e3f);
+  const float3 inv = safe_inv(d);
+  uint64_t bits = 0ull;
+  constexpr int DEPTH = 24;
+  uint32_t stack[DEPTH];
+  int sp = 0;
+  uint32_t n = 0;
+  for (uint32_t guard = 0;; guard++) {
+    if (guard > 2u * C.n_nodes + 2u) return ~0ull;
+    const float4 a = __ldg(C.nodes + 2u * n), b = __ldg(C.nodes + 2u * n + 1u);
+    const uint32_t ref = __float_as_uint(a.w), cnt = __float_as_uint(b.w);
+    if (slab(xyz(a), xyz(b), o, inv, 0.0f, te) < BIG) {
+      if (cnt == 0u) {
+        if (sp >= DEPTH) return ~0ull;
+        stack[sp++] = ref + 1u;
+        n = ref;
+        continue;
+      }
+      for (uint32_t k = 0; k < cnt; k++) {
+        const float4* it = C.items + 4u * (ref + k);
+        const float4 lo = __ldg(it), hi = __ldg(it + 1);
+        const uint32_t q = __float_as_uint(lo.w), body = __float_as_uint(hi.w);
+        if ((((have | bits) >> q) & 1ull) || ((skip >> body) & 1u)) continue;
+        if (slab(xyz(lo), xyz(hi), o, inv, 0.0f, te) >= BIG) continue;
+        const float4 ca = __ldg(it + 2), cb = __ldg(it + 3);
+        if (seg_near_capsule(o, d, 0.0f, tc, xyz(ca), xyz(cb), ca.w * 1.001f + 1e-5f)) bits |= 1ull << q;
+      }
+    }
+    if (!sp) break;
+    n = stack[--sp];
+  }
+  return bits;
 }
 
 // paths of the wave: sub-sample index i in [i0, i0 + n_i), pixel id in [0, n_pix); path p = (i - i0) * n_pix + id
 __global__ void __launch_bounds__(WAVE_THREADS) wave_gen(const CamParams cp, WaveBufs wb, uint32_t i0, uint32_t n_i, uint32_t n_pix) {
   const uint32_t total = n_i * n_pix;
-  const float3 rx = f3(cp.rx[0], cp.rx[1], cp.rx[2]), ry = f3(cp.ry[0], cp.ry[1], cp.ry[2]), rz = f3(cp.rz[0], cp.rz[1], cp.rz[2]);
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
     const uint32_t id = p % n_pix, i = i0 + p / n_pix;
-    uint32_t x, y;
-    const bool valid = pixel_xy(cp, id, x, y);
-    const uint32_t hs = hash3(x, y, cp.seed * 64u + cp.cam_index);   // kernels.wgsl.js:35 pixSeeds
-    float3 d = f3(0, 0, 1);
-    float tt = 0.0f;
-    if (valid) {
-      const float u = __fsub_rn(__fadd_rn(float(x), kr(i, R2A, u01(pcg(hs)))), 0.5f);
-      const float v = __fsub_rn(__fadd_rn(float(y), kr(i, R2B, u01(pcg(hs + 1u)))), 0.5f);
-      tt = mixr(cp.t0, cp.t1, kr(i, GOLD, u01(pcg(hs + 2u))));
-      const float3 dc = kb4_unproject(cp.lens, u, v);
-      d = normalize(rx * dc.x + ry * dc.y + rz * dc.z);
-    }
-    wb.o[p] = make_float4(cp.pos[0], cp.pos[1], cp.pos[2], tt);
-    wb.d[p] = make_float4(d.x, d.y, d.z, 0.0f);
-    wb.thr[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    wb.L[p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xfffeu));
-    wb.meta[p] = make_uint4(id, i, hs, valid ? 1u : 0u);      // bounce 1 (0: no pixel)
+    float4 o4, d4;
+    uint32_t hs;
+    const bool valid = camera_path(cp, id, i, o4, d4, hs);
+    init_path(wb, p, o4, d4, id, i, hs, valid);
     const uint32_t slot = warp_append(wb.count_in, valid);
     if (valid) wb.q_in[slot] = p;
   }
 }
 
+// a batch wave: paths p = i * n_pw + lp (all sub-samples i < spp of pixels px0 + lp)
+__global__ void __launch_bounds__(WAVE_THREADS) wave_gen_batch_kernel(const CamParams cp, WaveBufs wb) {
+  const uint32_t n_pw = wb.bc.n_pw, total = cp.spp * n_pw;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const uint32_t id = wb.bc.px0 + p % n_pw, i = p / n_pw;
+    float4 o4, d4;
+    uint32_t hs;
+    const bool valid = camera_path(cp, id, i, o4, d4, hs);
+    init_path(wb, p, o4, d4, id, i, hs, valid);
+    wb.bc.dirty[p] = 0ull;
+    const uint32_t slot = warp_append(wb.count_in, valid);
+    if (valid) wb.q_in[slot] = p;
+  }
+}
+
+// pair paths: pair j repeats shared path pair_src[j] (same pixel and sub-sample) under its own pose
+__global__ void __launch_bounds__(WAVE_THREADS) wave_gen_pairs_kernel(const CamParams cp, WaveBufs wb) {
+  const uint32_t n = *wb.count_in, n_pw = wb.bc.n_pw;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t p = wb.bc.pair_src[j];
+    const uint32_t id = wb.bc.px0 + p % n_pw, i = p / n_pw;
+    float4 o4, d4;
+    uint32_t hs;
+    const bool valid = camera_path(cp, id, i, o4, d4, hs);
+    init_path(wb, j, o4, d4, id, i, hs, valid);
+    wb.q_in[j] = j;
+  }
+}
+
+template <int VAR>
 __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t p = wb.q_in[k];
     const float4 o = wb.o[p], d = wb.d[p];
     const uint32_t b = wb.meta[p].w;
-    const Hit h = trace_scene<false>(S, cp.root, xyz(o), xyz(d), 0.0f, BIG, o.w, 3u, b == 1 ? cp.skip : 0u);
+    const uint32_t skip = b == 1 ? cp.skip : 0u;
+    const Hit h = trace_scene<false>(path_scene<VAR>(S, wb, p), cp.root, xyz(o), xyz(d), 0.0f, BIG, o.w, 3u,
+                                     VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip);
     wb.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
     wb.hinst[p] = h.inst;
+    if (VAR == WAVE_SHARED) {
+      const uint64_t have = wb.bc.dirty[p];
+      const uint64_t bits = cull_bits(wb.bc, xyz(o), xyz(d), h.t, skip, have);
+      if (bits & ~have) wb.bc.dirty[p] = have | bits;
+    }
   }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S, const CamParams cp, WaveBufs wb) {
+template <int MODE, int VAR>
+__global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S0, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
   const uint32_t nl = cp.n_light;
   const bool no_mis = (cp.options & VT_O_NO_MIS) != 0u;
-  const float emit_area = __ldg(S.su + 3);
+  const float emit_area = __ldg(S0.su + 3);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t p = wb.q_in[k];
+    const Scene S = path_scene<VAR>(S0, wb, p);
     const uint4 meta = wb.meta[p];
     const uint32_t i = meta.y, hs = meta.z, b = meta.w;
     const float4 o4 = wb.o[p], d4 = wb.d[p], hv = wb.hit[p];
@@ -196,24 +301,32 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S, const 
   }
 }
 
-__global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S, const CamParams cp, WaveBufs wb) {
+template <int VAR>
+__global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S0, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_sh;
   const uint32_t nl = cp.n_light;
-  const uint32_t skip = ldu(S.su + 7);
+  const uint32_t skip = ldu(S0.su + 7);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t p = wb.q_sh[k];
+    const Scene S = path_scene<VAR>(S0, wb, p);
     const float4 nee = wb.nee[p];
     const float4* rec = wb.sh + size_t(p) * nl * 3;
     float3 Ld = f3(0, 0, 0);
+    uint64_t have = 0ull, bits = 0ull;
+    if (VAR == WAVE_SHARED) have = wb.bc.dirty[p];
     for (uint32_t j = 0; j < nl; j++) {
       const float4 a = rec[3 * j], w = rec[3 * j + 1];
       if (w.w == 0.0f) continue;
-      const Hit sh = trace_scene<true>(S, cp.root, xyz(a), xyz(w), 0.0f, a.w, nee.w, 3u, skip);
-      if (sh.tri == MISS) Ld = Ld + xyz(rec[3 * j + 2]);
+      const Hit sh = trace_scene<true>(S, cp.root, xyz(a), xyz(w), 0.0f, a.w, nee.w, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip);
+      if (sh.tri == MISS) {
+        Ld = Ld + xyz(rec[3 * j + 2]);
+        if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, xyz(a), xyz(w), a.w, skip, have | bits);
+      }
     }
     const float4 L = wb.L[p];
     const float3 v = xyz(L) + xyz(nee) * (Ld / float(nl));
     wb.L[p] = make_float4(v.x, v.y, v.z, L.w);
+    if (VAR == WAVE_SHARED && bits) wb.bc.dirty[p] = have | bits;
   }
 }
 
@@ -270,13 +383,50 @@ WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix
   return w;
 }
 
+template <int VAR>
+void bounce_kernels(const Scene& S, const CamParams& cp, const WaveBufs& w, int blocks, cudaStream_t st) {
+  wave_extend<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  if (cp.mode == VT_SHADE_TWIN) wave_shade<VT_SHADE_TWIN, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  else wave_shade<VT_SHADE_PATH, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  wave_shadow<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+}
+
+void wave_bounces(const Scene& S, const CamParams& cp, WaveBufs wb, int var, int blocks, cudaStream_t st, uint64_t* launches) {
+  const uint32_t depth = cp.mode == VT_SHADE_TWIN ? 2u : cp.max_depth;
+  WaveBufs w = wb;
+  for (uint32_t b = 1; b <= depth; b++) {
+    // queue of this bounce in (qa | qb), next bounce's in the other; counters 0/1 alternate, 2 is the shadow count
+    w.q_in = (b & 1) ? wb.qa : wb.qb;
+    w.q_out = (b & 1) ? wb.qb : wb.qa;
+    w.count_in = wb.counts + ((b & 1) ? 0 : 1);
+    w.count_out = wb.counts + ((b & 1) ? 1 : 0);
+    w.count_sh = wb.counts + 2;
+    cudaMemsetAsync(w.count_out, 0, 4, st);
+    cudaMemsetAsync(w.count_sh, 0, 4, st);
+    if (var == WAVE_SHARED) bounce_kernels<WAVE_SHARED>(S, cp, w, blocks, st);
+    else if (var == WAVE_PAIRS) bounce_kernels<WAVE_PAIRS>(S, cp, w, blocks, st);
+    else bounce_kernels<WAVE_PLAIN>(S, cp, w, blocks, st);
+    if (launches) *launches += 3;
+  }
+}
+
+void wave_gen_batch(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t st) {
+  wb.q_in = wb.qa;
+  wb.count_in = wb.counts;
+  wave_gen_batch_kernel<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb);
+}
+
+void wave_gen_pairs(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t st) {
+  wb.q_in = wb.qa;
+  wb.count_in = wb.counts;
+  wave_gen_pairs_kernel<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb);
+}
+
 // one camera: waves of whole sub-sample indices, each bounce extend -> shade -> shadow over compacted queues
 void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave_paths, float4* out, int blocks, cudaStream_t st,
                  uint64_t* launches) {
-  const uint32_t tiles = ((cp.w + TILE_W - 1) / TILE_W) * ((cp.h + TILE_H - 1) / TILE_H);
-  const uint32_t n_pix = tiles * TILE_W * TILE_H;
+  const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t per_wave = std::max(1u, std::min(cp.spp, wave_paths / n_pix));
-  const uint32_t depth = cp.mode == VT_SHADE_TWIN ? 2u : cp.max_depth;
   uint64_t nlaunch = 0;
   for (uint32_t i0 = 0; i0 < cp.spp; i0 += per_wave) {
     const uint32_t n_i = std::min(per_wave, cp.spp - i0);
@@ -285,21 +435,7 @@ void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave
     w.q_in = wb.qa; w.count_in = wb.counts + 0;
     wave_gen<<<blocks, WAVE_THREADS, 0, st>>>(cp, w, i0, n_i, n_pix);
     nlaunch++;
-    for (uint32_t b = 1; b <= depth; b++) {
-      // queue of this bounce in (qa | qb), next bounce's in the other; counters 0/1 alternate, 2 + b is the shadow count
-      w.q_in = (b & 1) ? wb.qa : wb.qb;
-      w.q_out = (b & 1) ? wb.qb : wb.qa;
-      w.count_in = wb.counts + ((b & 1) ? 0 : 1);
-      w.count_out = wb.counts + ((b & 1) ? 1 : 0);
-      w.count_sh = wb.counts + 2;
-      cudaMemsetAsync(w.count_out, 0, 4, st);
-      cudaMemsetAsync(w.count_sh, 0, 4, st);
-      wave_extend<<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
-      if (cp.mode == VT_SHADE_TWIN) wave_shade<VT_SHADE_TWIN><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
-      else wave_shade<VT_SHADE_PATH><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
-      wave_shadow<<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
-      nlaunch += 3;
-    }
+    wave_bounces(S, cp, wb, WAVE_PLAIN, blocks, st, &nlaunch);
     const int last = i0 + n_i >= cp.spp;
     wave_finalize<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb, i0, n_i, n_pix, wb.acc, out, last);
     nlaunch++;
@@ -309,9 +445,9 @@ void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave
 
 int wave_blocks_per_sm() {
   int a = 0, b = 0, c = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, wave_extend, WAVE_THREADS, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_shade<VT_SHADE_PATH>, WAVE_THREADS, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, wave_shadow, WAVE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, wave_extend<WAVE_PLAIN>, WAVE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_shade<VT_SHADE_PATH, WAVE_PLAIN>, WAVE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, wave_shadow<WAVE_PLAIN>, WAVE_THREADS, 0);
   return std::max(1, std::max(a, std::max(b, c)));
 }
 

@@ -1,9 +1,32 @@
-// Wavefront path-state buffers and launchers (vt_wave.cu).
+// Wavefront path-state buffers and launchers (vt_wave.cu), and the pose-batch extensions (vt_batch.cu).
 #pragma once
 
 #include "vt_kernels.cuh"
 
 namespace vtk {
+
+// Kernel variants of the wavefront:
+//   WAVE_PLAIN   one pose: every path traced against the whole scene
+//   WAVE_SHARED  a pose batch's shared paths: bodies whose pose varies across the batch are skipped, and every
+//                segment is tested against all poses' copies of them (BatchCull) to mark the poses whose result
+//                may differ from the shared one
+//   WAVE_PAIRS   the (path, pose) pairs so marked, each traced whole against its own pose's scene uniform
+enum { WAVE_PLAIN = 0, WAVE_SHARED = 1, WAVE_PAIRS = 2 };
+
+// pose-batch data of the wavefront kernels
+struct BatchCull {
+  const float4* nodes;      // BVH over (pose, body) items: 2 float4 per node (lo, first|left bits) (hi, count bits; 0 = interior)
+  const float4* items;      // 4 float4 per item: (box lo, pose bits) (box hi, body bits) (capsule a, r) (capsule b, -)
+  uint32_t n_nodes;
+  uint32_t vary;            // bodies whose pose differs across the batch
+  const float* su_base;     // per-pose scene uniforms (WAVE_PAIRS)
+  uint32_t su_stride;       // words per uniform
+  uint64_t* dirty;          // per shared path: poses whose result may differ (WAVE_SHARED)
+  const uint32_t* pair_pose;// per pair path: its pose (WAVE_PAIRS)
+  const uint32_t* pair_src; // per pair path: the shared path it repeats (WAVE_PAIRS)
+  uint32_t n_pw;            // pixels of the batch wave (pixel id = px0 + path % n_pw, sub-sample = path / n_pw)
+  uint32_t px0;
+};
 
 // structure-of-arrays path state of one wave, carved from one device allocation
 struct WaveBufs {
@@ -27,6 +50,7 @@ struct WaveBufs {
   uint32_t* count_in;
   uint32_t* count_out;
   uint32_t* count_sh;
+  BatchCull bc;
 };
 
 size_t wave_bytes(uint32_t paths, uint32_t n_light, uint32_t n_pix);
@@ -34,5 +58,12 @@ WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix
 void wave_render(const vtd::Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave_paths, float4* out, int blocks, cudaStream_t st,
                  uint64_t* launches);
 int wave_blocks_per_sm();
+
+// one wave's bounces (extend, shade, shadow per bounce) over the paths queued in wb.qa / counts[0]
+void wave_bounces(const vtd::Scene& S, const CamParams& cp, WaveBufs wb, int var, int blocks, cudaStream_t st, uint64_t* launches);
+// camera rays of a batch wave: paths p = i * n_pw + lp, i < spp, pixel id px0 + lp; clears the dirty masks
+void wave_gen_batch(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t st);
+// camera rays of the pair paths (pair j repeats shared path pair_src[j]); count in counts[0]
+void wave_gen_pairs(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t st);
 
 }  // namespace vtk

@@ -91,6 +91,27 @@ class vt_sensor_uniform(C.Structure):
     _fields_ = [("words", C.c_uint32 * 64)]
 
 
+VT_BATCH_MAX_POSES = 64
+
+
+class vt_batch_req(C.Structure):
+    _fields_ = [("cameras", C.POINTER(C.c_uint32)), ("n_cameras", C.c_uint32), ("n_poses", C.c_uint32),
+                ("n_bodies", C.c_uint32), ("poses0", C.POINTER(C.c_double)), ("poses1", C.POINTER(C.c_double)),
+                ("spp", C.c_uint32), ("light_samples", C.c_uint32), ("seed", C.c_uint32), ("options", C.c_uint32),
+                ("max_depth", C.c_uint32), ("shutter", C.c_float * 2), ("scale", C.c_float),
+                ("sensor", C.POINTER(vt_sensor_uniform)), ("frame0", C.c_uint32), ("optics_scale", C.c_float),
+                ("use_graph", C.c_uint32), ("wave_paths", C.c_uint32)]
+
+
+class vt_batch_stats(C.Structure):
+    _fields_ = [("ms", C.c_double), ("shared_paths", C.c_uint64), ("pair_paths", C.c_uint64), ("samples", C.c_uint64),
+                ("waves", C.c_uint32), ("graph_replayed", C.c_uint32), ("reruns", C.c_uint32), ("vary_mask", C.c_uint32)]
+
+
+class vt_tune_row(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("ms_per_mpath", C.c_float)]
+
+
 class vt_solve_req(C.Structure):
     _fields_ = [("n", C.c_uint32), ("n_rhs", C.c_uint32), ("F", f32p), ("rho", f32p), ("E", f32p), ("B", f32p),
                 ("precision", C.c_uint32), ("max_iters", C.c_uint32), ("warm_start", C.c_uint32),

@@ -30,6 +30,9 @@ SIGNATURES = {
     "vt_readback": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t]),
     "vt_sensor_expose": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_sensor_uniform), C.c_void_p, C.c_void_p]),
     "vt_sensor_camera": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_float]),
+    "vt_render_batch": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_batch_req), C.c_void_p, C.c_void_p, C.POINTER(A.vt_batch_stats)]),
+    "vt_batch_autotune": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_batch_req), C.POINTER(A.vt_tune_row), C.c_uint32,
+                                      C.POINTER(C.c_uint32), C.POINTER(A.vt_tune_row)]),
     "vt_radiosity_solve": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_solve_req)]),
     "vt_form_factors": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vt_radiosity_solve_static": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,

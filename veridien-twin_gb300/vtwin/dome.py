@@ -266,11 +266,12 @@ def emitter_material():
     return m
 
 
-def make_dome_scene(seed: int = 1, width=640, height=480, level=5, with_instruments: int = 0):
+def make_dome_scene(seed: int = 1, width=640, height=480, level=5, with_instruments: int = 0, tool_radius: float = 0.006):
     """Config-0 dome: ~10.2k dome + 1984 floor + 12 table + 96 lamp triangles, 8 Lambertian materials
     (rho ~ U[0.2, 0.8] per channel from mulberry32(seed)), one KB4 camera, lamps L0 = 50 W sr^-1 m^-2, p = 1.
 
-    with_instruments > 0 adds that many 600-triangle capsule bodies (kind 'instrument'), posed by set_poses."""
+    with_instruments > 0 adds that many 600-triangle capsule bodies (kind 'instrument', radius `tool_radius`, length
+    0.25 m), posed by set_poses."""
     rng = Rng(seed)
     mats = [lambertian(f"mat{i}", [rng.uniform(0.2, 0.8) for _ in range(3)]) for i in range(8)]
     meshes, static = [], []
@@ -303,7 +304,7 @@ def make_dome_scene(seed: int = 1, width=640, height=480, level=5, with_instrume
         steel = len(mats)
         mats.append({**lambertian("steel", [0.0, 0.0, 0.0]), "metallic": 1, "f0": [0.56, 0.57, 0.58],
                      "roughness": 0.35, "ior": 1.5})
-        cap = capsule_geometry()
+        cap = capsule_geometry(radius=tool_radius)
         for k in range(with_instruments):
             meshes.append({"name": f"tool{k}", "mat": steel, "flags": MESH_FLAG["INSTRUMENT"],
                            "build_dir": [0.0, 0.0, 1.0], "layer": [0.0, 0.0]})
@@ -348,14 +349,15 @@ def _concat_static(static):
 
 
 def batched_cameras(seed=3, n=3, width=1920, height=1200):
-    """Three KB4 tracking cameras on the dome wall looking at the table: fx ~ U[550, 650],
-    k_i ~ N(0, 0.02) (Box-Muller of mulberry32, control/rng.js:19-27)."""
+    """Three KB4 tracking cameras on the dome wall looking at the table: fx ~ U[550, 650] at 1920 px wide (scaled by
+    width / 1920 for other sizes, so the field of view is kept), k_i ~ N(0, 0.02) (Box-Muller of mulberry32,
+    control/rng.js:19-27)."""
     rng = Rng(seed)
     cams = []
     for c in range(n):
         a = 2 * math.pi * c / n - math.pi / 2
         pos = (3.2 * math.cos(a), 3.2 * math.sin(a), 1.6)
-        fx = rng.uniform(550, 650)
+        fx = rng.uniform(550, 650) * width / 1920.0
         fy = fx * (1 + 0.004 * (rng.u() - 0.5))
         k = [rng.normal(0, 0.02) for _ in range(4)]
         cams.append(kb4_camera(f"CAM{c + 1}", (width, height), fx, fy, (width - 1) / 2.0, (height - 1) / 2.0, k,
@@ -387,6 +389,15 @@ def instrument_poses(n_poses=64, n_tools=6, seed=11, centre=(0.0, 0.0, 1.15)):
             T[:3, :3], T[:3, 3] = R, tr
             out[p, t] = T.T.ravel()  # column-major
     return out
+
+
+def batch_pose_array(tool_poses, n_fixed: int = 1) -> np.ndarray:
+    """(n_poses, n_fixed + n_tools, 16) body transforms for a pose batch: the scene's leading fixed bodies (the
+    lamps) at identity, then the tools' poses (instrument_poses)."""
+    tp = np.asarray(tool_poses, np.float64)
+    n = tp.shape[0]
+    eye = np.tile(np.eye(4).T.ravel(), (n, n_fixed, 1))
+    return np.ascontiguousarray(np.concatenate([eye, tp], axis=1))
 
 
 # ------------------------------------------------------------------------------------------------ radiosity

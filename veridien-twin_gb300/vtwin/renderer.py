@@ -191,6 +191,85 @@ class TwinRenderer:
             p, w, h, frame=self.frame if frame is None else frame, seed=seed, exposure=exposure_s, gain=gain, cam_index=c)]
         check(self.lib.vt_sensor_camera(self._ctx, c, C.byref(su), float(optics_scale)), self._ctx)
 
+    # ------------------------------------------------------------------------------------------- batches
+    def _batch_req(self, cameras, poses0, poses1, spp, lightSamples, seed, max_depth, shutter, scale, options, sensor, frame0,
+                   optics_scale, use_graph, wave_paths, exposure_s=1.0, gain=1.0):
+        cams = [self._cam(c) for c in cameras]
+        P0 = np.ascontiguousarray(poses0, np.float64)
+        if P0.ndim == 2:
+            P0 = P0[None]
+        n_poses, n_bodies = P0.shape[0], P0.shape[1]
+        P0 = P0.reshape(n_poses, n_bodies, 16)
+        P1 = None if poses1 is None else np.ascontiguousarray(poses1, np.float64).reshape(n_poses, n_bodies, 16)
+        cam_arr = np.ascontiguousarray(cams, np.uint32)
+        q = A.vt_batch_req(cameras=cam_arr.ctypes.data_as(C.POINTER(C.c_uint32)), n_cameras=len(cams), n_poses=n_poses,
+                           n_bodies=n_bodies, poses0=P0.ctypes.data_as(C.POINTER(C.c_double)),
+                           poses1=P1.ctypes.data_as(C.POINTER(C.c_double)) if P1 is not None else None,
+                           spp=int(spp), light_samples=int(lightSamples), seed=int(seed), options=int(options),
+                           max_depth=int(max_depth), scale=float(scale), frame0=int(frame0), optics_scale=float(optics_scale),
+                           use_graph=int(bool(use_graph)), wave_paths=int(wave_paths))
+        q.shutter[:] = [float(shutter[0]), float(shutter[1])]
+        keep = [cam_arr, P0, P1]
+        if sensor is not None:
+            p = {**self.sensor_p, **(sensor if isinstance(sensor, dict) else {})}
+            su = (A.vt_sensor_uniform * len(cams))()
+            for k, c in enumerate(cams):
+                w, h = self.scene["cameras"][c]["size"]
+                su[k].words[:] = [int(x) for x in sensor_mod.pack_sensor_uniform(p, w, h, frame=frame0, seed=seed, exposure=exposure_s,
+                                                                                  gain=gain, cam_index=c)]
+            q.sensor = C.cast(su, C.POINTER(A.vt_sensor_uniform))
+            keep.append(su)
+        return q, cams, n_poses, keep
+
+    def render_batch(self, cameras, poses0, poses1=None, spp=64, lightSamples=1, seed=0, max_depth=6, shutter=(0.0, 1.0), scale=1.0,
+                     options=0, sensor=None, frame0=0, optics_scale=1.0, use_graph=True, wave_paths=0, radiance=False,
+                     raw_out=None, radiance_out=None, exposure_s=1.0, gain=1.0):
+        """Many cameras x many kinematic poses in one call (renderFrame over a setPoses sweep, gpu/renderer.js:620,986).
+        poses0 / poses1: (n_poses, n_bodies, 16) column-major body transforms. sensor: None (radiance only) or sensor
+        parameters (dict, or True for the renderer's): raw uint16 frames, pose q exposing frame frame0 + q.
+        Returns {"raw": [per camera (n_poses, h, w) uint16], "radiance": [per camera (n_poses, h, w, 4)], "stats": {...}}.
+        raw_out / radiance_out: preallocated host arrays or device tensors (anything with data_ptr()) of all frames."""
+        q, cams, n_poses, keep = self._batch_req(cameras, poses0, poses1, spp, lightSamples, seed, max_depth, shutter, scale, options,
+                                                 None if sensor is None or sensor is False else (sensor if isinstance(sensor, dict) else {}),
+                                                 frame0, optics_scale, use_graph, wave_paths, exposure_s, gain)
+        sizes = [tuple(self.scene["cameras"][c]["size"]) for c in cams]
+        total = sum(n_poses * w * h for w, h in sizes)
+        want_raw = q.sensor is not None and bool(q.sensor)
+        raw = rad = None
+        if want_raw:
+            raw = raw_out if raw_out is not None else np.empty(total, np.uint16)
+        if radiance or radiance_out is not None:
+            rad = radiance_out if radiance_out is not None else np.empty(total * 4, np.float32)
+        ptr = lambda a: None if a is None else (C.c_void_p(a.data_ptr()) if hasattr(a, "data_ptr") else _p(a))
+        st = A.vt_batch_stats()
+        check(self.lib.vt_render_batch(self._ctx, C.byref(q), ptr(raw), ptr(rad), C.byref(st)), self._ctx)
+        out = {"stats": {"ms": st.ms, "shared_paths": st.shared_paths, "pair_paths": st.pair_paths, "samples": st.samples,
+                         "waves": st.waves, "graph_replayed": bool(st.graph_replayed), "reruns": st.reruns, "vary_mask": st.vary_mask}}
+        if raw_out is None and raw is not None:
+            out["raw"], o = [], 0
+            for w, h in sizes:
+                out["raw"].append(raw[o:o + n_poses * w * h].reshape(n_poses, h, w))
+                o += n_poses * w * h
+        if radiance_out is None and rad is not None:
+            out["radiance"], o = [], 0
+            for w, h in sizes:
+                out["radiance"].append(rad[4 * o:4 * (o + n_poses * w * h)].reshape(n_poses, h, w, 4))
+                o += n_poses * w * h
+        del keep
+        return out
+
+    def autotune_batch(self, cameras, poses0, poses1=None, spp=64, lightSamples=1, seed=0, max_depth=6, **kw):
+        """Time the batched renderer's candidate wave sizes and pixel tiles; the fastest is kept for later batches."""
+        q, cams, n_poses, keep = self._batch_req(cameras, poses0, poses1, spp, lightSamples, seed, max_depth, (0.0, 1.0), 1.0, 0, None, 0,
+                                                 1.0, False, 0)
+        rows = (A.vt_tune_row * 64)()
+        n = C.c_uint32(0)
+        best = A.vt_tune_row()
+        check(self.lib.vt_batch_autotune(self._ctx, C.byref(q), rows, 64, C.byref(n), C.byref(best)), self._ctx)
+        del keep
+        tab = [{"wave_paths": r.wave_paths, "tile": (r.tile_w, r.tile_h), "ms_per_mpath": r.ms_per_mpath} for r in rows[:n.value]]
+        return {"wave_paths": best.wave_paths, "tile": (best.tile_w, best.tile_h), "ms_per_mpath": best.ms_per_mpath}, tab
+
     # ------------------------------------------------------------------------------------------- queries
     def trace(self, o4, d4, mask=3, any_hit=False, root=0):
         """gpu/wgsl/kernels.wgsl.js:535 traceTest: rays (o.xyz, time), (d.xyz, -) -> (t, tri, inst, u), v."""
