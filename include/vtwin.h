@@ -267,8 +267,9 @@ typedef struct {
  * host/device rgba32f frames [camera][pose][h][w]. stats may be NULL. */
 vt_status vt_render_batch(vt_ctx* ctx, const vt_batch_req* req, uint16_t* raw_out, float* radiance_out, vt_batch_stats* stats);
 
-/* Autotuner of the batched renderer: times each candidate (wave size x pixel tile) on the request at
- * min(spp, 8) sub-samples and keeps the fastest in the context for later batches with wave_paths = 0.
+/* Autotuner of the batched renderer: times each candidate (wave size x pixel tile) on the request cut to
+ * min(spp, 4) sub-samples and its first 8 poses, and keeps the fastest in the context for later batches with
+ * wave_paths = 0 (results do not depend on either choice).
  * table (may be NULL): up to max_rows rows of (wave_paths, tile_w, tile_h, ms per million shared paths). */
 typedef struct { uint32_t wave_paths, tile_w, tile_h; float ms_per_mpath; } vt_tune_row;
 vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* table, uint32_t max_rows, uint32_t* n_rows,

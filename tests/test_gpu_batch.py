@@ -89,7 +89,7 @@ def test_wave_and_tile_do_not_change_results(rig):
     np.testing.assert_array_equal(small["radiance"][0], ref)
     best, table = r.autotune_batch([0], P, spp=4, max_depth=3, seed=1)
     print("\nautotune", best, len(table))
-    assert len(table) == 16 and best["wave_paths"] > 0
+    assert len(table) >= 4 and best["wave_paths"] > 0   # waves larger than the frames repeat a plan and are skipped
     tuned = r.render_batch([0], P, spp=4, max_depth=3, seed=1, radiance=True, use_graph=False)["radiance"][0]
     np.testing.assert_array_equal(tuned, ref)
 

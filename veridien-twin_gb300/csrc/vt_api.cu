@@ -567,8 +567,9 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   const uint32_t n = q->n, R = q->n_rhs;
   const size_t nb = size_t(n) * R * 4, nf = size_t(n) * n * 4;
   const bool dF = is_device_ptr(q->F);
-  const uint32_t max_blocks = (n + 7) / 8 + 8;
-  const size_t need = (dF ? 0 : nf) + 3 * nb + size_t(n) * 4 + size_t(max_blocks) * 16 + 64 + 1024;
+  const uint32_t max_blocks = std::max<uint32_t>((n + 7) / 8, uint32_t((size_t(n) * R / 4 + 255) / 256)) + 8;
+  const size_t gemm_work = R > 1 ? vtk::jacobi_gemm_fp32_work(n, R) : 0;
+  const size_t need = (dF ? 0 : nf) + 3 * nb + size_t(n) * 4 + size_t(max_blocks) * 16 + gemm_work + 64 + 2048;
   vt_status s = ensure_scratch(ctx, need);
   if (s != VT_OK) return s;
   char* base = static_cast<char*>(ctx->d_scratch);
@@ -580,6 +581,7 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   float* rho = reinterpret_cast<float*>(take(size_t(n) * 4));
   double* partials = reinterpret_cast<double*>(take(size_t(max_blocks) * 16));
   double* norms = reinterpret_cast<double*>(take(64));
+  float* work = gemm_work ? reinterpret_cast<float*>(take(gemm_work)) : nullptr;
   if (!dF && (s = to_device(ctx, const_cast<float*>(Fd), q->F, nf)) != VT_OK) return s;
   if ((s = to_device(ctx, E, q->E, nb)) != VT_OK) return s;
   if ((s = to_device(ctx, rho, q->rho, size_t(n) * 4)) != VT_OK) return s;
@@ -597,11 +599,11 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
     for (uint32_t j = 0; j < k; j++) {
       if (j == 0) VT_CK(cudaEventRecord(ctx->ev2, ctx->stream));
       if (R == 1) vtk::launch_jacobi_matvec(Fd, rho, E, cur, nxt, n, partials, &np, ctx->stream);
-      else vtk::launch_jacobi_gemm_fp32(Fd, rho, E, cur, nxt, n, R, partials, &np, ctx->stream);
+      else vtk::launch_jacobi_gemm_fp32(Fd, rho, E, cur, nxt, n, R, work, partials, &np, ctx->stream);
       if (j == 0) VT_CK(cudaEventRecord(ctx->ev3, ctx->stream));
       std::swap(cur, nxt);
     }
-    ctx->tim.launches += k + 1;
+    ctx->tim.launches += k * (work ? 2 : 1) + 1;
     it += k;
     vtk::launch_reduce_partials(partials, np, norms, ctx->stream);
     VT_CK(cudaGetLastError());

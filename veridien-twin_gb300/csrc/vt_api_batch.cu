@@ -376,16 +376,21 @@ vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* t
   vt_status s = validate(ctx, req, nullptr);
   if (s != VT_OK) return s;
   vt_batch_req q = *req;
-  q.spp = std::min(std::max(req->spp, 1u), 8u);
+  q.spp = std::min(std::max(req->spp, 1u), 4u);
+  q.n_poses = std::min(req->n_poses, 8u);
   q.sensor = nullptr;
   q.use_graph = 0;
   const uint32_t waves[] = {2u << 20, 4u << 20, 8u << 20, 16u << 20};
   const uint32_t tiles[][2] = {{8, 4}, {16, 2}, {4, 8}, {32, 1}};
   vt_tune_row top{0, 0, 0, INFINITY};
   uint32_t rows = 0;
+  uint32_t prev_pw = 0;
   for (uint32_t w : waves) {
+    Plan pl;
+    if ((s = plan_batch(ctx, &q, w, vtk::TILE_W, vtk::TILE_H, pl)) != VT_OK) return s;
+    if (pl.n_pw == prev_pw) continue;   // the frames already fit a smaller wave: the same plan
+    prev_pw = pl.n_pw;
     for (const auto& t : tiles) {
-      Plan pl;
       double ms = 0;
       bool overflow = false, replayed = false;
       uint32_t vary = 0;

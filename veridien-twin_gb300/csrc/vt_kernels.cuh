@@ -38,8 +38,10 @@ void launch_sensor_expose_u16(const SensorParams& su, const float4* E, float sca
 void launch_jacobi_matvec(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n,
                           double* partials, uint32_t* n_partials, cudaStream_t st);
 // B_out = E + rho (F B_in), n x R row-major (R <= 64, multiple of 4), CUDA-core FP32 GEMM
+// work: jacobi_gemm_fp32_work(n, R) bytes for the split-K partial products (null: no split)
+size_t jacobi_gemm_fp32_work(uint32_t n, uint32_t R);
 void launch_jacobi_gemm_fp32(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n, uint32_t R,
-                             double* partials, uint32_t* n_partials, cudaStream_t st);
+                             float* work, double* partials, uint32_t* n_partials, cudaStream_t st);
 // sum the partials into out[0..1] (deterministic order)
 void launch_reduce_partials(const double* partials, uint32_t n, double* out, cudaStream_t st);
 void launch_form_factors(uint32_t n, const float* C, const float* N, const float* A, float* F, cudaStream_t st);

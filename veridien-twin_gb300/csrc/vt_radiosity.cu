@@ -4,10 +4,13 @@
 //   jacobi_matvec   one right-hand side: one warp per row, F streamed with 128-bit loads (HBM- or L2-bound: 4 B of F
 //                   per 2 flops), B_in read from L1/L2; epilogue B_out = E + rho acc and the residual partials.
 //   jacobi_gemm     R right-hand sides (R <= 64): a 128 x 64 output tile per 256-thread block, 8 x 4 outputs per
-//                   thread, F and B staged through shared memory in 32-wide K slices. Compute-bound at 2 R flops per
-//                   4-byte element of F (R = 64: 32 flop/B) on the FP32 pipes.
+//                   thread, F and B staged through double-buffered shared memory in 16-wide K slices, K split across
+//                   blocks to fill the GPU. Compute-bound at 2 R flops per 4-byte element of F (R = 64: 32 flop/B)
+//                   on the FP32 pipes.
 // Every sweep also writes per-block sums of |B_out - B_in|^2 and |B_out|^2 in FP64; the relative update
 // |B_out - B_in| / |B_out| is the relative residual |E + rho F B_in - B_in| / |B_out| of the Jacobi iterate.
+#include <algorithm>
+
 #include "vt_kernels.cuh"
 
 namespace vtk {
@@ -71,56 +74,73 @@ void launch_jacobi_matvec(const float* F, const float* rho, const float* E, cons
 }
 
 // ---------------------------------------------------------------------------------------------- FP32 GEMM sweep
-constexpr int GM = 128, GN = 64, GK = 32, G_THREADS = 256;
+// 128 x 64 output tile per 256-thread block (8 x 4 outputs per thread), K in 16-wide slices double-buffered through
+// shared memory: the next slice's F and B loads are in flight in registers while the current slice is multiplied.
+// K is split over `splits` blocks per row tile so the grid fills the 152 SMs several times over; the split partial
+// products are summed in split order by the combine kernel, which also applies the Jacobi update.
+constexpr int GM = 128, GN = 64, GK = 16, G_THREADS = 256;
 
+template <bool SPLIT>
 __global__ void __launch_bounds__(G_THREADS) jacobi_gemm_fp32_kernel(const float* __restrict__ F, const float* __restrict__ rho,
                                                                      const float* __restrict__ E, const float* __restrict__ Bin,
-                                                                     float* __restrict__ Bout, uint32_t n, uint32_t R,
-                                                                     double* __restrict__ partials) {
-  __shared__ __align__(16) float As[GK][GM + 4];   // F tile, transposed: As[k][m]
-  __shared__ __align__(16) float Bs[GK][GN];       // B tile: Bs[k][c]
+                                                                     float* __restrict__ Bout, uint32_t n, uint32_t R, uint32_t kchunk,
+                                                                     float* __restrict__ part, double* __restrict__ partials) {
+  __shared__ __align__(16) float As[2][GK][GM + 4];   // F slices, transposed: As[b][k][m]
+  __shared__ __align__(16) float Bs[2][GK][GN];       // B slices: Bs[b][k][c]
   const uint32_t tid = threadIdx.x;
   const uint32_t row0 = blockIdx.x * GM;
+  const uint32_t kbeg = blockIdx.y * kchunk, kend = min(n, kbeg + kchunk);
   const uint32_t tm = tid / 16, tn = tid % 16;      // 16 x 16 threads, each 8 rows x 4 cols
+  const bool vec = (n & 3u) == 0u;
   float acc[8][4];
 #pragma unroll
   for (int i = 0; i < 8; i++)
 #pragma unroll
     for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
-  for (uint32_t k0 = 0; k0 < n; k0 += GK) {
-    // F tile 128 x 32: 1024 float4, 4 per thread
+  float4 fa[2], fb;
+  // F slice 128 x 16: 512 float4, 2 per thread; B slice 16 x 64: 256 float4, 1 per thread (columns >= R are zero)
+  auto load = [&](uint32_t k0) {
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const uint32_t idx = tid + q * G_THREADS;         // 0..1023
+    for (int q = 0; q < 2; q++) {
+      const uint32_t idx = tid + q * G_THREADS;
       const uint32_t r = idx / (GK / 4), c4 = idx % (GK / 4);
       const uint32_t gr = row0 + r, gk = k0 + c4 * 4;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (gr < n) {
         const float* p = F + size_t(gr) * n;
-        if ((n & 3u) == 0u && gk + 3 < n) v = __ldcs(reinterpret_cast<const float4*>(p + gk));   // 16-byte aligned rows
+        if (vec && gk + 3 < kend) v = __ldcs(reinterpret_cast<const float4*>(p + gk));   // 16-byte aligned rows
         else {
-          v.x = gk < n ? p[gk] : 0.f; v.y = gk + 1 < n ? p[gk + 1] : 0.f; v.z = gk + 2 < n ? p[gk + 2] : 0.f;
-          v.w = gk + 3 < n ? p[gk + 3] : 0.f;
+          v.x = gk < kend ? p[gk] : 0.f; v.y = gk + 1 < kend ? p[gk + 1] : 0.f; v.z = gk + 2 < kend ? p[gk + 2] : 0.f;
+          v.w = gk + 3 < kend ? p[gk + 3] : 0.f;
         }
       }
-      As[c4 * 4 + 0][r] = v.x; As[c4 * 4 + 1][r] = v.y; As[c4 * 4 + 2][r] = v.z; As[c4 * 4 + 3][r] = v.w;
+      fa[q] = v;
     }
-    // B tile 32 x 64: 512 float4, 2 per thread (columns >= R are zero)
+    const uint32_t r = tid / (GN / 4), c4 = tid % (GN / 4);
+    const uint32_t gk = k0 + r, gc = c4 * 4;
+    fb = (gk < kend && gc < R) ? __ldg(reinterpret_cast<const float4*>(Bin + size_t(gk) * R + gc)) : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  auto store = [&](int b) {
 #pragma unroll
     for (int q = 0; q < 2; q++) {
       const uint32_t idx = tid + q * G_THREADS;
-      const uint32_t r = idx / (GN / 4), c4 = idx % (GN / 4);
-      const uint32_t gk = k0 + r, gc = c4 * 4;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gk < n && gc < R) v = __ldg(reinterpret_cast<const float4*>(Bin + size_t(gk) * R + gc));
-      *reinterpret_cast<float4*>(&Bs[r][gc]) = v;
+      const uint32_t r = idx / (GK / 4), c4 = idx % (GK / 4);
+      As[b][c4 * 4 + 0][r] = fa[q].x; As[b][c4 * 4 + 1][r] = fa[q].y; As[b][c4 * 4 + 2][r] = fa[q].z; As[b][c4 * 4 + 3][r] = fa[q].w;
     }
-    __syncthreads();
-#pragma unroll 8
+    *reinterpret_cast<float4*>(&Bs[b][tid / (GN / 4)][(tid % (GN / 4)) * 4]) = fb;
+  };
+  load(kbeg);
+  store(0);
+  __syncthreads();
+  int buf = 0;
+  for (uint32_t k0 = kbeg; k0 < kend; k0 += GK) {
+    const bool more = k0 + GK < kend;
+    if (more) load(k0 + GK);
+#pragma unroll
     for (int k = 0; k < GK; k++) {
-      const float4 a0 = *reinterpret_cast<const float4*>(&As[k][tm * 8]);
-      const float4 a1 = *reinterpret_cast<const float4*>(&As[k][tm * 8 + 4]);
-      const float4 b = *reinterpret_cast<const float4*>(&Bs[k][tn * 4]);
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][k][tm * 8]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][k][tm * 8 + 4]);
+      const float4 b = *reinterpret_cast<const float4*>(&Bs[buf][k][tn * 4]);
       const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
       const float bb[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
@@ -128,7 +148,19 @@ __global__ void __launch_bounds__(G_THREADS) jacobi_gemm_fp32_kernel(const float
 #pragma unroll
         for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
     }
+    if (more) store(buf ^ 1);
     __syncthreads();
+    buf ^= 1;
+  }
+  if (SPLIT) {
+    // partial product of this K range: part[split][row][col]
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const uint32_t gr = row0 + tm * 8 + i, gc = tn * 4;
+      if (gr >= n || gc >= R) continue;
+      *reinterpret_cast<float4*>(part + (size_t(blockIdx.y) * n + gr) * R + gc) = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    }
+    return;
   }
   double d2 = 0.0, b2 = 0.0;
 #pragma unroll
@@ -151,11 +183,71 @@ __global__ void __launch_bounds__(G_THREADS) jacobi_gemm_fp32_kernel(const float
   block_sum2(d2, b2, partials);
 }
 
+// B_out = E + rho (sum over splits of the partial products, in split order), and the residual partials
+__global__ void __launch_bounds__(256) jacobi_gemm_combine_kernel(const float* __restrict__ part, uint32_t splits, const float* __restrict__ rho,
+                                                                  const float* __restrict__ E, const float* __restrict__ Bin,
+                                                                  float* __restrict__ Bout, uint32_t n, uint32_t R, double* __restrict__ partials) {
+  const size_t total = size_t(n) * R / 4, stride = size_t(n) * R / 4;
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  double d2 = 0.0, b2 = 0.0;
+  if (i < total) {
+    const float4* P = reinterpret_cast<const float4*>(part);
+    float4 a = P[i];
+    for (uint32_t s = 1; s < splits; s++) {
+      const float4 v = P[s * stride + i];
+      a.x += v.x; a.y += v.y; a.z += v.z; a.w += v.w;
+    }
+    const float rr = rho[(i * 4) / R];
+    const float4 e = reinterpret_cast<const float4*>(E)[i], bi = reinterpret_cast<const float4*>(Bin)[i];
+    const float4 b = make_float4(fmaf(rr, a.x, e.x), fmaf(rr, a.y, e.y), fmaf(rr, a.z, e.z), fmaf(rr, a.w, e.w));
+    reinterpret_cast<float4*>(Bout)[i] = b;
+    const double dx = double(b.x) - bi.x, dy = double(b.y) - bi.y, dz = double(b.z) - bi.z, dw = double(b.w) - bi.w;
+    d2 = dx * dx + dy * dy + dz * dz + dw * dw;
+    b2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z + double(b.w) * b.w;
+  }
+  block_sum2(d2, b2, partials);
+}
+
+namespace {
+uint32_t gemm_splits(uint32_t n, int sms) {
+  const uint32_t tiles = (n + GM - 1) / GM;
+  const uint32_t want = uint32_t(8 * std::max(sms, 1));   // about 8 blocks per SM in flight over the sweep
+  uint32_t s = std::max(1u, std::min(16u, (want + tiles - 1) / tiles));
+  while (s > 1 && (n + s - 1) / s < 4 * GK) s--;          // at least 64 columns of F per split
+  return s;
+}
+int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+}  // namespace
+
+size_t jacobi_gemm_fp32_work(uint32_t n, uint32_t R) {
+  const uint32_t s = gemm_splits(n, sm_count());
+  return s > 1 ? size_t(s) * n * R * 4 : 0;
+}
+
 void launch_jacobi_gemm_fp32(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n, uint32_t R,
-                             double* partials, uint32_t* n_partials, cudaStream_t st) {
-  const uint32_t blocks = (n + GM - 1) / GM;
+                             float* work, double* partials, uint32_t* n_partials, cudaStream_t st) {
+  const uint32_t tiles = (n + GM - 1) / GM;
+  const uint32_t s = work ? gemm_splits(n, sm_count()) : 1u;
+  const uint32_t kchunk = s > 1 ? ((n + s - 1) / s + GK - 1) / GK * GK : n;
+  const uint32_t splits = (n + kchunk - 1) / kchunk;
+  if (splits <= 1) {
+    *n_partials = tiles;
+    jacobi_gemm_fp32_kernel<false><<<dim3(tiles, 1), G_THREADS, 0, st>>>(F, rho, E, Bin, Bout, n, R, n, nullptr, partials);
+    return;
+  }
+  jacobi_gemm_fp32_kernel<true><<<dim3(tiles, splits), G_THREADS, 0, st>>>(F, rho, E, Bin, Bout, n, R, kchunk, work, partials);
+  const uint32_t blocks = uint32_t((size_t(n) * R / 4 + 255) / 256);
   *n_partials = blocks;
-  jacobi_gemm_fp32_kernel<<<blocks, G_THREADS, 0, st>>>(F, rho, E, Bin, Bout, n, R, partials);
+  jacobi_gemm_combine_kernel<<<blocks, 256, 0, st>>>(work, splits, rho, E, Bin, Bout, n, R, partials);
 }
 
 __global__ void reduce_partials_kernel(const double* __restrict__ p, uint32_t n, double* __restrict__ out) {
