@@ -275,6 +275,56 @@ typedef struct { uint32_t wave_paths, tile_w, tile_h; float ms_per_mpath; } vt_t
 vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* table, uint32_t max_rows, uint32_t* n_rows,
                             vt_tune_row* best);
 
+/* ------------------------------------------------------------------------------ differentiable calibration */
+
+/* No counterpart in the reference, which differentiates nothing (it has only the analytic dtheta_d/dtheta of
+ * gpu/lens.js:25). A forward/backward pair for calibrating the twin from camera images:
+ *
+ *   image model  per camera sub-sample (the path tracer's KB4 rays and sample numbers), up to max_depth vertices on
+ *                Lambertian surfaces: nL emitter samples per vertex (area CDF, power-heuristic MIS), cosine-weighted
+ *                continuation, and at the last vertex the node radiosity's light rho/pi x H(node), H = F B;
+ *   radiosity    n nodes (clusters of the static triangles), B = rho_node o (D L + F B) per colour channel: D the
+ *                direct transfer from each emitter triangle (visibility through the BVH), L the emitter triangles'
+ *                radiances, F the node form factors; `jacobi_iters` Jacobi sweeps;
+ *   loss         mean over pixels and channels of (I - T)^2 against per-camera target images (FP64 reduction).
+ *
+ * The backward replays every path from its sample numbers (path-replay backpropagation) and solves the transposed
+ * radiosity system lambda = F^T (g_H + rho o lambda) for the nodes' share. Parameters: per-material albedo (RGB, all
+ * in (0, 1]) and per-emitter-triangle radiance. KB4 intrinsics enter through vt_reproj_loss (analytic Jacobians);
+ * the image term's dependence on them (through visibility edges) is not differentiated. */
+typedef struct {
+  uint32_t n_nodes;       /* radiosity nodes (<= static triangles), e.g. 4096 */
+  uint32_t lamp_samples;  /* points per (node, emitter triangle) for D, e.g. 16 */
+} vt_calib_desc;
+typedef struct { uint32_t n_nodes, n_materials, n_lamps, n_static_tris; } vt_calib_info;
+vt_status vt_calib_setup(vt_ctx* ctx, const vt_calib_desc* desc, vt_calib_info* info);
+/* The calibration model's node data for checking (any pointer may be NULL): centres, normals (n x 3), areas (n),
+ * node materials (n), node of each static triangle slot, F (n x n), D (n x n_lamps). */
+vt_status vt_calib_export(vt_ctx* ctx, float* centres, float* normals, float* areas, uint32_t* node_mat, uint32_t* tri_node, float* F,
+                          float* D);
+typedef struct {
+  const uint32_t* cameras;
+  uint32_t n_cameras;
+  uint32_t spp, light_samples, seed, max_depth;  /* light_samples 1..4, max_depth 1..4 */
+  uint32_t jacobi_iters;                          /* radiosity sweeps, forward and adjoint (0: 96) */
+  const double* albedo;                           /* n_materials x 3 */
+  const double* lamp;                             /* n_lamps */
+  const float* targets;                           /* rgba32f target images of the cameras, concatenated; NULL: keep the last */
+  float* images;                                  /* optional out: the rendered images, same layout (host or device) */
+} vt_calib_req;
+/* Image loss of the request (and the images). Keeps the state the backward replays. */
+vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* req, double* loss);
+/* Gradient of the last forward's image loss: g_albedo (n_materials x 3), g_lamp (n_lamps). */
+vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp);
+/* KB4 intrinsics of a camera: fx, fy, cx, cy, k1..k4 (gpu/lens.js:8 lensParams; skew stays). */
+vt_status vt_set_camera_intrinsics(vt_ctx* ctx, uint32_t camera, const double K[8]);
+vt_status vt_get_camera_intrinsics(const vt_ctx* ctx, uint32_t camera, double K[8]);
+/* Reprojection loss of n_pts dome-frame points in the cameras (gpu/lens.js:43 project, FP64): mean over cameras,
+ * points and both coordinates of (uv - uv_target)^2, uv_target n_cameras x n_pts x 2; g_K (n_cameras x 8) its
+ * gradient with respect to each camera's (fx, fy, cx, cy, k1..k4) by the analytic KB4 Jacobian. */
+vt_status vt_reproj_loss(vt_ctx* ctx, const uint32_t* cameras, uint32_t n_cameras, const double* pts, uint32_t n_pts, const double* uv_target,
+                         double* loss, double* g_K);
+
 /* -------------------------------------------------------------------------------------- node radiosity */
 
 enum { VT_PREC_FP32 = 0, VT_PREC_BF16 = 1, VT_PREC_FP8 = 2 };

@@ -35,7 +35,7 @@ def lib():
         _lib.or_scene_create.argtypes = [C.c_void_p, C.c_int, C.c_int]
         for nm in ("or_scene_destroy", "or_scene_sizes", "or_scene_arrays", "or_scene_emitter", "or_scene_blas",
                    "or_scene_set_poses", "or_scene_set_eavg", "or_scene_uniform", "or_scene_set_node_state",
-                   "or_trace_wgsl", "or_render"):
+                   "or_trace_wgsl", "or_render", "or_calib_render", "or_direct_transfer"):
             getattr(_lib, nm).restype = None
         _lib.or_fresnel_average.restype = C.c_double
         _lib.or_disc_irradiance.restype = C.c_double
@@ -43,6 +43,7 @@ def lib():
         _lib.or_capsule_occ.restype = C.c_double
         _lib.or_jacobi64.restype = C.c_int
         _lib.or_bvh_build.restype = C.c_int
+        _lib.or_scene_emit_count.restype = C.c_uint32
     return _lib
 
 
@@ -227,6 +228,47 @@ class Scene:
         lib().or_render(self.h, C.byref(req), C.c_uint32(y0), C.c_uint32(y1), C.c_uint32(x0), C.c_uint32(x1), int(fp64),
                         int(threads), _p(out), _p(dbg, C.c_uint64))
         return out, dbg
+
+    # ----------------------------------------------------------------------------------------- calibration
+    def calib_render(self, camera, albedo, lamp, H, tri_node, spp=4, nl=1, seed=0, depth=3, y0=0, y1=None, fp64=True, threads=1):
+        """The calibration estimator of the CUDA library restated: rows [y0, y1) of a camera's image (h, w, 3)."""
+        cam = self.scene["cameras"][camera]
+        W, Hh = cam["size"]
+        y1 = Hh if y1 is None else y1
+        alb = np.ascontiguousarray(albedo, np.float64).ravel()
+        lam = np.ascontiguousarray(lamp, np.float64).ravel()
+        Hn = np.ascontiguousarray(H, np.float64).ravel()
+        tn = np.ascontiguousarray(tri_node, np.uint32)
+        out = np.zeros((y1 - y0, W, 3))
+        lib().or_calib_render(self.h, C.c_uint32(camera), C.c_uint32(spp), C.c_uint32(nl), C.c_uint32(seed), C.c_uint32(depth), _p(alb),
+                              _p(lam), _p(Hn), C.c_uint32(len(Hn) // 3), _p(tn, C.c_uint32), C.c_uint32(y0), C.c_uint32(y1), int(fp64),
+                              int(threads), _p(out))
+        return out
+
+    def direct_transfer(self, centres, normals, samples=16, fp64=True, threads=1):
+        """Irradiance at each node from each emitter triangle at unit radiance (n x n_lamps), with visibility."""
+        Cn = np.ascontiguousarray(centres, np.float32)
+        Nn = np.ascontiguousarray(normals, np.float32)
+        n = len(Cn)
+        D = np.zeros((n, int(lib().or_scene_emit_count(self.h))))
+        lib().or_direct_transfer(self.h, _p(Cn, C.c_float), _p(Nn, C.c_float), C.c_uint32(n), C.c_uint32(samples), int(fp64), int(threads),
+                                 _p(D))
+        return D
+
+
+def calib_radiosity(F, D, lamp, albedo, node_mat):
+    """The calibration model's node radiosity in FP64: B_c = rho_c o (D L + F B_c) by a direct solve per channel;
+    returns H = F B (3 x n) and B."""
+    F = np.asarray(F, np.float64)
+    n = len(F)
+    DL = np.asarray(D, np.float64) @ np.asarray(lamp, np.float64)
+    H = np.zeros((3, n))
+    B = np.zeros((3, n))
+    for c in range(3):
+        rho = np.asarray(albedo, np.float64)[np.asarray(node_mat), c]
+        B[c] = np.linalg.solve(np.eye(n) - rho[:, None] * F, rho * DL)
+        H[c] = F @ B[c]
+    return H, B
 
 
 def sensor_expose(su_words, E4):

@@ -753,6 +753,7 @@ struct Scene {
   // instance poses
   struct Pose4 { double q0[4], q1[4], p0[3], p1[3]; bool valid; };
   std::vector<Pose4> inst;
+  std::vector<uint32_t> emitOfTri;   // per triangle slot: index in the emitter table, or MISS
 };
 
 // gpu/scene_gpu.js:504 fitCapsule
@@ -808,11 +809,14 @@ static Scene* prepare_scene(const vt_scene_desc* sd, int leafSize, int albedoSam
   std::vector<BVH> bb;
   struct EmitTri { double v0[3], e1[3], e2[3], n[3], area, cdf; };
   std::vector<EmitTri> emit;
+  std::vector<std::vector<uint32_t>> emitIdx(sd->n_bodies);
   for (uint32_t bi = 0; bi < sd->n_bodies; bi++) {
     const vt_body_desc& B = sd->bodies[bi];
     bb.push_back(build_bvh(B.P, B.I, B.n_tris, leafSize));
+    emitIdx[bi].assign(B.n_tris, MISS);
     for (uint32_t t = 0; t < B.n_tris; t++) {
       if (!(sd->meshes[B.tri_mesh[t]].flags & VT_F_EMITTER)) continue;
+      emitIdx[bi][t] = uint32_t(emit.size());
       size_t a = size_t(B.I[3 * t]) * 3, b = size_t(B.I[3 * t + 1]) * 3, c = size_t(B.I[3 * t + 2]) * 3;
       EmitTri e;
       for (int k = 0; k < 3; k++) { e.v0[k] = B.P[a + k]; e.e1[k] = double(B.P[b + k]) - e.v0[k]; e.e2[k] = double(B.P[c + k]) - e.v0[k]; }
@@ -845,6 +849,7 @@ static Scene* prepare_scene(const vt_scene_desc* sd, int leafSize, int albedoSam
     std::copy(u.begin(), u.end(), S->nodes.begin() + size_t(S->blas[bi].root) * 16);
   }
   S->tris.assign(size_t(triTotal) * 16, 0);
+  S->emitOfTri.assign(triTotal, MISS);
   for (uint32_t k = 0; k < sd->n_static_tris; k++) {
     uint32_t t = sb.order[k];
     uint32_t m = sd->static_tri_mesh[t];
@@ -859,6 +864,7 @@ static Scene* prepare_scene(const vt_scene_desc* sd, int leafSize, int albedoSam
       uint32_t t = bb[bi].order[k];
       uint32_t m = B.tri_mesh[t];
       pack_tri(S->tris, S->blas[bi].tri_off + k, B.P, B.I, t, B.I[3 * t] + vbase, B.I[3 * t + 1] + vbase, B.I[3 * t + 2] + vbase, m, sd->meshes[m].flags);
+      S->emitOfTri[S->blas[bi].tri_off + k] = emitIdx[bi][t];
     }
     vbase += B.n_verts;
   }
@@ -1653,6 +1659,162 @@ template <typename R> static void render_pixel(Tracer<R>& tr, const Shader<R>& s
   out[3] = key == 0xfffeu ? 0.0 : 1.0;
 }
 
+// ============================================================================================ calibration
+// The differentiable calibration estimator of the CUDA library (its own model: the reference differentiates
+// nothing), restated for the CPU: Lambertian vertices (f = rho / pi), nL emitter samples per vertex with the power
+// heuristic against cosine sampling, cosine continuation (throughput x rho), the node term rho / pi x H(node) at the
+// last vertex, emitter hits MIS-weighted after the first vertex. Parameters: per-material albedo, per-emitter-
+// triangle radiance, node irradiance H (planar 3 x n).
+struct CalibIn {
+  const double* albedo; const double* lamp; const double* H; uint32_t nNodes; const uint32_t* triNode; uint32_t nStatic;
+};
+template <typename R> static V3<R> calib_path(Tracer<R>& tr, const Shader<R>& sh, const CalibIn& C, const V3<R>& pos, const V3<R>& d0, R tt,
+                                              uint32_t i, const PixSeeds& Sd, uint32_t nl, uint32_t depth, uint32_t skip) {
+  const Scene& S = tr.S;
+  V3<R> L, T(1, 1, 1), o = pos, d = d0;
+  const R area = R(tr.SU[3]);
+  R pbPrev = 0;
+  for (uint32_t b = 1; b <= depth; b++) {
+    Hit<R> h;
+    if (b == 1) {
+      h = tr.trace(o, d, R(0), R(BIGD), tt, false, 1u, 0u);
+      Hit<R> hd = tr.trace(o, d, R(0), h.t, tt, false, 2u, skip);
+      if (hd.tri != MISS) h = hd;
+    } else {
+      h = tr.trace(o, d, R(0), R(BIGD), tt, false, 3u, 0u);
+    }
+    if (h.tri == MISS) break;
+    Surf<R> s = sh.surface(h, o, d, tt);
+    if (s.flags & VT_F_EMITTER) {
+      V3<R> nE = sh.emitter_normal(h, s, tt);
+      R cosE = dot(-d, nE);
+      if (cosE > R(0)) {
+        R prof = sh.profile(std::acos(clampR(dot(-d, sh.emitter_axis_at(tt)), R(-1), R(1))));
+        R w = 1;
+        if (b > 1) {
+          R pL = h.t * h.t / (cosE * area);
+          w = pbPrev * pbPrev / (pbPrev * pbPrev + R(nl) * R(nl) * pL * pL);
+        }
+        uint32_t t = S.emitOfTri[h.tri];
+        L = L + T * (w * prof * R(C.lamp[t]));
+      }
+      break;
+    }
+    const double* alb = C.albedo + 3 * s.mat;
+    const V3<R> rho = V3<R>(R(alb[0]), R(alb[1]), R(alb[2]));
+    V3<R> n = s.ns, wo = -d;
+    R sum = 0;
+    for (uint32_t j = 0; j < nl; j++) {
+      V3<R> u;
+      if (b == 1) u = V3<R>(kr(i * nl + j, KL0, Sd.s[3]), kr(i * nl + j, KL1, Sd.s[4]), kr(i * nl + j, KL2, Sd.s[5]));
+      else u = V3<R>(kr(i * nl + j, KL0, bounce_shift(Sd, b, 0)), kr(i * nl + j, KL1, bounce_shift(Sd, b, 1)), kr(i * nl + j, KL2, bounce_shift(Sd, b, 2)));
+      // the emitter triangle of the sample (the same CDF search as sample_emitter)
+      uint32_t lo = 0, hi = S.emitN - 1;
+      for (uint32_t it = 0; it < 40 && lo < hi; it++) {
+        uint32_t m = (lo + hi) / 2;
+        if (R(sh.pv(S.emitOff + 4 * m)[3]) < u.x) lo = m + 1; else hi = m;
+      }
+      V3<R> lp, ln, la;
+      sh.sample_emitter(u, tt, lp, ln, la);
+      V3<R> wi = lp - s.p;
+      R d2 = dot(wi, wi), dist = std::sqrt(d2);
+      wi = wi / dist;
+      R cosE = dot(-wi, ln), cosS = dot(n, wi);
+      if (cosE <= R(0) || cosS <= R(0) || dot(s.ng, wi) <= R(0) || dot(n, wo) <= R(0)) continue;
+      R prof = sh.profile(std::acos(clampR(dot(-wi, la), R(-1), R(1))));
+      if (prof <= R(0)) continue;
+      R pdfW = d2 / (cosE * area), pb = cosS * R(INV_PI_D);
+      R w = R(nl) * R(nl) * pdfW * pdfW / (R(nl) * R(nl) * pdfW * pdfW + pb * pb);
+      Hit<R> shd = tr.trace(Shader<R>::offset_ray(s.p, s.ng, wi), wi, R(0), dist - R(2e-5), tt, true, 3u, tr.su_u(7));
+      if (shd.tri == MISS) sum = sum + R(C.lamp[lo]) * (prof * cosS * w * R(INV_PI_D) / pdfW);
+    }
+    V3<R> Tr = T * rho;
+    L = L + Tr * (sum / R(nl));
+    if (b == depth) {
+      if (h.inst == MISS && h.tri < C.nStatic) {
+        uint32_t nd = C.triNode[h.tri];
+        const V3<R> Hn = V3<R>(R(C.H[nd]), R(C.H[C.nNodes + nd]), R(C.H[2 * C.nNodes + nd]));
+        L = L + Tr * Hn * R(INV_PI_D);
+      }
+      break;
+    }
+    if (dot(n, wo) <= R(0)) break;
+    R u1 = b == 1 ? R(kr(i, KB1, Sd.s[7])) : R(kr(i, KB1, bounce_shift(Sd, b, 4)));
+    R u2 = b == 1 ? R(kr(i, KB2, Sd.s[8])) : R(kr(i, KB2, bounce_shift(Sd, b, 5)));
+    V3<R> tb = basis_t(n), bb = basis_b(n);
+    R r = std::sqrt(u1);
+    V3<R> l = tb * (r * std::cos(R(2) * R(M_PI) * u2)) + bb * (r * std::sin(R(2) * R(M_PI) * u2)) + n * std::sqrt(std::max(R(0), R(1) - u1));
+    R cl = dot(n, l);
+    if (cl <= R(0) || dot(s.ng, l) <= R(0)) break;
+    pbPrev = cl * R(INV_PI_D);
+    T = Tr;
+    o = Shader<R>::offset_ray(s.p, s.ng, l);
+    d = l;
+  }
+  return L;
+}
+
+template <typename R> static void calib_pixel(Tracer<R>& tr, const Shader<R>& sh, const CalibIn& C, const vt_camera_desc& cam, uint32_t camIndex,
+                                              uint32_t spp, uint32_t nl, uint32_t seed, uint32_t depth, uint32_t x, uint32_t y, uint32_t skip,
+                                              double out[3]) {
+  Lens L{double(float(cam.fx)), double(float(cam.fy)), double(float(cam.cx)), double(float(cam.cy)), double(float(cam.alpha)),
+         {double(float(cam.k[0])), double(float(cam.k[1])), double(float(cam.k[2])), double(float(cam.k[3]))}};
+  const double* T = cam.T_D_C;
+  auto col = [&](int a, int b, int c) { return V3<R>(R(float(T[a])), R(float(T[b])), R(float(T[c]))); };
+  V3<R> rx = col(0, 4, 8), ry = col(1, 5, 9), rz = col(2, 6, 10), pos = col(3, 7, 11);
+  PixSeeds Sd = pix_seeds(x, y, seed, camIndex);
+  V3<R> acc;
+  for (uint32_t i = 0; i < spp; i++) {
+    float uvx = float(x) + kr(i, R2A, Sd.s[0]);
+    uvx = uvx - 0.5f;
+    float uvy = float(y) + kr(i, R2B, Sd.s[1]);
+    uvy = uvy - 0.5f;
+    float tt = mixf(0.0f, 1.0f, kr(i, GOLD, Sd.s[2]));
+    V3<R> dc = kb4_unproject<R>(L, R(uvx), R(uvy));
+    V3<R> d = normalize(rx * dc.x + ry * dc.y + rz * dc.z);
+    acc = acc + calib_path<R>(tr, sh, C, pos, d, R(tt), i, Sd, nl, depth, skip);
+  }
+  R sc = R(1) / R(spp);
+  out[0] = double(acc.x * sc); out[1] = double(acc.y * sc); out[2] = double(acc.z * sc);
+}
+
+// irradiance at each node (centre, normal) from each emitter triangle at unit radiance: stratified points
+// (Kronecker, the sampler's triangle warp), cosines, profile, visibility through the BVH
+template <typename R> static void direct_transfer(Tracer<R>& tr, const Shader<R>& sh, const float* Cn, const float* Nn, uint32_t n0, uint32_t n1,
+                                                  uint32_t samples, double* D) {
+  const Scene& S = tr.S;
+  const uint32_t nL = S.emitN;
+  M3<R> M; V3<R> pp;
+  tr.inst_pose(tr.su_u(17), R(0.5), M, pp);
+  V3<R> axis = M.mul(ld3<R>(tr.SU + 4));
+  for (uint32_t i = n0; i < n1; i++) {
+    V3<R> c = ld3<R>(Cn + 3 * i), nn = ld3<R>(Nn + 3 * i);
+    V3<R> org = c + nn * R(1e-4);
+    for (uint32_t t = 0; t < nL; t++) {
+      const float* e = sh.pv(S.emitOff + 4 * t);
+      V3<R> v0 = ld3<R>(e), e1 = ld3<R>(e + 4), e2 = ld3<R>(e + 8), nl0 = ld3<R>(e + 12);
+      R At = R(0.5) * len(cross(e1, e2));
+      V3<R> nl = M.mul(nl0);
+      R acc = 0;
+      for (uint32_t s = 0; s < samples; s++) {
+        R u1 = R(kr(s, R2A, 0.5f)), u2 = R(kr(s, R2B, 0.5f));
+        R su = std::sqrt(u1);
+        V3<R> lp = M.mul(v0 + e1 * (su * (R(1) - u2)) + e2 * (su * u2)) + pp;
+        V3<R> w = lp - org;
+        R r2 = dot(w, w), r = std::sqrt(r2);
+        w = w / r;
+        R ci = dot(nn, w), ct = dot(nl, -w);
+        if (ci <= R(0) || ct <= R(0)) continue;
+        R prof = sh.profile(std::acos(clampR(dot(-w, axis), R(-1), R(1))));
+        if (prof <= R(0)) continue;
+        Hit<R> h = tr.trace(org, w, R(0), r - R(2e-5), R(0.5), true, 3u, tr.su_u(7));
+        if (h.tri == MISS) acc = acc + prof * ci * ct / r2;
+      }
+      D[size_t(i) * nL + t] = double(acc * At / R(samples));
+    }
+  }
+}
+
 // ============================================================================================ sensor (f32)
 // gpu/wgsl/sensor.wgsl.js:46-208. The elementary functions are this project's own fixed-order float32 versions
 // (the same sequence of correctly rounded operations on the device), so raw DN agree bit for bit:
@@ -2053,6 +2215,64 @@ void or_render(void* h, const vt_render_req* q, uint32_t y0, uint32_t y1, uint32
   }
   if (dbgOut) for (int k = 0; k < 16; k++) { dbgOut[k] = 0; for (auto& d : dbgs) dbgOut[k] += d.c[k]; }
 }
+
+void or_calib_render(void* h, uint32_t camera, uint32_t spp, uint32_t nl, uint32_t seed, uint32_t depth, const double* albedo,
+                     const double* lamp, const double* H, uint32_t nNodes, const uint32_t* triNode, uint32_t y0, uint32_t y1, int fp64,
+                     int threads, double* out) {
+  Scene* S = static_cast<Scene*>(h);
+  const vt_camera_desc& cam = S->cams[camera];
+  uint32_t skip = 0;
+  for (size_t i = 0; i < S->blas.size(); i++) if (S->blas[i].owner == int(camera)) skip |= 1u << i;
+  CalibIn C{albedo, lamp, H, nNodes, triNode, S->staticTris};
+  const uint32_t w = cam.width;
+  std::atomic<uint32_t> next(y0);
+  std::vector<Dbg> dbgs(std::max(1, threads));
+  auto work = [&](int t) {
+    auto run = [&](auto tag) {
+      using R = decltype(tag);
+      Tracer<R> tr(*S, dbgs[t]);
+      Shader<R> sh(tr);
+      for (;;) {
+        uint32_t y = next.fetch_add(1);
+        if (y >= y1) break;
+        for (uint32_t x = 0; x < w; x++) calib_pixel<R>(tr, sh, C, cam, camera, spp, nl, seed, depth, x, y, skip, out + (size_t(y - y0) * w + x) * 3);
+      }
+    };
+    if (fp64) run(double(0)); else run(float(0));
+  };
+  if (threads <= 1) work(0);
+  else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; t++) th.emplace_back(work, t);
+    for (auto& x : th) x.join();
+  }
+}
+
+void or_direct_transfer(void* h, const float* C, const float* N, uint32_t n, uint32_t samples, int fp64, int threads, double* D) {
+  Scene* S = static_cast<Scene*>(h);
+  std::atomic<uint32_t> next(0);
+  std::vector<Dbg> dbgs(std::max(1, threads));
+  auto work = [&](int t) {
+    auto run = [&](auto tag) {
+      using R = decltype(tag);
+      Tracer<R> tr(*S, dbgs[t]);
+      Shader<R> sh(tr);
+      for (;;) {
+        uint32_t i = next.fetch_add(16);
+        if (i >= n) break;
+        direct_transfer<R>(tr, sh, C, N, i, std::min(n, i + 16), samples, D);
+      }
+    };
+    if (fp64) run(double(0)); else run(float(0));
+  };
+  if (threads <= 1) work(0);
+  else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; t++) th.emplace_back(work, t);
+    for (auto& x : th) x.join();
+  }
+}
+uint32_t or_scene_emit_count(void* h) { return static_cast<Scene*>(h)->emitN; }
 
 void or_sensor_expose(const uint32_t* su, const float* E4, float* raw) { sensor_expose(su, E4, raw); }
 void or_vt_logf(const float* x, int n, float* out) { for (int i = 0; i < n; i++) out[i] = vt_logf(x[i]); }

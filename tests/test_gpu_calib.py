@@ -1,0 +1,213 @@
+"""Differentiable calibration: the forward render against the FP64 oracle, the emitter transfer D against the
+oracle, the path-replay + transposed-Jacobi gradient against central finite differences (h = 1e-4 relative) on the
+GPU and against the FP64 oracle's finite differences, and the analytic KB4 reprojection Jacobian."""
+import numpy as np
+import pytest
+
+import oracle as O
+from vtwin import dome
+from vtwin.renderer import TwinRenderer
+
+pytestmark = pytest.mark.gpu
+
+W, H = 96, 60
+
+
+@pytest.fixture(scope="module")
+def rig():
+    sc = dome.make_dome_scene(seed=1, width=W, height=H, level=3)
+    # the tracking cameras' poses and distortion, at the C0 camera's field of view (fx = 300 at 640 px): at this small
+    # size the configs' fx would put the image edge past 90 degrees, where 8 float32 Newton steps of the KB4 inverse
+    # (gpu/wgsl/lens.wgsl.js:24) and the FP64 oracle's part ways
+    # a third camera at 320 x 200 for the FP64 check: with more samples the few sub-samples whose shadow decision
+    # flips between float32 and float64 weigh less in the gradient. Its drawn distortion turns back (d theta_d /
+    # d theta < 0) inside the image, where the KB4 inverse has no solution and Newton's steps diverge differently in
+    # float32 and float64, so it takes the second camera's distortion.
+    sc["cameras"] = dome.batched_cameras(seed=3, n=2, width=W, height=H) + dome.batched_cameras(seed=3, n=3, width=320, height=200)[2:]
+    sc["cameras"][2]["k"] = list(sc["cameras"][1]["k"])
+    for cam in sc["cameras"]:
+        cam["fx"] = cam["fy"] = 300.0 * cam["size"][0] / 640.0
+    r = TwinRenderer.create(sc)
+    info = r.calib_setup(n_nodes=384, lamp_samples=8)
+    truth_alb = np.array([m["rho"] for m in sc["materials"]], np.float64)
+    truth_alb = np.clip(truth_alb, 0.05, 1.0)
+    truth_lamp = np.full(info["n_lamps"], 50.0)
+    rng = np.random.default_rng(7)
+    truth_lamp *= 1.0 + 0.2 * (rng.random(info["n_lamps"]) - 0.5)
+    _, targets = r.calib_forward([0, 1, 2], truth_alb, truth_lamp, spp=4, max_depth=3)
+    yield r, sc, info, truth_alb, truth_lamp, targets
+    r.destroy()
+
+
+def f32(x):
+    return np.asarray(x, np.float32).astype(np.float64)
+
+
+def test_forward_matches_fp64_oracle(rig):
+    r, sc, info, alb, lamp, _ = rig
+    alb, lamp = f32(alb), f32(lamp)
+    _, imgs = r.calib_forward([0, 1], alb, lamp, spp=4, max_depth=3)
+    ex = r.calib_export(with_F=True)
+    Hn, _ = O.calib_radiosity(ex["F"], ex["D"], lamp, alb, ex["node_mat"])
+    S = O.Scene(sc)
+    S.set_poses()
+    for c in range(2):
+        ref = S.calib_render(c, alb, lamp, Hn, ex["tri_node"], spp=4, depth=3, fp64=True, threads=8)
+        got = imgs[c][..., :3].astype(np.float64)
+        rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-3 * np.abs(ref).max())
+        print(f"\ncamera {c}: median rel {np.median(rel):.2e}, within 1e-4 {np.mean(rel <= 1e-4):.4f}, mean {got.mean():.5f} vs {ref.mean():.5f}")
+        assert np.median(rel) <= 1e-5
+        assert np.mean(rel <= 1e-4) >= 0.97
+        assert abs(got.mean() - ref.mean()) <= 1e-4 * ref.mean()
+
+
+def test_direct_transfer_matches_oracle(rig):
+    r, sc, info, *_ = rig
+    ex = r.calib_export()
+    S = O.Scene(sc)
+    S.set_poses()
+    D = S.direct_transfer(ex["centres"], ex["normals"], samples=8, fp64=True, threads=8)
+    rel = np.abs(ex["D"] - D) / max(D.max(), 1e-30)
+    print(f"\nD: max |diff| / max D {rel.max():.2e}, entries {D.size}, nonzero {np.count_nonzero(D)}")
+    assert np.count_nonzero(D) > 0.2 * D.size
+    assert np.mean(rel <= 1e-5) >= 0.99
+    assert abs(ex["D"].sum() - D.sum()) <= 1e-3 * D.sum()
+
+
+def fd_grad(r, params, which, idx, targets, h=1e-4, **kw):
+    """Central differences of the image loss in parameter (which, idx), FP64 loss reduction, with the denominator
+    taken from the float32-rounded parameters the device sees."""
+    alb, lamp = params
+    vals = []
+    for s in (+1, -1):
+        a, l = alb.copy(), lamp.copy()
+        if which == "albedo":
+            a.flat[idx] = np.float32(a.flat[idx] * (1 + s * h))
+            x = a.flat[idx]
+        else:
+            l[idx] = np.float32(l[idx] * (1 + s * h))
+            x = l[idx]
+        loss, _ = r.calib_forward([0, 1], a, l, targets=targets[:2], images=False, **kw)
+        vals.append((loss, x))
+    return (vals[0][0] - vals[1][0]) / (vals[0][1] - vals[1][1])
+
+
+def test_adjoint_matches_central_differences(rig):
+    """Central differences of the GPU's own loss (FP32 render, FP64 node radiosity and loss reduction). Every albedo
+    reaches every pixel through the node radiosity, so each perturbation re-rounds every float32 pixel: the noise of a
+    difference is ~1e-6 / h of the derivative's scale. h = 3e-3 balances it against the truncation error (the loss is
+    a low-degree polynomial in each parameter); the FP64 check below uses h = 1e-4."""
+    r, sc, info, t_alb, t_lamp, targets = rig
+    rng = np.random.default_rng(3)
+    alb = f32(np.clip(t_alb * (1 + 0.1 * (2 * rng.random(t_alb.shape) - 1)), 0.01, 1.0))
+    lamp = f32(t_lamp * (1 + 0.1 * (2 * rng.random(t_lamp.shape) - 1)))
+    kw = dict(spp=4, max_depth=3)
+    r.calib_forward([0, 1], alb, lamp, targets=targets[:2], images=False, **kw)
+    ga, gl = r.calib_backward()
+    for name, g, ids in (("albedo", ga.ravel(), range(24)), ("lamp", gl, np.linspace(0, info["n_lamps"] - 1, 12).astype(int))):
+        G = np.array([g[i] for i in ids])
+        FD = np.array([fd_grad(r, (alb, lamp), name, int(i), targets, h=3e-3, **kw) for i in ids])
+        vec = np.linalg.norm(G - FD) / np.linalg.norm(FD)
+        comp = np.max(np.abs(G - FD) / np.maximum(np.abs(FD), 1e-2 * np.abs(FD).max()))
+        print(f"\n{name}: {len(ids)} entries, vector relative error {vec:.2e}, worst entry {comp:.2e}")
+        assert vec <= 1e-3 and comp <= 5e-3
+
+
+def test_adjoint_matches_fp64_oracle_fd(rig):
+    """The FP64 CPU reference gradient: central differences of the oracle's FP64 image loss (FP64 radiosity solve,
+    FP64 estimator) on a 320 x 200 camera, against the GPU adjoint of the same loss."""
+    r, sc, info, t_alb, t_lamp, targets = rig
+    alb = f32(np.clip(t_alb * 1.07, 0.01, 1.0))
+    lamp = f32(t_lamp * 0.93)
+    kw = dict(spp=4, max_depth=3)
+    r.calib_forward([2], alb, lamp, targets=[targets[2]], images=False, **kw)
+    ga, gl = r.calib_backward()
+    ex = r.calib_export(with_F=True)
+    S = O.Scene(sc)
+    S.set_poses()
+    T2 = targets[2][..., :3].astype(np.float64)
+
+    def loss64(a, l):
+        Hn, _ = O.calib_radiosity(ex["F"], ex["D"], l, a, ex["node_mat"])
+        img = S.calib_render(2, a, l, Hn, ex["tri_node"], spp=4, depth=3, fp64=True, threads=16)
+        return np.mean((img - T2) ** 2)
+
+    h = 1e-4
+    cases = [("albedo", (m, m % 3)) for m in range(8)] + [("lamp", t) for t in (0, 5, 31, 60, 77, 95)]
+    G, FD = [], []
+    for which, idx in cases:
+        a, l = alb.copy(), lamp.copy()
+        if which == "albedo":
+            x = a[idx]
+            a[idx] = x * (1 + h); lp = loss64(a, l)
+            a[idx] = x * (1 - h); lm = loss64(a, l)
+            fd, g = (lp - lm) / (2 * h * x), ga[idx]
+        else:
+            x = l[idx]
+            l[idx] = x * (1 + h); lp = loss64(a, l)
+            l[idx] = x * (1 - h); lm = loss64(a, l)
+            fd, g = (lp - lm) / (2 * h * x), gl[idx]
+        err = abs(g - fd) / max(abs(fd), 1e-12)
+        print(f"\n{which} {idx}: adjoint {g:.6e} FP64 FD {fd:.6e} rel {err:.1e}")
+        G.append(g)
+        FD.append(fd)
+        assert err <= 3e-3
+    G, FD = np.array(G), np.array(FD)
+    # per group (albedo, lamp): the gradient vector's relative error (the float32 estimator and the FP64 oracle take
+    # different shadow decisions on ~2% of sub-samples, which moves single small entries by ~1e-3)
+    for sl in (slice(0, 8), slice(8, None)):
+        vec = np.linalg.norm(G[sl] - FD[sl]) / np.linalg.norm(FD[sl])
+        print(f"vector relative error {vec:.2e}")
+        assert vec <= 1e-3
+
+
+def test_reprojection_jacobian(rig):
+    r, sc, *_ = rig
+    rng = np.random.default_rng(11)
+    pts = dome.fib_hemisphere(200, 3.9)[0]
+    K0 = [r.get_intrinsics(c) for c in (0, 1)]
+    uv_t = np.zeros((2, 200, 2))
+    for c in (0, 1):
+        Kt = K0[c] * (1 + 0.01 * (rng.random(8) - 0.5))
+        r.set_intrinsics(c, Kt)
+        uv_t[c] = r.project(c, pts)
+        r.set_intrinsics(c, K0[c])
+    loss, g = r.reproj_loss([0, 1], pts, uv_t)
+    assert loss > 0
+    for c in (0, 1):
+        for k in range(8):
+            h = 1e-6 * max(1.0, abs(K0[c][k]))
+            Kp, Km = K0[c].copy(), K0[c].copy()
+            Kp[k] += h
+            Km[k] -= h
+            r.set_intrinsics(c, Kp)
+            lp, _ = r.reproj_loss([0, 1], pts, uv_t)
+            r.set_intrinsics(c, Km)
+            lm, _ = r.reproj_loss([0, 1], pts, uv_t)
+            r.set_intrinsics(c, K0[c])
+            fd = (lp - lm) / (2 * h)
+            assert abs(g[c, k] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max()), (c, k, g[c, k], fd)
+
+
+def test_descent_recovers_parameters(rig):
+    """A few Adam steps on albedo and lamp radiance from a 10% perturbation reduce the image loss by 10x."""
+    r, sc, info, t_alb, t_lamp, targets = rig
+    rng = np.random.default_rng(5)
+    alb = np.clip(t_alb * (1 + 0.1 * (2 * rng.random(t_alb.shape) - 1)), 0.01, 1.0)
+    lamp = t_lamp * (1 + 0.1 * (2 * rng.random(t_lamp.shape) - 1))
+    x = np.concatenate([alb.ravel(), lamp / 50.0])
+    m = np.zeros_like(x)
+    v = np.zeros_like(x)
+    first = None
+    for it in range(1, 61):
+        a = np.clip(x[:alb.size].reshape(alb.shape), 0.01, 1.0)
+        l = np.maximum(x[alb.size:] * 50.0, 0.0)
+        loss, _ = r.calib_forward([0, 1], a, l, targets=targets[:2], images=False, spp=4, max_depth=3)
+        first = loss if first is None else first
+        ga, gl = r.calib_backward()
+        g = np.concatenate([ga.ravel(), gl * 50.0])
+        m = 0.9 * m + 0.1 * g
+        v = 0.999 * v + 0.001 * g * g
+        x = x - 0.01 * (m / (1 - 0.9 ** it)) / (np.sqrt(v / (1 - 0.999 ** it)) + 1e-12)
+    print(f"\nloss {first:.3e} -> {loss:.3e}")
+    assert loss < 0.1 * first

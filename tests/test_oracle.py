@@ -231,3 +231,29 @@ def test_form_factor_reciprocity_before_scaling():
     # the disk approximation is reciprocal up to its A_j in the denominator
     big = lhs > 1e-6
     assert np.median(np.abs(lhs[big] - rhs[big]) / lhs[big]) < 0.05
+
+
+def test_calibration_estimator_is_linear_in_emission():
+    """The calibration estimator is linear in the emitter radiances jointly with the node irradiance H (and exactly
+    so when both double), and polynomial in the albedos: the FP64 restatement checked on a 24 x 16 view."""
+    sc = dome.make_dome_scene(seed=1, width=24, height=16, level=2)
+    S = O.Scene(sc)
+    S.set_poses()
+    n_static = len(sc["static"]["I"])
+    n_nodes = 64
+    tri_node = (np.arange(n_static, dtype=np.uint64) * n_nodes // n_static).astype(np.uint32)
+    alb = np.clip(np.array([m["rho"] for m in sc["materials"]], np.float64), 0.05, 1.0)
+    lamp = np.full(S.emit_n, 50.0)
+    rng = np.random.default_rng(1)
+    Hn = rng.random((3, n_nodes)) * 5.0
+    a = S.calib_render(0, alb, lamp, Hn, tri_node, spp=2, depth=3)
+    b = S.calib_render(0, alb, 2 * lamp, 2 * Hn, tri_node, spp=2, depth=3)
+    assert a.max() > 0 and np.array_equal(b, 2 * a)
+    # emission and node light add: I(L, H) = I(L, 0) + I(0, H)
+    c = S.calib_render(0, alb, lamp, 0 * Hn, tri_node, spp=2, depth=3)
+    d = S.calib_render(0, alb, 0 * lamp, Hn, tri_node, spp=2, depth=3)
+    np.testing.assert_allclose(a, c + d, rtol=1e-12, atol=1e-12)
+    # depth 1 sees no albedo of its own vertex beyond the first factor: doubling every albedo at most doubles
+    e = S.calib_render(0, np.minimum(alb * 2, 1.0), lamp, 0 * Hn, tri_node, spp=2, depth=1)
+    f = S.calib_render(0, alb, lamp, 0 * Hn, tri_node, spp=2, depth=1)
+    assert np.all(e <= 2 * f + 1e-12)

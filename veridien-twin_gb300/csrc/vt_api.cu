@@ -103,6 +103,9 @@ vt_status vt_destroy(vt_ctx* ctx) {
   cudaFree(ctx->batch.su); cudaFree(ctx->batch.cull); cudaFree(ctx->batch.ctr); cudaFree(ctx->batch.sensor); cudaFree(ctx->batch.mem);
   cudaFree(ctx->batch.rad); cudaFree(ctx->batch.raw);
   if (ctx->batch.exec) cudaGraphExecDestroy(ctx->batch.exec);
+  cudaFree(ctx->calib.mem);
+  for (float4* p : ctx->calib.image) cudaFree(p);
+  for (float4* p : ctx->calib.target) cudaFree(p);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->ev2) cudaEventDestroy(ctx->ev2);

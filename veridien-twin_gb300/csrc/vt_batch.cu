@@ -20,6 +20,7 @@
 #include <algorithm>
 
 #include "vt_batch.cuh"
+#include "vt_camera.cuh"
 #include "vt_sensor.cuh"
 
 namespace vtk {
@@ -28,16 +29,6 @@ using namespace vtd;
 namespace {
 constexpr int T = 256;
 constexpr int SCAN = 1024;   // paths per scan block
-
-// pixel id (tiled order) -> x, y; identical to the wavefront's enumeration
-__device__ __forceinline__ bool pix_xy(const CamParams& cp, uint32_t id, uint32_t& x, uint32_t& y) {
-  const uint32_t tw = cp.tile_w, th = cp.tile_h;
-  const uint32_t tiles_x = (cp.w + tw - 1) / tw;
-  const uint32_t tile = id / (tw * th), within = id % (tw * th);
-  x = (tile % tiles_x) * tw + within % tw;
-  y = (tile / tiles_x) * th + within / tw;
-  return x < cp.w && y < cp.h;
-}
 
 // in-order sum of a pixel's sub-samples and its key, as wave_finalize computes it over a whole frame
 struct PixSum {
@@ -60,7 +51,7 @@ __global__ void __launch_bounds__(T) finalize_shared_kernel(const CamParams cp, 
                                                            uint32_t px0, uint32_t n_pw, float4* __restrict__ pix, uint64_t* __restrict__ pixmask) {
   for (uint32_t lp = blockIdx.x * blockDim.x + threadIdx.x; lp < n_pw; lp += gridDim.x * blockDim.x) {
     uint32_t x, y;
-    if (!pix_xy(cp, px0 + lp, x, y)) { pixmask[lp] = 0ull; continue; }
+    if (!pixel_xy(cp, px0 + lp, x, y)) { pixmask[lp] = 0ull; continue; }
     PixSum ps;
     uint64_t m = 0ull;
     for (uint32_t i = 0; i < cp.spp; i++) {
@@ -154,7 +145,7 @@ __global__ void __launch_bounds__(T) finalize_poses_kernel(const CamParams cp, B
   for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
     const uint32_t q = uint32_t(t / n_pw), lp = uint32_t(t % n_pw);
     uint32_t x, y;
-    if (!pix_xy(cp, px0 + lp, x, y)) continue;
+    if (!pixel_xy(cp, px0 + lp, x, y)) continue;
     float4 val;
     if (!((v.pixmask[lp] >> q) & 1ull)) {
       val = v.pix[lp];

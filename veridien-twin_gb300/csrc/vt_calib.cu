@@ -1,0 +1,417 @@
+// Differentiable calibration render on sm_103a. The reference has no differentiation (only the analytic dtheta_d /
+// dtheta of gpu/lens.js:25); this is the project's own estimator, built from the twin's pieces so that its gradient
+// with respect to material albedos and emitter radiances can be computed by path replay.
+//
+// Estimator (per camera sub-sample, the KB4 ray and sample numbers of the path tracer, gpu/wgsl/kernels.wgsl.js
+// :34-53): up to D vertices on Lambertian surfaces (f = rho / pi). At every vertex, nL emitter samples (area CDF,
+// power-heuristic MIS against cosine sampling, gpu/wgsl/shade.wgsl.js:135 lightEval); between vertices, cosine-
+// weighted continuation, so the throughput gains exactly rho per bounce; at vertex D, the light the node radiosity
+// carries: rho / pi x H(node), H = F B the irradiance from the other nodes. An emitter hit adds its radiance
+// (MIS-weighted after the first vertex). Nothing in the sampling depends on the parameters, so the estimator is a
+// polynomial in the albedos, linear in the emitter radiances and in H, and its derivative is exact by replay:
+// the same path is traced again from the same sample numbers, and each term's derivative is accumulated (FP64).
+//
+// The forward and the backward run the same kernel code for the path (one kernel, a uniform `backward` flag), so
+// the replayed path is bit-identical to the one the forward rendered.
+#include <utility>
+
+#include "vt_calib.cuh"
+#include "vt_camera.cuh"
+
+namespace vtk {
+using namespace vtd;
+
+namespace {
+constexpr int CT = 128;
+
+struct CalVertex {
+  uint32_t mat;
+  uint32_t lamp[CAL_MAX_NL];
+  float q[CAL_MAX_NL];   // contribution per unit emitter radiance, per unit albedo (0: no contribution)
+};
+struct CalPath {
+  uint32_t n;            // shading vertices
+  CalVertex v[CAL_MAX_DEPTH];
+  uint32_t emit_lamp;    // emitter hit after the n shading vertices (~0: none)
+  float emit_a;          // its MIS weight x profile
+  uint32_t node;         // node term at the last shading vertex (~0: none)
+};
+
+// emitter sample by the area CDF, with the index of the triangle (gpu/wgsl/shade.wgsl.js:31)
+__device__ __forceinline__ uint32_t sample_emitter_idx(const Scene& S, float3 u, float time, float3& p, float3& n, float3& axis) {
+  uint32_t lo = 0, hi = S.emit_n - 1u;
+  for (uint32_t it = 0; it < 40u && lo < hi; it++) {
+    const uint32_t m = (lo + hi) >> 1;
+    if (__ldg(S.params + S.emit_off + 4u * m).w < u.x) lo = m + 1u; else hi = m;
+  }
+  const float4* e = S.params + S.emit_off + 4u * lo;
+  const float3 v0 = xyz(__ldg(e)), e1 = xyz(__ldg(e + 1)), e2 = xyz(__ldg(e + 2)), nl = xyz(__ldg(e + 3));
+  const float su = sqrtf(u.y);
+  const float3 pl = v0 + e1 * (su * (1.0f - u.z)) + e2 * (su * u.z);
+  Rot R;
+  float3 pp;
+  inst_pose(S, ldu(S.su + 17), time, R, pp);
+  p = rmul(R, pl) + pp;
+  n = rmul(R, nl);
+  axis = rmul(R, ld3(S.su + 4));
+  return lo;
+}
+
+__device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, const CalibDev& C, uint32_t id, uint32_t i, CalPath& P) {
+  P.n = 0;
+  P.emit_lamp = MISS;
+  P.emit_a = 0.0f;
+  P.node = MISS;
+  float4 o4, d4;
+  uint32_t hs;
+  if (!camera_path(cp, id, i, o4, d4, hs)) return;
+  float3 o = xyz(o4), d = xyz(d4);
+  const float tt = o4.w;
+  const uint32_t nl = cp.n_light;
+  const float fnl = float(nl);
+  const float area = __ldg(S.su + 3);
+  const uint32_t skip_sh = ldu(S.su + 7);
+  float pb_prev = 0.0f;
+  for (uint32_t b = 1; b <= cp.max_depth; b++) {
+    const Hit h = trace_scene<false>(S, cp.root, o, d, 0.0f, BIG, tt, 3u, b == 1 ? cp.skip : 0u);
+    if (h.tri == MISS) return;
+    const Surf s = surface(S, h, o, d, tt);
+    if (s.flags & VT_F_EMITTER) {
+      const float3 nE = emitter_normal(S, h, s, tt);
+      const float cosE = dot(-d, nE);
+      if (cosE > 0.0f) {
+        const float prof = profile(S, acosf(clampf(dot(-d, emitter_axis_at(S, tt)), -1.0f, 1.0f)));
+        float w = 1.0f;
+        if (b > 1) {
+          const float pL = h.t * h.t / (cosE * area);
+          w = pb_prev * pb_prev / (pb_prev * pb_prev + fnl * fnl * pL * pL);
+        }
+        P.emit_lamp = __ldg(C.emit_of_tri + h.tri);
+        P.emit_a = w * prof;
+      }
+      return;
+    }
+    CalVertex& V = P.v[P.n];
+    V.mat = s.mat;
+    P.n++;
+    const float3 n = s.ns, wo = -d;
+    const float sh0 = b == 1 ? u01(pcg(hs + 3u)) : bounce_shift(hs, b, 0);
+    const float sh1 = b == 1 ? u01(pcg(hs + 4u)) : bounce_shift(hs, b, 1);
+    const float sh2 = b == 1 ? u01(pcg(hs + 5u)) : bounce_shift(hs, b, 2);
+    for (uint32_t j = 0; j < nl; j++) {
+      const float3 u = f3(kr(i * nl + j, KL0, sh0), kr(i * nl + j, KL1, sh1), kr(i * nl + j, KL2, sh2));
+      float3 lp, ln, la;
+      V.lamp[j] = sample_emitter_idx(S, u, tt, lp, ln, la);
+      V.q[j] = 0.0f;
+      float3 wi = lp - s.p;
+      const float d2 = dot(wi, wi), dist = sqrtf(d2);
+      wi = wi / dist;
+      const float cosE = dot(-wi, ln), cosS = dot(n, wi);
+      if (cosE <= 0.0f || cosS <= 0.0f || dot(s.ng, wi) <= 0.0f || dot(n, wo) <= 0.0f) continue;
+      const float prof = profile(S, acosf(clampf(dot(-wi, la), -1.0f, 1.0f)));
+      if (prof <= 0.0f) continue;
+      const float pdfW = d2 / (cosE * area), pb = cosS * INV_PI_F;
+      const float w = fnl * fnl * pdfW * pdfW / (fnl * fnl * pdfW * pdfW + pb * pb);
+      const Hit sh = trace_scene<true>(S, cp.root, offset_ray(s.p, s.ng, wi), wi, 0.0f, dist - 2e-5f, tt, 3u, skip_sh);
+      if (sh.tri == MISS) V.q[j] = prof * cosS * w * INV_PI_F / pdfW;
+    }
+    if (b == cp.max_depth) {
+      if (h.inst == MISS && h.tri < C.n_static_tris) P.node = __ldg(C.tri_node + h.tri);
+      return;
+    }
+    if (dot(n, wo) <= 0.0f) return;
+    const float u1 = b == 1 ? kr(i, KB1, u01(pcg(hs + 7u))) : kr(i, KB1, bounce_shift(hs, b, 4));
+    const float u2 = b == 1 ? kr(i, KB2, u01(pcg(hs + 8u))) : kr(i, KB2, bounce_shift(hs, b, 5));
+    const float3 t = basis_t(n), bb = basis_b(n);
+    const float r = sqrtf(u1);
+    float sp, cpz;
+    sincosf(2.0f * PI_F * u2, &sp, &cpz);
+    const float3 l = t * (r * cpz) + bb * (r * sp) + n * sqrtf(fmaxf(0.0f, 1.0f - u1));
+    const float cl = dot(n, l);
+    if (cl <= 0.0f || dot(s.ng, l) <= 0.0f) return;
+    pb_prev = cl * INV_PI_F;
+    o = offset_ray(s.p, s.ng, l);
+    d = l;
+  }
+}
+
+__device__ __forceinline__ float3 alb(const CalibDev& C, uint32_t m) { return f3(__ldg(C.albedo + 3 * m), __ldg(C.albedo + 3 * m + 1), __ldg(C.albedo + 3 * m + 2)); }
+
+// radiance of a recorded path
+__device__ __forceinline__ float3 path_value(const CalibDev& C, const CalPath& P, uint32_t nl) {
+  float3 L = f3(0, 0, 0), T = f3(1, 1, 1);
+  for (uint32_t k = 0; k < P.n; k++) {
+    const float3 rho = alb(C, P.v[k].mat);
+    float s = 0.0f;
+    for (uint32_t j = 0; j < nl; j++) if (P.v[k].q[j] != 0.0f) s += __ldg(C.lamp + P.v[k].lamp[j]) * P.v[k].q[j];
+    const float3 Tr = T * rho;
+    L = L + Tr * (s / float(nl));
+    if (k + 1 == P.n && P.node != MISS) {
+      const float3 Hn = f3(__ldg(C.H + P.node), __ldg(C.H + C.n_nodes + P.node), __ldg(C.H + 2 * C.n_nodes + P.node));
+      L = L + Tr * Hn * INV_PI_F;
+    }
+    T = Tr;
+  }
+  if (P.emit_lamp != MISS) L = L + T * (P.emit_a * __ldg(C.lamp + P.emit_lamp));
+  return L;
+}
+
+// d loss / d parameters of one recorded path, given g = d loss / d (path radiance); FP64 into shared accumulators
+__device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, uint32_t nl, double3 g, double* sh_alb, double* sh_lamp) {
+  double Tp[CAL_MAX_DEPTH + 1][3];
+  Tp[0][0] = Tp[0][1] = Tp[0][2] = 1.0;
+  for (uint32_t k = 0; k < P.n; k++) {
+    const float3 r = alb(C, P.v[k].mat);
+    Tp[k + 1][0] = Tp[k][0] * r.x; Tp[k + 1][1] = Tp[k][1] * r.y; Tp[k + 1][2] = Tp[k][2] * r.z;
+  }
+  // a term of value val (per channel) that carries the albedos of shading vertices 0..last
+  auto add_albedo = [&](const double val[3], uint32_t last) {
+    for (uint32_t l = 0; l <= last; l++) {
+      const uint32_t m = P.v[l].mat;
+      const float3 r = alb(C, m);
+      atomicAdd(sh_alb + 3 * m, g.x * val[0] / double(r.x));
+      atomicAdd(sh_alb + 3 * m + 1, g.y * val[1] / double(r.y));
+      atomicAdd(sh_alb + 3 * m + 2, g.z * val[2] / double(r.z));
+    }
+  };
+  for (uint32_t k = 0; k < P.n; k++) {
+    double s = 0.0;
+    for (uint32_t j = 0; j < nl; j++) {
+      const float q = P.v[k].q[j];
+      if (q == 0.0f) continue;
+      const double dl = (g.x * Tp[k + 1][0] + g.y * Tp[k + 1][1] + g.z * Tp[k + 1][2]) * double(q) / double(nl);
+      atomicAdd(sh_lamp + P.v[k].lamp[j], dl);
+      s += double(__ldg(C.lamp + P.v[k].lamp[j])) * double(q);
+    }
+    if (s != 0.0) {
+      const double val[3] = {Tp[k + 1][0] * s / nl, Tp[k + 1][1] * s / nl, Tp[k + 1][2] * s / nl};
+      add_albedo(val, k);
+    }
+    if (k + 1 == P.n && P.node != MISS) {
+      const double hx = __ldg(C.H + P.node), hy = __ldg(C.H + C.n_nodes + P.node), hz = __ldg(C.H + 2 * C.n_nodes + P.node);
+      const double ip = 1.0 / 3.14159265358979323846;
+      atomicAdd(C.g_H + P.node, g.x * Tp[k + 1][0] * ip);
+      atomicAdd(C.g_H + C.n_nodes + P.node, g.y * Tp[k + 1][1] * ip);
+      atomicAdd(C.g_H + 2 * C.n_nodes + P.node, g.z * Tp[k + 1][2] * ip);
+      const double val[3] = {Tp[k + 1][0] * hx * ip, Tp[k + 1][1] * hy * ip, Tp[k + 1][2] * hz * ip};
+      add_albedo(val, k);
+    }
+  }
+  if (P.emit_lamp != MISS && P.emit_a != 0.0f) {
+    const double a = P.emit_a;
+    atomicAdd(sh_lamp + P.emit_lamp, (g.x * Tp[P.n][0] + g.y * Tp[P.n][1] + g.z * Tp[P.n][2]) * a);
+    if (P.n) {
+      const double Le = a * double(__ldg(C.lamp + P.emit_lamp));
+      const double val[3] = {Tp[P.n][0] * Le, Tp[P.n][1] * Le, Tp[P.n][2] * Le};
+      add_albedo(val, P.n - 1);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(CT) calib_kernel(const Scene S, const CamParams cp, const CalibDev C, uint32_t n_pix, int backward) {
+  extern __shared__ double sm[];
+  double* sh_alb = sm;                       // n_mat x 3
+  double* sh_lamp = sm + 3 * C.n_mat;        // n_lamps
+  __shared__ double red[CT / 32];
+  if (backward) {
+    for (uint32_t k = threadIdx.x; k < 3 * C.n_mat + C.n_lamps; k += blockDim.x) sm[k] = 0.0;
+    __syncthreads();
+  }
+  double loss = 0.0;
+  const float sc = cp.scale / float(cp.spp);
+  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n_pix; id += gridDim.x * blockDim.x) {
+    uint32_t x, y;
+    if (!pixel_xy(cp, id, x, y)) continue;
+    const size_t px = size_t(y) * cp.w + x;
+    double3 g = make_double3(0.0, 0.0, 0.0);
+    if (backward) {
+      const float4 I = C.image[px], Tg = C.target ? C.target[px] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const double k = 2.0 * C.inv_count * double(sc);
+      g = make_double3(k * (double(I.x) - Tg.x), k * (double(I.y) - Tg.y), k * (double(I.z) - Tg.z));
+    }
+    float3 s = f3(0, 0, 0);
+    for (uint32_t i = 0; i < cp.spp; i++) {
+      CalPath P;
+      calib_path(S, cp, C, id, i, P);
+      if (backward) path_grad(C, P, cp.n_light, g, sh_alb, sh_lamp);
+      else s = s + path_value(C, P, cp.n_light);
+    }
+    if (!backward) {
+      const float4 I = make_float4(s.x * sc, s.y * sc, s.z * sc, 1.0f);
+      C.image[px] = I;
+      if (C.target) {
+        const float4 Tg = C.target[px];
+        const double dx = double(I.x) - Tg.x, dy = double(I.y) - Tg.y, dz = double(I.z) - Tg.z;
+        loss += dx * dx + dy * dy + dz * dz;
+      }
+    }
+  }
+  if (backward) {
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < 3 * C.n_mat; k += blockDim.x) if (sh_alb[k] != 0.0) atomicAdd(C.g_albedo + k, sh_alb[k]);
+    for (uint32_t k = threadIdx.x; k < C.n_lamps; k += blockDim.x) if (sh_lamp[k] != 0.0) atomicAdd(C.g_lamp + k, sh_lamp[k]);
+    return;
+  }
+  for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < CT / 32; w++) t += red[w];
+    C.partials[blockIdx.x] = t * C.inv_count;
+  }
+}
+
+// one thread per (node, emitter triangle): stratified points (Kronecker in the unit square, the sampler's
+// triangle warp), cosines, profile, visibility through the BVH
+__global__ void direct_transfer_kernel(const Scene S, const float* __restrict__ C, const float* __restrict__ N, uint32_t n, uint32_t n_lamps,
+                                       uint32_t samples, float* __restrict__ D) {
+  const size_t total = size_t(n) * n_lamps;
+  const uint32_t skip = ldu(S.su + 7);
+  for (size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x; k < total; k += size_t(gridDim.x) * blockDim.x) {
+    const uint32_t i = uint32_t(k / n_lamps), t = uint32_t(k % n_lamps);
+    const float3 c = f3(C[3 * i], C[3 * i + 1], C[3 * i + 2]), nn = f3(N[3 * i], N[3 * i + 1], N[3 * i + 2]);
+    const float4* e = S.params + S.emit_off + 4u * t;
+    const float3 v0 = xyz(__ldg(e)), e1 = xyz(__ldg(e + 1)), e2 = xyz(__ldg(e + 2)), nl0 = xyz(__ldg(e + 3));
+    const float At = 0.5f * length(cross(e1, e2));
+    Rot R;
+    float3 pp;
+    inst_pose(S, ldu(S.su + 17), 0.5f, R, pp);
+    const float3 nl = rmul(R, nl0), axis = rmul(R, ld3(S.su + 4));
+    const float3 org = c + nn * 1e-4f;
+    float acc = 0.0f;
+    for (uint32_t s = 0; s < samples; s++) {
+      const float u1 = kr(s, R2A, 0.5f), u2 = kr(s, R2B, 0.5f);
+      const float su = sqrtf(u1);
+      const float3 lp = rmul(R, v0 + e1 * (su * (1.0f - u2)) + e2 * (su * u2)) + pp;
+      float3 w = lp - org;
+      const float r2 = dot(w, w), r = sqrtf(r2);
+      w = w / r;
+      const float ci = dot(nn, w), ct = dot(nl, -w);
+      if (ci <= 0.0f || ct <= 0.0f) continue;
+      const float prof = profile(S, acosf(clampf(dot(-w, axis), -1.0f, 1.0f)));
+      if (prof <= 0.0f) continue;
+      const Hit h = trace_scene<true>(S, 0u, org, w, 0.0f, r - 2e-5f, 0.5f, 3u, skip);
+      if (h.tri == MISS) acc += prof * ci * ct / r2;
+    }
+    D[size_t(i) * n_lamps + t] = acc * At / float(samples);
+  }
+}
+
+__global__ void dl_kernel(const float* __restrict__ D, const float* __restrict__ L, uint32_t n, uint32_t n_lamps, float* __restrict__ y) {
+  const uint32_t row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+  if (row >= n) return;
+  float a = 0.0f;
+  for (uint32_t t = lane; t < n_lamps; t += 32) a = fmaf(D[size_t(row) * n_lamps + t], L[t], a);
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) y[row] = a;
+}
+
+constexpr uint32_t JT_SPLITS = 16, JT_COLS = 256;
+// partial[split][j] = sum over rows i of the split of F[i][j] (g_i + rho_i lam_i)
+__global__ void __launch_bounds__(JT_COLS) jacobi_t_kernel(const float* __restrict__ F, const double* __restrict__ g, const float* __restrict__ rho,
+                                                          const double* __restrict__ lam, uint32_t n, double* __restrict__ part) {
+  __shared__ double w[JT_COLS];
+  const uint32_t j = blockIdx.x * JT_COLS + threadIdx.x;
+  const uint32_t rows = (n + JT_SPLITS - 1) / JT_SPLITS, i0 = blockIdx.y * rows, i1 = min(n, i0 + rows);
+  double a = 0.0;
+  for (uint32_t ib = i0; ib < i1; ib += JT_COLS) {
+    const uint32_t ii = ib + threadIdx.x;
+    w[threadIdx.x] = ii < i1 ? g[ii] + double(rho[ii]) * lam[ii] : 0.0;
+    __syncthreads();
+    const uint32_t m = min(JT_COLS, i1 - ib);
+    if (j < n)
+      for (uint32_t k = 0; k < m; k++) a = fma(double(F[size_t(ib + k) * n + j]), w[k], a);
+    __syncthreads();
+  }
+  if (j < n) part[size_t(blockIdx.y) * n + j] = a;
+}
+__global__ void jacobi_t_combine(const double* __restrict__ part, uint32_t n, double* __restrict__ out) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double a = 0.0;
+  for (uint32_t s = 0; s < JT_SPLITS; s++) a += part[size_t(s) * n + j];
+  out[j] = a;
+}
+
+// B_out = rho o (DL + F B_in) in FP64 (F in FP32), one warp per row; with `H` set, H = F B_in (rounded to FP32) instead
+__global__ void __launch_bounds__(256) radiosity64_kernel(const float* __restrict__ F, const float* __restrict__ rho, const float* __restrict__ DL,
+                                                        const double* __restrict__ Bin, double* __restrict__ Bout, float* __restrict__ H,
+                                                        uint32_t n) {
+  const uint32_t row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+  if (row >= n) return;
+  const float* Fr = F + size_t(row) * n;
+  double a = 0.0;
+  for (uint32_t j = lane; j < n; j += 32) a = fma(double(Fr[j]), Bin[j], a);
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane) return;
+  if (H) H[row] = float(a);
+  else Bout[row] = double(rho[row]) * (double(DL[row]) + a);
+}
+__global__ void radiosity64_init(const float* __restrict__ rho, const float* __restrict__ DL, double* __restrict__ B, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) B[i] = double(rho[i]) * double(DL[i]);
+}
+
+__global__ void mul_kernel(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ y, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a[i] * b[i];
+}
+
+__global__ void sum_kernel(const double* __restrict__ p, uint32_t n, double* __restrict__ out) {
+  __shared__ double s[1024];
+  double a = 0.0;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) a += p[i];
+  s[threadIdx.x] = a;
+  __syncthreads();
+  for (uint32_t o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = s[0];
+}
+}  // namespace
+
+uint32_t launch_calib(const Scene& S, const CamParams& cp, const CalibDev& C, bool backward, int blocks, cudaStream_t st) {
+  const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
+  const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
+  const size_t smem = backward ? size_t(3 * C.n_mat + C.n_lamps) * 8 : 0;
+  calib_kernel<<<grid, CT, smem, st>>>(S, cp, C, n_pix, backward ? 1 : 0);
+  return grid;
+}
+
+void launch_direct_transfer(const Scene& S, const float* centres, const float* normals, uint32_t n, uint32_t n_lamps, uint32_t samples, float* D,
+                            cudaStream_t st) {
+  const size_t total = size_t(n) * n_lamps;
+  const uint32_t grid = uint32_t(std::min<size_t>((total + 127) / 128, 65535));
+  direct_transfer_kernel<<<grid, 128, 0, st>>>(S, centres, normals, n, n_lamps, samples, D);
+}
+
+void launch_dl(const float* D, const float* L, uint32_t n, uint32_t n_lamps, float* y, cudaStream_t st) {
+  dl_kernel<<<(n + 7) / 8, 256, 0, st>>>(D, L, n, n_lamps, y);
+}
+
+size_t jacobi_t_work(uint32_t n) { return size_t(JT_SPLITS) * n * 8; }
+
+void launch_jacobi_t(const float* F, const double* g, const float* rho, const double* lam_in, double* lam_out, uint32_t n, double* work,
+                     cudaStream_t st) {
+  jacobi_t_kernel<<<dim3((n + JT_COLS - 1) / JT_COLS, JT_SPLITS), JT_COLS, 0, st>>>(F, g, rho, lam_in, n, work);
+  jacobi_t_combine<<<(n + 255) / 256, 256, 0, st>>>(work, n, lam_out);
+}
+
+void launch_sum(const double* p, uint32_t n, double* out, cudaStream_t st) { sum_kernel<<<1, 1024, 0, st>>>(p, n, out); }
+
+void launch_mul(const float* a, const float* b, float* y, uint32_t n, cudaStream_t st) { mul_kernel<<<(n + 255) / 256, 256, 0, st>>>(a, b, y, n); }
+
+void launch_radiosity64(const float* F, const float* rho, const float* DL, uint32_t n, uint32_t iters, double* B0, double* B1, float* H,
+                        cudaStream_t st) {
+  radiosity64_init<<<(n + 255) / 256, 256, 0, st>>>(rho, DL, B0, n);
+  double *cur = B0, *nxt = B1;
+  for (uint32_t it = 0; it < iters; it++) {
+    radiosity64_kernel<<<(n + 7) / 8, 256, 0, st>>>(F, rho, DL, cur, nxt, nullptr, n);
+    std::swap(cur, nxt);
+  }
+  radiosity64_kernel<<<(n + 7) / 8, 256, 0, st>>>(F, rho, DL, cur, nullptr, H, n);
+}
+
+}  // namespace vtk

@@ -1,0 +1,48 @@
+// Differentiable calibration render (vt_calib.cu): the forward estimator, its path-replay adjoint, and the node
+// radiosity pieces of the calibration model (direct transfer from the emitter triangles, transposed Jacobi).
+#pragma once
+
+#include "vt_kernels.cuh"
+
+namespace vtk {
+
+constexpr uint32_t CAL_MAX_DEPTH = 4, CAL_MAX_NL = 4;
+
+// parameters, node data and accumulators of one calibration render (device pointers)
+struct CalibDev {
+  const float* albedo;          // n_mat x 3
+  const float* lamp;            // n_lamps: radiance of each emitter triangle
+  const uint32_t* emit_of_tri;  // per triangle slot: emitter index, or ~0
+  const uint32_t* tri_node;     // per static triangle slot: node
+  const float* H;               // 3 x n_nodes (planar): irradiance at the node from the other nodes' radiosity (F B)
+  uint32_t n_static_tris, n_mat, n_lamps, n_nodes;
+  const float4* target;         // this camera's target image, w x h row-major
+  float4* image;                // this camera's image: written by the forward, read by the backward
+  double inv_count;             // 1 / (3 x pixels of all cameras in the loss)
+  double* partials;             // forward: per-block loss sums
+  double* g_albedo;             // backward accumulators (FP64)
+  double* g_lamp;
+  double* g_H;                  // 3 x n_nodes
+};
+
+// forward: image + per-block loss partials (returns the number of partials); backward: gradients of the image loss
+uint32_t launch_calib(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, bool backward, int blocks, cudaStream_t st);
+// D[i][t]: irradiance at node i (centre, normal) from emitter triangle t at unit radiance, with visibility
+void launch_direct_transfer(const vtd::Scene& S, const float* centres, const float* normals, uint32_t n, uint32_t n_lamps,
+                            uint32_t samples, float* D, cudaStream_t st);
+// y = D L (n x n_lamps times n_lamps)
+void launch_dl(const float* D, const float* L, uint32_t n, uint32_t n_lamps, float* y, cudaStream_t st);
+// one transposed Jacobi sweep of the adjoint: lam_out = F^T (g + rho o lam_in), FP64 vectors; work: splits x n doubles
+void launch_jacobi_t(const float* F, const double* g, const float* rho, const double* lam_in, double* lam_out, uint32_t n, double* work,
+                     cudaStream_t st);
+size_t jacobi_t_work(uint32_t n);
+// y = a o b (n floats)
+void launch_mul(const float* a, const float* b, float* y, uint32_t n, cudaStream_t st);
+// the calibration model's node radiosity for one channel: B = rho o (DL + F B) by `iters` Jacobi sweeps from
+// B = rho o DL, in FP64 (F in FP32), then H = F B rounded to FP32; B0, B1: n doubles of work
+void launch_radiosity64(const float* F, const float* rho, const float* DL, uint32_t n, uint32_t iters, double* B0, double* B1, float* H,
+                        cudaStream_t st);
+// sum of n doubles (deterministic order) into out
+void launch_sum(const double* p, uint32_t n, double* out, cudaStream_t st);
+
+}  // namespace vtk

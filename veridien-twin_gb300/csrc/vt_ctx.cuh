@@ -64,6 +64,28 @@ struct vt_ctx {
     // tuned configuration (0: defaults)
     uint32_t wave_paths = 0, tile_w = 0, tile_h = 0;
   } batch;
+  // differentiable calibration: radiosity nodes (clusters of static triangles), F, the emitter transfer D, parameters,
+  // per-camera images and targets, and the last forward's state for the backward
+  struct Calib {
+    bool ready = false, have_forward = false;
+    uint32_t n = 0, n_lamps = 0, n_mat = 0, n_static = 0;
+    std::vector<float> centres, normals, areas, D_host;
+    std::vector<uint32_t> node_mat, tri_node;
+    void* mem = nullptr;            // device arena
+    float *F = nullptr, *D = nullptr, *C = nullptr, *N = nullptr, *A = nullptr;
+    uint32_t *tri_node_d = nullptr, *emit_of_tri_d = nullptr;
+    float *albedo = nullptr, *lamp = nullptr, *rho = nullptr /* 3 x n */, *DL = nullptr, *H = nullptr /* 3 x n */;
+    double *partials = nullptr, *g_alb = nullptr, *g_lamp = nullptr, *g_H = nullptr, *lam0 = nullptr, *lam1 = nullptr,
+           *lam = nullptr /* 3 x n */, *work = nullptr, *loss = nullptr;
+    uint32_t max_partials = 0;
+    std::vector<float4*> image, target;   // per scene camera (device, w x h)
+    std::vector<std::vector<float>> albedo_host;
+    // last forward
+    std::vector<uint32_t> cams;
+    uint32_t spp = 0, nl = 0, seed = 0, depth = 0, iters = 0;
+    double inv_count = 0;
+    std::vector<float> rho_host, lamp_host;
+  } calib;
 };
 
 namespace vtapi {

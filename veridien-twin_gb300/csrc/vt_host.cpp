@@ -405,11 +405,14 @@ Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_sa
   Bvh sb = sah_build(d.static_P, d.static_I, d.n_static_tris, leaf);
   std::vector<Bvh> bb(d.n_bodies);
   std::vector<Emit> emit;
+  std::vector<std::vector<uint32_t>> emit_idx(d.n_bodies);
   for (uint32_t b = 0; b < d.n_bodies; b++) {
     const vt_body_desc& B = d.bodies[b];
     bb[b] = sah_build(B.P, B.I, B.n_tris, leaf);
+    emit_idx[b].assign(B.n_tris, 0xffffffffu);
     for (uint32_t t = 0; t < B.n_tris; t++) {
       if (!(d.meshes[B.tri_mesh[t]].flags & VT_F_EMITTER)) continue;
+      emit_idx[b][t] = uint32_t(emit.size());
       const float* p0 = B.P + 3 * size_t(B.I[3 * t]);
       const float* p1 = B.P + 3 * size_t(B.I[3 * t + 1]);
       const float* p2 = B.P + 3 * size_t(B.I[3 * t + 2]);
@@ -448,6 +451,7 @@ Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_sa
     for (size_t o = 0; o < bb[b].words.size(); o += 8) dst[o + 3] += dst[o + 7] == 0 ? S.bodies[b].root : S.bodies[b].tri_off;
   }
   S.tris.assign(size_t(tris) * 16, 0u);
+  S.emit_of_tri.assign(tris, 0xffffffffu);
   for (uint32_t k = 0; k < d.n_static_tris; k++) {
     const uint32_t t = sb.order[k];
     const uint32_t* tri = d.static_I + 3 * size_t(t);
@@ -464,6 +468,7 @@ Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_sa
       const uint32_t* tri = B.I + 3 * size_t(t);
       const uint32_t mesh = B.tri_mesh[t];
       tri_record(S.tris.data() + size_t(S.bodies[b].tri_off + k) * 16, B.P, tri, tri[0] + vb, tri[1] + vb, tri[2] + vb, mesh, d.meshes[mesh].flags);
+      S.emit_of_tri[S.bodies[b].tri_off + k] = emit_idx[b][t];
     }
     vb += B.n_verts;
   }

@@ -46,6 +46,7 @@ struct Prepared {
   std::vector<uint32_t> nodes, tris, verts;   // 16, 16, 8 words per item
   std::vector<float> params;                  // vec4 array
   std::vector<float> node_area;
+  std::vector<uint32_t> emit_of_tri;          // per triangle slot: index in the emitter table, or ~0
   uint32_t node_count = 0, tri_count = 0, vert_count = 0, static_verts = 0, static_tris = 0;
   uint32_t mesh_off = 0, mat_off = 0, alb_off = 0, prof_off = 0, prof_n = 0, emit_off = 0, emit_n = 0, emit_tris = 0;
   std::vector<BodyRec> bodies;

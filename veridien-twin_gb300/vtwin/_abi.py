@@ -112,6 +112,21 @@ class vt_tune_row(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("ms_per_mpath", C.c_float)]
 
 
+class vt_calib_desc(C.Structure):
+    _fields_ = [("n_nodes", C.c_uint32), ("lamp_samples", C.c_uint32)]
+
+
+class vt_calib_info(C.Structure):
+    _fields_ = [("n_nodes", C.c_uint32), ("n_materials", C.c_uint32), ("n_lamps", C.c_uint32), ("n_static_tris", C.c_uint32)]
+
+
+class vt_calib_req(C.Structure):
+    _fields_ = [("cameras", C.POINTER(C.c_uint32)), ("n_cameras", C.c_uint32), ("spp", C.c_uint32), ("light_samples", C.c_uint32),
+                ("seed", C.c_uint32), ("max_depth", C.c_uint32), ("jacobi_iters", C.c_uint32),
+                ("albedo", C.POINTER(C.c_double)), ("lamp", C.POINTER(C.c_double)), ("targets", C.POINTER(C.c_float)),
+                ("images", C.POINTER(C.c_float))]
+
+
 class vt_solve_req(C.Structure):
     _fields_ = [("n", C.c_uint32), ("n_rhs", C.c_uint32), ("F", f32p), ("rho", f32p), ("E", f32p), ("B", f32p),
                 ("precision", C.c_uint32), ("max_iters", C.c_uint32), ("warm_start", C.c_uint32),

@@ -30,6 +30,14 @@ SIGNATURES = {
     "vt_readback": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t]),
     "vt_sensor_expose": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_sensor_uniform), C.c_void_p, C.c_void_p]),
     "vt_sensor_camera": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_float]),
+    "vt_calib_setup": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_calib_desc), C.POINTER(A.vt_calib_info)]),
+    "vt_calib_export": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_calib_forward": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_calib_req), C.POINTER(C.c_double)]),
+    "vt_calib_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_set_camera_intrinsics": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vt_get_camera_intrinsics": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vt_reproj_loss": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_double),
+                                   C.c_void_p]),
     "vt_render_batch": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_batch_req), C.c_void_p, C.c_void_p, C.POINTER(A.vt_batch_stats)]),
     "vt_batch_autotune": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_batch_req), C.POINTER(A.vt_tune_row), C.c_uint32,
                                       C.POINTER(C.c_uint32), C.POINTER(A.vt_tune_row)]),

@@ -270,6 +270,85 @@ class TwinRenderer:
         tab = [{"wave_paths": r.wave_paths, "tile": (r.tile_w, r.tile_h), "ms_per_mpath": r.ms_per_mpath} for r in rows[:n.value]]
         return {"wave_paths": best.wave_paths, "tile": (best.tile_w, best.tile_h), "ms_per_mpath": best.ms_per_mpath}, tab
 
+    # ------------------------------------------------------------------------------------------- calibration
+    def calib_setup(self, n_nodes=4096, lamp_samples=16) -> dict:
+        """Radiosity nodes (clusters of the static triangles), their form factors F and the emitter transfer D of
+        the differentiable calibration model (include/vtwin.h vt_calib_setup)."""
+        info = A.vt_calib_info()
+        check(self.lib.vt_calib_setup(self._ctx, C.byref(A.vt_calib_desc(n_nodes=int(n_nodes), lamp_samples=int(lamp_samples))),
+                                      C.byref(info)), self._ctx)
+        self.calib_info = {"n_nodes": info.n_nodes, "n_materials": info.n_materials, "n_lamps": info.n_lamps,
+                           "n_static_tris": info.n_static_tris}
+        return self.calib_info
+
+    def calib_export(self, with_F=False) -> dict:
+        i = self.calib_info
+        n, L = i["n_nodes"], i["n_lamps"]
+        out = {"centres": np.zeros((n, 3), np.float32), "normals": np.zeros((n, 3), np.float32), "areas": np.zeros(n, np.float32),
+               "node_mat": np.zeros(n, np.uint32), "tri_node": np.zeros(i["n_static_tris"], np.uint32), "D": np.zeros((n, L), np.float32)}
+        F = np.zeros((n, n), np.float32) if with_F else None
+        check(self.lib.vt_calib_export(self._ctx, _p(out["centres"]), _p(out["normals"]), _p(out["areas"]), _p(out["node_mat"]),
+                                       _p(out["tri_node"]), _p(F) if F is not None else None, _p(out["D"])), self._ctx)
+        if F is not None:
+            out["F"] = F
+        return out
+
+    def calib_forward(self, cameras, albedo, lamp, spp=32, lightSamples=1, seed=0, max_depth=3, jacobi_iters=0, targets=None,
+                      images=True):
+        """Image loss (mean of (I - T)^2 over pixels and channels) of the calibration render; returns (loss, images)
+        with images a list of (h, w, 4) float32 arrays per camera (or None)."""
+        cams = [self._cam(c) for c in cameras]
+        cam_arr = np.ascontiguousarray(cams, np.uint32)
+        alb = np.ascontiguousarray(albedo, np.float64).reshape(-1, 3)
+        lam = np.ascontiguousarray(lamp, np.float64).ravel()
+        sizes = [tuple(self.scene["cameras"][c]["size"]) for c in cams]
+        total = sum(w * h for w, h in sizes)
+        tg = None if targets is None else np.ascontiguousarray(
+            np.concatenate([np.asarray(t, np.float32).reshape(-1, 4) for t in targets]) if isinstance(targets, (list, tuple)) else targets,
+            np.float32)
+        img = np.empty((total, 4), np.float32) if images else None
+        q = A.vt_calib_req(cameras=cam_arr.ctypes.data_as(C.POINTER(C.c_uint32)), n_cameras=len(cams), spp=int(spp),
+                           light_samples=int(lightSamples), seed=int(seed), max_depth=int(max_depth), jacobi_iters=int(jacobi_iters),
+                           albedo=alb.ctypes.data_as(C.POINTER(C.c_double)), lamp=lam.ctypes.data_as(C.POINTER(C.c_double)),
+                           targets=tg.ctypes.data_as(C.POINTER(C.c_float)) if tg is not None else None,
+                           images=img.ctypes.data_as(C.POINTER(C.c_float)) if img is not None else None)
+        loss = C.c_double(0.0)
+        check(self.lib.vt_calib_forward(self._ctx, C.byref(q), C.byref(loss)), self._ctx)
+        out = None
+        if img is not None:
+            out, o = [], 0
+            for w, h in sizes:
+                out.append(img[o:o + w * h].reshape(h, w, 4))
+                o += w * h
+        return loss.value, out
+
+    def calib_backward(self):
+        """Gradient of the last calib_forward's loss: (d/d albedo (n_materials x 3), d/d lamp (n_lamps))."""
+        i = self.calib_info
+        ga = np.zeros((i["n_materials"], 3), np.float64)
+        gl = np.zeros(i["n_lamps"], np.float64)
+        check(self.lib.vt_calib_backward(self._ctx, _p(ga), _p(gl)), self._ctx)
+        return ga, gl
+
+    def set_intrinsics(self, name, K):
+        K = np.ascontiguousarray(K, np.float64)
+        check(self.lib.vt_set_camera_intrinsics(self._ctx, self._cam(name), _p(K)), self._ctx)
+
+    def get_intrinsics(self, name):
+        K = np.zeros(8, np.float64)
+        check(self.lib.vt_get_camera_intrinsics(self._ctx, self._cam(name), _p(K)), self._ctx)
+        return K
+
+    def reproj_loss(self, cameras, pts, uv_target):
+        """Reprojection loss of dome-frame points and its analytic gradient in each camera's KB4 intrinsics."""
+        cams = np.ascontiguousarray([self._cam(c) for c in cameras], np.uint32)
+        P = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        T = np.ascontiguousarray(uv_target, np.float64).reshape(len(cams), len(P), 2)
+        g = np.zeros((len(cams), 8), np.float64)
+        loss = C.c_double(0.0)
+        check(self.lib.vt_reproj_loss(self._ctx, _p(cams), len(cams), _p(P), len(P), _p(T), C.byref(loss), _p(g)), self._ctx)
+        return loss.value, g
+
     # ------------------------------------------------------------------------------------------- queries
     def trace(self, o4, d4, mask=3, any_hit=False, root=0):
         """gpu/wgsl/kernels.wgsl.js:535 traceTest: rays (o.xyz, time), (d.xyz, -) -> (t, tri, inst, u), v."""
