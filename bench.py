@@ -160,6 +160,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-radiosity", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-calib", action="store_true")
     ap.add_argument("--case", default=None, help="render:W:H:SPP or radiosity:N:PREC:SWEEPS (a small profiling case)")
     args = ap.parse_args()
     if args.case:
@@ -252,6 +253,8 @@ def main():
             line["radiosity"] = radiosity_bench(torch, cpu_check=not args.no_cpu_baseline)
         if not args.no_batch:
             line["batched"] = batch_bench(torch, local)
+        if not args.no_calib:
+            line["calibration"] = calib_bench(torch, local)
         print(json.dumps(line))
     r.destroy()
     if dist:
@@ -344,6 +347,90 @@ def batch_bench(torch, device=0):
                                     "how": "vt_set_poses + vt_render_camera + vt_sensor_camera, one view per call"},
             "speedup_vs_plain": value / pv, "clocks": clk.summary(),
             "l2": "working set (path state, 0.9 GB of raw frames) far above L2"}
+
+
+def calib_bench(torch, device=0):
+    """C4: differentiable calibration on the C0 scene with 3 KB4 cameras at 960x600, 32 spp, depth 3, and N = 4096
+    radiosity nodes. Parameters: 10 material albedos (RGB; the 8 dome/floor/table materials carry the loss), 96
+    emitter-triangle radiances, 3 x 8 KB4 intrinsics. Targets rendered at seeded ground truth; start = truth x
+    (1 +- 10%). Loss = pixel L2 + 1e-3 x reprojection of 200 fiducials on the dome (each in the cameras that see it). Forward and backward device
+    times, and the adjoint against central differences (h = 3e-3, FP32 render, FP64 loss reduction) on 8 entries."""
+    from vtwin import dome
+    from vtwin.calibrate import Calibration
+    from vtwin.renderer import TwinRenderer
+
+    W, H, SPP_C, DEPTH_C = 960, 600, 32, 3
+    sc = dome.make_dome_scene(seed=1, width=W, height=H, level=5)
+    sc["cameras"] = dome.batched_cameras(seed=3, n=3, width=W, height=H)
+    r = TwinRenderer.create(sc, device=device)
+    t0 = time.perf_counter()
+    info = r.calib_setup(n_nodes=4096, lamp_samples=16)
+    setup_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    t_alb = np.clip(np.array([m["rho"] for m in sc["materials"]], np.float64), 0.05, 1.0)
+    t_lamp = 50.0 * (1.0 + 0.2 * (rng.random(info["n_lamps"]) - 0.5))
+    cams = [0, 1, 2]
+    _, targets = r.calib_forward(cams, t_alb, t_lamp, spp=SPP_C, max_depth=DEPTH_C)
+    m = dome.Rng(21)
+    pts = []
+    while len(pts) < 200:                       # uniform on the dome (hemisphere r = 4), rejection from the cube
+        p = np.array([m.uniform(-1, 1), m.uniform(-1, 1), m.uniform(0, 1)])
+        if 0.05 < np.linalg.norm(p) <= 1.0:
+            pts.append(4.0 * p / np.linalg.norm(p))
+    pts = np.array(pts)
+    K_true = np.stack([r.get_intrinsics(c) for c in cams])
+    uv_t = np.stack([np.where(r.observed(c, pts, margin=2.0)[:, None], r.project(c, pts), np.nan) for c in cams])
+    cal = Calibration(r, cams, targets, fiducials=pts, uv_targets=uv_t, w_reproj=1e-3, spp=SPP_C, max_depth=DEPTH_C)
+    x_true = cal.pack(t_alb, t_lamp, K_true)
+    x0 = x_true * (1 + 0.1 * (2 * rng.random(x_true.shape) - 1))
+    x0[:3 * info["n_materials"]] = np.clip(x0[:3 * info["n_materials"]], 0.01, 1.0)
+    x0 = np.asarray(np.asarray(x0, np.float32), np.float64)
+    cal.loss_and_grad(x0)                          # warm
+    fw, bw = [], []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        loss0 = cal.forward(x0)
+        b = time.perf_counter()
+        g = cal.backward()
+        c = time.perf_counter()
+        fw.append(b - a)
+        bw.append(c - b)
+    samples = 3 * W * H * SPP_C
+    fms, bms = statistics.median(fw) * 1e3, statistics.median(bw) * 1e3
+    # adjoint vs central differences on 8 entries: 4 albedos, 2 lamps, 2 intrinsics (fx of camera 0, k1 of camera 2)
+    n_alb = 3 * info["n_materials"]
+    ids = [0, 4, 13, 20, n_alb + 7, n_alb + 60, n_alb + info["n_lamps"] + 0, n_alb + info["n_lamps"] + 16 + 4]
+    G, FD = [], []
+    n_par = n_alb + info["n_lamps"]
+    for i in ids:
+        h = 3e-3
+        xp, xm = x0.copy(), x0.copy()
+        xp[i] = np.float32(x0[i] * (1 + h)) if x0[i] != 0 else h
+        xm[i] = np.float32(x0[i] * (1 - h)) if x0[i] != 0 else -h
+        if i < n_par:
+            FD.append((cal.forward(xp) - cal.forward(xm)) / (xp[i] - xm[i]))
+        else:   # intrinsics: the gradient is the reprojection term's (the image term's K-dependence is not differentiated)
+            vals = []
+            for x in (xp, xm):
+                for c, k in zip(cams, cal.unpack(x)[2]):
+                    r.set_intrinsics(c, k)
+                vals.append(cal.w * r.reproj_loss(cams, pts, uv_t)[0])
+            FD.append((vals[0] - vals[1]) / (xp[i] - xm[i]))
+        G.append(g[i])
+    cal.forward(x0)
+    G, FD = np.array(G), np.array(FD)
+    vec = float(np.linalg.norm(G - FD) / np.linalg.norm(FD))
+    worst = float(np.max(np.abs(G - FD) / np.maximum(np.abs(FD), 1e-2 * np.abs(FD).max())))
+    r.destroy()
+    return {"workload": "C4 calibration: C0 scene, 3 KB4 cameras 960x600, 32 spp, depth 3, 4096 radiosity nodes, 144 parameters",
+            "params": 8 * 3 + info["n_lamps"] + 3 * 8, "parameter_vector": int(cal.n),
+            "params_note": "8 materials x RGB + emitter triangles + 3 x 8 intrinsics; the vector also holds the unused bench and "
+                           "emitter materials (zero gradient)", "setup_s": setup_s, "forward_ms": fms, "backward_ms": bms,
+            "forward_msamples_per_s": samples / (fms / 1e3) / 1e6, "loss_at_start": float(loss0),
+            "grad_check": {"entries": len(ids), "h": 3e-3, "vector_rel_err": vec, "worst_entry_rel_err": worst,
+                           "note": "GPU central differences of the FP32 render (FP64 loss); FP64-oracle differences at "
+                                   "h = 1e-4 are in tests/test_gpu_calib.py"}}
 
 
 def radiosity_bench(torch, cpu_check=True):

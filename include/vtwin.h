@@ -319,9 +319,10 @@ vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp);
 /* KB4 intrinsics of a camera: fx, fy, cx, cy, k1..k4 (gpu/lens.js:8 lensParams; skew stays). */
 vt_status vt_set_camera_intrinsics(vt_ctx* ctx, uint32_t camera, const double K[8]);
 vt_status vt_get_camera_intrinsics(const vt_ctx* ctx, uint32_t camera, double K[8]);
-/* Reprojection loss of n_pts dome-frame points in the cameras (gpu/lens.js:43 project, FP64): mean over cameras,
- * points and both coordinates of (uv - uv_target)^2, uv_target n_cameras x n_pts x 2; g_K (n_cameras x 8) its
- * gradient with respect to each camera's (fx, fy, cx, cy, k1..k4) by the analytic KB4 Jacobian. */
+/* Reprojection loss of n_pts dome-frame points in the cameras (gpu/lens.js:43 project, FP64): mean over the observed
+ * (camera, point) pairs and both coordinates of (uv - uv_target)^2, uv_target n_cameras x n_pts x 2 (NaN: not
+ * observed by that camera); g_K (n_cameras x 8) its gradient with respect to each camera's (fx, fy, cx, cy, k1..k4)
+ * by the analytic KB4 Jacobian. */
 vt_status vt_reproj_loss(vt_ctx* ctx, const uint32_t* cameras, uint32_t n_cameras, const double* pts, uint32_t n_pts, const double* uv_target,
                          double* loss, double* g_K);
 

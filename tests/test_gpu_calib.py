@@ -172,6 +172,7 @@ def test_reprojection_jacobian(rig):
         r.set_intrinsics(c, Kt)
         uv_t[c] = r.project(c, pts)
         r.set_intrinsics(c, K0[c])
+    uv_t[0, ::3] = np.nan                   # unobserved pairs are skipped
     loss, g = r.reproj_loss([0, 1], pts, uv_t)
     assert loss > 0
     for c in (0, 1):
@@ -211,3 +212,35 @@ def test_descent_recovers_parameters(rig):
         x = x - 0.01 * (m / (1 - 0.9 ** it)) / (np.sqrt(v / (1 - 0.999 ** it)) + 1e-12)
     print(f"\nloss {first:.3e} -> {loss:.3e}")
     assert loss < 0.1 * first
+
+
+def test_calibration_function_with_torch(rig):
+    """The packed forward/backward pair as a torch.autograd.Function: Adam on albedo, lamp radiance and the KB4
+    intrinsics (image loss + fiducial reprojection loss) from a 10% perturbation."""
+    torch = pytest.importorskip("torch")
+    from vtwin.calibrate import Calibration, CalibrationFunction
+
+    r, sc, info, t_alb, t_lamp, targets = rig
+    pts = dome.fib_hemisphere(200, 3.9)[0]
+    K_true = np.stack([r.get_intrinsics(c) for c in (0, 1)])
+    uv_t = np.stack([np.where(r.observed(c, pts, margin=2.0)[:, None], r.project(c, pts), np.nan) for c in (0, 1)])
+    cal = Calibration(r, [0, 1], targets[:2], fiducials=pts, uv_targets=uv_t, w_reproj=1e-3, spp=4, max_depth=3)
+    x_true = cal.pack(t_alb, t_lamp, K_true)
+    rng = np.random.default_rng(9)
+    x0 = x_true * (1 + 0.1 * (2 * rng.random(x_true.shape) - 1))
+    x0[:3 * info["n_materials"]] = np.clip(x0[:3 * info["n_materials"]], 0.01, 1.0)
+    scale = np.maximum(np.abs(x_true), 1e-3)
+    z = torch.tensor(x0 / scale, dtype=torch.float64, requires_grad=True)
+    opt = torch.optim.Adam([z], lr=3e-3)
+    first = None
+    for it in range(80):
+        opt.zero_grad()
+        x = z * torch.from_numpy(scale)
+        x = torch.cat([x[:3 * info["n_materials"]].clamp(0.01, 1.0), x[3 * info["n_materials"]:]])
+        loss = CalibrationFunction.apply(x, cal)
+        loss.backward()
+        opt.step()
+        first = float(loss) if first is None else first
+    err_K = np.abs(z.detach().numpy()[-16:] * scale[-16:] - x_true[-16:]) / np.abs(x_true[-16:]).clip(1e-3)
+    print(f"\nloss {first:.3e} -> {float(loss):.3e}; intrinsics max rel error {err_K.max():.2e} (start 1e-1)")
+    assert float(loss) < 0.05 * first

@@ -321,13 +321,17 @@ vt_status vt_reproj_loss(vt_ctx* ctx, const uint32_t* cameras, uint32_t n_camera
                          double* loss, double* g_K) {
   if (!ctx || !cameras || !n_cameras || (n_pts && (!pts || !uv_t)) || !loss) return VT_ERR_ARG;
   double L = 0.0;
-  const double norm = 1.0 / (2.0 * double(n_cameras) * double(std::max(1u, n_pts)));
+  size_t observed = 0;   // a NaN target: the point is not observed by that camera
+  for (size_t i = 0; i < size_t(n_cameras) * n_pts; i++) observed += std::isnan(uv_t[2 * i]) || std::isnan(uv_t[2 * i + 1]) ? 0 : 1;
+  const double norm = 1.0 / (2.0 * double(std::max<size_t>(1, observed)));
   for (uint32_t ci = 0; ci < n_cameras; ci++) {
     if (cameras[ci] >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(cameras[ci]));
     const vt_camera_desc& c = ctx->S.cams[cameras[ci]];
     const double* T = c.T_D_C;
     double g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (uint32_t i = 0; i < n_pts; i++) {
+      const double ut = uv_t[(size_t(ci) * n_pts + i) * 2], vt = uv_t[(size_t(ci) * n_pts + i) * 2 + 1];
+      if (std::isnan(ut) || std::isnan(vt)) continue;
       const double d[3] = {pts[3 * i] - T[3], pts[3 * i + 1] - T[7], pts[3 * i + 2] - T[11]};
       const double x = T[0] * d[0] + T[4] * d[1] + T[8] * d[2];
       const double y = T[1] * d[0] + T[5] * d[1] + T[9] * d[2];
@@ -351,7 +355,7 @@ vt_status vt_reproj_loss(vt_ctx* ctx, const uint32_t* cameras, uint32_t n_camera
           tp *= t2;
         }
       }
-      const double du = u - uv_t[(size_t(ci) * n_pts + i) * 2], dv = v - uv_t[(size_t(ci) * n_pts + i) * 2 + 1];
+      const double du = u - ut, dv = v - vt;
       L += (du * du + dv * dv) * norm;
       for (int k = 0; k < 8; k++) g[k] += 2.0 * norm * (du * J[0][k] + dv * J[1][k]);
     }

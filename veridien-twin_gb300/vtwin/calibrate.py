@@ -1,0 +1,91 @@
+"""Twin calibration as an autograd-style function of one flat parameter vector.
+
+    x = [albedo (n_materials x 3), lamp radiance (n_lamps), KB4 intrinsics (n_cameras x 8: fx, fy, cx, cy, k1..k4)]
+    loss(x) = image loss (mean over pixels and channels of (I - T)^2, vt_calib_forward)
+              + w_reproj x reprojection loss (mean over cameras, fiducials and both coordinates, vt_reproj_loss)
+
+`Calibration.forward(x)` returns the loss and keeps what `backward()` needs; `backward()` returns d loss / d x:
+the albedo and lamp entries by path replay and the transposed radiosity solve (vt_calib_backward), the intrinsics
+by the analytic KB4 Jacobian. The image term's dependence on the intrinsics (through visibility edges) is not
+differentiated: the intrinsics are pinned by the fiducials. `CalibrationFunction` wraps the pair as a
+torch.autograd.Function when torch is importable.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class Calibration:
+    def __init__(self, renderer, cameras, targets, fiducials=None, uv_targets=None, w_reproj=1.0, spp=32, light_samples=1, seed=0,
+                 max_depth=3, jacobi_iters=0):
+        self.r = renderer
+        self.cameras = [renderer._cam(c) for c in cameras]
+        self.targets = [np.ascontiguousarray(t, np.float32) for t in targets]
+        self.fid = None if fiducials is None else np.ascontiguousarray(fiducials, np.float64)
+        self.uv_t = None if uv_targets is None else np.ascontiguousarray(uv_targets, np.float64)
+        self.w = float(w_reproj)
+        self.kw = dict(spp=spp, lightSamples=light_samples, seed=seed, max_depth=max_depth, jacobi_iters=jacobi_iters)
+        info = renderer.calib_info
+        self.n_mat, self.n_lamps = info["n_materials"], info["n_lamps"]
+        self.n = 3 * self.n_mat + self.n_lamps + 8 * len(self.cameras)
+        self._last = None
+
+    # ------------------------------------------------------------------------------------------ packing
+    def pack(self, albedo, lamp, intrinsics) -> np.ndarray:
+        return np.concatenate([np.asarray(albedo, np.float64).ravel(), np.asarray(lamp, np.float64).ravel(),
+                               np.asarray(intrinsics, np.float64).ravel()])
+
+    def unpack(self, x):
+        x = np.asarray(x, np.float64)
+        a = x[:3 * self.n_mat].reshape(self.n_mat, 3)
+        l = x[3 * self.n_mat:3 * self.n_mat + self.n_lamps]
+        K = x[3 * self.n_mat + self.n_lamps:].reshape(len(self.cameras), 8)
+        return a, l, K
+
+    def current(self) -> np.ndarray:
+        """The renderer's intrinsics as a parameter vector tail (albedo and lamp parts zero)."""
+        K = np.stack([self.r.get_intrinsics(c) for c in self.cameras])
+        return self.pack(np.zeros((self.n_mat, 3)), np.zeros(self.n_lamps), K)
+
+    # ------------------------------------------------------------------------------------------ the pair
+    def forward(self, x) -> float:
+        a, l, K = self.unpack(x)
+        for c, k in zip(self.cameras, K):
+            self.r.set_intrinsics(c, k)
+        img, _ = self.r.calib_forward(self.cameras, a, l, targets=self.targets, images=False, **self.kw)
+        rep, gK = 0.0, np.zeros((len(self.cameras), 8))
+        if self.fid is not None:
+            rep, gK = self.r.reproj_loss(self.cameras, self.fid, self.uv_t)
+        self._last = (gK,)
+        self.parts = {"image": img, "reproj": rep}
+        return img + self.w * rep
+
+    def backward(self) -> np.ndarray:
+        if self._last is None:
+            raise RuntimeError("backward before forward")
+        (gK,) = self._last
+        ga, gl = self.r.calib_backward()
+        return self.pack(ga, gl, self.w * gK)
+
+    def loss_and_grad(self, x):
+        f = self.forward(x)
+        return f, self.backward()
+
+
+try:  # the autograd-style wrapper for callers that optimise with torch
+    import torch
+
+    class CalibrationFunction(torch.autograd.Function):
+        """loss = CalibrationFunction.apply(x, calibration): x a float64 tensor of the packed parameters."""
+
+        @staticmethod
+        def forward(ctx, x, calib):
+            ctx.calib = calib
+            return torch.tensor(calib.forward(x.detach().cpu().numpy()), dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, grad):
+            g = torch.from_numpy(ctx.calib.backward())
+            return grad * g, None
+except ImportError:  # pragma: no cover
+    CalibrationFunction = None

@@ -339,8 +339,25 @@ class TwinRenderer:
         check(self.lib.vt_get_camera_intrinsics(self._ctx, self._cam(name), _p(K)), self._ctx)
         return K
 
+    def observed(self, name, pts, margin=0.0, max_theta=None):
+        """Which dome-frame points a camera observes: in front of it and projecting inside its image (a fiducial
+        mask for reproj_loss)."""
+        c = self._cam(name)
+        cam = self.scene["cameras"][c]
+        T = np.asarray(cam["T_D_C"], np.float64).reshape(4, 4)
+        P = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+        Xc = (P - T[:3, 3]) @ T[:3, :3]
+        th = np.arctan2(np.hypot(Xc[:, 0], Xc[:, 1]), Xc[:, 2])
+        uv = self.project(c, P)
+        w, h = cam["size"]
+        ok = (uv[:, 0] >= margin) & (uv[:, 0] <= w - 1 - margin) & (uv[:, 1] >= margin) & (uv[:, 1] <= h - 1 - margin) & (Xc[:, 2] > 0)
+        if max_theta is not None:
+            ok &= th <= max_theta
+        return ok
+
     def reproj_loss(self, cameras, pts, uv_target):
-        """Reprojection loss of dome-frame points and its analytic gradient in each camera's KB4 intrinsics."""
+        """Reprojection loss of dome-frame points (NaN targets: not observed) and its analytic gradient in each
+        camera's KB4 intrinsics."""
         cams = np.ascontiguousarray([self._cam(c) for c in cameras], np.uint32)
         P = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
         T = np.ascontiguousarray(uv_target, np.float64).reshape(len(cams), len(P), 2)
