@@ -176,6 +176,7 @@ inline vtk::CamParams make_cam(const vt_ctx* ctx, uint32_t camera, uint32_t spp,
   cp.root = root;
   cp.t0 = shutter[0]; cp.t1 = shutter[1]; cp.scale = scale;
   cp.tile_w = vtk::TILE_W; cp.tile_h = vtk::TILE_H;
+  cp.refill = vtk::REFILL;
   return cp;
 }
 

@@ -439,6 +439,102 @@ __device__ __forceinline__ Hit trace_scene(const Scene& S, uint32_t root, float3
   return best;
 }
 
+// ------------------------------------------------------------------------------------------------ resumable trace
+// trace_scene split into single node visits, so that a warp of persistent lanes can take a new ray on any lane that
+// finishes while the others keep traversing. Per ray the sequence of operations is trace_scene's: the static BVH,
+// then each posed body that passes the same culls, each traversed by the same ordered descent; so are the hits.
+struct TraceState {
+  float3 ol, dl, inv;   // the ray in the current BVH's frame and its inverse direction
+  Hit best;
+  uint32_t node, sp, visits;
+  int k;                // current phase: -1 the static BVH, k >= 0 posed body k
+};
+
+// set up the first phase at or after `from` that has something to traverse; false when none is left
+__device__ __forceinline__ bool trace_phase(const Scene& S, uint32_t root, float3 o, float3 d, float tmin, float time, uint32_t mask,
+                                            uint32_t skip, TraceState& st, int from) {
+  int k = from;
+  if (k < 0) {
+    if (mask & 1u) {
+      st.k = -1; st.ol = o; st.dl = d; st.inv = safe_inv(d); st.node = root; st.sp = 0; st.visits = 0;
+      return true;
+    }
+    k = 0;
+  }
+  const int n_inst = (mask & 2u) ? int(min(ldu(S.su + 16), uint32_t(VT_MAX_INST))) : 0;
+  const float3 winv = safe_inv(d);
+  for (; k < n_inst; k++) {
+    const float* I = inst_rec(S, uint32_t(k));
+    if ((ldu(I + 15) & 2u) || ((skip >> k) & 1u)) continue;
+    if (slab(ld3(I + 16), ld3(I + 20), o, winv, tmin, st.best.t) >= st.best.t) continue;
+    if (!seg_near_capsule(o, d, tmin, fminf(st.best.t, 1e3f), ld3(I + 32), ld3(I + 36), __ldg(I + 35))) continue;
+    Rot R;
+    float3 p;
+    inst_pose(S, uint32_t(k), time, R, p);
+    st.ol = rtmul(R, o - p);
+    st.dl = rtmul(R, d);
+    st.inv = safe_inv(st.dl);
+    st.node = ldu(I + 11);
+    st.sp = 0;
+    st.visits = 0;
+    st.k = k;
+    return true;
+  }
+  st.k = n_inst;
+  return false;
+}
+
+// one node visit of the current phase (an iteration of traverse's loop): 0 continue, 1 the phase is finished,
+// 2 an any-hit query found its hit
+template <bool ANY>
+__device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceState& st, uint32_t* stN, float* stT) {
+  if (++st.visits > MAX_VISITS) { atomicAdd(S.dbg + DBG_VISITS, 1u); return 1; }
+  const uint32_t node = st.node;
+  const uint32_t inst = st.k < 0 ? MISS : uint32_t(st.k);
+  const float4* nb = S.nodes + 4u * node;
+  const float4 a0 = __ldg(nb), a1 = __ldg(nb + 1), a2 = __ldg(nb + 2), a3 = __ldg(nb + 3);
+  float t0 = slab(xyz(a0), xyz(a1), st.ol, st.inv, tmin, st.best.t);
+  float t1 = slab(xyz(a2), xyz(a3), st.ol, st.inv, tmin, st.best.t);
+  const uint32_t c0 = fu(a1.w), c1 = fu(a3.w), r0 = fu(a0.w), r1 = fu(a2.w);
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const float tc = c == 0 ? t0 : t1;
+    const uint32_t cnt = c == 0 ? c0 : c1, ref = c == 0 ? r0 : r1;
+    if (tc < st.best.t && cnt > 0u) {
+      if (cnt > MAX_LEAF) atomicAdd(S.dbg + DBG_LEAF, 1u);
+      const uint32_t end = ref + min(cnt, MAX_LEAF);
+      for (uint32_t k = ref; k < end; k++) {
+        float t, u, v;
+        if (tri_hit(S, k, st.ol, st.dl, tmin, st.best.t, t, u, v)) {
+          st.best.t = t; st.best.u = u; st.best.v = v; st.best.tri = k; st.best.inst = inst;
+          if (ANY) return 2;
+        }
+      }
+      if (c == 0) t0 = BIG; else t1 = BIG;
+    }
+  }
+  t0 = t0 < st.best.t ? t0 : BIG;
+  t1 = t1 < st.best.t ? t1 : BIG;
+  if ((t0 < BIG && c0 == 0u && r0 <= node) || (t1 < BIG && c1 == 0u && r1 <= node)) { atomicAdd(S.dbg + DBG_CORRUPT, 1u); return 1; }
+  const bool go0 = t0 < BIG, go1 = t1 < BIG;
+  if (go0 && go1) {
+    if (t1 < t0) { stN[st.sp] = r0; stT[st.sp] = t0; st.node = r1; }
+    else { stN[st.sp] = r1; stT[st.sp] = t1; st.node = r0; }
+    st.sp = min(st.sp + 1u, STACK - 1u);
+  } else if (go0) {
+    st.node = r0;
+  } else if (go1) {
+    st.node = r1;
+  } else {
+    while (st.sp > 0u) {
+      st.sp--;
+      if (stT[st.sp] < st.best.t) { st.node = stN[st.sp]; return 0; }
+    }
+    return 1;
+  }
+  return 0;
+}
+
 // ------------------------------------------------------------------------------------------------ surfaces
 struct Surf { float3 p, ng, ns, b; uint32_t vi0, vi1, vi2, mesh, flags, mat, inst; };
 

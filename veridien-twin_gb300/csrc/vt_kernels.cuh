@@ -16,10 +16,13 @@ struct CamParams {
   uint32_t w, h, spp, seed, cam_index, options, skip, n_light, mode, max_depth, root;
   float t0, t1, scale;
   uint32_t tile_w, tile_h;             // pixel enumeration order: tiles of tile_w x tile_h (product 32)
+  uint32_t refill;                     // traversal lanes: a warp takes new rays once this many of its lanes are idle
 };
 
 // default pixel tile: consecutive paths are neighbouring pixels of an 8 x 4 tile
 constexpr int TILE_W = 8, TILE_H = 4;
+// default refill threshold of the persistent traversal lanes
+constexpr uint32_t REFILL = 8;
 // padded pixel count of a w x h image in tile_w x tile_h tiles
 inline uint32_t tiled_pixels(uint32_t w, uint32_t h, uint32_t tw, uint32_t th) { return ((w + tw - 1) / tw) * ((h + th - 1) / th) * tw * th; }
 void launch_trace(const vtd::Scene& S, const float4* o4, const float4* d4, uint32_t n, uint32_t mask, uint32_t any_hit, uint32_t root,

@@ -137,23 +137,62 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_gen_pairs_kernel(const CamP
   }
 }
 
+// Persistent traversal lanes: every lane keeps one ray in flight, one node visit per loop iteration; once `refill`
+// lanes of the warp are idle they take the next queue entries with one atomic. Lanes stay busy until the queue
+// drains instead of waiting for the warp's slowest ray (warp-level ray compaction).
+template <typename F>
+__device__ __forceinline__ bool take_rays(bool& active, bool& exhausted, uint32_t* head, uint32_t n, uint32_t refill, F&& start) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+  if (!exhausted && idle && (__popc(idle) >= int(refill) || idle == 0xffffffffu)) {
+    const uint32_t leader = __ffs(idle) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(head, uint32_t(__popc(idle)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (base + uint32_t(__popc(idle)) >= n) exhausted = true;
+    if (!active) {
+      const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
+      if (idx < n) start(idx);
+    }
+  }
+  return __any_sync(0xffffffffu, active) || !exhausted;
+}
+
 template <int VAR>
 __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const uint32_t p = wb.q_in[k];
-    const float4 o = wb.o[p], d = wb.d[p];
-    const uint32_t b = wb.meta[p].w;
-    const uint32_t skip = b == 1 ? cp.skip : 0u;
-    const Hit h = trace_scene<false>(path_scene<VAR>(S, wb, p), cp.root, xyz(o), xyz(d), 0.0f, BIG, o.w, 3u,
-                                     VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip);
-    wb.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-    wb.hinst[p] = h.inst;
+  uint32_t stN[STACK];
+  float stT[STACK];
+  TraceState st;
+  Scene Sl = S;
+  float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
+  float tt = 0.0f;
+  uint32_t p = 0, skip = 0;
+  bool active = false, exhausted = false;
+  auto finish = [&]() {
+    wb.hit[p] = make_float4(st.best.t, st.best.u, st.best.v, __uint_as_float(st.best.tri));
+    wb.hinst[p] = st.best.inst;
     if (VAR == WAVE_SHARED) {
       const uint64_t have = wb.bc.dirty[p];
-      const uint64_t bits = cull_bits(wb.bc, xyz(o), xyz(d), h.t, skip, have);
+      const uint64_t bits = cull_bits(wb.bc, o, d, st.best.t, skip, have);
       if (bits & ~have) wb.bc.dirty[p] = have | bits;
     }
+    active = false;
+  };
+  auto start = [&](uint32_t idx) {
+    p = wb.q_in[idx];
+    const float4 o4 = wb.o[p], d4 = wb.d[p];
+    o = xyz(o4); d = xyz(d4); tt = o4.w;
+    skip = wb.meta[p].w == 1 ? cp.skip : 0u;
+    Sl = path_scene<VAR>(S, wb, p);
+    st.best = Hit{BIG, 0.0f, 0.0f, MISS, MISS};
+    active = trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, -1);
+    if (!active) { active = true; finish(); }
+  };
+  while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
+    if (!active) continue;
+    const int r = trace_visit<false>(Sl, 0.0f, st, stN, stT);
+    if (r != 0 && !trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, st.k + 1)) finish();
   }
 }
 
@@ -271,32 +310,70 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S0, const
   }
 }
 
+// any-hit of every queued path's light samples in sample order on persistent lanes; a lane moves to the path's next
+// sample when one finishes, and to a new path when the last one does
 template <int VAR>
 __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S0, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_sh;
   const uint32_t nl = cp.n_light;
-  const uint32_t skip = ldu(S0.su + 7);
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const uint32_t p = wb.q_sh[k];
-    const Scene S = path_scene<VAR>(S0, wb, p);
-    const float4 nee = wb.nee[p];
-    const float4* rec = wb.sh + size_t(p) * nl * 3;
-    float3 Ld = f3(0, 0, 0);
-    uint64_t have = 0ull, bits = 0ull;
-    if (VAR == WAVE_SHARED) have = wb.bc.dirty[p];
-    for (uint32_t j = 0; j < nl; j++) {
+  const uint32_t skip0 = ldu(S0.su + 7);
+  const uint32_t skip = VAR == WAVE_SHARED ? (skip0 | wb.bc.vary) : skip0;
+  uint32_t stN[STACK];
+  float stT[STACK];
+  TraceState st;
+  Scene S = S0;
+  float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
+  float4 nee = make_float4(0, 0, 0, 0);
+  float3 Ld = f3(0, 0, 0);
+  uint32_t p = 0, j = 0;
+  uint64_t have = 0ull, bits = 0ull;
+  bool active = false, exhausted = false;
+  const float4* rec = nullptr;
+  // the next light sample of the path with a valid record at or after j, set up as a ray; false when none is left
+  auto next_sample = [&]() -> bool {
+    for (; j < nl; j++) {
       const float4 a = rec[3 * j], w = rec[3 * j + 1];
       if (w.w == 0.0f) continue;
-      const Hit sh = trace_scene<true>(S, cp.root, xyz(a), xyz(w), 0.0f, a.w, nee.w, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip);
-      if (sh.tri == MISS) {
-        Ld = Ld + xyz(rec[3 * j + 2]);
-        if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, xyz(a), xyz(w), a.w, skip, have | bits);
-      }
+      o = xyz(a); d = xyz(w);
+      st.best = Hit{a.w, 0.0f, 0.0f, MISS, MISS};
+      if (trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, -1)) return true;
+      // nothing to traverse: the segment is unoccluded
+      Ld = Ld + xyz(rec[3 * j + 2]);
+      if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, o, d, a.w, skip0, have | bits);
     }
+    return false;
+  };
+  auto finish_path = [&]() {
     const float4 L = wb.L[p];
     const float3 v = xyz(L) + xyz(nee) * (Ld / float(nl));
     wb.L[p] = make_float4(v.x, v.y, v.z, L.w);
     if (VAR == WAVE_SHARED && bits) wb.bc.dirty[p] = have | bits;
+    active = false;
+  };
+  auto start = [&](uint32_t idx) {
+    p = wb.q_sh[idx];
+    S = path_scene<VAR>(S0, wb, p);
+    nee = wb.nee[p];
+    rec = wb.sh + size_t(p) * nl * 3;
+    Ld = f3(0, 0, 0);
+    j = 0;
+    bits = 0ull;
+    if (VAR == WAVE_SHARED) have = wb.bc.dirty[p];
+    active = true;
+    if (!next_sample()) finish_path();
+  };
+  while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
+    if (!active) continue;
+    const int r = trace_visit<true>(S, 0.0f, st, stN, stT);
+    bool done = r == 2;
+    if (r == 1) done = !trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, st.k + 1);
+    if (!done) continue;
+    if (st.best.tri == MISS) {
+      Ld = Ld + xyz(rec[3 * j + 2]);
+      if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, o, d, rec[3 * j].w, skip0, have | bits);
+    }
+    j++;
+    if (!next_sample()) finish_path();
   }
 }
 
@@ -350,14 +427,17 @@ WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix
   w.sh = reinterpret_cast<float4*>(take(P * size_t(n_light) * 48));
   w.acc = reinterpret_cast<float4*>(take(size_t(n_pix) * 16));
   w.counts = counts;
+  w.fetch = counts + 3;
   return w;
 }
 
 template <int VAR>
 void bounce_kernels(const Scene& S, const CamParams& cp, const WaveBufs& w, int blocks, cudaStream_t st) {
+  cudaMemsetAsync(w.fetch, 0, 4, st);
   wave_extend<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
   if (cp.mode == VT_SHADE_TWIN) wave_shade<VT_SHADE_TWIN, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
   else wave_shade<VT_SHADE_PATH, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  cudaMemsetAsync(w.fetch, 0, 4, st);
   wave_shadow<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
 }
 

@@ -50,6 +50,7 @@ struct WaveBufs {
   uint32_t* count_in;
   uint32_t* count_out;
   uint32_t* count_sh;
+  uint32_t* fetch;  // next queue entry to take, for the persistent traversal kernels (zeroed before each)
   BatchCull bc;
 };
 
