@@ -121,14 +121,18 @@ def traffic_per_sample():
     q = A.vt_render_req(camera=0, spp=SPP, light_samples=NL, seed=0, options=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
     q.shutter[:] = [0.0, 1.0]
     q.scale = 1.0
-    visits = tests = hits = 0
+    dbg = np.zeros(16)
     n = 0
     for y in range(0, H_, 40):
-        _, dbg = S.render(q, y0=y, y1=y + 1, fp64=False, threads=os.cpu_count() or 1)
-        visits += int(dbg[8]); tests += int(dbg[9]); hits += int(dbg[10])
+        _, d = S.render(q, y0=y, y1=y + 1, fp64=False, threads=os.cpu_count() or 1)
+        dbg += d
         n += W_ * SPP
-    return (64 * visits + 48 * tests + 256 * hits) / n, {"node_visits_per_sample": visits / n, "tri_tests_per_sample": tests / n,
-                                                         "hits_per_sample": hits / n}
+    visits, tests, hits = dbg[8], dbg[9], dbg[10]
+    ext_rays = max(dbg[13], 1)
+    return (64 * visits + 48 * tests + 256 * hits) / n, {
+        "node_visits_per_sample": visits / n, "tri_tests_per_sample": tests / n, "hits_per_sample": hits / n,
+        "extension_rays_per_sample": dbg[13] / n, "shadow_rays_per_sample": dbg[14] / n,
+        "bytes_per_extension_ray": (64 * dbg[11] + 48 * dbg[12]) / ext_rays}
 
 
 def run_reference(args):
@@ -188,6 +192,8 @@ def main():
     stream = torch.cuda.ExternalStream(r.lib.vt_stream(r._ctx))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     kw = dict(spp=SPP, lightSamples=NL, seed=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
+    # the autotuner (pixel tile, traversal refill threshold) on this frame, before anything is timed
+    tuned, _ = r.autotune_batch([0], poses[None], spp=SPP, max_depth=DEPTH)
     for _ in range(args.warmup):
         r.renderCamera(0, **kw)
     torch.cuda.synchronize()
@@ -227,6 +233,7 @@ def main():
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded dome, mulberry32)",
             "config": {"workload": WORKLOAD, "width": W_, "height": H_, "spp": SPP, "depth": DEPTH, "light_samples": NL,
+                       "tuned": {"tile": list(tuned["tile"]), "refill": tuned["refill"]},
                        "l2": "flushed between timed frames (256 MB write)", "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 24 * 4 + 48 * 4 * 24 + 16 * 8,
                     "d2h_bytes_per_step": W_ * H_ * 16},
@@ -240,12 +247,29 @@ def main():
         hbm = peaks.get("hbm_gbs", 6800.0)
         if not args.no_cpu_baseline:
             bps, cnt = traffic_per_sample()
-            per_launch = bps * W_ * H_ * SPP
-            ach = per_launch / (ms / args.steps / 1e3) / 1e9
-            line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
-                                "kernel": "render_kernel", "bytes_per_sample": bps, "note": "algorithmic bytes (BVH nodes, triangles, "
-                                "shading fetches) counted by the oracle on the same frame; the scene is L2-resident",
-                                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", **cnt}
+            # the dominant kernel, wave_extend, timed per launch with events on the library stream (a separate pass
+            # with kernel profiling on); algorithmic bytes per launch = its rays x the oracle's bytes per extension ray
+            r.kernel_profile(True, True)
+            for k in range(args.steps):
+                flush.fill_(float(k))
+                torch.cuda.synchronize()
+                r.renderCamera(0, **kw)
+            kt = r.timings()
+            r.kernel_profile(False, False)
+            launch_ms = kt["extend_ms"] / max(kt["extend_launches"], 1)
+            rays_per_launch = kt["extend_rays"] / max(kt["extend_launches"], 1)
+            per_launch = cnt["bytes_per_extension_ray"] * rays_per_launch
+            ach = per_launch / (launch_ms / 1e3) / 1e9
+            dram_per_ray = 17553408.0 / 307200.0     # ncu: wave_extend, bounce 1 of 320x240x4 (profiles/wave_kernels_320x240x4.md)
+            line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                                "traffic": dram_per_ray * rays_per_launch, "kernel": "wave_extend",
+                                "launch_ms": launch_ms, "rays_per_launch": rays_per_launch, "bytes_per_launch": per_launch,
+                                "note": "algorithmic bytes per launch = rays x (64 B per BVH node visit + 48 B per triangle test), "
+                                        "counted by the oracle on extension rays of the same frame; the scene is L2-resident, so "
+                                        "the DRAM traffic (ncu, scaled by rays) is far below it",
+                                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                                "frame_logical_gbs": bps * W_ * H_ * SPP / (ms / args.steps / 1e3) / 1e9, **cnt,
+                                "kernel_share": {"extend_ms": kt["extend_ms"], "shade_ms": kt["shade_ms"], "shadow_ms": kt["shadow_ms"]}}
             cv, info = cpu_baseline()
             line["cpu_baseline"] = {"value": cv, "unit": "Msamples/s", "cores": info["threads"], "kind": "port",
                                     "sample": f"{info['rows']} of {H_} rows x {W_} px x {SPP} spp ({info['samples']} samples, {info['seconds']:.1f} s)"}

@@ -267,11 +267,12 @@ typedef struct {
  * host/device rgba32f frames [camera][pose][h][w]. stats may be NULL. */
 vt_status vt_render_batch(vt_ctx* ctx, const vt_batch_req* req, uint16_t* raw_out, float* radiance_out, vt_batch_stats* stats);
 
-/* Autotuner of the batched renderer: times each candidate (wave size x pixel tile) on the request cut to
- * min(spp, 4) sub-samples and its first 8 poses, and keeps the fastest in the context for later batches with
- * wave_paths = 0 (results do not depend on either choice).
- * table (may be NULL): up to max_rows rows of (wave_paths, tile_w, tile_h, ms per million shared paths). */
-typedef struct { uint32_t wave_paths, tile_w, tile_h; float ms_per_mpath; } vt_tune_row;
+/* Autotuner of the batched renderer: times each candidate (wave size x pixel tile, then the traversal lanes' refill
+ * threshold) on the request cut to min(spp, 4) sub-samples and its first 8 poses, and keeps the fastest in the
+ * context for later batches with wave_paths = 0; the refill threshold also applies to vt_render_camera (results do
+ * not depend on any of these choices).
+ * table (may be NULL): up to max_rows rows of (wave_paths, tile_w, tile_h, ms per million shared paths, refill). */
+typedef struct { uint32_t wave_paths, tile_w, tile_h; float ms_per_mpath; uint32_t refill; } vt_tune_row;
 vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* table, uint32_t max_rows, uint32_t* n_rows,
                             vt_tune_row* best);
 
@@ -391,9 +392,20 @@ vt_status vt_bvh_build(const float* pos, uint32_t n_verts, const uint32_t* idx, 
 /* gpu/renderer.js:447 debugFlags(): loop-cap counters {traversalCap, leafCap, refined, refinedBody,
  * refinedShadow, refinedSubsample, corruptTree, packetCap, ...} (16 words). reset = 1 clears them. */
 vt_status vt_debug_flags(vt_ctx* ctx, uint32_t out[16], int reset);
-/* gpu/renderer.js:1271 timings(): device ms of the last render, sensor and solve calls, and kernel launches. */
-typedef struct { double render_ms, sensor_ms, solve_ms, trace_ms; uint64_t launches; } vt_timings;
+/* gpu/renderer.js:1271 timings(): device ms of the last render, sensor and solve calls, and kernel launches; with
+ * kernel profiling on, the summed device ms and launches of the path tracer's traversal and shading kernels and the
+ * rays they traced (since profiling was last reset). */
+typedef struct {
+  double render_ms, sensor_ms, solve_ms, trace_ms;
+  uint64_t launches;
+  double extend_ms, shade_ms, shadow_ms;           /* closest-hit, shading and any-hit kernels (profiling on) */
+  uint64_t extend_launches, shadow_launches;
+  uint64_t extend_rays, shadow_paths;              /* rays the closest-hit kernels traced, paths the any-hit kernels served */
+} vt_timings;
 vt_status vt_timings_get(const vt_ctx* ctx, vt_timings* out);
+/* Kernel profiling of vt_render_camera: events around each traversal and shading launch (enable 1), and the
+ * counters reset (reset 1). Adds a little launch overhead; off by default. */
+vt_status vt_kernel_profile(vt_ctx* ctx, int enable, int reset);
 /* The context's CUDA stream (cudaStream_t), for callers that order their own device work after ours. */
 void* vt_stream(vt_ctx* ctx);
 

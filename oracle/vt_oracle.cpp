@@ -1212,6 +1212,7 @@ template <typename R> struct Tracer {
       visits++;
       if (visits > 2048u) { dbg.c[0]++; break; }
       dbg.c[8]++;   // node fetched (64 B)
+      if (!anyHit) dbg.c[11]++;   // ... by a closest-hit query
       const float* a = N + size_t(node) * 16;
       R t0 = slab(ld3<R>(a), ld3<R>(a + 4), o, inv, tmin, best.t);
       R t1 = slab(ld3<R>(a + 8), ld3<R>(a + 12), o, inv, tmin, best.t);
@@ -1225,6 +1226,7 @@ template <typename R> struct Tracer {
           for (uint32_t k = ref0; k < ref0 + std::min(cnt, 64u); k++) {
             R t, u, v;
             dbg.c[9]++;   // triangle tested (v0, e1, e2: 48 B)
+            if (!anyHit) dbg.c[12]++;
             if (tri_hit(k, o, d, tmin, best.t, t, u, v) && t < best.t) {
               best.t = t; best.tri = k; best.u = u; best.v = v; best.inst = instI;
               if (anyHit) return true;
@@ -1307,6 +1309,7 @@ template <typename R> struct Tracer {
   // gpu/wgsl/trace.wgsl.js:302 traceSceneSkip
   Hit<R> trace(const V3<R>& o, const V3<R>& d, R tmin, R tmax, R time, bool anyHit, uint32_t mask, uint32_t skip) const {
     Hit<R> best{tmax, 0, 0, MISS, MISS};
+    if (mask & 1u) dbg.c[anyHit ? 14 : 13]++;   // rays: closest-hit (13) and any-hit (14) queries
     if (mask & 1u) if (traverse(gRoot, o, d, tmin, best, anyHit, MISS)) return best;
     if (mask & 2u) {
       V3<R> inv = safe_inv(d);

@@ -103,6 +103,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   cudaFree(ctx->batch.su); cudaFree(ctx->batch.cull); cudaFree(ctx->batch.ctr); cudaFree(ctx->batch.sensor); cudaFree(ctx->batch.mem);
   cudaFree(ctx->batch.rad); cudaFree(ctx->batch.raw);
   if (ctx->batch.exec) cudaGraphExecDestroy(ctx->batch.exec);
+  for (auto& e : ctx->kev) cudaEventDestroy(e);
   cudaFree(ctx->calib.mem);
   for (float4* p : ctx->calib.image) cudaFree(p);
   for (float4* p : ctx->calib.target) cudaFree(p);
@@ -270,9 +271,12 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
     if (cudaMalloc(&ctx->d_wave, need) != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "wavefront state allocation failed"); }
     ctx->wave_cap = need;
   }
-  const vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, paths, cp.n_light, n_pix, ctx->d_work);
+  vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, paths, cp.n_light, n_pix, ctx->d_work);
+  vtk::KernelTimer timer{ctx->kev.data(), ctx->kkind.data(), int(ctx->kev.size() / 2), 0};
+  if (ctx->kprof) wb.stats = reinterpret_cast<unsigned long long*>(ctx->d_work + 16);
   VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  vtk::wave_render(dev_scene(ctx), cp, wb, paths, ctx->cams[q->camera].radiance, ctx->wave_blocks, ctx->stream, &ctx->tim.launches);
+  vtk::wave_render(dev_scene(ctx), cp, wb, paths, ctx->cams[q->camera].radiance, ctx->wave_blocks, ctx->stream, &ctx->tim.launches,
+                   ctx->kprof ? &timer : nullptr);
   VT_CK(cudaGetLastError());
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   ctx->cams[q->camera].rendered = true;
@@ -284,6 +288,36 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   ctx->tim.render_ms = ms;
+  if (ctx->kprof) {
+    for (int i = 0; i < timer.n; i++) {
+      float k = 0;
+      cudaEventElapsedTime(&k, ctx->kev[2 * i], ctx->kev[2 * i + 1]);
+      if (ctx->kkind[i] == 0) { ctx->tim.extend_ms += k; ctx->tim.extend_launches++; }
+      else if (ctx->kkind[i] == 1) ctx->tim.shade_ms += k;
+      else { ctx->tim.shadow_ms += k; ctx->tim.shadow_launches++; }
+    }
+    unsigned long long st[2];
+    VT_CK(cudaMemcpy(st, ctx->d_work + 16, 16, cudaMemcpyDeviceToHost));
+    ctx->tim.extend_rays = st[0];
+    ctx->tim.shadow_paths = st[1];
+  }
+  return VT_OK;
+}
+
+vt_status vt_kernel_profile(vt_ctx* ctx, int enable, int reset) {
+  if (!ctx) return VT_ERR_ARG;
+  if (enable && ctx->kev.empty()) {
+    ctx->kev.resize(2 * 3 * 256);
+    ctx->kkind.resize(3 * 256);
+    for (auto& e : ctx->kev) VT_CK(cudaEventCreate(&e));
+  }
+  ctx->kprof = enable != 0;
+  if (reset) {
+    ctx->tim.extend_ms = ctx->tim.shade_ms = ctx->tim.shadow_ms = 0;
+    ctx->tim.extend_launches = ctx->tim.shadow_launches = ctx->tim.extend_rays = ctx->tim.shadow_paths = 0;
+    VT_CK(cudaMemsetAsync(ctx->d_work + 16, 0, 16, ctx->stream));
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+  }
   return VT_OK;
 }
 

@@ -152,7 +152,7 @@ vt_status validate(vt_ctx* ctx, const vt_batch_req* q, uint16_t* raw_out) {
   return VT_OK;
 }
 
-vt_status plan_batch(vt_ctx* ctx, const vt_batch_req* q, uint32_t wave_paths, uint32_t tw, uint32_t th, Plan& pl) {
+vt_status plan_batch(vt_ctx* ctx, const vt_batch_req* q, uint32_t wave_paths, uint32_t tw, uint32_t th, uint32_t refill, Plan& pl) {
   pl = Plan{};
   uint32_t n_pix_max = 0;
   for (uint32_t c = 0; c < q->n_cameras; c++) {
@@ -160,6 +160,7 @@ vt_status plan_batch(vt_ctx* ctx, const vt_batch_req* q, uint32_t wave_paths, ui
                                  q->scale);
     cp.tile_w = tw;
     cp.tile_h = th;
+    if (refill) cp.refill = refill;
     pl.cams.push_back(cp);
     pl.frame_off.push_back(pl.total_px);
     pl.total_px += size_t(q->n_poses) * cp.w * cp.h;
@@ -232,7 +233,7 @@ std::string graph_key(const vt_batch_req* q, const Plan& pl, const vtk::BatchCul
 
 // run the batch once; ms = device time; on a pair-capacity overflow returns VT_OK with *overflow set
 vt_status run_batch(vt_ctx* ctx, const vt_batch_req* q, uint16_t* raw_out, float* rad_out, uint32_t wave_paths, uint32_t tw, uint32_t th,
-                    bool allow_graph, Plan& pl, double& ms, bool& overflow, bool& replayed, uint32_t& vary, uint64_t& pairs) {
+                    uint32_t refill, bool allow_graph, Plan& pl, double& ms, bool& overflow, bool& replayed, uint32_t& vary, uint64_t& pairs) {
   auto& B = ctx->batch;
   overflow = false;
   replayed = false;
@@ -250,7 +251,7 @@ vt_status run_batch(vt_ctx* ctx, const vt_batch_req* q, uint16_t* raw_out, float
       return fail(ctx, VT_ERR_OOM, "batch allocation failed");
     }
   }
-  if ((s = plan_batch(ctx, q, wave_paths, tw, th, pl)) != VT_OK) return s;
+  if ((s = plan_batch(ctx, q, wave_paths, tw, th, refill, pl)) != VT_OK) return s;
   const bool want_raw = raw_out != nullptr, want_rad = rad_out != nullptr;
   size_t need = vtk::batch_wave_bytes(pl.P, pl.n_pw, pl.cap, pl.cams[0].n_light);
   if ((s = ensure(ctx, &B.mem, B.mem_bytes, need)) != VT_OK) return s;
@@ -352,7 +353,7 @@ vt_status vt_render_batch(vt_ctx* ctx, const vt_batch_req* q, uint16_t* raw_out,
   uint32_t vary = 0, reruns = 0;
   uint64_t pairs = 0;
   for (;;) {
-    s = run_batch(ctx, q, raw_out, radiance_out, wave, tw, th, true, pl, ms, overflow, replayed, vary, pairs);
+    s = run_batch(ctx, q, raw_out, radiance_out, wave, tw, th, 0, true, pl, ms, overflow, replayed, vary, pairs);
     if (s != VT_OK) return s;
     if (!overflow) break;
     if (++reruns > 3) return fail(ctx, VT_ERR_OOM, "render_batch: pair capacity kept overflowing");
@@ -382,29 +383,42 @@ vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* t
   q.use_graph = 0;
   const uint32_t waves[] = {2u << 20, 4u << 20, 8u << 20, 16u << 20};
   const uint32_t tiles[][2] = {{8, 4}, {16, 2}, {4, 8}, {32, 1}};
-  vt_tune_row top{0, 0, 0, INFINITY};
+  const uint32_t refills[] = {4, 16, 32};
+  vt_tune_row top{0, 0, 0, INFINITY, 0};
   uint32_t rows = 0;
+  auto trial = [&](uint32_t w, uint32_t tw, uint32_t th, uint32_t rf, Plan& pl) -> vt_status {
+    double ms = 0;
+    bool overflow = false, replayed = false;
+    uint32_t vary = 0;
+    uint64_t pairs = 0;
+    for (int rep = 0; rep < 4; rep++) {   // warm (and grow the pair capacity), then time
+      vt_status st = run_batch(ctx, &q, nullptr, nullptr, w, tw, th, rf, false, pl, ms, overflow, replayed, vary, pairs);
+      if (st != VT_OK) return st;
+      if (!overflow && rep >= 1) break;
+    }
+    if (overflow) return VT_OK;
+    const vt_tune_row r{w, tw, th, float(ms / (double(pl.shared_paths) / 1e6)), rf};
+    if (table && rows < max_rows) table[rows] = r;
+    rows++;
+    if (r.ms_per_mpath < top.ms_per_mpath) top = r;
+    return VT_OK;
+  };
+  // wave size x pixel tile at the default refill threshold, then the refill threshold at the best of those
   uint32_t prev_pw = 0;
   for (uint32_t w : waves) {
     Plan pl;
-    if ((s = plan_batch(ctx, &q, w, vtk::TILE_W, vtk::TILE_H, pl)) != VT_OK) return s;
+    if ((s = plan_batch(ctx, &q, w, vtk::TILE_W, vtk::TILE_H, 0, pl)) != VT_OK) return s;
     if (pl.n_pw == prev_pw) continue;   // the frames already fit a smaller wave: the same plan
     prev_pw = pl.n_pw;
     for (const auto& t : tiles) {
-      double ms = 0;
-      bool overflow = false, replayed = false;
-      uint32_t vary = 0;
-      uint64_t pairs = 0;
-      for (int rep = 0; rep < 4; rep++) {   // warm (and grow the pair capacity), then time
-        s = run_batch(ctx, &q, nullptr, nullptr, w, t[0], t[1], false, pl, ms, overflow, replayed, vary, pairs);
-        if (s != VT_OK) return s;
-        if (!overflow && rep >= 1) break;
-      }
-      if (overflow) continue;
-      const vt_tune_row r{w, t[0], t[1], float(ms / (double(pl.shared_paths) / 1e6))};
-      if (table && rows < max_rows) table[rows] = r;
-      rows++;
-      if (r.ms_per_mpath < top.ms_per_mpath) top = r;
+      if ((s = trial(w, t[0], t[1], vtk::REFILL, pl)) != VT_OK) return s;
+    }
+  }
+  if (top.wave_paths) {
+    const vt_tune_row base = top;
+    for (uint32_t rf : refills) {
+      Plan pl;
+      if ((s = trial(base.wave_paths, base.tile_w, base.tile_h, rf, pl)) != VT_OK) return s;
     }
   }
   if (n_rows) *n_rows = std::min(rows, max_rows);
@@ -412,6 +426,7 @@ vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* t
   ctx->batch.wave_paths = top.wave_paths;
   ctx->batch.tile_w = top.tile_w;
   ctx->batch.tile_h = top.tile_h;
+  ctx->batch.refill = top.refill;
   if (best) *best = top;
   return VT_OK;
 }

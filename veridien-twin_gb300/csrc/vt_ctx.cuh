@@ -37,6 +37,10 @@ struct vt_ctx {
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
   vt_timings tim{};
+  // kernel profiling of vt_render_camera: event pairs around the bounce kernels, ray counters at d_work + 64 B
+  bool kprof = false;
+  std::vector<cudaEvent_t> kev;
+  std::vector<uint8_t> kkind;
   // mixed-precision radiosity: converted copies of F and the solver's work buffers
   struct Tc {
     void* mem = nullptr;
@@ -61,8 +65,8 @@ struct vt_ctx {
     std::string key;
     uint64_t graph_launches = 0;   // kernels in the captured graph
     uint32_t cap = 0;               // pair capacity of a wave
-    // tuned configuration (0: defaults)
-    uint32_t wave_paths = 0, tile_w = 0, tile_h = 0;
+    // tuned configuration (0: defaults); tile and refill also apply to vt_render_camera
+    uint32_t wave_paths = 0, tile_w = 0, tile_h = 0, refill = 0;
   } batch;
   // differentiable calibration: radiosity nodes (clusters of static triangles), F, the emitter transfer D, parameters,
   // per-camera images and targets, and the last forward's state for the backward
@@ -175,8 +179,9 @@ inline vtk::CamParams make_cam(const vt_ctx* ctx, uint32_t camera, uint32_t spp,
   cp.max_depth = std::max(1u, std::min(max_depth, 64u));
   cp.root = root;
   cp.t0 = shutter[0]; cp.t1 = shutter[1]; cp.scale = scale;
-  cp.tile_w = vtk::TILE_W; cp.tile_h = vtk::TILE_H;
-  cp.refill = vtk::REFILL;
+  cp.tile_w = ctx->batch.tile_w ? ctx->batch.tile_w : vtk::TILE_W;
+  cp.tile_h = ctx->batch.tile_h ? ctx->batch.tile_h : vtk::TILE_H;
+  cp.refill = ctx->batch.refill ? ctx->batch.refill : vtk::REFILL;
   return cp;
 }
 

@@ -161,6 +161,7 @@ __device__ __forceinline__ bool take_rays(bool& active, bool& exhausted, uint32_
 template <int VAR>
 __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
+  if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats, (unsigned long long)n);
   uint32_t stN[STACK];
   float stT[STACK];
   TraceState st;
@@ -315,6 +316,7 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S0, const
 template <int VAR>
 __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S0, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_sh;
+  if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats + 1, (unsigned long long)n);
   const uint32_t nl = cp.n_light;
   const uint32_t skip0 = ldu(S0.su + 7);
   const uint32_t skip = VAR == WAVE_SHARED ? (skip0 | wb.bc.vary) : skip0;
@@ -431,17 +433,37 @@ WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix
   return w;
 }
 
+// event pair around one launch when a timer has room
+struct TimedLaunch {
+  KernelTimer* t;
+  cudaStream_t st;
+  int slot = -1;
+  TimedLaunch(KernelTimer* t_, cudaStream_t s, uint8_t kind) : t(t_), st(s) {
+    if (t && t->n + 1 <= t->cap) { slot = t->n++; t->kind[slot] = kind; cudaEventRecord(t->ev[2 * slot], st); }
+  }
+  ~TimedLaunch() { if (slot >= 0) cudaEventRecord(t->ev[2 * slot + 1], st); }
+};
+
 template <int VAR>
-void bounce_kernels(const Scene& S, const CamParams& cp, const WaveBufs& w, int blocks, cudaStream_t st) {
+void bounce_kernels(const Scene& S, const CamParams& cp, const WaveBufs& w, int blocks, cudaStream_t st, KernelTimer* timer) {
   cudaMemsetAsync(w.fetch, 0, 4, st);
-  wave_extend<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
-  if (cp.mode == VT_SHADE_TWIN) wave_shade<VT_SHADE_TWIN, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
-  else wave_shade<VT_SHADE_PATH, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  {
+    TimedLaunch tl(timer, st, 0);
+    wave_extend<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  }
+  {
+    TimedLaunch tl(timer, st, 1);
+    if (cp.mode == VT_SHADE_TWIN) wave_shade<VT_SHADE_TWIN, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+    else wave_shade<VT_SHADE_PATH, VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  }
   cudaMemsetAsync(w.fetch, 0, 4, st);
-  wave_shadow<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  {
+    TimedLaunch tl(timer, st, 2);
+    wave_shadow<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+  }
 }
 
-void wave_bounces(const Scene& S, const CamParams& cp, WaveBufs wb, int var, int blocks, cudaStream_t st, uint64_t* launches) {
+void wave_bounces(const Scene& S, const CamParams& cp, WaveBufs wb, int var, int blocks, cudaStream_t st, uint64_t* launches, KernelTimer* timer) {
   const uint32_t depth = cp.mode == VT_SHADE_TWIN ? 2u : cp.max_depth;
   WaveBufs w = wb;
   for (uint32_t b = 1; b <= depth; b++) {
@@ -453,9 +475,9 @@ void wave_bounces(const Scene& S, const CamParams& cp, WaveBufs wb, int var, int
     w.count_sh = wb.counts + 2;
     cudaMemsetAsync(w.count_out, 0, 4, st);
     cudaMemsetAsync(w.count_sh, 0, 4, st);
-    if (var == WAVE_SHARED) bounce_kernels<WAVE_SHARED>(S, cp, w, blocks, st);
-    else if (var == WAVE_PAIRS) bounce_kernels<WAVE_PAIRS>(S, cp, w, blocks, st);
-    else bounce_kernels<WAVE_PLAIN>(S, cp, w, blocks, st);
+    if (var == WAVE_SHARED) bounce_kernels<WAVE_SHARED>(S, cp, w, blocks, st, timer);
+    else if (var == WAVE_PAIRS) bounce_kernels<WAVE_PAIRS>(S, cp, w, blocks, st, timer);
+    else bounce_kernels<WAVE_PLAIN>(S, cp, w, blocks, st, timer);
     if (launches) *launches += 3;
   }
 }
@@ -474,7 +496,7 @@ void wave_gen_pairs(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t s
 
 // one camera: waves of whole sub-sample indices, each bounce extend -> shade -> shadow over compacted queues
 void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave_paths, float4* out, int blocks, cudaStream_t st,
-                 uint64_t* launches) {
+                 uint64_t* launches, KernelTimer* timer) {
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t per_wave = std::max(1u, std::min(cp.spp, wave_paths / n_pix));
   uint64_t nlaunch = 0;
@@ -485,7 +507,7 @@ void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave
     w.q_in = wb.qa; w.count_in = wb.counts + 0;
     wave_gen<<<blocks, WAVE_THREADS, 0, st>>>(cp, w, i0, n_i, n_pix);
     nlaunch++;
-    wave_bounces(S, cp, wb, WAVE_PLAIN, blocks, st, &nlaunch);
+    wave_bounces(S, cp, wb, WAVE_PLAIN, blocks, st, &nlaunch, timer);
     const int last = i0 + n_i >= cp.spp;
     wave_finalize<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb, i0, n_i, n_pix, wb.acc, out, last);
     nlaunch++;

@@ -51,17 +51,26 @@ struct WaveBufs {
   uint32_t* count_out;
   uint32_t* count_sh;
   uint32_t* fetch;  // next queue entry to take, for the persistent traversal kernels (zeroed before each)
+  unsigned long long* stats;   // optional: [0] rays of the closest-hit kernels, [1] paths of the any-hit kernels
   BatchCull bc;
+};
+
+// optional events around the bounce kernels (kernel profiling): pairs in launch order, kind 0 extend, 1 shade, 2 shadow
+struct KernelTimer {
+  cudaEvent_t* ev;
+  uint8_t* kind;
+  int cap, n;
 };
 
 size_t wave_bytes(uint32_t paths, uint32_t n_light, uint32_t n_pix);
 WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix, uint32_t* counts);
 void wave_render(const vtd::Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave_paths, float4* out, int blocks, cudaStream_t st,
-                 uint64_t* launches);
+                 uint64_t* launches, KernelTimer* timer = nullptr);
 int wave_blocks_per_sm();
 
 // one wave's bounces (extend, shade, shadow per bounce) over the paths queued in wb.qa / counts[0]
-void wave_bounces(const vtd::Scene& S, const CamParams& cp, WaveBufs wb, int var, int blocks, cudaStream_t st, uint64_t* launches);
+void wave_bounces(const vtd::Scene& S, const CamParams& cp, WaveBufs wb, int var, int blocks, cudaStream_t st, uint64_t* launches,
+                  KernelTimer* timer = nullptr);
 // camera rays of a batch wave: paths p = i * n_pw + lp, i < spp, pixel id px0 + lp; clears the dirty masks
 void wave_gen_batch(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t st);
 // camera rays of the pair paths (pair j repeats shared path pair_src[j]); count in counts[0]

@@ -109,7 +109,8 @@ class vt_batch_stats(C.Structure):
 
 
 class vt_tune_row(C.Structure):
-    _fields_ = [("wave_paths", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("ms_per_mpath", C.c_float)]
+    _fields_ = [("wave_paths", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("ms_per_mpath", C.c_float),
+                ("refill", C.c_uint32)]
 
 
 class vt_calib_desc(C.Structure):
@@ -141,7 +142,9 @@ class vt_bvh_result(C.Structure):
 
 class vt_timings(C.Structure):
     _fields_ = [("render_ms", C.c_double), ("sensor_ms", C.c_double), ("solve_ms", C.c_double),
-                ("trace_ms", C.c_double), ("launches", C.c_uint64)]
+                ("trace_ms", C.c_double), ("launches", C.c_uint64), ("extend_ms", C.c_double), ("shade_ms", C.c_double),
+                ("shadow_ms", C.c_double), ("extend_launches", C.c_uint64), ("shadow_launches", C.c_uint64),
+                ("extend_rays", C.c_uint64), ("shadow_paths", C.c_uint64)]
 
 
 def ptr(a: np.ndarray, ct):

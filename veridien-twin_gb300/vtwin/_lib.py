@@ -38,6 +38,7 @@ SIGNATURES = {
     "vt_get_camera_intrinsics": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_reproj_loss": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_double),
                                    C.c_void_p]),
+    "vt_kernel_profile": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
     "vt_render_batch": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_batch_req), C.c_void_p, C.c_void_p, C.POINTER(A.vt_batch_stats)]),
     "vt_batch_autotune": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_batch_req), C.POINTER(A.vt_tune_row), C.c_uint32,
                                       C.POINTER(C.c_uint32), C.POINTER(A.vt_tune_row)]),

@@ -267,8 +267,10 @@ class TwinRenderer:
         best = A.vt_tune_row()
         check(self.lib.vt_batch_autotune(self._ctx, C.byref(q), rows, 64, C.byref(n), C.byref(best)), self._ctx)
         del keep
-        tab = [{"wave_paths": r.wave_paths, "tile": (r.tile_w, r.tile_h), "ms_per_mpath": r.ms_per_mpath} for r in rows[:n.value]]
-        return {"wave_paths": best.wave_paths, "tile": (best.tile_w, best.tile_h), "ms_per_mpath": best.ms_per_mpath}, tab
+        tab = [{"wave_paths": r.wave_paths, "tile": (r.tile_w, r.tile_h), "refill": r.refill, "ms_per_mpath": r.ms_per_mpath}
+               for r in rows[:n.value]]
+        return {"wave_paths": best.wave_paths, "tile": (best.tile_w, best.tile_h), "refill": best.refill,
+                "ms_per_mpath": best.ms_per_mpath}, tab
 
     # ------------------------------------------------------------------------------------------- calibration
     def calib_setup(self, n_nodes=4096, lamp_samples=16) -> dict:
@@ -404,7 +406,13 @@ class TwinRenderer:
         t = A.vt_timings()
         check(self.lib.vt_timings_get(self._ctx, C.byref(t)), self._ctx)
         return {"render_ms": t.render_ms, "sensor_ms": t.sensor_ms, "solve_ms": t.solve_ms, "trace_ms": t.trace_ms,
-                "launches": int(t.launches)}
+                "launches": int(t.launches), "extend_ms": t.extend_ms, "shade_ms": t.shade_ms, "shadow_ms": t.shadow_ms,
+                "extend_launches": int(t.extend_launches), "shadow_launches": int(t.shadow_launches),
+                "extend_rays": int(t.extend_rays), "shadow_paths": int(t.shadow_paths)}
+
+    def kernel_profile(self, enable=True, reset=True):
+        """Events around the path tracer's bounce kernels (timings() then reports their device ms and rays)."""
+        check(self.lib.vt_kernel_profile(self._ctx, int(enable), int(reset)), self._ctx)
 
     # ------------------------------------------------------------------------------------------- radiosity
     def solve_radiosity(self, F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=1000, check_every=8, B0=None, reuse_f=False):
