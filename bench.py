@@ -14,6 +14,7 @@ bounded sample of the same frame; the reference itself is JavaScript + WebGPU an
 
   python bench.py --case render:W:H:SPP            one small path-traced frame (two renders), for profilers
   python bench.py --case radiosity:N:PREC:SWEEPS   one 64-RHS radiosity solve capped at SWEEPS sweeps (fp32|bf16|fp8)
+  python bench.py --case radiosity1:N:PREC:SWEEPS  the same with one right-hand side
 """
 import argparse
 import json
@@ -303,6 +304,18 @@ def run_case(spec):
         ms = r.timings()["render_ms"]
         print(json.dumps({"case": spec, "render_ms": ms, "msamples_per_s": w * h * spp / ms / 1e3}))
         r.destroy()
+    elif kind == "radiosity1":
+        from vtwin.renderer import form_factors, solve_radiosity
+
+        n, sweeps = int(a[0]), int(a[2])
+        prec = {"fp32": A.VT_PREC_FP32, "fp32tma": A.VT_PREC_FP32_TMA, "bf16": A.VT_PREC_BF16, "fp8": A.VT_PREC_FP8}[a[1]]
+        P = dome.dome_patches(n, seed=2)
+        F = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        form_factors(P["centres"], P["normals"], P["areas"], out=F)
+        E = dome.radiosity_rhs(n, P["lamps"], 1)
+        solve_radiosity(F, P["rho"], E, precision=prec, tol=1e-9, max_iters=sweeps)
+        _, info = solve_radiosity(F, P["rho"], E, precision=prec, tol=1e-9, max_iters=sweeps)
+        print(json.dumps({"case": spec, **{k: v for k, v in info.items() if isinstance(v, (int, float))}}))
     elif kind == "radiosity":
         from vtwin.renderer import form_factors, solve_radiosity
 

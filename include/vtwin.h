@@ -329,7 +329,8 @@ vt_status vt_reproj_loss(vt_ctx* ctx, const uint32_t* cameras, uint32_t n_camera
 
 /* -------------------------------------------------------------------------------------- node radiosity */
 
-enum { VT_PREC_FP32 = 0, VT_PREC_BF16 = 1, VT_PREC_FP8 = 2 };
+enum { VT_PREC_FP32 = 0, VT_PREC_BF16 = 1, VT_PREC_FP8 = 2,
+       VT_PREC_FP32_TMA = 3 };  /* FP32, one right-hand side, n % 4 == 0: F fed to shared memory by bulk copies */
 
 /* Dense node radiosity B = E + diag(rho) F B (the lite_nodes / TwinRenderer Jacobi, gpu/wgsl/kernels.wgsl.js
  * :416-461 jacobiGather + jacobiUpdate with Lambertian nodes, gpu/renderer.js:729 _submitJacobi, :804 converge).

@@ -204,6 +204,16 @@ def test_radiosity_fp32_matches_direct_fp64_solve():
         err = np.linalg.norm(B - Bd) / np.linalg.norm(Bd)
         print(f"\nradiosity FP32 R={R}: iters {info['iters']} residual {info['residual']:.2e} rel err vs FP64 {err:.2e}")
         assert info["status"] == 0 and err < 1e-5
+    # the bulk-copy (TMA) fed matvec: one right-hand side, n % 4 == 0
+    E = dome.radiosity_rhs(1024, P["lamps"], 1)
+    Bd = O.solve_dense(F, P["rho"], E)
+    B, info = solve_radiosity(F, P["rho"], E, precision=A.VT_PREC_FP32_TMA, tol=1e-6, max_iters=2000)
+    err = np.linalg.norm(B - Bd) / np.linalg.norm(Bd)
+    print(f"radiosity FP32 (bulk-copy matvec): iters {info['iters']} rel err vs FP64 {err:.2e}")
+    assert info["status"] == 0 and err < 1e-5
+    from vtwin._lib import VtError
+    with pytest.raises(VtError):
+        solve_radiosity(F, P["rho"], dome.radiosity_rhs(1024, P["lamps"], 8), precision=A.VT_PREC_FP32_TMA)
 
 
 def test_errors_are_reported(dome_small):

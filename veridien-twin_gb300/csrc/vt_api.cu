@@ -600,11 +600,15 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   if (q->n_rhs > 64) return fail(ctx, VT_ERR_ARG, "solve: at most 64 right-hand sides");
   if (q->n_rhs > 1 && (q->n_rhs % 4)) return fail(ctx, VT_ERR_ARG, "solve: several right-hand sides must be a multiple of 4");
   if (q->precision == VT_PREC_BF16 || q->precision == VT_PREC_FP8) return tc_solve(ctx, q);
-  if (q->precision != VT_PREC_FP32) return fail(ctx, VT_ERR_ARG, "solve: unknown precision");
+  if (q->precision != VT_PREC_FP32 && q->precision != VT_PREC_FP32_TMA) return fail(ctx, VT_ERR_ARG, "solve: unknown precision");
+  if (q->precision == VT_PREC_FP32_TMA && (q->n_rhs != 1 || q->n % 4u))
+    return fail(ctx, VT_ERR_ARG, "solve: the bulk-copy matvec takes one right-hand side and n % 4 == 0");
   const uint32_t n = q->n, R = q->n_rhs;
   const size_t nb = size_t(n) * R * 4, nf = size_t(n) * n * 4;
   const bool dF = is_device_ptr(q->F);
-  const uint32_t max_blocks = std::max<uint32_t>((n + 7) / 8, uint32_t((size_t(n) * R / 4 + 255) / 256)) + 8;
+  const bool tma = q->precision == VT_PREC_FP32_TMA;
+  const uint32_t max_blocks = std::max<uint32_t>(std::max<uint32_t>((n + 7) / 8, uint32_t((size_t(n) * R / 4 + 255) / 256)),
+                                                 tma ? vtk::jacobi_matvec_tma_blocks(n) : 0u) + 8;
   const size_t gemm_work = R > 1 ? vtk::jacobi_gemm_fp32_work(n, R) : 0;
   const size_t need = (dF ? 0 : nf) + 3 * nb + size_t(n) * 4 + size_t(max_blocks) * 16 + gemm_work + 64 + 2048;
   vt_status s = ensure_scratch(ctx, need);
@@ -635,7 +639,8 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
     const uint32_t k = std::min(check, max_it - it);
     for (uint32_t j = 0; j < k; j++) {
       if (j == 0) VT_CK(cudaEventRecord(ctx->ev2, ctx->stream));
-      if (R == 1) vtk::launch_jacobi_matvec(Fd, rho, E, cur, nxt, n, partials, &np, ctx->stream);
+      if (tma) vtk::launch_jacobi_matvec_tma(Fd, rho, E, cur, nxt, n, partials, &np, ctx->stream);
+      else if (R == 1) vtk::launch_jacobi_matvec(Fd, rho, E, cur, nxt, n, partials, &np, ctx->stream);
       else vtk::launch_jacobi_gemm_fp32(Fd, rho, E, cur, nxt, n, R, work, partials, &np, ctx->stream);
       if (j == 0) VT_CK(cudaEventRecord(ctx->ev3, ctx->stream));
       std::swap(cur, nxt);
@@ -657,6 +662,7 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   if ((s = from_device(ctx, q->B, cur, nb)) != VT_OK) return s;
   VT_CK(cudaStreamSynchronize(ctx->stream));
+  if (tma && vtk::matvec_error(ctx->stream, true)) return fail(ctx, VT_ERR_TIMEOUT, "solve: a bulk copy of F did not complete");
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   q->iters = it; q->refinements = 0; q->residual = resid; q->ms = ms;

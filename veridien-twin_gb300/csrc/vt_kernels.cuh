@@ -40,6 +40,12 @@ void launch_sensor_expose_u16(const SensorParams& su, const float4* E, float sca
 // B_out = E + rho (F B_in), n x 1, and per-block partial sums of |B_out - B_in|^2 and |B_out|^2 (doubles)
 void launch_jacobi_matvec(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n,
                           double* partials, uint32_t* n_partials, cudaStream_t st);
+// the same with F's rows fed into shared memory by bulk copies (n % 4 == 0); bounded waits raise matvec_error
+void launch_jacobi_matvec_tma(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n,
+                              double* partials, uint32_t* n_partials, cudaStream_t st);
+uint32_t jacobi_matvec_tma_blocks(uint32_t n);
+// nonzero when a bulk copy of the TMA-fed matvec did not land in time (and reset it)
+uint32_t matvec_error(cudaStream_t st, bool reset);
 // B_out = E + rho (F B_in), n x R row-major (R <= 64, multiple of 4), CUDA-core FP32 GEMM
 // work: jacobi_gemm_fp32_work(n, R) bytes for the split-K partial products (null: no split)
 size_t jacobi_gemm_fp32_work(uint32_t n, uint32_t R);

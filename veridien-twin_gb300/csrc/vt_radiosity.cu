@@ -3,6 +3,8 @@
 //
 //   jacobi_matvec   one right-hand side: one warp per row, F streamed with 128-bit loads (HBM- or L2-bound: 4 B of F
 //                   per 2 flops), B_in read from L1/L2; epilogue B_out = E + rho acc and the residual partials.
+//   jacobi_matvec_tma  the same sweep with F's rows fed into shared memory by bulk copies (VT_PREC_FP32_TMA; ~20%
+//                   slower than the plain kernel's 128-bit streaming loads on GB300, which stay the default).
 //   jacobi_gemm     R right-hand sides (R <= 64): a 128 x 64 output tile per 256-thread block, 8 x 4 outputs per
 //                   thread, F and B staged through double-buffered shared memory in 16-wide K slices, K split across
 //                   blocks to fill the GPU. Compute-bound at 2 R flops per 4-byte element of F (R = 64: 32 flop/B)
@@ -11,6 +13,7 @@
 // |B_out - B_in| / |B_out| is the relative residual |E + rho F B_in - B_in| / |B_out| of the Jacobi iterate.
 #include <algorithm>
 
+#include "vt_async.cuh"
 #include "vt_kernels.cuh"
 
 namespace vtk {
@@ -64,6 +67,109 @@ __global__ void __launch_bounds__(MV_THREADS) jacobi_matvec_kernel(const float* 
     }
   }
   block_sum2(d2, b2, partials);
+}
+
+// ------------------------------------------------------------------------------------------ TMA-fed matvec
+// One right-hand side, F rows streamed by the copy engine: thread 0 of each block keeps MVT_STAGES bulk copies
+// (cp.async.bulk, 8 KB chunks of a row) in flight into a shared-memory ring, completing on mbarriers; all threads
+// multiply a chunk from shared memory with B (L1/L2) while the next ones land. Each block takes rows blockIdx.x,
+// blockIdx.x + gridDim.x, ...; a row's partial sums meet in a block reduction. Rows must start 16-byte aligned
+// (n % 4 == 0). Every mbarrier wait is bounded (error flag, no hang).
+constexpr int MVT_THREADS = 256, MVT_STAGES = 4;
+constexpr uint32_t MVT_CHUNK = 2048;   // floats per bulk copy (8 KB)
+
+__device__ uint32_t g_matvec_err;
+
+__global__ void __launch_bounds__(MVT_THREADS) jacobi_matvec_tma_kernel(const float* __restrict__ F, const float* __restrict__ rho,
+                                                                       const float* __restrict__ E, const float* __restrict__ Bin,
+                                                                       float* __restrict__ Bout, uint32_t n, double* __restrict__ partials) {
+  extern __shared__ __align__(128) float ring[];   // MVT_STAGES x MVT_CHUNK
+  __shared__ __align__(8) uint64_t full[MVT_STAGES];
+  __shared__ float red[MVT_THREADS / 32];
+  using namespace async;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t chunks = (n + MVT_CHUNK - 1) / MVT_CHUNK;
+  const uint32_t rows = blockIdx.x < n ? (n - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+  const uint32_t items = rows * chunks;
+  if (tid == 0) {
+    for (int s = 0; s < MVT_STAGES; s++) mbar_init(smem_u32(full + s), 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto issue = [&](uint32_t i) {
+    const uint32_t s = i % MVT_STAGES, row = blockIdx.x + (i / chunks) * gridDim.x, c = i % chunks;
+    const uint32_t bytes = min(MVT_CHUNK, n - c * MVT_CHUNK) * 4u;
+    mbar_expect_tx(smem_u32(full + s), bytes);
+    bulk_g2s(smem_u32(ring + s * MVT_CHUNK), F + size_t(row) * n + size_t(c) * MVT_CHUNK, bytes, smem_u32(full + s));
+  };
+  if (tid == 0)
+    for (uint32_t i = 0; i < min(uint32_t(MVT_STAGES), items); i++) issue(i);
+  float acc = 0.0f;
+  double d2 = 0.0, b2 = 0.0;
+  for (uint32_t i = 0; i < items; i++) {
+    const uint32_t s = i % MVT_STAGES, c = i % chunks, row = blockIdx.x + (i / chunks) * gridDim.x;
+    const bool ok = mbar_wait(smem_u32(full + s), (i / MVT_STAGES) & 1u, &g_matvec_err);
+    if (__syncthreads_or(!ok)) break;   // a copy that never lands: every thread stops
+    const uint32_t cnt4 = min(MVT_CHUNK, n - c * MVT_CHUNK) / 4u;
+    const float4* f4 = reinterpret_cast<const float4*>(ring + s * MVT_CHUNK);
+    const float4* b4 = reinterpret_cast<const float4*>(Bin + size_t(c) * MVT_CHUNK);
+    for (uint32_t k = tid; k < cnt4; k += MVT_THREADS) {
+      const float4 f = f4[k], b = __ldg(b4 + k);
+      acc = fmaf(f.x, b.x, acc); acc = fmaf(f.y, b.y, acc); acc = fmaf(f.z, b.z, acc); acc = fmaf(f.w, b.w, acc);
+    }
+    __syncthreads();   // stage s read by every thread: it may be refilled
+    if (tid == 0 && i + MVT_STAGES < items) issue(i + MVT_STAGES);
+    if (c == chunks - 1) {
+      float a = acc;
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if ((tid & 31u) == 0) red[tid >> 5] = a;
+      __syncthreads();
+      if (tid == 0) {
+        float t = 0.0f;
+        for (int w = 0; w < MVT_THREADS / 32; w++) t += red[w];
+        const float b = fmaf(rho[row], t, E[row]);
+        Bout[row] = b;
+        const double dd = double(b) - double(Bin[row]);
+        d2 += dd * dd;
+        b2 += double(b) * double(b);
+      }
+      __syncthreads();
+      acc = 0.0f;
+    }
+  }
+  block_sum2(d2, b2, partials);
+}
+
+uint32_t jacobi_matvec_tma_blocks(uint32_t n) {
+  static int per_sm = 0, sms = 0;
+  if (!per_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_matvec_tma_kernel, MVT_THREADS, MVT_STAGES * MVT_CHUNK * 4);
+    per_sm = std::max(per_sm, 1);
+    sms = std::max(sms, 1);
+  }
+  return std::max(1u, std::min(n, uint32_t(per_sm * sms)));
+}
+
+void launch_jacobi_matvec_tma(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n, double* partials,
+                              uint32_t* n_partials, cudaStream_t st) {
+  const uint32_t blocks = jacobi_matvec_tma_blocks(n);
+  *n_partials = blocks;
+  jacobi_matvec_tma_kernel<<<blocks, MVT_THREADS, MVT_STAGES * MVT_CHUNK * 4, st>>>(F, rho, E, Bin, Bout, n, partials);
+}
+
+uint32_t matvec_error(cudaStream_t st, bool reset) {
+  uint32_t e = 0;
+  cudaMemcpyFromSymbolAsync(&e, g_matvec_err, 4, 0, cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  if (reset && e) {
+    const uint32_t z = 0;
+    cudaMemcpyToSymbolAsync(g_matvec_err, &z, 4, 0, cudaMemcpyHostToDevice, st);
+    cudaStreamSynchronize(st);
+  }
+  return e;
 }
 
 void launch_jacobi_matvec(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n, double* partials,

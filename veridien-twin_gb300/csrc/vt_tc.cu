@@ -18,6 +18,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "vt_async.cuh"
 #include "vt_tc.cuh"
 
 namespace vtk {
@@ -27,33 +28,8 @@ namespace {
 constexpr int TC_THREADS = 128;
 constexpr uint32_t A_BYTES = 128 * 128;   // 128 rows x 128 B
 constexpr uint32_t B_BYTES = 64 * 128;    // 64 rows x 128 B
-constexpr unsigned long long WAIT_CYCLES = 4000000000ull;   // ~2 s at 2 GHz
+using namespace async;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-// bounded wait for the completion of the phase with parity `parity`; false (and *err set) when it runs out
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t* err) {
-  const unsigned long long t0 = clock64();
-  for (;;) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.u32 %0, 1, 0, P;\n}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (clock64() - t0 > WAIT_CYCLES) { atomicOr(err, 1u); return false; }
-  }
-}
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const TcMap* map, int32_t c0, int32_t c1, uint32_t bar) {
   asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
                "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
