@@ -14,7 +14,9 @@ bounded sample of the same frame; the reference itself is JavaScript + WebGPU an
 
   python bench.py --case render:W:H:SPP            one small path-traced frame (two renders), for profilers
   python bench.py --case radiosity:N:PREC:SWEEPS   one 64-RHS radiosity solve capped at SWEEPS sweeps (fp32|bf16|fp8)
-  python bench.py --case radiosity1:N:PREC:SWEEPS  the same with one right-hand side
+  python bench.py --case radiosity1:N:PREC:SWEEPS  the same with one right-hand side (fp32|fp32tma|bf16|fp8)
+  python bench.py --case batch:W:H:SPP:POSES       one 3-camera pose batch (6 instruments, depth 6, sensor on)
+  python bench.py --case calib:W:H:SPP             one calibration forward + backward (3 cameras, depth 3, 4096 nodes)
 """
 import argparse
 import json
@@ -326,6 +328,37 @@ def run_case(spec):
         E = dome.radiosity_rhs(n, P["lamps"], 64, seed=5)
         _, info = solve_radiosity(F, P["rho"], E, precision=prec, tol=1e-5, max_iters=sweeps)
         print(json.dumps({"case": spec, **{k: v for k, v in info.items() if isinstance(v, (int, float))}}))
+    elif kind == "batch":
+        from vtwin import sensor as sensor_mod
+        from vtwin.renderer import TwinRenderer
+
+        w, h, spp, npose = (int(x) for x in a)
+        sc = dome.make_dome_scene(seed=1, width=w, height=h, level=5, with_instruments=6)
+        sc["cameras"] = dome.batched_cameras(seed=3, n=3, width=w, height=h)
+        r = TwinRenderer.create(sc)
+        P = dome.batch_pose_array(dome.instrument_poses(n_poses=npose, n_tools=6, seed=11))
+        for _ in range(2):
+            out = r.render_batch([0, 1, 2], P, spp=spp, max_depth=6, sensor=sensor_mod.unit_radiance_sensor(), use_graph=False)
+        print(json.dumps({"case": spec, **out["stats"]}))
+        r.destroy()
+    elif kind == "calib":
+        from vtwin.renderer import TwinRenderer
+
+        w, h, spp = (int(x) for x in a)
+        sc = dome.make_dome_scene(seed=1, width=w, height=h, level=5)
+        sc["cameras"] = dome.batched_cameras(seed=3, n=3, width=w, height=h)
+        r = TwinRenderer.create(sc)
+        info = r.calib_setup(n_nodes=4096, lamp_samples=16)
+        alb = np.clip(np.array([m["rho"] for m in sc["materials"]], np.float64), 0.05, 1.0)
+        lamp = np.full(info["n_lamps"], 50.0)
+        _, tg = r.calib_forward([0, 1, 2], alb, lamp, spp=spp, max_depth=3)
+        t0 = time.perf_counter()
+        loss, _ = r.calib_forward([0, 1, 2], alb * 0.9, lamp, targets=tg, images=False, spp=spp, max_depth=3)
+        t1 = time.perf_counter()
+        r.calib_backward()
+        t2 = time.perf_counter()
+        print(json.dumps({"case": spec, "loss": loss, "forward_s": t1 - t0, "backward_s": t2 - t1}))
+        r.destroy()
     else:
         raise SystemExit(f"unknown case {spec!r}")
 
