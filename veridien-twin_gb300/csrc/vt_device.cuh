@@ -484,10 +484,24 @@ __device__ __forceinline__ bool trace_phase(const Scene& S, uint32_t root, float
   return false;
 }
 
+// the traversal stack of a lane: its first SH_DEPTH entries in shared memory (entry-major, so a warp's accesses are
+// consecutive words), the rest of the 32 in local memory
+constexpr uint32_t SH_DEPTH = 16;
+struct LaneStack {
+  uint2* sh;           // shared: SH_DEPTH x stride entries of (node, t bits)
+  uint32_t lane, stride;
+  uint2 deep[STACK - SH_DEPTH];
+  __device__ __forceinline__ void set(uint32_t i, uint32_t node, float t) {
+    const uint2 v = make_uint2(node, __float_as_uint(t));
+    if (i < SH_DEPTH) sh[i * stride + lane] = v; else deep[i - SH_DEPTH] = v;
+  }
+  __device__ __forceinline__ uint2 get(uint32_t i) const { return i < SH_DEPTH ? sh[i * stride + lane] : deep[i - SH_DEPTH]; }
+};
+
 // one node visit of the current phase (an iteration of traverse's loop): 0 continue, 1 the phase is finished,
 // 2 an any-hit query found its hit
 template <bool ANY>
-__device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceState& st, uint32_t* stN, float* stT) {
+__device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceState& st, LaneStack& stk) {
   if (++st.visits > MAX_VISITS) { atomicAdd(S.dbg + DBG_VISITS, 1u); return 1; }
   const uint32_t node = st.node;
   const uint32_t inst = st.k < 0 ? MISS : uint32_t(st.k);
@@ -518,8 +532,8 @@ __device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceStat
   if ((t0 < BIG && c0 == 0u && r0 <= node) || (t1 < BIG && c1 == 0u && r1 <= node)) { atomicAdd(S.dbg + DBG_CORRUPT, 1u); return 1; }
   const bool go0 = t0 < BIG, go1 = t1 < BIG;
   if (go0 && go1) {
-    if (t1 < t0) { stN[st.sp] = r0; stT[st.sp] = t0; st.node = r1; }
-    else { stN[st.sp] = r1; stT[st.sp] = t1; st.node = r0; }
+    if (t1 < t0) { stk.set(st.sp, r0, t0); st.node = r1; }
+    else { stk.set(st.sp, r1, t1); st.node = r0; }
     st.sp = min(st.sp + 1u, STACK - 1u);
   } else if (go0) {
     st.node = r0;
@@ -528,7 +542,8 @@ __device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceStat
   } else {
     while (st.sp > 0u) {
       st.sp--;
-      if (stT[st.sp] < st.best.t) { st.node = stN[st.sp]; return 0; }
+      const uint2 e = stk.get(st.sp);
+      if (__uint_as_float(e.y) < st.best.t) { st.node = e.x; return 0; }
     }
     return 1;
   }

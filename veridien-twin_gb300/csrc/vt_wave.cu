@@ -162,8 +162,9 @@ template <int VAR>
 __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
   if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats, (unsigned long long)n);
-  uint32_t stN[STACK];
-  float stT[STACK];
+  __shared__ uint2 stack_sh[SH_DEPTH * WAVE_THREADS];
+  LaneStack stk;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = WAVE_THREADS;
   TraceState st;
   Scene Sl = S;
   float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, co
   };
   while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
     if (!active) continue;
-    const int r = trace_visit<false>(Sl, 0.0f, st, stN, stT);
+    const int r = trace_visit<false>(Sl, 0.0f, st, stk);
     if (r != 0 && !trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, st.k + 1)) finish();
   }
 }
@@ -320,8 +321,9 @@ __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S0, c
   const uint32_t nl = cp.n_light;
   const uint32_t skip0 = ldu(S0.su + 7);
   const uint32_t skip = VAR == WAVE_SHARED ? (skip0 | wb.bc.vary) : skip0;
-  uint32_t stN[STACK];
-  float stT[STACK];
+  __shared__ uint2 stack_sh[SH_DEPTH * WAVE_THREADS];
+  LaneStack stk;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = WAVE_THREADS;
   TraceState st;
   Scene S = S0;
   float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
@@ -366,7 +368,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S0, c
   };
   while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
     if (!active) continue;
-    const int r = trace_visit<true>(S, 0.0f, st, stN, stT);
+    const int r = trace_visit<true>(S, 0.0f, st, stk);
     bool done = r == 2;
     if (r == 1) done = !trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, st.k + 1);
     if (!done) continue;
