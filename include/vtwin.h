@@ -289,8 +289,9 @@ vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* t
  *                radiances, F the node form factors; `jacobi_iters` Jacobi sweeps;
  *   loss         mean over pixels and channels of (I - T)^2 against per-camera target images (FP64 reduction).
  *
- * The backward replays every path from its sample numbers (path-replay backpropagation) and solves the transposed
- * radiosity system lambda = F^T (g_H + rho o lambda) for the nodes' share. Parameters: per-material albedo (RGB, all
+ * The backward differentiates every path (path-replay backpropagation: from its record kept by a wavefront forward,
+ * or by tracing it again from its sample numbers when the records do not fit) and solves the transposed radiosity
+ * system lambda = F^T (g_H + rho o lambda) for the nodes' share. Parameters: per-material albedo (RGB, all
  * in (0, 1]) and per-emitter-triangle radiance. KB4 intrinsics enter through vt_reproj_loss (analytic Jacobians);
  * the image term's dependence on them (through visibility edges) is not differentiated. */
 typedef struct {
@@ -312,6 +313,9 @@ typedef struct {
   const double* lamp;                             /* n_lamps */
   const float* targets;                           /* rgba32f target images of the cameras, concatenated; NULL: keep the last */
   float* images;                                  /* optional out: the rendered images, same layout (host or device) */
+  uint32_t replay;                                /* 1: the backward traces every path again from its sample numbers;
+                                                     0: the forward keeps each path's record (160 B) when they fit in half
+                                                     the free device memory, and replays otherwise */
 } vt_calib_req;
 /* Image loss of the request (and the images). Keeps the state the backward replays. */
 vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* req, double* loss);

@@ -244,3 +244,23 @@ def test_calibration_function_with_torch(rig):
     err_K = np.abs(z.detach().numpy()[-16:] * scale[-16:] - x_true[-16:]) / np.abs(x_true[-16:]).clip(1e-3)
     print(f"\nloss {first:.3e} -> {float(loss):.3e}; intrinsics max rel error {err_K.max():.2e} (start 1e-1)")
     assert float(loss) < 0.05 * first
+
+
+def test_stored_and_replayed_paths_agree(rig):
+    """The wavefront forward that keeps each path's record and the per-pixel forward that the replay backward
+    re-traces compute the same estimator: same images, same gradients."""
+    r, sc, info, t_alb, t_lamp, targets = rig
+    alb = f32(np.clip(t_alb * 1.05, 0.01, 1.0))
+    lamp = f32(t_lamp * 0.95)
+    kw = dict(spp=4, max_depth=3, targets=targets[:2])
+    l_s, im_s = r.calib_forward([0, 1], alb, lamp, replay=False, **kw)
+    ga_s, gl_s = r.calib_backward()
+    l_r, im_r = r.calib_forward([0, 1], alb, lamp, replay=True, **kw)
+    ga_r, gl_r = r.calib_backward()
+    same = np.mean([np.mean(a == b) for a, b in zip(im_s, im_r)])
+    worst = max(np.abs(a - b).max() for a, b in zip(im_s, im_r))
+    print(f"\nstored vs replayed: identical pixels {same:.5f}, worst |diff| {worst:.2e}, loss {l_s:.9e} vs {l_r:.9e}")
+    assert same >= 0.999 and worst <= 1e-5
+    assert abs(l_s - l_r) <= 1e-6 * l_r
+    np.testing.assert_allclose(ga_s, ga_r, rtol=1e-5, atol=1e-9 * np.abs(ga_r).max())
+    np.testing.assert_allclose(gl_s, gl_r, rtol=1e-5, atol=1e-9 * np.abs(gl_r).max())

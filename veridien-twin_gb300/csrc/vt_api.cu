@@ -105,6 +105,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   if (ctx->batch.exec) cudaGraphExecDestroy(ctx->batch.exec);
   for (auto& e : ctx->kev) cudaEventDestroy(e);
   cudaFree(ctx->calib.mem);
+  cudaFree(ctx->calib.records);
   for (float4* p : ctx->calib.image) cudaFree(p);
   for (float4* p : ctx->calib.target) cudaFree(p);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);

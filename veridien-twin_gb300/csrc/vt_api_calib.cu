@@ -219,13 +219,59 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
     if (q->targets) VT_CK(cudaMemcpyAsync(K.target[cam], q->targets + 4 * off, px * 16, cudaMemcpyDefault, ctx->stream));
     off += px;
   }
+  // stored form when every path's record fits in half the free device memory (and replay is not asked for)
+  std::vector<vtk::CamParams> cps;
+  size_t rec_total = 0;
+  K.rec_off.clear();
+  for (uint32_t c = 0; c < q->n_cameras; c++) {
+    cps.push_back(calib_cam(ctx, q->cameras[c], q->spp, q->light_samples, q->seed, q->max_depth));
+    K.rec_off.push_back(rec_total);
+    rec_total += size_t(vtk::tiled_pixels(cps[c].w, cps[c].h, cps[c].tile_w, cps[c].tile_h)) * cps[c].spp;
+  }
+  K.stored = false;
+  uint32_t wave_paths = 0;
+  if (!q->replay) {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    const size_t rec_bytes = vtk::calib_record_bytes(uint32_t(std::min<size_t>(rec_total, 0xffffffffu)));
+    wave_paths = uint32_t(std::min<size_t>(8u << 20, rec_total));
+    const size_t wave_need = vtk::wave_bytes(wave_paths, cps[0].n_light, 0);
+    if (rec_total < 0xffffffffu && rec_bytes + (ctx->wave_cap >= wave_need ? 0 : wave_need) <= fr / 2) {
+      vt_status st = VT_OK;
+      if (K.rec_cap < rec_bytes) {
+        VT_CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(K.records);
+        K.records = nullptr;
+        K.rec_cap = 0;
+        if (cudaMalloc(&K.records, rec_bytes) != cudaSuccess) { cudaGetLastError(); st = VT_ERR_OOM; }
+        else K.rec_cap = rec_bytes;
+      }
+      if (st == VT_OK && ctx->wave_cap < wave_need) {
+        VT_CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->d_wave);
+        ctx->d_wave = nullptr;
+        ctx->wave_cap = 0;
+        if (cudaMalloc(&ctx->d_wave, wave_need) != cudaSuccess) { cudaGetLastError(); st = VT_ERR_OOM; }
+        else ctx->wave_cap = wave_need;
+      }
+      K.stored = st == VT_OK;
+    }
+  }
   double total = 0.0;
   off = 0;
   for (uint32_t c = 0; c < q->n_cameras; c++) {
     const uint32_t cam = q->cameras[c];
-    const vtk::CamParams cp = calib_cam(ctx, cam, q->spp, q->light_samples, q->seed, q->max_depth);
+    const vtk::CamParams& cp = cps[c];
     const vtk::CalibDev C = calib_dev(ctx, cam);
-    const uint32_t nb = vtk::launch_calib(dev_scene(ctx), cp, C, false, std::min<int>(ctx->wave_blocks * 2, int(K.max_partials)), ctx->stream);
+    const int blocks = std::min<int>(ctx->wave_blocks * 2, int(K.max_partials));
+    uint32_t nb;
+    if (K.stored) {
+      const vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, wave_paths, cp.n_light, 0, ctx->d_work);
+      nb = vtk::calib_wave_forward(dev_scene(ctx), cp, C, wb, wave_paths, static_cast<char*>(K.records) + K.rec_off[c] * vtk::calib_record_bytes(1),
+                                   std::min<int>(ctx->wave_blocks, int(K.max_partials)), ctx->stream);
+    } else {
+      nb = vtk::launch_calib(dev_scene(ctx), cp, C, false, blocks, ctx->stream);
+    }
     vtk::launch_sum(K.partials, nb, K.loss, ctx->stream);
     VT_CK(cudaGetLastError());
     double l = 0;
@@ -253,10 +299,15 @@ vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp) {
   VT_CK(cudaMemsetAsync(K.g_alb, 0, size_t(K.n_mat) * 24, ctx->stream));
   VT_CK(cudaMemsetAsync(K.g_lamp, 0, size_t(K.n_lamps) * 8, ctx->stream));
   VT_CK(cudaMemsetAsync(K.g_H, 0, n * 24, ctx->stream));
-  // path replay over every camera of the forward
-  for (uint32_t cam : K.cams) {
+  // every camera of the forward: from the kept records, or by tracing each path again
+  for (size_t c = 0; c < K.cams.size(); c++) {
+    const uint32_t cam = K.cams[c];
     const vtk::CamParams cp = calib_cam(ctx, cam, K.spp, K.nl, K.seed, K.depth);
-    vtk::launch_calib(dev_scene(ctx), cp, calib_dev(ctx, cam), true, ctx->wave_blocks * 2, ctx->stream);
+    if (K.stored)
+      vtk::calib_records_backward(cp, calib_dev(ctx, cam), static_cast<char*>(K.records) + K.rec_off[c] * vtk::calib_record_bytes(1),
+                                  ctx->wave_blocks * 2, ctx->stream);
+    else
+      vtk::launch_calib(dev_scene(ctx), cp, calib_dev(ctx, cam), true, ctx->wave_blocks * 2, ctx->stream);
   }
   VT_CK(cudaGetLastError());
   // transposed Jacobi: lambda = F^T (g_H + rho o lambda) per channel, from lambda = 0

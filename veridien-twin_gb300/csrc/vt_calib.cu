@@ -17,12 +17,26 @@
 
 #include "vt_calib.cuh"
 #include "vt_camera.cuh"
+#include "vt_wave.cuh"
 
 namespace vtk {
 using namespace vtd;
 
 namespace {
 constexpr int CT = 128;
+
+// append `want` lanes' items to a queue with one atomic per warp; returns the slot of this lane (if want)
+__device__ __forceinline__ uint32_t warp_append_c(uint32_t* count, bool want) {
+  const uint32_t act = __activemask();
+  const uint32_t mask = __ballot_sync(act, want);
+  if (!mask) return 0;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, uint32_t(__popc(mask)));
+  base = __shfl_sync(act, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
 
 struct CalVertex {
   uint32_t mat;
@@ -208,6 +222,201 @@ __device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, u
   }
 }
 
+// ------------------------------------------------------------------------------------ wavefront form, stored paths
+// The same estimator as calib_path, split like the path tracer: the closest-hit kernel of the wavefront, then
+// calib_shade (one vertex: the record of the vertex, its light samples' unshadowed contributions and shadow
+// segments, the cosine continuation), then calib_shadow (any hit per light sample; an occluded sample's contribution
+// is cleared in the record). Each path's record (CalPath) stays in HBM, so the backward evaluates path_grad on the
+// records without tracing again. Records of path (i, id) of a camera sit at rec[i n_pix + id].
+constexpr int WT = 256;
+
+__global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const CamParams cp, const CalibDev C, WaveBufs wb, CalPath* rec,
+                                                        uint32_t b) {
+  const uint32_t n = *wb.count_in;
+  const uint32_t nl = cp.n_light;
+  const float fnl = float(nl);
+  const float area = __ldg(S.su + 3);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = wb.q_in[k];
+    CalPath& P = rec[p];
+    if (b == 1) { P.n = 0; P.emit_lamp = MISS; P.emit_a = 0.0f; P.node = MISS; }
+    const uint4 meta = wb.meta[p];
+    const uint32_t i = meta.y, hs = meta.z;
+    const float4 o4 = wb.o[p], d4 = wb.d[p], hv = wb.hit[p];
+    const float3 o = xyz(o4), d = xyz(d4);
+    const float tt = o4.w, pb_prev = d4.w;
+    const Hit h{hv.x, hv.y, hv.z, __float_as_uint(hv.w), wb.hinst[p]};
+    bool cont = false, shadow = false;
+    if (h.tri != MISS) {
+      const Surf s = surface(S, h, o, d, tt);
+      if (s.flags & VT_F_EMITTER) {
+        const float3 nE = emitter_normal(S, h, s, tt);
+        const float cosE = dot(-d, nE);
+        if (cosE > 0.0f) {
+          const float prof = profile(S, acosf(clampf(dot(-d, emitter_axis_at(S, tt)), -1.0f, 1.0f)));
+          float w = 1.0f;
+          if (b > 1) {
+            const float pL = h.t * h.t / (cosE * area);
+            w = pb_prev * pb_prev / (pb_prev * pb_prev + fnl * fnl * pL * pL);
+          }
+          P.emit_lamp = __ldg(C.emit_of_tri + h.tri);
+          P.emit_a = w * prof;
+        }
+      } else {
+        const uint32_t vk = P.n;
+        CalVertex& V = P.v[vk];
+        V.mat = s.mat;
+        P.n = vk + 1;
+        const float3 nrm = s.ns, wo = -d;
+        const float sh0 = b == 1 ? u01(pcg(hs + 3u)) : bounce_shift(hs, b, 0);
+        const float sh1 = b == 1 ? u01(pcg(hs + 4u)) : bounce_shift(hs, b, 1);
+        const float sh2 = b == 1 ? u01(pcg(hs + 5u)) : bounce_shift(hs, b, 2);
+        float4* srec = wb.sh + size_t(p) * nl * 3;
+        for (uint32_t j = 0; j < nl; j++) {
+          const float3 u = f3(kr(i * nl + j, KL0, sh0), kr(i * nl + j, KL1, sh1), kr(i * nl + j, KL2, sh2));
+          float3 lp, ln, la;
+          V.lamp[j] = sample_emitter_idx(S, u, tt, lp, ln, la);
+          V.q[j] = 0.0f;
+          srec[3 * j + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          float3 wi = lp - s.p;
+          const float d2 = dot(wi, wi), dist = sqrtf(d2);
+          wi = wi / dist;
+          const float cosE = dot(-wi, ln), cosS = dot(nrm, wi);
+          if (cosE <= 0.0f || cosS <= 0.0f || dot(s.ng, wi) <= 0.0f || dot(nrm, wo) <= 0.0f) continue;
+          const float prof = profile(S, acosf(clampf(dot(-wi, la), -1.0f, 1.0f)));
+          if (prof <= 0.0f) continue;
+          const float pdfW = d2 / (cosE * area), pb = cosS * INV_PI_F;
+          const float w = fnl * fnl * pdfW * pdfW / (fnl * fnl * pdfW * pdfW + pb * pb);
+          V.q[j] = prof * cosS * w * INV_PI_F / pdfW;
+          const float3 so = offset_ray(s.p, s.ng, wi);
+          srec[3 * j] = make_float4(so.x, so.y, so.z, dist - 2e-5f);
+          srec[3 * j + 1] = make_float4(wi.x, wi.y, wi.z, 1.0f);
+          srec[3 * j + 2] = make_float4(0.0f, 0.0f, __uint_as_float(vk), 0.0f);
+          shadow = true;
+        }
+        if (shadow) wb.nee[p] = make_float4(0.0f, 0.0f, 0.0f, tt);
+        if (b == cp.max_depth) {
+          if (h.inst == MISS && h.tri < C.n_static_tris) P.node = __ldg(C.tri_node + h.tri);
+        } else if (dot(nrm, wo) > 0.0f) {
+          const float u1 = b == 1 ? kr(i, KB1, u01(pcg(hs + 7u))) : kr(i, KB1, bounce_shift(hs, b, 4));
+          const float u2 = b == 1 ? kr(i, KB2, u01(pcg(hs + 8u))) : kr(i, KB2, bounce_shift(hs, b, 5));
+          const float3 t = basis_t(nrm), bb = basis_b(nrm);
+          const float r = sqrtf(u1);
+          float sp, cpz;
+          sincosf(2.0f * PI_F * u2, &sp, &cpz);
+          const float3 l = t * (r * cpz) + bb * (r * sp) + nrm * sqrtf(fmaxf(0.0f, 1.0f - u1));
+          const float cl = dot(nrm, l);
+          if (cl > 0.0f && dot(s.ng, l) > 0.0f) {
+            const float3 no = offset_ray(s.p, s.ng, l);
+            wb.o[p] = make_float4(no.x, no.y, no.z, tt);
+            wb.d[p] = make_float4(l.x, l.y, l.z, cl * INV_PI_F);
+            wb.meta[p] = make_uint4(meta.x, meta.y, meta.z, b + 1u);
+            cont = true;
+          }
+        }
+      }
+    }
+    const uint32_t qs = warp_append_c(wb.count_out, cont);
+    if (cont) wb.q_out[qs] = p;
+    const uint32_t ss = warp_append_c(wb.count_sh, shadow);
+    if (shadow) wb.q_sh[ss] = p;
+  }
+}
+
+// any hit of the pending light samples on persistent lanes; an occluded sample's contribution is cleared in the record
+__global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, const CamParams cp, WaveBufs wb, CalPath* rec) {
+  const uint32_t n = *wb.count_sh;
+  const uint32_t nl = cp.n_light;
+  const uint32_t skip = ldu(S.su + 7);
+  __shared__ uint2 stack_sh[SH_DEPTH * WT];
+  LaneStack stk;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = WT;
+  TraceState st;
+  float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
+  float tt = 0.0f;
+  uint32_t p = 0, j = 0;
+  bool active = false, exhausted = false;
+  const float4* srec = nullptr;
+  auto next_sample = [&]() -> bool {
+    for (; j < nl; j++) {
+      const float4 a = srec[3 * j], w = srec[3 * j + 1];
+      if (w.w == 0.0f) continue;
+      o = xyz(a); d = xyz(w);
+      st.best = Hit{a.w, 0.0f, 0.0f, MISS, MISS};
+      if (trace_phase(S, cp.root, o, d, 0.0f, tt, 3u, skip, st, -1)) return true;
+    }
+    return false;
+  };
+  auto start = [&](uint32_t idx) {
+    p = wb.q_sh[idx];
+    tt = wb.nee[p].w;
+    srec = wb.sh + size_t(p) * nl * 3;
+    j = 0;
+    active = next_sample();
+  };
+  while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
+    if (!active) continue;
+    const int r = trace_visit<true>(S, 0.0f, st, stk);
+    bool done = r == 2;
+    if (r == 1) done = !trace_phase(S, cp.root, o, d, 0.0f, tt, 3u, skip, st, st.k + 1);
+    if (!done) continue;
+    if (st.best.tri != MISS) rec[p].v[__float_as_uint(srec[3 * j + 2].z)].q[j] = 0.0f;
+    j++;
+    active = next_sample();
+  }
+}
+
+// per pixel: the image value from the records in sub-sample order, its loss partial (forward); or the gradient of
+// every record (backward)
+__global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, const CalibDev C, const CalPath* __restrict__ rec, uint32_t n_pix,
+                                                          int backward) {
+  extern __shared__ double sm[];
+  double* sh_alb = sm;
+  double* sh_lamp = sm + 3 * C.n_mat;
+  __shared__ double red[CT / 32];
+  if (backward) {
+    for (uint32_t k = threadIdx.x; k < 3 * C.n_mat + C.n_lamps; k += blockDim.x) sm[k] = 0.0;
+    __syncthreads();
+  }
+  double loss = 0.0;
+  const float sc = cp.scale / float(cp.spp);
+  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n_pix; id += gridDim.x * blockDim.x) {
+    uint32_t x, y;
+    if (!pixel_xy(cp, id, x, y)) continue;
+    const size_t px = size_t(y) * cp.w + x;
+    if (backward) {
+      const float4 I = C.image[px], Tg = C.target ? C.target[px] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const double k = 2.0 * C.inv_count * double(sc);
+      const double3 g = make_double3(k * (double(I.x) - Tg.x), k * (double(I.y) - Tg.y), k * (double(I.z) - Tg.z));
+      for (uint32_t i = 0; i < cp.spp; i++) path_grad(C, rec[size_t(i) * n_pix + id], cp.n_light, g, sh_alb, sh_lamp);
+    } else {
+      float3 s = f3(0, 0, 0);
+      for (uint32_t i = 0; i < cp.spp; i++) s = s + path_value(C, rec[size_t(i) * n_pix + id], cp.n_light);
+      const float4 I = make_float4(s.x * sc, s.y * sc, s.z * sc, 1.0f);
+      C.image[px] = I;
+      if (C.target) {
+        const float4 Tg = C.target[px];
+        const double dx = double(I.x) - Tg.x, dy = double(I.y) - Tg.y, dz = double(I.z) - Tg.z;
+        loss += dx * dx + dy * dy + dz * dz;
+      }
+    }
+  }
+  if (backward) {
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < 3 * C.n_mat; k += blockDim.x) if (sm[k] != 0.0) atomicAdd(C.g_albedo + k, sm[k]);
+    for (uint32_t k = threadIdx.x; k < C.n_lamps; k += blockDim.x) if (sh_lamp[k] != 0.0) atomicAdd(C.g_lamp + k, sh_lamp[k]);
+    return;
+  }
+  for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < CT / 32; w++) t += red[w];
+    C.partials[blockIdx.x] = t * C.inv_count;
+  }
+}
+
 __global__ void __launch_bounds__(CT) calib_kernel(const Scene S, const CamParams cp, const CalibDev C, uint32_t n_pix, int backward) {
   extern __shared__ double sm[];
   double* sh_alb = sm;                       // n_mat x 3
@@ -371,6 +580,44 @@ __global__ void sum_kernel(const double* __restrict__ p, uint32_t n, double* __r
   if (threadIdx.x == 0) *out = s[0];
 }
 }  // namespace
+
+size_t calib_record_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalPath); }
+
+uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records, int blocks,
+                            cudaStream_t st) {
+  CalPath* rec = static_cast<CalPath*>(records);
+  const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
+  const uint32_t per_wave = std::max(1u, std::min(cp.spp, wave_paths / std::max(1u, n_pix)));
+  for (uint32_t i0 = 0; i0 < cp.spp; i0 += per_wave) {
+    const uint32_t n_i = std::min(per_wave, cp.spp - i0);
+    cudaMemsetAsync(wb.counts, 0, 16, st);
+    launch_wave_gen(cp, wb, i0, n_i, n_pix, blocks, st);
+    CalPath* rb = rec + size_t(i0) * n_pix;
+    for (uint32_t b = 1; b <= cp.max_depth; b++) {
+      WaveBufs w = wb;
+      w.q_in = (b & 1) ? wb.qa : wb.qb;
+      w.q_out = (b & 1) ? wb.qb : wb.qa;
+      w.count_in = wb.counts + ((b & 1) ? 0 : 1);
+      w.count_out = wb.counts + ((b & 1) ? 1 : 0);
+      w.count_sh = wb.counts + 2;
+      cudaMemsetAsync(w.count_out, 0, 4, st);
+      cudaMemsetAsync(w.count_sh, 0, 4, st);
+      launch_wave_extend(S, cp, w, blocks, st);
+      calib_shade_kernel<<<blocks, WT, 0, st>>>(S, cp, C, w, rb, b);
+      cudaMemsetAsync(w.fetch, 0, 4, st);
+      calib_shadow_kernel<<<blocks, WT, 0, st>>>(S, cp, w, rb);
+    }
+  }
+  const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
+  calib_records_kernel<<<grid, CT, 0, st>>>(cp, C, rec, n_pix, 0);
+  return grid;
+}
+
+void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* records, int blocks, cudaStream_t st) {
+  const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
+  const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
+  calib_records_kernel<<<grid, CT, size_t(3 * C.n_mat + C.n_lamps) * 8, st>>>(cp, C, static_cast<const CalPath*>(records), n_pix, 1);
+}
 
 uint32_t launch_calib(const Scene& S, const CamParams& cp, const CalibDev& C, bool backward, int blocks, cudaStream_t st) {
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);

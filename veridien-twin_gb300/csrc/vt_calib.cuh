@@ -2,7 +2,7 @@
 // radiosity pieces of the calibration model (direct transfer from the emitter triangles, transposed Jacobi).
 #pragma once
 
-#include "vt_kernels.cuh"
+#include "vt_wave.cuh"
 
 namespace vtk {
 
@@ -25,7 +25,15 @@ struct CalibDev {
   double* g_H;                  // 3 x n_nodes
 };
 
-// forward: image + per-block loss partials (returns the number of partials); backward: gradients of the image loss
+// stored-path form: the wavefront forward of one camera (records of all its paths kept, path (i, id) at
+// records[i n_pix + id]), the image and per-block loss partials (returns their number); and the backward from the
+// records, without tracing
+size_t calib_record_bytes(uint32_t paths);
+uint32_t calib_wave_forward(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records,
+                            int blocks, cudaStream_t st);
+void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* records, int blocks, cudaStream_t st);
+// replay form, forward: image + per-block loss partials (returns the number of partials); backward: gradients of the
+// image loss, every path traced again from its sample numbers
 uint32_t launch_calib(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, bool backward, int blocks, cudaStream_t st);
 // D[i][t]: irradiance at node i (centre, normal) from emitter triangle t at unit radiance, with visibility
 void launch_direct_transfer(const vtd::Scene& S, const float* centres, const float* normals, uint32_t n, uint32_t n_lamps,

@@ -84,6 +84,11 @@ struct vt_ctx {
     uint32_t max_partials = 0;
     std::vector<float4*> image, target;   // per scene camera (device, w x h)
     std::vector<std::vector<float>> albedo_host;
+    // path records of the last forward (stored form), per camera of the request
+    void* records = nullptr;
+    size_t rec_cap = 0;
+    std::vector<size_t> rec_off;
+    bool stored = false;
     // last forward
     std::vector<uint32_t> cams;
     uint32_t spp = 0, nl = 0, seed = 0, depth = 0, iters = 0;

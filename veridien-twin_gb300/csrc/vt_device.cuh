@@ -550,6 +550,27 @@ __device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceStat
   return 0;
 }
 
+// Persistent traversal lanes: every lane keeps one ray in flight, one node visit per loop iteration; once `refill`
+// lanes of the warp are idle they take the next queue entries with one atomic. Lanes stay busy until the queue
+// drains instead of waiting for the warp's slowest ray (warp-level ray compaction).
+template <typename F>
+__device__ __forceinline__ bool take_rays(bool& active, bool& exhausted, uint32_t* head, uint32_t n, uint32_t refill, F&& start) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+  if (!exhausted && idle && (__popc(idle) >= int(refill) || idle == 0xffffffffu)) {
+    const uint32_t leader = __ffs(idle) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(head, uint32_t(__popc(idle)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (base + uint32_t(__popc(idle)) >= n) exhausted = true;
+    if (!active) {
+      const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
+      if (idx < n) start(idx);
+    }
+  }
+  return __any_sync(0xffffffffu, active) || !exhausted;
+}
+
 // ------------------------------------------------------------------------------------------------ surfaces
 struct Surf { float3 p, ng, ns, b; uint32_t vi0, vi1, vi2, mesh, flags, mat, inst; };
 

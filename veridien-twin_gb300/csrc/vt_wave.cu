@@ -137,27 +137,6 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_gen_pairs_kernel(const CamP
   }
 }
 
-// Persistent traversal lanes: every lane keeps one ray in flight, one node visit per loop iteration; once `refill`
-// lanes of the warp are idle they take the next queue entries with one atomic. Lanes stay busy until the queue
-// drains instead of waiting for the warp's slowest ray (warp-level ray compaction).
-template <typename F>
-__device__ __forceinline__ bool take_rays(bool& active, bool& exhausted, uint32_t* head, uint32_t n, uint32_t refill, F&& start) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t idle = __ballot_sync(0xffffffffu, !active);
-  if (!exhausted && idle && (__popc(idle) >= int(refill) || idle == 0xffffffffu)) {
-    const uint32_t leader = __ffs(idle) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(head, uint32_t(__popc(idle)));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (base + uint32_t(__popc(idle)) >= n) exhausted = true;
-    if (!active) {
-      const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
-      if (idx < n) start(idx);
-    }
-  }
-  return __any_sync(0xffffffffu, active) || !exhausted;
-}
-
 template <int VAR>
 __global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
@@ -482,6 +461,17 @@ void wave_bounces(const Scene& S, const CamParams& cp, WaveBufs wb, int var, int
     else bounce_kernels<WAVE_PLAIN>(S, cp, w, blocks, st, timer);
     if (launches) *launches += 3;
   }
+}
+
+void launch_wave_extend(const Scene& S, const CamParams& cp, const WaveBufs& wb, int blocks, cudaStream_t st) {
+  cudaMemsetAsync(wb.fetch, 0, 4, st);
+  wave_extend<WAVE_PLAIN><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, wb);
+}
+
+void launch_wave_gen(const CamParams& cp, WaveBufs wb, uint32_t i0, uint32_t n_i, uint32_t n_pix, int blocks, cudaStream_t st) {
+  wb.q_in = wb.qa;
+  wb.count_in = wb.counts;
+  wave_gen<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb, i0, n_i, n_pix);
 }
 
 void wave_gen_batch(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t st) {

@@ -71,6 +71,10 @@ int wave_blocks_per_sm();
 // one wave's bounces (extend, shade, shadow per bounce) over the paths queued in wb.qa / counts[0]
 void wave_bounces(const vtd::Scene& S, const CamParams& cp, WaveBufs wb, int var, int blocks, cudaStream_t st, uint64_t* launches,
                   KernelTimer* timer = nullptr);
+// the closest-hit kernel over wb.qa / counts (plain scene) and the camera rays of sub-samples [i0, i0 + n_i) of all
+// n_pix pixel ids (path p = (i - i0) n_pix + id), queued in wb.qa / counts[0]
+void launch_wave_extend(const vtd::Scene& S, const CamParams& cp, const WaveBufs& wb, int blocks, cudaStream_t st);
+void launch_wave_gen(const CamParams& cp, WaveBufs wb, uint32_t i0, uint32_t n_i, uint32_t n_pix, int blocks, cudaStream_t st);
 // camera rays of a batch wave: paths p = i * n_pw + lp, i < spp, pixel id px0 + lp; clears the dirty masks
 void wave_gen_batch(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t st);
 // camera rays of the pair paths (pair j repeats shared path pair_src[j]); count in counts[0]

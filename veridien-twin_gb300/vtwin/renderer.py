@@ -296,7 +296,7 @@ class TwinRenderer:
         return out
 
     def calib_forward(self, cameras, albedo, lamp, spp=32, lightSamples=1, seed=0, max_depth=3, jacobi_iters=0, targets=None,
-                      images=True):
+                      images=True, replay=False):
         """Image loss (mean of (I - T)^2 over pixels and channels) of the calibration render; returns (loss, images)
         with images a list of (h, w, 4) float32 arrays per camera (or None)."""
         cams = [self._cam(c) for c in cameras]
@@ -313,7 +313,7 @@ class TwinRenderer:
                            light_samples=int(lightSamples), seed=int(seed), max_depth=int(max_depth), jacobi_iters=int(jacobi_iters),
                            albedo=alb.ctypes.data_as(C.POINTER(C.c_double)), lamp=lam.ctypes.data_as(C.POINTER(C.c_double)),
                            targets=tg.ctypes.data_as(C.POINTER(C.c_float)) if tg is not None else None,
-                           images=img.ctypes.data_as(C.POINTER(C.c_float)) if img is not None else None)
+                           images=img.ctypes.data_as(C.POINTER(C.c_float)) if img is not None else None, replay=int(bool(replay)))
         loss = C.c_double(0.0)
         check(self.lib.vt_calib_forward(self._ctx, C.byref(q), C.byref(loss)), self._ctx)
         out = None
