@@ -4,7 +4,7 @@
 //
 // PARITY UNPINNED: the reference is JavaScript + WGSL. Neither runs on this machine or the GPU machine (no node, no
 // WebGPU), and the reference carries no golden vectors for this path (its hot-path tests are not in the tree).
-// This restatement is anchored instead on the reference's own stated known answers: brute force judges the BVH
+// This restatement is anchored instead on the reference's own stated known answers: brute force checks the BVH
 // (gpu/bvh.js:3, :253), the KB4 round trip (gpu/lens.js:43-62), the Gauss-Legendre disc irradiance
 // (gpu/shade_ref.js:40-62), fresnelAverage by Simpson (gpu/bsdf.js:34-42), the furnace test and the direct FP64
 // linear solve of the radiosity.

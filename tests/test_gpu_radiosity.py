@@ -1,6 +1,6 @@
 """Mixed-precision node radiosity (tcgen05 BF16 / FP8 sweeps + iterative refinement) against a direct FP64 solve.
 
-The bar (the benchmark spec): at most 1e-4 relative error against FP64, for one and for many right-hand sides.
+The bar: at most 1e-4 relative error against FP64, for one and for many right-hand sides.
 """
 import numpy as np
 import pytest

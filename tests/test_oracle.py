@@ -1,7 +1,7 @@
 """The oracle pinned against the reference's known answers (CPU only).
 
 Golden vectors from the reference's own configuration (tests/golden/physics_kat.json, made by make_golden.py),
-and the known-answer methods the reference's source states: brute force judges the BVH (gpu/bvh.js:3),
+and the known-answer methods the reference's source states: brute force checks the BVH (gpu/bvh.js:3),
 the KB4 round trip (gpu/lens.js:43-62), the Gauss-Legendre disc irradiance (gpu/shade_ref.js:40-62), the
 furnace (tools/gpu_bench.py:7), reciprocity, and the direct FP64 solve of the radiosity.
 """
