@@ -505,11 +505,16 @@ def calib_bench(torch, device=0):
 
 def radiosity_bench(torch, cpu_check=True):
     """Node radiosity B = E + diag(rho) F B on the seeded dome patches, plain FP32 against the mixed-precision solves.
-    C1: N = 4096, one right-hand side, to relative residual 1e-6. C2: N = 32768, 64 right-hand sides (random lamp
-    masks, intensities U[10, 100]), to 1e-4 relative error against FP64 (residual tolerance 1e-5). Device times."""
+    F: disk form factors x each pair's visibility through the dome scene (stratified rays per pair: 64 at C1, 4 at C2
+    to bound the build to seconds), rows scaled to <= 1. C1: N = 4096, one right-hand side, to relative residual 1e-6.
+    C2: N = 32768, 64 right-hand sides (random lamp masks, intensities U[10, 100]), to 1e-4 relative error against
+    FP64 (residual tolerance 1e-5). Device times."""
     from vtwin import _abi as A
     from vtwin import dome
-    from vtwin.renderer import form_factors, solve_radiosity
+    from vtwin.renderer import TwinRenderer, solve_radiosity
+
+    scene_r = TwinRenderer.create(dome.make_dome_scene(seed=1, width=32, height=24, level=5))
+    scene_r.set_pose_array(A.identity_poses(1))
 
     out = {}
     precs = (("fp32", A.VT_PREC_FP32), ("bf16", A.VT_PREC_BF16), ("fp8", A.VT_PREC_FP8))
@@ -519,12 +524,12 @@ def radiosity_bench(torch, cpu_check=True):
     except (OSError, ValueError):
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    for key, n, R, tol in (("c1", 4096, 1, 1e-6), ("c2", 32768, 64, 1e-5)):
+    for key, n, R, tol, K in (("c1", 4096, 1, 1e-6, 64), ("c2", 32768, 64, 1e-5, 4)):
         P = dome.dome_patches(n, seed=2)
         F = torch.empty((n, n), dtype=torch.float32, device="cuda")
-        form_factors(P["centres"], P["normals"], P["areas"], out=F)
+        scene_r.form_factors_visible(P["centres"], P["normals"], P["areas"], rays=K, out=F)
         E = dome.radiosity_rhs(n, P["lamps"], R, seed=5)
-        res = {"n": n, "rhs": R, "tol": tol}
+        res = {"n": n, "rhs": R, "tol": tol, "F": {"rays_per_pair": K, "build_ms": scene_r.timings()["trace_ms"]}}
         sols = {}
         for name, prec in precs:
             solve_radiosity(F, P["rho"], E, precision=prec, tol=tol, max_iters=400)          # warm; converts F once
@@ -544,6 +549,7 @@ def radiosity_bench(torch, cpu_check=True):
         out[key] = res
         del F
         torch.cuda.empty_cache()
+    scene_r.destroy()
     return out
 
 

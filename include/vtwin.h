@@ -370,6 +370,12 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* req);
  * n x n row-major. Unoccluded (the scene's visibility is not applied). */
 vt_status vt_form_factors(vt_ctx* ctx, uint32_t n, const float* centres, const float* normals, const float* areas,
                           float* F);
+/* The same with visibility through the context's scene (static BVH and posed bodies at their current poses, the
+ * emitter body not occluding): F_ij x V_ij, V_ij the fraction of `rays` (1..255) stratified rays between the two
+ * patch discs (half radius, lifted 5 mm + a tenth of it) that nothing blocks, then rows scaled to <= 1; n <= 65535
+ * (gpu/wgsl/kernels.wgsl.js:271 gatherDir, dense). */
+vt_status vt_form_factors_visible(vt_ctx* ctx, uint32_t n, const float* centres, const float* normals, const float* areas, uint32_t rays,
+                                  float* F);
 
 /* One-right-hand-side node radiosity (B = E + diag(rho) F B, plain FP32 Jacobi as vt_radiosity_solve) that allocates
  * no device memory. No counterpart in the reference. For callers that cannot allocate while they run: a per-frame

@@ -35,7 +35,7 @@ def lib():
         _lib.or_scene_create.argtypes = [C.c_void_p, C.c_int, C.c_int]
         for nm in ("or_scene_destroy", "or_scene_sizes", "or_scene_arrays", "or_scene_emitter", "or_scene_blas",
                    "or_scene_set_poses", "or_scene_set_eavg", "or_scene_uniform", "or_scene_set_node_state",
-                   "or_trace_wgsl", "or_render", "or_calib_render", "or_direct_transfer"):
+                   "or_trace_wgsl", "or_render", "or_calib_render", "or_direct_transfer", "or_form_factors_visible"):
             getattr(_lib, nm).restype = None
         _lib.or_fresnel_average.restype = C.c_double
         _lib.or_disc_irradiance.restype = C.c_double
@@ -254,6 +254,18 @@ class Scene:
         lib().or_direct_transfer(self.h, _p(Cn, C.c_float), _p(Nn, C.c_float), C.c_uint32(n), C.c_uint32(samples), int(fp64), int(threads),
                                  _p(D))
         return D
+
+    def form_factors_visible(self, centres, normals, areas, rays=16, fp64=True, threads=1):
+        """Dense node form factors with visibility through this scene (n x n float32) and the visible-ray counts."""
+        Cn = np.ascontiguousarray(centres, np.float32)
+        Nn = np.ascontiguousarray(normals, np.float32)
+        An = np.ascontiguousarray(areas, np.float32)
+        n = len(Cn)
+        F = np.zeros((n, n), np.float32)
+        cnt = np.zeros((n, n), np.uint8)
+        lib().or_form_factors_visible(self.h, n, _p(Cn, C.c_float), _p(Nn, C.c_float), _p(An, C.c_float), int(rays), int(fp64), int(threads),
+                                      _p(F, C.c_float), _p(cnt, C.c_uint8))
+        return F, cnt
 
 
 def calib_radiosity(F, D, lamp, albedo, node_mat):

@@ -2277,6 +2277,75 @@ void or_direct_transfer(void* h, const float* C, const float* N, uint32_t n, uin
 }
 uint32_t or_scene_emit_count(void* h) { return static_cast<Scene*>(h)->emitN; }
 
+// dense form factors with visibility through the scene, restated: disk form factor of the centres x the fraction
+// of K rays between the two patch discs (half radius, Kronecker sample k on each disc with its own shift, lifted
+// 5 mm + a tenth of the half radius) that no surface blocks (the emitter body does not occlude); each unordered
+// pair traced once; rows
+// scaled to a sum <= 1 in FP64
+void or_form_factors_visible(void* h, int n, const float* C, const float* Nn, const float* A, int K, int fp64, int threads, float* F,
+                             uint8_t* counts) {
+  Scene* S = static_cast<Scene*>(h);
+  std::vector<Dbg> dbgs(std::max(1, threads));
+  std::atomic<int> next(0);
+  auto work = [&](int t) {
+    auto run = [&](auto tag) {
+      using R = decltype(tag);
+      Tracer<R> tr(*S, dbgs[t]);
+      auto disc = [&](int i, float u, float v) {
+        V3<R> c = ld3<R>(C + 3 * i), nn = ld3<R>(Nn + 3 * i);
+        R rh = R(0.5) * std::sqrt(R(A[i]) * R(INV_PI_D)), r = rh * std::sqrt(R(u));
+        R ph = R(2) * R(M_PI) * R(v);
+        return c + basis_t(nn) * (r * std::cos(ph)) + basis_b(nn) * (r * std::sin(ph)) + nn * (R(5e-3) + R(0.1) * rh);
+      };
+      for (;;) {
+        int i = next.fetch_add(1);
+        if (i >= n) break;
+        for (int j = i + 1; j < n; j++) {
+          float wx = C[3 * j] - C[3 * i], wy = C[3 * j + 1] - C[3 * i + 1], wz = C[3 * j + 2] - C[3 * i + 2];
+          bool face = Nn[3 * i] * wx + Nn[3 * i + 1] * wy + Nn[3 * i + 2] * wz > 0.0f && Nn[3 * j] * wx + Nn[3 * j + 1] * wy + Nn[3 * j + 2] * wz < 0.0f;
+          int vis = 0;
+          if (face) {
+            for (int k = 0; k < K; k++) {
+              V3<R> a = disc(i, kr(k, R2A, 0.5f), kr(k, R2B, 0.5f)), b = disc(j, kr(k, R2A, 0.25f), kr(k, R2B, 0.75f));
+              V3<R> w = b - a;
+              R dist = len(w);
+              if (!(dist > R(2e-4))) { vis++; continue; }
+              Hit<R> hh = tr.trace(a, w / dist, R(0), dist - R(1e-4), R(0.5), true, 3u, tr.su_u(7));
+              if (hh.tri == MISS) vis++;
+            }
+          }
+          counts[size_t(i) * n + j] = counts[size_t(j) * n + i] = uint8_t(vis);
+        }
+      }
+    };
+    if (fp64) run(double(0)); else run(float(0));
+  };
+  for (int i = 0; i < n; i++) counts[size_t(i) * n + i] = 0;
+  if (threads <= 1) work(0);
+  else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; t++) th.emplace_back(work, t);
+    for (auto& x : th) x.join();
+  }
+  for (int i = 0; i < n; i++) {
+    std::vector<double> row(n, 0.0);
+    double s = 0;
+    for (int j = 0; j < n; j++) {
+      if (j == i || !counts[size_t(i) * n + j]) continue;
+      double wx = double(C[3 * j]) - C[3 * i], wy = double(C[3 * j + 1]) - C[3 * i + 1], wz = double(C[3 * j + 2]) - C[3 * i + 2];
+      double r2 = wx * wx + wy * wy + wz * wz, r = std::sqrt(r2);
+      if (!(r > 0)) continue;
+      double ci = (Nn[3 * i] * wx + Nn[3 * i + 1] * wy + Nn[3 * i + 2] * wz) / r;
+      double cj = -(Nn[3 * j] * wx + Nn[3 * j + 1] * wy + Nn[3 * j + 2] * wz) / r;
+      if (ci <= 0 || cj <= 0) continue;
+      row[j] = double(A[j]) * ci * cj / (M_PI * r2 + double(A[j])) * (double(counts[size_t(i) * n + j]) / K);
+      s += row[j];
+    }
+    double sc = s > 1.0 ? 1.0 / s : 1.0;
+    for (int j = 0; j < n; j++) F[size_t(i) * n + j] = float(row[j] * sc);
+  }
+}
+
 void or_sensor_expose(const uint32_t* su, const float* E4, float* raw) { sensor_expose(su, E4, raw); }
 void or_vt_logf(const float* x, int n, float* out) { for (int i = 0; i < n; i++) out[i] = vt_logf(x[i]); }
 void or_vt_expf(const float* x, int n, float* out) { for (int i = 0; i < n; i++) out[i] = vt_expf(x[i]); }

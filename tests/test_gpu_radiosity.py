@@ -45,3 +45,34 @@ def test_reuse_of_converted_f(system):
     B2, i2 = r.solve_radiosity(F, P["rho"], E, precision=A.VT_PREC_BF16, tol=1e-6, reuse_f=True)
     assert np.array_equal(B1, B2) and i1["iters"] == i2["iters"]
     r.destroy()
+
+
+def test_form_factors_with_visibility_match_oracle():
+    """Dense F with each pair's visibility traced through the dome scene (the table occludes floor-to-floor and
+    floor-to-dome pairs) against the FP64 restatement: the visible-ray counts agree on nearly every pair (shadow
+    decisions at grazing rays may flip between float32 and float64), rows sum to <= 1, and F is below the
+    unoccluded F."""
+    from vtwin.renderer import TwinRenderer
+
+    sc = dome.make_dome_scene(seed=1, width=32, height=24, level=5)
+    r = TwinRenderer.create(sc)
+    r.set_pose_array(A.identity_poses(1))
+    n, K = 384, 16
+    P = dome.dome_patches(n, seed=2)
+    F = r.form_factors_visible(P["centres"], P["normals"], P["areas"], rays=K)
+    S = O.Scene(sc)
+    S.set_poses()
+    F64, cnt = S.form_factors_visible(P["centres"], P["normals"], P["areas"], rays=K, fp64=True, threads=16)
+    F0 = form_factors(P["centres"], P["normals"], P["areas"])
+    facing = F0 > 0
+    occluded = np.mean(cnt[facing] < K)
+    row = np.abs(F - F64).sum(axis=1) / np.maximum(F64.sum(axis=1), 1e-30)
+    whole = np.abs(F - F64).sum() / F64.sum()
+    print(f"\nvisibility: {occluded:.3f} of facing pairs partly occluded; relative L1 difference {whole:.2e} overall, "
+          f"rows within 1e-2: {np.mean(row <= 1e-2):.4f}, worst row {row.max():.2e}")
+    assert occluded > 0.01
+    # a ray that flips between float32 and float64 moves one entry by 1/K (and its row's scale)
+    assert whole <= 1e-3 and np.mean(row <= 1e-2) >= 0.98
+    assert np.all(F.sum(axis=1) <= 1 + 1e-5)
+    assert np.all(F.sum(axis=1) <= F0.sum(axis=1) * (1 + 1e-5) + 1e-7)   # occlusion only takes light away
+    r.destroy()

@@ -418,6 +418,35 @@ vt_status vt_form_factors(vt_ctx* ctx, uint32_t n, const float* centres, const f
   return VT_OK;
 }
 
+vt_status vt_form_factors_visible(vt_ctx* ctx, uint32_t n, const float* centres, const float* normals, const float* areas, uint32_t rays,
+                                  float* F) {
+  if (!ctx || !n || !centres || !normals || !areas || !F) return VT_ERR_ARG;
+  if (n > 65535 || rays < 1 || rays > 255) return fail(ctx, VT_ERR_ARG, "form factors: n <= 65535 and 1..255 rays per pair");
+  const size_t nn = size_t(n) * n * 4;
+  const bool dF = is_device_ptr(F);
+  const size_t head = (size_t(n) * 28 + 255) / 256 * 256, cnt = head + 256, out = cnt + (size_t(n) * n + 255) / 256 * 256;
+  vt_status s = ensure_scratch(ctx, out + (dF ? 0 : nn) + 256);
+  if (s != VT_OK) return s;
+  char* base = static_cast<char*>(ctx->d_scratch);
+  float *dC = reinterpret_cast<float*>(base), *dN = dC + 3 * size_t(n), *dA = dN + 3 * size_t(n);
+  if ((s = to_device(ctx, dC, centres, size_t(n) * 12)) != VT_OK) return s;
+  if ((s = to_device(ctx, dN, normals, size_t(n) * 12)) != VT_OK) return s;
+  if ((s = to_device(ctx, dA, areas, size_t(n) * 4)) != VT_OK) return s;
+  float* dOut = dF ? F : reinterpret_cast<float*>(base + out);
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  vtk::launch_form_factors_visible(dev_scene(ctx), n, dC, dN, dA, rays, reinterpret_cast<uint32_t*>(base + head), reinterpret_cast<uint8_t*>(base + cnt),
+                                   dOut, ctx->wave_blocks, ctx->stream);
+  VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  ctx->tim.launches += 2;
+  if (!dF) VT_CK(cudaMemcpyAsync(F, dOut, nn, cudaMemcpyDeviceToHost, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->tim.trace_ms = ms;
+  return VT_OK;
+}
+
 vt_status vt_debug_flags(vt_ctx* ctx, uint32_t out[16], int reset) {
   if (!ctx || !out) return VT_ERR_ARG;
   VT_CK(cudaMemcpyAsync(out, ctx->d_dbg, 64, cudaMemcpyDeviceToHost, ctx->stream));

@@ -54,5 +54,9 @@ void launch_jacobi_gemm_fp32(const float* F, const float* rho, const float* E, c
 // sum the partials into out[0..1] (deterministic order)
 void launch_reduce_partials(const double* partials, uint32_t n, double* out, cudaStream_t st);
 void launch_form_factors(uint32_t n, const float* C, const float* N, const float* A, float* F, cudaStream_t st);
+// the same with each pair's visibility through the scene: K rays per unordered pair (K <= 255, n <= 65535);
+// counts: n x n bytes of work, head: one word
+void launch_form_factors_visible(const vtd::Scene& S, uint32_t n, const float* C, const float* N, const float* A, uint32_t K, uint32_t* head,
+                                 uint8_t* counts, float* F, int blocks, cudaStream_t st);
 
 }  // namespace vtk

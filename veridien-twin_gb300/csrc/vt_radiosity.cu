@@ -17,6 +17,7 @@
 #include "vt_kernels.cuh"
 
 namespace vtk {
+using namespace vtd;
 
 constexpr int MV_THREADS = 256;
 
@@ -408,6 +409,122 @@ __global__ void form_factor_kernel(uint32_t n, const float* __restrict__ C, cons
 void launch_form_factors(uint32_t n, const float* C, const float* N, const float* A, float* F, cudaStream_t st) {
   if (!n) return;
   form_factor_kernel<<<n, 256, 0, st>>>(n, C, N, A, F);
+}
+
+// ------------------------------------------------------------------------------------- form factors with visibility
+// F_ij = (disk form factor of the centres) x V_ij, V_ij the fraction of K stratified rays between points of the two
+// patch discs that no surface of the scene blocks (the gather of gpu/wgsl/kernels.wgsl.js:271 gatherDir, dense),
+// then each row scaled to a sum <= 1. A patch is a disc of its area around its centre, tangent to its normal; ray
+// k joins the points of the discs' half radius at Kronecker sample k (each disc its own shift), each lifted along
+// its normal by 5 mm + a tenth of that radius (so that a tangent disc on a curved, faceted surface starts in front
+// of it). V is symmetric: each unordered pair is traced once, on persistent traversal lanes.
+constexpr int FV_THREADS = 256;
+
+__device__ __forceinline__ float3 disc_point(const float* C, const float* N, const float* A, uint32_t i, float u, float v) {
+  const float3 c = f3(C[3 * i], C[3 * i + 1], C[3 * i + 2]), nn = f3(N[3 * i], N[3 * i + 1], N[3 * i + 2]);
+  const float rh = 0.5f * sqrtf(A[i] * INV_PI_F), r = rh * sqrtf(u);
+  float sp, cp;
+  sincosf(2.0f * PI_F * v, &sp, &cp);
+  return c + basis_t(nn) * (r * cp) + basis_b(nn) * (r * sp) + nn * (5e-3f + 0.1f * rh);
+}
+__device__ __forceinline__ bool facing(const float* C, const float* N, uint32_t i, uint32_t j) {
+  const float wx = C[3 * j] - C[3 * i], wy = C[3 * j + 1] - C[3 * i + 1], wz = C[3 * j + 2] - C[3 * i + 2];
+  return N[3 * i] * wx + N[3 * i + 1] * wy + N[3 * i + 2] * wz > 0.0f && N[3 * j] * wx + N[3 * j + 1] * wy + N[3 * j + 2] * wz < 0.0f;
+}
+
+__global__ void __launch_bounds__(FV_THREADS, 4) ff_visibility_kernel(const Scene S, const float* __restrict__ C, const float* __restrict__ N,
+                                                                     const float* __restrict__ A, uint32_t n, uint32_t K, uint32_t* head,
+                                                                     uint8_t* __restrict__ counts) {
+  __shared__ uint2 stack_sh[SH_DEPTH * FV_THREADS];
+  LaneStack stk;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = FV_THREADS;
+  TraceState st;
+  const uint32_t skip = ldu(S.su + 7);
+  const uint32_t total = n * n;
+  float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
+  uint32_t i = 0, j = 0, k = 0, vis = 0;
+  bool active = false, exhausted = false;
+  auto next_ray = [&]() -> bool {
+    for (; k < K; k++) {
+      const float3 a = disc_point(C, N, A, i, kr(k, R2A, 0.5f), kr(k, R2B, 0.5f));
+      const float3 b = disc_point(C, N, A, j, kr(k, R2A, 0.25f), kr(k, R2B, 0.75f));
+      const float3 w = b - a;
+      const float dist = length(w);
+      if (!(dist > 2e-4f)) { vis++; continue; }
+      o = a;
+      d = w / dist;
+      st.best = Hit{dist - 1e-4f, 0.0f, 0.0f, MISS, MISS};
+      if (trace_phase(S, 0u, o, d, 0.0f, 0.5f, 3u, skip, st, -1)) return true;
+      vis++;
+    }
+    return false;
+  };
+  auto finish = [&]() {
+    counts[size_t(i) * n + j] = uint8_t(vis);
+    counts[size_t(j) * n + i] = uint8_t(vis);
+    active = false;
+  };
+  auto start = [&](uint32_t idx) {
+    i = idx / n;
+    j = idx % n;
+    if (j <= i) return;
+    if (!facing(C, N, i, j)) { vis = 0; finish(); return; }
+    k = 0;
+    vis = 0;
+    active = true;
+    if (!next_ray()) finish();
+  };
+  while (take_rays(active, exhausted, head, total, REFILL, start)) {
+    if (!active) continue;
+    const int r = trace_visit<true>(S, 0.0f, st, stk);
+    bool done = r == 2;
+    if (r == 1) done = !trace_phase(S, 0u, o, d, 0.0f, 0.5f, 3u, skip, st, st.k + 1);
+    if (!done) continue;
+    if (st.best.tri == MISS) vis++;
+    k++;
+    if (!next_ray()) finish();
+  }
+}
+
+__global__ void ff_rows_kernel(uint32_t n, const float* __restrict__ C, const float* __restrict__ N, const float* __restrict__ A,
+                               const uint8_t* __restrict__ counts, uint32_t K, float* __restrict__ F) {
+  const uint32_t i = blockIdx.x;
+  const float cx = C[3 * i], cy = C[3 * i + 1], cz = C[3 * i + 2];
+  const float nx = N[3 * i], ny = N[3 * i + 1], nz = N[3 * i + 2];
+  const double inv_k = 1.0 / double(K);
+  auto ff = [&](uint32_t j) -> double {
+    if (j == i) return 0.0;
+    const uint8_t c = counts[size_t(i) * n + j];
+    if (!c) return 0.0;
+    const double wx = double(C[3 * j]) - cx, wy = double(C[3 * j + 1]) - cy, wz = double(C[3 * j + 2]) - cz;
+    const double r2 = wx * wx + wy * wy + wz * wz;
+    const double r = sqrt(r2);
+    if (!(r > 0.0)) return 0.0;
+    const double ci = (nx * wx + ny * wy + nz * wz) / r;
+    const double cj = -(N[3 * j] * wx + N[3 * j + 1] * wy + N[3 * j + 2] * wz) / r;
+    if (ci <= 0.0 || cj <= 0.0) return 0.0;
+    return double(A[j]) * ci * cj / (3.14159265358979323846 * r2 + double(A[j])) * (double(c) * inv_k);
+  };
+  double s = 0.0;
+  for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) s += ff(j);
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  const double sc = red[0] > 1.0 ? 1.0 / red[0] : 1.0;
+  for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) F[size_t(i) * n + j] = float(ff(j) * sc);
+}
+
+void launch_form_factors_visible(const Scene& S, uint32_t n, const float* C, const float* N, const float* A, uint32_t K, uint32_t* head,
+                                 uint8_t* counts, float* F, int blocks, cudaStream_t st) {
+  if (!n) return;
+  cudaMemsetAsync(counts, 0, size_t(n) * n, st);
+  cudaMemsetAsync(head, 0, 4, st);
+  ff_visibility_kernel<<<blocks, FV_THREADS, 0, st>>>(S, C, N, A, n, K, head, counts);
+  ff_rows_kernel<<<n, 256, 0, st>>>(n, C, N, A, counts, K, F);
 }
 
 }  // namespace vtk

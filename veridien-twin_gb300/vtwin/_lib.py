@@ -44,6 +44,7 @@ SIGNATURES = {
                                       C.POINTER(C.c_uint32), C.POINTER(A.vt_tune_row)]),
     "vt_radiosity_solve": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_solve_req)]),
     "vt_form_factors": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_form_factors_visible": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_radiosity_solve_static": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                               C.c_double, C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
     "vt_bvh_capacity": (C.c_uint32, [C.c_uint32, C.c_uint32]),

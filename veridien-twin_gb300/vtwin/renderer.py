@@ -421,6 +421,19 @@ class TwinRenderer:
     def form_factors(self, centres, normals, areas, out=None):
         return form_factors(centres, normals, areas, out, ctx=self._ctx)
 
+    def form_factors_visible(self, centres, normals, areas, rays=64, out=None):
+        """Dense node form factors with each pair's visibility through this scene (vt_form_factors_visible): `rays`
+        stratified rays per pair. out: a numpy array or a device tensor (data_ptr()) of n x n float32."""
+        C_ = np.ascontiguousarray(centres, np.float32)
+        n = len(C_)
+        N_ = np.ascontiguousarray(normals, np.float32)
+        A_ = np.ascontiguousarray(areas, np.float32)
+        if out is None:
+            out = np.zeros((n, n), np.float32)
+        optr = C.c_void_p(out.data_ptr()) if hasattr(out, "data_ptr") else out.ctypes.data_as(C.c_void_p)
+        check(self.lib.vt_form_factors_visible(self._ctx, n, _p(C_), _p(N_), _p(A_), int(rays), optr), self._ctx)
+        return out
+
 
 def key_missing(bodies: dict, key: str) -> bool:
     return key not in bodies
