@@ -200,6 +200,9 @@ typedef struct {
   uint32_t frame;          /* frame counter (scene uniform info.w) */
   float shutter[2];        /* exposure open/close in [0, 1] between poses0 and poses1 */
   float scale;             /* output scale (gpu/renderer.js:888 _packCam expo.z; 1) */
+  uint32_t refine;         /* pass-2 extra sub-samples (0..64) on edge, posed-body and (VT_O_REFINE_SHADOW) shadowed
+                              pixels, continuing the same sequences (gpu/wgsl/kernels.wgsl.js:218 camRefine) */
+  uint32_t refine_light_samples; /* emitter samples per pass-2 sub-sample (0: light_samples) */
 } vt_render_req;
 
 /* Render one camera into its device radiance image (rgba32f, w x h; alpha 0 where every sub-sample missed).

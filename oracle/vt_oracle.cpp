@@ -1338,6 +1338,7 @@ template <typename R> struct Shader {
   const Scene& S;
   const float* P;     // params
   const float* NS;    // node state
+  mutable bool shadowTraced = false;   // a light sample of the current vertex reached its shadow ray
   Shader(Tracer<R>& t) : tr(t), S(t.S), P(t.S.params.data()), NS(t.S.nodeState.data()) {}
   const float* pv(uint32_t i) const { return P + size_t(i) * 4; }
   const float* vert(uint32_t i, int row) const { return tr.V + size_t(i) * 8 + row * 4; }
@@ -1473,6 +1474,7 @@ template <typename R> struct Shader {
     V3<R> f = eval_bsdf(M, n, wi, wo);
     if (maxc(f) <= R(0)) return V3<R>();
     V3<R> o = offset_ray(s.p, s.ng, wi);
+    shadowTraced = true;
     Hit<R> sh = tr.trace(o, wi, R(0), dist - R(2e-5), time, true, 3u, tr.su_u(7));
     if (sh.tri != MISS) return V3<R>();
     R pdfW = d2 / (cosE * R(tr.SU[3]));
@@ -1542,11 +1544,13 @@ template <typename R> struct Shader {
     bool isStatic = (s.flags & VT_F_STATIC) != 0;
     bool mis = !isStatic && !(opts & VT_O_NO_MIS);
     uint32_t nl = std::min<uint32_t>(std::max<uint32_t>(nLight, 1u), 16u);
+    shadowTraced = false;
     V3<R> L = direct_light(s, n, M, wo, time, ul, mis, R(nl));
     for (uint32_t j = 1; j < nl; j++) {
       V3<R> uj(kr(lightIndex + j, KL0, Sd.s[3]), kr(lightIndex + j, KL1, Sd.s[4]), kr(lightIndex + j, KL2, Sd.s[5]));
       L = L + direct_light(s, n, M, wo, time, uj, mis, R(nl));
     }
+    if (shadowTraced) key |= 0x20000u;   // shade.wgsl.js:177 (no shadow culling: every sample that gets this far)
     L = L / R(nl);
     if (isStatic) {
       if (!(opts & (VT_O_NO_INDIRECT | VT_O_DIRECT_ONLY))) {
@@ -1600,12 +1604,14 @@ template <typename R> struct Shader {
       bool mis = !(opts & VT_O_NO_MIS);
       V3<R> ub = ub0;
       V3<R> Ld;
+      shadowTraced = false;
       for (uint32_t j = 0; j < nl; j++) {
         V3<R> uj;
         if (b == 1) uj = j == 0 ? ul0 : V3<R>(kr(i * nl + j, KL0, Sd.s[3]), kr(i * nl + j, KL1, Sd.s[4]), kr(i * nl + j, KL2, Sd.s[5]));
         else uj = V3<R>(kr(i * nl + j, KL0, bounce_shift(Sd, b, 0)), kr(i * nl + j, KL1, bounce_shift(Sd, b, 1)), kr(i * nl + j, KL2, bounce_shift(Sd, b, 2)));
         Ld = Ld + direct_light(s, n, M, wo, time, uj, mis, R(nl));
       }
+      if (b == 1 && shadowTraced) key |= 0x20000u;
       L = L + thr * (Ld / R(nl));
       if (b == maxDepth) break;
       if (b > 1) ub = V3<R>(kr(i, KB0, bounce_shift(Sd, b, 3)), kr(i, KB1, bounce_shift(Sd, b, 4)), kr(i, KB2, bounce_shift(Sd, b, 5)));
@@ -1621,22 +1627,21 @@ template <typename R> struct Shader {
   }
 };
 
-// gpu/wgsl/kernels.wgsl.js:161-213 camMain for one pixel (no caches, no packet traversal, refine = 0)
-template <typename R> static void render_pixel(Tracer<R>& tr, const Shader<R>& sh, const vt_camera_desc& cam, uint32_t camIndex,
-                                               const vt_render_req& q, uint32_t x, uint32_t y, uint32_t skip, double out[4]) {
+// gpu/wgsl/kernels.wgsl.js:161-213 camMain / :70 cachedSubSample for one pixel (no caches, no packet traversal):
+// sub-samples [i0, i1) with nl light samples each, summed in index order into acc; the key (first-hit mesh, posed
+// body 0x10000, shadow traced 0x20000, mesh change among the sub-samples 0x40000) is carried across calls
+template <typename R> static void pixel_samples(Tracer<R>& tr, const Shader<R>& sh, const vt_camera_desc& cam, uint32_t camIndex,
+                                                const vt_render_req& q, uint32_t x, uint32_t y, uint32_t skip, uint32_t i0, uint32_t i1,
+                                                uint32_t lightSamples, V3<R>& acc, uint32_t& key) {
   // the camera uniform is float32 (gpu/renderer.js:888-898 _packCam): lens and axes are priced at those values
   Lens L{double(float(cam.fx)), double(float(cam.fy)), double(float(cam.cx)), double(float(cam.cy)), double(float(cam.alpha)),
          {double(float(cam.k[0])), double(float(cam.k[1])), double(float(cam.k[2])), double(float(cam.k[3]))}};
   const double* T = cam.T_D_C;
   auto col = [&](int a, int b, int c) { return V3<R>(R(float(T[a])), R(float(T[b])), R(float(T[c]))); };
   V3<R> rx = col(0, 4, 8), ry = col(1, 5, 9), rz = col(2, 6, 10), pos = col(3, 7, 11);
-  uint32_t sppMax = q.mode == VT_SHADE_TWIN ? 64u : 4096u;
-  uint32_t spp = std::min(std::max(q.spp, 1u), sppMax);
   PixSeeds Sd = pix_seeds(x, y, q.seed, camIndex);
-  V3<R> acc;
-  uint32_t key = 0;
-  uint32_t nl = std::max(1u, q.light_samples);
-  for (uint32_t i = 0; i < spp; i++) {
+  uint32_t nl = std::max(1u, lightSamples);
+  for (uint32_t i = i0; i < i1; i++) {
     float uvx = float(x) + kr(i, R2A, Sd.s[0]);
     uvx = uvx - 0.5f;
     float uvy = float(y) + kr(i, R2B, Sd.s[1]);
@@ -1650,13 +1655,23 @@ template <typename R> static void render_pixel(Tracer<R>& tr, const Shader<R>& s
     Hit<R> hd = tr.trace(pos, d, R(0), h.t, R(tt), false, 2u, skip);
     if (hd.tri != MISS) h = hd;
     uint32_t gk;
-    V3<R> c = q.mode == VT_SHADE_TWIN ? sh.shade_hit(h, pos, d, R(tt), ul, ub, q.options, i * nl, Sd, q.light_samples, gk)
-                                      : sh.radiance_path(h, pos, d, R(tt), ul, ub, q.options, i, Sd, q.light_samples, std::max(1u, q.max_depth), gk);
+    V3<R> c = q.mode == VT_SHADE_TWIN ? sh.shade_hit(h, pos, d, R(tt), ul, ub, q.options, i * nl, Sd, lightSamples, gk)
+                                      : sh.radiance_path(h, pos, d, R(tt), ul, ub, q.options, i, Sd, lightSamples, std::max(1u, q.max_depth), gk);
     acc = acc + c;
     if (i == 0) key = gk;
     else if ((gk & 0xffffu) != (key & 0xffffu)) key |= 0x40000u;
     key |= (gk & 0x30000u);
   }
+}
+
+static uint32_t pass1_spp(const vt_render_req& q) { return std::min(std::max(q.spp, 1u), q.mode == VT_SHADE_TWIN ? 64u : 4096u); }
+
+template <typename R> static void render_pixel(Tracer<R>& tr, const Shader<R>& sh, const vt_camera_desc& cam, uint32_t camIndex,
+                                               const vt_render_req& q, uint32_t x, uint32_t y, uint32_t skip, double out[4]) {
+  const uint32_t spp = pass1_spp(q);
+  V3<R> acc;
+  uint32_t key = 0;
+  pixel_samples<R>(tr, sh, cam, camIndex, q, x, y, skip, 0, spp, q.light_samples, acc, key);
   R sc = R(q.scale) / R(spp);
   out[0] = double(acc.x * sc); out[1] = double(acc.y * sc); out[2] = double(acc.z * sc);
   out[3] = key == 0xfffeu ? 0.0 : 1.0;
@@ -2193,29 +2208,93 @@ void or_render(void* h, const vt_render_req* q, uint32_t y0, uint32_t y1, uint32
   const vt_camera_desc& cam = S->cams[q->camera];
   uint32_t skip = 0;
   for (size_t i = 0; i < S->blas.size(); i++) if (S->blas[i].owner == int(q->camera)) skip |= 1u << i;
-  uint32_t w = x1 - x0;
-  std::atomic<uint32_t> next(y0);
+  const uint32_t w = x1 - x0, extra = std::min(q->refine, 64u);
+  // with a refinement pass, pass 1 covers the region grown by one pixel (the 3x3 neighbourhood test)
+  const uint32_t gy0 = extra && y0 > 0 ? y0 - 1 : y0, gy1 = extra ? std::min(y1 + 1, cam.height) : y1;
+  const uint32_t gx0 = extra && x0 > 0 ? x0 - 1 : x0, gx1 = extra ? std::min(x1 + 1, cam.width) : x1, gw = gx1 - gx0;
+  std::vector<double> acc1(extra ? size_t(gy1 - gy0) * gw * 3 : 0);
+  std::vector<uint32_t> key1(extra ? size_t(gy1 - gy0) * gw : 0);
   std::vector<Dbg> dbgs(std::max(1, threads));
-  auto work = [&](int t) {
-    auto run = [&](auto tag) {
-      using R = decltype(tag);
+  auto parallel = [&](uint32_t r0, uint32_t r1, auto&& row) {
+    std::atomic<uint32_t> next(r0);
+    auto work = [&](int t) {
+      for (;;) {
+        uint32_t y = next.fetch_add(1);
+        if (y >= r1) break;
+        row(t, y);
+      }
+    };
+    if (threads <= 1) work(0);
+    else {
+      std::vector<std::thread> th;
+      for (int t = 0; t < threads; t++) th.emplace_back(work, t);
+      for (auto& x : th) x.join();
+    }
+  };
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    if (!extra) {
+      parallel(y0, y1, [&](int t, uint32_t y) {
+        Tracer<R> tr(*S, dbgs[t]);
+        tr.gRoot = q->root;
+        Shader<R> sh(tr);
+        for (uint32_t x = x0; x < x1; x++) render_pixel<R>(tr, sh, cam, q->camera, *q, x, y, skip, out + (size_t(y - y0) * w + (x - x0)) * 4);
+      });
+      return;
+    }
+    const uint32_t spp = pass1_spp(*q);
+    parallel(gy0, gy1, [&](int t, uint32_t y) {
       Tracer<R> tr(*S, dbgs[t]);
       tr.gRoot = q->root;
       Shader<R> sh(tr);
-      for (;;) {
-        uint32_t y = next.fetch_add(1);
-        if (y >= y1) break;
-        for (uint32_t x = x0; x < x1; x++) render_pixel<R>(tr, sh, cam, q->camera, *q, x, y, skip, out + (size_t(y - y0) * w + (x - x0)) * 4);
+      for (uint32_t x = gx0; x < gx1; x++) {
+        V3<R> a;
+        uint32_t k = 0;
+        pixel_samples<R>(tr, sh, cam, q->camera, *q, x, y, skip, 0, spp, q->light_samples, a, k);
+        const size_t j = size_t(y - gy0) * gw + (x - gx0);
+        acc1[3 * j] = double(a.x); acc1[3 * j + 1] = double(a.y); acc1[3 * j + 2] = double(a.z);
+        key1[j] = k;
       }
-    };
-    if (fp64) run(double(0)); else run(float(0));
+    });
+    // gpu/wgsl/kernels.wgsl.js:218-252 camRefine
+    std::vector<Dbg> rdbg(std::max(1, threads));
+    const uint32_t nl2 = q->refine_light_samples ? q->refine_light_samples : q->light_samples;
+    parallel(y0, y1, [&](int t, uint32_t y) {
+      Tracer<R> tr(*S, dbgs[t]);
+      tr.gRoot = q->root;
+      Shader<R> sh(tr);
+      for (uint32_t x = x0; x < x1; x++) {
+        const size_t j = size_t(y - gy0) * gw + (x - gx0);
+        uint32_t k = key1[j];
+        bool want = (k & 0x50000u) != 0u || ((k & 0x20000u) != 0u && (q->options & VT_O_REFINE_SHADOW) != 0u);
+        for (int dy = -1; dy <= 1 && !want; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            const uint32_t xx = uint32_t(std::min(std::max(int(x) + dx, 0), int(cam.width) - 1));
+            const uint32_t yy = uint32_t(std::min(std::max(int(y) + dy, 0), int(cam.height) - 1));
+            if ((key1[size_t(yy - gy0) * gw + (xx - gx0)] & 0xffffu) != (k & 0xffffu)) want = true;
+          }
+        V3<R> a(R(acc1[3 * j]), R(acc1[3 * j + 1]), R(acc1[3 * j + 2]));
+        double* o = out + (size_t(y - y0) * w + (x - x0)) * 4;
+        if (!want) {
+          R sc = R(q->scale) / R(spp);
+          o[0] = double(a.x * sc); o[1] = double(a.y * sc); o[2] = double(a.z * sc);
+          o[3] = k == 0xfffeu ? 0.0 : 1.0;
+          continue;
+        }
+        rdbg[t].c[2]++;
+        if (k & 0x10000u) rdbg[t].c[3]++;
+        if (k & 0x20000u) rdbg[t].c[4]++;
+        if (k & 0x40000u) rdbg[t].c[5]++;
+        pixel_samples<R>(tr, sh, cam, q->camera, *q, x, y, skip, spp, spp + extra, nl2, a, k);
+        R sc = R(q->scale) / R(spp + extra);
+        o[0] = double(a.x * sc); o[1] = double(a.y * sc); o[2] = double(a.z * sc);
+        o[3] = 1.0;
+      }
+    });
+    for (int t = 0; t < std::max(1, threads); t++)
+      for (int c = 2; c <= 5; c++) dbgs[t].c[c] += rdbg[t].c[c];
   };
-  if (threads <= 1) work(0);
-  else {
-    std::vector<std::thread> th;
-    for (int t = 0; t < threads; t++) th.emplace_back(work, t);
-    for (auto& x : th) x.join();
-  }
+  if (fp64) run(double(0)); else run(float(0));
   if (dbgOut) for (int k = 0; k < 16; k++) { dbgOut[k] = 0; for (auto& d : dbgs) dbgOut[k] += d.c[k]; }
 }
 

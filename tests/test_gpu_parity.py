@@ -172,6 +172,47 @@ def test_path_radiance_matches_fp64_oracle(dome_small):
     assert s["median"] < 1e-5 and s["within_1e-4"] > 0.9 and s["mean_rel"] < 2e-3 and s["alpha_same"] == 1.0
 
 
+def test_refinement_pass(inst_scene, inst_poses):
+    """gpu/wgsl/kernels.wgsl.js:218 camRefine: every pixel is bit-exactly its spp render or its spp + refine render
+    (the same sub-samples summed in the same order); the refined set and the image agree with the FP64 oracle."""
+    r = TwinRenderer.create(inst_scene)
+    ref = O.Scene(inst_scene)
+    r.set_pose_array(inst_poses)
+    ref.set_poses(inst_poses)
+    W, H = inst_scene["cameras"][0]["size"]
+
+    def render(refineShadows=False, **o):
+        out = np.zeros((H, W, 4), np.float32)
+        q = r.renderCamera(0, out=out, lightSamples=2, seed=3, refineShadows=refineShadows, **o)
+        return out, q
+
+    a, _ = render(spp=2)
+    b, _ = render(spp=5)
+    r.debugFlags(reset=True)
+    c, q = render(spp=2, refine=3, refineLightSamples=2)
+    f = r.debugFlags(reset=True)
+    same_a = np.all(c == a, -1)
+    same_b = np.all(c[..., :3] == b[..., :3], -1) & (c[..., 3] == 1.0)
+    assert np.all(same_a | same_b)
+    assert int((same_b & ~same_a).sum()) <= f["refined"] <= int(same_b.sum())
+    assert 0 < f["refined"] < W * H and f["refinedBody"] > 0
+    img64, dbg = ref.render(q, fp64=True, threads=8)
+    s = _radiance_stats(c, img64)
+    print("\nrefinement: gpu refined", f, "oracle refined", dbg[2:6], s)
+    assert abs(f["refined"] - int(dbg[2])) <= 0.01 * int(dbg[2]) + 4
+    assert s["median"] < 1e-5 and s["within_1e-4"] > 0.95 and s["mean_rel"] < 1e-3
+    # one light sample per refinement sub-sample (the reference's default): the same pixels refined
+    d, _ = render(spp=2, refine=3, refineLightSamples=1)
+    g = r.debugFlags(reset=True)
+    assert g["refined"] == f["refined"] and np.all(np.isfinite(d))
+    known_plain = same_a & ~same_b
+    assert np.all(d[known_plain] == a[known_plain])
+    # shadow-traced pixels too
+    render(spp=2, refine=3, refineLightSamples=1, refineShadows=True)
+    assert r.debugFlags(reset=True)["refined"] > f["refined"]
+    r.destroy()
+
+
 def test_sensor_expose_bit_exact():
     W, H = 320, 240
     rng = np.random.default_rng(8)

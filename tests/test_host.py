@@ -93,3 +93,33 @@ def test_no_gpu_fails_loudly(dome_small):
 
     with pytest.raises(VtError):
         TwinRenderer.create(dome_small)
+
+
+def test_ctypes_mirror_matches_header_layout(tmp_path):
+    """Every struct of include/vtwin.h has the size and field offsets that vtwin/_abi.py gives it (compiled with gcc)."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    from vtwin import _abi as A
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    names = [n for n in dir(A) if n.startswith("vt_") and isinstance(getattr(A, n), type) and issubclass(getattr(A, n), ctypes.Structure)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vtwin.h"', "int main(void) {"]
+    for n in names:
+        lines.append(f'  printf("{n} %zu\\n", sizeof({n}));')
+        for f in getattr(A, n)._fields_:
+            lines.append(f'  printf("{n}.{f[0]} %zu\\n", offsetof({n}, {f[0]}));')
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(root, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines())
+    for n in names:
+        S = getattr(A, n)
+        assert int(got[n]) == ctypes.sizeof(S), n
+        for f in S._fields_:
+            assert int(got[f"{n}.{f[0]}"]) == getattr(S, f[0]).offset, f"{n}.{f[0]}"

@@ -257,3 +257,41 @@ def test_calibration_estimator_is_linear_in_emission():
     e = S.calib_render(0, np.minimum(alb * 2, 1.0), lamp, 0 * Hn, tri_node, spp=2, depth=1)
     f = S.calib_render(0, alb, lamp, 0 * Hn, tri_node, spp=2, depth=1)
     assert np.all(e <= 2 * f + 1e-12)
+
+
+def _refine_req(spp, nl, refine, refine_nl, options=0):
+    from vtwin import _abi as A
+
+    q = A.vt_render_req(camera=0, spp=spp, light_samples=nl, seed=3, options=options, mode=A.VT_SHADE_TWIN, max_depth=2,
+                        root=0, frame=0, refine=refine, refine_light_samples=refine_nl)
+    q.shutter[:] = [0.0, 1.0]
+    q.scale = 1.0
+    return q
+
+
+def test_refinement_pass_continues_the_sub_sample_sequences():
+    """gpu/wgsl/kernels.wgsl.js:218 camRefine restated: a refined pixel is its (spp + refine)-sample value, exactly
+    (the same sub-samples summed in the same order), every other pixel its spp-sample value; refined pixels are edges
+    in the 3x3 neighbourhood, posed bodies and (VT_O_REFINE_SHADOW) pixels whose shadow rays were traced."""
+    from vtwin import _abi as A
+
+    sc = dome.make_dome_scene(seed=1, width=40, height=30, level=2, with_instruments=2)
+    S = O.Scene(sc)
+    T = dome.instrument_poses(n_poses=1, n_tools=2, seed=11)[0]
+    S.set_poses(np.concatenate([A.identity_poses(1), T]))
+    a, _ = S.render(_refine_req(2, 2, 0, 0), threads=8)
+    b, _ = S.render(_refine_req(5, 2, 0, 0), threads=8)
+    c, dbg = S.render(_refine_req(2, 2, 3, 2), threads=8)
+    same_a = np.all(c == a, -1)
+    same_b = np.all(c[..., :3] == b[..., :3], -1) & (c[..., 3] == 1.0)
+    assert np.all(same_a | same_b)
+    refined = int(dbg[2])
+    assert int((same_b & ~same_a).sum()) <= refined <= int(same_b.sum())
+    assert 0 < refined < c.shape[0] * c.shape[1]
+    assert dbg[3] > 0                      # posed bodies in view
+    # a region renders as the same pixels of the whole image (the neighbourhood test reads one pixel beyond it)
+    part, _ = S.render(_refine_req(2, 2, 3, 2), y0=7, y1=19, x0=5, x1=31, threads=4)
+    assert np.array_equal(part, c[7:19, 5:31])
+    # shadow-traced pixels join the refinement with VT_O_REFINE_SHADOW
+    d, dbg2 = S.render(_refine_req(2, 2, 3, 2, options=A.OPTION_BITS["REFINE_SHADOW"]), threads=8)
+    assert dbg2[2] > dbg[2] and dbg2[4] > 0

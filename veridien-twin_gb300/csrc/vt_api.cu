@@ -256,14 +256,18 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   if (q->root >= ctx->S.node_count) return fail(ctx, VT_ERR_ARG, "render: root out of range");
   if (q->mode != VT_SHADE_TWIN && q->mode != VT_SHADE_PATH) return fail(ctx, VT_ERR_ARG, "render: unknown mode");
   const vt_camera_desc& c = ctx->S.cams[q->camera];
-  const vtk::CamParams cp = make_cam(ctx, q->camera, q->spp, q->light_samples, q->seed, q->options, q->mode, q->max_depth, q->root, q->shutter,
-                                     q->scale);
+  vtk::CamParams cp = make_cam(ctx, q->camera, q->spp, q->light_samples, q->seed, q->options, q->mode, q->max_depth, q->root, q->shutter,
+                               q->scale);
+  cp.refine = std::min(q->refine, 64u);   // kernels.wgsl.js:224 extra = min(expo.w, 64)
+  vtk::CamParams cp2 = make_cam(ctx, q->camera, q->spp, q->refine_light_samples ? q->refine_light_samples : q->light_samples, q->seed,
+                                q->options, q->mode, q->max_depth, q->root, q->shutter, q->scale);
+  cp2.refine = cp.refine;
   if (q->frame != ctx->frame) { ctx->frame = q->frame; vt_status s = write_su(ctx); if (s != VT_OK) return s; }
   // wave of up to 8 M paths (whole sub-sample indices): ~1.4 GB of path state at one light sample
   const uint32_t n_pix = vtk::tiled_pixels(c.width, c.height, cp.tile_w, cp.tile_h);
   const uint32_t per_wave = std::max(1u, std::min(cp.spp, (8u << 20) / std::max(1u, n_pix)));
   const uint32_t paths = per_wave * n_pix;
-  const size_t need = vtk::wave_bytes(paths, cp.n_light, n_pix);
+  const size_t need = vtk::wave_bytes(paths, std::max(cp.n_light, cp2.n_light), n_pix);
   if (ctx->wave_cap < need) {
     VT_CK(cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->d_wave);
@@ -272,12 +276,13 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
     if (cudaMalloc(&ctx->d_wave, need) != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "wavefront state allocation failed"); }
     ctx->wave_cap = need;
   }
-  vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, paths, cp.n_light, n_pix, ctx->d_work);
+  vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, paths, std::max(cp.n_light, cp2.n_light), n_pix, ctx->d_work);
+  wb.rcount = ctx->d_work + 12;
   vtk::KernelTimer timer{ctx->kev.data(), ctx->kkind.data(), int(ctx->kev.size() / 2), 0};
   if (ctx->kprof) wb.stats = reinterpret_cast<unsigned long long*>(ctx->d_work + 16);
   VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
   vtk::wave_render(dev_scene(ctx), cp, wb, paths, ctx->cams[q->camera].radiance, ctx->wave_blocks, ctx->stream, &ctx->tim.launches,
-                   ctx->kprof ? &timer : nullptr);
+                   ctx->kprof ? &timer : nullptr, &cp2);
   VT_CK(cudaGetLastError());
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   ctx->cams[q->camera].rendered = true;

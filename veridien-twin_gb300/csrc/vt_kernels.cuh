@@ -17,6 +17,7 @@ struct CamParams {
   float t0, t1, scale;
   uint32_t tile_w, tile_h;             // pixel enumeration order: tiles of tile_w x tile_h (product 32)
   uint32_t refill;                     // traversal lanes: a warp takes new rays once this many of its lanes are idle
+  uint32_t refine;                     // pass-2 extra sub-samples (camRefine), 0 none
 };
 
 // default pixel tile: consecutive paths are neighbouring pixels of an 8 x 4 tile

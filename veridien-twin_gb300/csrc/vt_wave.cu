@@ -255,6 +255,8 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S0, const
           shadow |= ok;
         }
         if (shadow) wb.nee[p] = make_float4(thr.x, thr.y, thr.z, tt);
+        // key bit 0x20000: a first-hit light sample needs its shadow ray (shade.wgsl.js:177; no shadow culling here)
+        if (b == 1 && shadow) L4.w = __uint_as_float(__float_as_uint(L4.w) | 0x20000u);
         bool bounce;
         if (MODE == VT_SHADE_TWIN) {
           bounce = !is_static;
@@ -386,9 +388,80 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_finalize(const CamParams cp
   }
 }
 
+// ------------------------------------------------------------------------------------------------ refinement
+// gpu/wgsl/kernels.wgsl.js:218 camRefine: after pass 1, a pixel whose sub-samples saw different meshes (key bit
+// 0x40000), a posed body (0x10000), a shadow-traced pixel when VT_O_REFINE_SHADOW is set (0x20000), or whose 3x3
+// neighbourhood has another first-hit mesh gets cp.refine more sub-samples (indices spp .. spp + refine - 1, the same
+// sequences), added in order to its pass-1 sum: value = sum * scale / (spp + refine), alpha 1. The others keep the
+// pass-1 value. Refined pixels are counted into dbg[2..5] (total, posed body, shadow, sub-sample mesh change).
+__device__ __forceinline__ uint32_t pixel_id(const CamParams& cp, uint32_t x, uint32_t y) {
+  const uint32_t tw = cp.tile_w, th = cp.tile_h, tiles_x = (cp.w + tw - 1) / tw;
+  return ((y / th) * tiles_x + x / tw) * (tw * th) + (y % th) * tw + (x % tw);
+}
+
+__global__ void __launch_bounds__(WAVE_THREADS) refine_select(const CamParams cp, const Scene S, WaveBufs wb, uint32_t n_pix, float4* __restrict__ out) {
+  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n_pix; id += gridDim.x * blockDim.x) {
+    uint32_t x, y;
+    bool want = false;
+    if (pixel_xy(cp, id, x, y)) {
+      const float4 a = wb.acc[id];
+      const uint32_t k = __float_as_uint(a.w);
+      want = (k & 0x50000u) != 0u || ((k & 0x20000u) != 0u && (cp.options & VT_O_REFINE_SHADOW) != 0u);
+      for (int dy = -1; dy <= 1 && !want; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          const uint32_t xx = uint32_t(min(max(int(x) + dx, 0), int(cp.w) - 1)), yy = uint32_t(min(max(int(y) + dy, 0), int(cp.h) - 1));
+          if ((__float_as_uint(wb.acc[pixel_id(cp, xx, yy)].w) & 0xffffu) != (k & 0xffffu)) { want = true; break; }
+        }
+      if (want) {
+        atomicAdd(S.dbg + 2, 1u);
+        if (k & 0x10000u) atomicAdd(S.dbg + 3, 1u);
+        if (k & 0x20000u) atomicAdd(S.dbg + 4, 1u);
+        if (k & 0x40000u) atomicAdd(S.dbg + 5, 1u);
+      } else {
+        const float sc = cp.scale / float(cp.spp);
+        out[size_t(y) * cp.w + x] = make_float4(a.x * sc, a.y * sc, a.z * sc, k == 0xfffeu ? 0.0f : 1.0f);
+      }
+    }
+    const uint32_t slot = warp_append(wb.rcount, want);
+    if (want) wb.rlist[slot] = id;
+  }
+}
+
+// refinement paths p = e * n_list + l: sub-sample spp + e0 + e of listed pixel l
+__global__ void __launch_bounds__(WAVE_THREADS) refine_gen(const CamParams cp, WaveBufs wb, uint32_t spp1, uint32_t e0, uint32_t n_e) {
+  const uint32_t n_list = *wb.rcount, total = n_list * n_e;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const uint32_t l = p % n_list, i = spp1 + e0 + p / n_list, id = wb.rlist[l];
+    float4 o4, d4;
+    uint32_t hs;
+    const bool valid = camera_path(cp, id, i, o4, d4, hs);
+    init_path(wb, p, o4, d4, id, i, hs, valid);
+    const uint32_t slot = warp_append(wb.count_in, valid);
+    if (valid) wb.q_in[slot] = p;
+  }
+}
+
+__global__ void __launch_bounds__(WAVE_THREADS) refine_finalize(const CamParams cp, WaveBufs wb, uint32_t spp1, uint32_t e0, uint32_t n_e,
+                                                               float4* __restrict__ out, int last) {
+  const uint32_t n_list = *wb.rcount;
+  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < n_list; l += gridDim.x * blockDim.x) {
+    const uint32_t id = wb.rlist[l];
+    float3 s = xyz(e0 == 0 ? wb.acc[id] : wb.acc2[l]);
+    for (uint32_t e = 0; e < n_e; e++) s = s + xyz(wb.L[size_t(e) * n_list + l]);
+    if (last) {
+      uint32_t x, y;
+      pixel_xy(cp, id, x, y);
+      const float sc = cp.scale / float(spp1 + cp.refine);
+      out[size_t(y) * cp.w + x] = make_float4(s.x * sc, s.y * sc, s.z * sc, 1.0f);
+    } else {
+      wb.acc2[l] = make_float4(s.x, s.y, s.z, 0.0f);
+    }
+  }
+}
+
 size_t wave_bytes(uint32_t paths, uint32_t n_light, uint32_t n_pix) {
   const size_t P = paths;
-  return P * (16 * 7 + 4 * 4) + P * size_t(n_light) * 48 + size_t(n_pix) * 16 + 16 * 256;
+  return P * (16 * 7 + 4 * 4) + P * size_t(n_light) * 48 + size_t(n_pix) * 36 + 18 * 256;
 }
 
 WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix, uint32_t* counts) {
@@ -409,6 +482,9 @@ WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix
   w.q_sh = reinterpret_cast<uint32_t*>(take(P * 4));
   w.sh = reinterpret_cast<float4*>(take(P * size_t(n_light) * 48));
   w.acc = reinterpret_cast<float4*>(take(size_t(n_pix) * 16));
+  w.acc2 = reinterpret_cast<float4*>(take(size_t(n_pix) * 16));
+  w.rlist = reinterpret_cast<uint32_t*>(take(size_t(n_pix) * 4));
+  w.rcount = nullptr;
   w.counts = counts;
   w.fetch = counts + 3;
   return w;
@@ -488,7 +564,7 @@ void wave_gen_pairs(const CamParams& cp, WaveBufs wb, int blocks, cudaStream_t s
 
 // one camera: waves of whole sub-sample indices, each bounce extend -> shade -> shadow over compacted queues
 void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave_paths, float4* out, int blocks, cudaStream_t st,
-                 uint64_t* launches, KernelTimer* timer) {
+                 uint64_t* launches, KernelTimer* timer, const CamParams* cp2) {
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t per_wave = std::max(1u, std::min(cp.spp, wave_paths / n_pix));
   uint64_t nlaunch = 0;
@@ -500,9 +576,25 @@ void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave
     wave_gen<<<blocks, WAVE_THREADS, 0, st>>>(cp, w, i0, n_i, n_pix);
     nlaunch++;
     wave_bounces(S, cp, wb, WAVE_PLAIN, blocks, st, &nlaunch, timer);
-    const int last = i0 + n_i >= cp.spp;
+    const int last = i0 + n_i >= cp.spp && !(cp.refine && cp2 && wb.rcount);
     wave_finalize<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb, i0, n_i, n_pix, wb.acc, out, last);
     nlaunch++;
+  }
+  if (cp.refine && cp2 && wb.rcount) {
+    cudaMemsetAsync(wb.rcount, 0, 4, st);
+    refine_select<<<blocks, WAVE_THREADS, 0, st>>>(cp, S, wb, n_pix, out);
+    nlaunch++;
+    const uint32_t per = std::max(1u, std::min(cp.refine, wave_paths / n_pix));
+    for (uint32_t e0 = 0; e0 < cp.refine; e0 += per) {
+      const uint32_t n_e = std::min(per, cp.refine - e0);
+      cudaMemsetAsync(wb.counts, 0, 16, st);
+      WaveBufs w = wb;
+      w.q_in = wb.qa; w.count_in = wb.counts + 0;
+      refine_gen<<<blocks, WAVE_THREADS, 0, st>>>(*cp2, w, cp.spp, e0, n_e);
+      wave_bounces(S, *cp2, wb, WAVE_PLAIN, blocks, st, &nlaunch, timer);
+      refine_finalize<<<blocks, WAVE_THREADS, 0, st>>>(cp, wb, cp.spp, e0, n_e, out, e0 + n_e >= cp.refine);
+      nlaunch += 2;
+    }
   }
   if (launches) *launches += nlaunch;
 }

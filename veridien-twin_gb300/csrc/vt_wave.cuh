@@ -43,6 +43,9 @@ struct WaveBufs {
   uint32_t* q_sh;   // paths with light samples to test
   float4* sh;       // per path and light sample: (shadow origin, tmax) (direction, valid) (contribution)
   float4* acc;      // per pixel running sum across waves, key bits
+  float4* acc2;     // per refined pixel: running sum of the refinement waves
+  uint32_t* rlist;  // refined pixel ids
+  uint32_t* rcount; // their number (refinement only)
   uint32_t* counts; // queue lengths
   // the current bounce's view
   uint32_t* q_in;
@@ -64,8 +67,10 @@ struct KernelTimer {
 
 size_t wave_bytes(uint32_t paths, uint32_t n_light, uint32_t n_pix);
 WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix, uint32_t* counts);
+// one camera: pass 1 (cp.spp sub-samples per pixel), then when cp.refine > 0 pass 2 over the selected pixels with
+// cp2 (the refinement's light samples) continuing the sub-sample sequences
 void wave_render(const vtd::Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave_paths, float4* out, int blocks, cudaStream_t st,
-                 uint64_t* launches, KernelTimer* timer = nullptr);
+                 uint64_t* launches, KernelTimer* timer = nullptr, const CamParams* cp2 = nullptr);
 int wave_blocks_per_sm();
 
 // one wave's bounces (extend, shade, shadow per bounce) over the paths queued in wb.qa / counts[0]

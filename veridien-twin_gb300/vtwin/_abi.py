@@ -84,7 +84,8 @@ class vt_blas_info(C.Structure):
 class vt_render_req(C.Structure):
     _fields_ = [("camera", C.c_uint32), ("spp", C.c_uint32), ("light_samples", C.c_uint32), ("seed", C.c_uint32),
                 ("options", C.c_uint32), ("mode", C.c_uint32), ("max_depth", C.c_uint32), ("root", C.c_uint32),
-                ("frame", C.c_uint32), ("shutter", C.c_float * 2), ("scale", C.c_float)]
+                ("frame", C.c_uint32), ("shutter", C.c_float * 2), ("scale", C.c_float), ("refine", C.c_uint32),
+                ("refine_light_samples", C.c_uint32)]
 
 
 class vt_sensor_uniform(C.Structure):

@@ -14,8 +14,12 @@ from . import _abi as A
 from ._lib import VtError, check, load
 from . import sensor as sensor_mod
 
-DEFAULTS = {"spp": 1, "refine": 0, "lightSamples": 4, "leafSize": 4, "albedoSamples": 1024}
-PRESETS = {"judge": {}, "balanced": {"spp": 1, "lightSamples": 2}, "live": {"spp": 1, "lightSamples": 1}}
+# gpu/renderer.js:31 DEFAULTS, except refine: the refinement pass is opt-in here (the reference adds 6 sub-samples on
+# edges by default), so that a default render is the plain pass-1 estimator
+DEFAULTS = {"spp": 1, "refine": 0, "refineLightSamples": 1, "refineShadows": True, "lightSamples": 4, "leafSize": 4,
+            "albedoSamples": 1024}
+PRESETS = {"judge": {}, "balanced": {"spp": 1, "lightSamples": 2, "refine": 2, "refineLightSamples": 1, "refineShadows": False},
+           "live": {"spp": 1, "lightSamples": 1, "refine": 0}}
 
 
 def _p(a):
@@ -133,11 +137,21 @@ class TwinRenderer:
 
     # ------------------------------------------------------------------------------------------- rendering
     def request(self, name, spp=None, lightSamples=None, seed=0, options=0, mode=A.VT_SHADE_TWIN, max_depth=2,
-                shutter=(0.0, 1.0), scale=1.0, root=0, frame=None) -> A.vt_render_req:
+                shutter=(0.0, 1.0), scale=1.0, root=0, frame=None, refine=None, refineLightSamples=None,
+                refineShadows=None) -> A.vt_render_req:
+        """gpu/renderer.js:935 _submitCamera's options: pass 1 (spp sub-samples, lightSamples each) and the refinement
+        pass (refine more sub-samples on edges, posed bodies and, with refineShadows, pixels whose shadow rays were
+        traced; refineLightSamples each)."""
+        opts = int(options)
+        if refineShadows if refineShadows is not None else self.opts.get("refineShadows", True):
+            opts |= A.OPTION_BITS["REFINE_SHADOW"]
         q = A.vt_render_req(camera=self._cam(name), spp=int(spp if spp is not None else self.opts["spp"]),
                             light_samples=int(lightSamples if lightSamples is not None else self.opts["lightSamples"]),
-                            seed=int(seed), options=int(options), mode=int(mode), max_depth=int(max_depth), root=int(root),
-                            frame=int(self.frame if frame is None else frame))
+                            seed=int(seed), options=opts, mode=int(mode), max_depth=int(max_depth), root=int(root),
+                            frame=int(self.frame if frame is None else frame),
+                            refine=int(refine if refine is not None else self.opts.get("refine", 0)),
+                            refine_light_samples=int(refineLightSamples if refineLightSamples is not None
+                                                     else self.opts.get("refineLightSamples", 1)))
         q.shutter[:] = [float(shutter[0]), float(shutter[1])]
         q.scale = float(scale)
         return q
