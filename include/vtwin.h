@@ -392,6 +392,56 @@ vt_status vt_form_factors_visible(vt_ctx* ctx, uint32_t n, const float* centres,
 vt_status vt_radiosity_solve_static(const float* F, const float* rho, const float* E, float* B, uint32_t n, uint32_t max_iters,
                                     uint32_t check_every, double tol, void* stream, uint32_t* iters, double* residual);
 
+/* ------------------------------------------------------------------------------- scene node radiosity */
+/* The twin's own node radiosity, the producer of the node state the camera shading reads (gpu/renderer.js:456
+ * _buildGatherTable, :713 _submitNodeDirect, :730 _submitJacobi, :771 _ensureRadiosity, :804 converge, :825
+ * nodeSummary; gpu/wgsl/kernels.wgsl.js:271-461). Nodes are the static vertices. The gather table holds, per node,
+ * the nearest node hit by each of K cosine-distributed rays (MISS for an escape or a back face); nodes with at most
+ * K/2 escapes are active. Each update computes the direct light of the active nodes (node_samples emitter samples
+ * with shadow rays) and Jacobi steps of the separable transport, smoothed over same-facing neighbours. */
+typedef struct {
+  uint32_t gather_k;        /* gather rays per node (gpu/renderer.js:38, 64; 1..1024) */
+  uint32_t node_samples;    /* emitter samples per node per update (4) */
+  uint32_t nbr_k;           /* smoothing neighbours kept per node (16; 1..64) */
+  float smooth_sigma;       /* Gaussian sigma of the smoothing (m, 0.003; 0: no smoothing) */
+  float smooth_radius;      /* neighbours within this distance (m, 0.006) */
+  uint32_t radiosity_every; /* update on every n-th pose change (1) */
+  uint32_t iters_per_frame; /* Jacobi steps per update (4) */
+  uint32_t iters_initial;   /* Jacobi steps of the first solve, 8 at once and the rest spread over updates (96) */
+} vt_nodes_opts;
+typedef struct {
+  uint32_t n_nodes;         /* static vertices */
+  uint32_t n_active;
+  uint32_t gather_k, nbr_k;
+  double build_ms;          /* gather table: build, count, remap (device time) */
+  double neighbour_ms;      /* smoothing neighbours (host) */
+} vt_nodes_info;
+/* Build the gather table, the active list and the neighbours (static BVH only); node state reset to its initial
+ * values. Afterwards renders run vt_nodes_update first (like renderCamera), until vt_set_node_state. opts NULL =
+ * defaults. info may be NULL. */
+vt_status vt_nodes_build(vt_ctx* ctx, const vt_nodes_opts* opts, vt_nodes_info* info);
+/* Direct light at the active nodes at mid-exposure; moved != 0: only nodes whose segment to the emitter passes near
+ * a body of the mask, where it is now or where it was at the last full update. */
+vt_status vt_nodes_direct(vt_ctx* ctx, uint32_t moved);
+/* `iters` Jacobi steps (gather, then update, ping-pong of the Ls slots 1 and 2). */
+vt_status vt_nodes_jacobi(vt_ctx* ctx, uint32_t iters);
+/* _ensureRadiosity: bring the node radiosity up to the current poses (nothing when they did not change, an
+ * incremental update when only bodies other than the emitter moved, else a full one). what (may be NULL): 0 nothing
+ * to do, 1 full, 2 incremental, 3 reused (poses set but nothing moved). */
+vt_status vt_nodes_update(vt_ctx* ctx, int force, uint32_t* what);
+/* converge(iters): the direct light if the poses changed since, then `iters` Jacobi steps, then the node summary
+ * (eAvg written to the scene uniform). */
+vt_status vt_converge(vt_ctx* ctx, uint32_t iters);
+/* nodeSummary: area-weighted means over the active nodes of the indirect irradiance (E_free V), the direct
+ * irradiance (B_dir / hh) and Ls x hh; eAvg = indirect + direct, also written to the scene uniform. out: area,
+ * mean_indirect[3], mean_direct[3], mean_lout[3], eavg[3]. */
+vt_status vt_node_summary(vt_ctx* ctx, double out[13]);
+/* Copies of the node radiosity's tables: gtable n_nodes x gather_k, active n_active, nbr n_active x nbr_k x 2 words
+ * (active index, float weight bits; weight 0 ends a list), misses n_nodes. Any pointer may be NULL. */
+vt_status vt_nodes_export(vt_ctx* ctx, uint32_t* gtable, uint32_t* active, uint32_t* nbr, float* misses);
+/* The node state (n_nodes x 16 floats) and its latest slot. */
+vt_status vt_get_node_state(vt_ctx* ctx, float* state, uint32_t* slot);
+
 /* ---------------------------------------------------------------------------------------- bvh (pure) */
 
 /* gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}): binned SAH BVH2 on the host. nodes_out must hold

@@ -255,6 +255,48 @@ class Scene:
                                  _p(D))
         return D
 
+    # ------------------------------------------------------------------------------------- node radiosity
+    def gather_table(self, K=64, fp64=True, threads=8):
+        """The gather table of every static vertex (n x K node ids, MISS = escape) and the escapes per node."""
+        n = self.static_verts
+        g = np.zeros(n * K, np.uint32)
+        m = np.zeros(n, np.float32)
+        lib().or_gather_table(self.h, C.c_uint32(K), int(fp64), int(threads), _p(g, C.c_uint32), _p(m, C.c_float))
+        return g.reshape(n, K), m
+
+    def node_neighbours(self, active, nbr_k=16, radius=0.006, sigma=0.003):
+        """Smoothing neighbours by brute force: (n_active, nbr_k, 2) uint32 (active index, float weight bits)."""
+        act = np.ascontiguousarray(active, np.uint32)
+        out = np.zeros(len(act) * nbr_k * 2, np.uint32)
+        lib().or_node_neighbours(self.h, _p(act, C.c_uint32), C.c_uint32(len(act)), C.c_uint32(nbr_k), C.c_double(radius),
+                                 C.c_double(sigma), _p(out, C.c_uint32))
+        return out.reshape(len(act), nbr_k, 2)
+
+    def node_direct(self, active, state, node_samples=4, moved=0, fp64=True, threads=8):
+        """nodeDirect of the active nodes applied to a copy of `state` (n x 16, float64)."""
+        act = np.ascontiguousarray(active, np.uint32)
+        st = np.array(state, np.float64).reshape(-1, 16).copy()
+        lib().or_node_direct(self.h, _p(act, C.c_uint32), C.c_uint32(len(act)), C.c_uint32(node_samples), C.c_uint32(moved), int(fp64),
+                             int(threads), _p(st))
+        return st
+
+    def node_jacobi(self, gtable, active, nbr, state, slot, iters, fp64=True, threads=8):
+        """`iters` Jacobi steps of the node transport on a copy of `state`; returns (state, final slot)."""
+        g = np.ascontiguousarray(gtable, np.uint32)
+        act = np.ascontiguousarray(active, np.uint32)
+        nb = np.ascontiguousarray(nbr, np.uint32)
+        st = np.array(state, np.float64).reshape(-1, 16).copy()
+        out = lib().or_node_jacobi(self.h, _p(g, C.c_uint32), C.c_uint32(g.shape[1]), _p(act, C.c_uint32), C.c_uint32(len(act)),
+                                   _p(nb, C.c_uint32), C.c_uint32(nb.shape[1]), C.c_uint32(slot), C.c_uint32(iters), int(fp64), int(threads),
+                                   _p(st))
+        return st, int(out)
+
+    def set_solved_caps(self, caps):
+        """Bounding capsules of the last node update (n_bodies x 8), written to the scene uniform."""
+        c = np.ascontiguousarray(caps, np.float32)
+        lib().or_scene_set_solved_caps(self.h, _p(c, C.c_float), C.c_uint32(len(c) // 8 if c.ndim == 1 else len(c)),
+                                       C.c_uint32(self.slot), C.c_uint32(self.frame))
+
     def form_factors_visible(self, centres, normals, areas, rays=16, fp64=True, threads=1):
         """Dense node form factors with visibility through this scene (n x n float32) and the visible-ray counts."""
         Cn = np.ascontiguousarray(centres, np.float32)

@@ -754,6 +754,7 @@ struct Scene {
   struct Pose4 { double q0[4], q1[4], p0[3], p1[3]; bool valid; };
   std::vector<Pose4> inst;
   std::vector<uint32_t> emitOfTri;   // per triangle slot: index in the emitter table, or MISS
+  std::vector<float> solvedCaps;     // 8 per body: bounding capsules at the last node update (empty: the current ones)
 };
 
 // gpu/scene_gpu.js:504 fitCapsule
@@ -1125,7 +1126,8 @@ static void write_scene_u(Scene& S, uint32_t slot, uint32_t frame) {
       motion *= 1.5;
     }
     float bc[8] = {float(ca[0]), float(ca[1]), float(ca[2]), float(bl.cap_r * 1.0001 + 1e-6 + motion), float(cb[0]), float(cb[1]), float(cb[2]), 0};
-    for (int k = 0; k < 8; k++) { f[o + 32 + k] = bc[k]; f[o + 40 + k] = bc[k]; }
+    const bool havePc = S.solvedCaps.size() >= 8 * (i + 1) && !std::isnan(S.solvedCaps[8 * i]);
+    for (int k = 0; k < 8; k++) { f[o + 32 + k] = bc[k]; f[o + 40 + k] = havePc ? S.solvedCaps[8 * i + k] : bc[k]; }
   }
 }
 static void set_poses(Scene& S, const double* T0, const double* T1, uint32_t nb) {
@@ -2058,6 +2060,138 @@ static void form_factors(int n, const float* C, const float* Nn, const float* A,
 
 using namespace orc;
 
+// ============================================================================================ node radiosity
+// The scene's own node radiosity (gpu/wgsl/kernels.wgsl.js:255-461; gpu/renderer.js:456-851), restated for the CPU:
+// the gather table, its escape counts and remap, the smoothing neighbours, the nodes' direct light and the Jacobi
+// steps of the separable transport. Precision R for the geometry and transport; the gather directions' sample
+// numbers (the spiral radius and angle fraction) in float32, rounded per operation as the CUDA kernels draw them.
+template <typename R> struct NodeRad {
+  Tracer<R>& tr;
+  Shader<R>& sh;
+  const Scene& S;
+  NodeRad(Tracer<R>& t, Shader<R>& s) : tr(t), sh(s), S(t.S) {}
+  V3<R> pos(uint32_t i) const { return ld3<R>(tr.V + 8 * size_t(i)); }
+  V3<R> nrm(uint32_t i) const { return normalize(ld3<R>(tr.V + 8 * size_t(i) + 4)); }
+  uint32_t mat(uint32_t i) const { return as_u(sh.pv(S.meshOff + 2 * S.verts[8 * size_t(i) + 3])[3]); }
+  // gpu/wgsl/kernels.wgsl.js:271 gatherDir
+  static V3<R> dir(uint32_t i, uint32_t j, uint32_t K, const V3<R>& n) {
+    V3<R> t = basis_t(n), b = basis_b(n);
+    float rot = u01(pcg(i * 2654435761u + 17u));
+    float rr = std::sqrt((float(j) + 0.5f) / float(K));
+    float a = float(j) * 0.6180339887498949f;
+    a = a + rot;
+    float fr = a - std::floor(a);
+    R ph = R(2) * R(M_PI) * R(fr), r = R(rr);
+    return normalize(t * (r * std::cos(ph)) + b * (r * std::sin(ph)) + n * std::sqrt(std::max(R(0), R(1) - r * r)));
+  }
+  // gpu/wgsl/kernels.wgsl.js:284 gatherBuild (one entry)
+  uint32_t build(uint32_t i, uint32_t j, uint32_t K) const {
+    V3<R> p = pos(i), n = nrm(i), d = dir(i, j, K, n);
+    Hit<R> h = tr.trace(p + n * R(2e-6), d, R(0), R(BIGD), R(0.5), false, 1u, 0u);
+    if (h.tri == MISS) return MISS;
+    V3<R> bb(R(1) - h.u - h.v, h.u, h.v);
+    const uint32_t* ru = S.tris.data() + size_t(h.tri) * 16;
+    uint32_t v0 = ru[3], v1 = ru[7], v2 = ru[11];
+    V3<R> nv = ld3<R>(tr.V + 8 * size_t(v0) + 4) * bb.x + ld3<R>(tr.V + 8 * size_t(v1) + 4) * bb.y + ld3<R>(tr.V + 8 * size_t(v2) + 4) * bb.z;
+    if (!(dot(nv, d) < R(0))) return MISS;
+    if (bb.x >= bb.y && bb.x >= bb.z) return v0;
+    return bb.y >= bb.z ? v1 : v2;
+  }
+  // gpu/wgsl/kernels.wgsl.js:300 gatherRemap (one entry)
+  uint32_t remap(uint32_t i, uint32_t j, uint32_t K, uint32_t v0, const float* misses) const {
+    const float half = 0.5f * float(K);
+    if (v0 == MISS || misses[v0] <= half) return v0;
+    V3<R> p = pos(i), n = nrm(i), d = dir(i, j, K, n);
+    Hit<R> h = tr.trace(p + n * R(2e-6), d, R(0), R(BIGD), R(0.5), false, 1u, 0u);
+    if (h.tri == MISS) return v0;
+    V3<R> bb(R(1) - h.u - h.v, h.u, h.v);
+    const uint32_t* ru = S.tris.data() + size_t(h.tri) * 16;
+    uint32_t a = ru[3], b = ru[7], c = ru[11], best = v0;
+    R bw = -1;
+    if (misses[a] <= half && bb.x > bw) { best = a; bw = bb.x; }
+    if (misses[b] <= half && bb.y > bw) { best = b; bw = bb.y; }
+    if (misses[c] <= half && bb.z > bw) { best = c; bw = bb.z; }
+    return best;
+  }
+  // gpu/wgsl/kernels.wgsl.js:348 nodeDirect (one node): B_dir (3), visibility code, capsule visibility
+  bool direct(uint32_t i, uint32_t NS, uint32_t moved, R out[5]) const {
+    V3<R> p = pos(i), n = nrm(i);
+    if (moved) {
+      M3<R> M; V3<R> pp;
+      tr.inst_pose(tr.su_u(17), R(0.5), M, pp);
+      V3<R> dE = (M.mul(ld3<R>(tr.SU + 20)) + pp) - p;
+      R rr = R(tr.SU[23]) + R(1e-3);
+      bool near = false;
+      for (uint32_t b = 0; b < std::min<uint32_t>(tr.su_u(16), VT_MAX_INST) && !near; b++) {
+        if (!((moved >> b) & 1u)) continue;
+        const float* I = tr.inst(b);
+        near = Tracer<R>::seg_near_capsule(p, dE, R(0), R(1), ld3<R>(I + 32), ld3<R>(I + 36), R(I[35]) + rr) ||
+               Tracer<R>::seg_near_capsule(p, dE, R(0), R(1), ld3<R>(I + 40), ld3<R>(I + 44), R(I[43]) + rr);
+      }
+      if (!near) return false;
+    }
+    uint32_t m = mat(i);
+    uint32_t hs = pcg(i * 2246822519u + 3u);
+    float s0 = u01(pcg(hs)), s1 = u01(pcg(hs + 1u)), s2 = u01(pcg(hs + 2u));
+    V3<R> B;
+    uint32_t nLit = 0, nVis = 0;
+    V3<R> o = p + n * R(2e-6);
+    for (uint32_t s = 0; s < NS; s++) {
+      V3<R> lp, ln, la;
+      sh.sample_emitter(V3<R>(kr(s, KL0, s0), kr(s, KL1, s1), kr(s, KL2, s2)), R(0.5), lp, ln, la);
+      V3<R> wi = lp - p;
+      R d2 = dot(wi, wi), dist = std::sqrt(d2);
+      wi = wi / dist;
+      R cosE = dot(-wi, ln), cosN = dot(n, wi);
+      if (cosE <= R(0) || cosN <= R(0)) continue;
+      V3<R> Le = sh.emitted(ln, la, -wi);
+      if (maxc(Le) <= R(0)) continue;
+      nLit++;
+      if (tr.trace(o, wi, R(0), dist - R(2e-5), R(0.5), true, 3u, tr.su_u(7)).tri != MISS) continue;
+      nVis++;
+      B = B + Le * (cosE * cosN * R(tr.SU[3]) / d2) * sh.albedo_all(m, cosN);
+    }
+    B = B / R(NS);
+    out[0] = B.x; out[1] = B.y; out[2] = B.z;
+    out[3] = nLit == 0 ? R(-1) : nVis == nLit ? R(1) : nVis == 0 ? R(0) : R(0.5);
+    out[4] = sh.capsule_vis(p, n);
+    return true;
+  }
+  // gpu/wgsl/kernels.wgsl.js:416 jacobiGather (one active node)
+  V3<R> gather(uint32_t i, uint32_t K, const uint32_t* gtable, const double* st, uint32_t slotIn) const {
+    V3<R> n = nrm(i);
+    uint32_t mi = mat(i);
+    V3<R> acc;
+    for (uint32_t j = 0; j < K; j++) {
+      uint32_t h = gtable[size_t(i) * K + j];
+      if (h == MISS) continue;
+      V3<R> d = dir(i, j, K, n);
+      R muIn = std::sqrt(std::max(R(0), R(1) - (R(j) + R(0.5)) / R(K)));
+      R muOut = clampR(-dot(d, nrm(h)), R(0), R(1));
+      const double* L = st + 16 * size_t(h) + 4 * slotIn;
+      acc = acc + sh.albedo_all(mi, muIn) * sh.albedo_all(mat(h), muOut) * V3<R>(R(L[0]), R(L[1]), R(L[2]));
+    }
+    V3<R> hh = sh.load_mat(mi).hh;
+    R sc = R(M_PI) / R(K);
+    return V3<R>(acc.x * sc / std::max(hh.x, R(1e-4)), acc.y * sc / std::max(hh.y, R(1e-4)), acc.z * sc / std::max(hh.z, R(1e-4)));
+  }
+};
+
+template <typename F> static void parallel_for(size_t n, int threads, F&& f) {
+  std::atomic<size_t> next(0);
+  auto work = [&]() {
+    for (;;) {
+      size_t k = next.fetch_add(64);
+      if (k >= n) break;
+      for (size_t q = k; q < std::min(n, k + 64); q++) f(q);
+    }
+  };
+  if (threads <= 1) { work(); return; }
+  std::vector<std::thread> th;
+  for (int t = 0; t < threads; t++) th.emplace_back(work);
+  for (auto& x : th) x.join();
+}
+
 extern "C" {
 
 void or_mulberry32(uint32_t seed, int n, double* out) { Mulberry32 m(seed); for (int i = 0; i < n; i++) out[i] = m.next(); }
@@ -2436,4 +2570,137 @@ int or_jacobi64(int n, const float* F, const float* rho, const float* E, int R, 
 }
 void or_form_factors(int n, const float* C, const float* Nn, const float* A, float* F) { form_factors(n, C, Nn, A, F); }
 
+// gather table of every static vertex (K rays each): build, escape counts, remap (gpu/renderer.js:456-500)
+void or_gather_table(void* h, uint32_t K, int fp64, int threads, uint32_t* gtable, float* misses) {
+  Scene* S = static_cast<Scene*>(h);
+  const uint32_t n = S->staticVerts;
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    Dbg dbg;
+    parallel_for(size_t(n) * K, threads, [&](size_t r) {
+      Dbg d;
+      Tracer<R> tr(*S, d);
+      Shader<R> sh(tr);
+      NodeRad<R> nr(tr, sh);
+      gtable[r] = nr.build(uint32_t(r / K), uint32_t(r % K), K);
+    });
+    for (uint32_t i = 0; i < n; i++) {
+      uint32_t m = 0;
+      for (uint32_t j = 0; j < K; j++) m += gtable[size_t(i) * K + j] == MISS;
+      misses[i] = float(m);
+    }
+    parallel_for(size_t(n) * K, threads, [&](size_t r) {
+      Dbg d;
+      Tracer<R> tr(*S, d);
+      Shader<R> sh(tr);
+      NodeRad<R> nr(tr, sh);
+      gtable[r] = nr.remap(uint32_t(r / K), uint32_t(r % K), K, gtable[r], misses);
+    });
+  };
+  if (fp64) run(double(0)); else run(float(0));
+}
+
+// gpu/renderer.js:573 _neighbours by brute force: the nbrK largest Gaussian weights (ties: smaller active index)
+// over active nodes within R that face the same way (n.n >= 0.9); out: nA x nbrK x (index, float weight bits)
+void or_node_neighbours(void* h, const uint32_t* active, uint32_t nA, uint32_t nbrK, double R, double sg, uint32_t* out) {
+  Scene* S = static_cast<Scene*>(h);
+  std::fill(out, out + size_t(nA) * nbrK * 2, 0u);
+  auto vf = [&](uint32_t i, int w) { return double(as_f(S->verts[8 * size_t(i) + w])); };
+  for (uint32_t k = 0; k < nA; k++) {
+    if (!(sg > 0)) { out[size_t(k) * nbrK * 2] = k; float one = 1.0f; std::memcpy(&out[size_t(k) * nbrK * 2 + 1], &one, 4); continue; }
+    const uint32_t i = active[k];
+    std::vector<std::pair<double, uint32_t>> c;
+    for (uint32_t m = 0; m < nA; m++) {
+      const uint32_t j = active[m];
+      double ex = vf(j, 0) - vf(i, 0), ey = vf(j, 1) - vf(i, 1), ez = vf(j, 2) - vf(i, 2), d2 = ex * ex + ey * ey + ez * ez;
+      if (d2 > R * R) continue;
+      if (vf(i, 4) * vf(j, 4) + vf(i, 5) * vf(j, 5) + vf(i, 6) * vf(j, 6) < 0.9) continue;
+      c.push_back({std::exp(-0.5 * d2 / (sg * sg)), m});
+    }
+    std::sort(c.begin(), c.end(), [](const auto& a, const auto& b) { return a.first > b.first || (a.first == b.first && a.second < b.second); });
+    for (size_t q = 0; q < std::min<size_t>(c.size(), nbrK); q++) {
+      float w = float(c[q].first);
+      out[(size_t(k) * nbrK + q) * 2] = c[q].second;
+      std::memcpy(&out[(size_t(k) * nbrK + q) * 2 + 1], &w, 4);
+    }
+  }
+}
+
+// nodeDirect over the active nodes (moved != 0: only those near a moved body); st: n x 16 doubles, in and out
+void or_node_direct(void* h, const uint32_t* active, uint32_t nA, uint32_t NS, uint32_t moved, int fp64, int threads, double* st) {
+  Scene* S = static_cast<Scene*>(h);
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    parallel_for(nA, threads, [&](size_t k) {
+      Dbg d;
+      Tracer<R> tr(*S, d);
+      Shader<R> sh(tr);
+      NodeRad<R> nr(tr, sh);
+      const uint32_t i = active[k];
+      R o[5];
+      if (!nr.direct(i, NS, moved, o)) return;
+      double* q = st + 16 * size_t(i);
+      q[12] = double(o[0]); q[13] = double(o[1]); q[14] = double(o[2]); q[15] = double(o[3]); q[3] = double(o[4]);
+    });
+  };
+  if (fp64) run(double(0)); else run(float(0));
+}
+
+// `iters` Jacobi steps from slot slotIn (gather into aux, then update, ping-pong); returns the final slot
+uint32_t or_node_jacobi(void* h, const uint32_t* gtable, uint32_t K, const uint32_t* active, uint32_t nA, const uint32_t* nbr, uint32_t nbrK,
+                        uint32_t slotIn, uint32_t iters, int fp64, int threads, double* st) {
+  Scene* S = static_cast<Scene*>(h);
+  std::vector<double> aux(size_t(nA) * 3);
+  uint32_t slot = slotIn;
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    for (uint32_t it = 0; it < iters; it++) {
+      const uint32_t out = slot == 1 ? 2 : 1;
+      parallel_for(nA, threads, [&](size_t k) {
+        Dbg d;
+        Tracer<R> tr(*S, d);
+        Shader<R> sh(tr);
+        NodeRad<R> nr(tr, sh);
+        V3<R> a = nr.gather(active[k], K, gtable, st, slot);
+        aux[3 * k] = double(a.x); aux[3 * k + 1] = double(a.y); aux[3 * k + 2] = double(a.z);
+      });
+      parallel_for(nA, threads, [&](size_t k) {
+        Dbg d;
+        Tracer<R> tr(*S, d);
+        Shader<R> sh(tr);
+        NodeRad<R> nr(tr, sh);
+        const uint32_t i = active[k];
+        V3<R> ef;
+        R ws = 0;
+        for (uint32_t j = 0; j < nbrK; j++) {
+          const uint32_t* e = nbr + (k * nbrK + j) * 2;
+          R w = R(as_f(e[1]));
+          if (w <= R(0)) break;
+          ef = ef + V3<R>(R(aux[3 * e[0]]), R(aux[3 * e[0] + 1]), R(aux[3 * e[0] + 2])) * w;
+          ws = ws + w;
+        }
+        ef = ws > R(0) ? ef / ws : V3<R>(R(aux[3 * k]), R(aux[3 * k + 1]), R(aux[3 * k + 2]));
+        double* q = st + 16 * size_t(i);
+        V3<R> hh = sh.load_mat(nr.mat(i)).hh;
+        R hm[3] = {std::max(hh.x, R(1e-4)), std::max(hh.y, R(1e-4)), std::max(hh.z, R(1e-4))};
+        R e3[3] = {ef.x, ef.y, ef.z};
+        const R V = R(q[3]);
+        for (int c = 0; c < 3; c++) q[4 * out + c] = double((R(q[12 + c]) + e3[c] * V * hm[c]) * R(INV_PI_D) / hm[c]);
+        q[4 * out + 3] = 1.0;
+        q[0] = double(ef.x); q[1] = double(ef.y); q[2] = double(ef.z);
+      });
+      slot = out;
+    }
+  };
+  if (fp64) run(double(0)); else run(float(0));
+  return slot;
+}
+
+void or_scene_set_solved_caps(void* h, const float* caps, uint32_t nb, uint32_t slot, uint32_t frame) {
+  Scene* S = static_cast<Scene*>(h);
+  S->solvedCaps.assign(caps, caps + 8 * size_t(nb));
+  write_scene_u(*S, slot, frame);
+}
+
 }  // extern "C"
+

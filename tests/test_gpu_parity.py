@@ -191,6 +191,10 @@ def test_refinement_pass(inst_scene, inst_poses):
     r.debugFlags(reset=True)
     c, q = render(spp=2, refine=3, refineLightSamples=2)
     f = r.debugFlags(reset=True)
+    # the first twin render brought the node radiosity up to the poses: the oracle shades with the same node state
+    st, slot = r.get_node_state()
+    ref.set_node_state(st, slot)
+    ref.set_eavg(r.scene_uniform()[8:11])
     same_a = np.all(c == a, -1)
     same_b = np.all(c[..., :3] == b[..., :3], -1) & (c[..., 3] == 1.0)
     assert np.all(same_a | same_b)

@@ -295,3 +295,41 @@ def test_refinement_pass_continues_the_sub_sample_sequences():
     # shadow-traced pixels join the refinement with VT_O_REFINE_SHADOW
     d, dbg2 = S.render(_refine_req(2, 2, 3, 2, options=A.OPTION_BITS["REFINE_SHADOW"]), threads=8)
     assert dbg2[2] > dbg[2] and dbg2[4] > 0
+
+
+def test_node_transport_reduces_to_the_linear_system():
+    """With Lambertian nodes (A(mu) = rho = hh) and no smoothing, the Jacobi steps of the separable node transport
+    (gpu/wgsl/kernels.wgsl.js:416-461) converge to M = B_dir + diag(rho V) F M, M = pi rho Ls the exitance and
+    F_ih = #{j : gtable[i, j] = h} / K over the active nodes: the restatement checked against a direct solve."""
+    sc = dome.make_dome_scene(seed=1, width=32, height=24, level=3)
+    S = O.Scene(sc)
+    S.set_poses()
+    K = 32
+    g, mis = S.gather_table(K)
+    act = np.nonzero(mis <= K / 2)[0].astype(np.uint32)
+    assert 0 < len(act) < S.static_verts
+    # every entry is MISS or a node; after the remap no entry names an inactive node that has an active alternative
+    assert np.all((g == 0xFFFFFFFF) | (g < S.static_verts))
+    nb = S.node_neighbours(act, nbr_k=4, sigma=0.0)
+    assert np.array_equal(nb[:, 0, 0], np.arange(len(act))) and np.all(nb[:, 1:, 1] == 0)
+    st = np.zeros((S.static_verts, 16))
+    st[:, 3] = 1.0
+    st[:, 15] = -1.0
+    st = S.node_direct(act, st)
+    assert np.all(st[act, 12:15] >= 0) and st[act, 12:15].max() > 0
+    out, slot = S.node_jacobi(g, act, nb, st, 1, 200)
+    # the linear system over the active nodes (entries on inactive nodes read their zero source)
+    pos = {int(i): k for k, i in enumerate(act)}
+    n = len(act)
+    F = np.zeros((n, n))
+    for k, i in enumerate(act):
+        for h in g[i]:
+            if int(h) in pos:
+                F[k, pos[int(h)]] += 1.0 / K
+    # the albedo tables and hh hold rho in float32
+    rho = np.array([sc["materials"][sc["meshes"][m]["mat"]]["rho"] for m in sc["static"]["vert_mesh"][act]], np.float32).astype(np.float64)
+    V = st[act, 3]
+    for c in range(3):
+        M = np.linalg.solve(np.eye(n) - (rho[:, c] * V)[:, None] * F, st[act, 12 + c])
+        got = np.pi * rho[:, c] * out[act, 4 * slot + c]
+        np.testing.assert_allclose(got, M, rtol=1e-9, atol=1e-12 * M.max())

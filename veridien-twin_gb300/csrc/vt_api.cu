@@ -105,6 +105,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   if (ctx->batch.exec) cudaGraphExecDestroy(ctx->batch.exec);
   for (auto& e : ctx->kev) cudaEventDestroy(e);
   cudaFree(ctx->calib.mem);
+  cudaFree(ctx->nodes.mem);
   cudaFree(ctx->calib.records);
   for (float4* p : ctx->calib.image) cudaFree(p);
   for (float4* p : ctx->calib.target) cudaFree(p);
@@ -157,6 +158,7 @@ vt_status vt_set_poses(vt_ctx* ctx, const double* T0, const double* T1, uint32_t
   if (!ctx) return VT_ERR_ARG;
   if (n_bodies && !T0) return fail(ctx, VT_ERR_ARG, "poses: T0 is null");
   ctx->inst = vt::poses_from(ctx->S, T0, T1, n_bodies);
+  ctx->nodes.poses_version++;
   return write_su(ctx);
 }
 
@@ -177,6 +179,7 @@ vt_status vt_set_node_state(vt_ctx* ctx, const float* state, uint32_t slot) {
   vt_status s = to_device(ctx, ctx->d_nstate, state, size_t(ctx->S.static_verts) * 64);
   if (s != VT_OK) return s;
   ctx->slot = slot;
+  ctx->nodes.auto_update = false;   // a caller-supplied state stays until vt_converge or vt_nodes_build
   return write_su(ctx);
 }
 
@@ -255,6 +258,11 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   if (q->camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(q->camera));
   if (q->root >= ctx->S.node_count) return fail(ctx, VT_ERR_ARG, "render: root out of range");
   if (q->mode != VT_SHADE_TWIN && q->mode != VT_SHADE_PATH) return fail(ctx, VT_ERR_ARG, "render: unknown mode");
+  // gpu/renderer.js:976 renderCamera: _ensureRadiosity first (the twin shading reads the node state; path mode does not)
+  if (ctx->nodes.built && ctx->nodes.auto_update && q->mode == VT_SHADE_TWIN) {
+    vt_status s = vt_nodes_update(ctx, 0, nullptr);
+    if (s != VT_OK) return s;
+  }
   const vt_camera_desc& c = ctx->S.cams[q->camera];
   vtk::CamParams cp = make_cam(ctx, q->camera, q->spp, q->light_samples, q->seed, q->options, q->mode, q->max_depth, q->root, q->shutter,
                                q->scale);

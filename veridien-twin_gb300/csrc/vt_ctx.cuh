@@ -95,6 +95,27 @@ struct vt_ctx {
     double inv_count = 0;
     std::vector<float> rho_host, lamp_host;
   } calib;
+  // the scene's node radiosity (vt_nodes_*): gather table, active list, neighbours, update bookkeeping
+  struct Nodes {
+    bool built = false, auto_update = false;
+    vt_nodes_opts o{};
+    uint32_t n = 0, n_active = 0, n_mat = 0;
+    void* mem = nullptr;
+    uint32_t* gtable = nullptr;
+    float4* aux = nullptr;
+    uint32_t* active = nullptr;
+    uint2* nbr = nullptr;
+    float4* amu = nullptr;
+    std::vector<uint32_t> active_h;
+    std::vector<float> misses;
+    uint64_t poses_version = 0;
+    int64_t solved_version = -1;
+    int64_t pending = 0;
+    bool eavg_settled = false;
+    std::vector<vt::InstPose> solved_inst;   // poses of the last update
+    std::vector<float> solved_caps;          // 8 floats per body: bounding capsules of the last update
+    double build_ms = 0, nbr_ms = 0;
+  } nodes;
 };
 
 namespace vtapi {
@@ -145,7 +166,8 @@ inline vtd::Scene dev_scene(vt_ctx* ctx) {
 }
 
 inline vt_status write_su(vt_ctx* ctx) {
-  vt::scene_uniform(ctx->S, ctx->inst, ctx->eavg, ctx->slot, ctx->frame, ctx->su_host);
+  vt::scene_uniform(ctx->S, ctx->inst, ctx->eavg, ctx->slot, ctx->frame, ctx->su_host,
+                    ctx->nodes.solved_caps.empty() ? nullptr : ctx->nodes.solved_caps.data());
   VT_CK(cudaMemcpyAsync(ctx->d_su, ctx->su_host, sizeof(ctx->su_host), cudaMemcpyHostToDevice, ctx->stream));
   return VT_OK;
 }

@@ -683,7 +683,8 @@ std::vector<InstPose> poses_from(const Prepared& S, const double* T0, const doub
   return out;
 }
 
-void scene_uniform(const Prepared& S, const std::vector<InstPose>& inst, const float eavg[3], uint32_t slot, uint32_t frame, float* f) {
+void scene_uniform(const Prepared& S, const std::vector<InstPose>& inst, const float eavg[3], uint32_t slot, uint32_t frame, float* f,
+                   const float* pcaps) {
   uint32_t* u = reinterpret_cast<uint32_t*>(f);
   std::fill(f, f + SU_WORDS, 0.0f);
   f[0] = S.L0[0]; f[1] = S.L0[1]; f[2] = S.L0[2]; f[3] = S.emit_area != 0 ? float(S.emit_area) : 1e-12f;
@@ -750,7 +751,64 @@ void scene_uniform(const Prepared& S, const std::vector<InstPose>& inst, const f
       motion *= 1.5;
     }
     const float bc[8] = {float(ca[0]), float(ca[1]), float(ca[2]), float(bl.cap_r * 1.0001 + 1e-6 + motion), float(cb[0]), float(cb[1]), float(cb[2]), 0};
-    for (int k = 0; k < 8; k++) { o[32 + k] = bc[k]; o[40 + k] = bc[k]; }
+    const bool have_pc = pcaps && !std::isnan(pcaps[8 * i]);
+    for (int k = 0; k < 8; k++) { o[32 + k] = bc[k]; o[40 + k] = have_pc ? pcaps[8 * i + k] : bc[k]; }
+  }
+}
+
+void node_neighbours(const Prepared& S, const std::vector<uint32_t>& active, uint32_t K, double R, double sg, std::vector<uint32_t>& out) {
+  const size_t n = active.size();
+  out.assign(n * K * 2, 0u);
+  if (!(sg > 0)) {
+    const float one = 1.0f;
+    for (size_t k = 0; k < n; k++) { out[k * K * 2] = uint32_t(k); std::memcpy(&out[k * K * 2 + 1], &one, 4); }
+    return;
+  }
+  auto vf = [&](uint32_t i, int w) { float x; std::memcpy(&x, &S.verts[8 * size_t(i) + w], 4); return double(x); };
+  // cells of side R: every node within R of another lies in one of the 27 cells around it
+  auto cell = [&](double x) { return int64_t(std::floor(x / R)); };
+  auto key = [](int64_t x, int64_t y, int64_t z) {
+    return (uint64_t(x + (1 << 20)) << 42) | (uint64_t(y + (1 << 20)) << 21) | uint64_t(z + (1 << 20));
+  };
+  std::vector<uint64_t> keys(n);
+  for (size_t k = 0; k < n; k++) keys[k] = key(cell(vf(active[k], 0)), cell(vf(active[k], 1)), cell(vf(active[k], 2)));
+  std::vector<uint32_t> order(n);
+  for (size_t k = 0; k < n; k++) order[k] = uint32_t(k);
+  std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return keys[a] < keys[b] || (keys[a] == keys[b] && a < b); });
+  std::vector<uint64_t> sorted(n);
+  for (size_t q = 0; q < n; q++) sorted[q] = keys[order[q]];
+  std::vector<double> cw(K);
+  std::vector<uint32_t> cm(K);
+  for (size_t k = 0; k < n; k++) {
+    const uint32_t i = active[k];
+    const double px = vf(i, 0), py = vf(i, 1), pz = vf(i, 2), nx = vf(i, 4), ny = vf(i, 5), nz = vf(i, 6);
+    const int64_t cx = cell(px), cy = cell(py), cz = cell(pz);
+    uint32_t cnt = 0;
+    for (int dx = -1; dx <= 1; dx++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dz = -1; dz <= 1; dz++) {
+          const uint64_t kk = key(cx + dx, cy + dy, cz + dz);
+          auto lo = std::lower_bound(sorted.begin(), sorted.end(), kk);
+          for (size_t q = size_t(lo - sorted.begin()); q < n && sorted[q] == kk; q++) {
+            const uint32_t m = order[q], j = active[m];
+            const double ex = vf(j, 0) - px, ey = vf(j, 1) - py, ez = vf(j, 2) - pz, d2 = ex * ex + ey * ey + ez * ez;
+            if (d2 > R * R) continue;
+            if (nx * vf(j, 4) + ny * vf(j, 5) + nz * vf(j, 6) < 0.9) continue;
+            const double w = std::exp(-0.5 * d2 / (sg * sg));
+            // keep the K largest (descending weight, then ascending index)
+            uint32_t pos = cnt < K ? cnt : K;
+            while (pos > 0 && (cw[pos - 1] < w || (cw[pos - 1] == w && cm[pos - 1] > m))) pos--;
+            if (pos >= K) continue;
+            for (uint32_t z = std::min(cnt, K - 1); z > pos; z--) { cw[z] = cw[z - 1]; cm[z] = cm[z - 1]; }
+            cw[pos] = w; cm[pos] = m;
+            if (cnt < K) cnt++;
+          }
+        }
+    for (uint32_t z = 0; z < cnt; z++) {
+      const float wf = float(cw[z]);
+      out[(k * K + z) * 2] = cm[z];
+      std::memcpy(&out[(k * K + z) * 2 + 1], &wf, 4);
+    }
   }
 }
 

@@ -65,8 +65,17 @@ struct InstPose { bool valid = false; double q0[4], q1[4], p0[3], p1[3]; };
 // gpu/renderer.js:620 setPoses: quaternion + translation per body (T column-major 4x4; NaN hides a body)
 std::vector<InstPose> poses_from(const Prepared& S, const double* T0, const double* T1, uint32_t n);
 // gpu/renderer.js:642-705 _writeSceneU
+// pcaps: 8 floats per body, each body's bounding capsule at the last node-radiosity update (NaN first word or a
+// null pointer: its current capsule)
 void scene_uniform(const Prepared& S, const std::vector<InstPose>& inst, const float eavg[3], uint32_t slot, uint32_t frame,
-                   float* out /* SU_WORDS */);
+                   float* out /* SU_WORDS */, const float* pcaps = nullptr);
+
+// Smoothing neighbours of the active nodes (gpu/renderer.js:573 _neighbours): for each active node the nbr_k largest
+// Gaussian weights exp(-d^2 / 2 sigma^2) (ties: smaller active index first) over active nodes within `radius` whose
+// normals agree (n.n >= 0.9), as (active index, float weight bits) pairs, weight 0 after the last. sigma <= 0: each
+// node alone with weight 1.
+void node_neighbours(const Prepared& S, const std::vector<uint32_t>& active, uint32_t nbr_k, double radius, double sigma,
+                     std::vector<uint32_t>& out);
 // gpu/renderer.js:635 _poseAt
 bool pose_at(const InstPose& I, double t, double R[3][3], double p[3]);
 

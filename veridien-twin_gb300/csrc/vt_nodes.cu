@@ -1,0 +1,254 @@
+// The twin's node radiosity on the device (gpu/wgsl/kernels.wgsl.js:255-461): the gather table, the direct light of
+// the nodes, and the Jacobi steps of the separable node transport. Nodes are the static vertices (verts[2i] = position
+// | mesh bits, verts[2i+1] = normal | area); the node state is 4 float4 per node: E_free|V, Ls slot 1, Ls slot 2,
+// B_dir|vis (gpu/renderer.js:316-326).
+//
+// Layout in HBM: gtable u32[n_nodes x K] node-major (the K rays of a node are contiguous, so a warp reads a node's
+// row in one or two coalesced transactions), aux float4[n_nodes] (escapes after the build, then one gather result
+// per active node), active u32[n_active] ascending, nbr uint2[n_active x nbr_k] (active index, weight bits).
+// The gather kernel runs one warp per active node: a lane takes rays j = lane, lane + 32, ... and the warp adds
+// its terms by shuffles. A(mu_in) of ray j depends only on the node's material, so it comes from a per-material
+// table (n_mat x K) built once per table build instead of two albedo-table lerps per ray.
+#include "vt_kernels.cuh"
+#include "vt_nodes.cuh"
+
+namespace vtk {
+
+using namespace vtd;
+
+// gpu/wgsl/kernels.wgsl.js:271 gatherDir: K cosine-distributed rays (Fibonacci spiral on the disk, rotated per node).
+// The spiral's angle fraction is rounded after each product and sum (like the Kronecker numbers), so the CPU
+// restatement draws the same directions.
+__device__ __forceinline__ float3 gather_dir(uint32_t i, uint32_t j, uint32_t K, float3 n) {
+  const float3 t = basis_t(n), b = basis_b(n);
+  const float rot = u01(pcg(i * 2654435761u + 17u));
+  const float rr = sqrtf(__fdiv_rn(float(j) + 0.5f, float(K)));
+  const float a = __fadd_rn(__fmul_rn(float(j), GOLD), rot);
+  const float ph = 2.0f * PI_F * (a - floorf(a));
+  float sn, cs;
+  sincosf(ph, &sn, &cs);
+  return normalize(t * (rr * cs) + b * (rr * sn) + n * sqrtf(fmaxf(0.0f, 1.0f - rr * rr)));
+}
+__device__ __forceinline__ float3 node_pos(const Scene& S, uint32_t i) { return xyz(__ldg(S.verts + 2u * i)); }
+__device__ __forceinline__ float3 node_nrm(const Scene& S, uint32_t i) { return normalize(xyz(__ldg(S.verts + 2u * i + 1u))); }
+__device__ __forceinline__ uint32_t node_mat(const Scene& S, uint32_t i) {
+  return fu(__ldg(S.params + S.mesh_off + 2u * fu(__ldg(S.verts + 2u * i).w)).w);
+}
+
+// the node a gather ray lands on: the hit triangle's vertex of largest barycentric, if the ray meets its front
+__device__ __forceinline__ uint32_t gather_hit(const Scene& S, uint32_t i, uint32_t j, uint32_t K, uint32_t* tri_out, float3* bb_out) {
+  const float3 p = node_pos(S, i), n = node_nrm(S, i);
+  const float3 dir = gather_dir(i, j, K, n);
+  const Hit h = trace_scene<false>(S, 0u, p + n * EPS_OFF, dir, 0.0f, BIG, 0.5f, 1u, 0u);
+  *tri_out = h.tri;
+  if (h.tri == MISS) return MISS;
+  const float3 bb = f3(1.0f - h.u - h.v, h.u, h.v);
+  *bb_out = bb;
+  const float4* r = S.tris + 4u * h.tri;
+  const uint32_t v0 = fu(__ldg(r).w), v1 = fu(__ldg(r + 1).w), v2 = fu(__ldg(r + 2).w);
+  const float3 nv = xyz(__ldg(S.verts + 2u * v0 + 1u)) * bb.x + xyz(__ldg(S.verts + 2u * v1 + 1u)) * bb.y + xyz(__ldg(S.verts + 2u * v2 + 1u)) * bb.z;
+  if (!(dot(nv, dir) < 0.0f)) return MISS;
+  if (bb.x >= bb.y && bb.x >= bb.z) return v0;
+  return bb.y >= bb.z ? v1 : v2;
+}
+
+__global__ void gather_build_kernel(const Scene S, uint32_t n_nodes, uint32_t K, uint32_t* __restrict__ gtable) {
+  const size_t total = size_t(n_nodes) * K;
+  for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < total; r += size_t(gridDim.x) * blockDim.x) {
+    uint32_t tri;
+    float3 bb;
+    gtable[r] = gather_hit(S, uint32_t(r / K), uint32_t(r % K), K, &tri, &bb);
+  }
+}
+
+// escapes per node (gpu/wgsl/kernels.wgsl.js:326 gatherCount)
+__global__ void gather_count_kernel(uint32_t n_nodes, uint32_t K, const uint32_t* __restrict__ gtable, float4* __restrict__ aux) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_nodes; i += gridDim.x * blockDim.x) {
+    uint32_t m = 0;
+    for (uint32_t j = 0; j < K; j++) m += gtable[size_t(i) * K + j] == MISS;
+    aux[i] = make_float4(float(m), 0.0f, 0.0f, 0.0f);
+  }
+}
+
+// entries that point at an inactive node go to the hit triangle's active vertex of largest barycentric, if any
+// (gpu/wgsl/kernels.wgsl.js:300 gatherRemap)
+__global__ void gather_remap_kernel(const Scene S, uint32_t n_nodes, uint32_t K, uint32_t* __restrict__ gtable, const float4* __restrict__ aux) {
+  const size_t total = size_t(n_nodes) * K;
+  const float half = 0.5f * float(K);
+  for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < total; r += size_t(gridDim.x) * blockDim.x) {
+    const uint32_t v0 = gtable[r];
+    if (v0 == MISS || aux[v0].x <= half) continue;
+    const uint32_t i = uint32_t(r / K), j = uint32_t(r % K);
+    const float3 p = node_pos(S, i), n = node_nrm(S, i);
+    const float3 dir = gather_dir(i, j, K, n);
+    const Hit h = trace_scene<false>(S, 0u, p + n * EPS_OFF, dir, 0.0f, BIG, 0.5f, 1u, 0u);
+    if (h.tri == MISS) continue;
+    const float3 bb = f3(1.0f - h.u - h.v, h.u, h.v);
+    const float4* t = S.tris + 4u * h.tri;
+    const uint32_t a = fu(__ldg(t).w), b = fu(__ldg(t + 1).w), c = fu(__ldg(t + 2).w);
+    uint32_t best = v0;
+    float bw = -1.0f;
+    if (aux[a].x <= half && bb.x > bw) { best = a; bw = bb.x; }
+    if (aux[b].x <= half && bb.y > bw) { best = b; bw = bb.y; }
+    if (aux[c].x <= half && bb.z > bw) { best = c; bw = bb.z; }
+    gtable[r] = best;
+  }
+}
+
+// A(mu_in of ray j) per material: amu[m * K + j] (the table the gather kernel reads)
+__global__ void amu_kernel(const Scene S, uint32_t n_mat, uint32_t K, float4* __restrict__ amu) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_mat * K; k += gridDim.x * blockDim.x) {
+    const uint32_t m = k / K, j = k % K;
+    const float mu = sqrtf(fmaxf(0.0f, 1.0f - __fdiv_rn(float(j) + 0.5f, float(K))));
+    const float3 a = albedo(S, m, mu);
+    amu[k] = make_float4(a.x, a.y, a.z, 0.0f);
+  }
+}
+
+// gpu/wgsl/kernels.wgsl.js:348 nodeDirect: direct irradiance at each active node from node_samples emitter samples
+// (shadow rays through the whole scene at mid-exposure), its first reflection B_dir = sum E_s A(mu_s), the
+// visibility code (1 all lit samples visible, 0 none, 0.5 mixed, -1 no lit sample) and the capsule visibility V.
+// moved != 0: only nodes whose segment to the emitter passes near a moved body's bounding capsule, now or at the
+// last full update.
+__global__ void node_direct_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t NS, uint32_t moved,
+                                   float4* __restrict__ nstate) {
+  const uint32_t skip = ldu(S.su + 7);
+  const float area = __ldg(S.su + 3);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_active; k += gridDim.x * blockDim.x) {
+    const uint32_t i = active[k];
+    const float3 p = node_pos(S, i), n = node_nrm(S, i);
+    if (moved) {
+      Rot R;
+      float3 pp;
+      inst_pose(S, ldu(S.su + 17), 0.5f, R, pp);
+      const float3 dE = (rmul(R, ld3(S.su + 20)) + pp) - p;
+      const float rr = __ldg(S.su + 23) + 1e-3f;
+      bool near = false;
+      const uint32_t cnt = min(ldu(S.su + 16), uint32_t(VT_MAX_INST));
+      for (uint32_t b = 0; b < cnt && !near; b++) {
+        if (!((moved >> b) & 1u)) continue;
+        const float* I = inst_rec(S, b);
+        near = seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 32), ld3(I + 36), __ldg(I + 35) + rr) ||
+               seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 40), ld3(I + 44), __ldg(I + 43) + rr);
+      }
+      if (!near) continue;
+    }
+    const uint32_t m = node_mat(S, i);
+    const uint32_t hs = pcg(i * 2246822519u + 3u);
+    const float s0 = u01(pcg(hs)), s1 = u01(pcg(hs + 1u)), s2 = u01(pcg(hs + 2u));
+    float3 B = f3(0, 0, 0);
+    uint32_t n_lit = 0, n_vis = 0;
+    const float3 o = p + n * EPS_OFF;
+    for (uint32_t s = 0; s < NS; s++) {
+      float3 lp, ln, la;
+      sample_emitter(S, f3(kr(s, KL0, s0), kr(s, KL1, s1), kr(s, KL2, s2)), 0.5f, lp, ln, la);
+      float3 wi = lp - p;
+      const float d2 = dot(wi, wi), dist = sqrtf(d2);
+      wi = wi / dist;
+      const float cosE = dot(-wi, ln), cosN = dot(n, wi);
+      if (cosE <= 0.0f || cosN <= 0.0f) continue;
+      const float3 Le = emitted(S, ln, la, -wi);
+      if (maxc(Le) <= 0.0f) continue;
+      n_lit++;
+      if (trace_scene<true>(S, 0u, o, wi, 0.0f, dist - 2e-5f, 0.5f, 3u, skip).tri != MISS) continue;
+      n_vis++;
+      B = B + Le * (cosE * cosN * area / d2) * albedo(S, m, cosN);
+    }
+    B = B / float(NS);
+    const float vis = n_lit == 0 ? -1.0f : n_vis == n_lit ? 1.0f : n_vis == 0 ? 0.0f : 0.5f;
+    nstate[4u * i + 3u] = make_float4(B.x, B.y, B.z, vis);
+    const float4 old = nstate[4u * i];
+    nstate[4u * i] = make_float4(old.x, old.y, old.z, capsule_vis(S, p, n));
+  }
+}
+
+// jacobiGather (gpu/wgsl/kernels.wgsl.js:416): aux[k] = (pi / K) sum_j A_i(mu_in_j) A_h(mu_out_j) Ls_h / hh_i over
+// the rays that land on a node h. One warp per active node.
+__global__ void __launch_bounds__(256) jacobi_gather_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t K,
+                                                            const uint32_t* __restrict__ gtable, const float4* __restrict__ amu,
+                                                            uint32_t slot_in, const float4* __restrict__ nstate, float4* __restrict__ aux) {
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n_active; k += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t i = active[k];
+    const float3 n = node_nrm(S, i);
+    const uint32_t mi = node_mat(S, i);
+    float3 acc = f3(0, 0, 0);
+    for (uint32_t j = lane; j < K; j += 32) {
+      const uint32_t h = gtable[size_t(i) * K + j];
+      if (h == MISS) continue;
+      const float3 dir = gather_dir(i, j, K, n);
+      const float mu_out = clampf(-dot(dir, node_nrm(S, h)), 0.0f, 1.0f);
+      acc = acc + xyz(__ldg(amu + mi * K + j)) * albedo(S, node_mat(S, h), mu_out) * xyz(nstate[4u * h + slot_in]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+    }
+    if (lane == 0) {
+      const float4* M = S.params + S.mat_off + 5u * mi;
+      const float3 hh = xyz(__ldg(M + 2));
+      const float sc = PI_F / float(K);
+      aux[k] = make_float4(acc.x * sc / fmaxf(hh.x, 1e-4f), acc.y * sc / fmaxf(hh.y, 1e-4f), acc.z * sc / fmaxf(hh.z, 1e-4f), 0.0f);
+    }
+  }
+}
+
+// jacobiUpdate (gpu/wgsl/kernels.wgsl.js:440): E_free = weighted mean of aux over the node's neighbours, and the
+// separable source Ls = (B_dir + E_free V hh) / (pi hh) into slot_out (w = 1 marks a solved node)
+__global__ void jacobi_update_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, const uint2* __restrict__ nbr,
+                                     uint32_t nbr_k, const float4* __restrict__ aux, uint32_t slot_out, float4* __restrict__ nstate) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_active; k += gridDim.x * blockDim.x) {
+    const uint32_t i = active[k];
+    float3 ef = f3(0, 0, 0);
+    float ws = 0.0f;
+    for (uint32_t j = 0; j < nbr_k; j++) {
+      const uint2 e = nbr[size_t(k) * nbr_k + j];
+      const float w = __uint_as_float(e.y);
+      if (w <= 0.0f) break;
+      ef = ef + xyz(aux[e.x]) * w;
+      ws += w;
+    }
+    ef = ws > 0.0f ? ef / ws : xyz(aux[k]);
+    const float4 st = nstate[4u * i];
+    const float4* M = S.params + S.mat_off + 5u * node_mat(S, i);
+    const float3 hh = xyz(__ldg(M + 2));
+    const float3 hm = f3(fmaxf(hh.x, 1e-4f), fmaxf(hh.y, 1e-4f), fmaxf(hh.z, 1e-4f));
+    const float3 bd = xyz(nstate[4u * i + 3u]);
+    const float3 L = f3((bd.x + ef.x * st.w * hm.x) * INV_PI_F / hm.x, (bd.y + ef.y * st.w * hm.y) * INV_PI_F / hm.y,
+                        (bd.z + ef.z * st.w * hm.z) * INV_PI_F / hm.z);
+    nstate[4u * i] = make_float4(ef.x, ef.y, ef.z, st.w);
+    nstate[4u * i + slot_out] = make_float4(L.x, L.y, L.z, 1.0f);
+  }
+}
+
+static int grid_for(size_t work, int threads) {
+  const size_t g = (work + threads - 1) / threads;
+  return int(std::max<size_t>(1, std::min<size_t>(g, 152 * 64)));
+}
+
+void launch_gather_build(const Scene& S, uint32_t n_nodes, uint32_t K, uint32_t* gtable, float4* aux, cudaStream_t st) {
+  const size_t rays = size_t(n_nodes) * K;
+  gather_build_kernel<<<grid_for(rays, 128), 128, 0, st>>>(S, n_nodes, K, gtable);
+  gather_count_kernel<<<grid_for(n_nodes, 128), 128, 0, st>>>(n_nodes, K, gtable, aux);
+  gather_remap_kernel<<<grid_for(rays, 128), 128, 0, st>>>(S, n_nodes, K, gtable, aux);
+}
+
+void launch_amu(const Scene& S, uint32_t n_mat, uint32_t K, float4* amu, cudaStream_t st) {
+  amu_kernel<<<grid_for(size_t(n_mat) * K, 128), 128, 0, st>>>(S, n_mat, K, amu);
+}
+
+void launch_node_direct(const Scene& S, const uint32_t* active, uint32_t n_active, uint32_t NS, uint32_t moved, float4* nstate,
+                        cudaStream_t st) {
+  if (!n_active) return;
+  node_direct_kernel<<<grid_for(n_active, 64), 64, 0, st>>>(S, active, n_active, NS, moved, nstate);
+}
+
+void launch_jacobi_step(const Scene& S, const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, const float4* amu,
+                        const uint2* nbr, uint32_t nbr_k, uint32_t slot_in, uint32_t slot_out, float4* nstate, float4* aux, cudaStream_t st) {
+  if (!n_active) return;
+  jacobi_gather_kernel<<<grid_for(size_t(n_active) * 32, 256), 256, 0, st>>>(S, active, n_active, K, gtable, amu, slot_in, nstate, aux);
+  jacobi_update_kernel<<<grid_for(n_active, 128), 128, 0, st>>>(S, active, n_active, nbr, nbr_k, aux, slot_out, nstate);
+}
+
+}  // namespace vtk

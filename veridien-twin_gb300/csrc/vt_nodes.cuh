@@ -1,0 +1,18 @@
+// Launchers of the node radiosity kernels (vt_nodes.cu).
+#pragma once
+
+#include "vt_device.cuh"
+
+namespace vtk {
+
+// gather table of n_nodes x K rays (build, escape count into aux[i].x, remap to active nodes)
+void launch_gather_build(const vtd::Scene& S, uint32_t n_nodes, uint32_t K, uint32_t* gtable, float4* aux, cudaStream_t st);
+// A(mu_in) of each gather ray per material: n_mat x K
+void launch_amu(const vtd::Scene& S, uint32_t n_mat, uint32_t K, float4* amu, cudaStream_t st);
+void launch_node_direct(const vtd::Scene& S, const uint32_t* active, uint32_t n_active, uint32_t NS, uint32_t moved, float4* nstate,
+                        cudaStream_t st);
+// one Jacobi step: gather from slot_in into aux, update into slot_out
+void launch_jacobi_step(const vtd::Scene& S, const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, const float4* amu,
+                        const uint2* nbr, uint32_t nbr_k, uint32_t slot_in, uint32_t slot_out, float4* nstate, float4* aux, cudaStream_t st);
+
+}  // namespace vtk

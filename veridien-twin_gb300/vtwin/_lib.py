@@ -45,6 +45,14 @@ SIGNATURES = {
     "vt_radiosity_solve": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_solve_req)]),
     "vt_form_factors": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vt_form_factors_visible": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vt_nodes_build": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_nodes_opts), C.POINTER(A.vt_nodes_info)]),
+    "vt_nodes_direct": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "vt_nodes_jacobi": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "vt_nodes_update": (C.c_int32, [C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]),
+    "vt_converge": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "vt_node_summary": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vt_nodes_export": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_get_node_state": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]),
     "vt_radiosity_solve_static": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                               C.c_double, C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
     "vt_bvh_capacity": (C.c_uint32, [C.c_uint32, C.c_uint32]),

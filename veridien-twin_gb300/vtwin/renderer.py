@@ -17,9 +17,11 @@ from . import sensor as sensor_mod
 # gpu/renderer.js:31 DEFAULTS, except refine: the refinement pass is opt-in here (the reference adds 6 sub-samples on
 # edges by default), so that a default render is the plain pass-1 estimator
 DEFAULTS = {"spp": 1, "refine": 0, "refineLightSamples": 1, "refineShadows": True, "lightSamples": 4, "leafSize": 4,
-            "albedoSamples": 1024}
-PRESETS = {"judge": {}, "balanced": {"spp": 1, "lightSamples": 2, "refine": 2, "refineLightSamples": 1, "refineShadows": False},
-           "live": {"spp": 1, "lightSamples": 1, "refine": 0}}
+            "albedoSamples": 1024, "radiosityEvery": 1, "gatherK": 64, "nodeSamples": 4, "itersPerFrame": 4, "itersInitial": 96,
+            "smoothSigma": 0.003, "smoothRadius": 0.006, "nbrK": 16, "nodes": True}
+PRESETS = {"judge": {}, "balanced": {"spp": 1, "lightSamples": 2, "refine": 2, "refineLightSamples": 1, "refineShadows": False,
+                                     "radiosityEvery": 2, "itersPerFrame": 1},
+           "live": {"spp": 1, "lightSamples": 1, "refine": 0, "radiosityEvery": 2, "itersPerFrame": 1}}
 
 
 def _p(a):
@@ -52,8 +54,72 @@ class TwinRenderer:
         r.bodies = [b["key"] for b in scene.get("bodies", [])]
         r.frame = 0
         r.sensor_p = sensor_mod.sensor_params((opts or {}).get("sensor"))
+        r.nodes_info = None
+        if r.opts.get("nodes", True):     # gpu/renderer.js:256: the gather table is part of create
+            r.build_nodes()
         r.set_poses({"bodies": {}})
         return r
+
+    # ------------------------------------------------------------------------------------------- node radiosity
+    def build_nodes(self, **o):
+        """gpu/renderer.js:456 _buildGatherTable: gather table, active nodes, smoothing neighbours. Renders then keep
+        the node radiosity up to date with the poses (renderCamera's _ensureRadiosity) until set_node_state."""
+        op = {**self.opts, **o}
+        q = A.vt_nodes_opts(gather_k=int(op["gatherK"]), node_samples=int(op["nodeSamples"]), nbr_k=int(op["nbrK"]),
+                            smooth_sigma=float(op["smoothSigma"]), smooth_radius=float(op["smoothRadius"]),
+                            radiosity_every=int(op["radiosityEvery"]), iters_per_frame=int(op["itersPerFrame"]),
+                            iters_initial=int(op["itersInitial"]))
+        info = A.vt_nodes_info()
+        check(self.lib.vt_nodes_build(self._ctx, C.byref(q), C.byref(info)), self._ctx)
+        self.nodes_info = {"nodes": info.n_nodes, "activeNodes": info.n_active, "gatherK": info.gather_k, "nbrK": info.nbr_k,
+                           "gatherBuildMs": info.build_ms, "neighbourMs": info.neighbour_ms}
+        return self.nodes_info
+
+    def converge(self, iters=200):
+        """gpu/renderer.js:804 converge(iters): direct light if the poses changed, `iters` Jacobi steps, node summary
+        (eAvg). A boolean means a full solve (True: 200 steps) or none."""
+        if isinstance(iters, bool) or not isinstance(iters, (int, float)) or not np.isfinite(iters):
+            iters = 0 if iters is False else 200
+        check(self.lib.vt_converge(self._ctx, int(iters)), self._ctx)
+        return self.nodeSummary()
+
+    def nodeSummary(self) -> dict:
+        """gpu/renderer.js:825 nodeSummary(): area-weighted means over the active nodes; refreshes eAvg."""
+        out = np.zeros(13)
+        check(self.lib.vt_node_summary(self._ctx, _p(out)), self._ctx)
+        return {"area": out[0], "meanIndirect": out[1:4], "meanDirect": out[4:7], "meanLout": out[7:10], "eAvg": out[10:13]}
+
+    node_summary = nodeSummary
+
+    def update_nodes(self, force=False) -> str:
+        """gpu/renderer.js:771 _ensureRadiosity: 'none', 'full', 'incremental' or 'reused'."""
+        w = C.c_uint32(0)
+        check(self.lib.vt_nodes_update(self._ctx, int(force), C.byref(w)), self._ctx)
+        return ["none", "full", "incremental", "reused"][w.value]
+
+    def node_direct(self, moved=0):
+        check(self.lib.vt_nodes_direct(self._ctx, int(moved)), self._ctx)
+
+    def node_jacobi(self, iters):
+        check(self.lib.vt_nodes_jacobi(self._ctx, int(iters)), self._ctx)
+
+    def nodes_export(self) -> dict:
+        """Copies of the gather table (n x K), the active list, the neighbours (n_active x nbrK x 2) and the escapes."""
+        i = self.nodes_info
+        n, na, K, nk = i["nodes"], i["activeNodes"], i["gatherK"], i["nbrK"]
+        g = np.zeros((n, K), np.uint32)
+        act = np.zeros(na, np.uint32)
+        nb = np.zeros((na, nk, 2), np.uint32)
+        mis = np.zeros(n, np.float32)
+        check(self.lib.vt_nodes_export(self._ctx, _p(g), _p(act), _p(nb), _p(mis)), self._ctx)
+        return {"gtable": g, "active": act, "nbr": nb, "misses": mis}
+
+    def get_node_state(self):
+        """The node state (n_static_verts x 16 float32) and its latest slot."""
+        st = np.zeros((len(self.scene["static"]["P"]), 16), np.float32)
+        slot = C.c_uint32(0)
+        check(self.lib.vt_get_node_state(self._ctx, _p(st), C.byref(slot)), self._ctx)
+        return st, slot.value
 
     def destroy(self):
         if self._ctx is not None:
