@@ -17,6 +17,7 @@ bounded sample of the same frame; the reference itself is JavaScript + WebGPU an
   python bench.py --case radiosity1:N:PREC:SWEEPS  the same with one right-hand side (fp32|fp32tma|bf16|fp8)
   python bench.py --case batch:W:H:SPP:POSES       one 3-camera pose batch (6 instruments, depth 6, sensor on)
   python bench.py --case calib:W:H:SPP             one calibration forward + backward (3 cameras, depth 3, 4096 nodes)
+  python bench.py --case nodes                     the scene node radiosity on the level-5 and level-8 domes
 """
 import argparse
 import json
@@ -168,6 +169,7 @@ def main():
     ap.add_argument("--no-radiosity", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-calib", action="store_true")
+    ap.add_argument("--no-nodes", action="store_true")
     ap.add_argument("--case", default=None, help="render:W:H:SPP or radiosity:N:PREC:SWEEPS (a small profiling case)")
     args = ap.parse_args()
     if args.case:
@@ -282,6 +284,8 @@ def main():
             line["batched"] = batch_bench(torch, local)
         if not args.no_calib:
             line["calibration"] = calib_bench(torch, local)
+        if not args.no_nodes:
+            line["scene_nodes"] = nodes_bench(torch, local)
         print(json.dumps(line))
     r.destroy()
     if dist:
@@ -341,6 +345,8 @@ def run_case(spec):
             out = r.render_batch([0, 1, 2], P, spp=spp, max_depth=6, sensor=sensor_mod.unit_radiance_sensor(), use_graph=False)
         print(json.dumps({"case": spec, **out["stats"]}))
         r.destroy()
+    elif kind == "nodes":
+        print(json.dumps({"case": spec, **nodes_bench(torch)}))
     elif kind == "calib":
         from vtwin.renderer import TwinRenderer
 
@@ -501,6 +507,52 @@ def calib_bench(torch, device=0):
             "grad_check": {"entries": len(ids), "h": 3e-3, "vector_rel_err": vec, "worst_entry_rel_err": worst,
                            "note": "GPU central differences of the FP32 render (FP64 loss); FP64-oracle differences at "
                                    "h = 1e-4 are in tests/test_gpu_calib.py"}}
+
+
+def nodes_bench(torch, device=0):
+    """The scene's node radiosity (gpu/renderer.js:456-851): gather-table build, one live-preset update (direct light
+    of every active node + one Jacobi step, the reference's "per update"), Jacobi steps from the transport table and
+    with per-step factors, and converge(96). On the config-0 dome and on a level-8 dome (657k triangles, 331k
+    nodes), the size of the reference's own scene (~0.5 M triangles)."""
+    from vtwin import dome
+    from vtwin.renderer import TwinRenderer
+
+    out = {}
+    for name, level in (("dome_l5", 5), ("dome_l8", 8)):
+        sc = dome.make_dome_scene(seed=1, width=64, height=48, level=level)
+        res = {}
+        for per_step in (False, True):
+            r = TwinRenderer.create(sc, device=device, perStepFactors=per_step)
+            info = dict(r.nodes_info)
+            r.node_direct(0)
+            r.node_jacobi(8)                       # warm-up
+            torch.cuda.synchronize()
+            d_ms, j_ms = [], []
+            for _ in range(5):
+                r.node_direct(0)
+                r.node_jacobi(1)
+                t = r.timings()
+                d_ms.append(t["node_direct_ms"])
+                j_ms.append(t["node_jacobi_ms"])
+            r.node_jacobi(50)
+            step_ms = r.timings()["node_jacobi_ms"] / 50
+            key = "per_step_factors" if per_step else "table"
+            res[key] = {"jacobi_step_ms": step_ms, "update_ms": float(np.median(d_ms) + np.median(j_ms)),
+                        "direct_ms": float(np.median(d_ms))}
+            if not per_step:
+                t0 = time.perf_counter()
+                s = r.converge(96)
+                res["converge96_wall_ms"] = (time.perf_counter() - t0) * 1e3
+                res["converge96_jacobi_ms"] = r.timings()["node_jacobi_ms"]
+                res["eAvg"] = [float(x) for x in s["eAvg"]]
+                res.update(nodes=info["nodes"], active=info["activeNodes"], table_entries=info["tableEntries"],
+                           gather_build_ms=info["gatherBuildMs"], neighbour_ms=info["neighbourMs"], gather_k=info["gatherK"])
+                # algorithmic bytes of a table step: entries (16 B) + the landing nodes' Ls (16 B each) + aux / state
+                res["table_step_bytes"] = info["tableEntries"] * 32 + info["activeNodes"] * (16 * 3 + 16 * info["nbrK"])
+            r.destroy()
+        res["table_step_gbs"] = res["table_step_bytes"] / (res["table"]["jacobi_step_ms"] / 1e3) / 1e9
+        out[name] = res
+    return out
 
 
 def radiosity_bench(torch, cpu_check=True):

@@ -408,6 +408,8 @@ typedef struct {
   uint32_t radiosity_every; /* update on every n-th pose change (1) */
   uint32_t iters_per_frame; /* Jacobi steps per update (4) */
   uint32_t iters_initial;   /* Jacobi steps of the first solve, 8 at once and the rest spread over updates (96) */
+  uint32_t per_step_factors;/* 0: each landing ray's transport factor is evaluated once per build into a table of
+                               16 B per ray (a Jacobi gather is then a sparse product); 1: evaluated in every step */
 } vt_nodes_opts;
 typedef struct {
   uint32_t n_nodes;         /* static vertices */
@@ -415,6 +417,7 @@ typedef struct {
   uint32_t gather_k, nbr_k;
   double build_ms;          /* gather table: build, count, remap (device time) */
   double neighbour_ms;      /* smoothing neighbours (host) */
+  uint64_t table_entries;   /* landing rays in the transport table (0: factors evaluated per step) */
 } vt_nodes_info;
 /* Build the gather table, the active list and the neighbours (static BVH only); node state reset to its initial
  * values. Afterwards renders run vt_nodes_update first (like renderCamera), until vt_set_node_state. opts NULL =
@@ -465,6 +468,8 @@ typedef struct {
   double extend_ms, shade_ms, shadow_ms;           /* closest-hit, shading and any-hit kernels (profiling on) */
   uint64_t extend_launches, shadow_launches;
   uint64_t extend_rays, shadow_paths;              /* rays the closest-hit kernels traced, paths the any-hit kernels served */
+  double node_direct_ms, node_jacobi_ms;           /* the node radiosity's last vt_nodes_direct / vt_nodes_jacobi (device) */
+  uint32_t node_jacobi_steps, reserved;            /* steps of that vt_nodes_jacobi call */
 } vt_timings;
 vt_status vt_timings_get(const vt_ctx* ctx, vt_timings* out);
 /* Kernel profiling of vt_render_camera: events around each traversal and shading launch (enable 1), and the

@@ -64,6 +64,8 @@ vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx**
   if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess || cudaEventCreate(&ctx->ev2) != cudaSuccess ||
       cudaEventCreate(&ctx->ev3) != cudaSuccess)
     return bail(VT_ERR_CUDA);
+  for (cudaEvent_t& e : ctx->nev)
+    if (cudaEventCreate(&e) != cudaSuccess) return bail(VT_ERR_CUDA);
   const vt::Prepared& S = ctx->S;
   vt_status s;
   if ((s = upload(ctx, &ctx->d_nodes, S.nodes.data(), S.nodes.size() * 4)) != VT_OK) return bail(s);
@@ -106,6 +108,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   for (auto& e : ctx->kev) cudaEventDestroy(e);
   cudaFree(ctx->calib.mem);
   cudaFree(ctx->nodes.mem);
+  cudaFree(ctx->nodes.table_mem);
   cudaFree(ctx->calib.records);
   for (float4* p : ctx->calib.image) cudaFree(p);
   for (float4* p : ctx->calib.target) cudaFree(p);
@@ -113,6 +116,8 @@ vt_status vt_destroy(vt_ctx* ctx) {
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->ev2) cudaEventDestroy(ctx->ev2);
   if (ctx->ev3) cudaEventDestroy(ctx->ev3);
+  for (cudaEvent_t e : ctx->nev)
+    if (e) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -471,6 +476,13 @@ vt_status vt_debug_flags(vt_ctx* ctx, uint32_t out[16], int reset) {
 vt_status vt_timings_get(const vt_ctx* ctx, vt_timings* out) {
   if (!ctx || !out) return VT_ERR_ARG;
   *out = ctx->tim;
+  // the node radiosity's last direct-light and Jacobi calls (events on the context's stream)
+  float ms = 0;
+  if (ctx->nodes.timed_direct && cudaEventSynchronize(ctx->nev[1]) == cudaSuccess && cudaEventElapsedTime(&ms, ctx->nev[0], ctx->nev[1]) == cudaSuccess)
+    out->node_direct_ms = ms;
+  if (ctx->nodes.timed_jacobi && cudaEventSynchronize(ctx->nev[3]) == cudaSuccess && cudaEventElapsedTime(&ms, ctx->nev[2], ctx->nev[3]) == cudaSuccess)
+    out->node_jacobi_ms = ms;
+  out->node_jacobi_steps = ctx->nodes.last_steps;
   return VT_OK;
 }
 

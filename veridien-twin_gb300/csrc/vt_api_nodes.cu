@@ -66,6 +66,7 @@ vt_status vt_nodes_build(vt_ctx* ctx, const vt_nodes_opts* opts, vt_nodes_info* 
                b_nbr = al(size_t(n) * o.nbr_k * 8 + 8), b_amu = al(size_t(n_mat) * K * 16);
   VT_CK(cudaStreamSynchronize(ctx->stream));
   cudaFree(N.mem);
+  cudaFree(N.table_mem);
   N = vt_ctx::Nodes{};
   if (cudaMalloc(&N.mem, b_g + b_aux + b_act + b_nbr + b_amu) != cudaSuccess) {
     cudaGetLastError();
@@ -116,12 +117,35 @@ vt_status vt_nodes_build(vt_ctx* ctx, const vt_nodes_opts* opts, vt_nodes_info* 
   }
   vtk::launch_amu(S, n_mat, K, N.amu, ctx->stream);
   VT_CK(cudaGetLastError());
+  // the transport table: row offsets from the landing-ray counts (aux holds the counts for a moment), then entries
+  if (!o.per_step_factors && N.n_active) {
+    uint32_t* cnt_d = reinterpret_cast<uint32_t*>(N.aux);
+    vtk::launch_transport_count(N.active, N.n_active, K, N.gtable, cnt_d, ctx->stream);
+    std::vector<uint32_t> cnt(N.n_active), row(size_t(N.n_active) + 1, 0u);
+    VT_CK(cudaMemcpyAsync(cnt.data(), cnt_d, size_t(N.n_active) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+    uint64_t nnz = 0;
+    for (uint32_t k = 0; k < N.n_active; k++) { row[k] = uint32_t(nnz); nnz += cnt[k]; }
+    const size_t b_row = al((size_t(N.n_active) + 1) * 4);
+    if (nnz < (uint64_t(1) << 32) && cudaMalloc(&N.table_mem, b_row + size_t(nnz) * 16 + 16) == cudaSuccess) {
+      row[N.n_active] = uint32_t(nnz);
+      N.row = static_cast<uint32_t*>(N.table_mem);
+      N.ent = reinterpret_cast<float4*>(static_cast<char*>(N.table_mem) + b_row);
+      N.nnz = nnz;
+      VT_CK(cudaMemcpyAsync(N.row, row.data(), row.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+      vtk::launch_transport_fill(S, N.active, N.n_active, K, N.gtable, N.amu, N.row, N.ent, ctx->stream);
+      VT_CK(cudaGetLastError());
+    } else {
+      cudaGetLastError();   // too large for the device: the factors are evaluated per step
+      N.table_mem = nullptr;
+    }
+  }
   VT_CK(cudaStreamSynchronize(ctx->stream));
   N.built = true;
   N.auto_update = true;
   if (info) {
     info->n_nodes = n; info->n_active = N.n_active; info->gather_k = K; info->nbr_k = o.nbr_k;
-    info->build_ms = N.build_ms; info->neighbour_ms = N.nbr_ms;
+    info->build_ms = N.build_ms; info->neighbour_ms = N.nbr_ms; info->table_entries = N.nnz;
   }
   return VT_OK;
 }
@@ -129,8 +153,11 @@ vt_status vt_nodes_build(vt_ctx* ctx, const vt_nodes_opts* opts, vt_nodes_info* 
 vt_status vt_nodes_direct(vt_ctx* ctx, uint32_t moved) {
   if (!ctx) return VT_ERR_ARG;
   if (!ctx->nodes.built) return fail(ctx, VT_ERR_ARG, "nodes: vt_nodes_build first");
+  VT_CK(cudaEventRecord(ctx->nev[0], ctx->stream));
   vtk::launch_node_direct(dev_scene(ctx), ctx->nodes.active, ctx->nodes.n_active, ctx->nodes.o.node_samples, moved, ctx->d_nstate, ctx->stream);
   VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->nev[1], ctx->stream));
+  ctx->nodes.timed_direct = true;
   return VT_OK;
 }
 
@@ -140,13 +167,17 @@ vt_status vt_nodes_jacobi(vt_ctx* ctx, uint32_t iters) {
   if (!N.built) return fail(ctx, VT_ERR_ARG, "nodes: vt_nodes_build first");
   const vtd::Scene S = dev_scene(ctx);
   uint32_t slot = ctx->slot ? ctx->slot : 1;
+  VT_CK(cudaEventRecord(ctx->nev[2], ctx->stream));
   for (uint32_t k = 0; k < iters; k++) {
     const uint32_t out = slot == 1 ? 2 : 1;
-    vtk::launch_jacobi_step(S, N.active, N.n_active, N.o.gather_k, N.gtable, N.amu, N.nbr, N.o.nbr_k, slot, out, ctx->d_nstate, N.aux,
-                            ctx->stream);
+    vtk::launch_jacobi_step(S, N.active, N.n_active, N.o.gather_k, N.gtable, N.amu, N.row, N.ent, N.nbr, N.o.nbr_k, slot, out,
+                            ctx->d_nstate, N.aux, ctx->stream);
     slot = out;
   }
   VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->nev[3], ctx->stream));
+  N.timed_jacobi = true;
+  N.last_steps = iters;
   ctx->slot = slot;
   return write_su(ctx);
 }

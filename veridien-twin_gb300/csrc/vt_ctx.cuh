@@ -17,6 +17,7 @@ struct vt_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  cudaEvent_t nev[4] = {nullptr, nullptr, nullptr, nullptr};   // node radiosity: direct light, Jacobi steps
   std::string err;
   vt::Prepared S;
   std::vector<vt::InstPose> inst;
@@ -106,6 +107,10 @@ struct vt_ctx {
     uint32_t* active = nullptr;
     uint2* nbr = nullptr;
     float4* amu = nullptr;
+    void* table_mem = nullptr;               // transport table: row offsets, then entries
+    uint32_t* row = nullptr;
+    float4* ent = nullptr;
+    uint64_t nnz = 0;
     std::vector<uint32_t> active_h;
     std::vector<float> misses;
     uint64_t poses_version = 0;
@@ -115,6 +120,8 @@ struct vt_ctx {
     std::vector<vt::InstPose> solved_inst;   // poses of the last update
     std::vector<float> solved_caps;          // 8 floats per body: bounding capsules of the last update
     double build_ms = 0, nbr_ms = 0;
+    bool timed_direct = false, timed_jacobi = false;
+    uint32_t last_steps = 0;
   } nodes;
 };
 

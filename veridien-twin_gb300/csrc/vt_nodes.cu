@@ -162,6 +162,84 @@ __global__ void node_direct_kernel(const Scene S, const uint32_t* __restrict__ a
   }
 }
 
+// The same with one thread per (node, emitter sample): G = NS threads of a warp share a node (NS divides 32), each
+// traces one shadow ray, and the node's first lane adds the group's terms in sample order as the loop above does.
+template <uint32_t G>
+__global__ void __launch_bounds__(256) node_direct_group_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t moved,
+                                                                float4* __restrict__ nstate) {
+  const uint32_t skip = ldu(S.su + 7);
+  const float area = __ldg(S.su + 3);
+  const uint32_t lane = threadIdx.x & 31u, s = lane % G, lead = lane - s;
+  const size_t total = size_t(n_active) * G;
+  const size_t stride = size_t(gridDim.x) * blockDim.x;
+  // whole warps iterate together (the shuffles below need every lane)
+  for (size_t base = size_t(blockIdx.x) * blockDim.x + (threadIdx.x - lane); base < total; base += stride) {
+    const size_t t = base + lane;
+    const bool in = t < total;
+    const uint32_t k = in ? uint32_t(t / G) : 0u;
+    const uint32_t i = in ? active[k] : 0u;
+    const float3 p = node_pos(S, i), n = node_nrm(S, i);
+    bool run = in;
+    if (in && moved) {
+      Rot R;
+      float3 pp;
+      inst_pose(S, ldu(S.su + 17), 0.5f, R, pp);
+      const float3 dE = (rmul(R, ld3(S.su + 20)) + pp) - p;
+      const float rr = __ldg(S.su + 23) + 1e-3f;
+      bool near = false;
+      const uint32_t cnt = min(ldu(S.su + 16), uint32_t(VT_MAX_INST));
+      for (uint32_t b = 0; b < cnt && !near; b++) {
+        if (!((moved >> b) & 1u)) continue;
+        const float* I = inst_rec(S, b);
+        near = seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 32), ld3(I + 36), __ldg(I + 35) + rr) ||
+               seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 40), ld3(I + 44), __ldg(I + 43) + rr);
+      }
+      run = near;
+    }
+    float3 c = f3(0, 0, 0);
+    uint32_t lit = 0, vis = 0;
+    const uint32_t m = run ? node_mat(S, i) : 0u;
+    if (run) {
+      const uint32_t hs = pcg(i * 2246822519u + 3u);
+      const float s0 = u01(pcg(hs)), s1 = u01(pcg(hs + 1u)), s2 = u01(pcg(hs + 2u));
+      float3 lp, ln, la;
+      sample_emitter(S, f3(kr(s, KL0, s0), kr(s, KL1, s1), kr(s, KL2, s2)), 0.5f, lp, ln, la);
+      float3 wi = lp - p;
+      const float d2 = dot(wi, wi), dist = sqrtf(d2);
+      wi = wi / dist;
+      const float cosE = dot(-wi, ln), cosN = dot(n, wi);
+      if (cosE > 0.0f && cosN > 0.0f) {
+        const float3 Le = emitted(S, ln, la, -wi);
+        if (maxc(Le) > 0.0f) {
+          lit = 1;
+          if (trace_scene<true>(S, 0u, p + n * EPS_OFF, wi, 0.0f, dist - 2e-5f, 0.5f, 3u, skip).tri == MISS) {
+            vis = 1;
+            c = Le * (cosE * cosN * area / d2) * albedo(S, m, cosN);
+          }
+        }
+      }
+    }
+    // the group's lead adds the terms of samples 0, 1, ... in order
+    float3 B = f3(0, 0, 0);
+    uint32_t n_lit = 0, n_vis = 0;
+    for (uint32_t q = 0; q < G; q++) {
+      const float cx = __shfl_sync(0xffffffffu, c.x, lead + q), cy = __shfl_sync(0xffffffffu, c.y, lead + q),
+                  cz = __shfl_sync(0xffffffffu, c.z, lead + q);
+      const uint32_t lq = __shfl_sync(0xffffffffu, lit, lead + q), vq = __shfl_sync(0xffffffffu, vis, lead + q);
+      if (vq) B = B + f3(cx, cy, cz);
+      n_lit += lq;
+      n_vis += vq;
+    }
+    if (run && s == 0) {
+      B = B / float(G);
+      const float v = n_lit == 0 ? -1.0f : n_vis == n_lit ? 1.0f : n_vis == 0 ? 0.0f : 0.5f;
+      nstate[4u * i + 3u] = make_float4(B.x, B.y, B.z, v);
+      const float4 old = nstate[4u * i];
+      nstate[4u * i] = make_float4(old.x, old.y, old.z, capsule_vis(S, p, n));
+    }
+  }
+}
+
 // jacobiGather (gpu/wgsl/kernels.wgsl.js:416): aux[k] = (pi / K) sum_j A_i(mu_in_j) A_h(mu_out_j) Ls_h / hh_i over
 // the rays that land on a node h. One warp per active node.
 __global__ void __launch_bounds__(256) jacobi_gather_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t K,
@@ -222,6 +300,69 @@ __global__ void jacobi_update_kernel(const Scene S, const uint32_t* __restrict__
   }
 }
 
+// ------------------------------------------------------------------------------------------------ transport table
+// The gather's per-ray factor (pi / K) A_i(mu_in_j) A_h(mu_out_j) / hh_i depends only on the static geometry and
+// the materials, so it is evaluated once per table build into a compressed row per active node: one float4 per
+// landing ray (weight rgb, node bits), rays in index order, escapes dropped. A Jacobi gather is then a sparse
+// matrix-vector product: one coalesced 16-byte load per entry plus the landing node's Ls (L2-resident).
+__global__ void transport_count_kernel(const uint32_t* __restrict__ active, uint32_t n_active, uint32_t K, const uint32_t* __restrict__ gtable,
+                                       uint32_t* __restrict__ cnt) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_active; k += gridDim.x * blockDim.x) {
+    const uint32_t i = active[k];
+    uint32_t c = 0;
+    for (uint32_t j = 0; j < K; j++) c += gtable[size_t(i) * K + j] != MISS;
+    cnt[k] = c;
+  }
+}
+
+__global__ void __launch_bounds__(256) transport_fill_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t K,
+                                                             const uint32_t* __restrict__ gtable, const float4* __restrict__ amu,
+                                                             const uint32_t* __restrict__ row, float4* __restrict__ ent) {
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n_active; k += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t i = active[k];
+    const float3 n = node_nrm(S, i);
+    const uint32_t mi = node_mat(S, i);
+    const float3 hh = xyz(__ldg(S.params + S.mat_off + 5u * mi + 2u));
+    const float sc = PI_F / float(K);
+    const float3 f = f3(sc / fmaxf(hh.x, 1e-4f), sc / fmaxf(hh.y, 1e-4f), sc / fmaxf(hh.z, 1e-4f));
+    uint32_t base = row[k];
+    for (uint32_t j0 = 0; j0 < K; j0 += 32) {
+      const uint32_t j = j0 + lane;
+      const uint32_t h = j < K ? gtable[size_t(i) * K + j] : MISS;
+      const bool valid = h != MISS;
+      const uint32_t m = __ballot_sync(0xffffffffu, valid);
+      if (valid) {
+        const float3 dir = gather_dir(i, j, K, n);
+        const float mu_out = clampf(-dot(dir, node_nrm(S, h)), 0.0f, 1.0f);
+        const float3 w = xyz(__ldg(amu + mi * K + j)) * albedo(S, node_mat(S, h), mu_out) * f;
+        ent[base + __popc(m & ((1u << lane) - 1u))] = make_float4(w.x, w.y, w.z, __uint_as_float(h));
+      }
+      base += __popc(m);
+    }
+  }
+}
+
+// jacobiGather over the transport table: aux[k] = sum over the row of weight x Ls_h
+__global__ void __launch_bounds__(256) jacobi_gather_table_kernel(const uint32_t* __restrict__ row, const float4* __restrict__ ent, uint32_t n_active,
+                                                                  uint32_t slot_in, const float4* __restrict__ nstate, float4* __restrict__ aux) {
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n_active; k += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t e0 = row[k], e1 = row[k + 1];
+    float3 acc = f3(0, 0, 0);
+    for (uint32_t e = e0 + lane; e < e1; e += 32) {
+      const float4 w = __ldg(ent + e);
+      acc = acc + xyz(w) * xyz(nstate[4u * __float_as_uint(w.w) + slot_in]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+    }
+    if (lane == 0) aux[k] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+  }
+}
+
 static int grid_for(size_t work, int threads) {
   const size_t g = (work + threads - 1) / threads;
   return int(std::max<size_t>(1, std::min<size_t>(g, 152 * 64)));
@@ -241,13 +382,37 @@ void launch_amu(const Scene& S, uint32_t n_mat, uint32_t K, float4* amu, cudaStr
 void launch_node_direct(const Scene& S, const uint32_t* active, uint32_t n_active, uint32_t NS, uint32_t moved, float4* nstate,
                         cudaStream_t st) {
   if (!n_active) return;
-  node_direct_kernel<<<grid_for(n_active, 64), 64, 0, st>>>(S, active, n_active, NS, moved, nstate);
+  const size_t t = size_t(n_active);
+  switch (NS) {   // one thread per emitter sample when the samples of a node fit a warp evenly
+    case 1: node_direct_group_kernel<1><<<grid_for(t, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
+    case 2: node_direct_group_kernel<2><<<grid_for(t * 2, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
+    case 4: node_direct_group_kernel<4><<<grid_for(t * 4, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
+    case 8: node_direct_group_kernel<8><<<grid_for(t * 8, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
+    case 16: node_direct_group_kernel<16><<<grid_for(t * 16, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
+    case 32: node_direct_group_kernel<32><<<grid_for(t * 32, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
+    default: node_direct_kernel<<<grid_for(t, 64), 64, 0, st>>>(S, active, n_active, NS, moved, nstate);
+  }
+}
+
+void launch_transport_count(const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, uint32_t* cnt, cudaStream_t st) {
+  if (!n_active) return;
+  transport_count_kernel<<<grid_for(n_active, 128), 128, 0, st>>>(active, n_active, K, gtable, cnt);
+}
+
+void launch_transport_fill(const Scene& S, const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, const float4* amu,
+                           const uint32_t* row, float4* ent, cudaStream_t st) {
+  if (!n_active) return;
+  transport_fill_kernel<<<grid_for(size_t(n_active) * 32, 256), 256, 0, st>>>(S, active, n_active, K, gtable, amu, row, ent);
 }
 
 void launch_jacobi_step(const Scene& S, const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, const float4* amu,
-                        const uint2* nbr, uint32_t nbr_k, uint32_t slot_in, uint32_t slot_out, float4* nstate, float4* aux, cudaStream_t st) {
+                        const uint32_t* row, const float4* ent, const uint2* nbr, uint32_t nbr_k, uint32_t slot_in, uint32_t slot_out,
+                        float4* nstate, float4* aux, cudaStream_t st) {
   if (!n_active) return;
-  jacobi_gather_kernel<<<grid_for(size_t(n_active) * 32, 256), 256, 0, st>>>(S, active, n_active, K, gtable, amu, slot_in, nstate, aux);
+  if (ent)
+    jacobi_gather_table_kernel<<<grid_for(size_t(n_active) * 32, 256), 256, 0, st>>>(row, ent, n_active, slot_in, nstate, aux);
+  else
+    jacobi_gather_kernel<<<grid_for(size_t(n_active) * 32, 256), 256, 0, st>>>(S, active, n_active, K, gtable, amu, slot_in, nstate, aux);
   jacobi_update_kernel<<<grid_for(n_active, 128), 128, 0, st>>>(S, active, n_active, nbr, nbr_k, aux, slot_out, nstate);
 }
 

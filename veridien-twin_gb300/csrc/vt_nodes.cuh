@@ -11,8 +11,14 @@ void launch_gather_build(const vtd::Scene& S, uint32_t n_nodes, uint32_t K, uint
 void launch_amu(const vtd::Scene& S, uint32_t n_mat, uint32_t K, float4* amu, cudaStream_t st);
 void launch_node_direct(const vtd::Scene& S, const uint32_t* active, uint32_t n_active, uint32_t NS, uint32_t moved, float4* nstate,
                         cudaStream_t st);
-// one Jacobi step: gather from slot_in into aux, update into slot_out
+// transport table: landing rays per active node, then the rows (row: n_active + 1 offsets, exclusive)
+void launch_transport_count(const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, uint32_t* cnt, cudaStream_t st);
+void launch_transport_fill(const vtd::Scene& S, const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, const float4* amu,
+                           const uint32_t* row, float4* ent, cudaStream_t st);
+// one Jacobi step: gather from slot_in into aux (from the transport table when ent is set, else evaluating each
+// ray's factor), update into slot_out
 void launch_jacobi_step(const vtd::Scene& S, const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, const float4* amu,
-                        const uint2* nbr, uint32_t nbr_k, uint32_t slot_in, uint32_t slot_out, float4* nstate, float4* aux, cudaStream_t st);
+                        const uint32_t* row, const float4* ent, const uint2* nbr, uint32_t nbr_k, uint32_t slot_in, uint32_t slot_out,
+                        float4* nstate, float4* aux, cudaStream_t st);
 
 }  // namespace vtk

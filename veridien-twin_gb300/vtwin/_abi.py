@@ -144,19 +144,20 @@ class vt_bvh_result(C.Structure):
 class vt_nodes_opts(C.Structure):
     _fields_ = [("gather_k", C.c_uint32), ("node_samples", C.c_uint32), ("nbr_k", C.c_uint32), ("smooth_sigma", C.c_float),
                 ("smooth_radius", C.c_float), ("radiosity_every", C.c_uint32), ("iters_per_frame", C.c_uint32),
-                ("iters_initial", C.c_uint32)]
+                ("iters_initial", C.c_uint32), ("per_step_factors", C.c_uint32)]
 
 
 class vt_nodes_info(C.Structure):
     _fields_ = [("n_nodes", C.c_uint32), ("n_active", C.c_uint32), ("gather_k", C.c_uint32), ("nbr_k", C.c_uint32),
-                ("build_ms", C.c_double), ("neighbour_ms", C.c_double)]
+                ("build_ms", C.c_double), ("neighbour_ms", C.c_double), ("table_entries", C.c_uint64)]
 
 
 class vt_timings(C.Structure):
     _fields_ = [("render_ms", C.c_double), ("sensor_ms", C.c_double), ("solve_ms", C.c_double),
                 ("trace_ms", C.c_double), ("launches", C.c_uint64), ("extend_ms", C.c_double), ("shade_ms", C.c_double),
                 ("shadow_ms", C.c_double), ("extend_launches", C.c_uint64), ("shadow_launches", C.c_uint64),
-                ("extend_rays", C.c_uint64), ("shadow_paths", C.c_uint64)]
+                ("extend_rays", C.c_uint64), ("shadow_paths", C.c_uint64), ("node_direct_ms", C.c_double),
+                ("node_jacobi_ms", C.c_double), ("node_jacobi_steps", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 def ptr(a: np.ndarray, ct):

@@ -68,11 +68,11 @@ class TwinRenderer:
         q = A.vt_nodes_opts(gather_k=int(op["gatherK"]), node_samples=int(op["nodeSamples"]), nbr_k=int(op["nbrK"]),
                             smooth_sigma=float(op["smoothSigma"]), smooth_radius=float(op["smoothRadius"]),
                             radiosity_every=int(op["radiosityEvery"]), iters_per_frame=int(op["itersPerFrame"]),
-                            iters_initial=int(op["itersInitial"]))
+                            iters_initial=int(op["itersInitial"]), per_step_factors=int(bool(op.get("perStepFactors", False))))
         info = A.vt_nodes_info()
         check(self.lib.vt_nodes_build(self._ctx, C.byref(q), C.byref(info)), self._ctx)
         self.nodes_info = {"nodes": info.n_nodes, "activeNodes": info.n_active, "gatherK": info.gather_k, "nbrK": info.nbr_k,
-                           "gatherBuildMs": info.build_ms, "neighbourMs": info.neighbour_ms}
+                           "gatherBuildMs": info.build_ms, "neighbourMs": info.neighbour_ms, "tableEntries": int(info.table_entries)}
         return self.nodes_info
 
     def converge(self, iters=200):
@@ -488,7 +488,8 @@ class TwinRenderer:
         return {"render_ms": t.render_ms, "sensor_ms": t.sensor_ms, "solve_ms": t.solve_ms, "trace_ms": t.trace_ms,
                 "launches": int(t.launches), "extend_ms": t.extend_ms, "shade_ms": t.shade_ms, "shadow_ms": t.shadow_ms,
                 "extend_launches": int(t.extend_launches), "shadow_launches": int(t.shadow_launches),
-                "extend_rays": int(t.extend_rays), "shadow_paths": int(t.shadow_paths)}
+                "extend_rays": int(t.extend_rays), "shadow_paths": int(t.shadow_paths), "node_direct_ms": t.node_direct_ms,
+                "node_jacobi_ms": t.node_jacobi_ms, "node_jacobi_steps": int(t.node_jacobi_steps)}
 
     def kernel_profile(self, enable=True, reset=True):
         """Events around the path tracer's bounce kernels (timings() then reports their device ms and rays)."""
