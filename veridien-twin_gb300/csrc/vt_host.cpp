@@ -9,6 +9,7 @@
 #include <cstring>
 #include <limits>
 #include <stdexcept>
+#include <thread>
 
 namespace vt {
 
@@ -777,39 +778,47 @@ void node_neighbours(const Prepared& S, const std::vector<uint32_t>& active, uin
   std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return keys[a] < keys[b] || (keys[a] == keys[b] && a < b); });
   std::vector<uint64_t> sorted(n);
   for (size_t q = 0; q < n; q++) sorted[q] = keys[order[q]];
-  std::vector<double> cw(K);
-  std::vector<uint32_t> cm(K);
-  for (size_t k = 0; k < n; k++) {
-    const uint32_t i = active[k];
-    const double px = vf(i, 0), py = vf(i, 1), pz = vf(i, 2), nx = vf(i, 4), ny = vf(i, 5), nz = vf(i, 6);
-    const int64_t cx = cell(px), cy = cell(py), cz = cell(pz);
-    uint32_t cnt = 0;
-    for (int dx = -1; dx <= 1; dx++)
-      for (int dy = -1; dy <= 1; dy++)
-        for (int dz = -1; dz <= 1; dz++) {
-          const uint64_t kk = key(cx + dx, cy + dy, cz + dz);
-          auto lo = std::lower_bound(sorted.begin(), sorted.end(), kk);
-          for (size_t q = size_t(lo - sorted.begin()); q < n && sorted[q] == kk; q++) {
-            const uint32_t m = order[q], j = active[m];
-            const double ex = vf(j, 0) - px, ey = vf(j, 1) - py, ez = vf(j, 2) - pz, d2 = ex * ex + ey * ey + ez * ez;
-            if (d2 > R * R) continue;
-            if (nx * vf(j, 4) + ny * vf(j, 5) + nz * vf(j, 6) < 0.9) continue;
-            const double w = std::exp(-0.5 * d2 / (sg * sg));
-            // keep the K largest (descending weight, then ascending index)
-            uint32_t pos = cnt < K ? cnt : K;
-            while (pos > 0 && (cw[pos - 1] < w || (cw[pos - 1] == w && cm[pos - 1] > m))) pos--;
-            if (pos >= K) continue;
-            for (uint32_t z = std::min(cnt, K - 1); z > pos; z--) { cw[z] = cw[z - 1]; cm[z] = cm[z - 1]; }
-            cw[pos] = w; cm[pos] = m;
-            if (cnt < K) cnt++;
+  // nodes are independent: split them over the host's threads
+  auto range = [&](size_t k0, size_t k1) {
+    std::vector<double> cw(K);
+    std::vector<uint32_t> cm(K);
+    for (size_t k = k0; k < k1; k++) {
+      const uint32_t i = active[k];
+      const double px = vf(i, 0), py = vf(i, 1), pz = vf(i, 2), nx = vf(i, 4), ny = vf(i, 5), nz = vf(i, 6);
+      const int64_t cx = cell(px), cy = cell(py), cz = cell(pz);
+      uint32_t cnt = 0;
+      for (int dx = -1; dx <= 1; dx++)
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dz = -1; dz <= 1; dz++) {
+            const uint64_t kk = key(cx + dx, cy + dy, cz + dz);
+            auto lo = std::lower_bound(sorted.begin(), sorted.end(), kk);
+            for (size_t q = size_t(lo - sorted.begin()); q < n && sorted[q] == kk; q++) {
+              const uint32_t m = order[q], j = active[m];
+              const double ex = vf(j, 0) - px, ey = vf(j, 1) - py, ez = vf(j, 2) - pz, d2 = ex * ex + ey * ey + ez * ez;
+              if (d2 > R * R) continue;
+              if (nx * vf(j, 4) + ny * vf(j, 5) + nz * vf(j, 6) < 0.9) continue;
+              const double w = std::exp(-0.5 * d2 / (sg * sg));
+              // keep the K largest (descending weight, then ascending index)
+              uint32_t pos = cnt < K ? cnt : K;
+              while (pos > 0 && (cw[pos - 1] < w || (cw[pos - 1] == w && cm[pos - 1] > m))) pos--;
+              if (pos >= K) continue;
+              for (uint32_t z = std::min(cnt, K - 1); z > pos; z--) { cw[z] = cw[z - 1]; cm[z] = cm[z - 1]; }
+              cw[pos] = w; cm[pos] = m;
+              if (cnt < K) cnt++;
+            }
           }
-        }
-    for (uint32_t z = 0; z < cnt; z++) {
-      const float wf = float(cw[z]);
-      out[(k * K + z) * 2] = cm[z];
-      std::memcpy(&out[(k * K + z) * 2 + 1], &wf, 4);
+      for (uint32_t z = 0; z < cnt; z++) {
+        const float wf = float(cw[z]);
+        out[(k * K + z) * 2] = cm[z];
+        std::memcpy(&out[(k * K + z) * 2 + 1], &wf, 4);
+      }
     }
-  }
+  };
+  const size_t nt = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), (n + 4095) / 4096));
+  if (nt == 1) { range(0, n); return; }
+  std::vector<std::thread> th;
+  for (size_t t = 0; t < nt; t++) th.emplace_back(range, n * t / nt, n * (t + 1) / nt);
+  for (auto& x : th) x.join();
 }
 
 }  // namespace vt

@@ -350,9 +350,14 @@ __global__ void __launch_bounds__(256) jacobi_gather_table_kernel(const uint32_t
   for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n_active; k += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t e0 = row[k], e1 = row[k + 1];
     float3 acc = f3(0, 0, 0);
-    for (uint32_t e = e0 + lane; e < e1; e += 32) {
-      const float4 w = __ldg(ent + e);
-      acc = acc + xyz(w) * xyz(nstate[4u * __float_as_uint(w.w) + slot_in]);
+    // 64 entries per pass, two per lane, both entry loads and then both Ls loads in flight before any use
+    for (uint32_t b = e0; b < e1; b += 64) {
+      const uint32_t ea = b + lane, eb = b + 32u + lane;
+      const float4 wa = ea < e1 ? __ldg(ent + ea) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float4 wb = eb < e1 ? __ldg(ent + eb) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float4 la = ea < e1 ? nstate[4u * __float_as_uint(wa.w) + slot_in] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float4 lb = eb < e1 ? nstate[4u * __float_as_uint(wb.w) + slot_in] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      acc = acc + xyz(wa) * xyz(la) + xyz(wb) * xyz(lb);
     }
     for (int o = 16; o > 0; o >>= 1) {
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
