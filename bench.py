@@ -18,6 +18,7 @@ bounded sample of the same frame; the reference itself is JavaScript + WebGPU an
   python bench.py --case batch:W:H:SPP:POSES       one 3-camera pose batch (6 instruments, depth 6, sensor on)
   python bench.py --case calib:W:H:SPP             one calibration forward + backward (3 cameras, depth 3, 4096 nodes)
   python bench.py --case nodes                     the scene node radiosity on the level-5 and level-8 domes
+  python bench.py --case sensor                    the camera sensor chain at 1280x720 and 1920x1200
 """
 import argparse
 import json
@@ -170,6 +171,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-calib", action="store_true")
     ap.add_argument("--no-nodes", action="store_true")
+    ap.add_argument("--no-sensor", action="store_true")
     ap.add_argument("--case", default=None, help="render:W:H:SPP or radiosity:N:PREC:SWEEPS (a small profiling case)")
     args = ap.parse_args()
     if args.case:
@@ -286,6 +288,8 @@ def main():
             line["calibration"] = calib_bench(torch, local)
         if not args.no_nodes:
             line["scene_nodes"] = nodes_bench(torch, local)
+        if not args.no_sensor:
+            line["sensor_chain"] = sensor_bench(torch, local)
         print(json.dumps(line))
     r.destroy()
     if dist:
@@ -347,6 +351,8 @@ def run_case(spec):
         r.destroy()
     elif kind == "nodes":
         print(json.dumps({"case": spec, **nodes_bench(torch)}))
+    elif kind == "sensor":
+        print(json.dumps({"case": spec, **sensor_bench(torch)}))
     elif kind == "calib":
         from vtwin.renderer import TwinRenderer
 
@@ -408,7 +414,7 @@ def batch_bench(torch, device=0):
         r.set_pose_array(P[q])
         r.renderCamera(c, spp=SPP_B, lightSamples=1, seed=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH_B)
         ms = r.timings()["render_ms"]
-        r.sensor(c, seed=0, frame=q, params=sens)
+        r.expose(c, seed=0, frame=q, params=sens)
         plain.append(W * H * SPP_B / ((ms + r.timings()["sensor_ms"]) / 1e3) / 1e6)
     r.destroy()
     pv = statistics.mean(plain)
@@ -507,6 +513,38 @@ def calib_bench(torch, device=0):
             "grad_check": {"entries": len(ids), "h": 3e-3, "vector_rel_err": vec, "worst_entry_rel_err": worst,
                            "note": "GPU central differences of the FP32 render (FP64 loss); FP64-oracle differences at "
                                    "h = 1e-4 are in tests/test_gpu_calib.py"}}
+
+
+def sensor_bench(torch, device=0):
+    """The camera sensor chain (vt_sensor_frame: optics + RI, glare, expose, demosaic, WB/CCM, NR, tone, YCbCr) at 1280x720
+    (the frame of the reference's quoted 0.195 ms on an RTX 4090 for its full chain) and 1920x1200, with the default
+    ISP and with every stage on (glare, Hamilton-Adams, bilateral NR, S-curve, unsharp mask). Device time per frame
+    (events around the chain), median of 20 frames after 3 warm-up frames."""
+    from vtwin import _abi as A
+    from vtwin import dome
+    from vtwin.renderer import TwinRenderer
+
+    full = {"glareFraction": 0.05, "demosaic": "hamilton", "noiseReduction": "bilateral", "sCurveC": 1.3, "sharpenAmount": 0.5}
+    out = {}
+    for w, h in ((1280, 720), (1920, 1200)):
+        sc = dome.make_dome_scene(seed=1, width=w, height=h, level=4)
+        r = TwinRenderer.create(sc, device=device, nodes=False)
+        r.renderCamera(0, spp=1, lightSamples=1, seed=0, mode=A.VT_SHADE_PATH, max_depth=2)
+        res = {}
+        for name, params in (("default", {}), ("all_stages", full)):
+            ms = []
+            for k in range(23):
+                r.sensor(0, seed=0, frame=k, exposure_s=2e-3, gain=1.0, params=params)
+                if k >= 3:
+                    ms.append(r.timings()["sensor_ms"])
+            res[name + "_ms"] = float(np.median(ms))
+        # algorithmic bytes of the default chain: radiance 16 B + RI 4 B in, A 16 B out / in twice, raw 4 B out / in,
+        # green plane 4 B, B 16 B out / in, 8-bit RGB 4 B and YUV 1.5 B out
+        bpp = 16 + 4 + 16 + 16 + 4 + 4 + 4 + 4 + 16 + 16 + 16 + 4 + 1.5
+        res["default_gbs"] = bpp * w * h / (res["default_ms"] / 1e3) / 1e9
+        out[f"{w}x{h}"] = res
+        r.destroy()
+    return out
 
 
 def nodes_bench(torch, device=0):

@@ -209,9 +209,10 @@ typedef struct {
  * out_rgba: NULL (stay on the device) or a host/device buffer of w*h*4 floats receiving a copy. */
 vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* req, float* out_rgba);
 
-/* gpu/renderer.js:1191 readback(name, 'linear'|'raw'): copy a camera's last radiance (rgba32f) or raw DN image
- * (f32) into a host buffer of `bytes`. */
-enum { VT_READ_LINEAR = 0, VT_READ_RAW = 1 };
+/* gpu/renderer.js:1191 readback(name, 'linear'|'raw'|'rgba8'|'rgb8'|'yuv420'): copy a camera's last radiance
+ * (rgba32f), raw DN image (f32), 8-bit RGB (4 or 3 bytes per pixel) or YCbCr 4:2:0 planes (Y w x h, then Cb and Cr
+ * ceil(w/2) x ceil(h/2), one byte per sample) into a host buffer of `bytes`. The 8-bit kinds need vt_sensor_frame. */
+enum { VT_READ_LINEAR = 0, VT_READ_RAW = 1, VT_READ_RGBA8 = 2, VT_READ_RGB8 = 3, VT_READ_YUV420 = 4 };
 vt_status vt_readback(vt_ctx* ctx, uint32_t camera, uint32_t kind, void* out, size_t bytes);
 
 /* ------------------------------------------------------------------------------------------------- sensor */
@@ -226,6 +227,22 @@ vt_status vt_sensor_expose(vt_ctx* ctx, const vt_sensor_uniform* su, const float
 /* gpu/renderer.js:1092 sensor(name, opts) for the expose stage: the camera's last radiance (scaled by
  * `optics_scale`, the pi T / (4 N^2) x RI factor, 1 for the configs' unit-radiance sensor) -> its raw DN image. */
 vt_status vt_sensor_camera(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, float optics_scale);
+
+/* gpu/renderer.js:1141 sensor(name, opts) (the passes of :1074 _encodeSensor, gpu/wgsl/sensor.wgsl.js): the whole
+ * chain on the camera's last radiance. sensorOptics (E = L pi T / (4 N^2) RI, horizontal optics blur), veiling glare
+ * on a 1/F level when its fraction is > 0, sensorExpose (vertical blur, glare mix, raw DN), demosaic (bilinear,
+ * edge-aware or Hamilton-Adams), white balance and CCM, noise reduction (3x3 bilateral), sensorOutput (tone curve,
+ * unsharp mask, BT.601 YCbCr with 4:2:0 or 4:4:4 chroma, 8-bit RGB). stats (may be NULL): the sum of the 8-bit luma
+ * (AE) and the raw channel sums R, G, B of the black-subtracted values x 1023 (AWB), as the reference's stats
+ * buffer. The relative illumination map is the one set by vt_set_relative_illumination (else computed with
+ * pupil exponent 1 and no vignetting). */
+vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, uint32_t stats[4]);
+/* gpu/sensor.js:98 relativeIlluminationMap: relative illumination x vignetting per pixel of a camera (w x h floats),
+ * cos^q(theta) sin(theta) / (theta_d dtheta_d/dtheta) from its KB4 lens in FP64 times the vignetting table (n_vig
+ * knots, theta in degrees, linear between), computed when ri is NULL, else copied (host or device). */
+vt_status vt_set_relative_illumination(vt_ctx* ctx, uint32_t camera, const float* ri, double pupil_exponent, const double* vig_theta_deg,
+                                       const double* vig, uint32_t n_vig);
+vt_status vt_get_relative_illumination(vt_ctx* ctx, uint32_t camera, float* ri);
 
 /* -------------------------------------------------------------------------------------- batched rendering */
 

@@ -255,6 +255,15 @@ class Scene:
                                  _p(D))
         return D
 
+    def ri_map(self, camera, pupil_exponent=1.0, vig_theta_deg=(0.0, 90.0), vig=(1.0, 1.0)):
+        """gpu/sensor.js:98 relativeIlluminationMap of a camera (h x w float32, FP64 arithmetic)."""
+        W, H = self.scene["cameras"][camera]["size"]
+        vt = np.ascontiguousarray(vig_theta_deg, np.float64)
+        vv = np.ascontiguousarray(vig, np.float64)
+        out = np.zeros((H, W), np.float32)
+        lib().or_scene_ri_map(self.h, C.c_uint32(camera), C.c_double(pupil_exponent), _p(vt), _p(vv), C.c_uint32(len(vt)), _p(out, C.c_float))
+        return out
+
     # ------------------------------------------------------------------------------------- node radiosity
     def gather_table(self, K=64, fp64=True, threads=8):
         """The gather table of every static vertex (n x K node ids, MISS = escape) and the escapes per node."""
@@ -368,3 +377,21 @@ def form_factors(C_, N_, A_):
     lib().or_form_factors(n, _p(C_, C.c_float), _p(np.ascontiguousarray(N_, np.float32), C.c_float),
                           _p(np.ascontiguousarray(A_, np.float32), C.c_float), _p(F, C.c_float))
     return F
+
+
+def isp_chain(su_words, radiance, ri):
+    """The sensor chain restated (gpu/wgsl/sensor.wgsl.js:67-427): radiance (h, w, 4) float32, relative illumination
+    (h, w) -> raw DN (h, w) float32, 8-bit RGBA (h, w, 4), YCbCr planes (y, cb, cr) and the stats words."""
+    su = np.ascontiguousarray(su_words, np.uint32)
+    L = np.ascontiguousarray(radiance, np.float32)
+    R = np.ascontiguousarray(ri, np.float32)
+    W, H = int(su[0]), int(su[1])
+    cw, ch = (W + 1) // 2, (H + 1) // 2
+    raw = np.zeros((H, W), np.float32)
+    rgba = np.zeros((H, W, 4), np.uint8)
+    yuv = np.zeros(W * H + 2 * cw * ch, np.uint8)
+    st = np.zeros(4, np.uint32)
+    lib().or_isp_chain(_p(su, C.c_uint32), _p(L, C.c_float), _p(R, C.c_float), _p(raw, C.c_float), _p(rgba, C.c_uint8), _p(yuv, C.c_uint8),
+                       _p(st, C.c_uint32))
+    planes = {"y": yuv[:W * H].reshape(H, W), "cb": yuv[W * H:W * H + cw * ch].reshape(ch, cw), "cr": yuv[W * H + cw * ch:].reshape(ch, cw)}
+    return raw, rgba, planes, st

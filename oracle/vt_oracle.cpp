@@ -1960,6 +1960,333 @@ static void sensor_expose(const uint32_t* su, const float* E4, float* raw) {
   }
 }
 
+// ============================================================================================ sensor chain (f32)
+// gpu/wgsl/sensor.wgsl.js:67-427 restated per pixel, each multiply and add rounded separately in the order the
+// reference's expressions give (the CUDA translation unit is compiled without contraction to match): optics with
+// the relative-illumination map and the horizontal blur, veiling glare on a 1/F level, expose, demosaic (three
+// modes), white balance + CCM with the AWB sums, bilateral noise reduction, tone curve, unsharp mask, YCbCr 4:2:0.
+static inline float vt_powf(float x, float y) {
+  if (!(x > 0.0f)) return y == 0.0f ? 1.0f : 0.0f;
+  return vt_expf(y * vt_logf(x));
+}
+static inline int clampi(int v, int a, int b) { return v < a ? a : v > b ? b : v; }
+static inline float clamp01(float v) { return std::min(std::max(v, 0.0f), 1.0f); }
+static inline uint32_t cfa_ch(uint32_t code, uint32_t x, uint32_t y) {
+  static const uint32_t pats[4][4] = {{0, 1, 1, 2}, {1, 0, 2, 1}, {1, 2, 0, 1}, {2, 1, 1, 0}};
+  return pats[code & 3u][(y & 1u) * 2u + (x & 1u)];
+}
+static inline float srgb_oetf(float v) { return v <= 0.0031308f ? 12.92f * v : 1.055f * vt_powf(v, 0.41666666666666669f) - 0.055f; }
+
+struct IspRef {
+  const uint32_t* w;
+  const float* f;
+  int W, H;
+  IspRef(const uint32_t* su) : w(su), f(reinterpret_cast<const float*>(su)), W(int(su[0])), H(int(su[1])) {}
+  float tone(float x) const {   // sensor.wgsl.js:364 toneC
+    float m = f[44];
+    if (m > 2.5f) {
+      float b = f[57];
+      float v = clamp01((x - b) / (1.0f - b));
+      float u = srgb_oetf(v);
+      float cc = f[56];
+      float a = vt_powf(u, cc);
+      return a / std::max(a + vt_powf(1.0f - u, cc), 1e-12f);
+    }
+    float c = clamp01(x);
+    if (m < 0.5f) return srgb_oetf(c);
+    if (m < 1.5f) return vt_powf(c, 1.0f / std::max(f[45], 1e-3f));
+    return c;
+  }
+};
+
+static void isp_chain(const uint32_t* su, const float* L4, const float* ri, float* raw, uint8_t* rgba, uint8_t* yuv, uint32_t* stats) {
+  IspRef I(su);
+  const int W = I.W, H = I.H;
+  const float* f = I.f;
+  const size_t px = size_t(W) * H;
+  std::vector<float> A(px * 3), Bv(px * 3), gpl(px);
+  // sensorOptics (:67)
+  const float sg = f[5];
+  const int r = gaussTaps(sg);
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      float a[3] = {0, 0, 0}, ws = 0;
+      for (int k = -r; k <= r; k++) {
+        int xx = clampi(x + k, 0, W - 1);
+        float w = tapW(k, sg);
+        const float* l = L4 + (size_t(y) * W + xx) * 4;
+        float m = ri[size_t(y) * W + xx];
+        for (int c = 0; c < 3; c++) a[c] = a[c] + w * l[c] * m;
+        ws = ws + w;
+      }
+      float s = f[4] / ws;
+      for (int c = 0; c < 3; c++) A[(size_t(y) * W + x) * 3 + c] = a[c] * s;
+    }
+  // veiling glare (:86-141)
+  const float kgl = f[52];
+  const int F = int(f[54]);
+  const int gw = (W + F - 1) / F, gh = (H + F - 1) / F;
+  std::vector<float> GA, GB;
+  if (kgl > 0.0f) {
+    GA.assign(size_t(gw) * gh * 3, 0.0f);
+    GB.assign(size_t(gw) * gh * 3, 0.0f);
+    for (int y = 0; y < gh; y++)
+      for (int x = 0; x < gw; x++) {
+        float a[3] = {0, 0, 0}, n = 0;
+        for (int j = 0; j < std::min(F, 32); j++)
+          for (int i = 0; i < std::min(F, 32); i++) {
+            int xx = x * F + i, yy = y * F + j;
+            if (xx >= W || yy >= H) continue;
+            const float* l = L4 + (size_t(yy) * W + xx) * 4;
+            float m = ri[size_t(yy) * W + xx];
+            for (int c = 0; c < 3; c++) a[c] = a[c] + l[c] * m;
+            n = n + 1.0f;
+          }
+        float s = f[4] / std::max(n, 1.0f);
+        for (int c = 0; c < 3; c++) GA[(size_t(y) * gw + x) * 3 + c] = a[c] * s;
+      }
+    const float gs = std::max(f[53], 1e-3f);
+    for (int dir = 0; dir < 2; dir++) {
+      const std::vector<float>& in = dir == 0 ? GA : GB;
+      std::vector<float>& out = dir == 0 ? GB : GA;
+      std::vector<float> tmp(in.size());
+      for (int y = 0; y < gh; y++)
+        for (int x = 0; x < gw; x++) {
+          int n = dir == 0 ? gw : gh, c0 = dir == 0 ? x : y;
+          float a[3] = {0, 0, 0};
+          for (int k = 0; k < std::min(n, 256); k++) {
+            float d = float(k - c0);
+            float w = vt_expf(-0.5f * d * d / (gs * gs));
+            const float* g = &in[(dir == 0 ? size_t(y) * gw + k : size_t(k) * gw + x) * 3];
+            for (int c = 0; c < 3; c++) a[c] = a[c] + w * g[c];
+          }
+          float s = gs * 2.5066282746f;
+          for (int c = 0; c < 3; c++) tmp[(size_t(y) * gw + x) * 3 + c] = a[c] / s;
+        }
+      out = tmp;
+    }
+  }
+  auto glare_at = [&](int x, int y, float g[3]) {
+    float Ff = f[54];
+    float pxf = (float(x) + 0.5f) / Ff - 0.5f, pyf = (float(y) + 0.5f) / Ff - 0.5f;
+    float fx0 = std::floor(pxf), fy0 = std::floor(pyf);
+    int x0 = int(fx0), y0 = int(fy0);
+    float fx = pxf - fx0, fy = pyf - fy0;
+    auto at = [&](int xx, int yy, int c) { return GA[(size_t(clampi(yy, 0, gh - 1)) * gw + clampi(xx, 0, gw - 1)) * 3 + c]; };
+    auto mix = [](float p, float q, float t) { return p * (1.0f - t) + q * t; };
+    for (int c = 0; c < 3; c++) g[c] = mix(mix(at(x0, y0, c), at(x0 + 1, y0, c), fx), mix(at(x0, y0 + 1, c), at(x0 + 1, y0 + 1, c), fx), fy);
+  };
+  // sensorExpose (:177)
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      float e[3] = {0, 0, 0}, ws = 0;
+      for (int k = -r; k <= r; k++) {
+        int yy = clampi(y + k, 0, H - 1);
+        float w = tapW(k, sg);
+        for (int c = 0; c < 3; c++) e[c] = e[c] + w * A[(size_t(yy) * W + x) * 3 + c];
+        ws = ws + w;
+      }
+      for (int c = 0; c < 3; c++) e[c] = e[c] / ws;
+      if (kgl > 0.0f) {
+        float g[3];
+        glare_at(x, y, g);
+        for (int c = 0; c < 3; c++) e[c] = (1.0f - kgl) * e[c] + kgl * g[c];
+      }
+      uint32_t ch = cfa_ch(su[2], uint32_t(x), uint32_t(y));
+      const float* row = f + 8 + 4 * ch;
+      float texp = f[6];
+      float d = std::fma(row[2], e[2], std::fma(row[1], e[1], row[0] * e[0]));
+      float lam = std::fma(std::max(0.0f, d), texp, f[22] * texp);
+      uint32_t h = pcgS((uint32_t(y * W + x) * 0x9E3779B9u) ^ pcgS((su[3] * 0x85ebca6bu) ^ pcgS(su[26] ^ (su[49] * 0xc2b2ae35u))));
+      float el = lam;
+      if (f[27] > 0.5f) el = std::fma(f[20], gauss(h ^ 0x27d4eb2fu), poisson(lam, h));
+      el = std::min(el, f[21]);
+      float t = el * f[23];
+      t = std::fma(t, f[7], f[25]);
+      raw[size_t(y) * W + x] = std::min(std::max(std::floor(t + 0.5f), 0.0f), f[24]);
+    }
+  auto raw_at = [&](int x, int y) {
+    if (x < 0) x = -x;
+    if (x >= W) x = 2 * (W - 1) - x;
+    if (y < 0) y = -y;
+    if (y >= H) y = 2 * (H - 1) - y;
+    return raw[size_t(clampi(y, 0, H - 1)) * W + clampi(x, 0, W - 1)];
+  };
+  // demosaicG (:222)
+  const uint32_t mode = su[50];
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      float g = raw_at(x, y);
+      if (cfa_ch(su[2], uint32_t(x), uint32_t(y)) != 1u) {
+        float gl = raw_at(x - 1, y), gr = raw_at(x + 1, y), gu = raw_at(x, y - 1), gd = raw_at(x, y + 1);
+        if (mode == 0) g = 0.25f * (gl + gr + gu + gd);
+        else if (mode == 1) {
+          float dh = std::fabs(gl - gr), dv = std::fabs(gu - gd);
+          g = dh < dv ? 0.5f * (gl + gr) : dv < dh ? 0.5f * (gu + gd) : 0.25f * (gl + gr + gu + gd);
+        } else {
+          float c = g;
+          float lh = 2.0f * c - raw_at(x - 2, y) - raw_at(x + 2, y);
+          float lv = 2.0f * c - raw_at(x, y - 2) - raw_at(x, y + 2);
+          float dh = std::fabs(gl - gr) + std::fabs(lh), dv = std::fabs(gu - gd) + std::fabs(lv);
+          float gh2 = 0.5f * (gl + gr) + 0.25f * lh, gv = 0.5f * (gu + gd) + 0.25f * lv;
+          g = dh < dv ? gh2 : dv < dh ? gv : 0.5f * (gh2 + gv);
+          g = std::min(std::max(g, 0.0f), f[24]);
+        }
+      }
+      gpl[size_t(y) * W + x] = g;
+    }
+  // demosaicRB (:264)
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  auto g_at = [&](int x, int y) { return gpl[size_t(clampi(y, 0, H - 1)) * W + clampi(x, 0, W - 1)]; };
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      uint32_t own = cfa_ch(su[2], uint32_t(x), uint32_t(y));
+      float g = g_at(x, y);
+      float sr = 0, sb = 0, cr = 0, cb = 0;
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          int xx = clampi(x + dx, 0, W - 1), yy = clampi(y + dy, 0, H - 1);
+          uint32_t ch = cfa_ch(su[2], uint32_t(xx), uint32_t(yy));
+          if (ch == 1u) continue;
+          if (ch == own && !(dx == 0 && dy == 0)) continue;
+          float d = raw_at(xx, yy) - g_at(xx, yy);
+          if (ch == 0u) { sr = sr + d; cr = cr + 1.0f; } else { sb = sb + d; cb = cb + 1.0f; }
+        }
+      float rgb[3] = {g + sr / std::max(cr, 1.0f), g, g + sb / std::max(cb, 1.0f)};
+      if (mode <= 1u) {
+        float s3[3] = {0, 0, 0}, c3[3] = {0, 0, 0};
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            int xx = clampi(x + dx, 0, W - 1), yy = clampi(y + dy, 0, H - 1);
+            uint32_t ch = cfa_ch(su[2], uint32_t(xx), uint32_t(yy));
+            if (ch == own && !(dx == 0 && dy == 0)) continue;
+            if (ch == 1u && own == 1u && !(dx == 0 && dy == 0)) continue;
+            s3[ch] = s3[ch] + raw_at(xx, yy);
+            c3[ch] = c3[ch] + 1.0f;
+          }
+        for (int c = 0; c < 3; c++) rgb[c] = s3[c] / std::max(c3[c], 1.0f);
+        if (mode == 1u) rgb[1] = g;
+      }
+      float black = f[25], full = std::max(f[24] - black, 1.0f);
+      float c[3];
+      for (int k = 0; k < 3; k++) c[k] = (rgb[k] - black) / full;
+      for (int k = 0; k < 3; k++) stats[1 + k] += uint32_t(std::nearbyint(clamp01(c[k]) * 1023.0f));
+      for (int k = 0; k < 3; k++) c[k] = c[k] * f[28 + k];
+      for (int k = 0; k < 3; k++) Bv[(size_t(y) * W + x) * 3 + k] = f[32 + 4 * k] * c[0] + f[33 + 4 * k] * c[1] + f[34 + 4 * k] * c[2];
+    }
+  // sensorNR (:321) into A
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      const float* c0 = &Bv[(size_t(y) * W + x) * 3];
+      float* o = &A[(size_t(y) * W + x) * 3];
+      if (su[51] == 0u || f[58] <= 0.0f) { o[0] = c0[0]; o[1] = c0[1]; o[2] = c0[2]; continue; }
+      float Y0 = std::max(c0[0] * 0.2126f + c0[1] * 0.7152f + c0[2] * 0.0722f, 0.0f);
+      float fullE = std::max(f[24] - f[25], 1.0f) / std::max(f[23] * f[7], 1e-9f);
+      float sn = std::sqrt(Y0 * fullE + f[20] * f[20]) / fullE;
+      float rs = std::max(f[59] * sn, 1e-6f), ss = f[58];
+      float a[3] = {0, 0, 0}, ws = 0;
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          const float* c = &Bv[(size_t(clampi(y + dy, 0, H - 1)) * W + clampi(x + dx, 0, W - 1)) * 3];
+          float dY = (c[0] - c0[0]) * 0.2126f + (c[1] - c0[1]) * 0.7152f + (c[2] - c0[2]) * 0.0722f;
+          float w = vt_expf(-0.5f * float(dx * dx + dy * dy) / (ss * ss) - 0.5f * dY * dY / (rs * rs));
+          for (int k = 0; k < 3; k++) a[k] = a[k] + w * c[k];
+          ws = ws + w;
+        }
+      for (int k = 0; k < 3; k++) o[k] = a[k] / ws;
+    }
+  // sensorOutput (:387), one 2x2 block at a time
+  auto toned = [&](int x, int y, float c[3]) {
+    const float* a = &A[(size_t(clampi(y, 0, H - 1)) * W + clampi(x, 0, W - 1)) * 3];
+    for (int k = 0; k < 3; k++) c[k] = I.tone(a[k]);
+  };
+  auto luma = [](const float c[3]) { return c[0] * 0.299f + c[1] * 0.587f + c[2] * 0.114f; };
+  const float amt = f[46];
+  const int rad = clampi(int(std::nearbyint(f[47])), 1, 4);
+  const bool c420 = su[48] != 0u;
+  const int cw = (W + 1) / 2, chh = (H + 1) / 2;
+  for (int gy = 0; gy < chh; gy++)
+    for (int gx = 0; gx < cw; gx++) {
+      int bx = 2 * gx, by = 2 * gy;
+      float Ys[4] = {0, 0, 0, 0}, cb = 0, cr = 0, nb = 0;
+      for (int q = 0; q < 4; q++) {
+        int x = bx + (q & 1), y = by + (q >> 1);
+        if (x >= W || y >= H) continue;
+        float c[3];
+        toned(x, y, c);
+        if (amt > 0.0f) {
+          float m = 0, n = 0;
+          for (int dy = -rad; dy <= rad; dy++)
+            for (int dx = -rad; dx <= rad; dx++) {
+              float t[3];
+              toned(x + dx, y + dy, t);
+              m = m + luma(t);
+              n = n + 1.0f;
+            }
+          float sh = amt * (luma(c) - m / n);
+          for (int k = 0; k < 3; k++) c[k] = c[k] + sh;
+        }
+        float r8 = clamp01(c[0]) * 255.0f, g8 = clamp01(c[1]) * 255.0f, b8 = clamp01(c[2]) * 255.0f;
+        Ys[q] = 0.299f * r8 + 0.587f * g8 + 0.114f * b8;
+        cb = cb + (128.0f - 0.168736f * r8 - 0.331264f * g8 + 0.5f * b8);
+        cr = cr + (128.0f + 0.5f * r8 - 0.418688f * g8 - 0.081312f * b8);
+        nb = nb + 1.0f;
+        if (!c420) {
+          float y8 = std::min(std::max(std::nearbyint(Ys[q]), 0.0f), 255.0f);
+          uint8_t* o = rgba + (size_t(y) * W + x) * 4;
+          o[0] = uint8_t(std::nearbyint(r8)); o[1] = uint8_t(std::nearbyint(g8)); o[2] = uint8_t(std::nearbyint(b8)); o[3] = 255;
+          stats[0] += uint32_t(y8);
+        }
+      }
+      if (c420) {
+        float Cb = std::min(std::max(std::nearbyint(cb / nb), 0.0f), 255.0f), Cr = std::min(std::max(std::nearbyint(cr / nb), 0.0f), 255.0f);
+        for (int q = 0; q < 4; q++) {
+          int x = bx + (q & 1), y = by + (q >> 1);
+          if (x >= W || y >= H) continue;
+          float y8 = std::min(std::max(std::nearbyint(Ys[q]), 0.0f), 255.0f);
+          float rr = y8 + 1.402f * (Cr - 128.0f);
+          float gg = y8 - 0.344136f * (Cb - 128.0f) - 0.714136f * (Cr - 128.0f);
+          float bb = y8 + 1.772f * (Cb - 128.0f);
+          uint8_t* o = rgba + (size_t(y) * W + x) * 4;
+          o[0] = uint8_t(std::min(std::max(std::nearbyint(rr), 0.0f), 255.0f));
+          o[1] = uint8_t(std::min(std::max(std::nearbyint(gg), 0.0f), 255.0f));
+          o[2] = uint8_t(std::min(std::max(std::nearbyint(bb), 0.0f), 255.0f));
+          o[3] = 255;
+          yuv[size_t(y) * W + x] = uint8_t(y8);
+          stats[0] += uint32_t(y8);
+        }
+        yuv[px + size_t(gy) * cw + gx] = uint8_t(Cb);
+        yuv[px + size_t(cw) * chh + size_t(gy) * cw + gx] = uint8_t(Cr);
+      }
+    }
+}
+
+// gpu/sensor.js:98 relativeIlluminationMap (FP64, lens.js unproject / distort / distortDeriv)
+static void ri_map(const vt_camera_desc& c, double q, const double* vdeg, const double* vv, uint32_t nv, float* out) {
+  Lens L{c.fx, c.fy, c.cx, c.cy, c.alpha, {c.k[0], c.k[1], c.k[2], c.k[3]}};
+  for (uint32_t y = 0; y < c.height; y++)
+    for (uint32_t x = 0; x < c.width; x++) {
+      double uv[2] = {double(x), double(y)}, r[3];
+      unproject(L, uv, r);
+      double th = std::acos(std::max(-1.0, std::min(1.0, r[2])));
+      double ri = 1.0;
+      if (th > 1e-6) ri = std::pow(std::cos(th), q) * std::sin(th) / (distort(L, th) * distort_deriv(L, th));
+      double vg = 1.0;
+      if (nv) {
+        double t0 = vdeg[0] * M_PI / 180.0;
+        if (th <= t0) vg = vv[0];
+        else {
+          vg = vv[nv - 1];
+          for (uint32_t i = 1; i < nv; i++) {
+            double ti = vdeg[i] * M_PI / 180.0, tp = vdeg[i - 1] * M_PI / 180.0;
+            if (th <= ti) { vg = vv[i - 1] + (vv[i] - vv[i - 1]) * (th - tp) / (ti - tp); break; }
+          }
+        }
+      }
+      out[size_t(y) * c.width + x] = float(std::max(0.0, ri) * vg);
+    }
+}
+
 // ============================================================================================ radiosity (FP64)
 
 // Direct FP64 solve of (I - diag(rho) F) B = E (Gaussian elimination with partial pivoting), R right-hand sides.
@@ -2560,6 +2887,12 @@ void or_form_factors_visible(void* h, int n, const float* C, const float* Nn, co
 }
 
 void or_sensor_expose(const uint32_t* su, const float* E4, float* raw) { sensor_expose(su, E4, raw); }
+void or_isp_chain(const uint32_t* su, const float* L4, const float* ri, float* raw, uint8_t* rgba, uint8_t* yuv, uint32_t* stats) {
+  isp_chain(su, L4, ri, raw, rgba, yuv, stats);
+}
+void or_scene_ri_map(void* h, uint32_t camera, double q, const double* vdeg, const double* vv, uint32_t nv, float* out) {
+  ri_map(static_cast<Scene*>(h)->cams[camera], q, vdeg, vv, nv, out);
+}
 void or_vt_logf(const float* x, int n, float* out) { for (int i = 0; i < n; i++) out[i] = vt_logf(x[i]); }
 void or_vt_expf(const float* x, int n, float* out) { for (int i = 0; i < n; i++) out[i] = vt_expf(x[i]); }
 void or_vt_cos2pi(const float* x, int n, float* out) { for (int i = 0; i < n; i++) out[i] = vt_cos2pi(x[i]); }

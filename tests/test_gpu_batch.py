@@ -37,7 +37,7 @@ def per_pose(r, cams, P, spp, depth, seed, sensor=None, frame0=0):
             r.renderCamera(c, spp=spp, lightSamples=1, seed=seed, mode=A.VT_SHADE_PATH, max_depth=depth)
             rc.append(r.readback(c, "linear").reshape(H, W, 4))
             if sensor is not None:
-                r.sensor(c, seed=seed, frame=frame0 + q, params=sensor)
+                r.expose(c, seed=seed, frame=frame0 + q, params=sensor)
                 wc.append(r.readback(c, "raw").reshape(H, W))
         rad.append(np.stack(rc))
         raw.append(np.stack(wc) if wc else None)

@@ -333,3 +333,58 @@ def test_node_transport_reduces_to_the_linear_system():
         M = np.linalg.solve(np.eye(n) - (rho[:, c] * V)[:, None] * F, st[act, 12 + c])
         got = np.pi * rho[:, c] * out[act, 4 * slot + c]
         np.testing.assert_allclose(got, M, rtol=1e-9, atol=1e-12 * M.max())
+
+
+def test_sensor_chain_known_answers():
+    """The restated sensor chain (gpu/wgsl/sensor.wgsl.js) on inputs with closed-form outputs: a flat grey field with
+    noise off, no blur, unit relative illumination and a linear tone curve gives raw DN = round(M E t g + black) per
+    CFA site, the same value in every demosaiced channel, 8-bit RGB = round(255 (DN - black) / (max - black)), and
+    4:2:0 chroma 128 with Y from BT.601."""
+    from vtwin import sensor as S
+
+    W, H = 12, 8
+    L = np.zeros((H, W, 4), np.float32)
+    L[..., :3] = 0.8
+    ri = np.ones((H, W), np.float32)
+    for demosaic in ("bilinear", "edge-aware", "hamilton"):
+        p = S.sensor_params({"noise": False, "esfSigmaPx": 0.0, "esfIncludesAperture": False, "tone": "linear", "demosaic": demosaic,
+                             "responseMatrix": [[1000.0, 0, 0], [0, 1000.0, 0], [0, 0, 1000.0]], "blackLevel": 64.0,
+                             "conversionGain": 1.0, "fullWell": 1e9, "cfa": "RGGB"})
+        su = S.pack_sensor_uniform(p, W, H, exposure=5.0, gain=1.0)
+        raw, rgba, yuv, st = O.isp_chain(su, L, ri)
+        E = np.float32(0.8) * np.float32(np.pi * 0.9 / 16)
+        want_dn = np.floor(np.float32(1000.0) * E * np.float32(5.0) + np.float32(64.0) + np.float32(0.5))
+        assert np.all(raw == want_dn), (raw[0, :4], want_dn)
+        c8 = np.round((want_dn - 64.0) / (4095.0 - 64.0) * 255.0)
+        assert np.all(rgba[..., :3] == c8) and np.all(rgba[..., 3] == 255)
+        assert np.all(yuv["cb"] == 128) and np.all(yuv["cr"] == 128)
+        assert np.all(yuv["y"] == np.round(0.299 * c8 + 0.587 * c8 + 0.114 * c8))
+        assert st[0] == yuv["y"].astype(np.int64).sum() and st[1] == st[2] == st[3] == W * H * round((want_dn - 64.0) / 4031.0 * 1023)
+    # 4:4:4 and an sRGB tone: the 8-bit value is the sRGB OETF of the normalised DN
+    p = S.sensor_params({"noise": False, "esfSigmaPx": 0.0, "esfIncludesAperture": False, "chroma": "4:4:4", "conversionGain": 1.0,
+                         "responseMatrix": [[1000.0, 0, 0], [0, 1000.0, 0], [0, 0, 1000.0]], "fullWell": 1e9})
+    su = S.pack_sensor_uniform(p, W, H, exposure=5.0, gain=1.0)
+    raw, rgba, yuv, st = O.isp_chain(su, L, ri)
+    v = (raw[0, 0] - 0.0) / 4095.0
+    want = round(255 * (1.055 * v ** (1 / 2.4) - 0.055))
+    assert np.all(np.abs(rgba[..., :3].astype(int) - want) <= 1)
+
+
+def test_relative_illumination_pinhole_closed_form():
+    """gpu/sensor.js:98 relativeIlluminationMap with k = 0 (theta_d = theta): RI = cos^q(theta) sin(theta) / theta."""
+    sc = dome.make_dome_scene(seed=1, width=48, height=32, level=1)
+    sc["cameras"][0]["k"] = [0.0, 0.0, 0.0, 0.0]
+    S = O.Scene(sc)
+    lens = S.scene["cameras"][0]
+    q = 1.5
+    ri = S.ri_map(0, q, (0.0, 90.0), (1.0, 1.0))
+    from vtwin import _abi as A
+
+    p = A.lens_params(lens)
+    fx, fy, cx, cy, alpha, k = p[0], p[1], p[2], p[3], p[4], p[5:9]
+    ys, xs = np.mgrid[0:32, 0:48].astype(np.float64)
+    yd = (ys - cy) / fy
+    xd = (xs - cx) / fx - alpha * yd
+    th = np.hypot(xd, yd)
+    want = np.where(th > 1e-6, np.cos(th) ** q * np.sin(th) / np.maximum(th, 1e-300), 1.0)
+    np.testing.assert_allclose(ri, want.astype(np.float32), rtol=2e-7)

@@ -99,7 +99,7 @@ vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx**
 vt_status vt_destroy(vt_ctx* ctx) {
   if (!ctx) return VT_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); }
+  for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); cudaFree(c.ri); cudaFree(c.isp_mem); }
   cudaFree(ctx->d_nodes); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
   cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave); cudaFree(ctx->tc.mem);
   cudaFree(ctx->batch.su); cudaFree(ctx->batch.cull); cudaFree(ctx->batch.ctr); cudaFree(ctx->batch.sensor); cudaFree(ctx->batch.mem);
@@ -355,6 +355,26 @@ vt_status vt_readback(vt_ctx* ctx, uint32_t camera, uint32_t kind, void* out, si
     if (bytes < px * 4) return VT_ERR_ARG;
     vt_status s = from_device(ctx, out, C.raw, px * 4);
     if (s != VT_OK) return s;
+  } else if (kind == VT_READ_RGBA8 || kind == VT_READ_RGB8 || kind == VT_READ_YUV420) {
+    if (!C.processed) return fail(ctx, VT_ERR_STATE, "8-bit readback before vt_sensor_frame");
+    const uint32_t W = ctx->S.cams[camera].width, H = ctx->S.cams[camera].height;
+    if (kind == VT_READ_RGBA8) {
+      if (bytes < px * 4) return VT_ERR_ARG;
+      vt_status s = from_device(ctx, out, C.isp.out, px * 4);
+      if (s != VT_OK) return s;
+    } else if (kind == VT_READ_YUV420) {
+      const size_t n = px + 2 * size_t((W + 1) / 2) * ((H + 1) / 2);
+      if (bytes < n) return VT_ERR_ARG;
+      vt_status s = from_device(ctx, out, C.isp.yuv, n);
+      if (s != VT_OK) return s;
+    } else {
+      if (bytes < px * 3) return VT_ERR_ARG;
+      std::vector<uint8_t> rgba(px * 4);
+      VT_CK(cudaMemcpyAsync(rgba.data(), C.isp.out, px * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      VT_CK(cudaStreamSynchronize(ctx->stream));
+      uint8_t* o = static_cast<uint8_t*>(out);
+      for (size_t i = 0; i < px; i++) { o[3 * i] = rgba[4 * i]; o[3 * i + 1] = rgba[4 * i + 1]; o[3 * i + 2] = rgba[4 * i + 2]; }
+    }
   } else {
     return fail(ctx, VT_ERR_ARG, "readback kind");
   }
@@ -413,6 +433,99 @@ vt_status vt_sensor_camera(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   ctx->tim.sensor_ms = ms;
+  return VT_OK;
+}
+
+vt_status vt_set_relative_illumination(vt_ctx* ctx, uint32_t camera, const float* ri, double pupil_exponent, const double* vig_theta_deg,
+                                       const double* vig, uint32_t n_vig) {
+  if (!ctx) return VT_ERR_ARG;
+  if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
+  if (n_vig && (!vig_theta_deg || !vig)) return fail(ctx, VT_ERR_ARG, "relative illumination: vignetting table is null");
+  const vt_camera_desc& c = ctx->S.cams[camera];
+  const size_t px = size_t(c.width) * c.height;
+  auto& C = ctx->cams[camera];
+  if (!C.ri && cudaMalloc(&C.ri, px * 4) != cudaSuccess) { cudaGetLastError(); C.ri = nullptr; return fail(ctx, VT_ERR_OOM, "relative illumination map"); }
+  if (ri) return to_device(ctx, C.ri, ri, px * 4);
+  std::vector<float> m(px);
+  vt::relative_illumination(c, pupil_exponent, vig_theta_deg, vig, n_vig, m.data());
+  VT_CK(cudaMemcpyAsync(C.ri, m.data(), px * 4, cudaMemcpyHostToDevice, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  return VT_OK;
+}
+
+vt_status vt_get_relative_illumination(vt_ctx* ctx, uint32_t camera, float* ri) {
+  if (!ctx || !ri) return VT_ERR_ARG;
+  if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
+  const auto& C = ctx->cams[camera];
+  if (!C.ri) return fail(ctx, VT_ERR_STATE, "no relative illumination map (vt_set_relative_illumination)");
+  vt_status s = from_device(ctx, ri, C.ri, size_t(ctx->S.cams[camera].width) * ctx->S.cams[camera].height * 4);
+  if (s != VT_OK) return s;
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  return VT_OK;
+}
+
+vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, uint32_t stats[4]) {
+  if (!ctx || !su) return VT_ERR_ARG;
+  if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
+  auto& C = ctx->cams[camera];
+  if (!C.rendered) return fail(ctx, VT_ERR_STATE, "sensor before renderCamera");
+  const vt_camera_desc& cd = ctx->S.cams[camera];
+  const uint32_t W = cd.width, H = cd.height;
+  if (su->words[0] != W || su->words[1] != H) return fail(ctx, VT_ERR_ARG, "sensor: size mismatch");
+  float F;
+  std::memcpy(&F, &su->words[54], 4);
+  if (!(F >= 1.0f && F <= 4096.0f)) return fail(ctx, VT_ERR_ARG, "sensor: glare level factor out of range");
+  if (!C.ri) {   // gpu/sensor.js defaults: pupil obliquity exponent 1, no vignetting
+    const double vt[2] = {0.0, 90.0}, vv[2] = {1.0, 1.0};
+    vt_status s = vt_set_relative_illumination(ctx, camera, nullptr, 1.0, vt, vv, 2);
+    if (s != VT_OK) return s;
+  }
+  const size_t Fi = size_t(F), lev = ((W + Fi - 1) / Fi) * ((H + Fi - 1) / Fi);
+  if (C.isp_mem && lev > C.isp_lev) {   // a finer glare level than the buffers hold: size them again
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(C.isp_mem);
+    C.isp_mem = nullptr;
+    C.processed = false;
+  }
+  if (!C.isp_mem) {
+    const size_t px = size_t(W) * H;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t b4 = al(px * 16), bl = al(std::max<size_t>(lev, 1) * 16), b1 = al(px * 4), bo = al(px * 4),
+                 by = al(px + 2 * size_t((W + 1) / 2) * ((H + 1) / 2)), bs = 256;
+    if (cudaMalloc(&C.isp_mem, 2 * b4 + 2 * bl + b1 + bo + by + bs) != cudaSuccess) {
+      cudaGetLastError();
+      C.isp_mem = nullptr;
+      return fail(ctx, VT_ERR_OOM, "sensor chain buffers");
+    }
+    char* p = static_cast<char*>(C.isp_mem);
+    C.isp.A = reinterpret_cast<float4*>(p); p += b4;
+    C.isp.B = reinterpret_cast<float4*>(p); p += b4;
+    C.isp.GA = reinterpret_cast<float4*>(p); p += bl;
+    C.isp.GB = reinterpret_cast<float4*>(p); p += bl;
+    C.isp.gpl = reinterpret_cast<float*>(p); p += b1;
+    C.isp.out = reinterpret_cast<uchar4*>(p); p += bo;
+    C.isp.yuv = reinterpret_cast<uint8_t*>(p); p += by;
+    C.isp.stats = reinterpret_cast<uint32_t*>(p);
+    C.isp_lev = std::max<size_t>(lev, 1);
+  }
+  C.isp.L = C.radiance;
+  C.isp.ri = C.ri;
+  C.isp.raw = C.raw;
+  vtk::SensorParams sp;
+  std::memcpy(sp.w, su->words, sizeof(sp.w));
+  VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  vtk::launch_isp(sp, C.isp, ctx->stream);
+  VT_CK(cudaGetLastError());
+  VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  uint32_t st[4];
+  VT_CK(cudaMemcpyAsync(st, C.isp.stats, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  if (stats) std::memcpy(stats, st, 16);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->tim.sensor_ms = ms;
+  ctx->tim.launches += 6;
+  C.exposed = C.processed = true;
   return VT_OK;
 }
 

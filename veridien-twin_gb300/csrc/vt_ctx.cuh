@@ -11,6 +11,7 @@
 
 #include "vt_host.h"
 #include "vt_kernels.cuh"
+#include "vt_isp.cuh"
 #include "vt_wave.cuh"
 
 struct vt_ctx {
@@ -32,7 +33,17 @@ struct vt_ctx {
   int wave_blocks = 0;
   void* d_wave = nullptr;       // wavefront path state (grown on demand)
   size_t wave_cap = 0;
-  struct Cam { float4* radiance = nullptr; float* raw = nullptr; bool rendered = false, exposed = false; };
+  struct Cam {
+    float4* radiance = nullptr;
+    float* raw = nullptr;
+    bool rendered = false, exposed = false;
+    // the sensor chain (vt_sensor_frame): relative illumination map and its working buffers, grown on first use
+    float* ri = nullptr;
+    void* isp_mem = nullptr;
+    vtk::IspBufs isp{};
+    size_t isp_lev = 0;   // glare-level pixels the buffers hold
+    bool processed = false;
+  };
   std::vector<Cam> cams;
   // scratch for ray queries and the solver (grown on demand)
   void* d_scratch = nullptr;

@@ -757,6 +757,48 @@ void scene_uniform(const Prepared& S, const std::vector<InstPose>& inst, const f
   }
 }
 
+void relative_illumination(const vt_camera_desc& c, double q, const double* vdeg, const double* vv, uint32_t nv, float* out) {
+  const double k[4] = {c.k[0], c.k[1], c.k[2], c.k[3]};
+  auto distort = [&](double th) { const double t2 = th * th; return th * (1 + t2 * (k[0] + t2 * (k[1] + t2 * (k[2] + t2 * k[3])))); };
+  auto deriv = [&](double th) { const double t2 = th * th; return 1 + t2 * (3 * k[0] + t2 * (5 * k[1] + t2 * (7 * k[2] + t2 * 9 * k[3]))); };
+  std::vector<double> vt(nv), vw(nv);
+  for (uint32_t i = 0; i < nv; i++) { vt[i] = vdeg[i] * M_PI / 180.0; vw[i] = vv[i]; }
+  auto vig = [&](double th) {
+    if (!nv) return 1.0;
+    if (th <= vt[0]) return vw[0];
+    for (uint32_t i = 1; i < nv; i++)
+      if (th <= vt[i]) return vw[i - 1] + (vw[i] - vw[i - 1]) * (th - vt[i - 1]) / (vt[i] - vt[i - 1]);
+    return vw[nv - 1];
+  };
+  const uint32_t W = c.width, H = c.height;
+  auto rows = [&](uint32_t y0, uint32_t y1) {
+    for (uint32_t y = y0; y < y1; y++)
+      for (uint32_t x = 0; x < W; x++) {
+        // the pixel's unit ray (KB4 inverse, lens.js unproject); only its z is needed
+        const double yd = (double(y) - c.cy) / c.fy, xd = (double(x) - c.cx) / c.fx - c.alpha * yd;
+        const double thd = std::hypot(xd, yd);
+        double z = 1.0;
+        if (thd >= 1e-300) {
+          double th = thd;
+          for (int it = 0; it < 20; it++) {
+            const double step = (distort(th) - thd) / deriv(th);
+            th -= step;
+            if (std::fabs(step) < 1e-15) break;
+          }
+          z = std::cos(th);
+        }
+        const double th = std::acos(std::max(-1.0, std::min(1.0, z)));
+        double ri = 1.0;
+        if (th > 1e-6) ri = std::pow(std::cos(th), q) * std::sin(th) / (distort(th) * deriv(th));
+        out[size_t(y) * W + x] = float(std::max(0.0, ri) * vig(th));
+      }
+  };
+  const uint32_t nt = std::max(1u, std::min(std::thread::hardware_concurrency(), (H + 63) / 64));
+  std::vector<std::thread> th;
+  for (uint32_t t = 0; t < nt; t++) th.emplace_back(rows, H * t / nt, H * (t + 1) / nt);
+  for (auto& t : th) t.join();
+}
+
 void node_neighbours(const Prepared& S, const std::vector<uint32_t>& active, uint32_t K, double R, double sg, std::vector<uint32_t>& out) {
   const size_t n = active.size();
   out.assign(n * K * 2, 0u);

@@ -70,6 +70,12 @@ std::vector<InstPose> poses_from(const Prepared& S, const double* T0, const doub
 void scene_uniform(const Prepared& S, const std::vector<InstPose>& inst, const float eavg[3], uint32_t slot, uint32_t frame,
                    float* out /* SU_WORDS */, const float* pcaps = nullptr);
 
+// Relative illumination x vignetting per pixel of a KB4 camera (gpu/sensor.js:98 relativeIlluminationMap), FP64:
+// RI = cos^q(theta) sin(theta) / (theta_d dtheta_d/dtheta) at the pixel's ray (Newton inverse of the distortion, at
+// most 20 steps), times the vignetting table (n knots, theta in degrees, linear between). out: w x h floats.
+void relative_illumination(const vt_camera_desc& cam, double pupil_exponent, const double* vig_theta_deg, const double* vig, uint32_t n_vig,
+                           float* out);
+
 // Smoothing neighbours of the active nodes (gpu/renderer.js:573 _neighbours): for each active node the nbr_k largest
 // Gaussian weights exp(-d^2 / 2 sigma^2) (ties: smaller active index first) over active nodes within `radius` whose
 // normals agree (n.n >= 0.9), as (active index, float weight bits) pairs, weight 0 after the last. sigma <= 0: each

@@ -14,7 +14,7 @@ VT_OK, VT_ERR_ARG, VT_ERR_CUDA, VT_ERR_OOM, VT_ERR_TIMEOUT, VT_ERR_STATE = 0, 1,
 VT_ERR_UNKNOWN_CAMERA, VT_ERR_TOO_MANY_BODIES, VT_ERR_NO_DEVICE, VT_ERR_NOT_CONVERGED = 6, 7, 8, 9
 VT_SHADE_TWIN, VT_SHADE_PATH = 0, 1
 VT_PREC_FP32, VT_PREC_BF16, VT_PREC_FP8, VT_PREC_FP32_TMA = 0, 1, 2, 3
-VT_READ_LINEAR, VT_READ_RAW = 0, 1
+VT_READ_LINEAR, VT_READ_RAW, VT_READ_RGBA8, VT_READ_RGB8, VT_READ_YUV420 = 0, 1, 2, 3, 4
 VT_MAX_INST = 24
 VT_MISS = 0xFFFFFFFF
 BODY_KIND = {"instrument": 0, "scope": 1, "board": 2, "fixed": 3, "fixture": 4}

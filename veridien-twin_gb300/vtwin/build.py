@@ -22,6 +22,11 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr"]
 
 
+# per-file flags: the sensor chain is compiled without multiply-add contraction, so its arithmetic is the sequence of
+# separately rounded operations that the CPU restatement performs
+EXTRA = {"vt_isp.cu": ["--fmad=false"]}
+
+
 def nvcc() -> str:
     for c in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if c and os.path.exists(c):
@@ -46,7 +51,7 @@ def needs_build() -> bool:
 
 def _compile(src: str, verbose_ptxas: bool) -> str:
     out = os.path.join(OBJ, src + ".o")
-    cmd = [nvcc(), *ARCH, *COMMON, "-c", os.path.join(CSRC, src), "-o", out]
+    cmd = [nvcc(), *ARCH, *COMMON, *EXTRA.get(src, []), "-c", os.path.join(CSRC, src), "-o", out]
     if verbose_ptxas and src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

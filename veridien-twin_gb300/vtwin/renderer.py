@@ -55,6 +55,7 @@ class TwinRenderer:
         r.frame = 0
         r.sensor_p = sensor_mod.sensor_params((opts or {}).get("sensor"))
         r.nodes_info = None
+        r._sens = {}
         if r.opts.get("nodes", True):     # gpu/renderer.js:256: the gather table is part of create
             r.build_nodes()
         r.set_poses({"bodies": {}})
@@ -245,7 +246,7 @@ class TwinRenderer:
     render_frame = renderFrame
 
     def readback(self, name, kind="linear"):
-        """gpu/renderer.js:1191 readback(name, 'linear'|'raw') -> Float32Array copy."""
+        """gpu/renderer.js:1191 readback(name, 'linear'|'raw'|'rgb8'|'rgba8'|'yuv420') -> a host copy."""
         c = self._cam(name)
         w, h = self.scene["cameras"][c]["size"]
         if kind == "linear":
@@ -254,13 +255,22 @@ class TwinRenderer:
         elif kind == "raw":
             out = np.zeros((h, w), np.float32)
             check(self.lib.vt_readback(self._ctx, c, A.VT_READ_RAW, _p(out), out.nbytes), self._ctx)
+        elif kind in ("rgb8", "rgba8"):
+            out = np.zeros((h, w, 3 if kind == "rgb8" else 4), np.uint8)
+            check(self.lib.vt_readback(self._ctx, c, A.VT_READ_RGB8 if kind == "rgb8" else A.VT_READ_RGBA8, _p(out), out.nbytes), self._ctx)
+        elif kind == "yuv420":
+            cw, ch = (w + 1) // 2, (h + 1) // 2
+            buf = np.zeros(w * h + 2 * cw * ch, np.uint8)
+            check(self.lib.vt_readback(self._ctx, c, A.VT_READ_YUV420, _p(buf), buf.nbytes), self._ctx)
+            return {"width": w, "height": h, "y": buf[:w * h].reshape(h, w), "cb": buf[w * h:w * h + cw * ch].reshape(ch, cw),
+                    "cr": buf[w * h + cw * ch:].reshape(ch, cw)}
         else:
-            raise VtError(A.VT_ERR_ARG, f"readback kind {kind} is not produced by this library (linear, raw)")
+            raise VtError(A.VT_ERR_ARG, f"readback kind {kind} (linear, raw, rgb8, rgba8, yuv420)")
         return out
 
-    def sensor(self, name, seed=0, frame=None, noise=True, exposure_s=1.0, gain=1.0, params=None, optics_scale=1.0):
-        """gpu/renderer.js:1092 sensor(name, {seed, frame, noise, exposure_s, gain, params}): the expose stage
-        (CFA, shot + read noise, ADC) of the camera's last radiance into its raw DN image."""
+    def expose(self, name, seed=0, frame=None, noise=True, exposure_s=1.0, gain=1.0, params=None, optics_scale=1.0):
+        """The expose stage alone (gpu/wgsl/sensor.wgsl.js:177 sensorExpose with the vertical blur): the camera's last
+        radiance x `optics_scale` -> its raw DN image (vt_sensor_camera)."""
         c = self._cam(name)
         w, h = self.scene["cameras"][c]["size"]
         p = {**self.sensor_p, **(params or {})}
@@ -270,6 +280,75 @@ class TwinRenderer:
         su.words[:] = [int(x) for x in sensor_mod.pack_sensor_uniform(
             p, w, h, frame=self.frame if frame is None else frame, seed=seed, exposure=exposure_s, gain=gain, cam_index=c)]
         check(self.lib.vt_sensor_camera(self._ctx, c, C.byref(su), float(optics_scale)), self._ctx)
+
+    def _sensor_state(self, c):
+        st = self._sens.get(c)
+        if st is None:
+            p = self.sensor_p
+            st = self._sens[c] = {"ae": sensor_mod.AutoExposure(p, exposure_units=p.get("exposureUnits0", 10)), "awb": None, "manual": None,
+                                  "ri": False, "meanLuma": None, "meanRGB": None}
+        return st
+
+    def set_exposure(self, name, e):
+        """gpu/renderer.js:1042 _manualExposure: a number (seconds), {time_s, gain}, or None / 'auto' for AE."""
+        st = self._sensor_state(self._cam(name))
+        if e is None or e == "auto":
+            st["manual"] = None
+        elif isinstance(e, (int, float)):
+            st["manual"] = {"time_s": float(e), "gain": 1.0}
+        else:
+            st["manual"] = {"time_s": float(e.get("time_s", e.get("exposure_s", e.get("time")))), "gain": float(e.get("gain", 1.0))}
+
+    def exposureOf(self, name) -> dict:
+        """gpu/renderer.js:1049 exposureOf: the exposure the next sensor() uses (AE or manual)."""
+        st = self._sensor_state(self._cam(name))
+        if st["manual"]:
+            return {**st["manual"], "auto": False}
+        ae = st["ae"]
+        return {"time_s": ae.exposure, "gain": ae.gain, "gainUnits": ae.gain_units, "units": ae.units, "auto": True}
+
+    exposure_of = exposureOf
+
+    def sensor(self, name, seed=0, frame=None, noise=True, exposure_s=None, gain=None, params=None):
+        """gpu/renderer.js:1141 sensor(name, {seed, frame, noise, exposure_s, gain, params}): the whole chain on the
+        camera's last radiance (optics with relative illumination, glare, expose, demosaic, white balance + CCM, noise
+        reduction, tone, YCbCr) into its raw, 8-bit RGB and YCbCr images; then the auto exposure and auto white
+        balance take this frame's statistics for the next (gpu/renderer.js:1117 _afterSensor)."""
+        c = self._cam(name)
+        w, h = self.scene["cameras"][c]["size"]
+        st = self._sensor_state(c)
+        base = self.sensor_p
+        if not st["ri"]:
+            vt = np.ascontiguousarray(base["vignettingThetaDeg"], np.float64)
+            vv = np.ascontiguousarray(base["vignetting"], np.float64)
+            check(self.lib.vt_set_relative_illumination(self._ctx, c, None, float(base["pupilExponent"]), _p(vt), _p(vv), len(vt)), self._ctx)
+            st["ri"] = True
+        ex = self.exposureOf(name)
+        p = {**base, **(params or {})}
+        if p.get("awb") and st["awb"] is not None and not (params and "wb" in params):
+            p["wb"] = [g * a for g, a in zip(p["wb"], st["awb"])]
+        if noise is False:
+            p["noise"] = False
+        su = A.vt_sensor_uniform()
+        su.words[:] = [int(x) for x in sensor_mod.pack_sensor_uniform(
+            p, w, h, frame=self.frame if frame is None else frame, seed=seed, exposure=ex["time_s"] if exposure_s is None else exposure_s,
+            gain=ex["gain"] if gain is None else gain, cam_index=c)]
+        stats = np.zeros(4, np.uint32)
+        check(self.lib.vt_sensor_frame(self._ctx, c, C.byref(su), _p(stats)), self._ctx)
+        st["meanLuma"] = float(stats[0]) / (w * h * 255)
+        st["meanRGB"] = [float(x) / (w * h * 1023) for x in stats[1:]]
+        if not st["manual"]:
+            st["ae"].update(st["meanLuma"])
+        if base.get("awb"):
+            st["awb"] = sensor_mod.update_awb(st["awb"], st["meanRGB"], base.get("awbDamping", 0.3))
+        return {"stats": stats, "meanLuma": st["meanLuma"], "meanRGB": st["meanRGB"], "uniform": np.array(su.words, np.uint32)}
+
+    def relative_illumination(self, name):
+        c = self._cam(name)
+        w, h = self.scene["cameras"][c]["size"]
+        out = np.zeros((h, w), np.float32)
+        check(self.lib.vt_get_relative_illumination(self._ctx, c, _p(out)), self._ctx)
+        return out
 
     # ------------------------------------------------------------------------------------------- batches
     def _batch_req(self, cameras, poses0, poses1, spp, lightSamples, seed, max_depth, shutter, scale, options, sensor, frame0,

@@ -1,6 +1,6 @@
 """gpu/sensor.js host logic: sensor parameters with defaults (sensorParams), the 256-byte sensor uniform
-(packSensorUniform), the modelled raw noise and the analogue-gain map. The GPU stage itself is libvtwin's
-sensor-expose kernel."""
+(packSensorUniform), the modelled raw noise, the analogue-gain map, the UVC-style auto exposure and the grey-world
+auto white balance. The GPU stages are libvtwin's sensor chain (vt_sensor_frame) and expose stage."""
 from __future__ import annotations
 
 import math
@@ -25,6 +25,9 @@ def sensor_params(over: dict | None = None) -> dict:
         "demosaic": "bilinear", "noiseReduction": "none", "nrSigmaPx": 0.4, "nrRangeScale": 2.0,
         "glareFraction": 0.0, "glareSigmaFrac": 0.25, "glareLevel": 16, "gamma": 2.2, "sharpenAmount": 0.0,
         "sharpenRadius": 1.0, "chroma": "4:2:0", "noise": True, "analogGainMax": 8.0,
+        "pupilExponent": 1.0, "vignettingThetaDeg": [0.0, 90.0], "vignetting": [1.0, 1.0],
+        "exposureUnit": 1e-4, "exposureRange": [1, 5000], "gainRange": [0, 100], "fps": 20, "aeTarget": 0.45,
+        "aeDamping": 0.3, "aeMaxStep": 2.0, "awb": True, "awbDamping": 0.3, "exposureUnits0": 10,
     }
     p.update(over or {})
     return p
@@ -75,7 +78,59 @@ def raw_noise_dn(p: dict, e: float, gain: float) -> float:
     return math.sqrt(max(0.0, e) + p["readNoise"] ** 2) * p["conversionGain"] * gain
 
 
-def analog_gain(p: dict, uvc_gain: float, gain_range=(0, 100)) -> float:
+def analog_gain(p: dict, uvc_gain: float, gain_range=None) -> float:
     """gpu/sensor.js:93 analogGain: UVC gain units -> linear analogue gain."""
-    g0, g1 = gain_range
+    g0, g1 = gain_range or p.get("gainRange", (0, 100))
     return 1 + (min(g1, max(g0, uvc_gain)) - g0) / max(1, g1 - g0) * (p["analogGainMax"] - 1)
+
+
+class AutoExposure:
+    """gpu/sensor.js:128 AutoExposure: exposure time first (whole exposure units, up to the frame time), then
+    analogue gain, damped toward the target mean luma; fed the previous frame's mean output luma."""
+
+    def __init__(self, p: dict, exposure_units=10, gain_units=0, enabled=True):
+        self.p, self.units, self.gain_units, self.enabled = p, exposure_units, gain_units, enabled
+        self.product = self.units * p["exposureUnit"] * analog_gain(p, gain_units)
+
+    @property
+    def exposure(self) -> float:
+        return self.units * self.p["exposureUnit"]
+
+    @property
+    def gain(self) -> float:
+        return analog_gain(self.p, self.gain_units)
+
+    def update(self, mean_luma: float) -> dict:
+        if not self.enabled:
+            return {"exposure": self.exposure, "gain": self.gain}
+        p = self.p
+        gam = 1.0 if p["tone"] == "linear" else 2.2
+        ratio = (p["aeTarget"] / mean_luma) ** gam if mean_luma > 1e-4 else 8.0
+        ratio = min(8.0, max(1 / 8, ratio))
+        ms = p.get("aeMaxStep") or 2.0
+        step = min(ms, max(1 / ms, ratio ** p["aeDamping"]))
+        self.product *= step
+        unit = p["exposureUnit"]
+        max_units = min(p["exposureRange"][1], math.floor(1 / (p["fps"] * unit)))
+        want = self.product / unit
+        self.units = max(p["exposureRange"][0], min(max_units, _js_round(want)))
+        g = self.product / (self.units * unit)
+        g0, g1 = p["gainRange"]
+        gu = g0 + (max(1.0, min(p["analogGainMax"], g)) - 1) / (p["analogGainMax"] - 1) * (g1 - g0)
+        self.gain_units = _js_round(gu)
+        self.product = max(p["exposureRange"][0] * unit, min(max_units * unit * p["analogGainMax"], self.product))
+        return {"exposure": self.exposure, "gain": self.gain}
+
+
+def _js_round(x: float) -> int:
+    """JavaScript Math.round: halves go up."""
+    return int(math.floor(x + 0.5))
+
+
+def update_awb(prev, mean_rgb, damping=0.3):
+    """gpu/sensor.js:184 updateAWB: grey-world gains equalising the raw channel means, damped in the log domain."""
+    g = list(prev) if prev is not None else [1.0, 1.0, 1.0]
+    if not (mean_rgb[0] > 1e-4 and mean_rgb[1] > 1e-4 and mean_rgb[2] > 1e-4):
+        return g
+    target = [mean_rgb[1] / mean_rgb[0], 1.0, mean_rgb[1] / mean_rgb[2]]
+    return [math.exp(math.log(x) + damping * (math.log(target[c]) - math.log(x))) for c, x in enumerate(g)]
