@@ -491,8 +491,9 @@ vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform*
     const size_t px = size_t(W) * H;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t b4 = al(px * 16), bl = al(std::max<size_t>(lev, 1) * 16), b1 = al(px * 4), bo = al(px * 4),
-                 by = al(px + 2 * size_t((W + 1) / 2) * ((H + 1) / 2)), bs = 256;
-    if (cudaMalloc(&C.isp_mem, 2 * b4 + 2 * bl + b1 + bo + by + bs) != cudaSuccess) {
+                 by = al(px + 2 * size_t((W + 1) / 2) * ((H + 1) / 2)), bs = 256,
+                 bp = al(size_t((W + 31) / 32) * ((H + 7) / 8) * 12 + 12);
+    if (cudaMalloc(&C.isp_mem, 2 * b4 + 2 * bl + b1 + bo + by + bs + bp) != cudaSuccess) {
       cudaGetLastError();
       C.isp_mem = nullptr;
       return fail(ctx, VT_ERR_OOM, "sensor chain buffers");
@@ -505,7 +506,8 @@ vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform*
     C.isp.gpl = reinterpret_cast<float*>(p); p += b1;
     C.isp.out = reinterpret_cast<uchar4*>(p); p += bo;
     C.isp.yuv = reinterpret_cast<uint8_t*>(p); p += by;
-    C.isp.stats = reinterpret_cast<uint32_t*>(p);
+    C.isp.stats = reinterpret_cast<uint32_t*>(p); p += bs;
+    C.isp.part = reinterpret_cast<uint32_t*>(p);
     C.isp_lev = std::max<size_t>(lev, 1);
   }
   C.isp.L = C.radiance;
@@ -524,7 +526,7 @@ vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform*
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   ctx->tim.sensor_ms = ms;
-  ctx->tim.launches += 6;
+  ctx->tim.launches += 8;
   C.exposed = C.processed = true;
   return VT_OK;
 }

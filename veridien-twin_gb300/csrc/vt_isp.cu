@@ -7,7 +7,8 @@
 //   isp_nr           3x3 bilateral on linear RGB, range sigma from the modelled shot + read noise
 //   isp_output       tone curve, unsharp mask on luma, BT.601 full-range YCbCr, 4:2:0 chroma, 8-bit RGB, luma sum
 // Each stage is one pass over the frame (a 1920x1200 frame is 2.3 M pixels: every pass is HBM/L2-bound at a few
-// microseconds); the statistics are integer sums, one atomic per block, so they do not depend on scheduling.
+// microseconds); the statistics are integer sums of per-block partials added by one small kernel, so they do not
+// depend on scheduling.
 //
 // This translation unit is compiled without multiply-add contraction (--fmad=false) and uses the fixed-order
 // elementary functions of vt_sensor.cuh, so every value is the one the CPU restatement computes from the same
@@ -42,17 +43,26 @@ __device__ __forceinline__ uint32_t cfa_channel(uint32_t code, uint32_t x, uint3
 
 }  // namespace
 
+// the blur's tap weights depend only on the tap: each block evaluates them once into shared memory
+__device__ __forceinline__ void block_taps(float sg, int r, float* taps) {
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  if (t <= 2 * r) taps[t] = tapW(t - r, sg);
+  __syncthreads();
+}
+
 __global__ void isp_optics_kernel(const SensorParams P, const float4* __restrict__ L, const float* __restrict__ ri, float4* __restrict__ A) {
+  __shared__ float taps[25];
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
   const float sg = su.f(5);
   const int r = gauss_taps(sg);
+  block_taps(sg, r, taps);
+  if (x >= W || y >= H) return;
   float ax = 0.0f, ay = 0.0f, az = 0.0f, ws = 0.0f;
   for (int k = -r; k <= r; k++) {
     const int xx = clampi(x + k, 0, W - 1);
-    const float w = tapW(k, sg);
+    const float w = taps[k + r];
     const float4 l = __ldg(L + size_t(y) * W + xx);
     const float m = __ldg(ri + size_t(y) * W + xx);
     ax = ax + w * l.x * m;
@@ -125,16 +135,18 @@ __device__ __forceinline__ float3 glare_at(const Su& su, const float4* __restric
 }
 
 __global__ void isp_expose_kernel(const SensorParams P, const float4* __restrict__ A, const float4* __restrict__ G, float* __restrict__ raw) {
+  __shared__ float taps[25];
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
   const float sg = su.f(5);
   const int r = gauss_taps(sg);
+  block_taps(sg, r, taps);
+  if (x >= W || y >= H) return;
   float ex = 0.0f, ey = 0.0f, ez = 0.0f, ws = 0.0f;
   for (int k = -r; k <= r; k++) {
     const int yy = clampi(y + k, 0, H - 1);
-    const float w = tapW(k, sg);
+    const float w = taps[k + r];
     const float4 e = A[size_t(yy) * W + x];
     ex = ex + w * e.x;
     ey = ey + w * e.y;
@@ -189,8 +201,25 @@ __global__ void demosaic_g_kernel(const SensorParams P, const float* __restrict_
   gpl[size_t(y) * W + x] = g;
 }
 
+// a block's sums of v[0..2] (256 threads) written to out[0..2]
+__device__ __forceinline__ void block_sum3(const uint32_t v[3], uint32_t* out) {
+  __shared__ uint32_t sm[8][3];
+  const int t = threadIdx.y * blockDim.x + threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t a[3] = {v[0], v[1], v[2]};
+  for (int k = 0; k < 3; k++)
+    for (int s = 16; s > 0; s >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], s);
+  if (lane == 0)
+    for (int k = 0; k < 3; k++) sm[warp][k] = a[k];
+  __syncthreads();
+  if (t < 3) {
+    uint32_t s = 0;
+    for (int w = 0; w < int(blockDim.x * blockDim.y) / 32; w++) s += sm[w][t];
+    out[t] = s;
+  }
+}
+
 __global__ void __launch_bounds__(256) demosaic_rb_kernel(const SensorParams P, const float* __restrict__ raw, const float* __restrict__ gpl,
-                                                          float4* __restrict__ B, uint32_t* __restrict__ stats) {
+                                                          float4* __restrict__ B, uint32_t* __restrict__ part) {
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -235,12 +264,8 @@ __global__ void __launch_bounds__(256) demosaic_rb_kernel(const SensorParams P, 
     for (int k = 0; k < 3; k++) o[k] = su.f(32 + 4 * k) * c[0] + su.f(33 + 4 * k) * c[1] + su.f(34 + 4 * k) * c[2];
     B[size_t(y) * W + x] = make_float4(o[0], o[1], o[2], 1.0f);
   }
-  // white-balance statistics: integer sums, a warp reduction and one atomic per warp
-  for (int k = 0; k < 3; k++) {
-    uint32_t v = q[k];
-    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-    if ((threadIdx.x + threadIdx.y * blockDim.x) % 32u == 0 && v) atomicAdd(stats + 1 + k, v);
-  }
+  // white-balance statistics: integer sums per block into this block's partial (added up by isp_stats_kernel)
+  block_sum3(q, part + 3 * size_t(blockIdx.y * gridDim.x + blockIdx.x));
 }
 
 __global__ void isp_nr_kernel(const SensorParams P, const float4* __restrict__ B, float4* __restrict__ A) {
@@ -292,7 +317,7 @@ __device__ __forceinline__ float luma601(float3 c) { return c.x * 0.299f + c.y *
 
 // one thread per 2x2 block
 __global__ void __launch_bounds__(256) isp_output_kernel(const SensorParams P, const float4* __restrict__ A, uchar4* __restrict__ out,
-                                                         uint8_t* __restrict__ yuv, uint32_t* __restrict__ stats) {
+                                                         uint8_t* __restrict__ yuv, uint32_t* __restrict__ part) {
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
   const int gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y * blockDim.y + threadIdx.y;
@@ -348,8 +373,26 @@ __global__ void __launch_bounds__(256) isp_output_kernel(const SensorParams P, c
       yuv[size_t(W) * H + size_t(cw) * chh + size_t(gy) * cw + gx] = uint8_t(Cr);
     }
   }
-  for (int s = 16; s > 0; s >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, s);
-  if ((threadIdx.x + threadIdx.y * blockDim.x) % 32u == 0 && lsum) atomicAdd(stats, lsum);
+  const uint32_t v[3] = {lsum, 0u, 0u};
+  block_sum3(v, part + 3 * size_t(blockIdx.y * gridDim.x + blockIdx.x));
+}
+
+// stats[k] = the sum of the blocks' partials of statistic k (n blocks, 3 words each): one block, fixed order
+__global__ void __launch_bounds__(1024) isp_stats_kernel(const uint32_t* __restrict__ part, uint32_t n, int k0, int k1, uint32_t* __restrict__ stats) {
+  __shared__ uint32_t sm[32];
+  for (int k = k0; k < k1; k++) {
+    uint32_t s = 0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += part[3 * size_t(i) + (k - k0)];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31u) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t t = 0;
+      for (int w = 0; w < int(blockDim.x) / 32; w++) t += sm[w];
+      stats[k] = t;
+    }
+    __syncthreads();
+  }
 }
 
 static float host_float(uint32_t u) {
@@ -361,7 +404,6 @@ static float host_float(uint32_t u) {
 void launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
   const uint32_t W = P.w[0], H = P.w[1];
   const dim3 blk(32, 8), g((W + 31) / 32, (H + 7) / 8);
-  cudaMemsetAsync(b.stats, 0, 16, st);
   isp_optics_kernel<<<g, blk, 0, st>>>(P, b.L, b.ri, b.A);
   const float k = host_float(P.w[52]);
   if (k > 0.0f) {
@@ -374,10 +416,15 @@ void launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
   }
   isp_expose_kernel<<<g, blk, 0, st>>>(P, b.A, b.GA, b.raw);
   demosaic_g_kernel<<<g, blk, 0, st>>>(P, b.raw, b.gpl);
-  demosaic_rb_kernel<<<g, blk, 0, st>>>(P, b.raw, b.gpl, b.B, b.stats);
-  isp_nr_kernel<<<g, blk, 0, st>>>(P, b.B, b.A);
+  demosaic_rb_kernel<<<g, blk, 0, st>>>(P, b.raw, b.gpl, b.B, b.part);
+  isp_stats_kernel<<<1, 1024, 0, st>>>(b.part, g.x * g.y, 1, 4, b.stats);
+  // noise reduction off: the output stage reads the demosaiced image directly (the kernel would copy it)
+  const bool nr = P.w[51] != 0u && host_float(P.w[58]) > 0.0f;
+  if (nr) isp_nr_kernel<<<g, blk, 0, st>>>(P, b.B, b.A);
   const uint32_t cw = (W + 1) / 2, ch = (H + 1) / 2;
-  isp_output_kernel<<<dim3((cw + 31) / 32, (ch + 7) / 8), blk, 0, st>>>(P, b.A, b.out, b.yuv, b.stats);
+  const dim3 go((cw + 31) / 32, (ch + 7) / 8);
+  isp_output_kernel<<<go, blk, 0, st>>>(P, nr ? b.A : b.B, b.out, b.yuv, b.part);
+  isp_stats_kernel<<<1, 1024, 0, st>>>(b.part, go.x * go.y, 0, 1, b.stats);
 }
 
 }  // namespace vtk

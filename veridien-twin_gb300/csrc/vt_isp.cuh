@@ -17,6 +17,7 @@ struct IspBufs {
   uchar4* out;       // 8-bit RGB (alpha 255)
   uint8_t* yuv;      // Y (w x h), then Cb and Cr (ceil(w/2) x ceil(h/2) each)
   uint32_t* stats;   // luma sum, white-balance sums R, G, B
+  uint32_t* part;    // per-block partial sums (3 words per block of 32 x 8 pixels)
 };
 
 // the whole chain for one frame of the uniform's size
