@@ -486,7 +486,10 @@ __device__ __forceinline__ bool trace_phase(const Scene& S, uint32_t root, float
 
 // the traversal stack of a lane: its first SH_DEPTH entries in shared memory (entry-major, so a warp's accesses are
 // consecutive words), the rest of the 32 in local memory
-constexpr uint32_t SH_DEPTH = 16;
+#ifndef VT_SH_DEPTH
+#define VT_SH_DEPTH 16
+#endif
+constexpr uint32_t SH_DEPTH = VT_SH_DEPTH;
 struct LaneStack {
   uint2* sh;           // shared: SH_DEPTH x stride entries of (node, t bits)
   uint32_t lane, stride;

@@ -5,6 +5,7 @@
 #include "vt_host.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -44,6 +45,10 @@ class SahBuilder {
     for (uint32_t i = 0; i < n; i++) out_.order[i] = i;
   }
 
+  // The children of a node are decided (bounds, split and partition of their slot ranges) independently of every
+  // other node's, so subtrees are decided in parallel on the host's threads; the node numbering is then replayed in
+  // the sequential builder's task order (LIFO, both children of a node numbered before either is expanded), which
+  // gives the same node array as building one task at a time.
   Bvh run() {
     uint32_t root = new_node();
     Box all = bounds(0, n_);
@@ -60,24 +65,12 @@ class SahBuilder {
         if (n_ > 1) { Box b1 = bounds(h, n_); put(root, 1, b1.lo, b1.hi, h, n_ - h); }
         else put(root, 1, all.lo, all.hi, 0, n_);
       } else {
-        tasks_.push_back({root, 0, int64_t(n_), m, 1});
-      }
-    }
-    while (!tasks_.empty()) {
-      Task t = tasks_.back();
-      tasks_.pop_back();
-      out_.max_depth = std::max(out_.max_depth, t.depth);
-      const int64_t lo[2] = {t.s, t.m}, hi[2] = {t.m, t.e};
-      for (int slot = 0; slot < 2; slot++) {
-        Box b = bounds(lo[slot], hi[slot]);
-        int64_t mm = choose(lo[slot], hi[slot], b);
-        if (mm < 0) {
-          put(t.node, slot, b.lo, b.hi, uint32_t(lo[slot]), uint32_t(hi[slot] - lo[slot]));
-        } else {
-          uint32_t child = new_node();
-          put(t.node, slot, b.lo, b.hi, child, 0);
-          tasks_.push_back({child, lo[slot], hi[slot], mm, t.depth + 1});
-        }
+        shapes_.resize(std::max<size_t>(1, n_));
+        shapes_[0].s = 0; shapes_[0].e = int64_t(n_); shapes_[0].m = m;
+        n_shapes_ = 1;
+        threads_left_ = int(std::max(1u, std::thread::hardware_concurrency())) - 1;
+        decide(0);
+        number(root);
       }
     }
     for (int k = 0; k < 3; k++) { out_.lo[k] = float(all.lo[k]); out_.hi[k] = float(all.hi[k]); }
@@ -85,8 +78,68 @@ class SahBuilder {
   }
 
  private:
-  struct Task { uint32_t node; int64_t s, e, m; uint32_t depth; };
+  // an interior node: its range [s, e) split at m, and per child its bounds and either a leaf or an interior child
+  struct Shape {
+    int64_t s = 0, e = 0, m = 0;
+    Box b[2];
+    int64_t child[2] = {-1, -1};
+  };
   static constexpr int kBins = 16;
+  static constexpr int64_t kParallelMin = 8192;   // ranges at least this large are decided on their own thread
+
+  void decide(int64_t si) {
+    const int64_t lo[2] = {shapes_[si].s, shapes_[si].m}, hi[2] = {shapes_[si].m, shapes_[si].e};
+    auto slot_of = [&](int slot) {
+      Shape& S = shapes_[si];
+      S.b[slot] = bounds(lo[slot], hi[slot]);
+      const int64_t mm = choose(lo[slot], hi[slot], S.b[slot]);
+      if (mm >= 0) {
+        const int64_t c = n_shapes_.fetch_add(1);
+        shapes_[c].s = lo[slot]; shapes_[c].e = hi[slot]; shapes_[c].m = mm;
+        S.child[slot] = c;
+      }
+    };
+    const bool split = hi[0] - lo[0] >= kParallelMin && hi[1] - lo[1] >= kParallelMin && take_thread();
+    if (split) {
+      std::thread t([&] { slot_of(0); if (shapes_[si].child[0] >= 0) decide(shapes_[si].child[0]); });
+      slot_of(1);
+      if (shapes_[si].child[1] >= 0) decide(shapes_[si].child[1]);
+      t.join();
+      threads_left_.fetch_add(1);
+    } else {
+      slot_of(0);
+      slot_of(1);
+      for (int slot = 0; slot < 2; slot++)
+        if (shapes_[si].child[slot] >= 0) decide(shapes_[si].child[slot]);
+    }
+  }
+  bool take_thread() {
+    int k = threads_left_.load();
+    while (k > 0)
+      if (threads_left_.compare_exchange_weak(k, k - 1)) return true;
+    return false;
+  }
+  // node numbers in task order: pop a node, number its interior children (slot 0 then 1), push them
+  void number(uint32_t root) {
+    struct Item { int64_t shape; uint32_t node, depth; };
+    std::vector<Item> stack{{0, root, 1}};
+    while (!stack.empty()) {
+      const Item it = stack.back();
+      stack.pop_back();
+      out_.max_depth = std::max(out_.max_depth, it.depth);
+      const Shape& S = shapes_[it.shape];
+      const int64_t lo[2] = {S.s, S.m}, hi[2] = {S.m, S.e};
+      for (int slot = 0; slot < 2; slot++) {
+        if (S.child[slot] < 0) {
+          put(it.node, slot, S.b[slot].lo, S.b[slot].hi, uint32_t(lo[slot]), uint32_t(hi[slot] - lo[slot]));
+        } else {
+          const uint32_t child = new_node();
+          put(it.node, slot, S.b[slot].lo, S.b[slot].hi, child, 0);
+          stack.push_back({S.child[slot], child, it.depth + 1});
+        }
+      }
+    }
+  }
 
   uint32_t new_node() { out_.words.resize(out_.words.size() + VT_NODE_WORDS, 0u); return out_.node_count++; }
   void put(uint32_t node, int slot, const double* lo, const double* hi, uint32_t ref, uint32_t count) {
@@ -94,7 +147,7 @@ class SahBuilder {
     w[0] = fbits(float(lo[0])); w[1] = fbits(float(lo[1])); w[2] = fbits(float(lo[2])); w[3] = ref;
     w[4] = fbits(float(hi[0])); w[5] = fbits(float(hi[1])); w[6] = fbits(float(hi[2])); w[7] = count;
   }
-  Box bounds(int64_t s, int64_t e) const {
+  Box bounds_serial(int64_t s, int64_t e) const {
     Box b;
     for (int k = 0; k < 3; k++) { b.lo[k] = kBig; b.hi[k] = -kBig; b.clo[k] = kBig; b.chi[k] = -kBig; }
     for (int64_t i = s; i < e; i++) {
@@ -108,6 +161,42 @@ class SahBuilder {
       }
     }
     return b;
+  }
+  // minima and maxima do not depend on the order they are taken in: large ranges are split over threads
+  Box bounds(int64_t s, int64_t e) const {
+    const int nt = chunks(e - s);
+    if (nt <= 1) return bounds_serial(s, e);
+    std::vector<Box> part(nt);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) th.emplace_back([&, t] { part[t] = bounds_serial(s + (e - s) * t / nt, s + (e - s) * (t + 1) / nt); });
+    for (auto& x : th) x.join();
+    Box b = part[0];
+    for (int t = 1; t < nt; t++)
+      for (int k = 0; k < 3; k++) {
+        b.lo[k] = std::min(b.lo[k], part[t].lo[k]); b.hi[k] = std::max(b.hi[k], part[t].hi[k]);
+        b.clo[k] = std::min(b.clo[k], part[t].clo[k]); b.chi[k] = std::max(b.chi[k], part[t].chi[k]);
+      }
+    return b;
+  }
+  static int chunks(int64_t n) {
+    if (n < 131072) return 1;
+    return int(std::max<int64_t>(1, std::min<int64_t>(std::thread::hardware_concurrency(), n / 65536)));
+  }
+  struct Bins {
+    uint32_t count[16];
+    double lo[16][3], hi[16][3];
+  };
+  void bin_range(int64_t s, int64_t e, int ax, double origin, double scale, Bins& B) const {
+    for (int b = 0; b < kBins; b++) { B.count[b] = 0; for (int k = 0; k < 3; k++) { B.lo[b][k] = kBig; B.hi[b][k] = -kBig; } }
+    for (int64_t i = s; i < e; i++) {
+      const uint32_t t = out_.order[i];
+      const int64_t b = bin_of(t, ax, origin, scale);
+      B.count[b]++;
+      for (int k = 0; k < 3; k++) {
+        if (bmin_[3 * t + k] < B.lo[b][k]) B.lo[b][k] = bmin_[3 * t + k];
+        if (bmax_[3 * t + k] > B.hi[b][k]) B.hi[b][k] = bmax_[3 * t + k];
+      }
+    }
   }
   static double half_area(const double* lo, const double* hi) {
     double x = std::max(0.0, hi[0] - lo[0]), y = std::max(0.0, hi[1] - lo[1]), z = std::max(0.0, hi[2] - lo[2]);
@@ -127,19 +216,27 @@ class SahBuilder {
     for (int ax = 0; ax < 3; ax++) {
       const double origin = B.clo[ax], extent = B.chi[ax] - origin;
       if (!(extent > 0)) continue;
-      uint32_t count[kBins] = {};
-      double blo[kBins][3], bhi[kBins][3];
-      for (int b = 0; b < kBins; b++) for (int k = 0; k < 3; k++) { blo[b][k] = kBig; bhi[b][k] = -kBig; }
       const double scale = kBins / extent;
-      for (int64_t i = s; i < e; i++) {
-        const uint32_t t = out_.order[i];
-        const int64_t b = bin_of(t, ax, origin, scale);
-        count[b]++;
-        for (int k = 0; k < 3; k++) {
-          if (bmin_[3 * t + k] < blo[b][k]) blo[b][k] = bmin_[3 * t + k];
-          if (bmax_[3 * t + k] > bhi[b][k]) bhi[b][k] = bmax_[3 * t + k];
-        }
+      // counts, minima and maxima per bin: exact whatever the order, so large ranges are binned over threads
+      Bins all;
+      const int nt = chunks(cnt);
+      if (nt <= 1) {
+        bin_range(s, e, ax, origin, scale, all);
+      } else {
+        std::vector<Bins> part(nt);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; t++) th.emplace_back([&, t] { bin_range(s + cnt * t / nt, s + cnt * (t + 1) / nt, ax, origin, scale, part[t]); });
+        for (auto& x : th) x.join();
+        all = part[0];
+        for (int t = 1; t < nt; t++)
+          for (int b = 0; b < kBins; b++) {
+            all.count[b] += part[t].count[b];
+            for (int k = 0; k < 3; k++) { all.lo[b][k] = std::min(all.lo[b][k], part[t].lo[b][k]); all.hi[b][k] = std::max(all.hi[b][k], part[t].hi[b][k]); }
+          }
       }
+      const uint32_t* count = all.count;
+      const double(*blo)[3] = all.lo;
+      const double(*bhi)[3] = all.hi;
       uint32_t right_count[kBins];
       double right_area[kBins];
       double lo[3] = {kBig, kBig, kBig}, hi[3] = {-kBig, -kBig, -kBig};
@@ -176,7 +273,9 @@ class SahBuilder {
 
   uint32_t n_, leaf_;
   std::vector<float> bmin_, bmax_, cen_;
-  std::vector<Task> tasks_;
+  std::vector<Shape> shapes_;
+  std::atomic<int64_t> n_shapes_{0};
+  std::atomic<int> threads_left_{0};
   Bvh out_;
 };
 }  // namespace

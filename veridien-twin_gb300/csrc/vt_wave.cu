@@ -21,6 +21,10 @@ namespace vtk {
 using namespace vtd;
 
 constexpr int WAVE_THREADS = 256;
+// resident blocks per SM the traversal kernels are compiled for (register budget 65536 / (256 x this))
+#ifndef VT_TRACE_BLOCKS
+#define VT_TRACE_BLOCKS 4
+#endif
 
 // append `want` lanes' items to a queue with one atomic per warp; returns the slot of this lane (if want)
 __device__ __forceinline__ uint32_t warp_append(uint32_t* count, bool want) {
@@ -138,7 +142,7 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_gen_pairs_kernel(const CamP
 }
 
 template <int VAR>
-__global__ void __launch_bounds__(WAVE_THREADS, 4) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
+__global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
   if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats, (unsigned long long)n);
   __shared__ uint2 stack_sh[SH_DEPTH * WAVE_THREADS];
@@ -296,7 +300,7 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S0, const
 // any-hit of every queued path's light samples in sample order on persistent lanes; a lane moves to the path's next
 // sample when one finishes, and to a new path when the last one does
 template <int VAR>
-__global__ void __launch_bounds__(WAVE_THREADS, 4) wave_shadow(const Scene S0, const CamParams cp, WaveBufs wb) {
+__global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(const Scene S0, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_sh;
   if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats + 1, (unsigned long long)n);
   const uint32_t nl = cp.n_light;
