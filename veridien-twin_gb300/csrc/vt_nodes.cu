@@ -281,7 +281,7 @@ __global__ void jacobi_update_kernel(const Scene S, const uint32_t* __restrict__
     float3 ef = f3(0, 0, 0);
     float ws = 0.0f;
     for (uint32_t j = 0; j < nbr_k; j++) {
-      const uint2 e = nbr[size_t(k) * nbr_k + j];
+      const uint2 e = __ldcs(nbr + size_t(k) * nbr_k + j);
       const float w = __uint_as_float(e.y);
       if (w <= 0.0f) break;
       ef = ef + xyz(aux[e.x]) * w;
@@ -343,28 +343,42 @@ __global__ void __launch_bounds__(256) transport_fill_kernel(const Scene S, cons
   }
 }
 
-// jacobiGather over the transport table: aux[k] = sum over the row of weight x Ls_h
+// jacobiGather over the transport table: aux[k] = sum over the row of weight x Ls_h. A half-warp per row, four
+// 16-byte entries per lane in flight (a row of K = 64 rays in one pass), then the landing nodes' Ls; the entry
+// stream is the only DRAM traffic that grows with the rays; it is loaded evict-first, so the node state (21 MB at
+// 331k nodes) stays in L2 for the gathers.
 __global__ void __launch_bounds__(256) jacobi_gather_table_kernel(const uint32_t* __restrict__ row, const float4* __restrict__ ent, uint32_t n_active,
                                                                   uint32_t slot_in, const float4* __restrict__ nstate, float4* __restrict__ aux) {
-  const uint32_t lane = threadIdx.x & 31u;
-  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n_active; k += (gridDim.x * blockDim.x) >> 5) {
-    const uint32_t e0 = row[k], e1 = row[k + 1];
+  const uint32_t hl = threadIdx.x & 15u;
+  const uint32_t half = (blockIdx.x * blockDim.x + threadIdx.x) >> 4, halves = (gridDim.x * blockDim.x) >> 4;
+  // whole warps iterate together (the half-warp shuffles need both halves present)
+  const uint32_t rounds = (n_active + halves - 1) / halves;
+  for (uint32_t it = 0; it < rounds; it++) {
+    const uint32_t k = half + it * halves;
+    const bool in = k < n_active;
+    const uint32_t e0 = in ? row[k] : 0u, e1 = in ? row[k + 1] : 0u;
     float3 acc = f3(0, 0, 0);
-    // 64 entries per pass, two per lane, both entry loads and then both Ls loads in flight before any use
     for (uint32_t b = e0; b < e1; b += 64) {
-      const uint32_t ea = b + lane, eb = b + 32u + lane;
-      const float4 wa = ea < e1 ? __ldg(ent + ea) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      const float4 wb = eb < e1 ? __ldg(ent + eb) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      const float4 la = ea < e1 ? nstate[4u * __float_as_uint(wa.w) + slot_in] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      const float4 lb = eb < e1 ? nstate[4u * __float_as_uint(wb.w) + slot_in] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      acc = acc + xyz(wa) * xyz(la) + xyz(wb) * xyz(lb);
+      float4 w[4], l[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint32_t e = b + hl + 16u * q;
+        w[q] = e < e1 ? __ldcs(ent + e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);   // streamed: keep Ls in L2
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint32_t e = b + hl + 16u * q;
+        l[q] = e < e1 ? nstate[4u * __float_as_uint(w[q].w) + slot_in] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc = acc + xyz(w[q]) * xyz(l[q]);
     }
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = 8; o > 0; o >>= 1) {
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
       acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
     }
-    if (lane == 0) aux[k] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+    if (in && hl == 0) aux[k] = make_float4(acc.x, acc.y, acc.z, 0.0f);
   }
 }
 
@@ -415,7 +429,7 @@ void launch_jacobi_step(const Scene& S, const uint32_t* active, uint32_t n_activ
                         float4* nstate, float4* aux, cudaStream_t st) {
   if (!n_active) return;
   if (ent)
-    jacobi_gather_table_kernel<<<grid_for(size_t(n_active) * 32, 256), 256, 0, st>>>(row, ent, n_active, slot_in, nstate, aux);
+    jacobi_gather_table_kernel<<<grid_for(size_t(n_active) * 16, 256), 256, 0, st>>>(row, ent, n_active, slot_in, nstate, aux);
   else
     jacobi_gather_kernel<<<grid_for(size_t(n_active) * 32, 256), 256, 0, st>>>(S, active, n_active, K, gtable, amu, slot_in, nstate, aux);
   jacobi_update_kernel<<<grid_for(n_active, 128), 128, 0, st>>>(S, active, n_active, nbr, nbr_k, aux, slot_out, nstate);
