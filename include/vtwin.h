@@ -462,6 +462,13 @@ vt_status vt_nodes_export(vt_ctx* ctx, uint32_t* gtable, uint32_t* active, uint3
 /* The node state (n_nodes x 16 floats) and its latest slot. */
 vt_status vt_get_node_state(vt_ctx* ctx, float* state, uint32_t* slot);
 
+/* The bounded-wait path of the device pipelines (the tcgen05 and bulk-copy ring buffers), exercised on purpose:
+ * one block waits on an mbarrier phase for at most `cycles` SM clocks (1 .. 2^36); with arrive = 1 the phase
+ * completes and the call returns VT_OK, with arrive = 0 nothing arrives, the wait runs out and the call returns
+ * VT_ERR_TIMEOUT with the context still usable. No counterpart in the reference (its device waits are the
+ * browser's). */
+vt_status vt_wait_check(vt_ctx* ctx, uint64_t cycles, int arrive);
+
 /* ---------------------------------------------------------------------------------------- bvh (pure) */
 
 /* gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}): binned SAH BVH2 on the host. nodes_out must hold

@@ -588,6 +588,18 @@ vt_status vt_debug_flags(vt_ctx* ctx, uint32_t out[16], int reset) {
   return VT_OK;
 }
 
+vt_status vt_wait_check(vt_ctx* ctx, uint64_t cycles, int arrive) {
+  if (!ctx || cycles == 0 || cycles > (1ull << 36)) return VT_ERR_ARG;
+  uint32_t* err = ctx->d_work + 32;
+  VT_CK(cudaMemsetAsync(err, 0, 4, ctx->stream));
+  vtk::launch_wait_check(cycles, arrive ? 1u : 0u, err, ctx->stream);
+  VT_CK(cudaGetLastError());
+  uint32_t e = 0;
+  VT_CK(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  return e ? fail(ctx, VT_ERR_TIMEOUT, "wait check: the barrier phase did not complete within the limit") : VT_OK;
+}
+
 vt_status vt_timings_get(const vt_ctx* ctx, vt_timings* out) {
   if (!ctx || !out) return VT_ERR_ARG;
   *out = ctx->tim;

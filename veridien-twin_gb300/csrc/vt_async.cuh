@@ -26,7 +26,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 // bounded wait for the completion of the phase with parity `parity`; false (and *err set) when it runs out
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t* err) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t* err, unsigned long long limit = WAIT_CYCLES) {
   const unsigned long long t0 = clock64();
   for (;;) {
     uint32_t ok;
@@ -36,7 +36,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (clock64() - t0 > WAIT_CYCLES) { atomicOr(err, 1u); return false; }
+    if (clock64() - t0 > limit) { atomicOr(err, 1u); return false; }
   }
 }
 // untiled bulk copy global -> shared, completing on an mbarrier (both addresses 16-byte aligned, bytes % 16 == 0)

@@ -422,3 +422,24 @@ void tc_combine_residual(const float* partials, uint32_t splits, uint32_t n, uin
 void tc_axpy(float* B, const float* d, size_t count, cudaStream_t st) { axpy_kernel<<<1216, 256, 0, st>>>(B, d, count); }
 
 }  // namespace vtk
+
+// ------------------------------------------------------------------------------------------------ wait check
+// The bounded-wait path of the pipelines above, exercised on purpose: one block waits on an mbarrier phase that
+// completes only if `arrive` is set (one arrival of the barrier's count of 1). Without it the wait runs out after
+// `cycles`, sets the error word and the kernel returns: the host sees a timeout and the context stays usable.
+namespace vtk {
+__global__ void wait_check_kernel(uint64_t cycles, uint32_t arrive, uint32_t* err) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t b = async::smem_u32(&bar);
+  if (threadIdx.x == 0) {
+    async::mbar_init(b, 1);
+    async::mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && arrive) async::mbar_arrive(b);
+  if (threadIdx.x == 0) async::mbar_wait(b, 0, err, cycles);
+}
+void launch_wait_check(uint64_t cycles, uint32_t arrive, uint32_t* err, cudaStream_t st) {
+  wait_check_kernel<<<1, 32, 0, st>>>(cycles, arrive, err);
+}
+}  // namespace vtk

@@ -39,4 +39,7 @@ void tc_combine_residual(const float* partials, uint32_t splits, uint32_t n, uin
 // B += d
 void tc_axpy(float* B, const float* d, size_t count, cudaStream_t st);
 
+// one bounded mbarrier wait that completes only when `arrive` is set; *err is set when it runs out after `cycles`
+void launch_wait_check(uint64_t cycles, uint32_t arrive, uint32_t* err, cudaStream_t st);
+
 }  // namespace vtk

@@ -64,6 +64,7 @@ SIGNATURES = {
     "vt_debug_flags": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int]),
     "vt_timings_get": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_timings)]),
     "vt_stream": (C.c_void_p, [C.c_void_p]),
+    "vt_wait_check": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_int]),
 }
 
 _lib = None
