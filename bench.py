@@ -44,6 +44,19 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def job_rate(ms_local, samples_per_rank, world, dist=None, device="cuda"):
+    """Whole-job rate of `world` replicas: the samples of all ranks over the slowest rank's time (max over ranks).
+    Returns (Msamples/s, the max time in ms)."""
+    ms = float(ms_local)
+    if dist is not None and world > 1:
+        import torch
+
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return samples_per_rank * world / (ms / 1e3) / 1e6, ms
+
+
 class Clocks:
     """nvidia-smi samples every 200 ms while the timed region runs."""
     Q = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
@@ -219,12 +232,7 @@ def main():
         torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in evs)
     launches = r.timings()["launches"] - launches0
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    samples = W_ * H_ * SPP * args.steps * world
-    value = samples / (ms / 1e3) / 1e6
+    value, ms = job_rate(ms, W_ * H_ * SPP * args.steps, world, dist, "cuda")
     # end to end through the public API: pose upload + render + radiance copy to pinned host memory
     host = torch.empty((H_, W_, 4), dtype=torch.float32).pin_memory()
     hnp = host.numpy()
