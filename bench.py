@@ -19,6 +19,7 @@ bounded sample of the same frame; the reference itself is JavaScript + WebGPU an
   python bench.py --case calib:W:H:SPP             one calibration forward + backward (3 cameras, depth 3, 4096 nodes)
   python bench.py --case nodes                     the scene node radiosity on the level-5 and level-8 domes
   python bench.py --case sensor                    the camera sensor chain at 1280x720 and 1920x1200
+  python bench.py --case twin[:LEVEL]              the reference's twin frame (3 x 1280x720, presets live / balanced / judge)
 """
 import argparse
 import json
@@ -185,6 +186,7 @@ def main():
     ap.add_argument("--no-calib", action="store_true")
     ap.add_argument("--no-nodes", action="store_true")
     ap.add_argument("--no-sensor", action="store_true")
+    ap.add_argument("--no-twin-frame", action="store_true")
     ap.add_argument("--case", default=None, help="render:W:H:SPP or radiosity:N:PREC:SWEEPS (a small profiling case)")
     args = ap.parse_args()
     if args.case:
@@ -298,6 +300,8 @@ def main():
             line["scene_nodes"] = nodes_bench(torch, local)
         if not args.no_sensor:
             line["sensor_chain"] = sensor_bench(torch, local)
+        if not args.no_twin_frame:
+            line["twin_frame"] = twin_frame_bench(torch, local)
         print(json.dumps(line))
     r.destroy()
     if dist:
@@ -361,6 +365,8 @@ def run_case(spec):
         print(json.dumps({"case": spec, **nodes_bench(torch)}))
     elif kind == "sensor":
         print(json.dumps({"case": spec, **sensor_bench(torch)}))
+    elif kind == "twin":
+        print(json.dumps({"case": spec, **twin_frame_bench(torch, level=int(a[0]) if a else 8)}))
     elif kind == "calib":
         from vtwin.renderer import TwinRenderer
 
@@ -521,6 +527,46 @@ def calib_bench(torch, device=0):
             "grad_check": {"entries": len(ids), "h": 3e-3, "vector_rel_err": vec, "worst_entry_rel_err": worst,
                            "note": "GPU central differences of the FP32 render (FP64 loss); FP64-oracle differences at "
                                    "h = 1e-4 are in tests/test_gpu_calib.py"}}
+
+
+PRESETS_REF = {   # gpu/renderer.js:31-66 DEFAULTS (the judge preset) and the live / balanced presets
+    "live": {"spp": 1, "lightSamples": 1, "refine": 0, "radiosityEvery": 2, "itersPerFrame": 1},
+    "balanced": {"spp": 1, "lightSamples": 2, "refine": 2, "refineLightSamples": 1, "refineShadows": False, "radiosityEvery": 2,
+                 "itersPerFrame": 1},
+    "judge": {"spp": 1, "refine": 6, "lightSamples": 4, "refineLightSamples": 1, "refineShadows": True, "radiosityEvery": 1,
+              "itersPerFrame": 4},
+}
+
+
+def twin_frame_bench(torch, device=0, level=8, frames=10, warmup=3):
+    """The reference's own frame (gpu/renderer.js:55-59 quotes ~45 / ~84 / ~190-245 ms per frame for the live /
+    balanced / judge presets on an Apple M4, WebGPU): three 1280x720 KB4 tracking cameras, six instruments moving
+    every frame, renderFrame with the twin shading (node radiosity kept up to date with the poses: incremental
+    updates, Jacobi steps per the preset), then the sensor chain of every camera. On a level-8 dome (657k static
+    triangles, 331k nodes), the size of the reference's scene. Wall time per frame (every call synchronises)."""
+    from vtwin import _abi as A
+    from vtwin import dome
+    from vtwin.renderer import TwinRenderer
+
+    sc = dome.make_dome_scene(seed=1, width=64, height=48, level=level, with_instruments=6)
+    sc["cameras"] = dome.batched_cameras(seed=3, n=3, width=1280, height=720)
+    poses = dome.instrument_poses(n_poses=frames + warmup, n_tools=6, seed=21)
+    out = {"workload": f"3 KB4 cameras 1280x720, twin shading, 6 moving instruments, level-{level} dome "
+                       f"({len(sc['static']['I'])} static triangles, {len(sc['static']['P'])} nodes), sensor chain"}
+    for name, preset in PRESETS_REF.items():
+        r = TwinRenderer.create(sc, device=device, **preset)
+        t_create = r.nodes_info["gatherBuildMs"]
+        ms = []
+        for k in range(frames + warmup):
+            r.set_pose_array(np.concatenate([A.identity_poses(1), poses[k]]))
+            t0 = time.perf_counter()
+            r.renderFrame(sensor=True, sensorOpts={"exposure_s": 2e-3, "gain": 1.0})
+            if k >= warmup:
+                ms.append((time.perf_counter() - t0) * 1e3)
+        out[name] = {"ms_per_frame": float(np.median(ms)), "min_ms": float(min(ms)), "gather_build_ms": t_create, **preset}
+        r.destroy()
+    out["reference_m4_ms"] = {"live": 45, "balanced": 84, "judge": "190-245"}
+    return out
 
 
 def sensor_bench(torch, device=0):

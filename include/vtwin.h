@@ -43,10 +43,18 @@ enum {
 enum { VT_F_STATIC = 1, VT_F_EMITTER = 2, VT_F_LAYER = 4, VT_F_BOARD = 8, VT_F_INSTRUMENT = 16, VT_F_SCOPE = 32,
        VT_F_BENCH = 64, VT_F_TEXTURED = 128 };
 
-/* camera option bits, gpu/renderer.js:26 OPTION_BITS (the cache bits 2048/4096/8192 are accepted and ignored:
- * the first-hit and static-occlusion caches are a WebGPU-era device; see the render request) */
+/* camera option bits, gpu/renderer.js:26 OPTION_BITS. VT_O_CACHE_WRITE / VT_O_CACHE_READ (either) turn on the static
+ * first-hit cache of the camera (gpu/renderer.js:941-950 hitCache): each sub-sample's closest hit in the static BVH
+ * is traced once and kept while the seed, the BVH root, the camera pose and lens and the pixel tiling hold (the
+ * library keeps the key and fills empty entries), so later renders trace only the posed bodies for camera rays.
+ * Exact: the images are the uncached ones bit for bit. VT_O_SHADOW_CACHE with the first-hit cache, in twin mode,
+ * adds the static-occlusion cache (gpu/wgsl/shade.wgsl.js:270-301): per first-hit light sample on a static surface
+ * whether the static scene hides it, kept while the emitter body stays where it was (the posed bodies are traced
+ * every frame). The radiance is the same; as in the reference, the refinement's shadow key bit then marks pixels
+ * where a posed body blocks a sample, penumbrae and uneven light samples instead of every traced shadow ray. */
 enum { VT_O_CUT = 1, VT_O_AID = 2, VT_O_NO_INDIRECT = 4, VT_O_DIRECT_ONLY = 8, VT_O_LAYER = 16, VT_O_NO_CAPSULE = 32,
-       VT_O_NORMALS = 64, VT_O_NO_MIS = 128, VT_O_SPEC_STATIC = 256, VT_O_PACKET = 512, VT_O_REFINE_SHADOW = 1024 };
+       VT_O_NORMALS = 64, VT_O_NO_MIS = 128, VT_O_SPEC_STATIC = 256, VT_O_PACKET = 512, VT_O_REFINE_SHADOW = 1024,
+       VT_O_CACHE_WRITE = 2048, VT_O_CACHE_READ = 4096, VT_O_SHADOW_CACHE = 8192 };
 
 /* body kinds (gpu/scene_gpu.js:218-235 bodyOfPart) */
 enum { VT_BODY_INSTRUMENT = 0, VT_BODY_SCOPE = 1, VT_BODY_BOARD = 2, VT_BODY_FIXED = 3, VT_BODY_FIXTURE = 4 };

@@ -1487,6 +1487,33 @@ template <typename R> struct Shader {
     }
     return f * Le * (cosS * w / pdfW);
   }
+  // gpu/wgsl/shade.wgsl.js:135 lightEval: the sample's contribution before the shadow test and its shadow segment
+  bool light_eval(const Surf<R>& s, const V3<R>& n, const MatR<R>& M, const V3<R>& wo, R time, const V3<R>& u, bool mis, R nL,
+                  V3<R>& c, V3<R>& o, V3<R>& wi, R& tmax) const {
+    V3<R> lp, ln, la;
+    sample_emitter(u, time, lp, ln, la);
+    wi = lp - s.p;
+    R d2 = dot(wi, wi), dist = std::sqrt(d2);
+    wi = wi / dist;
+    R cosE = dot(-wi, ln);
+    if (cosE <= R(0)) return false;
+    R cosS = dot(n, wi);
+    if (cosS <= R(0) || dot(s.ng, wi) <= R(0)) return false;
+    V3<R> Le = emitted(ln, la, -wi);
+    if (maxc(Le) <= R(0)) return false;
+    V3<R> f = eval_bsdf(M, n, wi, wo);
+    if (maxc(f) <= R(0)) return false;
+    R pdfW = d2 / (cosE * R(tr.SU[3]));
+    R w = 1;
+    if (mis) {
+      R pb = pdf_bsdf(M, n, wo, wi);
+      w = nL * nL * pdfW * pdfW / (nL * nL * pdfW * pdfW + pb * pb);
+    }
+    c = f * Le * (cosS * w / pdfW);
+    o = offset_ray(s.p, s.ng, wi);
+    tmax = dist - R(2e-5);
+    return true;
+  }
   // gpu/wgsl/shade.wgsl.js:194-209 nodeWeights / nodeEfree / nodeLout
   V3<R> node_weights(const uint32_t* vi, const V3<R>& b) const {
     uint32_t slot = tr.su_u(18);
@@ -1546,13 +1573,37 @@ template <typename R> struct Shader {
     bool isStatic = (s.flags & VT_F_STATIC) != 0;
     bool mis = !isStatic && !(opts & VT_O_NO_MIS);
     uint32_t nl = std::min<uint32_t>(std::max<uint32_t>(nLight, 1u), 16u);
-    shadowTraced = false;
-    V3<R> L = direct_light(s, n, M, wo, time, ul, mis, R(nl));
-    for (uint32_t j = 1; j < nl; j++) {
-      V3<R> uj(kr(lightIndex + j, KL0, Sd.s[3]), kr(lightIndex + j, KL1, Sd.s[4]), kr(lightIndex + j, KL2, Sd.s[5]));
-      L = L + direct_light(s, n, M, wo, time, uj, mis, R(nl));
+    V3<R> L;
+    if (isStatic && (opts & VT_O_SHADOW_CACHE) && (opts & (VT_O_CACHE_WRITE | VT_O_CACHE_READ))) {
+      // shade.wgsl.js:270-301, the static-occlusion cache's branch: the static scene and the posed bodies are asked
+      // separately, and the shadow key bit marks a body blocking a sample, a penumbra or uneven light samples
+      uint32_t nvis = 0, nlit = 0;
+      R lmin = R(BIGD), lmax = 0;
+      bool dyn = false;
+      for (uint32_t j = 0; j < nl; j++) {
+        V3<R> uj = j == 0 ? ul : V3<R>(kr(lightIndex + j, KL0, Sd.s[3]), kr(lightIndex + j, KL1, Sd.s[4]), kr(lightIndex + j, KL2, Sd.s[5]));
+        V3<R> c, o, wi;
+        R tmax;
+        if (!light_eval(s, n, M, wo, time, uj, mis, R(nl), c, o, wi, tmax)) continue;
+        nlit++;
+        if (tr.trace(o, wi, R(0), tmax, time, true, 1u, 0u).tri != MISS) continue;
+        if (tr.trace(o, wi, R(0), tmax, time, true, 2u, tr.su_u(7)).tri != MISS) { dyn = true; continue; }
+        nvis++;
+        L = L + c;
+        R y = c.x * R(0.2126) + c.y * R(0.7152) + c.z * R(0.0722);
+        lmin = std::min(lmin, y);
+        lmax = std::max(lmax, y);
+      }
+      if (dyn || (nvis > 0 && nvis < nlit) || (nvis > 1 && lmax - lmin > R(0.2) * (lmax + lmin) * R(0.5))) key |= 0x20000u;
+    } else {
+      shadowTraced = false;
+      L = direct_light(s, n, M, wo, time, ul, mis, R(nl));
+      for (uint32_t j = 1; j < nl; j++) {
+        V3<R> uj(kr(lightIndex + j, KL0, Sd.s[3]), kr(lightIndex + j, KL1, Sd.s[4]), kr(lightIndex + j, KL2, Sd.s[5]));
+        L = L + direct_light(s, n, M, wo, time, uj, mis, R(nl));
+      }
+      if (shadowTraced) key |= 0x20000u;   // shade.wgsl.js:177 (no shadow culling: every sample that gets this far)
     }
-    if (shadowTraced) key |= 0x20000u;   // shade.wgsl.js:177 (no shadow culling: every sample that gets this far)
     L = L / R(nl);
     if (isStatic) {
       if (!(opts & (VT_O_NO_INDIRECT | VT_O_DIRECT_ONLY))) {

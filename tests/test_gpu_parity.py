@@ -217,6 +217,64 @@ def test_refinement_pass(inst_scene, inst_poses):
     r.destroy()
 
 
+def test_static_first_hit_cache_is_exact(inst_scene, inst_poses):
+    """gpu/renderer.js:941-956 hitCache and shadowCache: a twin camera's static first hits and their static occlusion
+    are traced once and kept; renders that read them (the instruments moved in between) equal renders without the
+    caches bit for bit (refinement included, with the refinement's shadow criterion off: the caches change which
+    pixels it picks, as they do in the reference)."""
+    r = TwinRenderer.create(inst_scene)
+    W, H = inst_scene["cameras"][0]["size"]
+    T = dome.instrument_poses(n_poses=3, n_tools=3, seed=5)
+
+    def render(cache):
+        out = np.zeros((H, W, 4), np.float32)
+        r.renderCamera(0, out=out, spp=2, lightSamples=2, seed=3, refine=2, refineShadows=False, hitCache=cache)
+        return out
+
+    for k in range(3):                     # k = 0 fills the cache, k = 1, 2 read it
+        # one pose change per k (a pose change also brings the node radiosity along, so both renders follow it)
+        r.set_pose_array(np.concatenate([A.identity_poses(1), T[k]]))
+        a = render(True)
+        b = render(False)
+        assert np.array_equal(a, b), (k, (a != b).sum())
+    # a new seed changes the key: the cache is traced again, and still exact
+    r.set_pose_array(np.concatenate([A.identity_poses(1), T[0]]))
+    a = np.zeros((H, W, 4), np.float32)
+    b = np.zeros_like(a)
+    r.renderCamera(0, out=a, spp=2, lightSamples=2, seed=4, hitCache=True)
+    r.renderCamera(0, out=b, spp=2, lightSamples=2, seed=4, hitCache=False)
+    assert np.array_equal(a, b)
+    r.destroy()
+
+
+def test_shadow_cache_refinement_matches_oracle(inst_scene, inst_poses):
+    """With the static-occlusion cache the refinement's shadow criterion is the reference's cached one (a posed body
+    blocks a sample, a penumbra, light samples more than 20 % apart): the refined pixels and the image against the
+    FP64 oracle restating that branch, on the frame that fills the caches and on one that reads them."""
+    r = TwinRenderer.create(inst_scene)
+    ref = O.Scene(inst_scene)
+    W, H = inst_scene["cameras"][0]["size"]
+    T = dome.instrument_poses(n_poses=2, n_tools=3, seed=5)
+    for k in range(2):
+        P = np.concatenate([A.identity_poses(1), T[k]])
+        r.set_pose_array(P)
+        ref.set_poses(P)
+        r.debugFlags(reset=True)
+        out = np.zeros((H, W, 4), np.float32)
+        q = r.renderCamera(0, out=out, spp=2, lightSamples=3, seed=3, refine=3, refineLightSamples=3, refineShadows=True)
+        f = r.debugFlags(reset=True)
+        assert q.options & A.OPTION_BITS["SHADOW_CACHE"]
+        st, slot = r.get_node_state()
+        ref.set_node_state(st, slot)
+        ref.set_eavg(r.scene_uniform()[8:11])
+        img64, dbg = ref.render(q, fp64=True, threads=8)
+        s = _radiance_stats(out, img64)
+        print(f"\nshadow cache, frame {k}: refined gpu {f['refined']} (shadow {f['refinedShadow']}) oracle {int(dbg[2])} ({int(dbg[4])}); {s}")
+        assert abs(f["refined"] - int(dbg[2])) <= 0.01 * int(dbg[2]) + 6
+        assert s["median"] < 1e-5 and s["within_1e-4"] > 0.95
+    r.destroy()
+
+
 def test_sensor_expose_bit_exact():
     W, H = 320, 240
     rng = np.random.default_rng(8)

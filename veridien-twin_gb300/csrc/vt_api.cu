@@ -99,7 +99,7 @@ vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx**
 vt_status vt_destroy(vt_ctx* ctx) {
   if (!ctx) return VT_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); cudaFree(c.ri); cudaFree(c.isp_mem); }
+  for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); cudaFree(c.ri); cudaFree(c.isp_mem); cudaFree(c.hcache); cudaFree(c.scache); }
   cudaFree(ctx->d_nodes); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
   cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave); cudaFree(ctx->tc.mem);
   cudaFree(ctx->batch.su); cudaFree(ctx->batch.cull); cudaFree(ctx->batch.ctr); cudaFree(ctx->batch.sensor); cudaFree(ctx->batch.mem);
@@ -291,6 +291,53 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   }
   vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, paths, std::max(cp.n_light, cp2.n_light), n_pix, ctx->d_work);
   wb.rcount = ctx->d_work + 12;
+  if (q->options & (VT_O_CACHE_WRITE | VT_O_CACHE_READ)) {
+    // the cache stays valid while what decides a camera ray's static hit holds (its time does not: the static
+    // BVH does not move)
+    auto& C = ctx->cams[q->camera];
+    std::vector<double> key = {double(q->seed), double(q->root), double(cp.tile_w), double(cp.tile_h), double(n_pix), c.fx, c.fy, c.cx, c.cy,
+                               c.alpha, c.k[0], c.k[1], c.k[2], c.k[3]};
+    key.insert(key.end(), c.T_D_C, c.T_D_C + 16);
+    const uint32_t cap = std::max(1u, std::min(cp.spp, 64u) + cp.refine);
+    if (key != C.hc_key || cap > C.hc_cap) {
+      VT_CK(cudaStreamSynchronize(ctx->stream));
+      cudaFree(C.hcache);
+      cudaFree(C.scache);
+      C.hcache = nullptr;
+      C.scache = nullptr;
+      C.hc_cap = 0;
+      C.hc_key.clear();
+      C.sc_key.clear();
+      if (cudaMalloc(&C.hcache, size_t(n_pix) * cap * 16) != cudaSuccess) { cudaGetLastError(); C.hcache = nullptr; }
+      else {
+        VT_CK(cudaMemsetAsync(C.hcache, 0, size_t(n_pix) * cap * 16, ctx->stream));
+        C.hc_cap = cap;
+        C.hc_stride = n_pix;
+        C.hc_key = key;
+      }
+    }
+    if (C.hcache) { wb.hcache = C.hcache; wb.hc_stride = C.hc_stride; wb.hc_cap = C.hc_cap; }
+    // the static-occlusion cache (twin shading of static first hits): also keyed on the emitter body's pose over the
+    // exposure and both passes' light-sample counts (gpu/renderer.js:952-956)
+    if (C.hcache && (q->options & VT_O_SHADOW_CACHE) && q->mode == VT_SHADE_TWIN) {
+      std::vector<double> sk = C.hc_key;
+      sk.push_back(double(cp.n_light));
+      sk.push_back(double(cp2.n_light));
+      sk.push_back(double(C.hc_cap));
+      const int sc = ctx->S.scope_index;
+      if (sc >= 0 && size_t(sc) < ctx->inst.size() && ctx->inst[sc].valid) {
+        const vt::InstPose& I = ctx->inst[sc];
+        sk.insert(sk.end(), I.q0, I.q0 + 4); sk.insert(sk.end(), I.q1, I.q1 + 4);
+        sk.insert(sk.end(), I.p0, I.p0 + 3); sk.insert(sk.end(), I.p1, I.p1 + 3);
+      }
+      if (!C.scache || sk != C.sc_key) {
+        if (!C.scache && cudaMalloc(&C.scache, size_t(C.hc_stride) * C.hc_cap * 4) != cudaSuccess) { cudaGetLastError(); C.scache = nullptr; }
+        if (C.scache) VT_CK(cudaMemsetAsync(C.scache, 0, size_t(C.hc_stride) * C.hc_cap * 4, ctx->stream));
+        C.sc_key = C.scache ? sk : std::vector<double>();
+      }
+      if (C.scache) wb.scache = C.scache;
+    }
+  }
   vtk::KernelTimer timer{ctx->kev.data(), ctx->kkind.data(), int(ctx->kev.size() / 2), 0};
   if (ctx->kprof) wb.stats = reinterpret_cast<unsigned long long*>(ctx->d_work + 16);
   VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));

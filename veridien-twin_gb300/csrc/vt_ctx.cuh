@@ -43,6 +43,13 @@ struct vt_ctx {
     vtk::IspBufs isp{};
     size_t isp_lev = 0;   // glare-level pixels the buffers hold
     bool processed = false;
+    // static first-hit cache (VT_O_CACHE_*): entries, sub-samples held, and the key they were traced under
+    float4* hcache = nullptr;
+    uint32_t hc_cap = 0, hc_stride = 0;
+    std::vector<double> hc_key;
+    // static-occlusion cache (VT_O_SHADOW_CACHE), indexed like the first-hit cache, and its key
+    uint32_t* scache = nullptr;
+    std::vector<double> sc_key;
   };
   std::vector<Cam> cams;
   // scratch for ray queries and the solver (grown on demand)

@@ -164,19 +164,39 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(con
     }
     active = false;
   };
+  // static first-hit cache (camera rays of a fixed camera, gpu/wgsl/kernels.wgsl.js:82 staticFirstHit): a cached
+  // entry replaces the static phase (the instance phases then start from it, exactly as after tracing it); an empty
+  // one is filled when the static phase ends
+  uint32_t ci = MISS;
   auto start = [&](uint32_t idx) {
     p = wb.q_in[idx];
     const float4 o4 = wb.o[p], d4 = wb.d[p];
     o = xyz(o4); d = xyz(d4); tt = o4.w;
-    skip = wb.meta[p].w == 1 ? cp.skip : 0u;
+    const uint4 meta = wb.meta[p];
+    skip = meta.w == 1 ? cp.skip : 0u;
     Sl = path_scene<VAR>(S, wb, p);
     st.best = Hit{BIG, 0.0f, 0.0f, MISS, MISS};
-    active = trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, -1);
+    int from = -1;
+    ci = MISS;
+    if (VAR == WAVE_PLAIN && wb.hcache && meta.w == 1 && meta.y < wb.hc_cap) {
+      ci = meta.y * wb.hc_stride + meta.x;
+      const float4 h = wb.hcache[ci];
+      if (h.x > 0.0f) { st.best = Hit{h.x, h.y, h.z, __float_as_uint(h.w), MISS}; from = 0; ci = MISS; }
+    }
+    active = trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, from);
+    if (ci != MISS && st.k != -1) {   // no static phase to wait for: the static hit is none
+      wb.hcache[ci] = make_float4(BIG, 0.0f, 0.0f, __uint_as_float(MISS));
+      ci = MISS;
+    }
     if (!active) { active = true; finish(); }
   };
   while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
     if (!active) continue;
     const int r = trace_visit<false>(Sl, 0.0f, st, stk);
+    if (r != 0 && VAR == WAVE_PLAIN && ci != MISS && st.k == -1) {
+      wb.hcache[ci] = make_float4(st.best.t, st.best.u, st.best.v, __uint_as_float(st.best.tri));
+      ci = MISS;
+    }
     if (r != 0 && !trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, st.k + 1)) finish();
   }
 }
@@ -246,21 +266,36 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S0, const
         const float sh0 = b == 1 ? u01(pcg(hs + 3u)) : bounce_shift(hs, b, 0);
         const float sh1 = b == 1 ? u01(pcg(hs + 4u)) : bounce_shift(hs, b, 1);
         const float sh2 = b == 1 ? u01(pcg(hs + 5u)) : bounce_shift(hs, b, 2);
-        // nL emitter samples: the unshadowed contribution and the shadow segment of each (shade.wgsl.js:135 lightEval)
+        // nL emitter samples: the unshadowed contribution and the shadow segment of each (shade.wgsl.js:135 lightEval).
+        // The record's flag: 0 no contribution, 1 trace it (static scene and posed bodies); with the static-occlusion
+        // cache (a static first hit, shade.wgsl.js:270-301): 4 trace the static scene (its answer fills the cache) then
+        // the bodies, 5 the static scene is known clear (trace the bodies), 6 the static scene is known to hide it
+        const bool cached = MODE == VT_SHADE_TWIN && VAR == WAVE_PLAIN && b == 1 && is_static && wb.scache && i < wb.hc_cap;
+        uint32_t word = 0;
+        if (cached) word = wb.scache[i * wb.hc_stride + meta.x];
         float4* rec = wb.sh + size_t(p) * nl * 3;
+        uint32_t nlit = 0;
         for (uint32_t j = 0; j < nl; j++) {
           const float3 u = f3(kr(i * nl + j, KL0, sh0), kr(i * nl + j, KL1, sh1), kr(i * nl + j, KL2, sh2));
           float3 c, so, wi;
           float tmax;
           const bool ok = light_sample(S, s, n, M, wo, tt, u, mis, float(nl), c, so, wi, tmax);
+          float flag = ok ? 1.0f : 0.0f;
+          if (cached && ok) flag = (word >> 31) ? (((word >> j) & 1u) ? 6.0f : 5.0f) : 4.0f;
           rec[3 * j] = make_float4(so.x, so.y, so.z, tmax);
-          rec[3 * j + 1] = make_float4(wi.x, wi.y, wi.z, ok ? 1.0f : 0.0f);
+          rec[3 * j + 1] = make_float4(wi.x, wi.y, wi.z, flag);
           rec[3 * j + 2] = make_float4(c.x, c.y, c.z, 0.0f);
-          shadow |= ok;
+          nlit += ok ? 1u : 0u;
+          shadow |= ok && flag != 6.0f;
+        }
+        if (cached) {
+          rec[2].w = __uint_as_float(nlit);   // the shadow kernel's penumbra test needs the lit count
+          if (!(word >> 31) && nlit == 0) wb.scache[i * wb.hc_stride + meta.x] = 0x80000000u;
         }
         if (shadow) wb.nee[p] = make_float4(thr.x, thr.y, thr.z, tt);
-        // key bit 0x20000: a first-hit light sample needs its shadow ray (shade.wgsl.js:177; no shadow culling here)
-        if (b == 1 && shadow) L4.w = __uint_as_float(__float_as_uint(L4.w) | 0x20000u);
+        // key bit 0x20000: a first-hit light sample needs its shadow ray (shade.wgsl.js:177, no shadow culling); with
+        // the static-occlusion cache the shadow kernel decides it (a body blocks a sample, a penumbra, uneven samples)
+        if (b == 1 && shadow && !cached) L4.w = __uint_as_float(__float_as_uint(L4.w) | 0x20000u);
         bool bounce;
         if (MODE == VT_SHADE_TWIN) {
           bounce = !is_static;
@@ -318,16 +353,31 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
   uint64_t have = 0ull, bits = 0ull;
   bool active = false, exhausted = false;
   const float4* rec = nullptr;
+  // the static-occlusion cache's bookkeeping of the current path (shade.wgsl.js:270-301): lit and visible samples,
+  // their luminance range, a posed body blocking one, and the occlusion word to store
+  bool cm = false, dyn = false, fill = false;
+  uint32_t nvis = 0, nlit = 0, word = 0, ci = 0;
+  float lmin = BIG, lmax = 0.0f;
+  auto visible = [&](uint32_t jj) {
+    const float3 c = xyz(rec[3 * jj + 2]);
+    Ld = Ld + c;
+    if (cm) {
+      nvis++;
+      const float y = lum(c);
+      lmin = fminf(lmin, y);
+      lmax = fmaxf(lmax, y);
+    }
+  };
   // the next light sample of the path with a valid record at or after j, set up as a ray; false when none is left
   auto next_sample = [&]() -> bool {
     for (; j < nl; j++) {
       const float4 a = rec[3 * j], w = rec[3 * j + 1];
-      if (w.w == 0.0f) continue;
+      if (w.w == 0.0f || w.w == 6.0f) continue;   // no contribution, or hidden by the static scene (cached)
       o = xyz(a); d = xyz(w);
       st.best = Hit{a.w, 0.0f, 0.0f, MISS, MISS};
-      if (trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, -1)) return true;
+      if (trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, w.w == 5.0f ? 0 : -1)) return true;
       // nothing to traverse: the segment is unoccluded
-      Ld = Ld + xyz(rec[3 * j + 2]);
+      visible(j);
       if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, o, d, a.w, skip0, have | bits);
     }
     return false;
@@ -335,7 +385,12 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
   auto finish_path = [&]() {
     const float4 L = wb.L[p];
     const float3 v = xyz(L) + xyz(nee) * (Ld / float(nl));
-    wb.L[p] = make_float4(v.x, v.y, v.z, L.w);
+    uint32_t key = __float_as_uint(L.w);
+    if (cm) {
+      if (fill) wb.scache[ci] = word | 0x80000000u;
+      if (dyn || (nvis > 0u && nvis < nlit) || (nvis > 1u && lmax - lmin > 0.2f * (lmax + lmin) * 0.5f)) key |= 0x20000u;
+    }
+    wb.L[p] = make_float4(v.x, v.y, v.z, __uint_as_float(key));
     if (VAR == WAVE_SHARED && bits) wb.bc.dirty[p] = have | bits;
     active = false;
   };
@@ -348,6 +403,23 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
     j = 0;
     bits = 0ull;
     if (VAR == WAVE_SHARED) have = wb.bc.dirty[p];
+    cm = fill = dyn = false;
+    if (VAR == WAVE_PLAIN && wb.scache) {
+      for (uint32_t q = 0; q < nl; q++) {
+        const float f = rec[3 * q + 1].w;
+        cm |= f >= 4.0f;
+        fill |= f == 4.0f;
+      }
+      if (cm) {
+        const uint4 meta = wb.meta[p];
+        ci = meta.y * wb.hc_stride + meta.x;
+        nlit = __float_as_uint(rec[2].w);
+        nvis = 0;
+        word = 0;
+        lmin = BIG;
+        lmax = 0.0f;
+      }
+    }
     active = true;
     if (!next_sample()) finish_path();
   };
@@ -358,8 +430,11 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
     if (r == 1) done = !trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, st.k + 1);
     if (!done) continue;
     if (st.best.tri == MISS) {
-      Ld = Ld + xyz(rec[3 * j + 2]);
+      visible(j);
       if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, o, d, rec[3 * j].w, skip0, have | bits);
+    } else if (cm) {
+      if (st.k < 0) word |= 1u << j;   // the static scene hides it
+      else dyn = true;                 // a posed body does
     }
     j++;
     if (!next_sample()) finish_path();
@@ -489,6 +564,9 @@ WaveBufs wave_carve(void* base, uint32_t paths, uint32_t n_light, uint32_t n_pix
   w.acc2 = reinterpret_cast<float4*>(take(size_t(n_pix) * 16));
   w.rlist = reinterpret_cast<uint32_t*>(take(size_t(n_pix) * 4));
   w.rcount = nullptr;
+  w.hcache = nullptr;
+  w.scache = nullptr;
+  w.hc_stride = w.hc_cap = 0;
   w.counts = counts;
   w.fetch = counts + 3;
   return w;

@@ -54,6 +54,13 @@ struct WaveBufs {
   uint32_t* count_out;
   uint32_t* count_sh;
   uint32_t* fetch;  // next queue entry to take, for the persistent traversal kernels (zeroed before each)
+  // static first-hit cache of a fixed camera (null: off): per (sub-sample i, pixel id) at i * hc_stride + id the
+  // closest hit in the static BVH (t, u, v, triangle bits), t = 0 while empty
+  float4* hcache;
+  uint32_t hc_stride, hc_cap;   // pixel ids per sub-sample, sub-samples held
+  // static-occlusion cache of a fixed camera with a still emitter (null: off), indexed like hcache: per first-hit
+  // light sample j bit j set when the static scene hides it, bit 31 once the word is valid
+  uint32_t* scache;
   unsigned long long* stats;   // optional: [0] rays of the closest-hit kernels, [1] paths of the any-hit kernels
   BatchCull bc;
 };

@@ -19,7 +19,8 @@ VT_MAX_INST = 24
 VT_MISS = 0xFFFFFFFF
 BODY_KIND = {"instrument": 0, "scope": 1, "board": 2, "fixed": 3, "fixture": 4}
 OPTION_BITS = {"CUT": 1, "AID": 2, "NO_INDIRECT": 4, "DIRECT_ONLY": 8, "LAYER": 16, "NO_CAPSULE": 32, "NORMALS": 64,
-               "NO_MIS": 128, "SPEC_STATIC": 256, "PACKET": 512, "REFINE_SHADOW": 1024}
+               "NO_MIS": 128, "SPEC_STATIC": 256, "PACKET": 512, "REFINE_SHADOW": 1024, "CACHE_WRITE": 2048, "CACHE_READ": 4096,
+               "SHADOW_CACHE": 8192}
 
 f32p = C.POINTER(C.c_float)
 u32p = C.POINTER(C.c_uint32)

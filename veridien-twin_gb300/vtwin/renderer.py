@@ -205,13 +205,19 @@ class TwinRenderer:
     # ------------------------------------------------------------------------------------------- rendering
     def request(self, name, spp=None, lightSamples=None, seed=0, options=0, mode=A.VT_SHADE_TWIN, max_depth=2,
                 shutter=(0.0, 1.0), scale=1.0, root=0, frame=None, refine=None, refineLightSamples=None,
-                refineShadows=None) -> A.vt_render_req:
+                refineShadows=None, hitCache=None, shadowCache=None, exactShadows=False) -> A.vt_render_req:
         """gpu/renderer.js:935 _submitCamera's options: pass 1 (spp sub-samples, lightSamples each) and the refinement
         pass (refine more sub-samples on edges, posed bodies and, with refineShadows, pixels whose shadow rays were
         traced; refineLightSamples each)."""
         opts = int(options)
         if refineShadows if refineShadows is not None else self.opts.get("refineShadows", True):
             opts |= A.OPTION_BITS["REFINE_SHADOW"]
+        # gpu/renderer.js:944 the static first-hit cache of the twin's camera feeds (exact; the library keeps its key)
+        if int(mode) == A.VT_SHADE_TWIN and (hitCache if hitCache is not None else self.opts.get("hitCache", True)):
+            opts |= A.OPTION_BITS["CACHE_WRITE"]
+            # :952 the static-occlusion cache, unless exact shadows are asked for
+            if (shadowCache if shadowCache is not None else self.opts.get("shadowCache", True)) and not exactShadows:
+                opts |= A.OPTION_BITS["SHADOW_CACHE"]
         q = A.vt_render_req(camera=self._cam(name), spp=int(spp if spp is not None else self.opts["spp"]),
                             light_samples=int(lightSamples if lightSamples is not None else self.opts["lightSamples"]),
                             seed=int(seed), options=opts, mode=int(mode), max_depth=int(max_depth), root=int(root),
