@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_gen_pairs_kernel(const CamP
   }
 }
 
-template <int VAR>
+// HC: the static first-hit cache is on (compiled separately, so the plain kernel keeps its registers)
+template <int VAR, bool HC = false>
 __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(const Scene S, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_in;
   if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats, (unsigned long long)n);
@@ -178,13 +179,13 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(con
     st.best = Hit{BIG, 0.0f, 0.0f, MISS, MISS};
     int from = -1;
     ci = MISS;
-    if (VAR == WAVE_PLAIN && wb.hcache && meta.w == 1 && meta.y < wb.hc_cap) {
+    if (HC && VAR == WAVE_PLAIN && meta.w == 1 && meta.y < wb.hc_cap) {
       ci = meta.y * wb.hc_stride + meta.x;
       const float4 h = wb.hcache[ci];
       if (h.x > 0.0f) { st.best = Hit{h.x, h.y, h.z, __float_as_uint(h.w), MISS}; from = 0; ci = MISS; }
     }
     active = trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, from);
-    if (ci != MISS && st.k != -1) {   // no static phase to wait for: the static hit is none
+    if (HC && ci != MISS && st.k != -1) {   // no static phase to wait for: the static hit is none
       wb.hcache[ci] = make_float4(BIG, 0.0f, 0.0f, __uint_as_float(MISS));
       ci = MISS;
     }
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(con
   while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
     if (!active) continue;
     const int r = trace_visit<false>(Sl, 0.0f, st, stk);
-    if (r != 0 && VAR == WAVE_PLAIN && ci != MISS && st.k == -1) {
+    if (HC && r != 0 && VAR == WAVE_PLAIN && ci != MISS && st.k == -1) {
       wb.hcache[ci] = make_float4(st.best.t, st.best.u, st.best.v, __uint_as_float(st.best.tri));
       ci = MISS;
     }
@@ -334,7 +335,8 @@ __global__ void __launch_bounds__(WAVE_THREADS) wave_shade(const Scene S0, const
 
 // any-hit of every queued path's light samples in sample order on persistent lanes; a lane moves to the path's next
 // sample when one finishes, and to a new path when the last one does
-template <int VAR>
+// SC: the static-occlusion cache is on (compiled separately, so the plain kernel keeps its registers)
+template <int VAR, bool SC = false>
 __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(const Scene S0, const CamParams cp, WaveBufs wb) {
   const uint32_t n = *wb.count_sh;
   if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats + 1, (unsigned long long)n);
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
   auto visible = [&](uint32_t jj) {
     const float3 c = xyz(rec[3 * jj + 2]);
     Ld = Ld + c;
-    if (cm) {
+    if (SC && cm) {
       nvis++;
       const float y = lum(c);
       lmin = fminf(lmin, y);
@@ -372,10 +374,10 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
   auto next_sample = [&]() -> bool {
     for (; j < nl; j++) {
       const float4 a = rec[3 * j], w = rec[3 * j + 1];
-      if (w.w == 0.0f || w.w == 6.0f) continue;   // no contribution, or hidden by the static scene (cached)
+      if (w.w == 0.0f || (SC && w.w == 6.0f)) continue;   // no contribution, or hidden by the static scene (cached)
       o = xyz(a); d = xyz(w);
       st.best = Hit{a.w, 0.0f, 0.0f, MISS, MISS};
-      if (trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, w.w == 5.0f ? 0 : -1)) return true;
+      if (trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, SC && w.w == 5.0f ? 0 : -1)) return true;
       // nothing to traverse: the segment is unoccluded
       visible(j);
       if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, o, d, a.w, skip0, have | bits);
@@ -386,7 +388,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
     const float4 L = wb.L[p];
     const float3 v = xyz(L) + xyz(nee) * (Ld / float(nl));
     uint32_t key = __float_as_uint(L.w);
-    if (cm) {
+    if (SC && cm) {
       if (fill) wb.scache[ci] = word | 0x80000000u;
       if (dyn || (nvis > 0u && nvis < nlit) || (nvis > 1u && lmax - lmin > 0.2f * (lmax + lmin) * 0.5f)) key |= 0x20000u;
     }
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
     bits = 0ull;
     if (VAR == WAVE_SHARED) have = wb.bc.dirty[p];
     cm = fill = dyn = false;
-    if (VAR == WAVE_PLAIN && wb.scache) {
+    if (SC && VAR == WAVE_PLAIN) {
       for (uint32_t q = 0; q < nl; q++) {
         const float f = rec[3 * q + 1].w;
         cm |= f >= 4.0f;
@@ -432,7 +434,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
     if (st.best.tri == MISS) {
       visible(j);
       if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, o, d, rec[3 * j].w, skip0, have | bits);
-    } else if (cm) {
+    } else if (SC && cm) {
       if (st.k < 0) word |= 1u << j;   // the static scene hides it
       else dyn = true;                 // a posed body does
     }
@@ -588,7 +590,8 @@ void bounce_kernels(const Scene& S, const CamParams& cp, const WaveBufs& w, int 
   cudaMemsetAsync(w.fetch, 0, 4, st);
   {
     TimedLaunch tl(timer, st, 0);
-    wave_extend<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+    if (VAR == WAVE_PLAIN && w.hcache) wave_extend<VAR, true><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+    else wave_extend<VAR, false><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
   }
   {
     TimedLaunch tl(timer, st, 1);
@@ -598,7 +601,8 @@ void bounce_kernels(const Scene& S, const CamParams& cp, const WaveBufs& w, int 
   cudaMemsetAsync(w.fetch, 0, 4, st);
   {
     TimedLaunch tl(timer, st, 2);
-    wave_shadow<VAR><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+    if (VAR == WAVE_PLAIN && w.scache) wave_shadow<VAR, true><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
+    else wave_shadow<VAR, false><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, w);
   }
 }
 
@@ -623,7 +627,7 @@ void wave_bounces(const Scene& S, const CamParams& cp, WaveBufs wb, int var, int
 
 void launch_wave_extend(const Scene& S, const CamParams& cp, const WaveBufs& wb, int blocks, cudaStream_t st) {
   cudaMemsetAsync(wb.fetch, 0, 4, st);
-  wave_extend<WAVE_PLAIN><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, wb);
+  wave_extend<WAVE_PLAIN, false><<<blocks, WAVE_THREADS, 0, st>>>(S, cp, wb);
 }
 
 void launch_wave_gen(const CamParams& cp, WaveBufs wb, uint32_t i0, uint32_t n_i, uint32_t n_pix, int blocks, cudaStream_t st) {
@@ -683,9 +687,9 @@ void wave_render(const Scene& S, const CamParams& cp, WaveBufs wb, uint32_t wave
 
 int wave_blocks_per_sm() {
   int a = 0, b = 0, c = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, wave_extend<WAVE_PLAIN>, WAVE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, wave_extend<WAVE_PLAIN, false>, WAVE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_shade<VT_SHADE_PATH, WAVE_PLAIN>, WAVE_THREADS, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, wave_shadow<WAVE_PLAIN>, WAVE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, wave_shadow<WAVE_PLAIN, false>, WAVE_THREADS, 0);
   return std::max(1, std::max(a, std::max(b, c)));
 }
 
