@@ -252,6 +252,21 @@ vt_status vt_set_relative_illumination(vt_ctx* ctx, uint32_t camera, const float
                                        const double* vig, uint32_t n_vig);
 vt_status vt_get_relative_illumination(vt_ctx* ctx, uint32_t camera, float* ri);
 
+/* gpu/renderer.js:986 renderFrame({cameras, sensor}): every listed camera rendered with `render` (its camera field
+ * ignored; in twin mode the node radiosity is brought up to the poses first), then, when `sensors` is set, each
+ * camera's sensor chain (vt_sensor_frame) with its uniform; everything queued on the context's stream with one
+ * synchronisation at the end. stats (n_cameras x 4, may be NULL) receives each camera's AE / AWB statistics; ms the
+ * frame's device time. Radiance, raw and 8-bit images stay on the device for vt_readback. */
+typedef struct {
+  const uint32_t* cameras;
+  uint32_t n_cameras;
+  vt_render_req render;
+  const vt_sensor_uniform* sensors;   /* n_cameras uniforms, or NULL: no sensor stage */
+  uint32_t* stats;
+  double ms;                          /* out */
+} vt_frame_req;
+vt_status vt_render_frame(vt_ctx* ctx, vt_frame_req* frame);
+
 /* -------------------------------------------------------------------------------------- batched rendering */
 
 /* Many cameras x many kinematic poses of one scene in one call: the twin's renderFrame (gpu/renderer.js:986) over

@@ -92,3 +92,33 @@ def test_auto_exposure_converges(rendered):
     # a manual exposure holds
     r.set_exposure(0, 1e-3)
     assert r.exposureOf(0)["time_s"] == 1e-3 and not r.exposureOf(0)["auto"]
+
+
+def test_render_frame_matches_per_camera_calls():
+    """renderFrame queues every camera's render and sensor chain in one library call (vt_render_frame) with one
+    synchronisation; the images, statistics and the AE / AWB state it leaves must equal those of renderCamera +
+    sensor called camera by camera (gpu/renderer.js:986)."""
+    sc = dome.make_dome_scene(seed=1, width=97, height=63, level=4, with_instruments=2)
+    sc["cameras"] = dome.batched_cameras(seed=3, n=3, width=80, height=56)
+    T = dome.instrument_poses(n_poses=2, n_tools=2, seed=11)
+    a, b = TwinRenderer.create(sc), TwinRenderer.create(sc)
+    try:
+        for k in range(2):
+            for r in (a, b):
+                r.set_pose_array(np.concatenate([A.identity_poses(1), T[k]]))
+            fr = a.renderFrame(sensor=True, spp=2, lightSamples=2, seed=k)
+            names = list(a.cameras)
+            for c in names:
+                b.renderCamera(c, spp=2, lightSamples=2, seed=k)
+            st = {c: b.sensor(c) for c in names}
+            b.frame += 1
+            assert fr["ms"] > 0 and len(names) == 3
+            for c in names:
+                assert np.array_equal(a.readback(c, "linear"), b.readback(c, "linear")), (k, c)
+                assert np.array_equal(a.readback(c, "rgba8"), b.readback(c, "rgba8")), (k, c)
+                assert np.array_equal(fr[c]["stats"], st[c]["stats"]), (k, c)
+                assert a.exposureOf(c) == b.exposureOf(c)
+                assert a._sens[a._cam(c)]["awb"] == b._sens[b._cam(c)]["awb"]
+    finally:
+        a.destroy()
+        b.destroy()

@@ -118,6 +118,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   if (ctx->ev3) cudaEventDestroy(ctx->ev3);
   for (cudaEvent_t e : ctx->nev)
     if (e) cudaEventDestroy(e);
+  if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -258,7 +259,8 @@ vt_status vt_project(vt_ctx* ctx, uint32_t camera, const double* pts, uint32_t n
   return VT_OK;
 }
 
-vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba) {
+// one camera's render; sync = false leaves it queued on the context's stream (vt_render_frame)
+static vt_status render_impl(vt_ctx* ctx, const vt_render_req* q, float* out_rgba, bool sync) {
   if (!ctx || !q) return VT_ERR_ARG;
   if (q->camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(q->camera));
   if (q->root >= ctx->S.node_count) return fail(ctx, VT_ERR_ARG, "render: root out of range");
@@ -346,6 +348,7 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   VT_CK(cudaGetLastError());
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   ctx->cams[q->camera].rendered = true;
+  if (!sync) return VT_OK;
   if (out_rgba) {
     vt_status s = from_device(ctx, out_rgba, ctx->cams[q->camera].radiance, size_t(c.width) * c.height * 16);
     if (s != VT_OK) return s;
@@ -369,6 +372,8 @@ vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba)
   }
   return VT_OK;
 }
+
+vt_status vt_render_camera(vt_ctx* ctx, const vt_render_req* q, float* out_rgba) { return render_impl(ctx, q, out_rgba, true); }
 
 vt_status vt_kernel_profile(vt_ctx* ctx, int enable, int reset) {
   if (!ctx) return VT_ERR_ARG;
@@ -483,6 +488,47 @@ vt_status vt_sensor_camera(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform
   return VT_OK;
 }
 
+static vt_status sensor_impl(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, uint32_t* stats, bool sync);
+
+vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, uint32_t stats[4]) {
+  return sensor_impl(ctx, camera, su, stats, true);
+}
+
+vt_status vt_render_frame(vt_ctx* ctx, vt_frame_req* f) {
+  if (!ctx || !f || !f->cameras || !f->n_cameras) return VT_ERR_ARG;
+  for (uint32_t k = 0; k < f->n_cameras; k++)
+    if (f->cameras[k] >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(f->cameras[k]));
+  if (f->stats && f->sensors) {   // pinned host words for the statistics copies that stay queued until the end
+    const size_t need = size_t(f->n_cameras) * 16;
+    if (ctx->h_stats_bytes < need) {
+      if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+      ctx->h_stats = nullptr;
+      ctx->h_stats_bytes = 0;
+      if (cudaMallocHost(&ctx->h_stats, need) != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "frame: pinned statistics"); }
+      ctx->h_stats_bytes = need;
+    }
+  }
+  VT_CK(cudaEventRecord(ctx->ev2, ctx->stream));
+  for (uint32_t k = 0; k < f->n_cameras; k++) {
+    vt_render_req q = f->render;
+    q.camera = f->cameras[k];
+    vt_status s = render_impl(ctx, &q, nullptr, false);
+    if (s != VT_OK) return s;
+  }
+  if (f->sensors)
+    for (uint32_t k = 0; k < f->n_cameras; k++) {
+      vt_status s = sensor_impl(ctx, f->cameras[k], &f->sensors[k], f->stats ? static_cast<uint32_t*>(ctx->h_stats) + 4 * k : nullptr, false);
+      if (s != VT_OK) return s;
+    }
+  VT_CK(cudaEventRecord(ctx->ev3, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev2, ctx->ev3);
+  f->ms = ms;
+  if (f->stats && f->sensors) std::memcpy(f->stats, ctx->h_stats, size_t(f->n_cameras) * 16);
+  return VT_OK;
+}
+
 vt_status vt_set_relative_illumination(vt_ctx* ctx, uint32_t camera, const float* ri, double pupil_exponent, const double* vig_theta_deg,
                                        const double* vig, uint32_t n_vig) {
   if (!ctx) return VT_ERR_ARG;
@@ -511,7 +557,8 @@ vt_status vt_get_relative_illumination(vt_ctx* ctx, uint32_t camera, float* ri) 
   return VT_OK;
 }
 
-vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, uint32_t stats[4]) {
+// the sensor chain of one camera; sync = false queues it and an asynchronous copy of its statistics into stats_async
+static vt_status sensor_impl(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform* su, uint32_t* stats, bool sync) {
   if (!ctx || !su) return VT_ERR_ARG;
   if (camera >= ctx->S.cams.size()) return fail(ctx, VT_ERR_UNKNOWN_CAMERA, "unknown camera " + std::to_string(camera));
   auto& C = ctx->cams[camera];
@@ -566,6 +613,12 @@ vt_status vt_sensor_frame(vt_ctx* ctx, uint32_t camera, const vt_sensor_uniform*
   vtk::launch_isp(sp, C.isp, ctx->stream);
   VT_CK(cudaGetLastError());
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if (!sync) {
+    if (stats) VT_CK(cudaMemcpyAsync(stats, C.isp.stats, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->tim.launches += 8;
+    C.exposed = C.processed = true;
+    return VT_OK;
+  }
   uint32_t st[4];
   VT_CK(cudaMemcpyAsync(st, C.isp.stats, 16, cudaMemcpyDeviceToHost, ctx->stream));
   VT_CK(cudaStreamSynchronize(ctx->stream));

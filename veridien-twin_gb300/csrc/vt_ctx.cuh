@@ -19,6 +19,8 @@ struct vt_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   cudaEvent_t nev[4] = {nullptr, nullptr, nullptr, nullptr};   // node radiosity: direct light, Jacobi steps
+  void* h_stats = nullptr;       // pinned host words for a frame's sensor statistics (vt_render_frame)
+  size_t h_stats_bytes = 0;
   std::string err;
   vt::Prepared S;
   std::vector<vt::InstPose> inst;

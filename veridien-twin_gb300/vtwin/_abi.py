@@ -93,6 +93,11 @@ class vt_sensor_uniform(C.Structure):
     _fields_ = [("words", C.c_uint32 * 64)]
 
 
+class vt_frame_req(C.Structure):
+    _fields_ = [("cameras", C.POINTER(C.c_uint32)), ("n_cameras", C.c_uint32), ("render", vt_render_req),
+                ("sensors", C.POINTER(vt_sensor_uniform)), ("stats", C.POINTER(C.c_uint32)), ("ms", C.c_double)]
+
+
 VT_BATCH_MAX_POSES = 64
 
 

@@ -31,6 +31,7 @@ SIGNATURES = {
     "vt_sensor_expose": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_sensor_uniform), C.c_void_p, C.c_void_p]),
     "vt_sensor_camera": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_float]),
     "vt_sensor_frame": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_void_p]),
+    "vt_render_frame": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_frame_req)]),
     "vt_set_relative_illumination": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_uint32]),
     "vt_get_relative_illumination": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_calib_setup": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_calib_desc), C.POINTER(A.vt_calib_info)]),

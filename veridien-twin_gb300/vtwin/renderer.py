@@ -239,15 +239,32 @@ class TwinRenderer:
     render_camera = renderCamera
 
     def renderFrame(self, cameras=None, sensor=False, sensorOpts=None, **o):
-        """gpu/renderer.js:986 renderFrame({cameras, sensor}): every listed camera, then its sensor stage."""
+        """gpu/renderer.js:986 renderFrame({cameras, sensor}): every listed camera, then its sensor stage, queued as
+        one call on the library's stream with one synchronisation (vt_render_frame); AE / AWB then take each camera's
+        statistics. Returns the frame's device time in ms under "ms" and, with a sensor, each camera's statistics."""
         names = cameras or list(self.cameras)
-        for n in names:
-            self.renderCamera(n, **o)
+        idx = [self._cam(n) for n in names]
+        q = self.request(idx[0], **o)
+        f = A.vt_frame_req()
+        cams = (C.c_uint32 * len(idx))(*idx)
+        f.cameras = C.cast(cams, C.POINTER(C.c_uint32))
+        f.n_cameras = len(idx)
+        f.render = q
+        sus, stats = None, None
         if sensor:
-            for n in names:
-                self.sensor(n, **(sensorOpts or {}))
+            so = sensorOpts or {}
+            sus = (A.vt_sensor_uniform * len(idx))(*[self._sensor_uniform(c, **so) for c in idx])
+            stats = np.zeros((len(idx), 4), np.uint32)
+            f.sensors = C.cast(sus, C.POINTER(A.vt_sensor_uniform))
+            f.stats = stats.ctypes.data_as(C.POINTER(C.c_uint32))
+        check(self.lib.vt_render_frame(self._ctx, C.byref(f)), self._ctx)
+        out = {n: {"linear": n} for n in names}
+        if sensor:
+            for k, (n, c) in enumerate(zip(names, idx)):
+                out[n].update(self._after_sensor(c, stats[k], sus[k]))
         self.frame += 1
-        return {n: {"linear": n} for n in names}
+        out["ms"] = float(f.ms)
+        return out
 
     render_frame = renderFrame
 
@@ -315,12 +332,9 @@ class TwinRenderer:
 
     exposure_of = exposureOf
 
-    def sensor(self, name, seed=0, frame=None, noise=True, exposure_s=None, gain=None, params=None):
-        """gpu/renderer.js:1141 sensor(name, {seed, frame, noise, exposure_s, gain, params}): the whole chain on the
-        camera's last radiance (optics with relative illumination, glare, expose, demosaic, white balance + CCM, noise
-        reduction, tone, YCbCr) into its raw, 8-bit RGB and YCbCr images; then the auto exposure and auto white
-        balance take this frame's statistics for the next (gpu/renderer.js:1117 _afterSensor)."""
-        c = self._cam(name)
+    def _sensor_uniform(self, c, seed=0, frame=None, noise=True, exposure_s=None, gain=None, params=None):
+        """The camera's sensor uniform for its next frame: AE / manual exposure, AWB gains (gpu/renderer.js:1141);
+        the relative-illumination map is set on first use."""
         w, h = self.scene["cameras"][c]["size"]
         st = self._sensor_state(c)
         base = self.sensor_p
@@ -329,7 +343,7 @@ class TwinRenderer:
             vv = np.ascontiguousarray(base["vignetting"], np.float64)
             check(self.lib.vt_set_relative_illumination(self._ctx, c, None, float(base["pupilExponent"]), _p(vt), _p(vv), len(vt)), self._ctx)
             st["ri"] = True
-        ex = self.exposureOf(name)
+        ex = self.exposureOf(c)
         p = {**base, **(params or {})}
         if p.get("awb") and st["awb"] is not None and not (params and "wb" in params):
             p["wb"] = [g * a for g, a in zip(p["wb"], st["awb"])]
@@ -339,15 +353,31 @@ class TwinRenderer:
         su.words[:] = [int(x) for x in sensor_mod.pack_sensor_uniform(
             p, w, h, frame=self.frame if frame is None else frame, seed=seed, exposure=ex["time_s"] if exposure_s is None else exposure_s,
             gain=ex["gain"] if gain is None else gain, cam_index=c)]
-        stats = np.zeros(4, np.uint32)
-        check(self.lib.vt_sensor_frame(self._ctx, c, C.byref(su), _p(stats)), self._ctx)
+        return su
+
+    def _after_sensor(self, c, stats, su):
+        """gpu/renderer.js:1117 _afterSensor: this frame's statistics drive the next frame's AE and AWB."""
+        w, h = self.scene["cameras"][c]["size"]
+        st = self._sensor_state(c)
         st["meanLuma"] = float(stats[0]) / (w * h * 255)
         st["meanRGB"] = [float(x) / (w * h * 1023) for x in stats[1:]]
         if not st["manual"]:
             st["ae"].update(st["meanLuma"])
-        if base.get("awb"):
-            st["awb"] = sensor_mod.update_awb(st["awb"], st["meanRGB"], base.get("awbDamping", 0.3))
-        return {"stats": stats, "meanLuma": st["meanLuma"], "meanRGB": st["meanRGB"], "uniform": np.array(su.words, np.uint32)}
+        if self.sensor_p.get("awb"):
+            st["awb"] = sensor_mod.update_awb(st["awb"], st["meanRGB"], self.sensor_p.get("awbDamping", 0.3))
+        return {"stats": np.array(stats, np.uint32), "meanLuma": st["meanLuma"], "meanRGB": st["meanRGB"],
+                "uniform": np.array(su.words, np.uint32)}
+
+    def sensor(self, name, seed=0, frame=None, noise=True, exposure_s=None, gain=None, params=None):
+        """gpu/renderer.js:1141 sensor(name, {seed, frame, noise, exposure_s, gain, params}): the whole chain on the
+        camera's last radiance (optics with relative illumination, glare, expose, demosaic, white balance + CCM, noise
+        reduction, tone, YCbCr) into its raw, 8-bit RGB and YCbCr images; then the auto exposure and auto white
+        balance take this frame's statistics for the next (gpu/renderer.js:1117 _afterSensor)."""
+        c = self._cam(name)
+        su = self._sensor_uniform(c, seed, frame, noise, exposure_s, gain, params)
+        stats = np.zeros(4, np.uint32)
+        check(self.lib.vt_sensor_frame(self._ctx, c, C.byref(su), _p(stats)), self._ctx)
+        return self._after_sensor(c, stats, su)
 
     def relative_illumination(self, name):
         c = self._cam(name)
