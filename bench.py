@@ -20,6 +20,7 @@ bounded sample of the same frame; the reference itself is JavaScript + WebGPU an
   python bench.py --case nodes                     the scene node radiosity on the level-5 and level-8 domes
   python bench.py --case sensor                    the camera sensor chain at 1280x720 and 1920x1200
   python bench.py --case twin[:LEVEL]              the reference's twin frame (3 x 1280x720, presets live / balanced / judge)
+  python bench.py --case lite[:LEVEL]              the lite_nodes raster frame (3 KB4 cameras + SCOPE, 1280x720 each)
 """
 import argparse
 import json
@@ -367,6 +368,8 @@ def run_case(spec):
         print(json.dumps({"case": spec, **sensor_bench(torch)}))
     elif kind == "twin":
         print(json.dumps({"case": spec, **twin_frame_bench(torch, level=int(a[0]) if a else 8)}))
+    elif kind == "lite":
+        print(json.dumps({"case": spec, **lite_frame_bench(torch, level=int(a[0]) if a else 7)}))
     elif kind == "calib":
         from vtwin.renderer import TwinRenderer
 
@@ -569,6 +572,48 @@ def twin_frame_bench(torch, device=0, level=8, frames=10, warmup=3):
                      "gather_build_ms": t_create, **preset}
         r.destroy()
     out["reference_m4_ms"] = {"live": 45, "balanced": 84, "judge": "190-245"}
+    return out
+
+
+def lite_frame_bench(torch, device=0, level=7, frames=12, warmup=3):
+    """The lite_nodes raster frame (lite_nodes/renderer.js:844 renderCamera + :892 sensor): three 1280x720 KB4 cameras
+    and the 1280x720 SCOPE, 4x MSAA raster with per-vertex KB4, 4 sector shadow maps (2048^2), 24 / 96 emitter
+    samples per fragment, node irradiance per vertex, on the scope-scale dome (radius 0.35 m; level 7: 3 mm nodes)
+    with six 2.5 mm instruments moving every frame and the scope moving every fourth frame (the static casters' maps
+    re-rendered then). Wall time per frame (every camera call synchronises) and the device time of each pass."""
+    from vtwin import dome
+    from vtwin.lite import LiteNodesRenderer
+
+    sc = dome.make_scope_scene(seed=2, level=level, n_tools=6, width=1280, height=720)
+    poses = dome.scope_poses(frames + warmup, 6, seed=21)
+    t0 = time.perf_counter()
+    r = LiteNodesRenderer.create(sc, device=device)
+    load_ms = (time.perf_counter() - t0) * 1e3
+    wall, cam_ms, dyn_ms, stat_ms = [], [], [], []
+    for k in range(frames + warmup):
+        p = poses[k].copy()
+        p[0] = poses[(k // 4) * 4][0]                  # the scope moves every fourth frame
+        r.set_pose_array(p)
+        t = time.perf_counter()
+        per = []
+        for c in r.cameras:
+            r.renderCamera(c)
+            i = r.info()
+            per.append(i)
+            r.sensor(c)
+        if k >= warmup:
+            wall.append((time.perf_counter() - t) * 1e3)
+            cam_ms.append(sum(x["cameraMs"] for x in per))
+            dyn_ms.append(sum(x["shadowDynMs"] for x in per))
+            if any(x["shadowStaticMs"] > 0 for x in per):
+                stat_ms.append(sum(x["shadowStaticMs"] for x in per))
+    out = {"workload": f"3 KB4 cameras + SCOPE at 1280x720, 4x MSAA raster, 4 sector shadow maps 2048^2, scope-scale dome level {level} "
+                       f"({r.stats['staticTris']} static + {r.stats['rasterTris'] - r.stats['staticTris']} sliced posed-body triangles)",
+           "ms_per_frame": float(np.median(wall)), "camera_pass_ms_per_frame": float(np.median(cam_ms)),
+           "camera_pass_ms_per_view": float(np.median(cam_ms)) / 4, "shadow_dynamic_ms": float(np.median(dyn_ms)),
+           "shadow_static_ms": float(np.median(stat_ms)) if stat_ms else None, "load_ms": load_ms,
+           "nodes": r.tr.nodes_info["activeNodes"], "big_tris_last": r.info()["bigTris"]}
+    r.destroy()
     return out
 
 

@@ -492,6 +492,75 @@ vt_status vt_get_node_state(vt_ctx* ctx, float* state, uint32_t* slot);
  * browser's). */
 vt_status vt_wait_check(vt_ctx* ctx, uint64_t cycles, int arrive);
 
+/* ------------------------------------------------------------------- lite_nodes: the raster camera pass */
+
+/* lite_nodes/renderer.js: a raster live renderer that keeps the node radiosity (vt_nodes_*) and replaces the camera
+ * path tracing by a rasterised view. Camera view: 4-sample MSAA raster of the static mesh (its vertices are the
+ * radiosity nodes) and of the posed bodies sliced to <= subdiv_h (sliceTris :443), per-vertex KB4 projection
+ * (SCOPE: a pinhole camera that follows the scope body); per fragment the BSDF over ns_static / ns_dyn stratified
+ * emitter samples, soft shadows from 4 sector shadow maps (equidistant about the emission axis, 3x3 taps of 2x2
+ * bilinear depth compares, static and dynamic casters in separate maps), node irradiance interpolated per vertex
+ * times the capsule occlusion on static surfaces, a uniform environment on posed bodies (SHADER :92-360). The
+ * multisample buffer is resolved through half floats and scaled back (FINISH :363). Rasterisation is this
+ * library's own: clip against 0 <= z <= w and a guard band, vertices snapped to 1/256 pixel, exact integer edge
+ * functions with a tie rule that gives a shared edge's samples to exactly one triangle, 'less' depth with ties to
+ * the earlier triangle, shading once per (pixel, triangle) at the pixel centre, as in a 4x MSAA raster pipeline. */
+typedef struct {
+  uint32_t ns_static, ns_dyn;            /* emitter samples per fragment: static surfaces / posed bodies (24, 96) */
+  uint32_t sm_res;                       /* shadow map side (2048) */
+  uint32_t scope_width, scope_height;    /* SCOPE image (1280 x 720) */
+  uint32_t env_material;                 /* material whose hemispherical albedo sets the posed bodies' environment */
+  uint32_t debug;                        /* 0; 1 no shadows; 2 shadow visibility as grey */
+  uint32_t reserved;
+  double sm_theta_max_deg;               /* shadow map cone half-angle (62) */
+  double far_m;                          /* depth range (1.0 m) */
+  double subdiv_h, subdiv_fixture;       /* posed-body slicing step, fixtures (0.003, 0.01 m) */
+  double scope_hfov_deg, scope_circle_frac;      /* SCOPE pinhole (75 deg, image circle 0.95 of the width) */
+  double scope_view_dir[3], scope_objective[3];  /* scope frame: view direction (0, 0.5, 0.866), objective (0, 0, 0) */
+} vt_lite_opts;
+typedef struct {
+  uint32_t raster_tris, static_tris, dyn_verts, n_cameras;   /* n_cameras = scene cameras + SCOPE (the last) */
+  double build_ms;
+  double shadow_static_ms, shadow_dyn_ms, camera_ms;          /* device ms of the last render's passes */
+  uint32_t big_tris, launches;                                /* triangles of the last camera pass rasterised by
+                                                                 the many-pixel path; kernel launches */
+} vt_lite_info;
+/* lite_nodes/renderer.js:497 _init (geometry :527, emitter samples :598, cameras :696). Needs vt_nodes_build. */
+vt_status vt_lite_create(vt_ctx* ctx, const vt_lite_opts* opts, vt_lite_info* info);
+vt_status vt_lite_info_get(vt_ctx* ctx, vt_lite_info* info);
+/* The raster geometry alone, on the host (no device needed): counts = [vertices, triangles]; verts (8 words each:
+ * position | mesh + instance << 16, normal | node) and idx (3 per triangle) are filled when not NULL and large
+ * enough for the counts of a previous call. lite_nodes/renderer.js:527 _buildGeometry with sliceTris (:443). */
+vt_status vt_lite_geometry(const vt_scene_desc* scene, double subdiv_h, double subdiv_fixture, uint32_t counts[2], uint32_t* verts, uint32_t* idx);
+/* lite_nodes/renderer.js:844 renderCamera: node radiosity brought up to the poses, shadow maps re-rendered when
+ * the scope (static casters) or any pose (dynamic casters) changed, then the camera pass into the camera's
+ * radiance (w x h rgba32f; out_rgba receives a copy when not NULL). camera: scene camera index, or n_cameras - 1
+ * for SCOPE. */
+vt_status vt_lite_render_camera(vt_ctx* ctx, uint32_t camera, float* out_rgba);
+/* lite_nodes/renderer.js:892 sensor (the DISPLAY pass :369): exposure, relative illumination of the KB4 cameras,
+ * global-mean glare, white balance, sRGB + S-curve into rgba8; du = (gain, glare k, 0, scaleY, wb rgb, 0, c, black,
+ * 0, 0, fx, fy, cx, cy, 0 x 4); prev: the previous frame's statistics (sum of scaled luma, count); stats: this
+ * frame's. */
+vt_status vt_lite_display(vt_ctx* ctx, uint32_t camera, const float du[20], const uint32_t prev[4], uint32_t stats[4]);
+/* lite_nodes/renderer.js:940 readback('linear' | 'rgb8' | 'rgba8'): VT_READ_LINEAR, VT_READ_RGB8, VT_READ_RGBA8. */
+vt_status vt_lite_readback(vt_ctx* ctx, uint32_t camera, int kind, void* dst, size_t bytes);
+/* The raster pass's intermediate buffers, for checking each stage on its own (bytes: the buffer's size, or
+ * larger). VIEW: the camera's view uniform (128 floats, lite_nodes/renderer.js:766 _viewData layout); CLIP: clip
+ * coordinates of every raster vertex for the camera's last pass (float4); KEYS: its 4 samples per pixel (uint64:
+ * depth bits << 32 | triangle, all ones = empty); SM_STATIC / SM_DYN: the shadow maps (4 x res x res depth bits,
+ * all ones = cleared); SM_CLIP: the last shadow pass's clip coordinates (4 x raster vertices float4); GEOM: raster
+ * vertices (8 words: position | mesh + instance << 16, normal | node); INDEX: 3 per triangle; EMIT: the emitter
+ * samples in the world (8 floats: position | sector, normal | area). */
+enum { VT_LITE_VIEW = 0, VT_LITE_CLIP = 1, VT_LITE_KEYS = 2, VT_LITE_SM_STATIC = 3, VT_LITE_SM_DYN = 4, VT_LITE_SM_CLIP = 5,
+       VT_LITE_GEOM = 6, VT_LITE_INDEX = 7, VT_LITE_EMIT = 8 };
+vt_status vt_lite_debug(vt_ctx* ctx, int what, uint32_t camera, void* dst, size_t bytes);
+/* The rasteriser on its own: triangles (3 indices each) over clip-space vertices (x, y, z, w) into a w x h target
+ * of `samples` (4: the MSAA positions (0.375, 0.125), (0.875, 0.375), (0.125, 0.625), (0.625, 0.875); 1: the pixel
+ * centre) per pixel; keys: w x h x samples uint64, depth bits << 32 | triangle index, all ones where nothing passed
+ * (1 sample: a shadow-map layer, depth only, the triangle bits all ones). Host or device buffers. */
+vt_status vt_raster(vt_ctx* ctx, const float* clip, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris, uint32_t width,
+                    uint32_t height, uint32_t samples, uint64_t* keys);
+
 /* ---------------------------------------------------------------------------------------- bvh (pure) */
 
 /* gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}): binned SAH BVH2 on the host. nodes_out must hold

@@ -35,7 +35,9 @@ def lib():
         _lib.or_scene_create.argtypes = [C.c_void_p, C.c_int, C.c_int]
         for nm in ("or_scene_destroy", "or_scene_sizes", "or_scene_arrays", "or_scene_emitter", "or_scene_blas",
                    "or_scene_set_poses", "or_scene_set_eavg", "or_scene_uniform", "or_scene_set_node_state",
-                   "or_trace_wgsl", "or_render", "or_calib_render", "or_direct_transfer", "or_form_factors_visible"):
+                   "or_trace_wgsl", "or_render", "or_calib_render", "or_direct_transfer", "or_form_factors_visible",
+                   "or_lite_geometry_size", "or_lite_geometry", "or_lite_emitter", "or_lite_vertex", "or_raster", "or_lite_shade",
+                   "or_lite_display", "or_scene_load_uniform"):
             getattr(_lib, nm).restype = None
         _lib.or_fresnel_average.restype = C.c_double
         _lib.or_disc_irradiance.restype = C.c_double
@@ -306,6 +308,54 @@ class Scene:
         lib().or_scene_set_solved_caps(self.h, _p(c, C.c_float), C.c_uint32(len(c) // 8 if c.ndim == 1 else len(c)),
                                        C.c_uint32(self.slot), C.c_uint32(self.frame))
 
+    # ---- raster pass (lite_nodes)
+    def lite_geometry(self, subdiv=0.003, subdiv_fixture=0.01):
+        """Raster vertices (n x 8 words) and triangles (m x 3) of lite_nodes/renderer.js:527 _buildGeometry."""
+        cnt = np.zeros(2, np.uint32)
+        lib().or_lite_geometry_size(self.h, C.c_double(subdiv), C.c_double(subdiv_fixture), _p(cnt, C.c_uint32))
+        V = np.zeros((int(cnt[0]), 8), np.uint32)
+        I = np.zeros((int(cnt[1]), 3), np.uint32)
+        lib().or_lite_geometry(self.h, C.c_double(subdiv), C.c_double(subdiv_fixture), _p(V, C.c_uint32), _p(I, C.c_uint32))
+        return V, I
+
+    def lite_emitter(self, n, T_scope):
+        """The n emitter samples in the world (n x 8 float32) for the scope pose (column-major 4x4) and the four
+        sector origins in the scope frame."""
+        T = np.ascontiguousarray(T_scope, np.float64).reshape(16)
+        out = np.zeros((n, 8), np.float32)
+        sc = np.zeros((4, 3))
+        lib().or_lite_emitter(self.h, C.c_uint32(n), _p(T), _p(out, C.c_float), _p(sc))
+        return out, sc
+
+    def lite_vertex(self, view, verts, shadow=0, base=None):
+        """Clip coordinates of the raster vertices for a view (128 float32): camera (n x 4) or, shadow = 1 / 2, the
+        static / dynamic casters' four sector layers (4 x n x 4, other vertices taken from `base`)."""
+        v = np.ascontiguousarray(view, np.float32)
+        V = np.ascontiguousarray(verts, np.uint32)
+        n = len(V)
+        out = np.zeros((n, 4) if not shadow else (4, n, 4), np.float32) if base is None else np.array(base, np.float32, copy=True)
+        lib().or_lite_vertex(self.h, _p(v, C.c_float), _p(V, C.c_uint32), C.c_uint32(n), int(shadow), _p(out, C.c_float))
+        return out
+
+    def load_uniform(self, su):
+        s = np.ascontiguousarray(su, np.float32)
+        lib().or_scene_load_uniform(self.h, _p(s, C.c_float))
+
+    def lite_shade(self, view, verts, idx, clip, keys, es, sm_static, sm_dyn, inv_scale, circle=0.0, y0=0, y1=None, threads=8):
+        """Fragment stage + resolve + finish (h x w x 4 float32) from the given per-sample keys, clip coordinates and
+        shadow maps."""
+        v = np.ascontiguousarray(view, np.float32)
+        W, H = int(v[24]), int(v[25])
+        out = np.zeros((H, W, 4), np.float32)
+        res = int(np.asarray(sm_static).shape[-1])
+        lib().or_lite_shade(self.h, _p(v, C.c_float), _p(np.ascontiguousarray(verts, np.uint32), C.c_uint32),
+                            _p(np.ascontiguousarray(idx, np.uint32), C.c_uint32), _p(np.ascontiguousarray(clip, np.float32), C.c_float),
+                            _p(np.ascontiguousarray(keys, np.uint64), C.c_uint64), _p(np.ascontiguousarray(es, np.float32), C.c_float),
+                            _p(np.ascontiguousarray(sm_static, np.uint32), C.c_uint32), _p(np.ascontiguousarray(sm_dyn, np.uint32), C.c_uint32),
+                            C.c_uint32(res), C.c_float(inv_scale), C.c_float(circle), C.c_uint32(y0), C.c_uint32(H if y1 is None else y1),
+                            int(threads), _p(out, C.c_float))
+        return out
+
     def form_factors_visible(self, centres, normals, areas, rays=16, fp64=True, threads=1):
         """Dense node form factors with visibility through this scene (n x n float32) and the visible-ray counts."""
         Cn = np.ascontiguousarray(centres, np.float32)
@@ -395,3 +445,27 @@ def isp_chain(su_words, radiance, ri):
                        _p(st, C.c_uint32))
     planes = {"y": yuv[:W * H].reshape(H, W), "cb": yuv[W * H:W * H + cw * ch].reshape(ch, cw), "cr": yuv[W * H + cw * ch:].reshape(ch, cw)}
     return raw, rgba, planes, st
+
+
+def raster(clip, idx, width, height, samples=4, t0=0, nt=None):
+    """The rasteriser restated: keys (h x w x samples uint64: depth bits << 32 | triangle; 1 sample: triangle bits
+    all ones), all ones where nothing passed."""
+    c = np.ascontiguousarray(clip, np.float32).reshape(-1, 4)
+    I = np.ascontiguousarray(idx, np.uint32).reshape(-1, 3)
+    nt = len(I) - t0 if nt is None else nt
+    keys = np.zeros((height, width, samples), np.uint64)
+    lib().or_raster(_p(c, C.c_float), _p(I, C.c_uint32), C.c_uint32(t0), C.c_uint32(nt), C.c_uint32(width), C.c_uint32(height),
+                    C.c_uint32(samples), _p(keys, C.c_uint64))
+    return keys
+
+
+def lite_display(du, prev, radiance):
+    """The raster pass's display look restated (lite_nodes/renderer.js:369): rgba8 (h x w x 4) and stats."""
+    L = np.ascontiguousarray(radiance, np.float32)
+    H, W = L.shape[:2]
+    rgba = np.zeros((H, W, 4), np.uint8)
+    st = np.zeros(4, np.uint32)
+    lib().or_lite_display(_p(np.ascontiguousarray(du, np.float32), C.c_float), _p(np.ascontiguousarray(prev, np.uint32), C.c_uint32),
+                          _p(L, C.c_float), C.c_uint32(W), C.c_uint32(H), _p(rgba, C.c_uint8), _p(st, C.c_uint32))
+    return rgba, st
+

@@ -16,6 +16,7 @@
 #include "../include/vtwin.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -755,6 +756,7 @@ struct Scene {
   std::vector<Pose4> inst;
   std::vector<uint32_t> emitOfTri;   // per triangle slot: index in the emitter table, or MISS
   std::vector<float> solvedCaps;     // 8 per body: bounding capsules at the last node update (empty: the current ones)
+  std::vector<double> emitTris;      // 14 per emitter triangle (scope frame): v0, e1, e2, n, area, cdf
 };
 
 // gpu/scene_gpu.js:504 fitCapsule
@@ -941,6 +943,14 @@ static Scene* prepare_scene(const vt_scene_desc* sd, int leafSize, int albedoSam
   }
   S->radius = radius;
   S->emitArea = emitArea;
+  for (const auto& e : emit) {
+    for (int k = 0; k < 3; k++) S->emitTris.push_back(e.v0[k]);
+    for (int k = 0; k < 3; k++) S->emitTris.push_back(e.e1[k]);
+    for (int k = 0; k < 3; k++) S->emitTris.push_back(e.e2[k]);
+    for (int k = 0; k < 3; k++) S->emitTris.push_back(e.n[k]);
+    S->emitTris.push_back(e.area);
+    S->emitTris.push_back(e.cdf);
+  }
   // capsules, rhoEff (gpu/scene_gpu.js:431-456); no overview_only meshes: occCapsule = capsule
   for (uint32_t bi = 0; bi < sd->n_bodies; bi++) {
     const vt_body_desc& B = sd->bodies[bi];
@@ -2570,6 +2580,458 @@ template <typename F> static void parallel_for(size_t n, int threads, F&& f) {
   for (auto& x : th) x.join();
 }
 
+// ============================================================================================ raster pass
+// lite_nodes/renderer.js restated for the CPU: the raster geometry (sliceTris :443, _buildGeometry :527), the
+// emitter samples (:598, posed by setPoses :729), the vertex stage (vsCam / vsShadow :224-265), a rasteriser with
+// the rules the library documents (clip 0 <= z <= w and |x|, |y| <= 8 w; 1/256-pixel snap; int64 edge functions,
+// ties to the edge with dy < 0 or dy = 0 and dx > 0; screen-linear depth clamped to [0, 1] and kept below 1 and
+// below the sample's, ties to the earlier triangle), the fragment stage (fsCam :284, smVis :267) with the MSAA
+// resolve through half floats and FINISH (:363), and the display look (DISPLAY :369). Float32 arithmetic in the
+// order the kernels use (this file is built with -ffp-contract=off), so raster keys, shadow maps and display bytes
+// compare bit for bit, radiance to float rounding.
+
+namespace lite {
+
+struct SV { double p[3], n[3]; };
+static bool sv_before(const SV& a, const SV& b) {
+  for (int k = 0; k < 2; k++) if (a.p[k] != b.p[k]) return a.p[k] < b.p[k];
+  return a.p[2] < b.p[2];
+}
+static void unit(double* v) {
+  double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  if (l == 0 || std::isnan(l)) l = 1;
+  v[0] /= l; v[1] /= l; v[2] /= l;
+}
+// the point of edge (A, B) on the plane p[ax] = c, computed from the lexicographically smaller endpoint
+static SV crossing(const SV& A, const SV& B, int ax, double c) {
+  const bool ab = sv_before(A, B);
+  const SV& lo = ab ? A : B;
+  const SV& hi = ab ? B : A;
+  const double f = (c - lo.p[ax]) / (hi.p[ax] - lo.p[ax]);
+  SV X;
+  for (int k = 0; k < 3; k++) { X.p[k] = lo.p[k] + f * (hi.p[k] - lo.p[k]); X.n[k] = lo.n[k] + f * (hi.n[k] - lo.n[k]); }
+  X.p[ax] = c;
+  unit(X.n);
+  return X;
+}
+using Tri3 = std::array<SV, 3>;
+static void fan_out(const std::vector<SV>& poly, std::vector<Tri3>& out) {
+  for (size_t j = 2; j < poly.size(); j++) out.push_back(Tri3{poly[0], poly[j - 1], poly[j]});
+}
+static std::vector<Tri3> slice(std::vector<Tri3> tris, double h) {
+  for (int ax = 0; ax < 3; ax++) {
+    std::vector<Tri3> next;
+    for (const Tri3& t : tris) {
+      double lo = t[0].p[ax], hi = t[0].p[ax];
+      for (int j = 1; j < 3; j++) { lo = std::min(lo, t[j].p[ax]); hi = std::max(hi, t[j].p[ax]); }
+      const long long first = (long long)std::floor(lo / h) + 1, last = (long long)std::ceil(hi / h) - 1;
+      if (last < first) { next.push_back(t); continue; }
+      std::vector<SV> poly(t.begin(), t.end());
+      bool done = false;
+      for (long long k = first; k <= last && !done; k++) {
+        const double c = double(k) * h;
+        std::vector<SV> below, above;
+        for (size_t j = 0; j < poly.size(); j++) {
+          const SV& A = poly[j];
+          const SV& B = poly[(j + 1) % poly.size()];
+          const double sa = A.p[ax] - c, sb = B.p[ax] - c;
+          if (sa <= 0) below.push_back(A);
+          if (sa >= 0) above.push_back(A);
+          if ((sa < 0 && sb > 0) || (sa > 0 && sb < 0)) { SV X = crossing(A, B, ax, c); below.push_back(X); above.push_back(X); }
+        }
+        if (below.size() >= 3) fan_out(below, next);
+        if (above.size() < 3) done = true;
+        else poly = above;
+      }
+      if (!done) fan_out(poly, next);
+    }
+    tris.swap(next);
+  }
+  return tris;
+}
+
+static void geometry(const Scene& S, double h, double hfix, std::vector<uint32_t>& V, std::vector<uint32_t>& I) {
+  V.clear();
+  I.clear();
+  for (uint32_t i = 0; i < S.staticVerts; i++) {
+    const uint32_t* s = S.verts.data() + 8 * size_t(i);
+    const uint32_t w[8] = {s[0], s[1], s[2], (s[3] & 0xffffu) | 0xffff0000u, s[4], s[5], s[6], i};
+    V.insert(V.end(), w, w + 8);
+  }
+  for (uint32_t k = 0; k < S.staticTris; k++) {
+    const uint32_t* t = S.tris.data() + 16 * size_t(k);
+    I.push_back(t[3]); I.push_back(t[7]); I.push_back(t[11]);
+  }
+  uint32_t next = S.staticVerts;
+  for (size_t b = 0; b < S.blas.size(); b++) {
+    const Blas& B = S.blas[b];
+    std::vector<uint32_t> meshes;
+    for (uint32_t k = 0; k < B.tri_count; k++) {
+      const uint32_t m = S.tris[16 * size_t(B.tri_off + k) + 12];
+      if (std::find(meshes.begin(), meshes.end(), m) == meshes.end()) meshes.push_back(m);
+    }
+    for (uint32_t m : meshes) {
+      std::vector<Tri3> tris;
+      for (uint32_t k = 0; k < B.tri_count; k++) {
+        const uint32_t* t = S.tris.data() + 16 * size_t(B.tri_off + k);
+        if (t[12] != m) continue;
+        Tri3 tr;
+        for (int j = 0; j < 3; j++) {
+          const uint32_t* v = S.verts.data() + 8 * size_t(t[3 + 4 * j]);
+          for (int q = 0; q < 3; q++) { tr[j].p[q] = double(as_f(v[q])); tr[j].n[q] = double(as_f(v[4 + q])); }
+        }
+        tris.push_back(tr);
+      }
+      for (const Tri3& t : slice(tris, B.kind == VT_BODY_FIXTURE ? hfix : h))
+        for (const SV& v : t) {
+          const uint32_t w[8] = {as_u(float(v.p[0])), as_u(float(v.p[1])), as_u(float(v.p[2])), (m & 0xffffu) | (uint32_t(b) << 16),
+                                 as_u(float(v.n[0])), as_u(float(v.n[1])), as_u(float(v.n[2])), MISS};
+          V.insert(V.end(), w, w + 8);
+          I.push_back(next++);
+        }
+    }
+  }
+}
+
+// the emitter samples in the world for the scope pose T (column-major 4x4): 8 floats each
+static void emitter_world(const Scene& S, uint32_t n, const double* T, std::vector<float>& out, double sectC[4][3]) {
+  const double* c = S.centroid;
+  const double* nr = S.emitNormal;
+  double t[3], up[3] = {0, 0, 0};
+  up[std::fabs(nr[0]) < 0.9 ? 0 : 1] = 1;
+  t[0] = up[1] * nr[2] - up[2] * nr[1]; t[1] = up[2] * nr[0] - up[0] * nr[2]; t[2] = up[0] * nr[1] - up[1] * nr[0];
+  unit(t);
+  const double bb[3] = {nr[1] * t[2] - nr[2] * t[1], nr[2] * t[0] - nr[0] * t[2], nr[0] * t[1] - nr[1] * t[0]};
+  const double g = 1.22074408460575947536;
+  const size_t nt = S.emitTris.size() / 14;
+  std::vector<double> P(3 * size_t(n)), N(3 * size_t(n));
+  std::vector<int> sect(n);
+  for (uint32_t i = 0; i < n; i++) {
+    const double u1 = std::fmod(0.5 + i / g, 1.0), u2 = std::fmod(0.5 + i / (g * g), 1.0), u3 = std::fmod(0.5 + i / (g * g * g), 1.0);
+    size_t a = 0, z = nt ? nt - 1 : 0;
+    while (a < z) { const size_t m = (a + z) / 2; if (S.emitTris[14 * m + 13] < u1) a = m + 1; else z = m; }
+    const double* e = S.emitTris.data() + 14 * a;
+    const double su = std::sqrt(u2);
+    double d[3];
+    for (int k = 0; k < 3; k++) {
+      P[3 * i + k] = nt ? e[k] + e[3 + k] * su * (1 - u3) + e[6 + k] * su * u3 : 0.0;
+      N[3 * i + k] = nt ? e[9 + k] : (k == 2 ? 1.0 : 0.0);
+      d[k] = P[3 * i + k] - c[k];
+    }
+    const double ang = std::atan2(d[0] * bb[0] + d[1] * bb[1] + d[2] * bb[2], d[0] * t[0] + d[1] * t[1] + d[2] * t[2]);
+    sect[i] = std::min(3, int(std::floor((ang + M_PI) / (2 * M_PI) * 4)));
+  }
+  auto W = [&](const double* v, double* o) { for (int i = 0; i < 3; i++) o[i] = T[i] * v[0] + T[4 + i] * v[1] + T[8 + i] * v[2] + T[12 + i]; };
+  for (int k = 0; k < 4; k++) {
+    double acc[3] = {0, 0, 0};
+    int cnt = 0;
+    for (uint32_t i = 0; i < n; i++) if (sect[i] == k) { for (int j = 0; j < 3; j++) acc[j] += P[3 * i + j]; cnt++; }
+    for (int j = 0; j < 3; j++) sectC[k][j] = cnt ? acc[j] / cnt : c[j];
+  }
+  out.assign(8 * size_t(n), 0.0f);
+  for (uint32_t i = 0; i < n; i++) {
+    double w[3];
+    W(&P[3 * i], w);
+    float* o = out.data() + 8 * size_t(i);
+    for (int k = 0; k < 3; k++) {
+      o[k] = float(w[k]);
+      o[4 + k] = float(T[k] * N[3 * i] + T[4 + k] * N[3 * i + 1] + T[8 + k] * N[3 * i + 2]);
+    }
+    o[3] = float(sect[i]);
+    o[7] = float(S.emitArea);
+  }
+}
+
+struct View {
+  const float* f;
+  uint32_t u(int i) const { return as_u(f[i]); }
+  V3<float> v3(int i) const { return V3<float>(f[i], f[i + 1], f[i + 2]); }
+};
+static inline float hyp(float x, float y) { return std::sqrt(x * x + y * y); }
+
+static bool world_of(Tracer<float>& tr, const View& V, const uint32_t* w, V3<float>& p, V3<float>& n) {
+  p = V3<float>(as_f(w[0]), as_f(w[1]), as_f(w[2]));
+  n = V3<float>(as_f(w[4]), as_f(w[5]), as_f(w[6]));
+  const uint32_t inst = w[3] >> 16;
+  if (inst == 0xffffu) return true;
+  if (inst >= VT_MAX_INST || (tr.su_u(24 + 48 * inst + 15) & 2u) || ((V.u(28) >> inst) & 1u)) return false;
+  M3<float> M;
+  V3<float> t;
+  tr.inst_pose(inst, V.f[35], M, t);
+  p = M.mul(p) + t;
+  n = M.mul(n);
+  return true;
+}
+static void project_cam(const View& V, const V3<float>& p, float o[4]) {
+  const V3<float> d = p - V.v3(12);
+  const float x = dot(d, V.v3(0)), y = dot(d, V.v3(4)), z = dot(d, V.v3(8));
+  const float W = V.f[24], H = V.f[25], FAR = V.f[47];
+  const float fx = V.f[16], fy = V.f[17], cx = V.f[18], cy = V.f[19];
+  if (V.f[15] > 0.5f) {
+    const float nz = 1e-3f;
+    o[0] = (2.0f * fx * x + (2.0f * (cx + 0.5f) - W) * z) / W;
+    o[1] = ((H - 2.0f * (cy + 0.5f)) * z - 2.0f * fy * y) / H;
+    o[2] = (z - nz) * FAR / (FAR - nz);
+    o[3] = z;
+    return;
+  }
+  const float r = hyp(x, y);
+  const float th = std::atan2(r, z);
+  if (th > V.f[26]) {
+    const float ex = fx * x / W + 1e-12f, ey = -fy * y / H;
+    const float l = hyp(ex, ey);
+    o[0] = ex / l; o[1] = ey / l; o[2] = -1e-3f; o[3] = -1e-3f;
+    return;
+  }
+  const float t2 = th * th;
+  const float thd = th * (1.0f + t2 * (V.f[20] + t2 * (V.f[21] + t2 * (V.f[22] + t2 * V.f[23]))));
+  const float s = thd / std::max(r, 1e-12f);
+  const float u = fx * x * s + cx + 0.5f, v = fy * y * s + cy + 0.5f;
+  o[0] = 2.0f * u / W - 1.0f; o[1] = 1.0f - 2.0f * v / H; o[2] = len(d) / FAR; o[3] = 1.0f;
+}
+static V3<float> sm_project(const View& V, const V3<float>& pw, int k) {
+  const V3<float> d = pw - V.v3(48 + 4 * k);
+  const float x = dot(d, V.v3(40)), y = dot(d, V.v3(44)), z = dot(d, V.v3(36));
+  const float rho = hyp(x, y);
+  const float s = std::atan2(rho, z) / (V.f[43] * std::max(rho, 1e-12f));
+  return V3<float>(x * s, y * s, len(d));
+}
+
+// ------------------------------------------------------------------------------------------- rasteriser
+static float pdist(const float* v, int p) {
+  const float G = 8.0f;
+  switch (p) {
+    case 0: return v[2];
+    case 1: return v[3] - v[2];
+    case 2: return G * v[3] - v[0];
+    case 3: return G * v[3] + v[0];
+    case 4: return G * v[3] - v[1];
+    default: return G * v[3] + v[1];
+  }
+}
+struct Pt { long long x, y; float z; };
+// clip + snap: the polygon's snapped vertices (empty: nothing to draw)
+static std::vector<Pt> setup(const float* c0, const float* c1, const float* c2, uint32_t W, uint32_t H) {
+  std::vector<std::array<float, 4>> poly = {{c0[0], c0[1], c0[2], c0[3]}, {c1[0], c1[1], c1[2], c1[3]}, {c2[0], c2[1], c2[2], c2[3]}};
+  bool inside = true;
+  for (auto& v : poly) for (int p = 0; p < 6; p++) inside = inside && pdist(v.data(), p) >= 0.0f;
+  if (!inside) {
+    for (int p = 0; p < 6; p++) {
+      std::vector<std::array<float, 4>> out;
+      for (size_t i = 0; i < poly.size(); i++) {
+        const auto& A = poly[i];
+        const auto& B = poly[(i + 1) % poly.size()];
+        const float da = pdist(A.data(), p), db = pdist(B.data(), p);
+        if (da >= 0.0f && out.size() < 9) out.push_back(A);
+        if ((da >= 0.0f) != (db >= 0.0f) && out.size() < 9) {
+          const auto& In = da >= 0.0f ? A : B;
+          const auto& Out = da >= 0.0f ? B : A;
+          const float di = da >= 0.0f ? da : db, dq = da >= 0.0f ? db : da;
+          const float t = di / (di - dq);
+          out.push_back({In[0] + t * (Out[0] - In[0]), In[1] + t * (Out[1] - In[1]), In[2] + t * (Out[2] - In[2]), In[3] + t * (Out[3] - In[3])});
+        }
+      }
+      poly.swap(out);
+      if (poly.size() < 3) return {};
+    }
+  }
+  const float W2 = float(W) * 0.5f, H2 = float(H) * 0.5f;
+  std::vector<Pt> P;
+  for (auto& v : poly) {
+    if (!(v[3] > 0.0f)) return {};
+    const float nx = v[0] / v[3], ny = v[1] / v[3];
+    const float X = (nx + 1.0f) * W2, Y = (1.0f - ny) * H2;
+    if (!(std::fabs(X) < 1e6f) || !(std::fabs(Y) < 1e6f)) return {};
+    P.push_back(Pt{(long long)std::lrint(X * 256.0f), (long long)std::lrint(Y * 256.0f), v[2] / v[3]});
+  }
+  return P;
+}
+static long long fdiv256(long long v) { return v >= 0 ? v / 256 : -((255 - v) / 256); }
+
+// raster triangles [t0, t0 + nt) of layer `layer` into keys (samples 4: 64-bit keys; 1: depth bits in the high word)
+static void raster(const float* clip, const uint32_t* idx, uint32_t t0, uint32_t nt, uint32_t W, uint32_t H, uint32_t samples, uint64_t* keys) {
+  static const int SX[4] = {96, 224, 32, 160}, SY[4] = {32, 96, 160, 224};
+  for (uint32_t t = t0; t < t0 + nt; t++) {
+    const std::vector<Pt> P = setup(clip + 4 * size_t(idx[3 * t]), clip + 4 * size_t(idx[3 * t + 1]), clip + 4 * size_t(idx[3 * t + 2]), W, H);
+    for (size_t k = 1; k + 1 < P.size(); k++) {
+      Pt a = P[0], b = P[k], c = P[k + 1];
+      long long A = (b.x - a.x) * (c.y - a.y) - (b.y - a.y) * (c.x - a.x);
+      if (A == 0) continue;
+      if (A < 0) { std::swap(b, c); A = -A; }
+      const Pt* ends[3][2] = {{&b, &c}, {&c, &a}, {&a, &b}};
+      long long dx[3], dy[3], ox[3], oy[3];
+      int bias[3];
+      for (int e = 0; e < 3; e++) {
+        dx[e] = ends[e][1]->x - ends[e][0]->x; dy[e] = ends[e][1]->y - ends[e][0]->y;
+        ox[e] = ends[e][0]->x; oy[e] = ends[e][0]->y;
+        bias[e] = (dy[e] < 0 || (dy[e] == 0 && dx[e] > 0)) ? 0 : -1;
+      }
+      const long long x0 = std::max(0LL, fdiv256(std::min(a.x, std::min(b.x, c.x)))), x1 = std::min((long long)W - 1, fdiv256(std::max(a.x, std::max(b.x, c.x))));
+      const long long y0 = std::max(0LL, fdiv256(std::min(a.y, std::min(b.y, c.y)))), y1 = std::min((long long)H - 1, fdiv256(std::max(a.y, std::max(b.y, c.y))));
+      const float fA = float(A);
+      for (long long py = y0; py <= y1; py++)
+        for (long long px = x0; px <= x1; px++)
+          for (uint32_t s = 0; s < samples; s++) {
+            const long long sx = px * 256 + (samples == 1 ? 128 : SX[s]), sy = py * 256 + (samples == 1 ? 128 : SY[s]);
+            long long w[3];
+            bool in = true;
+            for (int e = 0; e < 3; e++) { w[e] = dx[e] * (sy - oy[e]) - dy[e] * (sx - ox[e]); in = in && w[e] + bias[e] >= 0; }
+            if (!in) continue;
+            const float l1 = float(w[1]) / fA, l2 = float(w[2]) / fA;
+            float z = a.z + l1 * (b.z - a.z) + l2 * (c.z - a.z);
+            z = std::min(z, 1.0f);
+            if (!(z > 0.0f)) z = 0.0f;
+            if (!(z < 1.0f)) continue;
+            uint64_t key = (uint64_t(as_u(z)) << 32) | (samples == 1 ? 0xffffffffull : uint64_t(t));
+            uint64_t& slot = keys[(size_t(py) * W + px) * samples + s];
+            if (key < slot) slot = key;
+          }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------- fragment stage
+static float h16(float x) {
+  if (std::isnan(x) || std::isinf(x) || x == 0.0f) return x;
+  int ex;
+  std::frexp(double(x), &ex);
+  const double q = std::fabs(x) < 6.103515625e-05 ? std::ldexp(1.0, -24) : std::ldexp(1.0, ex - 11);
+  const double r = std::nearbyint(double(x) / q) * q;
+  if (std::fabs(r) > 65504.0) return x > 0 ? INFINITY : -INFINITY;
+  return float(r);
+}
+static float texel(const uint32_t* m, uint32_t res, int k, int x, int y) {
+  x = std::min(std::max(x, 0), int(res) - 1);
+  y = std::min(std::max(y, 0), int(res) - 1);
+  const uint32_t b = m[(size_t(k) * res + y) * res + x];
+  return b == 0xffffffffu ? 1.0f : as_f(b);
+}
+static float cmp(const uint32_t* m, uint32_t res, int k, float u, float v, float dref) {
+  const float tx = u * float(res) - 0.5f, ty = v * float(res) - 0.5f;
+  const float fx0 = std::floor(tx), fy0 = std::floor(ty);
+  const float fx = tx - fx0, fy = ty - fy0;
+  const int x0 = int(fx0), y0 = int(fy0);
+  const float c00 = dref < texel(m, res, k, x0, y0) ? 1.0f : 0.0f, c10 = dref < texel(m, res, k, x0 + 1, y0) ? 1.0f : 0.0f;
+  const float c01 = dref < texel(m, res, k, x0, y0 + 1) ? 1.0f : 0.0f, c11 = dref < texel(m, res, k, x0 + 1, y0 + 1) ? 1.0f : 0.0f;
+  return (1.0f - fx) * (1.0f - fy) * c00 + fx * (1.0f - fy) * c10 + (1.0f - fx) * fy * c01 + fx * fy * c11;
+}
+
+struct Frag {
+  Tracer<float>& tr;
+  Shader<float>& sh;
+  const View& V;
+  const uint32_t* Vx;       // raster vertices, 8 words
+  const uint32_t* idx;
+  const float* clip;
+  const float* es;
+  const uint32_t *sms, *smd;
+  uint32_t res;
+
+  float vis(const V3<float>& pw, int k, float bias) const {
+    const V3<float> q = sm_project(V, pw, k);
+    if (std::fabs(q.x) >= 1.0f || std::fabs(q.y) >= 1.0f) return 1.0f;
+    const float u = 0.5f + 0.5f * q.x, v = 0.5f - 0.5f * q.y, dref = (q.z - bias) / V.f[47], t = 1.0f / float(res);
+    float s = 0.0f;
+    for (int j = -1; j <= 1; j++)
+      for (int i = -1; i <= 1; i++) {
+        const float ou = u + float(i) * t, ov = v + float(j) * t;
+        s = s + std::min(cmp(sms, res, k, ou, ov, dref), cmp(smd, res, k, ou, ov, dref));
+      }
+    return s / 9.0f;
+  }
+  V3<float> shade(uint32_t tri, uint32_t px, uint32_t py) const {
+    const Scene& S = tr.S;
+    V3<float> wp[3], wn[3];
+    float X[3], Y[3];
+    const float W2 = V.f[24] * 0.5f, H2 = V.f[25] * 0.5f, sx = float(px) + 0.5f, sy = float(py) + 0.5f;
+    const uint32_t* vw[3];
+    for (int j = 0; j < 3; j++) {
+      const uint32_t vi = idx[3 * tri + j];
+      vw[j] = Vx + 8 * size_t(vi);
+      world_of(tr, V, vw[j], wp[j], wn[j]);
+      const float* c = clip + 4 * size_t(vi);
+      X[j] = (c[0] + c[3]) * W2 - sx * c[3];
+      Y[j] = (c[3] - c[1]) * H2 - sy * c[3];
+    }
+    float b[3] = {X[1] * Y[2] - X[2] * Y[1], X[2] * Y[0] - X[0] * Y[2], X[0] * Y[1] - X[1] * Y[0]};
+    const float sb = b[0] + b[1] + b[2];
+    if (sb != 0.0f) for (float& q : b) q = q / sb;
+    else for (float& q : b) q = 1.0f / 3.0f;
+    const V3<float> p = wp[0] * b[0] + wp[1] * b[1] + wp[2] * b[2];
+    const V3<float> nin = wn[0] * b[0] + wn[1] * b[1] + wn[2] * b[2];
+    const uint32_t slot = tr.su_u(18);
+    float ew[4] = {0, 0, 0, 0};
+    for (int j = 0; j < 3; j++) {
+      const uint32_t ni = vw[j][7];
+      if (ni == MISS) continue;
+      const float wa = S.nodeState[16 * size_t(ni) + 4 * slot + 3];
+      for (int k = 0; k < 3; k++) ew[k] = ew[k] + S.nodeState[16 * size_t(ni) + k] * wa * b[j];
+      ew[3] = ew[3] + wa * b[j];
+    }
+    const uint32_t mesh = vw[0][3] & 0xffffu, inst = vw[0][3] >> 16;
+    const uint32_t flags = as_u(sh.pv(S.meshOff + 2 * mesh + 1)[0]), mat = as_u(sh.pv(S.meshOff + 2 * mesh)[3]);
+    const V3<float> wo = normalize(V.v3(12) - p);
+    V3<float> ng = cross(wp[1] - wp[0], wp[2] - wp[0]);
+    if (dot(ng, ng) < 1e-30f) ng = nin;
+    ng = normalize(ng);
+    if (dot(ng, wo) < 0.0f) ng = -ng;
+    V3<float> ns = normalize(nin);
+    const V3<float> axis = V.v3(36);
+    const V3<float> L0 = V3<float>(tr.SU[0], tr.SU[1], tr.SU[2]);
+    if (flags & VT_F_EMITTER) {
+      if (dot(wo, ns) <= 0.0f) return V3<float>();
+      const V3<float> Le = L0 * sh.profile(std::acos(clampR(dot(wo, axis), -1.0f, 1.0f)));
+      return V3<float>(std::min(Le.x * V.f[27], 60000.0f), std::min(Le.y * V.f[27], 60000.0f), std::min(Le.z * V.f[27], 60000.0f));
+    }
+    if (dot(ns, ng) < 0.0f) ns = -ns;
+    if (dot(ns, wo) < 1e-4f) ns = ng;
+    const MatR<float> M = sh.load_mat(mat);
+    const bool st = inst == 0xffffu;
+    const uint32_t nS = st ? V.u(29) : V.u(30);
+    V3<float> acc[4];
+    for (uint32_t j = 0; j < nS; j++) {
+      const float* ea = es + 8 * size_t(j);
+      V3<float> wi = V3<float>(ea[0], ea[1], ea[2]) - p;
+      const float d2 = dot(wi, wi);
+      wi = wi * (1.0f / std::sqrt(d2));
+      const float cosE = dot(-wi, V3<float>(ea[4], ea[5], ea[6]));
+      if (cosE <= 0.0f) continue;
+      const float cosS = dot(ns, wi);
+      if (cosS <= 0.0f || dot(ng, wi) <= 0.0f) continue;
+      const float pr = sh.profile(std::acos(clampR(dot(-wi, axis), -1.0f, 1.0f)));
+      if (pr <= 0.0f) continue;
+      const V3<float> f = eval_bsdf(M, ns, wi, wo);
+      const int k = std::min(int(ea[3]), 3);
+      acc[k] = acc[k] + f * (pr * cosS * cosE * ea[7] / d2);
+    }
+    V3<float> L;
+    const V3<float> off = p + ng * (st ? 1.5e-4f : 6e-4f);
+    const uint32_t dbg = V.u(39);
+    float vsum = 0.0f;
+    for (int k = 0; k < 4; k++) {
+      const float vk = dbg != 1u ? vis(off, k, st ? V.f[51 + 4 * k] : 6e-4f) : 1.0f;
+      vsum = vsum + vk;
+      if (maxc(acc[k]) <= 0.0f) continue;
+      L = L + acc[k] * vk;
+    }
+    if (dbg == 2u) return V3<float>(vsum / 4.0f, vsum / 4.0f, vsum / 4.0f);
+    L = L * L0 / float(nS);
+    const float mu = std::max(dot(ns, wo), 0.0f);
+    const V3<float> Al = sh.albedo_all(mat, mu);
+    if (st) {
+      V3<float> E;
+      if (ew[3] > 1e-6f) E = V3<float>(ew[0], ew[1], ew[2]) / ew[3];
+      E = E * sh.capsule_vis(p, ns);
+      L = L + E * float(INV_PI_D) * Al;
+    } else {
+      L = L + V.v3(32) * Al;
+    }
+    return L * V.f[27];
+  }
+};
+
+}  // namespace lite
+
 extern "C" {
 
 void or_mulberry32(uint32_t seed, int n, double* out) { Mulberry32 m(seed); for (int i = 0; i < n; i++) out[i] = m.next(); }
@@ -3084,6 +3546,152 @@ void or_scene_set_solved_caps(void* h, const float* caps, uint32_t nb, uint32_t 
   Scene* S = static_cast<Scene*>(h);
   S->solvedCaps.assign(caps, caps + 8 * size_t(nb));
   write_scene_u(*S, slot, frame);
+}
+
+// ---- raster pass (lite_nodes)
+// sizes of the raster geometry: counts = [vertices, triangles]
+void or_lite_geometry_size(void* h, double subdiv, double subdiv_fixture, uint32_t* counts) {
+  std::vector<uint32_t> V, I;
+  lite::geometry(*static_cast<Scene*>(h), subdiv, subdiv_fixture, V, I);
+  counts[0] = uint32_t(V.size() / 8);
+  counts[1] = uint32_t(I.size() / 3);
+}
+void or_lite_geometry(void* h, double subdiv, double subdiv_fixture, uint32_t* verts, uint32_t* idx) {
+  std::vector<uint32_t> V, I;
+  lite::geometry(*static_cast<Scene*>(h), subdiv, subdiv_fixture, V, I);
+  std::copy(V.begin(), V.end(), verts);
+  std::copy(I.begin(), I.end(), idx);
+}
+// emitter samples in the world for scope pose T (column-major): 8 floats each; sector origins (4 x 3)
+void or_lite_emitter(void* h, uint32_t n, const double* T, float* out, double* sect_c) {
+  std::vector<float> es;
+  double sc[4][3];
+  lite::emitter_world(*static_cast<Scene*>(h), n, T, es, sc);
+  std::copy(es.begin(), es.end(), out);
+  for (int k = 0; k < 4; k++) for (int j = 0; j < 3; j++) sect_c[3 * k + j] = sc[k][j];
+}
+// vertex stage: shadow = 0 camera clip coordinates (n x 4); shadow = 1 / 2 the four sector layers (4 x n x 4) of
+// the static / dynamic casters (other vertices left as they are in out)
+void or_lite_vertex(void* h, const float* view, const uint32_t* verts, uint32_t n, int shadow, float* out) {
+  Scene* S = static_cast<Scene*>(h);
+  Dbg d;
+  Tracer<float> tr(*S, d);
+  lite::View V{view};
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t* w = verts + 8 * size_t(i);
+    V3<float> p, nn;
+    const bool ok = lite::world_of(tr, V, w, p, nn);
+    if (!shadow) {
+      float* o = out + 4 * size_t(i);
+      if (ok) lite::project_cam(V, p, o);
+      else { o[0] = 0.0f; o[1] = 0.0f; o[2] = -2.0f; o[3] = 1.0f; }
+      continue;
+    }
+    const bool st = (w[3] >> 16) == 0xffffu;
+    if ((shadow == 1) != st) continue;
+    const uint32_t flags = as_u(S->params[4 * (S->meshOff + 2 * (w[3] & 0xffffu) + 1)]);
+    const bool keep = ok && (flags & (VT_F_EMITTER | VT_F_SCOPE)) == 0u;
+    for (int k = 0; k < 4; k++) {
+      float* o = out + 4 * (size_t(k) * n + i);
+      if (!keep) { o[0] = 0.0f; o[1] = 0.0f; o[2] = -2.0f; o[3] = 1.0f; continue; }
+      const V3<float> q = lite::sm_project(V, p, k);
+      if (lite::hyp(q.x, q.y) > 1.0f) {
+        const float ex = q.x + 1e-12f, ey = q.y, l = lite::hyp(ex, ey);
+        o[0] = ex / l; o[1] = ey / l; o[2] = -1e-3f; o[3] = -1e-3f;
+      } else {
+        o[0] = q.x; o[1] = q.y; o[2] = q.z / view[47]; o[3] = 1.0f;
+      }
+    }
+  }
+}
+// rasteriser: keys (w x h x samples uint64) start all ones
+void or_raster(const float* clip, const uint32_t* idx, uint32_t t0, uint32_t nt, uint32_t W, uint32_t H, uint32_t samples, uint64_t* keys) {
+  std::fill(keys, keys + size_t(W) * H * samples, ~0ull);
+  lite::raster(clip, idx, t0, nt, W, H, samples, keys);
+}
+// fragment stage + resolve + finish for rows [y0, y1) from the given keys, clip coordinates and shadow maps
+void or_lite_shade(void* h, const float* view, const uint32_t* verts, const uint32_t* idx, const float* clip, const uint64_t* keys,
+                   const float* es, const uint32_t* sm_static, const uint32_t* sm_dyn, uint32_t res, float inv_scale, float circle,
+                   uint32_t y0, uint32_t y1, int threads, float* out) {
+  Scene* S = static_cast<Scene*>(h);
+  const uint32_t W = uint32_t(view[24]), H = uint32_t(view[25]);
+  y1 = std::min(y1, H);
+  parallel_for(y1 > y0 ? y1 - y0 : 0, threads, [&](size_t r) {
+    Dbg d;
+    Tracer<float> tr(*S, d);
+    Shader<float> sh(tr);
+    lite::View V{view};
+    lite::Frag F{tr, sh, V, verts, idx, clip, es, sm_static, sm_dyn, res};
+    const uint32_t py = y0 + uint32_t(r);
+    for (uint32_t px = 0; px < W; px++) {
+      const uint64_t* k = keys + (size_t(py) * W + px) * 4;
+      V3<float> col[4];
+      bool done[4] = {false, false, false, false};
+      for (int s = 0; s < 4; s++) {
+        if (done[s]) continue;
+        V3<float> c;
+        if (k[s] != ~0ull) {
+          c = F.shade(uint32_t(k[s] & 0xffffffffu), px, py);
+          c = V3<float>(lite::h16(c.x), lite::h16(c.y), lite::h16(c.z));
+        }
+        for (int t = s; t < 4; t++)
+          if (!done[t] && uint32_t(k[t]) == uint32_t(k[s])) { col[t] = c; done[t] = true; }
+      }
+      float rgb[3];
+      for (int ch = 0; ch < 3; ch++) {
+        const float v = ((((ch == 0 ? col[0].x : ch == 1 ? col[0].y : col[0].z) + (ch == 0 ? col[1].x : ch == 1 ? col[1].y : col[1].z)) +
+                          (ch == 0 ? col[2].x : ch == 1 ? col[2].y : col[2].z)) + (ch == 0 ? col[3].x : ch == 1 ? col[3].y : col[3].z)) * 0.25f;
+        rgb[ch] = lite::h16(v) * inv_scale;
+      }
+      if (circle > 0.0f) {
+        const float qx = float(px) + 0.5f - 0.5f * float(W), qy = float(py) + 0.5f - 0.5f * float(H);
+        if (lite::hyp(qx, qy) > circle) rgb[0] = rgb[1] = rgb[2] = 0.0f;
+      }
+      float* o = out + 4 * (size_t(py) * W + px);
+      o[0] = rgb[0]; o[1] = rgb[1]; o[2] = rgb[2]; o[3] = 1.0f;
+    }
+  });
+}
+// the display look (DISPLAY): rgba8 and stats (luma sum, count)
+void or_lite_display(const float* du, const uint32_t* prev, const float* L4, uint32_t W, uint32_t H, uint8_t* rgba, uint32_t* stats) {
+  stats[0] = stats[1] = stats[2] = stats[3] = 0;
+  const float n = std::max(float(prev[1]), 1.0f);
+  const float mean = float(prev[0]) / std::max(du[3], 1e-30f) / n;
+  for (uint32_t y = 0; y < H; y++)
+    for (uint32_t x = 0; x < W; x++) {
+      const float* l = L4 + 4 * (size_t(y) * W + x);
+      if ((x & 3u) == 0u && (y & 3u) == 0u) {
+        const float yl = l[0] * 0.2126f + l[1] * 0.7152f + l[2] * 0.0722f;
+        stats[0] += uint32_t(std::min(std::max(yl * du[3], 0.0f), 65535.0f));
+        stats[1] += 1;
+      }
+      float E[3] = {l[0], l[1], l[2]};
+      if (du[12] > 0.0f) {
+        const float qx = (float(x) + 0.5f - du[14]) / du[12], qy = (float(y) + 0.5f - du[15]) / du[13];
+        const float c = clamp01(std::sqrt(qx * qx + qy * qy) / 1.1f);
+        const float t = c * c;
+        const float f = 1.0f * (1.0f - t) + 0.57f * t;
+        for (float& e : E) e = e * f;
+      }
+      uint8_t* o = rgba + 4 * (size_t(y) * W + x);
+      for (int k = 0; k < 3; k++) {
+        const float e = (1.0f - du[1]) * E[k] + du[1] * mean;
+        const float xv = e * du[0] * du[4 + k];
+        const float v = clamp01((xv - du[9]) / (1.0f - du[9]));
+        float t = srgb_oetf(v);
+        if (du[8] > 0.0f) {
+          const float a = vt_powf(clamp01(t), du[8]);
+          t = a / (a + vt_powf(clamp01(1.0f - t), du[8]));
+        }
+        o[k] = uint8_t(std::lrint(t * 255.0f));
+      }
+      o[3] = 255;
+    }
+}
+// load a scene uniform as given (the raster pass's shading reads the poses, the slot and the capsules from it)
+void or_scene_load_uniform(void* h, const float* su) {
+  Scene* S = static_cast<Scene*>(h);
+  std::copy(su, su + 24 + 48 * VT_MAX_INST, S->sceneU);
 }
 
 }  // extern "C"

@@ -147,3 +147,18 @@ def test_ctypes_mirror_matches_header_layout(tmp_path):
         assert int(got[n]) == ctypes.sizeof(S), n
         for f in S._fields_:
             assert int(got[f"{n}.{f[0]}"]) == getattr(S, f[0]).offset, f"{n}.{f[0]}"
+
+
+def test_lite_geometry_matches_oracle():
+    """The raster pass's geometry (vt_lite_geometry: the static mesh + the posed bodies sliced by sliceTris,
+    lite_nodes/renderer.js:443-586) is the CPU restatement's, word for word; no device needed."""
+    import oracle as O
+    from vtwin import dome
+    from vtwin.lite import lite_geometry
+
+    sc = dome.make_scope_scene(seed=2, level=4, n_tools=2, width=64, height=36)
+    V, I = lite_geometry(sc, 0.003, 0.01)
+    Vo, Io = O.Scene(sc).lite_geometry(0.003, 0.01)
+    assert V.shape == Vo.shape and I.shape == Io.shape
+    assert np.array_equal(V, Vo) and np.array_equal(I, Io)
+    assert len(I) > len(sc["static"]["I"]) + 1000

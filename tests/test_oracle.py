@@ -388,3 +388,111 @@ def test_relative_illumination_pinhole_closed_form():
     th = np.hypot(xd, yd)
     want = np.where(th > 1e-6, np.cos(th) ** q * np.sin(th) / np.maximum(th, 1e-300), 1.0)
     np.testing.assert_allclose(ri, want.astype(np.float32), rtol=2e-7)
+
+
+# ------------------------------------------------------------------------------------------ raster pass (lite_nodes)
+def _grid_mesh(nx, ny, z=0.5, jitter=0.0, seed=0):
+    """A (nx x ny)-cell grid of clip-space triangles covering [-0.9, 0.9]^2 with shared (jittered) vertices."""
+    rng = np.random.default_rng(seed)
+    xs, ys = np.linspace(-0.9, 0.9, nx + 1), np.linspace(-0.9, 0.9, ny + 1)
+    P = np.array([[x, y] for y in ys for x in xs])
+    inner = (np.abs(P[:, 0]) < 0.89) & (np.abs(P[:, 1]) < 0.89)
+    P[inner] += rng.uniform(-jitter, jitter, (inner.sum(), 2))
+    clip = np.concatenate([P, np.full((len(P), 1), z), np.ones((len(P), 1))], 1).astype(np.float32)
+    idx = []
+    for j in range(ny):
+        for i in range(nx):
+            a, b, c, d = j * (nx + 1) + i, j * (nx + 1) + i + 1, (j + 1) * (nx + 1) + i + 1, (j + 1) * (nx + 1) + i
+            idx += [(a, b, c), (a, c, d)] if (i + j) % 2 else [(a, b, d), (b, c, d)]
+    return clip, np.array(idx, np.uint32)
+
+
+def test_raster_is_watertight_and_covers_each_sample_once():
+    """Shared edges of a jittered grid: every sample inside the grid is covered by exactly one triangle (no cracks, no
+    double hits), counted by drawing each triangle alone."""
+    clip, idx = _grid_mesh(9, 7, jitter=0.08, seed=3)
+    W, H = 61, 47
+    cover = np.zeros((H, W, 4), np.int32)
+    for t in range(len(idx)):
+        k = O.raster(clip, idx, W, H, 4, t0=t, nt=1)
+        cover += (k != np.uint64(2**64 - 1)).astype(np.int32)
+    # samples well inside the grid's outline
+    ys, xs = np.mgrid[0:H, 0:W]
+    offs = np.array([[0.375, 0.125], [0.875, 0.375], [0.125, 0.625], [0.625, 0.875]])
+    inside = np.ones((H, W, 4), bool)
+    for s in range(4):
+        nx = 2 * (xs + offs[s, 0]) / W - 1
+        ny = 1 - 2 * (ys + offs[s, 1]) / H
+        inside[..., s] = (np.abs(nx) < 0.88) & (np.abs(ny) < 0.88)
+    assert cover[inside].min() == 1 and cover[inside].max() == 1, np.unique(cover[inside], return_counts=True)
+    # and drawn together every such sample holds one of the triangles
+    k = O.raster(clip, idx, W, H, 4)
+    assert (k[inside] != np.uint64(2**64 - 1)).all()
+
+
+def test_raster_depth_order_ties_and_clipping():
+    """'less' depth: the nearer triangle wins wherever both cover; on equal depth the one drawn first; samples
+    beyond the far plane, behind the near plane or at depth 1 stay empty; a triangle crossing w = 0 keeps its
+    visible part."""
+    quad = lambda z, w=1.0: np.array([[-w, -w, z, w], [w, -w, z, w], [w, w, z, w], [-w, w, z, w]], np.float32)
+    I2 = np.array([[0, 1, 2], [0, 2, 3], [4, 5, 6], [4, 6, 7]], np.uint32)
+    E = np.uint64(2**64 - 1)
+    k = O.raster(np.concatenate([quad(0.6), quad(0.3)]), I2, 16, 12, 4)
+    assert set(np.unique(k & np.uint64(0xffffffff)).tolist()) <= {2, 3}
+    k = O.raster(np.concatenate([quad(0.4), quad(0.4)]), I2, 16, 12, 4)
+    assert set(np.unique(k & np.uint64(0xffffffff)).tolist()) <= {0, 1}
+    for z in (1.0, 1.2, -0.1):
+        assert (O.raster(quad(z), I2[:2], 16, 12, 4) == E).all(), z
+    # one vertex behind the camera (w < 0): the visible part is drawn, nothing from the part behind
+    clip = np.array([[-0.5, -0.5, 0.5, 1.0], [0.5, -0.5, 0.5, 1.0], [0.0, 0.2, -0.5, -0.5]], np.float32)
+    k = O.raster(clip, np.array([[0, 1, 2]], np.uint32), 32, 32, 4)
+    assert (k != E).sum() > 100
+    d = np.frombuffer(((k[k != E] >> np.uint64(32)).astype(np.uint32)).tobytes(), np.float32)
+    assert d.min() >= 0.0 and d.max() < 1.0
+
+
+def test_slice_tris_bounds_area_and_shared_vertices():
+    """sliceTris (lite_nodes/renderer.js:443): every piece spans at most h per axis, the area is kept, and the cut
+    points shared by neighbouring pieces are bit-identical (each sliced capsule stays closed: no edge is used by an
+    odd number of triangles)."""
+    sc = dome.make_scope_scene(level=3, n_tools=1, width=64, height=36)
+    S = O.Scene(sc)
+    V, I = S.lite_geometry(subdiv=0.003, subdiv_fixture=0.01)
+    ns = len(sc["static"]["P"])
+    dyn = V[ns:]
+    P = dyn[:, :3].view(np.float32).astype(np.float64)
+    tris = I[len(sc["static"]["I"]):] - ns
+    ext = P[tris].max(axis=1) - P[tris].min(axis=1)
+    assert ext.max() <= 0.003 + 1e-7, ext.max()   # float32 positions: a few ulps at 0.2 m
+    area = lambda p, t: 0.5 * np.linalg.norm(np.cross(p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]]), axis=1).sum()
+    b = sc["bodies"][1]
+    assert abs(area(P, tris[(dyn[tris[:, 0], 3] >> 16) == 1]) - area(b["P"].astype(np.float64), b["I"])) < 1e-4 * area(b["P"].astype(np.float64), b["I"])
+    # closed surface after slicing: undirected edges keyed by the vertices' exact bits
+    tool = tris[(dyn[tris[:, 0], 3] >> 16) == 1]
+    key = {tuple(dyn[v, :3]) for v in tool.ravel()}
+    ids = {k: i for i, k in enumerate(sorted(key))}
+    e = {}
+    for t in tool:
+        a, bb, c = (ids[tuple(dyn[v, :3])] for v in t)
+        for u, w in ((a, bb), (bb, c), (c, a)):
+            if u != w:
+                e[(min(u, w), max(u, w))] = e.get((min(u, w), max(u, w)), 0) + 1
+    counts = np.array(list(e.values()))
+    # no open edge (a crack would leave an edge used once; collinear cut points make some edges shared 4 or 6 times)
+    assert (counts % 2 == 0).all(), np.unique(counts, return_counts=True)
+
+
+def test_lite_emitter_samples_are_stratified_and_posed():
+    """The 96 outlet samples (lite_nodes/renderer.js:598): on the emitter, balanced over the 4 sectors, and moved
+    rigidly by the scope pose."""
+    sc = dome.make_scope_scene(level=3, n_tools=0, width=64, height=36)
+    S = O.Scene(sc)
+    es0, sc0 = S.lite_emitter(96, np.eye(4).T.ravel())
+    assert np.allclose(es0[:, 2], 0.0, atol=1e-7) and (np.hypot(es0[:, 0], es0[:, 1]) <= 0.004 + 1e-6).all()
+    cnt = np.bincount(es0[:, 3].astype(int), minlength=4)
+    assert cnt.min() >= 20, cnt
+    T = dome.scope_poses(1, 0, seed=5)[0, 0].reshape(4, 4).T
+    es1, _ = S.lite_emitter(96, T.T.ravel())
+    want = (T[:3, :3] @ es0[:, :3].astype(np.float64).T).T + T[:3, 3]
+    assert np.abs(es1[:, :3] - want).max() < 1e-6
+    assert np.array_equal(es1[:, 3], es0[:, 3]) and np.allclose(es1[:, 7], es0[:, 7])

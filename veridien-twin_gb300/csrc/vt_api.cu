@@ -119,6 +119,10 @@ vt_status vt_destroy(vt_ctx* ctx) {
   for (cudaEvent_t e : ctx->nev)
     if (e) cudaEventDestroy(e);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+  cudaFree(ctx->lite.mem);
+  for (auto& c : ctx->lite.cams) cudaFree(c.mem);
+  for (cudaEvent_t e : ctx->lite.ev)
+    if (e) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -165,6 +169,11 @@ vt_status vt_set_poses(vt_ctx* ctx, const double* T0, const double* T1, uint32_t
   if (n_bodies && !T0) return fail(ctx, VT_ERR_ARG, "poses: T0 is null");
   ctx->inst = vt::poses_from(ctx->S, T0, T1, n_bodies);
   ctx->nodes.poses_version++;
+  {
+    const int sc = ctx->S.scope_index;
+    const bool have = sc >= 0 && uint32_t(sc) < n_bodies && T0 && !std::isnan(T0[16 * size_t(sc)]);
+    for (int k = 0; k < 16; k++) ctx->scope_T[k] = have ? T0[16 * size_t(sc) + k] : (k % 5 == 0 ? 1.0 : 0.0);
+  }
   return write_su(ctx);
 }
 

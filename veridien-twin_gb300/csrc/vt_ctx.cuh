@@ -12,6 +12,7 @@
 #include "vt_host.h"
 #include "vt_kernels.cuh"
 #include "vt_isp.cuh"
+#include "vt_lite.cuh"
 #include "vt_wave.cuh"
 
 struct vt_ctx {
@@ -143,6 +144,44 @@ struct vt_ctx {
     bool timed_direct = false, timed_jacobi = false;
     uint32_t last_steps = 0;
   } nodes;
+  // the scope body's poses0 matrix (column-major), kept for the raster pass's emitter samples and SCOPE camera
+  double scope_T[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  // the raster camera pass (vt_lite_*): geometry, emitter samples, shadow maps, per-camera targets
+  struct Lite {
+    bool ready = false;
+    vt_lite_opts o{};
+    uint32_t n_verts = 0, n_tris = 0, n_static_verts = 0, n_static_tris = 0, dyn_verts = 0;
+    vt::LiteEmit em;
+    void* mem = nullptr;                 // geometry, emitter samples, clip buffers, big-triangle queue, shadow maps
+    uint4* v = nullptr;
+    uint32_t* idx = nullptr;
+    float4* es = nullptr;
+    float4* clip = nullptr;              // camera pass (n_verts)
+    float4* sclip = nullptr;             // shadow passes (K_SECT x n_verts)
+    uint32_t* big = nullptr;             // 1 + big_cap words
+    uint32_t big_cap = 0;
+    uint32_t *sm_static = nullptr, *sm_dyn = nullptr;
+    bool sm_static_dirty = true;
+    uint64_t sm_dyn_version = ~0ull;
+    std::vector<double> scope_key;
+    double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, P[3] = {0, 0, 0};   // scope pose of the current state
+    float axisW[3] = {0, 0, 1}, lt[3] = {1, 0, 0}, lb[3] = {0, 1, 0}, lo[4][3] = {};
+    double scopeR[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, scope_pos[3] = {0, 0, 0};
+    struct LCam {
+      uint32_t W = 0, H = 0;
+      void* mem = nullptr;
+      unsigned long long* key = nullptr;
+      float4* rad = nullptr;
+      uchar4* out = nullptr;
+      uint32_t* stats = nullptr;
+      bool rendered = false, displayed = false;
+    };
+    std::vector<LCam> cams;              // the scene cameras, then SCOPE
+    int32_t last_clip_cam = -1;
+    double build_ms = 0, sm_static_ms = 0, sm_dyn_ms = 0, cam_ms = 0;
+    uint32_t big_tris = 0, launches = 0;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  } lite;
 };
 
 namespace vtapi {

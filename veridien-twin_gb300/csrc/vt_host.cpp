@@ -462,7 +462,7 @@ void capsule_fit(const float* P, size_t n, double a[3], double b[3], double& r) 
   for (int k = 0; k < 3; k++) { a[k] = c[k] + smin * ax[k]; b[k] = c[k] + smax * ax[k]; }
 }
 
-struct Emit { double v0[3], e1[3], e2[3], n[3], area, cdf; };
+using Emit = EmitTri;
 
 // one 64-byte triangle record (v0|i0, e1|i1, e2|i2, mesh, flags, -, -)
 void tri_record(uint32_t* rec, const float* P, const uint32_t* tri, uint32_t i0, uint32_t i1, uint32_t i2, uint32_t mesh, uint32_t flags) {
@@ -646,6 +646,7 @@ Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_sa
   }
   S.emit_area = total;
   S.emit_tris = uint32_t(emit.size());
+  S.emitters = emit;
   // body capsules and effective albedo (scene_gpu.js:431-456); no overview-only meshes, so occlusion = bounding capsule
   for (uint32_t b = 0; b < d.n_bodies; b++) {
     const vt_body_desc& B = d.bodies[b];

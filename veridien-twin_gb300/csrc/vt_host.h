@@ -42,6 +42,9 @@ struct BodyRec {
   double cap_a[3], cap_b[3], cap_r = 0, occ_a[3], occ_b[3], occ_r = 0, rho_eff = 0;
 };
 
+// an emitter triangle in its body's frame with its area CDF (gpu/scene_gpu.js emitter.tris)
+struct EmitTri { double v0[3], e1[3], e2[3], n[3], area, cdf; };
+
 struct Prepared {
   std::vector<uint32_t> nodes, tris, verts;   // 16, 16, 8 words per item
   std::vector<float> params;                  // vec4 array
@@ -53,6 +56,7 @@ struct Prepared {
   std::vector<Material> mats;
   std::vector<vt_mesh> meshes;
   std::vector<vt_camera_desc> cams;
+  std::vector<EmitTri> emitters;
   double emit_area = 0, emit_axis[3] = {0, 0, 1}, emit_normal[3] = {0, 0, 1}, emit_centroid[3] = {0, 0, 0}, emit_radius = 0;
   bool shadow_skips_scope = false;
   int scope_index = -1;
@@ -84,5 +88,30 @@ void node_neighbours(const Prepared& S, const std::vector<uint32_t>& active, uin
                      std::vector<uint32_t>& out);
 // gpu/renderer.js:635 _poseAt
 bool pose_at(const InstPose& I, double t, double R[3][3], double p[3]);
+
+// ------------------------------------------------------------------------ the raster camera pass (lite_nodes)
+// lite_nodes/renderer.js:443 sliceTris: cut a mesh by the planes x = k h, y = k h, z = k h (one axis after the other)
+// so no triangle spans more than h along any axis; crossings are computed from canonically ordered endpoints, so
+// triangles that share an edge get bit-identical new vertices. In: positions / normals (3 per vertex, double),
+// indices; out: an unindexed triangle list (3 vertices per triangle).
+void slice_tris(const std::vector<double>& P, const std::vector<double>& N, const std::vector<uint32_t>& I, double h,
+                std::vector<double>& P2, std::vector<double>& N2);
+// lite_nodes/renderer.js:527 _buildGeometry: the raster vertices (8 words: position | mesh + instance << 16,
+// normal | node; the static part is the scene's static vertices, instance 0xffff, node = vertex) and triangles (the
+// static triangles in packed order, then every posed body's triangles mesh by mesh, sliced to h (fixtures: h_fixture))
+struct LiteGeom {
+  std::vector<uint32_t> v;      // 8 words per vertex
+  std::vector<uint32_t> idx;    // 3 per triangle
+  uint32_t n_static_verts = 0, n_static_tris = 0, n_verts = 0, n_tris = 0;
+};
+LiteGeom lite_geometry(const Prepared& S, double h, double h_fixture);
+// lite_nodes/renderer.js:598 _buildEmitterSamples: n stratified area samples of the emitter (scope frame), each in
+// one of 4 sectors about the emitter's centroid, and the sectors' centroids
+struct LiteEmit {
+  std::vector<double> p, n;     // 3 per sample
+  std::vector<uint32_t> sect;
+  double sect_c[4][3];
+};
+LiteEmit lite_emitter_samples(const Prepared& S, uint32_t n);
 
 }  // namespace vt

@@ -427,4 +427,59 @@ void launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
   isp_stats_kernel<<<1, 1024, 0, st>>>(b.part, go.x * go.y, 0, 1, b.stats);
 }
 
+// ------------------------------------------------------------------------------------- the raster pass's display
+// lite_nodes/renderer.js:369 DISPLAY (the lite renderer's sensor look): scaled luma of every 4th pixel in x and y
+// summed for the next frame's exposure; exposure gain, the KB4 cameras' cos-like falloff, veiling glare as the
+// previous frame's global mean, white balance, sRGB and S-curve into rgba8. The sums are per-warp reductions added
+// once per warp: integer, so independent of the order.
+__global__ void __launch_bounds__(256) lite_display_kernel(const LiteDisplay P, const float4* __restrict__ L, uchar4* __restrict__ out,
+                                                           uint32_t* __restrict__ stats) {
+  const uint32_t x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+  uint32_t sy = 0, cnt = 0;
+  if (x < P.W && y < P.H) {
+    const float4 l = L[size_t(y) * P.W + x];
+    if ((x & 3u) == 0u && (y & 3u) == 0u) {
+      const float yl = l.x * 0.2126f + l.y * 0.7152f + l.z * 0.0722f;
+      sy = __float2uint_rz(fminf(fmaxf(yl * P.du[3], 0.0f), 65535.0f));
+      cnt = 1;
+    }
+    const float n = fmaxf(float(P.prev[1]), 1.0f);
+    const float mean = float(P.prev[0]) / fmaxf(P.du[3], 1e-30f) / n;
+    float E[3] = {l.x, l.y, l.z};
+    if (P.du[12] > 0.0f) {
+      const float qx = (float(x) + 0.5f - P.du[14]) / P.du[12], qy = (float(y) + 0.5f - P.du[15]) / P.du[13];
+      const float c = clamp01(sqrtf(qx * qx + qy * qy) / 1.1f);
+      const float t = c * c;
+      const float f = 1.0f * (1.0f - t) + 0.57f * t;
+      for (int k = 0; k < 3; k++) E[k] = E[k] * f;
+    }
+    const float g = P.du[1], b = P.du[9], sc = P.du[8];
+    uint8_t o[3];
+    for (int k = 0; k < 3; k++) {
+      const float e = (1.0f - g) * E[k] + g * mean;
+      const float xv = e * P.du[0] * P.du[4 + k];
+      const float v = clamp01((xv - b) / (1.0f - b));
+      float t = srgb_oetf(v);
+      if (sc > 0.0f) {
+        const float a = vt_powf(clamp01(t), sc);
+        t = a / (a + vt_powf(clamp01(1.0f - t), sc));
+      }
+      o[k] = uint8_t(__float2uint_rn(t * 255.0f));
+    }
+    out[size_t(y) * P.W + x] = make_uchar4(o[0], o[1], o[2], 255);
+  }
+  sy = __reduce_add_sync(0xffffffffu, sy);
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
+  if (threadIdx.x == 0 && cnt) {
+    atomicAdd(stats, sy);
+    atomicAdd(stats + 1, cnt);
+  }
+}
+
+void launch_lite_display(const LiteDisplay& P, const float4* L, uchar4* out, uint32_t* stats, cudaStream_t st) {
+  cudaMemsetAsync(stats, 0, 16, st);
+  const dim3 blk(32, 8), g((P.W + 31) / 32, (P.H + 7) / 8);
+  lite_display_kernel<<<g, blk, 0, st>>>(P, L, out, stats);
+}
+
 }  // namespace vtk

@@ -23,4 +23,9 @@ struct IspBufs {
 // the whole chain for one frame of the uniform's size
 void launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st);
 
+// the raster pass's display look (vt_lite_display): du as lite_nodes/renderer.js:892 writes it, the previous frame's
+// statistics; stats receives this frame's (luma sum, count)
+struct LiteDisplay { float du[20]; uint32_t prev[4]; uint32_t W, H; };
+void launch_lite_display(const LiteDisplay& P, const float4* L, uchar4* out, uint32_t* stats, cudaStream_t st);
+
 }  // namespace vtk

@@ -153,6 +153,23 @@ class vt_nodes_opts(C.Structure):
                 ("iters_initial", C.c_uint32), ("per_step_factors", C.c_uint32)]
 
 
+class vt_lite_opts(C.Structure):
+    _fields_ = [("ns_static", C.c_uint32), ("ns_dyn", C.c_uint32), ("sm_res", C.c_uint32), ("scope_width", C.c_uint32),
+                ("scope_height", C.c_uint32), ("env_material", C.c_uint32), ("debug", C.c_uint32), ("reserved", C.c_uint32),
+                ("sm_theta_max_deg", C.c_double), ("far_m", C.c_double), ("subdiv_h", C.c_double), ("subdiv_fixture", C.c_double),
+                ("scope_hfov_deg", C.c_double), ("scope_circle_frac", C.c_double), ("scope_view_dir", C.c_double * 3),
+                ("scope_objective", C.c_double * 3)]
+
+
+class vt_lite_info(C.Structure):
+    _fields_ = [("raster_tris", C.c_uint32), ("static_tris", C.c_uint32), ("dyn_verts", C.c_uint32), ("n_cameras", C.c_uint32),
+                ("build_ms", C.c_double), ("shadow_static_ms", C.c_double), ("shadow_dyn_ms", C.c_double), ("camera_ms", C.c_double),
+                ("big_tris", C.c_uint32), ("launches", C.c_uint32)]
+
+
+VT_LITE_VIEW, VT_LITE_CLIP, VT_LITE_KEYS, VT_LITE_SM_STATIC, VT_LITE_SM_DYN, VT_LITE_SM_CLIP, VT_LITE_GEOM, VT_LITE_INDEX, VT_LITE_EMIT = range(9)
+
+
 class vt_nodes_info(C.Structure):
     _fields_ = [("n_nodes", C.c_uint32), ("n_active", C.c_uint32), ("gather_k", C.c_uint32), ("nbr_k", C.c_uint32),
                 ("build_ms", C.c_double), ("neighbour_ms", C.c_double), ("table_entries", C.c_uint64)]

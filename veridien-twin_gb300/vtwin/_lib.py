@@ -32,6 +32,15 @@ SIGNATURES = {
     "vt_sensor_camera": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_float]),
     "vt_sensor_frame": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_void_p]),
     "vt_render_frame": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_frame_req)]),
+    "vt_lite_create": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_lite_opts), C.POINTER(A.vt_lite_info)]),
+    "vt_lite_info_get": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_lite_info)]),
+    "vt_lite_geometry": (C.c_int32, [C.POINTER(A.vt_scene_desc), C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_lite_render_camera": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vt_lite_display": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_lite_readback": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_size_t]),
+    "vt_lite_debug": (C.c_int32, [C.c_void_p, C.c_int, C.c_uint32, C.c_void_p, C.c_size_t]),
+    "vt_raster": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                              C.c_void_p]),
     "vt_set_relative_illumination": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_uint32]),
     "vt_get_relative_illumination": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_calib_setup": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_calib_desc), C.POINTER(A.vt_calib_info)]),

@@ -22,9 +22,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr"]
 
 
-# per-file flags: the sensor chain is compiled without multiply-add contraction, so its arithmetic is the sequence of
-# separately rounded operations that the CPU restatement performs
-EXTRA = {"vt_isp.cu": ["--fmad=false"]}
+# per-file flags: the sensor chain and the rasteriser are compiled without multiply-add contraction, so their
+# arithmetic is the sequence of separately rounded operations that the CPU restatement performs
+EXTRA = {"vt_isp.cu": ["--fmad=false"], "vt_lite.cu": ["--fmad=false"]}
 
 
 def nvcc() -> str:

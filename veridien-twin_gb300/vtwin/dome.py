@@ -192,7 +192,7 @@ def torus_geometry(centre, R=0.35, r=0.04, nmaj=8, nmin=3):
 
 
 def capsule_geometry(radius=0.006, length=0.25, nring=20, nseg=14, ncap=8):
-    """Capsule along +z from 0 to `length`, radius `radius`, 600 triangles by default (instrument meshes)."""
+    """Capsule along +z from 0 to `length`, radius `radius`, 1240 triangles by default (instrument meshes)."""
     P, N = [], []
     rows = []  # (z, rho, nz)
     for k in range(ncap, 0, -1):  # bottom hemisphere rings (pole excluded)
@@ -270,7 +270,7 @@ def make_dome_scene(seed: int = 1, width=640, height=480, level=5, with_instrume
     """Config-0 dome: ~10.2k dome + 1984 floor + 12 table + 96 lamp triangles, 8 Lambertian materials
     (rho ~ U[0.2, 0.8] per channel from mulberry32(seed)), one KB4 camera, lamps L0 = 50 W sr^-1 m^-2, p = 1.
 
-    with_instruments > 0 adds that many 600-triangle capsule bodies (kind 'instrument', radius `tool_radius`, length
+    with_instruments > 0 adds that many 1240-triangle capsule bodies (kind 'instrument', radius `tool_radius`, length
     0.25 m), posed by set_poses."""
     rng = Rng(seed)
     mats = [lambertian(f"mat{i}", [rng.uniform(0.2, 0.8) for _ in range(3)]) for i in range(8)]
@@ -316,6 +316,96 @@ def make_dome_scene(seed: int = 1, width=640, height=480, level=5, with_instrume
     emitter = {"L0": [50.0, 50.0, 50.0], "theta": [0.0, math.pi], "p": [1.0, 1.0], "axis_deg": 0.0}
     return {"static": st, "bodies": bodies, "meshes": meshes, "materials": mats, "emitter": emitter,
             "cameras": [cam]}
+
+
+def disk_geometry(radius, n=24, z=0.0):
+    """Flat disk at height z facing +z: a fan of n triangles about its centre."""
+    P = [(0.0, 0.0, z)] + [(radius * math.cos(2 * math.pi * k / n), radius * math.sin(2 * math.pi * k / n), z) for k in range(n)]
+    I = [(0, 1 + k, 1 + (k + 1) % n) for k in range(n)]
+    N = [(0.0, 0.0, 1.0)] * len(P)
+    return np.array(P, np.float32), np.array(N, np.float32), np.array(I, np.uint32)
+
+
+def make_scope_scene(seed: int = 1, level: int = 7, n_tools: int = 6, width: int = 1280, height: int = 720, n_cams: int = 3,
+                     radius: float = 0.35):
+    """A dome at the scale of the twin's own (lite_nodes draws it: radius 0.35 m, 3 mm nodes at level 7, depth range
+    1 m): hemisphere + floor disk + a 16 x 12 x 3 cm pad (big triangles), a scope body (kind 'scope': a 5 mm shaft
+    along -z ending in a 4 mm emitting outlet at its origin that faces +z, emission profile falling to 0 at 55 deg),
+    `n_tools` 2.5 mm x 0.2 m instrument capsules and `n_cams` KB4 cameras on the dome wall looking at the pad (fx
+    ~ U[550, 650] at 1920 px, k_i ~ N(0, 0.02)). Poses: scope_poses."""
+    rng = Rng(seed)
+    mats = [lambertian(f"pla{i}", [rng.uniform(0.6, 0.9) for _ in range(3)]) for i in range(4)]
+    mats.append(lambertian("floor", [0.35, 0.35, 0.38]))
+    mats.append(lambertian("pad", [0.7, 0.3, 0.3]))
+    meshes, static = [], []
+    S = MESH_FLAG["STATIC"]
+
+    def add_static(name, mat, geo):
+        meshes.append({"name": name, "mat": mat, "flags": S, "build_dir": [0.0, 0.0, 1.0], "layer": [0.0, 0.0]})
+        static.append((len(meshes) - 1, geo))
+
+    for qi, g in enumerate(dome_geometry(radius=radius, level=level)):
+        add_static(f"dome_q{qi}", qi, g)
+    fin, fout = floor_geometry(radius=radius, rings=64, seg=256)
+    add_static("floor_in", 4, fin)
+    add_static("floor_out", 4, fout)
+    top, sides = box_geometry((-0.08, -0.06, 0.0), (0.08, 0.06, 0.03))
+    add_static("pad_top", 5, top)
+    add_static("pad_sides", 5, sides)
+    mats.append(lambertian("bench_white", [0.5, 0.5, 0.5]))
+    mats.append(emitter_material())
+    em = len(mats) - 1
+    steel = len(mats)
+    mats.append({**lambertian("steel", [0.0, 0.0, 0.0]), "metallic": 1, "f0": [0.56, 0.57, 0.58], "roughness": 0.35, "ior": 1.5})
+    meshes.append({"name": "scope_shaft", "mat": steel, "flags": MESH_FLAG["SCOPE"], "build_dir": [0.0, 0.0, 1.0], "layer": [0.0, 0.0]})
+    sp, sn, si = capsule_geometry(radius=0.005, length=0.3)
+    sp = sp.copy()
+    sp[:, 2] -= 0.3 + 0.0052
+    meshes.append({"name": "scope_outlet", "mat": em, "flags": MESH_FLAG["EMITTER"] | MESH_FLAG["SCOPE"],
+                   "build_dir": [0.0, 0.0, 1.0], "layer": [0.0, 0.0]})
+    bodies = [_body("scope", "scope", [(len(meshes) - 2, (sp, sn, si)), (len(meshes) - 1, disk_geometry(0.004))])]
+    cap = capsule_geometry(radius=0.0025, length=0.2)
+    for k in range(n_tools):
+        meshes.append({"name": f"tool{k}", "mat": steel, "flags": MESH_FLAG["INSTRUMENT"], "build_dir": [0.0, 0.0, 1.0],
+                       "layer": [0.0, 0.0]})
+        bodies.append(_body(f"tool{k}", "instrument", [(len(meshes) - 1, cap)]))
+    cams = []
+    for c in range(n_cams):
+        a = 2 * math.pi * c / n_cams - math.pi / 2
+        pos = (0.3 * math.cos(a), 0.3 * math.sin(a), 0.12)
+        fx = rng.uniform(550, 650) * width / 1920.0
+        fy = fx * (1 + 0.004 * (rng.u() - 0.5))
+        k = [rng.normal(0, 0.02) for _ in range(4)]
+        cams.append(kb4_camera(f"CAM{c + 1}", (width, height), fx, fy, (width - 1) / 2.0, (height - 1) / 2.0, k,
+                               look_at(pos, (0.0, 0.0, 0.04))))
+    th = [math.radians(x) for x in (0.0, 10.0, 25.0, 40.0, 50.0, 55.0)]
+    emitter = {"L0": [2.0e4, 1.9e4, 1.7e4], "theta": th, "p": [1.0, 0.97, 0.75, 0.35, 0.08, 0.0], "axis_deg": 0.0}
+    return {"static": _concat_static(static), "bodies": bodies, "meshes": meshes, "materials": mats, "emitter": emitter,
+            "cameras": cams}
+
+
+def scope_poses(n_poses=16, n_tools=6, seed=21):
+    """(n_poses, 1 + n_tools, 16) column-major body transforms for make_scope_scene: the scope tip 12-18 cm above
+    the pad pointing down within 20 deg of vertical, the tools rotated uniformly about points 4-12 cm above it."""
+    rng = Rng(seed)
+    out = np.zeros((n_poses, 1 + n_tools, 16), np.float64)
+    for p in range(n_poses):
+        tilt, az = math.radians(20.0) * rng.u(), 2 * math.pi * rng.u()
+        d = np.array([math.sin(tilt) * math.cos(az), math.sin(tilt) * math.sin(az), -math.cos(tilt)])   # +z of the scope
+        x = np.cross([0.0, 1.0, 0.0], d)
+        x /= np.linalg.norm(x)
+        y = np.cross(d, x)
+        T = np.eye(4)
+        T[:3, 0], T[:3, 1], T[:3, 2] = x, y, d
+        T[:3, 3] = [rng.uniform(-0.03, 0.03), rng.uniform(-0.03, 0.03), rng.uniform(0.12, 0.18)]
+        out[p, 0] = T.T.ravel()
+        for t in range(n_tools):
+            R = random_rotation(rng)
+            T = np.eye(4)
+            T[:3, :3] = R
+            T[:3, 3] = [rng.uniform(-0.06, 0.06), rng.uniform(-0.06, 0.06), rng.uniform(0.04, 0.12)]
+            out[p, 1 + t] = T.T.ravel()
+    return out
 
 
 def _body(key, kind, parts):
