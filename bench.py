@@ -589,7 +589,7 @@ def lite_frame_bench(torch, device=0, level=7, frames=12, warmup=3):
     t0 = time.perf_counter()
     r = LiteNodesRenderer.create(sc, device=device)
     load_ms = (time.perf_counter() - t0) * 1e3
-    wall, cam_ms, dyn_ms, stat_ms = [], [], [], []
+    wall, cam_ms, dyn_ms, stat_ms, ras_ms, sh_ms = [], [], [], [], [], []
     for k in range(frames + warmup):
         p = poses[k].copy()
         p[0] = poses[(k // 4) * 4][0]                  # the scope moves every fourth frame
@@ -604,15 +604,19 @@ def lite_frame_bench(torch, device=0, level=7, frames=12, warmup=3):
         if k >= warmup:
             wall.append((time.perf_counter() - t) * 1e3)
             cam_ms.append(sum(x["cameraMs"] for x in per))
+            ras_ms.append(sum(x["cameraRasterMs"] for x in per))
+            sh_ms.append(sum(x["cameraShadeMs"] for x in per))
             dyn_ms.append(sum(x["shadowDynMs"] for x in per))
             if any(x["shadowStaticMs"] > 0 for x in per):
                 stat_ms.append(sum(x["shadowStaticMs"] for x in per))
     out = {"workload": f"3 KB4 cameras + SCOPE at 1280x720, 4x MSAA raster, 4 sector shadow maps 2048^2, scope-scale dome level {level} "
                        f"({r.stats['staticTris']} static + {r.stats['rasterTris'] - r.stats['staticTris']} sliced posed-body triangles)",
            "ms_per_frame": float(np.median(wall)), "camera_pass_ms_per_frame": float(np.median(cam_ms)),
-           "camera_pass_ms_per_view": float(np.median(cam_ms)) / 4, "shadow_dynamic_ms": float(np.median(dyn_ms)),
+           "camera_pass_ms_per_view": float(np.median(cam_ms)) / 4, "raster_ms_per_view": float(np.median(ras_ms)) / 4,
+           "shade_ms_per_view": float(np.median(sh_ms)) / 4, "shadow_dynamic_ms": float(np.median(dyn_ms)),
            "shadow_static_ms": float(np.median(stat_ms)) if stat_ms else None, "load_ms": load_ms,
-           "nodes": r.tr.nodes_info["activeNodes"], "big_tris_last": r.info()["bigTris"]}
+           "nodes": r.tr.nodes_info["activeNodes"], "camera_big_tiles_last": r.info()["bigTiles"],
+           "shadow_big_tiles_last": r.info()["shadowBigTiles"]}
     r.destroy()
     return out
 

@@ -522,8 +522,10 @@ typedef struct {
   uint32_t raster_tris, static_tris, dyn_verts, n_cameras;   /* n_cameras = scene cameras + SCOPE (the last) */
   double build_ms;
   double shadow_static_ms, shadow_dyn_ms, camera_ms;          /* device ms of the last render's passes */
-  uint32_t big_tris, launches;                                /* triangles of the last camera pass rasterised by
-                                                                 the many-pixel path; kernel launches */
+  double camera_raster_ms, camera_shade_ms;                   /* the camera pass: vertices + raster, fragments */
+  uint32_t big_tris, launches;                                /* tiles queued for the many-pixel path by the last
+                                                                 camera pass; kernel launches */
+  uint32_t shadow_big_tiles, reserved;                        /* tiles queued by the last dynamic shadow pass */
 } vt_lite_info;
 /* lite_nodes/renderer.js:497 _init (geometry :527, emitter samples :598, cameras :696). Needs vt_nodes_build. */
 vt_status vt_lite_create(vt_ctx* ctx, const vt_lite_opts* opts, vt_lite_info* info);

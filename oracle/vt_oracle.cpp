@@ -2584,9 +2584,11 @@ template <typename F> static void parallel_for(size_t n, int threads, F&& f) {
 // lite_nodes/renderer.js restated for the CPU: the raster geometry (sliceTris :443, _buildGeometry :527), the
 // emitter samples (:598, posed by setPoses :729), the vertex stage (vsCam / vsShadow :224-265), a rasteriser with
 // the rules the library documents (clip 0 <= z <= w and |x|, |y| <= 8 w; 1/256-pixel snap; int64 edge functions,
-// ties to the edge with dy < 0 or dy = 0 and dx > 0; screen-linear depth clamped to [0, 1] and kept below 1 and
+// ties to the edge with dy < 0 or dy = 0 and dx > 0; screen-linear depth (edge weights times one reciprocal of the
+// doubled area) clamped to [0, 1] and kept below 1 and
 // below the sample's, ties to the earlier triangle), the fragment stage (fsCam :284, smVis :267) with the MSAA
-// resolve through half floats and FINISH (:363), and the display look (DISPLAY :369). Float32 arithmetic in the
+// resolve through half floats and FINISH (:363), and the display look (DISPLAY :369); the 3x3 shadow taps one texel
+// apart share the centre tap's bilinear fraction. Float32 arithmetic in the
 // order the kernels use (this file is built with -ffp-contract=off), so raster keys, shadow maps and display bytes
 // compare bit for bit, radiance to float rounding.
 
@@ -2868,7 +2870,7 @@ static void raster(const float* clip, const uint32_t* idx, uint32_t t0, uint32_t
       }
       const long long x0 = std::max(0LL, fdiv256(std::min(a.x, std::min(b.x, c.x)))), x1 = std::min((long long)W - 1, fdiv256(std::max(a.x, std::max(b.x, c.x))));
       const long long y0 = std::max(0LL, fdiv256(std::min(a.y, std::min(b.y, c.y)))), y1 = std::min((long long)H - 1, fdiv256(std::max(a.y, std::max(b.y, c.y))));
-      const float fA = float(A);
+      const float rA = 1.0f / float(A);
       for (long long py = y0; py <= y1; py++)
         for (long long px = x0; px <= x1; px++)
           for (uint32_t s = 0; s < samples; s++) {
@@ -2877,7 +2879,7 @@ static void raster(const float* clip, const uint32_t* idx, uint32_t t0, uint32_t
             bool in = true;
             for (int e = 0; e < 3; e++) { w[e] = dx[e] * (sy - oy[e]) - dy[e] * (sx - ox[e]); in = in && w[e] + bias[e] >= 0; }
             if (!in) continue;
-            const float l1 = float(w[1]) / fA, l2 = float(w[2]) / fA;
+            const float l1 = float(w[1]) * rA, l2 = float(w[2]) * rA;
             float z = a.z + l1 * (b.z - a.z) + l2 * (c.z - a.z);
             z = std::min(z, 1.0f);
             if (!(z > 0.0f)) z = 0.0f;
@@ -2900,22 +2902,13 @@ static float h16(float x) {
   if (std::fabs(r) > 65504.0) return x > 0 ? INFINITY : -INFINITY;
   return float(r);
 }
-static float texel(const uint32_t* m, uint32_t res, int k, int x, int y) {
+// depth compare of one texel (clamp to edge; all ones = cleared = depth 1)
+static int less_texel(const uint32_t* m, uint32_t res, int k, int x, int y, float dref) {
   x = std::min(std::max(x, 0), int(res) - 1);
   y = std::min(std::max(y, 0), int(res) - 1);
   const uint32_t b = m[(size_t(k) * res + y) * res + x];
-  return b == 0xffffffffu ? 1.0f : as_f(b);
+  return dref < (b == 0xffffffffu ? 1.0f : as_f(b)) ? 1 : 0;
 }
-static float cmp(const uint32_t* m, uint32_t res, int k, float u, float v, float dref) {
-  const float tx = u * float(res) - 0.5f, ty = v * float(res) - 0.5f;
-  const float fx0 = std::floor(tx), fy0 = std::floor(ty);
-  const float fx = tx - fx0, fy = ty - fy0;
-  const int x0 = int(fx0), y0 = int(fy0);
-  const float c00 = dref < texel(m, res, k, x0, y0) ? 1.0f : 0.0f, c10 = dref < texel(m, res, k, x0 + 1, y0) ? 1.0f : 0.0f;
-  const float c01 = dref < texel(m, res, k, x0, y0 + 1) ? 1.0f : 0.0f, c11 = dref < texel(m, res, k, x0 + 1, y0 + 1) ? 1.0f : 0.0f;
-  return (1.0f - fx) * (1.0f - fy) * c00 + fx * (1.0f - fy) * c10 + (1.0f - fx) * fy * c01 + fx * fy * c11;
-}
-
 struct Frag {
   Tracer<float>& tr;
   Shader<float>& sh;
@@ -2927,15 +2920,28 @@ struct Frag {
   const uint32_t *sms, *smd;
   uint32_t res;
 
+  // smVis: 3x3 taps one texel apart, each a bilinear blend of 2x2 depth compares ('less', clamp to edge), min of
+  // the static and dynamic maps per tap; the taps share the centre tap's bilinear fraction
   float vis(const V3<float>& pw, int k, float bias) const {
     const V3<float> q = sm_project(V, pw, k);
     if (std::fabs(q.x) >= 1.0f || std::fabs(q.y) >= 1.0f) return 1.0f;
-    const float u = 0.5f + 0.5f * q.x, v = 0.5f - 0.5f * q.y, dref = (q.z - bias) / V.f[47], t = 1.0f / float(res);
+    const float u = 0.5f + 0.5f * q.x, v = 0.5f - 0.5f * q.y, dref = (q.z - bias) / V.f[47];
+    const float tx = u * float(res) - 0.5f, ty = v * float(res) - 0.5f;
+    const float fx0 = std::floor(tx), fy0 = std::floor(ty), fx = tx - fx0, fy = ty - fy0;
+    const int x0 = int(fx0) - 1, y0 = int(fy0) - 1;
+    int cs[4][4], cd[4][4];
+    for (int j = 0; j < 4; j++)
+      for (int i = 0; i < 4; i++) {
+        cs[j][i] = less_texel(sms, res, k, x0 + i, y0 + j, dref);
+        cd[j][i] = less_texel(smd, res, k, x0 + i, y0 + j, dref);
+      }
+    const float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy), w01 = (1.0f - fx) * fy, w11 = fx * fy;
     float s = 0.0f;
-    for (int j = -1; j <= 1; j++)
-      for (int i = -1; i <= 1; i++) {
-        const float ou = u + float(i) * t, ov = v + float(j) * t;
-        s = s + std::min(cmp(sms, res, k, ou, ov, dref), cmp(smd, res, k, ou, ov, dref));
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < 3; i++) {
+        const float a = w00 * float(cs[j][i]) + w10 * float(cs[j][i + 1]) + w01 * float(cs[j + 1][i]) + w11 * float(cs[j + 1][i + 1]);
+        const float b = w00 * float(cd[j][i]) + w10 * float(cd[j][i + 1]) + w01 * float(cd[j + 1][i]) + w11 * float(cd[j + 1][i + 1]);
+        s = s + std::min(a, b);
       }
     return s / 9.0f;
   }

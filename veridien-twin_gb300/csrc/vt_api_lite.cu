@@ -168,9 +168,9 @@ vt_status shadow_pass(vt_ctx* ctx, uint32_t which) {
   vtl::launch_vertex_shadow(S, g, v, v0, nv, L.sclip, ctx->stream);
   vtl::Target T{};
   T.W = L.o.sm_res; T.H = L.o.sm_res; T.samples = 1; T.depth = map; T.big = L.big; T.big_cap = L.big_cap;
-  vtl::launch_raster(L.sclip, L.idx, L.n_verts, t0, nt, vtl::K_SECT, T, big_blocks(ctx), ctx->stream);
+  vtl::launch_raster(L.sclip, L.ssnap, L.idx, L.n_verts, v0, nv, t0, nt, vtl::K_SECT, T, big_blocks(ctx), ctx->stream);
   VT_CK(cudaGetLastError());
-  L.launches += 4;
+  L.launches += 5;
   return VT_OK;
 }
 
@@ -237,10 +237,11 @@ vt_status vt_lite_create(vt_ctx* ctx, const vt_lite_opts* opts, vt_lite_info* in
   L.o = o;
   L.n_verts = gm.n_verts; L.n_tris = gm.n_tris; L.n_static_verts = gm.n_static_verts; L.n_static_tris = gm.n_static_tris;
   L.dyn_verts = gm.n_verts - gm.n_static_verts;
-  L.big_cap = gm.n_tris * vtl::K_SECT;
+  L.big_cap = std::max<uint32_t>(1u << 22, std::min<uint64_t>(uint64_t(gm.n_tris) * vtl::K_SECT * 2, 1u << 26));
   const size_t smb = size_t(vtl::K_SECT) * o.sm_res * o.sm_res * 4;
   const size_t bytes = al(size_t(L.n_verts) * 32) + al(size_t(L.n_tris) * 12) + al(size_t(o.ns_dyn) * 32) + al(size_t(L.n_verts) * 16) +
-                       al(size_t(vtl::K_SECT) * L.n_verts * 16) + al((size_t(L.big_cap) + 1) * 4) + 2 * al(smb);
+                       al(size_t(vtl::K_SECT) * L.n_verts * 16) + al((size_t(L.big_cap) + 1) * 8) + 2 * al(smb) +
+                       al(size_t(L.n_verts) * 16) + al(size_t(vtl::K_SECT) * L.n_verts * 16);
   if (cudaMalloc(&L.mem, bytes) != cudaSuccess) { cudaGetLastError(); L.mem = nullptr; return fail(ctx, VT_ERR_OOM, "lite: device buffers"); }
   char* p = static_cast<char*>(L.mem);
   L.v = reinterpret_cast<uint4*>(p); p += al(size_t(L.n_verts) * 32);
@@ -248,9 +249,11 @@ vt_status vt_lite_create(vt_ctx* ctx, const vt_lite_opts* opts, vt_lite_info* in
   L.es = reinterpret_cast<float4*>(p); p += al(size_t(o.ns_dyn) * 32);
   L.clip = reinterpret_cast<float4*>(p); p += al(size_t(L.n_verts) * 16);
   L.sclip = reinterpret_cast<float4*>(p); p += al(size_t(vtl::K_SECT) * L.n_verts * 16);
-  L.big = reinterpret_cast<uint32_t*>(p); p += al((size_t(L.big_cap) + 1) * 4);
+  L.big = reinterpret_cast<uint32_t*>(p); p += al((size_t(L.big_cap) + 1) * 8);
   L.sm_static = reinterpret_cast<uint32_t*>(p); p += al(smb);
-  L.sm_dyn = reinterpret_cast<uint32_t*>(p);
+  L.sm_dyn = reinterpret_cast<uint32_t*>(p); p += al(smb);
+  L.snap = reinterpret_cast<int4*>(p); p += al(size_t(L.n_verts) * 16);
+  L.ssnap = reinterpret_cast<int4*>(p);
   VT_CK(cudaMemcpyAsync(L.v, gm.v.data(), gm.v.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
   VT_CK(cudaMemcpyAsync(L.idx, gm.idx.data(), gm.idx.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
   VT_CK(cudaMemsetAsync(L.sclip, 0, size_t(vtl::K_SECT) * L.n_verts * 16, ctx->stream));
@@ -299,7 +302,8 @@ vt_status vt_lite_info_get(vt_ctx* ctx, vt_lite_info* info) {
   info->n_cameras = uint32_t(L.cams.size());
   info->build_ms = L.build_ms;
   info->shadow_static_ms = L.sm_static_ms; info->shadow_dyn_ms = L.sm_dyn_ms; info->camera_ms = L.cam_ms;
-  info->big_tris = L.big_tris; info->launches = L.launches;
+  info->camera_raster_ms = L.raster_ms; info->camera_shade_ms = L.shade_ms;
+  info->big_tris = L.big_tris; info->launches = L.launches; info->shadow_big_tiles = L.shadow_big;
   return VT_OK;
 }
 
@@ -322,7 +326,11 @@ vt_status vt_lite_render_camera(vt_ctx* ctx, uint32_t camera, float* out_rgba) {
   VT_CK(cudaEventRecord(L.ev[0], ctx->stream));
   if (do_static) { if ((s = shadow_pass(ctx, 1)) != VT_OK) return s; L.sm_static_dirty = false; }
   VT_CK(cudaEventRecord(L.ev[1], ctx->stream));
-  if (do_dyn) { if ((s = shadow_pass(ctx, 2)) != VT_OK) return s; L.sm_dyn_version = ctx->nodes.poses_version; }
+  if (do_dyn) {
+    if ((s = shadow_pass(ctx, 2)) != VT_OK) return s;
+    L.sm_dyn_version = ctx->nodes.poses_version;
+    VT_CK(cudaMemcpyAsync(&L.shadow_big, L.big, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   VT_CK(cudaEventRecord(L.ev[2], ctx->stream));
   // the camera pass: vertices, raster into the 4-sample keys, fragments + resolve + finish
   const vtd::Scene S = dev_scene(ctx);
@@ -332,7 +340,8 @@ vt_status vt_lite_render_camera(vt_ctx* ctx, uint32_t camera, float* out_rgba) {
   VT_CK(cudaMemsetAsync(C.key, 0xff, size_t(C.W) * C.H * 32, ctx->stream));
   vtl::Target T{};
   T.W = C.W; T.H = C.H; T.samples = 4; T.key = C.key; T.big = L.big; T.big_cap = L.big_cap;
-  vtl::launch_raster(L.clip, L.idx, L.n_verts, 0, L.n_tris, 1, T, big_blocks(ctx), ctx->stream);
+  vtl::launch_raster(L.clip, L.snap, L.idx, L.n_verts, 0, L.n_verts, 0, L.n_tris, 1, T, big_blocks(ctx), ctx->stream);
+  VT_CK(cudaEventRecord(L.ev[4], ctx->stream));
   vtl::ShadeArgs a{};
   a.key = C.key; a.clip = L.clip; a.sm_static = L.sm_static; a.sm_dyn = L.sm_dyn; a.sm_res = L.o.sm_res;
   a.inv_scale = float(1.0 / out_scale(ctx));
@@ -341,7 +350,7 @@ vt_status vt_lite_render_camera(vt_ctx* ctx, uint32_t camera, float* out_rgba) {
   a.out = C.rad;
   vtl::launch_shade(S, g, v, a, ctx->stream);
   VT_CK(cudaGetLastError());
-  L.launches += 4;
+  L.launches += 5;
   VT_CK(cudaEventRecord(L.ev[3], ctx->stream));
   VT_CK(cudaMemcpyAsync(&L.big_tris, L.big, 4, cudaMemcpyDeviceToHost, ctx->stream));
   if (out_rgba) { if ((s = from_device(ctx, out_rgba, C.rad, size_t(C.W) * C.H * 16)) != VT_OK) return s; }
@@ -349,6 +358,8 @@ vt_status vt_lite_render_camera(vt_ctx* ctx, uint32_t camera, float* out_rgba) {
   L.sm_static_ms = do_static ? ms_between(L.ev[0], L.ev[1]) : 0.0;
   L.sm_dyn_ms = do_dyn ? ms_between(L.ev[1], L.ev[2]) : 0.0;
   L.cam_ms = ms_between(L.ev[2], L.ev[3]);
+  L.raster_ms = ms_between(L.ev[2], L.ev[4]);
+  L.shade_ms = ms_between(L.ev[4], L.ev[3]);
   L.last_clip_cam = int32_t(camera);
   C.rendered = true;
   C.displayed = false;
@@ -458,14 +469,16 @@ vt_status vt_raster(vt_ctx* ctx, const float* clip, uint32_t n_verts, const uint
   for (uint32_t i : hidx)
     if (i >= n_verts) return fail(ctx, VT_ERR_ARG, "raster: index out of range");
   const size_t nk = size_t(width) * height * 4;
-  const size_t bytes = al(size_t(n_verts) * 16) + al(hidx.size() * 4) + al(nk * 8) + al((size_t(n_tris) + 1) * 4);
+  const uint32_t cap = 1u << 20;
+  const size_t bytes = al(size_t(n_verts) * 16) + al(hidx.size() * 4) + al(nk * 8) + al((size_t(cap) + 1) * 8) + al(size_t(n_verts) * 16);
   void* mem = nullptr;
   if (cudaMalloc(&mem, bytes) != cudaSuccess) { cudaGetLastError(); return fail(ctx, VT_ERR_OOM, "raster: device buffers"); }
   char* p = static_cast<char*>(mem);
   float4* dclip = reinterpret_cast<float4*>(p); p += al(size_t(n_verts) * 16);
   uint32_t* didx = reinterpret_cast<uint32_t*>(p); p += al(hidx.size() * 4);
   unsigned long long* dkey = reinterpret_cast<unsigned long long*>(p); p += al(nk * 8);
-  uint32_t* dbig = reinterpret_cast<uint32_t*>(p);
+  uint32_t* dbig = reinterpret_cast<uint32_t*>(p); p += al((size_t(cap) + 1) * 8);
+  int4* dsnap = reinterpret_cast<int4*>(p);
   vt_status s = VT_OK;
   auto run = [&]() -> vt_status {
     vt_status r = to_device(ctx, dclip, clip, size_t(n_verts) * 16);
@@ -473,15 +486,15 @@ vt_status vt_raster(vt_ctx* ctx, const float* clip, uint32_t n_verts, const uint
     VT_CK(cudaMemcpyAsync(didx, hidx.data(), hidx.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     VT_CK(cudaMemsetAsync(dkey, 0xff, nk * 8, ctx->stream));
     vtl::Target T{};
-    T.W = width; T.H = height; T.samples = samples; T.big = dbig; T.big_cap = n_tris;
+    T.W = width; T.H = height; T.samples = samples; T.big = dbig; T.big_cap = cap;
     if (samples == 4) {
       T.key = dkey;
-      vtl::launch_raster(dclip, didx, n_verts, 0, n_tris, 1, T, big_blocks(ctx), ctx->stream);
+      vtl::launch_raster(dclip, dsnap, didx, n_verts, 0, n_verts, 0, n_tris, 1, T, big_blocks(ctx), ctx->stream);
     } else {
       // one 32-bit depth layer in the first half of the key buffer, triangles recovered below by a second pass
       T.depth = reinterpret_cast<uint32_t*>(dkey);
       vtl::launch_fill(T.depth, size_t(width) * height, 0xffffffffu, ctx->stream);
-      vtl::launch_raster(dclip, didx, n_verts, 0, n_tris, 1, T, big_blocks(ctx), ctx->stream);
+      vtl::launch_raster(dclip, dsnap, didx, n_verts, 0, n_verts, 0, n_tris, 1, T, big_blocks(ctx), ctx->stream);
     }
     VT_CK(cudaGetLastError());
     if (samples == 4) {

@@ -158,6 +158,7 @@ struct vt_ctx {
     float4* es = nullptr;
     float4* clip = nullptr;              // camera pass (n_verts)
     float4* sclip = nullptr;             // shadow passes (K_SECT x n_verts)
+    int4 *snap = nullptr, *ssnap = nullptr;   // snapped vertices of the camera pass and of the shadow passes
     uint32_t* big = nullptr;             // 1 + big_cap words
     uint32_t big_cap = 0;
     uint32_t *sm_static = nullptr, *sm_dyn = nullptr;
@@ -178,8 +179,8 @@ struct vt_ctx {
     };
     std::vector<LCam> cams;              // the scene cameras, then SCOPE
     int32_t last_clip_cam = -1;
-    double build_ms = 0, sm_static_ms = 0, sm_dyn_ms = 0, cam_ms = 0;
-    uint32_t big_tris = 0, launches = 0;
+    double build_ms = 0, sm_static_ms = 0, sm_dyn_ms = 0, cam_ms = 0, raster_ms = 0, shade_ms = 0;
+    uint32_t big_tris = 0, launches = 0, shadow_big = 0;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   } lite;
 };

@@ -1,21 +1,10 @@
-// The raster camera pass of lite_nodes on sm_103a: vertex stage, a software rasteriser with exact integer edge
-// functions and 64-bit depth|triangle keys, and the fragment stage fused with the MSAA resolve (lite_nodes/
-// renderer.js:92-374: vsCam, vsShadow, fsCam, FINISH).
+// The raster camera pass of lite_nodes on sm_103a, around the rasteriser of vt_lite_raster.cu: the vertex stage
+// (vsCam / vsShadow) and the fragment stage fused with the MSAA resolve and FINISH (lite_nodes/renderer.js:92-374).
 //
-// Rasterisation (this library's own rules, the ones a 4x MSAA raster pipeline with 'less' depth and no culling
-// follows): clip against 0 <= z <= w (the near and far planes) and a guard band |x|, |y| <= 8 w; snap x/w, y/w in
-// pixels to 1/256; a sample is covered when all three int64 edge functions are positive, or zero on an edge that
-// owns its ties (edge direction dy < 0, or dy = 0 and dx > 0: of two triangles that share an edge exactly one owns
-// it); its depth is z/w interpolated linearly in the screen with the covered sample's edge weights, clamped to
-// [0, 1], and it is kept when below 1 and below what the sample holds. atomicMin on (depth bits << 32 | triangle)
-// keeps the nearest fragment and, on equal depth, the one drawn first, which is what the ordered 'less' test keeps.
-// The fragment stage runs once per (pixel, triangle) among the pixel's surviving samples at the pixel centre,
-// with perspective-correct attributes of the unclipped triangle (2D-homogeneous barycentrics, Olano and Greer
-// 1997), as a raster pipeline's centre interpolation does.
-//
-// The translation unit is compiled without multiply-add contraction (--fmad=false), so the clip, snap, coverage and
-// depth arithmetic is the sequence of IEEE operations that the CPU restatement performs on the same clip
-// coordinates: sample keys and shadow maps are bit-identical to it.
+// The fragment stage runs once per (pixel, triangle) among the pixel's surviving samples at the pixel centre, with
+// perspective-correct attributes of the unclipped triangle (2D-homogeneous barycentrics, Olano and Greer 1997), as
+// a raster pipeline's centre interpolation does. The 3x3 shadow-map taps one texel apart share one bilinear
+// fraction, so the 16 texels under them are compared once per map.
 #include <cuda_fp16.h>
 
 #include "vt_lite.cuh"
@@ -121,216 +110,46 @@ __global__ void vertex_shadow_kernel(const Scene S, const Geo g, const View V, u
   }
 }
 
-// ---------------------------------------------------------------------------------------------- rasteriser
-__device__ __forceinline__ float plane_dist(const float4& v, int p) {
-  switch (p) {
-    case 0: return v.z;
-    case 1: return v.w - v.z;
-    case 2: return GUARD * v.w - v.x;
-    case 3: return GUARD * v.w + v.x;
-    case 4: return GUARD * v.w - v.y;
-    default: return GUARD * v.w + v.y;
-  }
-}
-__device__ __forceinline__ bool inside_all(const float4& v) {
-  bool in = true;
-#pragma unroll
-  for (int p = 0; p < 6; p++) in &= plane_dist(v, p) >= 0.0f;
-  return in;
-}
-
-// Sutherland-Hodgman against the six planes; a crossing point is interpolated from the inside endpoint, so a shared
-// edge gives its two triangles the same point. Returns the vertex count (0: nothing left), at most 9.
-__device__ int clip_poly(const float4 in[3], float4 out[9]) {
-  float4 a[9], b[9];
-  a[0] = in[0]; a[1] = in[1]; a[2] = in[2];
-  int n = 3;
-  for (int p = 0; p < 6; p++) {
-    int m = 0;
-    for (int i = 0; i < n; i++) {
-      const float4 A = a[i], B = a[i + 1 < n ? i + 1 : 0];
-      const float da = plane_dist(A, p), db = plane_dist(B, p);
-      if (da >= 0.0f && m < 9) b[m++] = A;
-      if ((da >= 0.0f) != (db >= 0.0f) && m < 9) {
-        const float4 I = da >= 0.0f ? A : B, O = da >= 0.0f ? B : A;
-        const float di = da >= 0.0f ? da : db, dq = da >= 0.0f ? db : da;
-        const float t = di / (di - dq);
-        b[m++] = make_float4(I.x + t * (O.x - I.x), I.y + t * (O.y - I.y), I.z + t * (O.z - I.z), I.w + t * (O.w - I.w));
-      }
-    }
-    n = m;
-    if (n < 3) return 0;
-    for (int i = 0; i < n; i++) a[i] = b[i];
-  }
-  for (int i = 0; i < n; i++) out[i] = a[i];
-  return n;
-}
-
-struct Snap { int x, y; float z; };
-// viewport transform and the 1/256-pixel snap; false for a vertex that cannot be projected (w <= 0 or not finite)
-__device__ __forceinline__ bool snap(const float4& c, float W2, float H2, Snap& s) {
-  if (!(c.w > 0.0f)) return false;
-  const float nx = c.x / c.w, ny = c.y / c.w;
-  const float X = (nx + 1.0f) * W2, Y = (1.0f - ny) * H2;
-  if (!(fabsf(X) < 1e6f) || !(fabsf(Y) < 1e6f)) return false;
-  s.x = __float2int_rn(X * 256.0f);
-  s.y = __float2int_rn(Y * 256.0f);
-  s.z = c.z / c.w;
-  return true;
-}
-
-__device__ __forceinline__ int floor_div256(int v) { return v >= 0 ? v >> 8 : -((255 - v) >> 8); }
-
-// sample offsets in 1/256 pixel: the 4x MSAA pattern, or the centre
-__device__ __forceinline__ void sample_pos(uint32_t samples, uint32_t s, int& ox, int& oy) {
-  if (samples == 1u) { ox = 128; oy = 128; return; }
-  const int sx[4] = {96, 224, 32, 160}, sy[4] = {32, 96, 160, 224};
-  ox = sx[s]; oy = sy[s];
-}
-
-struct Edge { long long dx, dy, x0, y0; int bias; };
-__device__ __forceinline__ Edge make_edge(const Snap& j, const Snap& k) {
-  Edge e;
-  e.dx = (long long)k.x - j.x;
-  e.dy = (long long)k.y - j.y;
-  e.x0 = j.x;
-  e.y0 = j.y;
-  e.bias = (e.dy < 0 || (e.dy == 0 && e.dx > 0)) ? 0 : -1;
-  return e;
-}
-__device__ __forceinline__ long long edge_at(const Edge& e, long long sx, long long sy) { return e.dx * (sy - e.y0) - e.dy * (sx - e.x0); }
-
-// the samples of pixel rows [py0, py1] x columns [px0, px1] that sub-triangle (a, b, c) covers, thread `lane` of
-// `lanes` taking every lanes-th pixel
-__device__ void raster_sub(Snap a, Snap b, Snap c, uint32_t id, uint32_t layer, const Target& T, int lane, int lanes) {
-  long long A = ((long long)b.x - a.x) * ((long long)c.y - a.y) - ((long long)b.y - a.y) * ((long long)c.x - a.x);
-  if (A == 0) return;
-  if (A < 0) { const Snap t = b; b = c; c = t; A = -A; }
-  const Edge e0 = make_edge(b, c), e1 = make_edge(c, a), e2 = make_edge(a, b);
-  const int xmin = min(a.x, min(b.x, c.x)), xmax = max(a.x, max(b.x, c.x));
-  const int ymin = min(a.y, min(b.y, c.y)), ymax = max(a.y, max(b.y, c.y));
-  const int px0 = max(0, floor_div256(xmin)), px1 = min(int(T.W) - 1, floor_div256(xmax));
-  const int py0 = max(0, floor_div256(ymin)), py1 = min(int(T.H) - 1, floor_div256(ymax));
-  if (px0 > px1 || py0 > py1) return;
-  const int nx = px1 - px0 + 1;
-  const int npx = nx * (py1 - py0 + 1);
-  const float fA = float(A);
-  for (int q = lane; q < npx; q += lanes) {
-    const int px = px0 + q % nx, py = py0 + q / nx;
-    for (uint32_t s = 0; s < T.samples; s++) {
-      int ox, oy;
-      sample_pos(T.samples, s, ox, oy);
-      const long long sx = (long long)px * 256 + ox, sy = (long long)py * 256 + oy;
-      const long long w0 = edge_at(e0, sx, sy), w1 = edge_at(e1, sx, sy), w2 = edge_at(e2, sx, sy);
-      if (w0 + e0.bias < 0 || w1 + e1.bias < 0 || w2 + e2.bias < 0) continue;
-      const float l1 = float(w1) / fA, l2 = float(w2) / fA;
-      float z = a.z + l1 * (b.z - a.z) + l2 * (c.z - a.z);
-      z = fminf(z, 1.0f);
-      if (!(z > 0.0f)) z = 0.0f;
-      if (!(z < 1.0f)) continue;
-      if (T.samples == 4u) {
-        const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
-        unsigned long long* p = T.key + (size_t(py) * T.W + px) * 4u + s;
-        if (*p > key) atomicMin(p, key);
-      } else {
-        uint32_t* p = T.depth + size_t(layer) * T.W * T.H + size_t(py) * T.W + px;
-        const uint32_t d = __float_as_uint(z);
-        if (*p > d) atomicMin(p, d);
-      }
-    }
-  }
-}
-
-// one triangle: clip, snap, then either raster here or (box larger than BIG_PIXELS) leave it to the block path
-__device__ __forceinline__ int setup_tri(const float4* clip, const uint32_t* idx, uint32_t n_verts, uint32_t tri, uint32_t layer,
-                                         const Target& T, Snap* P) {
-  const float4* C = clip + size_t(layer) * n_verts;
-  float4 in[3];
-  for (int j = 0; j < 3; j++) in[j] = __ldg(C + __ldg(idx + 3u * tri + j));
-  float4 poly[9];
-  int n;
-  if (inside_all(in[0]) && inside_all(in[1]) && inside_all(in[2])) {
-    poly[0] = in[0]; poly[1] = in[1]; poly[2] = in[2];
-    n = 3;
-  } else {
-    n = clip_poly(in, poly);
-  }
-  const float W2 = float(T.W) * 0.5f, H2 = float(T.H) * 0.5f;
-  for (int i = 0; i < n; i++)
-    if (!snap(poly[i], W2, H2, P[i])) return 0;
-  return n;
-}
-
-__global__ void raster_kernel(const float4* __restrict__ clip, const uint32_t* __restrict__ idx, uint32_t n_verts, uint32_t t0, uint32_t nt,
-                              uint32_t layers, const Target T) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nt * layers) return;
-  const uint32_t layer = i / nt, tri = t0 + i % nt;
-  Snap P[9];
-  const int n = setup_tri(clip, idx, n_verts, tri, layer, T, P);
-  if (n < 3) return;
-  int xmin = P[0].x, xmax = P[0].x, ymin = P[0].y, ymax = P[0].y;
-  for (int k = 1; k < n; k++) { xmin = min(xmin, P[k].x); xmax = max(xmax, P[k].x); ymin = min(ymin, P[k].y); ymax = max(ymax, P[k].y); }
-  const long long bw = (long long)min(int(T.W) - 1, floor_div256(xmax)) - max(0, floor_div256(xmin)) + 1;
-  const long long bh = (long long)min(int(T.H) - 1, floor_div256(ymax)) - max(0, floor_div256(ymin)) + 1;
-  if (bw <= 0 || bh <= 0) return;
-  if (bw * bh > (long long)BIG_PIXELS) {
-    const uint32_t slot = atomicAdd(T.big, 1u);
-    if (slot < T.big_cap) T.big[1 + slot] = tri | (layer << 28);
-    return;
-  }
-  for (int k = 1; k + 1 < n; k++) raster_sub(P[0], P[k], P[k + 1], tri, layer, T, 0, 1);
-}
-
-// the queued many-pixel triangles: one block per triangle, the block's threads over its pixels
-__global__ void raster_big_kernel(const float4* __restrict__ clip, const uint32_t* __restrict__ idx, uint32_t n_verts, const Target T) {
-  const uint32_t count = min(T.big[0], T.big_cap);
-  for (uint32_t q = blockIdx.x; q < count; q += gridDim.x) {
-    const uint32_t e = T.big[1 + q];
-    const uint32_t tri = e & 0x0fffffffu, layer = e >> 28;
-    Snap P[9];
-    const int n = setup_tri(clip, idx, n_verts, tri, layer, T, P);
-    for (int k = 1; k + 1 < n; k++) raster_sub(P[0], P[k], P[k + 1], tri, layer, T, threadIdx.x, blockDim.x);
-  }
-}
-
-__global__ void fill_kernel(uint32_t* p, size_t n, uint32_t value) {
-  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) p[i] = value;
-}
-
 // ---------------------------------------------------------------------------------------------- fragment stage
-__device__ __forceinline__ float sm_texel(const uint32_t* m, uint32_t res, uint32_t k, int x, int y) {
+__device__ __forceinline__ uint32_t sm_less(const uint32_t* m, uint32_t res, uint32_t k, int x, int y, float dref) {
   x = min(max(x, 0), int(res) - 1);
   y = min(max(y, 0), int(res) - 1);
   const uint32_t b = __ldg(m + (size_t(k) * res + y) * res + x);
-  return b == 0xffffffffu ? 1.0f : __uint_as_float(b);
+  return dref < (b == 0xffffffffu ? 1.0f : __uint_as_float(b)) ? 1u : 0u;
 }
-// textureSampleCompareLevel with a 'less' comparison sampler, linear filtering, clamp to edge: the 2x2 texels
-// around the point each compare dref < depth, blended bilinearly
-__device__ __forceinline__ float sm_cmp(const uint32_t* m, uint32_t res, uint32_t k, float u, float v, float dref) {
-  const float tx = u * float(res) - 0.5f, ty = v * float(res) - 0.5f;
-  const float fx0 = floorf(tx), fy0 = floorf(ty);
-  const float fx = tx - fx0, fy = ty - fy0;
-  const int x0 = int(fx0), y0 = int(fy0);
-  const float c00 = dref < sm_texel(m, res, k, x0, y0) ? 1.0f : 0.0f;
-  const float c10 = dref < sm_texel(m, res, k, x0 + 1, y0) ? 1.0f : 0.0f;
-  const float c01 = dref < sm_texel(m, res, k, x0, y0 + 1) ? 1.0f : 0.0f;
-  const float c11 = dref < sm_texel(m, res, k, x0 + 1, y0 + 1) ? 1.0f : 0.0f;
-  return (1.0f - fx) * (1.0f - fy) * c00 + fx * (1.0f - fy) * c10 + (1.0f - fx) * fy * c01 + fx * fy * c11;
-}
-// smVis (lite_nodes/renderer.js:267): 3x3 taps one texel apart, min of the static and dynamic maps per tap
+// smVis (lite_nodes/renderer.js:267): 3x3 taps one texel apart of textureSampleCompareLevel ('less' comparison,
+// linear filtering, clamp to edge: the 2x2 texels around a tap compare dref < depth and blend bilinearly), min of
+// the static and dynamic maps per tap. The taps share the bilinear fraction of the centre tap (they sit exactly one
+// texel apart), so the 4x4 texels under them are compared once per map.
 __device__ float sm_vis(const View& V, const ShadeArgs& a, float3 pw, uint32_t k, float bias) {
   const float3 q = sm_project(V, pw, k);
   if (fabsf(q.x) >= 1.0f || fabsf(q.y) >= 1.0f) return 1.0f;
   const float u = 0.5f + 0.5f * q.x, v = 0.5f - 0.5f * q.y;
   const float dref = (q.z - bias) / V.lb[3];
-  const float t = 1.0f / float(a.sm_res);
+  const float res = float(a.sm_res);
+  const float tx = u * res - 0.5f, ty = v * res - 0.5f;
+  const float fx0 = floorf(tx), fy0 = floorf(ty);
+  const float fx = tx - fx0, fy = ty - fy0;
+  const int x0 = int(fx0) - 1, y0 = int(fy0) - 1;
+  uint32_t ms = 0, md = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      ms |= sm_less(a.sm_static, a.sm_res, k, x0 + i, y0 + j, dref) << (4 * j + i);
+      md |= sm_less(a.sm_dyn, a.sm_res, k, x0 + i, y0 + j, dref) << (4 * j + i);
+    }
+  const float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy), w01 = (1.0f - fx) * fy, w11 = fx * fy;
   float s = 0.0f;
-  for (int j = -1; j <= 1; j++)
-    for (int i = -1; i <= 1; i++) {
-      const float ou = u + float(i) * t, ov = v + float(j) * t;
-      const float cs = sm_cmp(a.sm_static, a.sm_res, k, ou, ov, dref);
-      const float cd = sm_cmp(a.sm_dyn, a.sm_res, k, ou, ov, dref);
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const int b = 4 * j + i;
+      const float cs = w00 * float((ms >> b) & 1u) + w10 * float((ms >> (b + 1)) & 1u) + w01 * float((ms >> (b + 4)) & 1u) +
+                       w11 * float((ms >> (b + 5)) & 1u);
+      const float cd = w00 * float((md >> b) & 1u) + w10 * float((md >> (b + 1)) & 1u) + w01 * float((md >> (b + 4)) & 1u) +
+                       w11 * float((md >> (b + 5)) & 1u);
       s = s + fminf(cs, cd);
     }
   return s / 9.0f;
@@ -396,8 +215,8 @@ __device__ float3 fragment(const Scene& S, const Geo& g, const View& V, const Sh
   const Mat M = load_mat(S, mat);   // a textured board's print mask is a 1x1 white texture: the material as loaded
   const bool is_static = inst == STATIC_INST;
   const uint32_t nS = is_static ? V.misc[1] : V.misc[2];
-  float3 acc[K_SECT];
-  for (uint32_t k = 0; k < K_SECT; k++) acc[k] = f3(0.0f, 0.0f, 0.0f);
+  // per-sector sums in registers (the sample's sector is the same for every thread of a warp)
+  float3 acc0 = f3(0.0f, 0.0f, 0.0f), acc1 = acc0, acc2 = acc0, acc3 = acc0;
   for (uint32_t j = 0; j < nS; j++) {
     const float4 ea = __ldg(g.es + 2 * j), eb = __ldg(g.es + 2 * j + 1);
     float3 wi = xyz(ea) - p;
@@ -410,19 +229,25 @@ __device__ float3 fragment(const Scene& S, const Geo& g, const View& V, const Sh
     const float pr = profile(S, acosf(clampf(dot(-wi, axis), -1.0f, 1.0f)));
     if (pr <= 0.0f) continue;
     const float3 f = eval_bsdf(M, ns, wi, wo);
-    const uint32_t k = min(uint32_t(ea.w), K_SECT - 1u);
-    acc[k] = acc[k] + f * (pr * cosS * cosE * eb.w / d2);
+    const float3 add = f * (pr * cosS * cosE * eb.w / d2);
+    const uint32_t k = uint32_t(ea.w);
+    if (k == 0u) acc0 = acc0 + add;
+    else if (k == 1u) acc1 = acc1 + add;
+    else if (k == 2u) acc2 = acc2 + add;
+    else acc3 = acc3 + add;
   }
   float3 L = f3(0.0f, 0.0f, 0.0f);
   const float3 off = p + ng * (is_static ? 1.5e-4f : 6e-4f);
   const uint32_t dbg = __float_as_uint(V.axisW[3]);
   float vsum = 0.0f;
+#pragma unroll
   for (uint32_t k = 0; k < K_SECT; k++) {
+    const float3 ak = k == 0 ? acc0 : k == 1 ? acc1 : k == 2 ? acc2 : acc3;
     float vk = 1.0f;
     if (dbg != 1u) vk = sm_vis(V, a, off, k, is_static ? V.lo[k][3] : 6e-4f);
     vsum = vsum + vk;
-    if (maxc(acc[k]) <= 0.0f) continue;
-    L = L + acc[k] * vk;
+    if (maxc(ak) <= 0.0f) continue;
+    L = L + ak * vk;
   }
   if (dbg == 2u) return f3(vsum / float(K_SECT), vsum / float(K_SECT), vsum / float(K_SECT));
   L = L * ld3(S.su) / float(nS);
@@ -484,20 +309,9 @@ void launch_vertex_shadow(const Scene& S, const Geo& g, const View& v, uint32_t 
   if (!count) return;
   vertex_shadow_kernel<<<(count + 255) / 256, 256, 0, st>>>(S, g, v, first, count, clip);
 }
-void launch_raster(const float4* clip, const uint32_t* idx, uint32_t n_verts, uint32_t t0, uint32_t nt, uint32_t layers, const Target& T,
-                   int blocks_big, cudaStream_t st) {
-  cudaMemsetAsync(T.big, 0, 4, st);
-  const size_t n = size_t(nt) * layers;
-  if (n) raster_kernel<<<uint32_t((n + 127) / 128), 128, 0, st>>>(clip, idx, n_verts, t0, nt, layers, T);
-  raster_big_kernel<<<blocks_big, 256, 0, st>>>(clip, idx, n_verts, T);
-}
 void launch_shade(const Scene& S, const Geo& g, const View& v, const ShadeArgs& a, cudaStream_t st) {
   const uint32_t W = uint32_t(v.size[0]), H = uint32_t(v.size[1]);
   dim3 grid((W + 15) / 16, (H + 7) / 8);
   shade_kernel<<<grid, 128, 0, st>>>(S, g, v, a);
 }
-void launch_fill(uint32_t* p, size_t n, uint32_t value, cudaStream_t st) {
-  fill_kernel<<<1024, 256, 0, st>>>(p, n, value);
-}
-
 }  // namespace vtl

@@ -3,10 +3,10 @@
 // Pipeline per camera view (lite_nodes/renderer.js:844 renderCamera):
 //   vertex     one thread per raster vertex: world position (posed bodies at mid-exposure), clip coordinates
 //              (KB4 or pinhole camera; equidistant sector projection for the shadow maps, 4 sectors at once)
-//   raster     one thread per triangle: clip against 0 <= z <= w and a guard band |x|, |y| <= 8 w, snap to 1/256
-//              pixel, exact int64 edge functions; every covered sample takes atomicMin(depth bits << 32 | triangle)
-//              (64-bit keys for the camera's 4 samples, 32-bit depth for a shadow map). Triangles whose box holds
-//              more than 256 pixels go to a queue that whole blocks rasterise afterwards.
+//   raster     (vt_lite_raster.cu) one thread per triangle: clip against 0 <= z <= w and a guard band |x|, |y| <= 8 w,
+//              snap to 1/256 pixel, exact int64 edge functions; every covered sample takes atomicMin(depth bits << 32
+//              | triangle) (64-bit keys for the camera's 4 samples, 32-bit depth for a shadow map). Triangles whose
+//              box holds more than 256 samples are queued as 16 x 16-pixel tiles that a warp per tile rasterises.
 //   shade      one thread per pixel: each distinct triangle among its samples is shaded once at the pixel centre
 //              (the fragment stage), colours rounded to half, averaged, rounded to half, scaled back (the MSAA
 //              resolve into rgba16float and the FINISH pass)
@@ -22,7 +22,7 @@ namespace vtl {
 
 constexpr uint32_t K_SECT = 4;          // emitter sectors = shadow maps (lite_nodes/renderer.js:58)
 constexpr uint32_t STATIC_INST = 0xffffu;
-constexpr uint32_t BIG_PIXELS = 256;    // a triangle box larger than this goes to the block-per-triangle path
+constexpr uint32_t BIG_SAMPLES = 256;   // a triangle box with more samples goes to the warp-per-tile path
 constexpr float GUARD = 8.0f;           // clip-space guard band: |x|, |y| <= GUARD w
 constexpr unsigned long long EMPTY_KEY = ~0ull;
 
@@ -55,8 +55,8 @@ struct Target {
   uint32_t W, H, samples;
   unsigned long long* key;     // samples == 4
   uint32_t* depth;             // samples == 1: layers of W x H, one per sector
-  uint32_t* big;               // [0] count, then triangle (| sector << 28) entries
-  uint32_t big_cap;
+  uint32_t* big;               // [0] count, [1] unused, then (triangle | sector << 28, tile x | tile y << 16) items
+  uint32_t big_cap;            // items
 };
 
 struct ShadeArgs {
@@ -75,9 +75,10 @@ struct ShadeArgs {
 void launch_vertex_cam(const vtd::Scene& S, const Geo& g, const View& v, uint32_t first, uint32_t count, float4* clip, cudaStream_t st);
 // vertex stage of the shadow maps: K_SECT layers of clip coordinates, clip[k * n_verts + v]
 void launch_vertex_shadow(const vtd::Scene& S, const Geo& g, const View& v, uint32_t first, uint32_t count, float4* clip, cudaStream_t st);
-// raster of triangles [t0, t0 + nt) over clip (n_verts per layer; `layers` sector layers for a shadow target)
-void launch_raster(const float4* clip, const uint32_t* idx, uint32_t n_verts, uint32_t t0, uint32_t nt, uint32_t layers, const Target& T,
-                   int blocks_big, cudaStream_t st);
+// raster of triangles [t0, t0 + nt) over clip (n_verts per layer; `layers` sector layers for a shadow target), whose
+// vertices are [v0, v0 + nv); snaps: scratch of one int4 per clip entry
+void launch_raster(const float4* clip, int4* snaps, const uint32_t* idx, uint32_t n_verts, uint32_t v0, uint32_t nv, uint32_t t0, uint32_t nt,
+                   uint32_t layers, const Target& T, int blocks_big, cudaStream_t st);
 // fragment stage + resolve + finish
 void launch_shade(const vtd::Scene& S, const Geo& g, const View& v, const ShadeArgs& a, cudaStream_t st);
 // clear a 32-bit depth target to all ones

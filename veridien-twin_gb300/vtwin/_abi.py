@@ -164,7 +164,8 @@ class vt_lite_opts(C.Structure):
 class vt_lite_info(C.Structure):
     _fields_ = [("raster_tris", C.c_uint32), ("static_tris", C.c_uint32), ("dyn_verts", C.c_uint32), ("n_cameras", C.c_uint32),
                 ("build_ms", C.c_double), ("shadow_static_ms", C.c_double), ("shadow_dyn_ms", C.c_double), ("camera_ms", C.c_double),
-                ("big_tris", C.c_uint32), ("launches", C.c_uint32)]
+                ("camera_raster_ms", C.c_double), ("camera_shade_ms", C.c_double), ("big_tris", C.c_uint32), ("launches", C.c_uint32),
+                ("shadow_big_tiles", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 VT_LITE_VIEW, VT_LITE_CLIP, VT_LITE_KEYS, VT_LITE_SM_STATIC, VT_LITE_SM_DYN, VT_LITE_SM_CLIP, VT_LITE_GEOM, VT_LITE_INDEX, VT_LITE_EMIT = range(9)

@@ -24,7 +24,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 
 # per-file flags: the sensor chain and the rasteriser are compiled without multiply-add contraction, so their
 # arithmetic is the sequence of separately rounded operations that the CPU restatement performs
-EXTRA = {"vt_isp.cu": ["--fmad=false"], "vt_lite.cu": ["--fmad=false"]}
+EXTRA = {"vt_isp.cu": ["--fmad=false"], "vt_lite_raster.cu": ["--fmad=false"],
+         # the raster pass's shading: WGSL's own f32 precision (division 2.5 ulp, inverseSqrt 2 ulp), not IEEE division
+         "vt_lite.cu": ["--use_fast_math"]}
 
 
 def nvcc() -> str:

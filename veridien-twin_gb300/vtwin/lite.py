@@ -178,7 +178,8 @@ class LiteNodesRenderer:
         check(self.lib.vt_lite_info_get(self.tr._ctx, C.byref(i)), self.tr._ctx)
         return {"rasterTris": i.raster_tris, "staticTris": i.static_tris, "dynVerts": i.dyn_verts, "cameras": i.n_cameras,
                 "loadMs": i.build_ms, "shadowStaticMs": i.shadow_static_ms, "shadowDynMs": i.shadow_dyn_ms, "cameraMs": i.camera_ms,
-                "bigTris": i.big_tris, "launches": i.launches}
+                "cameraRasterMs": i.camera_raster_ms, "cameraShadeMs": i.camera_shade_ms,
+                "bigTiles": i.big_tris, "launches": i.launches, "shadowBigTiles": i.shadow_big_tiles}
 
     def timings(self) -> dict:
         """lite_nodes/renderer.js:982 timings: device ms of the last render's passes, load time, the tracer's."""
