@@ -155,6 +155,44 @@ __device__ float sm_vis(const View& V, const ShadeArgs& a, float3 pw, uint32_t k
   return s / 9.0f;
 }
 
+// evalBSDF (gpu/bsdf.js:98) for a fixed shading normal and view: the factors that depend only on n . v (the view's
+// Fresnel terms and GGX Smith lambdas) are computed once per fragment; each light direction then costs the rest.
+// The operations and their order are those of eval_bsdf, so the values are the same.
+struct BsdfView {
+  float nv, lam_v, lam_v_coat, F_v, Fv_coat_t;
+};
+__device__ __forceinline__ BsdfView bsdf_view(const Mat& M, float3 n, float3 v) {
+  BsdfView b;
+  b.nv = dot(n, v);
+  b.lam_v = ggx_lambda(b.nv, M.alpha);
+  b.lam_v_coat = M.metal > 1.5f ? ggx_lambda(b.nv, M.x.w) : 0.0f;
+  b.F_v = fresnel(b.nv, M.ior);
+  b.Fv_coat_t = 1.0f - b.F_v;
+  return b;
+}
+__device__ __forceinline__ float3 eval_bsdf_v(const Mat& M, const BsdfView& B, float3 n, float3 l, float3 v) {
+  const float nl = dot(n, l), nv = B.nv;
+  if (nl <= 0.0f || nv <= 0.0f) return f3(0, 0, 0);
+  const float3 h = normalize(l + v);
+  const float nh = dot(n, h), vh = fmaxf(0.0f, dot(v, h));
+  if (M.metal > 1.5f) {
+    const float ac = M.x.w;
+    const float coat = ggx_d(nh, ac) * (1.0f / (1.0f + ggx_lambda(nl, ac) + B.lam_v_coat)) * fresnel(vh, M.ior) / (4.0f * nl * nv);
+    const float t = (1.0f - fresnel(nl, M.ior)) * B.Fv_coat_t;
+    const float metal = ggx_d(nh, M.alpha) * (1.0f / (1.0f + ggx_lambda(nl, M.alpha) + B.lam_v)) / (4.0f * nl * nv);
+    const float ex = 1.0f / nl + 1.0f / nv;
+    const float3 tp = f3(powf(M.x.x, ex), powf(M.x.y, ex), powf(M.x.z, ex));
+    return f3(coat, coat, coat) + tp * schlick3(M.c, vh) * (t * metal);
+  }
+  const float spec = ggx_d(nh, M.alpha) * (1.0f / (1.0f + ggx_lambda(nl, M.alpha) + B.lam_v)) / (4.0f * nl * nv);
+  float3 out = fresnel_rgb(M, vh) * spec;
+  if (M.metal < 0.5f) {
+    const float kd = INV_PI_F * (1.0f - fresnel(nl, M.ior)) * (1.0f - B.F_v) / (1.0f - M.fbar);
+    out = out + M.c * kd;
+  }
+  return out;
+}
+
 // fsCam (lite_nodes/renderer.js:284) for triangle `tri` at the centre of pixel (px, py); radiance x outScale
 __device__ float3 fragment(const Scene& S, const Geo& g, const View& V, const ShadeArgs& a, uint32_t tri, uint32_t px, uint32_t py) {
   uint4 va[3], vb[3];
@@ -215,6 +253,7 @@ __device__ float3 fragment(const Scene& S, const Geo& g, const View& V, const Sh
   const Mat M = load_mat(S, mat);   // a textured board's print mask is a 1x1 white texture: the material as loaded
   const bool is_static = inst == STATIC_INST;
   const uint32_t nS = is_static ? V.misc[1] : V.misc[2];
+  const BsdfView BV = bsdf_view(M, ns, wo);
   // per-sector sums in registers (the sample's sector is the same for every thread of a warp)
   float3 acc0 = f3(0.0f, 0.0f, 0.0f), acc1 = acc0, acc2 = acc0, acc3 = acc0;
   for (uint32_t j = 0; j < nS; j++) {
@@ -228,7 +267,7 @@ __device__ float3 fragment(const Scene& S, const Geo& g, const View& V, const Sh
     if (cosS <= 0.0f || dot(ng, wi) <= 0.0f) continue;
     const float pr = profile(S, acosf(clampf(dot(-wi, axis), -1.0f, 1.0f)));
     if (pr <= 0.0f) continue;
-    const float3 f = eval_bsdf(M, ns, wi, wo);
+    const float3 f = eval_bsdf_v(M, BV, ns, wi, wo);
     const float3 add = f * (pr * cosS * cosE * eb.w / d2);
     const uint32_t k = uint32_t(ea.w);
     if (k == 0u) acc0 = acc0 + add;

@@ -6,7 +6,7 @@
 //   raster     (vt_lite_raster.cu) one thread per triangle: clip against 0 <= z <= w and a guard band |x|, |y| <= 8 w,
 //              snap to 1/256 pixel, exact int64 edge functions; every covered sample takes atomicMin(depth bits << 32
 //              | triangle) (64-bit keys for the camera's 4 samples, 32-bit depth for a shadow map). Triangles whose
-//              box holds more than 256 samples are queued as 16 x 16-pixel tiles that a warp per tile rasterises.
+//              box holds more than 256 samples are queued as 32 x 32-pixel tiles that a warp per tile rasterises.
 //   shade      one thread per pixel: each distinct triangle among its samples is shaded once at the pixel centre
 //              (the fragment stage), colours rounded to half, averaged, rounded to half, scaled back (the MSAA
 //              resolve into rgba16float and the FINISH pass)

@@ -10,9 +10,11 @@
 // equal depth, the one drawn first, which is what the ordered 'less' test keeps; a shadow map keeps the depth bits.
 //
 // Work split: one pass snaps every vertex once (a vertex inside every clip plane, nearly all, keeps its snapped
-// point); then one thread per triangle; a triangle of three such vertices needs no clipping; its box, if at most BIG_SAMPLES samples, is rasterised by that thread, else one (triangle,
-// 16 x 16-pixel tile) item per tile of its box is queued and a warp per item rasterises that tile afterwards, lanes
-// over its pixels (tiles that do not fit in the queue are rasterised by the triangle's own thread).
+// point); then one thread per triangle; a triangle of three such vertices needs no clipping. Its box, if at most
+// BIG_SAMPLES samples, is rasterised by that thread (edge functions stepped exactly from pixel to pixel), else one
+// (triangle, 32 x 32-pixel tile) item per tile of its box is queued and a warp per item rasterises that tile: the
+// lanes find the tile's 4 x 4-pixel sub-blocks that the triangle may cover, then take their pixels (tiles that do
+// not fit in the queue are rasterised by the triangle's own thread).
 //
 // The translation unit is compiled without multiply-add contraction (--fmad=false), so the clip, snap, coverage and
 // depth arithmetic is the sequence of IEEE operations that the CPU restatement performs on the same clip
@@ -170,10 +172,95 @@ __device__ void raster_sub_n(Snap a, Snap b, Snap c, uint32_t id, uint32_t layer
   }
 }
 
+// one sample's test and write (edge values w already include the tie bias)
+template <uint32_t NS>
+__device__ __forceinline__ void shade_sample(const Snap& a, float dz1, float dz2, float rA, long long w0, long long w1, long long w2, int b1, int b2,
+                                             uint32_t id, uint32_t layer, const Target& T, int px, int py, uint32_t s) {
+  if (w0 < 0 || w1 < 0 || w2 < 0) return;
+  const float l1 = float(w1 - b1) * rA, l2 = float(w2 - b2) * rA;
+  float z = a.z + l1 * dz1 + l2 * dz2;
+  z = fminf(z, 1.0f);
+  if (!(z > 0.0f)) z = 0.0f;
+  if (!(z < 1.0f)) return;
+  if (NS == 4u)
+    atomicMin(T.key + (size_t(py) * T.W + px) * 4u + s, ((unsigned long long)__float_as_uint(z) << 32) | id);   // a reduction
+  else
+    atomicMin(T.depth + size_t(layer) * T.W * T.H + size_t(py) * T.W + px, __float_as_uint(z));
+}
+
+// a tile (box `lim`, at most 32 x 32 pixels) of a many-pixel triangle, by a whole warp: each lane tests two of the
+// tile's 4 x 4-pixel sub-blocks against the three edges (the edge functions are linear: their largest value over a
+// sub-block's samples is at a corner of the samples' extent), then the warp covers the candidate sub-blocks two at a
+// time, one pixel per lane
+template <uint32_t NS>
+__device__ void raster_tile_n(Snap a, Snap b, Snap c, uint32_t id, uint32_t layer, const Target& T, const Box& lim, int lane) {
+  long long A = ((long long)b.x - a.x) * ((long long)c.y - a.y) - ((long long)b.y - a.y) * ((long long)c.x - a.x);
+  if (A == 0) return;
+  if (A < 0) { const Snap t = b; b = c; c = t; A = -A; }
+  const Snap P[3] = {a, b, c};
+  Box bx;
+  if (!box_of(P, 3, T, bx)) return;
+  bx.x0 = max(bx.x0, lim.x0); bx.x1 = min(bx.x1, lim.x1); bx.y0 = max(bx.y0, lim.y0); bx.y1 = min(bx.y1, lim.y1);
+  if (bx.x0 > bx.x1 || bx.y0 > bx.y1) return;
+  const Edge E[3] = {make_edge(b, c), make_edge(c, a), make_edge(a, b)};
+  const int nbx = (bx.x1 - bx.x0) / 4 + 1, nby = (bx.y1 - bx.y0) / 4 + 1;   // at most 8 x 8
+  bool cand[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int q = lane + 32 * h;
+    const int qx = q % 8, qy = q / 8;
+    bool in = qx < nbx && qy < nby;
+    if (in) {
+      const int x0 = bx.x0 + 4 * qx, x1 = min(x0 + 3, bx.x1), y0 = bx.y0 + 4 * qy, y1 = min(y0 + 3, bx.y1);
+      const long long sx0 = (long long)x0 * 256 + 32, sx1 = (long long)x1 * 256 + 224;
+      const long long sy0 = (long long)y0 * 256 + 32, sy1 = (long long)y1 * 256 + 224;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const long long m = max(max(edge_at(E[k], sx0, sy0), edge_at(E[k], sx1, sy0)), max(edge_at(E[k], sx0, sy1), edge_at(E[k], sx1, sy1)));
+        in = in && m + E[k].bias >= 0;
+      }
+    }
+    cand[h] = in;
+  }
+  unsigned long long mask = (unsigned long long)__ballot_sync(0xffffffffu, cand[0]) | ((unsigned long long)__ballot_sync(0xffffffffu, cand[1]) << 32);
+  long long off[3][NS];
+#pragma unroll
+  for (uint32_t s = 0; s < NS; s++) {
+    const long long ox = NS == 1u ? 128 : (long long)((0xa020e060u >> (8 * s)) & 0xffu);
+    const long long oy = NS == 1u ? 128 : 32 + 64 * (long long)s;
+#pragma unroll
+    for (int k = 0; k < 3; k++) off[k][s] = E[k].dx * oy - E[k].dy * ox + E[k].bias;
+  }
+  const float rA = 1.0f / float(A);
+  const float dz1 = b.z - a.z, dz2 = c.z - a.z;
+  while (mask) {
+    // two candidate sub-blocks: lanes 0-15 the first, 16-31 the second
+    const int q0 = __ffsll(mask) - 1;
+    mask &= mask - 1;
+    const int q1 = mask ? __ffsll(mask) - 1 : -1;
+    if (q1 >= 0) mask &= mask - 1;
+    const int q = lane < 16 ? q0 : q1;
+    if (q < 0) continue;
+    const int px = bx.x0 + 4 * (q % 8) + (lane & 3), py = bx.y0 + 4 * (q / 8) + ((lane >> 2) & 3);
+    if (px > bx.x1 || py > bx.y1) continue;
+    long long w[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) w[k] = edge_at(E[k], (long long)px * 256, (long long)py * 256);
+#pragma unroll
+    for (uint32_t s = 0; s < NS; s++)
+      shade_sample<NS>(a, dz1, dz2, rA, w[0] + off[0][s], w[1] + off[1][s], w[2] + off[2][s], E[1].bias, E[2].bias, id, layer, T, px, py, s);
+  }
+}
+
 __device__ __forceinline__ void raster_sub(Snap a, Snap b, Snap c, uint32_t id, uint32_t layer, const Target& T, const Box& lim, int lane,
                                            int lanes) {
-  if (T.samples == 4u) raster_sub_n<4>(a, b, c, id, layer, T, lim, lane, lanes);
-  else raster_sub_n<1>(a, b, c, id, layer, T, lim, lane, lanes);
+  if (lanes > 1) {
+    if (T.samples == 4u) raster_tile_n<4>(a, b, c, id, layer, T, lim, lane);
+    else raster_tile_n<1>(a, b, c, id, layer, T, lim, lane);
+    return;
+  }
+  if (T.samples == 4u) raster_sub_n<4>(a, b, c, id, layer, T, lim, 0, 1);
+  else raster_sub_n<1>(a, b, c, id, layer, T, lim, 0, 1);
 }
 
 __device__ __forceinline__ void load_tri(const float4* clip, const uint32_t* idx, uint32_t n_verts, uint32_t tri, uint32_t layer, float4 in[3]) {
@@ -191,10 +278,10 @@ __device__ __noinline__ int setup_clipped(const float4 in[3], const Target& T, S
   return n;
 }
 
-constexpr int TILE = 16;
+constexpr int TILE = 32;
 __device__ __forceinline__ Box everything() { return Box{0, 1 << 30, 0, 1 << 30}; }
 
-// a many-pixel triangle (polygon P of n snapped points, box b): one queued item per 16 x 16 tile of its box; the
+// a many-pixel triangle (polygon P of n snapped points, box b): one queued item per 32 x 32 tile of its box; the
 // tiles that do not fit in the queue are rasterised here
 __device__ void queue_tiles(const Target& T, uint32_t tri, uint32_t layer, const Box& b, const Snap* P, int n) {
   const int tx0 = b.x0 / TILE, tx1 = b.x1 / TILE, ty0 = b.y0 / TILE, ty1 = b.y1 / TILE;
