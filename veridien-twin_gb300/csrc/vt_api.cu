@@ -120,6 +120,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   cudaFree(ctx->lite.mem);
+  cudaFree(ctx->lite.frag_mem);
   for (auto& c : ctx->lite.cams) cudaFree(c.mem);
   for (cudaEvent_t e : ctx->lite.ev)
     if (e) cudaEventDestroy(e);

@@ -177,6 +177,23 @@ vt_status shadow_pass(vt_ctx* ctx, uint32_t which) {
 vt_status ensure_cam(vt_ctx* ctx, uint32_t camera) {
   auto& L = ctx->lite;
   auto& C = L.cams[camera];
+  const size_t px = size_t(C.W) * C.H;
+  if (L.frag_pixels < px) {
+    VT_CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(L.frag_mem);
+    L.frag_mem = nullptr;
+    L.frag_pixels = 0;
+    if (cudaMalloc(&L.frag_mem, al(px * 32) * 2 + al(px * 16) + al(16)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, VT_ERR_OOM, "lite: fragment list");
+    }
+    char* p = static_cast<char*>(L.frag_mem);
+    L.fb.frags = reinterpret_cast<uint2*>(p); p += al(px * 32);
+    L.fb.colors = reinterpret_cast<uint2*>(p); p += al(px * 32);
+    L.fb.sidx = reinterpret_cast<uint4*>(p); p += al(px * 16);
+    L.fb.counts = reinterpret_cast<uint32_t*>(p);
+    L.frag_pixels = px;
+  }
   if (C.mem) return VT_OK;
   const size_t n = size_t(C.W) * C.H;
   const size_t bytes = al(n * 32) + al(n * 16) + al(n * 4) + al(16);
@@ -348,9 +365,9 @@ vt_status vt_lite_render_camera(vt_ctx* ctx, uint32_t camera, float* out_rgba) {
   a.circle = camera == uint32_t(ctx->S.cams.size()) ? float(L.o.scope_circle_frac * L.o.scope_width / 2.0) : 0.0f;
   a.env_mat = L.o.env_material;
   a.out = C.rad;
-  vtl::launch_shade(S, g, v, a, ctx->stream);
+  vtl::launch_shade(S, g, v, a, L.fb, big_blocks(ctx) * 2, ctx->stream);
   VT_CK(cudaGetLastError());
-  L.launches += 5;
+  L.launches += 7;
   VT_CK(cudaEventRecord(L.ev[3], ctx->stream));
   VT_CK(cudaMemcpyAsync(&L.big_tris, L.big, 4, cudaMemcpyDeviceToHost, ctx->stream));
   if (out_rgba) { if ((s = from_device(ctx, out_rgba, C.rad, size_t(C.W) * C.H * 16)) != VT_OK) return s; }

@@ -178,6 +178,9 @@ struct vt_ctx {
       bool rendered = false, displayed = false;
     };
     std::vector<LCam> cams;              // the scene cameras, then SCOPE
+    void* frag_mem = nullptr;            // fragment-list scratch shared by the cameras (grown to the largest view)
+    size_t frag_pixels = 0;
+    vtl::FragBufs fb{};
     int32_t last_clip_cam = -1;
     double build_ms = 0, sm_static_ms = 0, sm_dyn_ms = 0, cam_ms = 0, raster_ms = 0, shade_ms = 0;
     uint32_t big_tris = 0, launches = 0, shadow_big = 0;

@@ -1,7 +1,9 @@
 // The raster camera pass of lite_nodes on sm_103a, around the rasteriser of vt_lite_raster.cu: the vertex stage
 // (vsCam / vsShadow) and the fragment stage fused with the MSAA resolve and FINISH (lite_nodes/renderer.js:92-374).
 //
-// The fragment stage runs once per (pixel, triangle) among the pixel's surviving samples at the pixel centre, with
+// The fragment stage runs once per (pixel, triangle) among the pixel's surviving samples at the pixel centre (a list
+// of such fragments is built first, static-surface and posed-body fragments apart, so the shading threads of a warp
+// do the same work), with
 // perspective-correct attributes of the unclipped triangle (2D-homogeneous barycentrics, Olano and Greer 1997), as
 // a raster pipeline's centre interpolation does. The 3x3 shadow-map taps one texel apart share one bilinear
 // fraction, so the 16 texels under them are compared once per map.
@@ -305,33 +307,84 @@ __device__ float3 fragment(const Scene& S, const Geo& g, const View& V, const Sh
 
 __device__ __forceinline__ float h16(float x) { return __half2float(__float2half_rn(x)); }
 
-__global__ void __launch_bounds__(128) shade_kernel(const Scene S, const Geo g, const View V, const ShadeArgs a) {
-  const uint32_t W = uint32_t(V.size[0]), H = uint32_t(V.size[1]);
-  const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15), py = blockIdx.y * 8 + (threadIdx.x >> 4);
-  if (px >= W || py >= H) return;
-  const size_t pix = size_t(py) * W + px;
-  unsigned long long k[4];
-  for (int s = 0; s < 4; s++) k[s] = a.key[pix * 4 + s];
-  float3 col[4];
-  uint32_t done = 0;
+// Fragment list: per pixel, each distinct triangle among its 4 samples becomes one fragment, static-surface
+// fragments (24 emitter samples, capsule occlusion) appended from the front of the list and posed-body fragments (96
+// emitter samples) from the back, so a warp of the shading kernel runs fragments of one kind; sidx[pixel] holds each
+// sample's fragment (MISS: empty). Appends are one atomic per warp and kind.
+__global__ void __launch_bounds__(256) frag_kernel(const unsigned long long* __restrict__ key, uint32_t W, uint32_t H, uint32_t n_static_tris,
+                                                    uint2* __restrict__ frags, uint32_t cap, uint32_t* __restrict__ counts, uint4* __restrict__ sidx) {
+  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = pix < W * H;
+  uint32_t id[4], f[4], ns = 0, nd = 0;
+  bool fresh[4];
   for (int s = 0; s < 4; s++) {
-    if (done & (1u << s)) continue;
-    float3 c = f3(0.0f, 0.0f, 0.0f);
-    if (k[s] != EMPTY_KEY) {
-      c = fragment(S, g, V, a, uint32_t(k[s] & 0xffffffffu), px, py);
-      c = f3(h16(c.x), h16(c.y), h16(c.z));
-    }
-    for (int t = s; t < 4; t++)
-      if (!(done & (1u << t)) && (uint32_t(k[t] & 0xffffffffu) == uint32_t(k[s] & 0xffffffffu)) && ((k[t] == EMPTY_KEY) == (k[s] == EMPTY_KEY))) {
-        col[t] = c;
-        done |= 1u << t;
-      }
+    const unsigned long long k = live ? key[size_t(pix) * 4 + s] : EMPTY_KEY;
+    id[s] = k == EMPTY_KEY ? MISS : uint32_t(k & 0xffffffffu);
+    fresh[s] = id[s] != MISS;
+    for (int t = 0; t < s; t++) fresh[s] = fresh[s] && id[t] != id[s];
+    if (fresh[s]) { if (id[s] < n_static_tris) ns++; else nd++; }
   }
-  // resolve (average of the samples into rgba16float), then FINISH: x 1 / outScale, the SCOPE circle mask
+  // warp-wide exclusive prefix sums of the new fragments of each kind
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t ps = ns, pd = nd;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t a = __shfl_up_sync(0xffffffffu, ps, o), b = __shfl_up_sync(0xffffffffu, pd, o);
+    if (lane >= uint32_t(o)) { ps += a; pd += b; }
+  }
+  const uint32_t ts = __shfl_sync(0xffffffffu, ps, 31), td = __shfl_sync(0xffffffffu, pd, 31);
+  uint32_t bs = 0, bd = 0;
+  if (lane == 0) { bs = ts ? atomicAdd(counts, ts) : 0; bd = td ? atomicAdd(counts + 1, td) : 0; }
+  bs = __shfl_sync(0xffffffffu, bs, 0) + ps - ns;
+  bd = __shfl_sync(0xffffffffu, bd, 0) + pd - nd;
+  if (!live) return;
+  for (int s = 0; s < 4; s++) {
+    if (id[s] == MISS) { f[s] = MISS; continue; }
+    if (!fresh[s]) {
+      for (int t = 0; t < s; t++)
+        if (id[t] == id[s]) { f[s] = f[t]; break; }
+      continue;
+    }
+    f[s] = id[s] < n_static_tris ? bs++ : cap - 1u - bd++;
+    frags[f[s]] = make_uint2(pix, id[s]);
+  }
+  sidx[pix] = make_uint4(f[0], f[1], f[2], f[3]);
+}
+
+// one thread per fragment: the static fragments, then the posed-body ones; colours stored as half floats (the
+// multisample target is rgba16float)
+__global__ void __launch_bounds__(128) shade_frag_kernel(const Scene S, const Geo g, const View V, const ShadeArgs a, const uint2* __restrict__ frags,
+                                                         uint32_t cap, const uint32_t* __restrict__ counts, uint2* __restrict__ colors) {
+  const uint32_t ns = counts[0], nd = counts[1];
+  const uint32_t W = uint32_t(V.size[0]);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ns + nd; i += gridDim.x * blockDim.x) {
+    const uint32_t fi = i < ns ? i : cap - nd + (i - ns);
+    const uint2 fr = frags[fi];
+    const float3 c = fragment(S, g, V, a, fr.y, fr.x % W, fr.x / W);
+    const __half2 rg = __floats2half2_rn(c.x, c.y), bz = __floats2half2_rn(c.z, 0.0f);
+    colors[fi] = make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&bz));
+  }
+}
+
+// resolve (average of the 4 samples into rgba16float), then FINISH: x 1 / outScale, the SCOPE circle mask
+__global__ void __launch_bounds__(256) resolve_kernel(const View V, const ShadeArgs a, const uint4* __restrict__ sidx, const uint2* __restrict__ colors) {
+  const uint32_t W = uint32_t(V.size[0]), H = uint32_t(V.size[1]);
+  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= W * H) return;
+  const uint4 f = sidx[pix];
+  const uint32_t fs[4] = {f.x, f.y, f.z, f.w};
+  float3 col[4];
+  for (int s = 0; s < 4; s++) {
+    col[s] = f3(0.0f, 0.0f, 0.0f);
+    if (fs[s] == MISS) continue;
+    const uint2 c = colors[fs[s]];
+    const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&c.x));
+    col[s] = f3(rg.x, rg.y, __low2float(*reinterpret_cast<const __half2*>(&c.y)));
+  }
   float3 r = f3(h16((((col[0].x + col[1].x) + col[2].x) + col[3].x) * 0.25f), h16((((col[0].y + col[1].y) + col[2].y) + col[3].y) * 0.25f),
                 h16((((col[0].z + col[1].z) + col[2].z) + col[3].z) * 0.25f));
   r = r * a.inv_scale;
   if (a.circle > 0.0f) {
+    const uint32_t px = pix % W, py = pix / W;
     const float qx = float(px) + 0.5f - 0.5f * float(W), qy = float(py) + 0.5f - 0.5f * float(H);
     if (len2(qx, qy) > a.circle) r = f3(0.0f, 0.0f, 0.0f);
   }
@@ -348,9 +401,12 @@ void launch_vertex_shadow(const Scene& S, const Geo& g, const View& v, uint32_t 
   if (!count) return;
   vertex_shadow_kernel<<<(count + 255) / 256, 256, 0, st>>>(S, g, v, first, count, clip);
 }
-void launch_shade(const Scene& S, const Geo& g, const View& v, const ShadeArgs& a, cudaStream_t st) {
+void launch_shade(const Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int blocks, cudaStream_t st) {
   const uint32_t W = uint32_t(v.size[0]), H = uint32_t(v.size[1]);
-  dim3 grid((W + 15) / 16, (H + 7) / 8);
-  shade_kernel<<<grid, 128, 0, st>>>(S, g, v, a);
+  const uint32_t cap = W * H * 4u;
+  cudaMemsetAsync(fb.counts, 0, 8, st);
+  frag_kernel<<<(W * H + 255) / 256, 256, 0, st>>>(a.key, W, H, g.n_static_tris, fb.frags, cap, fb.counts, fb.sidx);
+  shade_frag_kernel<<<blocks, 128, 0, st>>>(S, g, v, a, fb.frags, cap, fb.counts, fb.colors);
+  resolve_kernel<<<(W * H + 255) / 256, 256, 0, st>>>(v, a, fb.sidx, fb.colors);
 }
 }  // namespace vtl

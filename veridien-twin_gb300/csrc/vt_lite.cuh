@@ -7,9 +7,10 @@
 //              snap to 1/256 pixel, exact int64 edge functions; every covered sample takes atomicMin(depth bits << 32
 //              | triangle) (64-bit keys for the camera's 4 samples, 32-bit depth for a shadow map). Triangles whose
 //              box holds more than 256 samples are queued as 32 x 32-pixel tiles that a warp per tile rasterises.
-//   shade      one thread per pixel: each distinct triangle among its samples is shaded once at the pixel centre
-//              (the fragment stage), colours rounded to half, averaged, rounded to half, scaled back (the MSAA
-//              resolve into rgba16float and the FINISH pass)
+//   shade      a fragment list (each distinct triangle among a pixel's samples, static and posed-body fragments
+//              apart), one thread per fragment shading at the pixel centre (the fragment stage, colours rounded to
+//              half), then per pixel the average of the samples rounded to half and scaled back (the MSAA resolve
+//              into rgba16float and the FINISH pass)
 #pragma once
 
 #include <cuda_runtime.h>
@@ -79,8 +80,15 @@ void launch_vertex_shadow(const vtd::Scene& S, const Geo& g, const View& v, uint
 // vertices are [v0, v0 + nv); snaps: scratch of one int4 per clip entry
 void launch_raster(const float4* clip, int4* snaps, const uint32_t* idx, uint32_t n_verts, uint32_t v0, uint32_t nv, uint32_t t0, uint32_t nt,
                    uint32_t layers, const Target& T, int blocks_big, cudaStream_t st);
-// fragment stage + resolve + finish
-void launch_shade(const vtd::Scene& S, const Geo& g, const View& v, const ShadeArgs& a, cudaStream_t st);
+// the fragment list and its shading (scratch for a w x h view: frags and colors w*h*4 entries, sidx w*h)
+struct FragBufs {
+  uint2* frags;                // (pixel, triangle): static fragments from the front, posed-body ones from the back
+  uint2* colors;               // per fragment: rgb as half floats
+  uint4* sidx;                 // per pixel: each sample's fragment, MISS = empty
+  uint32_t* counts;            // [0] static, [1] posed-body fragments
+};
+// fragment list + fragment stage + resolve + finish
+void launch_shade(const vtd::Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int blocks, cudaStream_t st);
 // clear a 32-bit depth target to all ones
 void launch_fill(uint32_t* p, size_t n, uint32_t value, cudaStream_t st);
 
