@@ -188,6 +188,7 @@ def main():
     ap.add_argument("--no-nodes", action="store_true")
     ap.add_argument("--no-sensor", action="store_true")
     ap.add_argument("--no-twin-frame", action="store_true")
+    ap.add_argument("--no-lite", action="store_true")
     ap.add_argument("--case", default=None, help="render:W:H:SPP or radiosity:N:PREC:SWEEPS (a small profiling case)")
     args = ap.parse_args()
     if args.case:
@@ -303,6 +304,8 @@ def main():
             line["sensor_chain"] = sensor_bench(torch, local)
         if not args.no_twin_frame:
             line["twin_frame"] = twin_frame_bench(torch, local)
+        if not args.no_lite:
+            line["lite_frame"] = lite_frame_bench(torch, local)
         print(json.dumps(line))
     r.destroy()
     if dist:
