@@ -70,6 +70,8 @@ typedef struct {
   float build_dir[3];    /* FDM build direction (layer lines) */
   float layer_period;    /* m, 0 = no layer lines */
   float layer_depth;     /* m */
+  uint32_t overview_only;/* 1: scene.json `overview_only` (outside the cavity: left out of its body's occlusion capsule and
+                            effective albedo, gpu/scene_gpu.js:427-450, and of the raster pass, lite_nodes/renderer.js:529) */
 } vt_mesh;
 
 /* A material as gpu/bsdf.js:68 prepareMaterial receives it (values unwrapped from physics.yaml). */
@@ -562,6 +564,33 @@ vt_status vt_lite_debug(vt_ctx* ctx, int what, uint32_t camera, void* dst, size_
  * (1 sample: a shadow-map layer, depth only, the triangle bits all ones). Host or device buffers. */
 vt_status vt_raster(vt_ctx* ctx, const float* clip, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris, uint32_t width,
                     uint32_t height, uint32_t samples, uint64_t* keys);
+
+/* ------------------------------------------------------------------ scene preparation (host, no device) */
+
+/* The mesh clean-up the reference runs in JavaScript before packing (gpu/scene_gpu.js), for callers that load a
+ * scene directory (scene.json + meshes/\*.bin): results are library-owned until vt_mesh_free. Positions and normals
+ * are doubles (the JavaScript keeps numbers), indices 3 per triangle. */
+typedef struct {
+  double* P;           /* n_verts x 3 */
+  double* N;           /* n_verts x 3 */
+  uint32_t* I;         /* n_idx */
+  uint32_t n_verts, n_idx;
+  void* handle;
+} vt_mesh_out;
+/* gpu/scene_gpu.js:68 weld: merge vertices whose positions agree to 1e-7 m and normals to 1e-4 (keys rounded as
+ * JavaScript's Math.round does), in order of first appearance; triangles that become degenerate are dropped. */
+vt_status vt_weld(const float* P, const float* N, uint32_t n_verts, const uint32_t* I, uint32_t n_idx, vt_mesh_out* out);
+/* gpu/scene_gpu.js:95 subdivide: conforming edge bisection, every pass splitting all edges longer than h at their
+ * midpoints (one shared vertex per edge, numbered in the order the edges are met) and re-triangulating each
+ * triangle by its pattern of split edges, until no edge is longer than h or after max_passes (24). */
+vt_status vt_subdivide(const double* P, const double* N, uint32_t n_verts, const uint32_t* I, uint32_t n_idx, double h, uint32_t max_passes,
+                       vt_mesh_out* out);
+/* gpu/scene_gpu.js:146 benchMesh: a grid of cells <= h over `fine` (x0, y0, x1, y1) within `extent` and four coarse
+ * quads out to the extent, at height z, normal +z. */
+vt_status vt_bench_mesh(double z, const double extent[4], const double fine[4], double h, vt_mesh_out* out);
+/* gpu/scene_gpu.js:37 computeNormals: area-weighted vertex normals for a mesh shipped without them. */
+vt_status vt_compute_normals(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t n_idx, float* N);
+void vt_mesh_free(vt_mesh_out* mesh);
 
 /* ---------------------------------------------------------------------------------------- bvh (pure) */
 

@@ -6,6 +6,7 @@ ctypes front of oracle/libvtoracle.so, the CPU restatement of the reference's re
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 import sys
@@ -469,3 +470,134 @@ def lite_display(du, prev, radiance):
                           _p(L, C.c_float), C.c_uint32(W), C.c_uint32(H), _p(rgba, C.c_uint8), _p(st, C.c_uint32))
     return rgba, st
 
+
+
+# ---- scene preparation (gpu/scene_gpu.js:37-165), restated in plain Python for small meshes
+def _js_round(x):
+    return math.floor(x + 0.5)
+
+
+def _js_hypot3(x, y, z):
+    v = [abs(x), abs(y), abs(z)]
+    mx = max(v)
+    if mx == 0:
+        return 0.0
+    s = c = 0.0
+    for a in v:
+        n = a / mx
+        summand = n * n - c
+        pre = s + summand
+        c = (pre - s) - summand
+        s = pre
+    return math.sqrt(s) * mx
+
+
+def weld_ref(P, N, I):
+    P = np.asarray(P, np.float32).reshape(-1, 3).astype(np.float64)
+    N = np.asarray(N, np.float32).reshape(-1, 3).astype(np.float64)
+    seen, P2, N2, remap = {}, [], [], []
+    for v in range(len(P)):
+        k = tuple(_js_round(float(x) * 1e7) for x in P[v]) + tuple(_js_round(float(x) * 1e4) for x in N[v])
+        if k not in seen:
+            seen[k] = len(P2)
+            P2.append(P[v]); N2.append(N[v])
+        remap.append(seen[k])
+    I2 = []
+    for t in np.asarray(I, np.uint32).reshape(-1, 3):
+        a, b, c = remap[t[0]], remap[t[1]], remap[t[2]]
+        if a == b or b == c or a == c:
+            continue
+        I2 += [a, b, c]
+    return np.array(P2).reshape(-1, 3), np.array(N2).reshape(-1, 3), np.array(I2, np.uint32)
+
+
+def subdivide_ref(P, N, I, h, max_passes=24):
+    P = [list(map(float, p)) for p in np.asarray(P, np.float64).reshape(-1, 3)]
+    N = [list(map(float, n)) for n in np.asarray(N, np.float64).reshape(-1, 3)]
+    tris = [int(x) for x in np.asarray(I).ravel()]
+    h2 = h * h
+    len2 = lambda a, b: (P[a][0] - P[b][0]) ** 2 + (P[a][1] - P[b][1]) ** 2 + (P[a][2] - P[b][2]) ** 2
+    for _ in range(max_passes):
+        mid, anyc = {}, False
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key in mid:
+                return mid[key]
+            m = len(P)
+            P.append([0.5 * (P[a][k] + P[b][k]) for k in range(3)])
+            n = [N[a][k] + N[b][k] for k in range(3)]
+            l = _js_hypot3(*n)
+            N.append([x / l for x in n] if l > 1e-6 else list(N[a]))
+            mid[key] = m
+            return m
+
+        out = []
+        for k in range(0, len(tris), 3):
+            v = tris[k:k + 3]
+            mk = [len2(v[0], v[1]) > h2, len2(v[1], v[2]) > h2, len2(v[2], v[0]) > h2]
+            cnt = sum(mk)
+            if not cnt:
+                out += v
+                continue
+            anyc = True
+            if cnt == 3:
+                a, b, c = midpoint(v[0], v[1]), midpoint(v[1], v[2]), midpoint(v[2], v[0])
+                out += [v[0], a, c, a, v[1], b, c, b, v[2], a, b, c]
+            elif cnt == 1:
+                e = mk.index(True)
+                p, q, r = v[e], v[(e + 1) % 3], v[(e + 2) % 3]
+                m = midpoint(p, q)
+                out += [p, m, r, m, q, r]
+            else:
+                e = mk.index(False)
+                Aa, Bb, Cc = v[e], v[(e + 1) % 3], v[(e + 2) % 3]
+                mBC, mCA = midpoint(Bb, Cc), midpoint(Cc, Aa)
+                out += [mCA, mBC, Cc]
+                out += [Aa, Bb, mBC, Aa, mBC, mCA] if len2(Aa, mBC) < len2(Bb, mCA) else [Aa, Bb, mCA, Bb, mBC, mCA]
+        tris = out
+        if not anyc:
+            break
+    return np.array(P), np.array(N), np.array(tris, np.uint32)
+
+
+def bench_mesh_ref(z, extent, fine, h):
+    (ex0, ey0), (ex1, ey1) = extent
+    fx0, fy0, fx1, fy1 = max(ex0, fine[0][0]), max(ey0, fine[0][1]), min(ex1, fine[1][0]), min(ey1, fine[1][1])
+    nx, ny = max(1, math.ceil((fx1 - fx0) / (h * 0.999))), max(1, math.ceil((fy1 - fy0) / (h * 0.999)))
+    P, I = [], []
+
+    def v(x, y):
+        P.append([x, y, z])
+        return len(P) - 1
+
+    grid = [[v(fx0 + (fx1 - fx0) * i / nx, fy0 + (fy1 - fy0) * j / ny) for i in range(nx + 1)] for j in range(ny + 1)]
+    for j in range(ny):
+        for i in range(nx):
+            a, b, c, d = grid[j][i], grid[j][i + 1], grid[j + 1][i], grid[j + 1][i + 1]
+            I += [a, b, d, a, d, c] if (i + j) & 1 else [a, b, c, b, d, c]
+
+    def quad(x0, y0, x1, y1):
+        if not (x1 > x0 and y1 > y0):
+            return
+        a, b, c, d = v(x0, y0), v(x1, y0), v(x0, y1), v(x1, y1)
+        I.extend([a, b, d, a, d, c])
+
+    quad(ex0, ey0, ex1, fy0); quad(ex0, fy1, ex1, ey1); quad(ex0, fy0, fx0, fy1); quad(fx1, fy0, ex1, fy1)
+    return np.array(P), np.tile([0.0, 0.0, 1.0], (len(P), 1)), np.array(I, np.uint32)
+
+
+def compute_normals_ref(P, I):
+    P = np.asarray(P, np.float32).reshape(-1, 3)
+    N = np.zeros_like(P)
+    for t in np.asarray(I).reshape(-1, 3):
+        a, b, c = (P[i].astype(np.float64) for i in t)
+        u, w = b - a, c - a
+        n = [u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]]
+        for i in t:
+            for k in range(3):
+                N[i, k] = np.float32(float(N[i, k]) + n[k])
+    for i in range(len(N)):
+        l = _js_hypot3(float(N[i, 0]), float(N[i, 1]), float(N[i, 2])) or 1.0
+        N[i] = [np.float32(float(N[i, k]) / l) for k in range(3)]
+    return N

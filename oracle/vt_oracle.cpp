@@ -951,15 +951,31 @@ static Scene* prepare_scene(const vt_scene_desc* sd, int leafSize, int albedoSam
     S->emitTris.push_back(e.area);
     S->emitTris.push_back(e.cdf);
   }
-  // capsules, rhoEff (gpu/scene_gpu.js:431-456); no overview_only meshes: occCapsule = capsule
+  // capsules, rhoEff (gpu/scene_gpu.js:427-456): overview_only meshes (outside the cavity) are left out of the
+  // occlusion capsule and the effective albedo
   for (uint32_t bi = 0; bi < sd->n_bodies; bi++) {
     const vt_body_desc& B = sd->bodies[bi];
     Blas& bl = S->blas[bi];
     fit_capsule(B.P, B.n_verts, bl.cap_a, bl.cap_b, bl.cap_r);
-    for (int k = 0; k < 3; k++) { bl.occ_a[k] = bl.cap_a[k]; bl.occ_b[k] = bl.cap_b[k]; }
-    bl.occ_r = bl.cap_r;
+    std::vector<char> used(B.n_verts, 0);
+    bool dropped = false;
+    for (uint32_t t = 0; t < B.n_tris; t++) {
+      if (sd->meshes[B.tri_mesh[t]].overview_only) { dropped = true; continue; }
+      used[B.I[3 * t]] = used[B.I[3 * t + 1]] = used[B.I[3 * t + 2]] = 1;
+    }
+    if (!dropped) {
+      for (int k = 0; k < 3; k++) { bl.occ_a[k] = bl.cap_a[k]; bl.occ_b[k] = bl.cap_b[k]; }
+      bl.occ_r = bl.cap_r;
+    } else {
+      std::vector<float> kept;
+      for (uint32_t v = 0; v < B.n_verts; v++)
+        if (used[v]) { kept.push_back(B.P[3 * v]); kept.push_back(B.P[3 * v + 1]); kept.push_back(B.P[3 * v + 2]); }
+      if (kept.empty()) { for (int k = 0; k < 3; k++) bl.occ_a[k] = bl.occ_b[k] = 0; bl.occ_r = 0; }
+      else fit_capsule(kept.data(), kept.size() / 3, bl.occ_a, bl.occ_b, bl.occ_r);
+    }
     double ar = 0, rho = 0;
     for (uint32_t t = 0; t < B.n_tris; t++) {
+      if (dropped && sd->meshes[B.tri_mesh[t]].overview_only) continue;
       size_t a = size_t(B.I[3 * t]) * 3, c = size_t(B.I[3 * t + 1]) * 3, d = size_t(B.I[3 * t + 2]) * 3;
       double ux = double(B.P[c]) - B.P[a], uy = double(B.P[c + 1]) - B.P[a + 1], uz = double(B.P[c + 2]) - B.P[a + 2];
       double vx = double(B.P[d]) - B.P[a], vy = double(B.P[d + 1]) - B.P[a + 1], vz = double(B.P[d + 2]) - B.P[a + 2];
@@ -2670,6 +2686,7 @@ static void geometry(const Scene& S, double h, double hfix, std::vector<uint32_t
     std::vector<uint32_t> meshes;
     for (uint32_t k = 0; k < B.tri_count; k++) {
       const uint32_t m = S.tris[16 * size_t(B.tri_off + k) + 12];
+      if (m < S.meshes.size() && S.meshes[m].overview_only) continue;   // not drawn by the raster pass
       if (std::find(meshes.begin(), meshes.end(), m) == meshes.end()) meshes.push_back(m);
     }
     for (uint32_t m : meshes) {

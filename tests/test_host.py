@@ -19,7 +19,7 @@ from vtwin.renderer import build_bvh
 def declared_symbols():
     text = open(os.path.join(ROOT, "include", "vtwin.h")).read()
     # function declarations: a return type at the start of a line, then the vt_ name and its parameter list
-    return sorted(set(re.findall(r"^(?:vt_status|uint32_t|const char\*|void\*)\s+(vt_[a-z0-9_]+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:vt_status|uint32_t|const char\*|void\*|void)\s+(vt_[a-z0-9_]+)\s*\(", text, re.M)))
 
 
 def test_library_exports_every_declared_symbol():

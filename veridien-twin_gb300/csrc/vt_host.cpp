@@ -647,15 +647,31 @@ Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_sa
   S.emit_area = total;
   S.emit_tris = uint32_t(emit.size());
   S.emitters = emit;
-  // body capsules and effective albedo (scene_gpu.js:431-456); no overview-only meshes, so occlusion = bounding capsule
+  // body capsules and effective albedo (scene_gpu.js:427-456): the bounding capsule of every vertex; the occlusion
+  // capsule and the effective albedo from the triangles of meshes in the cavity (not overview-only)
   for (uint32_t b = 0; b < d.n_bodies; b++) {
     const vt_body_desc& B = d.bodies[b];
     BodyRec& r = S.bodies[b];
     capsule_fit(B.P, B.n_verts, r.cap_a, r.cap_b, r.cap_r);
-    for (int k = 0; k < 3; k++) { r.occ_a[k] = r.cap_a[k]; r.occ_b[k] = r.cap_b[k]; }
-    r.occ_r = r.cap_r;
+    std::vector<uint8_t> keep(B.n_verts, 0);
+    bool any_drop = false;
+    for (uint32_t t = 0; t < B.n_tris; t++) {
+      if (d.meshes[B.tri_mesh[t]].overview_only) { any_drop = true; continue; }
+      for (int k = 0; k < 3; k++) keep[B.I[3 * t + k]] = 1;
+    }
+    if (any_drop) {
+      std::vector<float> pc;
+      for (uint32_t v = 0; v < B.n_verts; v++)
+        if (keep[v]) for (int k = 0; k < 3; k++) pc.push_back(B.P[3 * size_t(v) + k]);
+      if (pc.empty()) { for (int k = 0; k < 3; k++) { r.occ_a[k] = 0; r.occ_b[k] = 0; } r.occ_r = 0; }
+      else capsule_fit(pc.data(), uint32_t(pc.size() / 3), r.occ_a, r.occ_b, r.occ_r);
+    } else {
+      for (int k = 0; k < 3; k++) { r.occ_a[k] = r.cap_a[k]; r.occ_b[k] = r.cap_b[k]; }
+      r.occ_r = r.cap_r;
+    }
     double ar = 0, rho = 0;
     for (uint32_t t = 0; t < B.n_tris; t++) {
+      if (any_drop && d.meshes[B.tri_mesh[t]].overview_only) continue;
       const float* p0 = B.P + 3 * size_t(B.I[3 * t]);
       const float* p1 = B.P + 3 * size_t(B.I[3 * t + 1]);
       const float* p2 = B.P + 3 * size_t(B.I[3 * t + 2]);

@@ -129,6 +129,7 @@ LiteGeom lite_geometry(const Prepared& S, double h, double h_fixture) {
     for (uint32_t k = 0; k < bl.tri_count; k++) {
       const uint32_t* t = S.tris.data() + size_t(bl.tri_off + k) * 16;
       const uint32_t mesh = t[12];
+      if (mesh < S.meshes.size() && S.meshes[mesh].overview_only) continue;   // outside the cavity: not drawn
       auto it = by_mesh.find(mesh);
       if (it == by_mesh.end()) { mesh_order.push_back(mesh); it = by_mesh.emplace(mesh, std::vector<uint32_t>()).first; }
       it->second.push_back(t[3]); it->second.push_back(t[7]); it->second.push_back(t[11]);

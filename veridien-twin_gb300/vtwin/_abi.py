@@ -29,7 +29,7 @@ f64p = C.POINTER(C.c_double)
 
 class vt_mesh(C.Structure):
     _fields_ = [("mat", C.c_uint32), ("flags", C.c_uint32), ("build_dir", C.c_float * 3),
-                ("layer_period", C.c_float), ("layer_depth", C.c_float)]
+                ("layer_period", C.c_float), ("layer_depth", C.c_float), ("overview_only", C.c_uint32)]
 
 
 class vt_material(C.Structure):
@@ -168,6 +168,11 @@ class vt_lite_info(C.Structure):
                 ("shadow_big_tiles", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class vt_mesh_out(C.Structure):
+    _fields_ = [("P", C.POINTER(C.c_double)), ("N", C.POINTER(C.c_double)), ("I", C.POINTER(C.c_uint32)), ("n_verts", C.c_uint32),
+                ("n_idx", C.c_uint32), ("handle", C.c_void_p)]
+
+
 VT_LITE_VIEW, VT_LITE_CLIP, VT_LITE_KEYS, VT_LITE_SM_STATIC, VT_LITE_SM_DYN, VT_LITE_SM_CLIP, VT_LITE_GEOM, VT_LITE_INDEX, VT_LITE_EMIT = range(9)
 
 
@@ -245,6 +250,7 @@ class SceneDesc:
             marr[i].build_dir[:] = [float(x) for x in m.get("build_dir", [0, 0, 1])]
             lay = m.get("layer", [0.0, 0.0])
             marr[i].layer_period, marr[i].layer_depth = float(lay[0]), float(lay[1])
+            marr[i].overview_only = int(bool(m.get("overview_only", False)))
         d.meshes, d.n_meshes = marr, len(meshes)
         mats = scene["materials"]
         tarr = (vt_material * len(mats))()

@@ -32,6 +32,11 @@ SIGNATURES = {
     "vt_sensor_camera": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_float]),
     "vt_sensor_frame": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(A.vt_sensor_uniform), C.c_void_p]),
     "vt_render_frame": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_frame_req)]),
+    "vt_weld": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(A.vt_mesh_out)]),
+    "vt_subdivide": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_double, C.c_uint32, C.POINTER(A.vt_mesh_out)]),
+    "vt_bench_mesh": (C.c_int32, [C.c_double, C.c_void_p, C.c_void_p, C.c_double, C.POINTER(A.vt_mesh_out)]),
+    "vt_compute_normals": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vt_mesh_free": (None, [C.POINTER(A.vt_mesh_out)]),
     "vt_lite_create": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_lite_opts), C.POINTER(A.vt_lite_info)]),
     "vt_lite_info_get": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_lite_info)]),
     "vt_lite_geometry": (C.c_int32, [C.POINTER(A.vt_scene_desc), C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
