@@ -245,3 +245,62 @@ def test_raster_entry_point_matches_restatement():
             assert (got != EMPTY).mean() > 0.3
     finally:
         tr.destroy()
+
+
+def test_parity_after_the_scope_moves(lite):
+    """A second pose with the scope moved: emitter samples, sector origins and both shadow maps re-made; keys and
+    maps bit-exact again, fragments within tolerance (also for SCOPE, whose camera follows the scope)."""
+    sc, r, S, poses = lite
+    r.set_pose_array(poses[2])
+    es, _ = S.lite_emitter(96, poses[2][0])
+    assert np.abs(r.debug_buffer(A.VT_LITE_EMIT) - es).max() <= 1e-7
+    V, I = r.debug_buffer(A.VT_LITE_GEOM), r.debug_buffer(A.VT_LITE_INDEX)
+    for c in (0, len(r.cameras) - 1):
+        w, h = r.size(c)
+        out = np.zeros((h, w, 4), np.float32)
+        r.renderCamera(c, out=out)
+        clip, keys = r.debug_buffer(A.VT_LITE_CLIP, c), r.debug_buffer(A.VT_LITE_KEYS, c)
+        assert np.array_equal(keys, O.raster(clip, I, w, h, 4))
+        st, slot = r.tr.get_node_state()
+        S.set_node_state(st, slot)
+        S.load_uniform(r.tr.scene_uniform())
+        sms, smd = r.debug_buffer(A.VT_LITE_SM_STATIC), r.debug_buffer(A.VT_LITE_SM_DYN)
+        circle = 0.95 * w / 2 if r.cameras[c] == "SCOPE" else 0.0
+        want = S.lite_shade(r.view(c), V, I, clip, keys, r.debug_buffer(A.VT_LITE_EMIT), sms, smd,
+                            float(1.0 / (1000.0 / max(sc["emitter"]["L0"]))), circle=circle)
+        g, wv = out[..., :3].astype(np.float64), want[..., :3].astype(np.float64)
+        rel = np.abs(g - wv) / np.maximum(np.abs(wv), 1e-3 * max(wv.max(), 1e-30))
+        print(f"\nmoved scope, camera {r.cameras[c]}: within 1e-3 {(rel <= 1e-3).mean():.5f}")
+        assert (rel <= 1e-3).mean() > 0.999
+    sclip = r.debug_buffer(A.VT_LITE_SM_CLIP)
+    ns = int(r.info()["staticTris"])
+    sm = r.debug_buffer(A.VT_LITE_SM_STATIC)
+    want = O.raster(sclip[1], I, 512, 512, 1, t0=0, nt=ns)[..., 0]
+    wd = (want >> np.uint64(32)).astype(np.uint32)
+    wd[want == EMPTY] = 0xFFFFFFFF
+    assert np.array_equal(sm[1], wd)
+    r.set_pose_array(poses[0])
+    for c in r.cameras:
+        r.renderCamera(c)
+
+
+def test_debug_modes_no_shadows_and_visibility():
+    """debug 1 renders without shadow maps (every sector visible), debug 2 writes the mean sector visibility as
+    grey (lite_nodes/renderer.js:330-336)."""
+    sc = dome.make_scope_scene(seed=3, level=4, n_tools=2, width=160, height=90)
+    T = dome.scope_poses(1, 2, seed=4)[0]
+    imgs = {}
+    for dbg in (0, 1, 2):
+        r = LiteNodesRenderer.create(sc, smRes=256, scopeSize=(160, 90), debug=dbg)
+        try:
+            r.set_pose_array(T)
+            out = np.zeros((90, 160, 4), np.float32)
+            r.renderCamera(0, out=out)
+            imgs[dbg] = out[..., :3]
+        finally:
+            r.destroy()
+    assert imgs[1].mean() >= imgs[0].mean()                        # no shadows: at least as bright
+    vis = imgs[2]
+    scale = 1000.0 / max(sc["emitter"]["L0"])
+    assert np.isfinite(vis).all() and 0.0 <= vis.min() and vis.max() <= 1.0 / scale * 1.001
+    assert vis.max() > 0

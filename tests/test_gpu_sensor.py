@@ -122,3 +122,22 @@ def test_render_frame_matches_per_camera_calls():
     finally:
         a.destroy()
         b.destroy()
+
+
+def test_render_frame_without_sensor():
+    """vt_render_frame with no sensor uniforms renders every camera as renderCamera does."""
+    sc = dome.make_dome_scene(seed=1, width=97, height=63, level=4, with_instruments=2)
+    sc["cameras"] = dome.batched_cameras(seed=3, n=2, width=64, height=40)
+    T = dome.instrument_poses(n_poses=1, n_tools=2, seed=11)[0]
+    a, b = TwinRenderer.create(sc), TwinRenderer.create(sc)
+    try:
+        for r in (a, b):
+            r.set_pose_array(np.concatenate([A.identity_poses(1), T]))
+        fr = a.renderFrame(spp=2, lightSamples=1, seed=5)
+        for c in list(b.cameras):
+            b.renderCamera(c, spp=2, lightSamples=1, seed=5)
+            assert np.array_equal(a.readback(c, "linear"), b.readback(c, "linear"))
+        assert fr["ms"] > 0 and "stats" not in fr[list(a.cameras)[0]]
+    finally:
+        a.destroy()
+        b.destroy()

@@ -162,3 +162,24 @@ def test_lite_geometry_matches_oracle():
     assert V.shape == Vo.shape and I.shape == Io.shape
     assert np.array_equal(V, Vo) and np.array_equal(I, Io)
     assert len(I) > len(sc["static"]["I"]) + 1000
+
+
+def test_lite_geometry_slices_fixtures_with_their_own_step():
+    """Bodies of kind 'fixture' are sliced with subdiv_fixture (lite_nodes/renderer.js:560), the others with
+    subdiv_h; same words as the restatement."""
+    import oracle as O
+    from vtwin import dome
+    from vtwin.lite import lite_geometry
+
+    sc = dome.make_scope_scene(seed=2, level=3, n_tools=2, width=64, height=36)
+    sc["bodies"][2] = {**sc["bodies"][2], "kind": "fixture"}
+    V, I = lite_geometry(sc, 0.003, 0.01)
+    Vo, Io = O.Scene(sc).lite_geometry(0.003, 0.01)
+    assert np.array_equal(V, Vo) and np.array_equal(I, Io)
+    ns = len(sc["static"]["P"])
+    inst = V[ns:, 3] >> 16
+    P = V[ns:, :3].view(np.float32)
+    tri_inst = inst[I[len(sc["static"]["I"]):, 0] - ns]
+    T = I[len(sc["static"]["I"]):] - ns
+    ext = lambda m: (P[T[m]].max(axis=1) - P[T[m]].min(axis=1)).max()
+    assert ext(tri_inst == 1) <= 0.003 + 1e-7 and 0.003 + 1e-7 < ext(tri_inst == 2) <= 0.01 + 1e-7

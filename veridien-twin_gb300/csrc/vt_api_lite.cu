@@ -463,7 +463,12 @@ vt_status vt_lite_debug(vt_ctx* ctx, int what, uint32_t camera, void* dst, size_
     case VT_LITE_SM_CLIP: src = L.sclip; n = size_t(vtl::K_SECT) * L.n_verts * 16; break;
     case VT_LITE_GEOM: src = L.v; n = size_t(L.n_verts) * 32; break;
     case VT_LITE_INDEX: src = L.idx; n = size_t(L.n_tris) * 12; break;
-    case VT_LITE_EMIT: src = L.es; n = size_t(L.o.ns_dyn) * 32; break;
+    case VT_LITE_EMIT: {
+      vt_status s = lite_poses(ctx);   // the samples as the current poses place them
+      if (s != VT_OK) return s;
+      src = L.es; n = size_t(L.o.ns_dyn) * 32;
+      break;
+    }
     default: return fail(ctx, VT_ERR_ARG, "lite debug: unknown buffer");
   }
   if (bytes < n) return fail(ctx, VT_ERR_ARG, "lite debug: buffer too small");
