@@ -674,7 +674,10 @@ __device__ __forceinline__ float3 emitter_normal(const Scene& S, const Hit& h, c
 }
 
 // ------------------------------------------------------------------------------------------------ indirect
-// cosine-weighted hemisphere fraction hidden by a thin cylinder (gpu/wgsl/shade.wgsl.js:59)
+// cosine-weighted hemisphere fraction hidden by a thin cylinder (gpu/wgsl/shade.wgsl.js:59). The integral's sines
+// come from the angles' tangents instead of sin(): with f = atan(t), sin 2f = 2t / (1 + t^2) and sin^2 f = t^2 /
+// (1 + t^2); an end clamped to f0 -+ pi/2 (f0 = atan2(na, np)) has sin 2f = -sin 2f0 = -2 na np / rho^2 and sin^2 f =
+// cos^2 f0 = np^2 / rho^2, rho^2 = na^2 + np^2. The same integral to float rounding, four sines fewer per capsule.
 __device__ __forceinline__ float capsule_occ(float3 p, float3 n, float3 a, float3 bb, float r) {
   const float3 ab = bb - a;
   const float L = length(ab);
@@ -688,13 +691,25 @@ __device__ __forceinline__ float capsule_occ(float3 p, float3 n, float3 a, float
   float3 ep = -perp / fmaxf(pl, 1e-12f);
   if (pl < 1e-12f) ep = normalize(cross(e, basis_t(e)));
   const float np = dot(n, ep), na = dot(n, e);
-  float f1 = atanf((0.0f - s0) / h), f2 = atanf((L - s0) / h);
+  const float t1 = (0.0f - s0) / h, t2 = (L - s0) / h;
+  float f1 = atanf(t1), f2 = atanf(t2);
   const float f0 = atan2f(na, np);
-  f1 = fmaxf(f1, f0 - 0.5f * PI_F);
-  f2 = fminf(f2, f0 + 0.5f * PI_F);
+  const float rho2 = na * na + np * np;
+  // sin 2f and sin^2 f of each end, clamped or not
+  float s2a = 2.0f * t1 / (1.0f + t1 * t1), sqa = t1 * t1 / (1.0f + t1 * t1);
+  float s2b = 2.0f * t2 / (1.0f + t2 * t2), sqb = t2 * t2 / (1.0f + t2 * t2);
+  if (f0 - 0.5f * PI_F > f1) {
+    f1 = f0 - 0.5f * PI_F;
+    s2a = rho2 > 0.0f ? -2.0f * na * np / rho2 : 0.0f;
+    sqa = rho2 > 0.0f ? np * np / rho2 : 1.0f;
+  }
+  if (f0 + 0.5f * PI_F < f2) {
+    f2 = f0 + 0.5f * PI_F;
+    s2b = rho2 > 0.0f ? -2.0f * na * np / rho2 : 0.0f;
+    sqb = rho2 > 0.0f ? np * np / rho2 : 1.0f;
+  }
   if (f2 <= f1) return 0.0f;
-  const float s1 = sinf(f1), s2 = sinf(f2);
-  const float I = np * (0.5f * (f2 - f1) + 0.25f * (sinf(2.0f * f2) - sinf(2.0f * f1))) + na * 0.5f * (s2 * s2 - s1 * s1);
+  const float I = np * (0.5f * (f2 - f1) + 0.25f * (s2b - s2a)) + na * 0.5f * (sqb - sqa);
   return clampf(INV_PI_F * (2.0f * r / h) * I, 0.0f, 1.0f);
 }
 __device__ __forceinline__ float capsule_vis(const Scene& S, float3 p, float3 n) {
