@@ -69,6 +69,11 @@ vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx**
   const vt::Prepared& S = ctx->S;
   vt_status s;
   if ((s = upload(ctx, &ctx->d_nodes, S.nodes.data(), S.nodes.size() * 4)) != VT_OK) return bail(s);
+  {
+    const std::vector<uint32_t> top = top_records(S.nodes, 0, vtd::TOP_NODES);
+    ctx->n_top = uint32_t(top.size() / VT_NODE_WORDS);
+    if (ctx->n_top && (s = upload(ctx, &ctx->d_top, top.data(), top.size() * 4)) != VT_OK) return bail(s);
+  }
   if ((s = upload(ctx, &ctx->d_tris, S.tris.data(), S.tris.size() * 4)) != VT_OK) return bail(s);
   if ((s = upload(ctx, &ctx->d_verts, S.verts.data(), S.verts.size() * 4)) != VT_OK) return bail(s);
   if ((s = upload(ctx, &ctx->d_params, S.params.data(), S.params.size() * 4)) != VT_OK) return bail(s);
@@ -100,7 +105,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   if (!ctx) return VT_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& c : ctx->cams) { cudaFree(c.radiance); cudaFree(c.raw); cudaFree(c.ri); cudaFree(c.isp_mem); cudaFree(c.hcache); cudaFree(c.scache); }
-  cudaFree(ctx->d_nodes); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
+  cudaFree(ctx->d_nodes); cudaFree(ctx->d_top); cudaFree(ctx->d_tris); cudaFree(ctx->d_verts); cudaFree(ctx->d_params); cudaFree(ctx->d_nstate);
   cudaFree(ctx->d_su); cudaFree(ctx->d_dbg); cudaFree(ctx->d_work); cudaFree(ctx->d_scratch); cudaFree(ctx->d_wave); cudaFree(ctx->tc.mem);
   cudaFree(ctx->batch.su); cudaFree(ctx->batch.cull); cudaFree(ctx->batch.ctr); cudaFree(ctx->batch.sensor); cudaFree(ctx->batch.mem);
   cudaFree(ctx->batch.rad); cudaFree(ctx->batch.raw);

@@ -30,6 +30,8 @@ struct vt_ctx {
   float su_host[vt::SU_WORDS];
   // device scene
   float4 *d_nodes = nullptr, *d_tris = nullptr, *d_verts = nullptr, *d_params = nullptr, *d_nstate = nullptr;
+  float4* d_top = nullptr;      // staged top levels of the static BVH (vtd::TOP_NODES records at most)
+  uint32_t n_top = 0;
   float* d_su = nullptr;
   uint32_t* d_dbg = nullptr;
   uint32_t* d_work = nullptr;   // queue counters of the wavefront path tracer
@@ -226,12 +228,46 @@ inline vt_status ensure_scratch(vt_ctx* ctx, size_t bytes) {
   return VT_OK;
 }
 
+// The staged top levels of the BVH rooted at `root` (the layout of vtd::TOP_NODES): a breadth-first walk assigns
+// slots to the first max_n nodes, and each staged record's references to staged children become TOP_BIT | slot.
+// Empty when a walked child index is not above its parent's or past the array (the traversal's own check then
+// meets it on the global records).
+inline std::vector<uint32_t> top_records(const std::vector<uint32_t>& nodes, uint32_t root, uint32_t max_n) {
+  const uint32_t count = uint32_t(nodes.size() / VT_NODE_WORDS);
+  if (!max_n || root >= count) return {};
+  std::vector<uint32_t> order{root}, out;
+  std::vector<std::pair<uint32_t, uint32_t>> slot_of;   // (node, slot), few entries
+  slot_of.emplace_back(root, 0);
+  for (size_t q = 0; q < order.size(); q++) {
+    const uint32_t* r = nodes.data() + size_t(order[q]) * VT_NODE_WORDS;
+    for (int c = 0; c < 2; c++) {
+      const uint32_t ref = r[8 * c + 3], cnt = r[8 * c + 7];
+      if (cnt) continue;
+      if (ref <= order[q] || ref >= count) return {};
+      if (order.size() < max_n) { slot_of.emplace_back(ref, uint32_t(order.size())); order.push_back(ref); }
+    }
+  }
+  for (uint32_t nd : order) {
+    const uint32_t* r = nodes.data() + size_t(nd) * VT_NODE_WORDS;
+    uint32_t w[VT_NODE_WORDS];
+    std::copy(r, r + VT_NODE_WORDS, w);
+    for (int c = 0; c < 2; c++) {
+      if (w[8 * c + 7]) continue;
+      for (const auto& ps : slot_of)
+        if (ps.first == w[8 * c + 3]) { w[8 * c + 3] = vtd::TOP_BIT | ps.second; break; }
+    }
+    out.insert(out.end(), w, w + VT_NODE_WORDS);
+  }
+  return out;
+}
+
 inline vtd::Scene dev_scene(vt_ctx* ctx) {
   vtd::Scene S;
   S.nodes = ctx->d_nodes; S.tris = ctx->d_tris; S.verts = ctx->d_verts; S.params = ctx->d_params;
   S.su = ctx->d_su; S.nstate = ctx->d_nstate; S.dbg = ctx->d_dbg;
   S.mesh_off = ctx->S.mesh_off; S.mat_off = ctx->S.mat_off; S.alb_off = ctx->S.alb_off; S.prof_off = ctx->S.prof_off;
   S.prof_n = ctx->S.prof_n; S.emit_off = ctx->S.emit_off; S.emit_n = ctx->S.emit_n;
+  S.top = ctx->d_top; S.n_top = ctx->n_top; S.top_root = 0;
   return S;
 }
 

@@ -38,7 +38,22 @@ struct Scene {
   const float4* __restrict__ nstate;
   uint32_t* dbg;
   uint32_t mesh_off, mat_off, alb_off, prof_off, prof_n, emit_off, emit_n;
+  const float4* __restrict__ top;   // the static BVH's top levels, staged in shared memory by the traversal lanes
+  uint32_t n_top, top_root;
 };
+
+// Top levels of the static BVH held in shared memory by the persistent traversal lanes: the first VT_TOP_NODES
+// nodes of a breadth-first walk from the static root, each a copy of its 64-byte record whose interior-child
+// references into the set are rewritten as TOP_BIT | slot (slot 0 is the root). A traversal started at TOP_BIT
+// therefore reads these levels from shared memory and leaves the set through an ordinary global reference; the
+// visit order, and so every hit and counter, is that of the global records. Off by default: on the 657k-triangle
+// dome (640x480, 16 spp, depth 4) the frame takes 24.4 ms with 32 to 256 staged nodes against 21.9 ms without,
+// images identical; the top levels already hit in L1.
+#ifndef VT_TOP_NODES
+#define VT_TOP_NODES 0
+#endif
+constexpr uint32_t TOP_NODES = VT_TOP_NODES;
+constexpr uint32_t TOP_BIT = 0x80000000u;
 
 // ------------------------------------------------------------------------------------------------ float3 math
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
@@ -492,6 +507,7 @@ __device__ __forceinline__ bool trace_phase(const Scene& S, uint32_t root, float
 constexpr uint32_t SH_DEPTH = VT_SH_DEPTH;
 struct LaneStack {
   uint2* sh;           // shared: SH_DEPTH x stride entries of (node, t bits)
+  const float4* top = nullptr;   // shared: the staged top levels (4 float4 per slot), when the kernel stages them
   uint32_t lane, stride;
   uint2 deep[STACK - SH_DEPTH];
   __device__ __forceinline__ void set(uint32_t i, uint32_t node, float t) {
@@ -508,8 +524,22 @@ __device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceStat
   if (++st.visits > MAX_VISITS) { atomicAdd(S.dbg + DBG_VISITS, 1u); return 1; }
   const uint32_t node = st.node;
   const uint32_t inst = st.k < 0 ? MISS : uint32_t(st.k);
+#if VT_TOP_NODES
+  const bool staged = (node & TOP_BIT) != 0u;
+  float4 a0, a1, a2, a3;
+  // a staged node from shared memory, the rest through the read-only global path
+  if (staged) {
+    const float4* nb = stk.top + 4u * (node & 0xffffu);
+    a0 = nb[0]; a1 = nb[1]; a2 = nb[2]; a3 = nb[3];
+  } else {
+    const float4* nb = S.nodes + 4u * node;
+    a0 = __ldg(nb); a1 = __ldg(nb + 1); a2 = __ldg(nb + 2); a3 = __ldg(nb + 3);
+  }
+#else
+  constexpr bool staged = false;
   const float4* nb = S.nodes + 4u * node;
   const float4 a0 = __ldg(nb), a1 = __ldg(nb + 1), a2 = __ldg(nb + 2), a3 = __ldg(nb + 3);
+#endif
   float t0 = slab(xyz(a0), xyz(a1), st.ol, st.inv, tmin, st.best.t);
   float t1 = slab(xyz(a2), xyz(a3), st.ol, st.inv, tmin, st.best.t);
   const uint32_t c0 = fu(a1.w), c1 = fu(a3.w), r0 = fu(a0.w), r1 = fu(a2.w);
@@ -532,7 +562,8 @@ __device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceStat
   }
   t0 = t0 < st.best.t ? t0 : BIG;
   t1 = t1 < st.best.t ? t1 : BIG;
-  if ((t0 < BIG && c0 == 0u && r0 <= node) || (t1 < BIG && c1 == 0u && r1 <= node)) { atomicAdd(S.dbg + DBG_CORRUPT, 1u); return 1; }
+  // staged records were checked for increasing child indices when the set was built
+  if (!staged && ((t0 < BIG && c0 == 0u && r0 <= node) || (t1 < BIG && c1 == 0u && r1 <= node))) { atomicAdd(S.dbg + DBG_CORRUPT, 1u); return 1; }
   const bool go0 = t0 < BIG, go1 = t1 < BIG;
   if (go0 && go1) {
     if (t1 < t0) { stk.set(st.sp, r0, t0); st.node = r1; }
@@ -572,6 +603,19 @@ __device__ __forceinline__ bool take_rays(bool& active, bool& exhausted, uint32_
     }
   }
   return __any_sync(0xffffffffu, active) || !exhausted;
+}
+
+// copy the staged top levels into the block's shared array; returns the root to start static traversals at
+__device__ __forceinline__ uint32_t stage_top(const Scene& S, float4* top_sh, uint32_t root) {
+#if VT_TOP_NODES
+  const uint32_t n = min(S.n_top, TOP_NODES) * 4u;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) top_sh[i] = __ldg(S.top + i);
+  __syncthreads();
+  return n && root == S.top_root ? TOP_BIT : root;
+#else
+  (void)S; (void)top_sh;
+  return root;
+#endif
 }
 
 // ------------------------------------------------------------------------------------------------ surfaces

@@ -147,9 +147,11 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(con
   const uint32_t n = *wb.count_in;
   if (wb.stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(wb.stats, (unsigned long long)n);
   __shared__ uint2 stack_sh[SH_DEPTH * WAVE_THREADS];
+  __shared__ float4 top_sh[4u * (TOP_NODES ? TOP_NODES : 1u)];
   LaneStack stk;
-  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = WAVE_THREADS;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = WAVE_THREADS; stk.top = top_sh;
   TraceState st;
+  const uint32_t root = stage_top(S, top_sh, cp.root);
   Scene Sl = S;
   float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
   float tt = 0.0f;
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(con
       const float4 h = wb.hcache[ci];
       if (h.x > 0.0f) { st.best = Hit{h.x, h.y, h.z, __float_as_uint(h.w), MISS}; from = 0; ci = MISS; }
     }
-    active = trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, from);
+    active = trace_phase(Sl, root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, from);
     if (HC && ci != MISS && st.k != -1) {   // no static phase to wait for: the static hit is none
       wb.hcache[ci] = make_float4(BIG, 0.0f, 0.0f, __uint_as_float(MISS));
       ci = MISS;
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(con
       wb.hcache[ci] = make_float4(st.best.t, st.best.u, st.best.v, __uint_as_float(st.best.tri));
       ci = MISS;
     }
-    if (r != 0 && !trace_phase(Sl, cp.root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, st.k + 1)) finish();
+    if (r != 0 && !trace_phase(Sl, root, o, d, 0.0f, tt, 3u, VAR == WAVE_SHARED ? (skip | wb.bc.vary) : skip, st, st.k + 1)) finish();
   }
 }
 
@@ -344,9 +346,11 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
   const uint32_t skip0 = ldu(S0.su + 7);
   const uint32_t skip = VAR == WAVE_SHARED ? (skip0 | wb.bc.vary) : skip0;
   __shared__ uint2 stack_sh[SH_DEPTH * WAVE_THREADS];
+  __shared__ float4 top_sh[4u * (TOP_NODES ? TOP_NODES : 1u)];
   LaneStack stk;
-  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = WAVE_THREADS;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = WAVE_THREADS; stk.top = top_sh;
   TraceState st;
+  const uint32_t root = stage_top(S0, top_sh, cp.root);
   Scene S = S0;
   float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
   float4 nee = make_float4(0, 0, 0, 0);
@@ -377,7 +381,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
       if (w.w == 0.0f || (SC && w.w == 6.0f)) continue;   // no contribution, or hidden by the static scene (cached)
       o = xyz(a); d = xyz(w);
       st.best = Hit{a.w, 0.0f, 0.0f, MISS, MISS};
-      if (trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, SC && w.w == 5.0f ? 0 : -1)) return true;
+      if (trace_phase(S, root, o, d, 0.0f, nee.w, 3u, skip, st, SC && w.w == 5.0f ? 0 : -1)) return true;
       // nothing to traverse: the segment is unoccluded
       visible(j);
       if (VAR == WAVE_SHARED) bits |= cull_bits(wb.bc, o, d, a.w, skip0, have | bits);
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
     if (!active) continue;
     const int r = trace_visit<true>(S, 0.0f, st, stk);
     bool done = r == 2;
-    if (r == 1) done = !trace_phase(S, cp.root, o, d, 0.0f, nee.w, 3u, skip, st, st.k + 1);
+    if (r == 1) done = !trace_phase(S, root, o, d, 0.0f, nee.w, 3u, skip, st, st.k + 1);
     if (!done) continue;
     if (st.best.tri == MISS) {
       visible(j);
