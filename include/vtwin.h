@@ -600,6 +600,10 @@ typedef struct { uint32_t node_count, max_depth; float bmin[3], bmax[3]; } vt_bv
 uint32_t vt_bvh_capacity(uint32_t n_tris, uint32_t leaf_size);
 vt_status vt_bvh_build(const float* pos, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris, uint32_t leaf_size,
                        uint32_t* nodes_out, uint32_t* order_out, vt_bvh_result* res);
+/* The same build on a CUDA device (gpu/bvh.js:18 buildBVH): identical nodes, order and result, host buffers in and
+ * out. vt_create builds the static scene's BVH this way. */
+vt_status vt_bvh_build_device(int32_t device, const float* pos, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris,
+                              uint32_t leaf_size, uint32_t* nodes_out, uint32_t* order_out, vt_bvh_result* res);
 
 /* -------------------------------------------------------------------------------------------- diagnostics */
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <stdexcept>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -41,6 +42,30 @@ vt_status vt_bvh_build(const float* pos, uint32_t n_verts, const uint32_t* idx, 
   return VT_OK;
 }
 
+vt_status vt_bvh_build_device(int32_t device, const float* pos, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris, uint32_t leaf_size,
+                              uint32_t* nodes_out, uint32_t* order_out, vt_bvh_result* res) {
+  if ((n_tris && (!pos || !idx)) || !nodes_out || !res || (n_tris && !order_out)) return VT_ERR_ARG;
+  for (uint64_t i = 0; i < uint64_t(n_tris) * 3; i++) if (idx[i] >= n_verts) return VT_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return VT_ERR_NO_DEVICE;
+  }
+  vt::Bvh b;
+  std::string err;
+  if (!vtk::gpu_sah_build(pos, n_verts, idx, n_tris, leaf_size, b, err)) {
+    if (!err.empty()) { g_static_err = "gpu bvh build failed"; return VT_ERR_CUDA; }
+    b = vt::sah_build(pos, idx, n_tris, leaf_size);
+  }
+  if (b.node_count > vt_bvh_capacity(n_tris, leaf_size)) return VT_ERR_ARG;
+  std::copy(b.words.begin(), b.words.end(), nodes_out);
+  std::copy(b.order.begin(), b.order.end(), order_out);
+  res->node_count = b.node_count;
+  res->max_depth = b.max_depth;
+  for (int k = 0; k < 3; k++) { res->bmin[k] = b.lo[k]; res->bmax[k] = b.hi[k]; }
+  return VT_OK;
+}
+
 vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx** out) {
   if (!scene || !out) return VT_ERR_ARG;
   *out = nullptr;
@@ -50,16 +75,25 @@ vt_status vt_create(const vt_scene_desc* scene, const vt_options* opts, vt_ctx**
   const uint32_t leaf = opts && opts->leaf_size ? opts->leaf_size : 4;
   const uint32_t albs = opts && opts->albedo_samples ? opts->albedo_samples : 1024;
   ctx->device = opts ? opts->device : 0;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) { cudaGetLastError(); delete ctx; return VT_ERR_NO_DEVICE; }
+  // the static BVH is built on the device (the host builder's tree); a root that is itself a leaf stays on the host
+  auto build_static = [](const float* P, uint32_t nv, const uint32_t* I, uint32_t n, uint32_t lf) {
+    vt::Bvh b;
+    std::string err;
+    if (vtk::gpu_sah_build(P, nv, I, n, lf, b, err)) return b;
+    if (!err.empty()) throw std::runtime_error(err);
+    return vt::sah_build(P, I, n, lf);
+  };
   try {
-    ctx->S = vt::prepare_scene(*scene, leaf, albs);
+    ctx->S = vt::prepare_scene(*scene, leaf, albs, build_static);
   } catch (const std::exception& e) {
     const std::string m = e.what();
     delete ctx;
     g_static_err = "scene preparation failed";
+    if (m.find("gpu bvh build") != std::string::npos) return VT_ERR_CUDA;
     return m.find("too many bodies") != std::string::npos ? VT_ERR_TOO_MANY_BODIES : VT_ERR_ARG;
   }
   auto bail = [&](vt_status s) { vt_destroy(ctx); return s; };
-  if (cudaSetDevice(ctx->device) != cudaSuccess) { cudaGetLastError(); delete ctx; return VT_ERR_NO_DEVICE; }
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(VT_ERR_CUDA);
   if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess || cudaEventCreate(&ctx->ev2) != cudaSuccess ||
       cudaEventCreate(&ctx->ev3) != cudaSuccess)

@@ -475,7 +475,7 @@ void tri_record(uint32_t* rec, const float* P, const uint32_t* tri, uint32_t i0,
 }
 }  // namespace
 
-Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_samples) {
+Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_samples, const StaticBuilder& build_static) {
   if (!d.meshes || !d.n_meshes || !d.materials || !d.n_materials) throw std::runtime_error("scene: no meshes or materials");
   if (d.n_static_tris && (!d.static_P || !d.static_N || !d.static_I || !d.static_tri_mesh || !d.static_vert_mesh))
     throw std::runtime_error("scene: static arrays missing");
@@ -502,7 +502,8 @@ Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf, uint32_t albedo_sa
   S.cams.assign(d.cameras, d.cameras + d.n_cameras);
   for (int k = 0; k < 3; k++) S.L0[k] = d.L0[k];
 
-  Bvh sb = sah_build(d.static_P, d.static_I, d.n_static_tris, leaf);
+  Bvh sb = build_static ? build_static(d.static_P, d.n_static_verts, d.static_I, d.n_static_tris, leaf)
+                       : sah_build(d.static_P, d.static_I, d.n_static_tris, leaf);
   std::vector<Bvh> bb(d.n_bodies);
   std::vector<Emit> emit;
   std::vector<std::vector<uint32_t>> emit_idx(d.n_bodies);

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/vtwin.h"
@@ -62,8 +63,10 @@ struct Prepared {
   int scope_index = -1;
   float L0[3] = {1, 1, 1};
 };
+// builder of the static BVH (positions, vertex count, indices, triangle count, leaf size); sah_build when empty
+using StaticBuilder = std::function<Bvh(const float*, uint32_t, const uint32_t*, uint32_t, uint32_t)>;
 // gpu/scene_gpu.js:241-472 + gpu/renderer.js:271-306; throws std::runtime_error on bad input
-Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf_size, uint32_t albedo_samples);
+Prepared prepare_scene(const vt_scene_desc& d, uint32_t leaf_size, uint32_t albedo_samples, const StaticBuilder& build_static = {});
 
 struct InstPose { bool valid = false; double q0[4], q1[4], p0[3], p1[3]; };
 // gpu/renderer.js:620 setPoses: quaternion + translation per body (T column-major 4x4; NaN hides a body)
@@ -115,3 +118,9 @@ struct LiteEmit {
 LiteEmit lite_emitter_samples(const Prepared& S, uint32_t n);
 
 }  // namespace vt
+
+namespace vtk {
+// the static BVH built on the current CUDA device: the same words and order as vt::sah_build. False with err empty
+// when the root is itself a leaf (a handful of triangles), with err set on a CUDA failure.
+bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t n, uint32_t leaf, vt::Bvh& out, std::string& err);
+}  // namespace vtk

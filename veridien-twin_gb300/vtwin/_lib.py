@@ -76,6 +76,8 @@ SIGNATURES = {
     "vt_bvh_capacity": (C.c_uint32, [C.c_uint32, C.c_uint32]),
     "vt_bvh_build": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                  C.POINTER(A.vt_bvh_result)]),
+    "vt_bvh_build_device": (C.c_int32, [C.c_int32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                        C.c_void_p, C.POINTER(A.vt_bvh_result)]),
     "vt_debug_flags": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int]),
     "vt_timings_get": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_timings)]),
     "vt_stream": (C.c_void_p, [C.c_void_p]),

@@ -714,8 +714,10 @@ def form_factors(centres, normals, areas, out=None, ctx=None):
     return out
 
 
-def build_bvh(pos, idx, leaf_size=4) -> dict:
-    """gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}) -> {nodes (uint32 words), nodeCount, order, bmin, bmax, maxDepth}."""
+def build_bvh(pos, idx, leaf_size=4, device=None) -> dict:
+    """gpu/bvh.js:18 buildBVH(pos, idx, {leafSize}) -> {nodes (uint32 words), nodeCount, order, bmin, bmax, maxDepth}.
+
+    device=None builds on the host's threads, an int on that CUDA device (the same tree)."""
     lib = load()
     pos = np.ascontiguousarray(pos, np.float32).ravel()
     idx = np.ascontiguousarray(idx, np.uint32).ravel()
@@ -724,6 +726,10 @@ def build_bvh(pos, idx, leaf_size=4) -> dict:
     nodes = np.zeros(cap * 16, np.uint32)
     order = np.zeros(max(1, n), np.uint32)
     res = A.vt_bvh_result()
-    check(lib.vt_bvh_build(_p(pos), len(pos) // 3, _p(idx), n, leaf_size, _p(nodes), _p(order), C.byref(res)))
+    if device is None:
+        check(lib.vt_bvh_build(_p(pos), len(pos) // 3, _p(idx), n, leaf_size, _p(nodes), _p(order), C.byref(res)))
+    else:
+        check(lib.vt_bvh_build_device(int(device), _p(pos), len(pos) // 3, _p(idx), n, leaf_size, _p(nodes), _p(order),
+                                      C.byref(res)))
     return {"nodes": nodes[: res.node_count * 16].copy(), "nodeCount": res.node_count, "order": order[:n].copy(),
             "bmin": np.array(res.bmin[:]), "bmax": np.array(res.bmax[:]), "maxDepth": res.max_depth}
