@@ -365,7 +365,7 @@ vt_status vt_lite_render_camera(vt_ctx* ctx, uint32_t camera, float* out_rgba) {
   a.circle = camera == uint32_t(ctx->S.cams.size()) ? float(L.o.scope_circle_frac * L.o.scope_width / 2.0) : 0.0f;
   a.env_mat = L.o.env_material;
   a.out = C.rad;
-  vtl::launch_shade(S, g, v, a, L.fb, big_blocks(ctx) * 2, ctx->stream);
+  vtl::launch_shade(S, g, v, a, L.fb, big_blocks(ctx) / 4, ctx->stream);
   VT_CK(cudaGetLastError());
   L.launches += 7;
   VT_CK(cudaEventRecord(L.ev[3], ctx->stream));

@@ -352,7 +352,12 @@ __global__ void __launch_bounds__(256) frag_kernel(const unsigned long long* __r
 
 // one thread per fragment: the static fragments, then the posed-body ones; colours stored as half floats (the
 // multisample target is rgba16float)
-__global__ void __launch_bounds__(128) shade_frag_kernel(const Scene S, const Geo g, const View V, const ShadeArgs a, const uint2* __restrict__ frags,
+// blocks of 128 an SM holds: 7 caps the registers at 72 (a few spills); measured per 1280x720 view 0.487 ms at
+// 6 (80 registers), 0.475 at 7, 0.472-0.477 at 8 (64 registers, 132 B of spills)
+#ifndef VT_SHADE_BLOCKS
+#define VT_SHADE_BLOCKS 7
+#endif
+__global__ void __launch_bounds__(128, VT_SHADE_BLOCKS) shade_frag_kernel(const Scene S, const Geo g, const View V, const ShadeArgs a, const uint2* __restrict__ frags,
                                                          uint32_t cap, const uint32_t* __restrict__ counts, uint2* __restrict__ colors) {
   const uint32_t ns = counts[0], nd = counts[1];
   const uint32_t W = uint32_t(V.size[0]);
@@ -401,7 +406,16 @@ void launch_vertex_shadow(const Scene& S, const Geo& g, const View& v, uint32_t 
   if (!count) return;
   vertex_shadow_kernel<<<(count + 255) / 256, 256, 0, st>>>(S, g, v, first, count, clip);
 }
-void launch_shade(const Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int blocks, cudaStream_t st) {
+// one resident wave: the grid is the SM count times the blocks of shade_frag_kernel an SM holds, so no block of
+// the grid-stride loop starts late and leaves a tail (a 1216-block grid with 912 resident took 0.548 ms per view,
+// one wave 0.487)
+void launch_shade(const Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int sms, cudaStream_t st) {
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shade_frag_kernel, 128, 0);
+    per_sm = per_sm > 0 ? per_sm : 1;
+  }
+  const int blocks = sms * per_sm;
   const uint32_t W = uint32_t(v.size[0]), H = uint32_t(v.size[1]);
   const uint32_t cap = W * H * 4u;
   cudaMemsetAsync(fb.counts, 0, 8, st);

@@ -88,7 +88,7 @@ struct FragBufs {
   uint32_t* counts;            // [0] static, [1] posed-body fragments
 };
 // fragment list + fragment stage + resolve + finish
-void launch_shade(const vtd::Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int blocks, cudaStream_t st);
+void launch_shade(const vtd::Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int sms, cudaStream_t st);
 // clear a 32-bit depth target to all ones
 void launch_fill(uint32_t* p, size_t n, uint32_t value, cudaStream_t st);
 
