@@ -357,6 +357,11 @@ __global__ void __launch_bounds__(256) frag_kernel(const unsigned long long* __r
 #ifndef VT_SHADE_BLOCKS
 #define VT_SHADE_BLOCKS 7
 #endif
+// waves of the grid: fragments cost 24 or 96 emitter samples, so more, shorter blocks balance the SMs. Per 1280x720
+// view: 0.477 ms at 1 wave, 0.468 at 2, 0.436 at 4, 0.421 at 8, 0.453 at 16
+#ifndef VT_SHADE_WAVES
+#define VT_SHADE_WAVES 8
+#endif
 __global__ void __launch_bounds__(128, VT_SHADE_BLOCKS) shade_frag_kernel(const Scene S, const Geo g, const View V, const ShadeArgs a, const uint2* __restrict__ frags,
                                                          uint32_t cap, const uint32_t* __restrict__ counts, uint2* __restrict__ colors) {
   const uint32_t ns = counts[0], nd = counts[1];
@@ -406,16 +411,15 @@ void launch_vertex_shadow(const Scene& S, const Geo& g, const View& v, uint32_t 
   if (!count) return;
   vertex_shadow_kernel<<<(count + 255) / 256, 256, 0, st>>>(S, g, v, first, count, clip);
 }
-// one resident wave: the grid is the SM count times the blocks of shade_frag_kernel an SM holds, so no block of
-// the grid-stride loop starts late and leaves a tail (a 1216-block grid with 912 resident took 0.548 ms per view,
-// one wave 0.487)
+// whole waves: the grid is VT_SHADE_WAVES x the SM count x the blocks of shade_frag_kernel an SM holds, so the last
+// wave is not a partial one that leaves a tail (a 1216-block grid with 912 resident took 0.548 ms per view)
 void launch_shade(const Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int sms, cudaStream_t st) {
   static int per_sm = 0;
   if (!per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shade_frag_kernel, 128, 0);
     per_sm = per_sm > 0 ? per_sm : 1;
   }
-  const int blocks = sms * per_sm;
+  const int blocks = sms * per_sm * VT_SHADE_WAVES;
   const uint32_t W = uint32_t(v.size[0]), H = uint32_t(v.size[1]);
   const uint32_t cap = W * H * 4u;
   cudaMemsetAsync(fb.counts, 0, 8, st);
