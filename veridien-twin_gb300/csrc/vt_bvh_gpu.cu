@@ -33,8 +33,14 @@ namespace vtk {
 namespace {
 
 constexpr int BINS = 16;
-constexpr int BT = 512;            // threads of a big task's block
-constexpr int BIG_TASK = 8192;     // ranges of at least this many slots are big tasks
+#ifndef VT_BVH_BLOCK
+#define VT_BVH_BLOCK 512
+#endif
+#ifndef VT_BVH_BIG
+#define VT_BVH_BIG 8192
+#endif
+constexpr int BT = VT_BVH_BLOCK;   // threads of a big task's block
+constexpr int BIG_TASK = VT_BVH_BIG;   // ranges of at least this many slots are big tasks
 constexpr int WPB = 8;             // warp tasks per 256-thread block
 constexpr double KBIG = 1e30;
 constexpr int THR_MIN = 64;        // ranges above this many slots bin through float thresholds
