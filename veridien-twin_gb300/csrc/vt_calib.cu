@@ -579,11 +579,8 @@ __global__ void sum_kernel(const double* __restrict__ p, uint32_t n, double* __r
   }
   if (threadIdx.x == 0) *out = s[0];
 }
-// calib_shade_kernel's grid-stride loop runs as whole waves of its own occupancy (3 blocks of 256 per SM at 80
-// registers) rather than on the traversal kernels' grid, of which it would hold three quarters
-#ifndef CALIB_SHADE_GRID
-#define CALIB_SHADE_GRID 1
-#endif
+// calib_shade_kernel's grid-stride loop runs as one wave of its own occupancy (3 blocks of 256 per SM at 80
+// registers) rather than on the traversal kernels' grid, a wave and a third of it (C4 forward 200 -> 196 ms)
 int calib_shade_grid() {
   static int g = 0;
   if (!g) {
@@ -619,7 +616,7 @@ uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev&
       cudaMemsetAsync(w.count_out, 0, 4, st);
       cudaMemsetAsync(w.count_sh, 0, 4, st);
       launch_wave_extend(S, cp, w, blocks, st);
-      calib_shade_kernel<<<CALIB_SHADE_GRID ? calib_shade_grid() : blocks, WT, 0, st>>>(S, cp, C, w, rb, b);
+      calib_shade_kernel<<<calib_shade_grid(), WT, 0, st>>>(S, cp, C, w, rb, b);
       cudaMemsetAsync(w.fetch, 0, 4, st);
       calib_shadow_kernel<<<blocks, WT, 0, st>>>(S, cp, w, rb);
     }
