@@ -42,6 +42,12 @@ W_, H_, SPP, DEPTH, NL = 640, 480, 16, 4, 1
 WORKLOAD = "C0 synthetic dome path tracer: 640x480 KB4 camera, 16 spp, depth 4, 1 light sample, ~12.4k tris"
 
 
+def bench_config(world):
+    """The workload's description, the same dict in both arms (the reference arm runs it on the host cores)."""
+    return {"workload": WORKLOAD, "width": W_, "height": H_, "spp": SPP, "depth": DEPTH, "light_samples": NL,
+            "l2": "flushed between timed frames (256 MB write)", "parallelism": "replicas" if world > 1 else "single"}
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -160,7 +166,9 @@ def run_reference(args):
     if rank != 0:
         return
     vals = []
+    flush = np.zeros(256 * 1024 * 1024 // 8)
     for i in range(args.warmup + args.steps):
+        flush.fill(float(i))                     # the host caches flushed between steps, as the GPU arm flushes L2
         v, info = cpu_baseline()
         if i >= args.warmup:
             vals.append(v)
@@ -168,7 +176,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": info["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dome, mulberry32)",
-            "config": {"workload": WORKLOAD, "spp": SPP, "depth": DEPTH, "width": W_, "height": H_},
+            "config": bench_config(world),
             "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": info["threads"], "kind": "port",
                              "sample": f"{info['rows']} of {H_} rows x {W_} px x {SPP} spp per step ({info['samples']} samples)"},
             "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -251,9 +259,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded dome, mulberry32)",
-            "config": {"workload": WORKLOAD, "width": W_, "height": H_, "spp": SPP, "depth": DEPTH, "light_samples": NL,
-                       "tuned": {"tile": list(tuned["tile"]), "refill": tuned["refill"]},
-                       "l2": "flushed between timed frames (256 MB write)", "parallelism": "replicas" if world > 1 else "single"},
+            "config": bench_config(world), "tuned": {"tile": list(tuned["tile"]), "refill": tuned["refill"]},
             "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": 24 * 4 + 48 * 4 * 24 + 16 * 8,
                     "d2h_bytes_per_step": W_ * H_ * 16},
             "gpu_launches": int(launches), "clocks": clk.summary()}

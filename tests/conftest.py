@@ -8,6 +8,15 @@ sys.path.insert(0, os.path.join(ROOT, "veridien-twin_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 
+# A checkout of the reference project, for the CPU tests that read its own files (scene meshes, configuration):
+# $VT_REFERENCE, else a sibling directory named `reference` beside this repository. Tests that need it skip without it.
+REFERENCE = os.environ.get("VT_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
+def reference_path(*parts) -> str:
+    return os.path.join(REFERENCE, *parts)
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 

@@ -4,14 +4,16 @@
   - light.profile theta_deg / p and its projected_solid_angle "2 pi int p(theta) cos sin dtheta of the tabulated,
     linearly interpolated p" (gpu/shade_ref.js:5 profile);
   - light.profile's half-radiance note is not a number and is not used.
-Run in a checkout that has the reference at ../reference or pass its path: python make_golden.py /path/to/reference
+Run beside a checkout of the reference (../reference from this repository, or $VT_REFERENCE), or pass its path:
+python make_golden.py /path/to/reference
 """
 import json
 import os
 import re
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VT_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference")
 text = open(os.path.join(ref, "configs", "twin", "physics.yaml")).read()
 val = lambda s: json.loads(s) if s.strip().startswith("[") else float(s)
 

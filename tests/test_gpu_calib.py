@@ -218,7 +218,20 @@ def test_calibration_function_with_torch(rig):
     """The packed forward/backward pair as a torch.autograd.Function: Adam on albedo, lamp radiance and the KB4
     intrinsics (image loss + fiducial reprojection loss) from a 10% perturbation."""
     torch = pytest.importorskip("torch")
-    from vtwin.calibrate import Calibration, CalibrationFunction
+    from vtwin.calibrate import Calibration
+
+    class CalibrationFunction(torch.autograd.Function):
+        """Test adapter: the packed forward/backward pair as a torch.autograd.Function, so that a torch optimiser
+        can drive it (loss = CalibrationFunction.apply(x, calibration), x float64)."""
+
+        @staticmethod
+        def forward(ctx, x, calib):
+            ctx.calib = calib
+            return torch.tensor(calib.forward(x.detach().cpu().numpy()), dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, grad):
+            return grad * torch.from_numpy(ctx.calib.backward()), None
 
     r, sc, info, t_alb, t_lamp, targets = rig
     pts = dome.fib_hemisphere(200, 3.9)[0]
@@ -240,10 +253,10 @@ def test_calibration_function_with_torch(rig):
         loss = CalibrationFunction.apply(x, cal)
         loss.backward()
         opt.step()
-        first = float(loss) if first is None else first
+        first = float(loss.detach()) if first is None else first
     err_K = np.abs(z.detach().numpy()[-16:] * scale[-16:] - x_true[-16:]) / np.abs(x_true[-16:]).clip(1e-3)
-    print(f"\nloss {first:.3e} -> {float(loss):.3e}; intrinsics max rel error {err_K.max():.2e} (start 1e-1)")
-    assert float(loss) < 0.05 * first
+    print(f"\nloss {first:.3e} -> {float(loss.detach()):.3e}; intrinsics max rel error {err_K.max():.2e} (start 1e-1)")
+    assert float(loss.detach()) < 0.05 * first
 
 
 def test_stored_and_replayed_paths_agree(rig):

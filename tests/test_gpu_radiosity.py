@@ -76,3 +76,26 @@ def test_form_factors_with_visibility_match_oracle():
     assert np.all(F.sum(axis=1) <= 1 + 1e-5)
     assert np.all(F.sum(axis=1) <= F0.sum(axis=1) * (1 + 1e-5) + 1e-7)   # occlusion only takes light away
     r.destroy()
+
+
+def test_offset_device_f_matches_aligned(system):
+    """A device F that is an offset view (rows not 16-byte aligned) gives the same FP32 solution as an aligned F,
+    for one right-hand side (the matvec) and for several (the GEMM sweep); the bulk-copy matvec refuses it."""
+    torch = pytest.importorskip("torch")
+    from vtwin.renderer import VtError
+
+    n, P, F = system
+    Fa = torch.from_numpy(F).cuda()
+    store = torch.empty(n * n + 1, dtype=torch.float32, device="cuda")
+    Fo = store[1:].view(n, n)
+    Fo.copy_(Fa)
+    assert Fo.data_ptr() % 16 == 4
+    for R in (1, 8):
+        E = dome.radiosity_rhs(n, P["lamps"], R, seed=3)
+        Ba, ia = solve_radiosity(Fa, P["rho"], E, tol=1e-6, max_iters=400)
+        Bo, io = solve_radiosity(Fo, P["rho"], E, tol=1e-6, max_iters=400)
+        assert ia["status"] == A.VT_OK and io["status"] == A.VT_OK and ia["iters"] == io["iters"]
+        assert np.linalg.norm(Bo - Ba) / np.linalg.norm(Ba) <= 1e-6
+    E = dome.radiosity_rhs(n, P["lamps"], 1, seed=3)
+    with pytest.raises(VtError):
+        solve_radiosity(Fo, P["rho"], E, precision=A.VT_PREC_FP32_TMA, tol=1e-6, max_iters=50)

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from conftest import reference_path
 from vtwin import dome
 from vtwin import scene_io as S
 
@@ -127,13 +128,13 @@ def test_scene_directory_loader(tmp_path):
     assert Osc.static_verts == len(st["P"]) and Osc.n_bodies == 3
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/assets/meshes"), reason="no twin scene files here")
+@pytest.mark.skipif(not os.path.isdir(reference_path("assets", "meshes")), reason="no twin scene files here")
 def test_real_mesh_weld_and_subdivide_match_restatement():
     """One of the twin's own meshes (the smallest static one) through weld + subdivide, native against the
     restatement."""
-    scene = json.load(open("/root/reference/assets/scene.json"))
+    scene = json.load(open(reference_path("assets", "scene.json")))
     m = min((x for x in scene["meshes"] if not x.get("dynamic")), key=lambda x: x["triangle_count"])
-    d = S.decode_mesh(m, open(os.path.join("/root/reference/assets", m["file"]), "rb").read())
+    d = S.decode_mesh(m, open(reference_path("assets", m["file"]), "rb").read())
     a = S.weld(d["P"], d["N"], d["I"])
     b = O.weld_ref(d["P"], d["N"], d["I"])
     assert all(np.array_equal(x, y) for x, y in zip(a, b))

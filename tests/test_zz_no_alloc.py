@@ -36,8 +36,34 @@ def test_static_solve_matches_allocating_solve_twice():
         assert info["status"] == A.VT_OK and info["iters"] == info_ref["iters"]
         err = np.linalg.norm(got - B_ref[:, 0]) / np.linalg.norm(B_ref[:, 0])
         assert err <= 1e-6, err
-    # sizes beyond the static maximum are refused, not truncated
+    # F as an offset view (rows not 16-byte aligned): the same solution as the aligned F
+    Fo_store = torch.empty(n * n + 1, dtype=torch.float32, device="cuda")
+    Fo = Fo_store[1:].view(n, n)
+    Fo.copy_(F)
+    assert Fo.data_ptr() % 16 == 4
+    B_ref, info_ref = solve_radiosity(F, P["rho"], E1, tol=1e-6, max_iters=500)
+    Ed = torch.from_numpy(np.ascontiguousarray(E1[:, 0])).cuda()
+    B = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+    info = solve_radiosity_static(Fo, rho, Ed, B, tol=1e-6, max_iters=500)
+    torch.cuda.synchronize()
+    assert info["status"] == A.VT_OK and info["iters"] == info_ref["iters"]
+    err = np.linalg.norm(B.cpu().numpy() - B_ref[:, 0]) / np.linalg.norm(B_ref[:, 0])
+    assert err <= 1e-6, err
+    # sizes beyond the static maximum are refused by the C side itself, not truncated
+    import ctypes as C
+
+    from vtwin.renderer import load
+
+    lib = load()
     big = 16385
-    Fb = torch.zeros((1,), dtype=torch.float32, device="cuda")
+    buf = torch.zeros((big,), dtype=torch.float32, device="cuda")
+    p = C.c_void_p(buf.data_ptr())
+    st = lib.vt_radiosity_solve_static(p, p, p, p, big, 10, 8, 1e-6, None, None, None)
+    assert st == A.VT_ERR_ARG
+    # a host pointer is refused (the entry point takes device buffers only)
+    h = np.zeros(16, np.float32)
+    hp = h.ctypes.data_as(C.c_void_p)
+    assert lib.vt_radiosity_solve_static(hp, p, p, p, 4, 10, 8, 1e-6, None, None, None) == A.VT_ERR_ARG
+    # and so are wrong-sized tensors, before anything reaches the C side
     with pytest.raises(VtError):
-        solve_radiosity_static(Fb, torch.zeros((big,), device="cuda"), Fb, Fb)
+        solve_radiosity_static(buf[:8], rho, Ed, B)

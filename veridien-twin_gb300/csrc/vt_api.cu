@@ -491,12 +491,15 @@ vt_status vt_sensor_expose(vt_ctx* ctx, const vt_sensor_uniform* su, const float
   if (!W || !H) return fail(ctx, VT_ERR_ARG, "sensor: empty image");
   if (glare != 0.0f) return fail(ctx, VT_ERR_ARG, "sensor: veiling glare is not supported by the expose stage (fraction must be 0)");
   const size_t px = size_t(W) * H;
-  const bool din = is_device_ptr(irradiance), dout = is_device_ptr(raw);
-  vt_status s = ensure_scratch(ctx, (din ? 0 : px * 16) + (dout ? 0 : px * 4) + 256);
+  vt_status s = reject_foreign(ctx, {irradiance, raw});
+  if (s != VT_OK) return s;
+  // a device irradiance is read as float4: one that is not 16-byte aligned is copied like a host one
+  const bool din = is_device_ptr(irradiance) && aligned16(irradiance), dout = is_device_ptr(raw);
+  s = ensure_scratch(ctx, (din ? 0 : px * 16) + (dout ? 0 : px * 4) + 256);
   if (s != VT_OK) return s;
   const float4* dE = reinterpret_cast<const float4*>(irradiance);
   char* base = static_cast<char*>(ctx->d_scratch);
-  if (!din) { VT_CK(cudaMemcpyAsync(base, irradiance, px * 16, cudaMemcpyHostToDevice, ctx->stream)); dE = reinterpret_cast<float4*>(base); base += px * 16; }
+  if (!din) { if ((s = to_device(ctx, base, irradiance, px * 16)) != VT_OK) return s; dE = reinterpret_cast<float4*>(base); base += px * 16; }
   float* dR = dout ? raw : reinterpret_cast<float*>(base);
   vtk::SensorParams sp;
   std::memcpy(sp.w, su->words, sizeof(sp.w));
@@ -683,8 +686,10 @@ static vt_status sensor_impl(vt_ctx* ctx, uint32_t camera, const vt_sensor_unifo
 vt_status vt_form_factors(vt_ctx* ctx, uint32_t n, const float* centres, const float* normals, const float* areas, float* F) {
   if (!ctx || !n || !centres || !normals || !areas || !F) return VT_ERR_ARG;
   const size_t nn = size_t(n) * n * 4;
+  vt_status s = reject_foreign(ctx, {F});
+  if (s != VT_OK) return s;
   const bool dF = is_device_ptr(F);
-  vt_status s = ensure_scratch(ctx, size_t(n) * 28 + (dF ? 0 : nn) + 256);
+  s = ensure_scratch(ctx, size_t(n) * 28 + (dF ? 0 : nn) + 256);
   if (s != VT_OK) return s;
   char* base = static_cast<char*>(ctx->d_scratch);
   float *dC = reinterpret_cast<float*>(base), *dN = dC + 3 * size_t(n), *dA = dN + 3 * size_t(n);
@@ -705,9 +710,11 @@ vt_status vt_form_factors_visible(vt_ctx* ctx, uint32_t n, const float* centres,
   if (!ctx || !n || !centres || !normals || !areas || !F) return VT_ERR_ARG;
   if (n > 65535 || rays < 1 || rays > 255) return fail(ctx, VT_ERR_ARG, "form factors: n <= 65535 and 1..255 rays per pair");
   const size_t nn = size_t(n) * n * 4;
+  vt_status s = reject_foreign(ctx, {F});
+  if (s != VT_OK) return s;
   const bool dF = is_device_ptr(F);
   const size_t head = (size_t(n) * 28 + 255) / 256 * 256, cnt = head + 256, out = cnt + (size_t(n) * n + 255) / 256 * 256;
-  vt_status s = ensure_scratch(ctx, out + (dF ? 0 : nn) + 256);
+  s = ensure_scratch(ctx, out + (dF ? 0 : nn) + 256);
   if (s != VT_OK) return s;
   char* base = static_cast<char*>(ctx->d_scratch);
   float *dC = reinterpret_cast<float*>(base), *dN = dC + 3 * size_t(n), *dA = dN + 3 * size_t(n);
@@ -930,6 +937,7 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   if (!ctx || !q || !q->n || !q->n_rhs || !q->F || !q->rho || !q->E || !q->B) return VT_ERR_ARG;
   if (q->n_rhs > 64) return fail(ctx, VT_ERR_ARG, "solve: at most 64 right-hand sides");
   if (q->n_rhs > 1 && (q->n_rhs % 4)) return fail(ctx, VT_ERR_ARG, "solve: several right-hand sides must be a multiple of 4");
+  if (reject_foreign(ctx, {q->F, q->rho, q->E, q->B}) != VT_OK) return VT_ERR_ARG;
   if (q->precision == VT_PREC_BF16 || q->precision == VT_PREC_FP8) return tc_solve(ctx, q);
   if (q->precision != VT_PREC_FP32 && q->precision != VT_PREC_FP32_TMA) return fail(ctx, VT_ERR_ARG, "solve: unknown precision");
   if (q->precision == VT_PREC_FP32_TMA && (q->n_rhs != 1 || q->n % 4u))
@@ -938,6 +946,7 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   const size_t nb = size_t(n) * R * 4, nf = size_t(n) * n * 4;
   const bool dF = is_device_ptr(q->F);
   const bool tma = q->precision == VT_PREC_FP32_TMA;
+  if (tma && dF && !aligned16(q->F)) return fail(ctx, VT_ERR_ARG, "solve: the bulk-copy matvec needs a 16-byte aligned F");
   const uint32_t max_blocks = std::max<uint32_t>(std::max<uint32_t>((n + 7) / 8, uint32_t((size_t(n) * R / 4 + 255) / 256)),
                                                  tma ? vtk::jacobi_matvec_tma_blocks(n) : 0u) + 8;
   const size_t gemm_work = R > 1 ? vtk::jacobi_gemm_fp32_work(n, R) : 0;

@@ -484,6 +484,7 @@ vt_status vt_raster(vt_ctx* ctx, const float* clip, uint32_t n_verts, const uint
   if (samples != 1 && samples != 4) return fail(ctx, VT_ERR_ARG, "raster: 1 or 4 samples per pixel");
   if (!width || !height || width > 16384 || height > 16384) return fail(ctx, VT_ERR_ARG, "raster: target size 1..16384");
   if (n_tris >= (1u << 28)) return fail(ctx, VT_ERR_ARG, "raster: more than 2^28 triangles");
+  if (reject_foreign(ctx, {clip, idx, keys}) != VT_OK) return VT_ERR_ARG;
   // every index in range before anything reaches the device
   std::vector<uint32_t> hidx(size_t(n_tris) * 3);
   if (is_device_ptr(idx)) { VT_CK(cudaMemcpy(hidx.data(), idx, hidx.size() * 4, cudaMemcpyDeviceToHost)); }

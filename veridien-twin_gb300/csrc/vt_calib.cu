@@ -582,15 +582,12 @@ __global__ void sum_kernel(const double* __restrict__ p, uint32_t n, double* __r
 // calib_shade_kernel's grid-stride loop runs as one wave of its own occupancy (3 blocks of 256 per SM at 80
 // registers) rather than on the traversal kernels' grid, a wave and a third of it (C4 forward 200 -> 196 ms)
 int calib_shade_grid() {
-  static int g = 0;
-  if (!g) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  static std::atomic<int> grid[MAX_DEVICES];
+  return per_device_value(grid, [](int dev) {
+    int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, calib_shade_kernel, WT, 0);
-    g = std::max(1, sms) * std::max(1, per);
-  }
-  return g;
+    return device_sms(dev) * std::max(1, per);
+  });
 }
 }  // namespace
 

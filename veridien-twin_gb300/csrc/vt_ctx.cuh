@@ -5,7 +5,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -205,12 +207,31 @@ inline vt_status fail(vt_ctx* ctx, vt_status s, const std::string& m) {
   return s;
 }
 
-inline bool is_device_ptr(const void* p) {
-  if (!p) return false;
+// Where a caller's pointer lives, seen from the current device: host memory (pageable, pinned or registered), this
+// device's memory (device or managed, allocated against this device), or another device's memory. A kernel on this
+// device must not be given the last kind: with peer access off that is an illegal-address fault.
+enum PtrKind { PTR_HOST = 0, PTR_DEVICE = 1, PTR_FOREIGN = 2 };
+
+inline PtrKind ptr_kind(const void* p) {
+  if (!p) return PTR_HOST;
   cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return PTR_HOST; }
+  if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) return PTR_HOST;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return PTR_FOREIGN; }
+  return a.device == dev ? PTR_DEVICE : PTR_FOREIGN;
 }
+
+inline bool is_device_ptr(const void* p) { return ptr_kind(p) == PTR_DEVICE; }
+
+// VT_ERR_ARG when any of the pointers is another device's memory
+inline vt_status reject_foreign(vt_ctx* ctx, std::initializer_list<const void*> ptrs) {
+  for (const void* p : ptrs)
+    if (ptr_kind(p) == PTR_FOREIGN) return fail(ctx, VT_ERR_ARG, "a buffer lives on another device than the context's");
+  return VT_OK;
+}
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 template <typename T>
 inline vt_status upload(vt_ctx* ctx, T** dst, const void* src, size_t bytes) {
@@ -286,11 +307,15 @@ inline uint32_t skip_mask(const vt_ctx* ctx, uint32_t cam) {
 
 // copy `bytes` from a host or device source into device memory `dst`
 inline vt_status to_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
-  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
+  const PtrKind k = ptr_kind(src);
+  if (k == PTR_FOREIGN) return fail(ctx, VT_ERR_ARG, "an input buffer lives on another device than the context's");
+  VT_CK(cudaMemcpyAsync(dst, src, bytes, k == PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
   return VT_OK;
 }
 inline vt_status from_device(vt_ctx* ctx, void* dst, const void* src, size_t bytes) {
-  VT_CK(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+  const PtrKind k = ptr_kind(dst);
+  if (k == PTR_FOREIGN) return fail(ctx, VT_ERR_ARG, "an output buffer lives on another device than the context's");
+  VT_CK(cudaMemcpyAsync(dst, src, bytes, k == PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
   return VT_OK;
 }
 

@@ -3,11 +3,35 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "vt_device.cuh"
 
 namespace vtk {
+
+// A launch size that depends only on the device (its SM count, a kernel's occupancy), computed once per device id
+// into a caller's table of atomics. Host threads that race on a device's first call compute the same value, so
+// the race is benign; a device id beyond the table is computed on every call.
+constexpr int MAX_DEVICES = 64;
+template <class Fn>
+inline int per_device_value(std::atomic<int> (&table)[MAX_DEVICES], Fn compute) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); dev = 0; }
+  if (dev < 0 || dev >= MAX_DEVICES) return std::max(1, compute(dev));
+  int v = table[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    v = std::max(1, compute(dev));
+    table[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+inline int device_sms(int dev) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) { cudaGetLastError(); sms = 1; }
+  return std::max(1, sms);
+}
 
 // one camera dispatch (the fields of gpu/renderer.js:888 _packCam that the estimators read)
 struct CamParams {

@@ -9,6 +9,7 @@
 // fraction, so the 16 texels under them are compared once per map.
 #include <cuda_fp16.h>
 
+#include "vt_kernels.cuh"
 #include "vt_lite.cuh"
 
 using namespace vtd;
@@ -414,11 +415,12 @@ void launch_vertex_shadow(const Scene& S, const Geo& g, const View& v, uint32_t 
 // whole waves: the grid is VT_SHADE_WAVES x the SM count x the blocks of shade_frag_kernel an SM holds, so the last
 // wave is not a partial one that leaves a tail (a 1216-block grid with 912 resident took 0.548 ms per view)
 void launch_shade(const Scene& S, const Geo& g, const View& v, const ShadeArgs& a, const FragBufs& fb, int sms, cudaStream_t st) {
-  static int per_sm = 0;
-  if (!per_sm) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shade_frag_kernel, 128, 0);
-    per_sm = per_sm > 0 ? per_sm : 1;
-  }
+  static std::atomic<int> occupancy[vtk::MAX_DEVICES];
+  const int per_sm = vtk::per_device_value(occupancy, [](int) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, shade_frag_kernel, 128, 0);
+    return per;
+  });
   const int blocks = sms * per_sm * VT_SHADE_WAVES;
   const uint32_t W = uint32_t(v.size[0]), H = uint32_t(v.size[1]);
   const uint32_t cap = W * H * 4u;

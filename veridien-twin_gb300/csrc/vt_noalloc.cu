@@ -33,10 +33,12 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
 
-bool on_device(const void* p) {
+// true for memory of device `dev` (device or managed memory allocated against it): the kernels run on `dev`, and
+// another GPU's memory would be an illegal address there with peer access off
+bool on_device(const void* p, int dev) {
   cudaPointerAttributes a;
   if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev;
 }
 
 }  // namespace
@@ -44,9 +46,9 @@ bool on_device(const void* p) {
 extern "C" vt_status vt_radiosity_solve_static(const float* F, const float* rho, const float* E, float* B, uint32_t n, uint32_t max_iters,
                                                uint32_t check_every, double tol, void* stream, uint32_t* iters, double* residual) {
   if (n == 0 || n > kMaxN) return VT_ERR_ARG;                        // the static scratch holds at most kMaxN nodes
-  if (!on_device(F) || !on_device(rho) || !on_device(E) || !on_device(B)) return VT_ERR_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) { cudaGetLastError(); return VT_ERR_NO_DEVICE; }
+  if (!on_device(F, dev) || !on_device(rho, dev) || !on_device(E, dev) || !on_device(B, dev)) return VT_ERR_ARG;
   unsigned char* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mutex);

@@ -45,7 +45,8 @@ __global__ void __launch_bounds__(MV_THREADS) jacobi_matvec_kernel(const float* 
   if (row < n) {
     const float* Fr = F + size_t(row) * n;
     float acc = 0.0f;
-    if ((n & 3u) == 0u) {
+    // 128-bit loads only when every row starts 16-byte aligned (a caller's F may be an offset view)
+    if ((n & 3u) == 0u && ((reinterpret_cast<uintptr_t>(F) | reinterpret_cast<uintptr_t>(Bin)) & 15u) == 0u) {
       const float4* F4 = reinterpret_cast<const float4*>(Fr);
       const float4* B4 = reinterpret_cast<const float4*>(Bin);
       const uint32_t n4 = n >> 2;
@@ -142,16 +143,13 @@ __global__ void __launch_bounds__(MVT_THREADS) jacobi_matvec_tma_kernel(const fl
 }
 
 uint32_t jacobi_matvec_tma_blocks(uint32_t n) {
-  static int per_sm = 0, sms = 0;
-  if (!per_sm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_matvec_tma_kernel, MVT_THREADS, MVT_STAGES * MVT_CHUNK * 4);
-    per_sm = std::max(per_sm, 1);
-    sms = std::max(sms, 1);
-  }
-  return std::max(1u, std::min(n, uint32_t(per_sm * sms)));
+  static std::atomic<int> grid[MAX_DEVICES];
+  const int g = per_device_value(grid, [](int dev) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, jacobi_matvec_tma_kernel, MVT_THREADS, MVT_STAGES * MVT_CHUNK * 4);
+    return device_sms(dev) * std::max(per, 1);
+  });
+  return std::max(1u, std::min(n, uint32_t(g)));
 }
 
 void launch_jacobi_matvec_tma(const float* F, const float* rho, const float* E, const float* Bin, float* Bout, uint32_t n, double* partials,
@@ -198,7 +196,7 @@ __global__ void __launch_bounds__(G_THREADS) jacobi_gemm_fp32_kernel(const float
   const uint32_t row0 = blockIdx.x * GM;
   const uint32_t kbeg = blockIdx.y * kchunk, kend = min(n, kbeg + kchunk);
   const uint32_t tm = tid / 16, tn = tid % 16;      // 16 x 16 threads, each 8 rows x 4 cols
-  const bool vec = (n & 3u) == 0u;
+  const bool vec = (n & 3u) == 0u && (reinterpret_cast<uintptr_t>(F) & 15u) == 0u;   // 16-byte aligned rows
   float acc[8][4];
 #pragma unroll
   for (int i = 0; i < 8; i++)
@@ -324,14 +322,8 @@ uint32_t gemm_splits(uint32_t n, int sms) {
   return s;
 }
 int sm_count() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  return sms;
+  static std::atomic<int> sms[MAX_DEVICES];
+  return per_device_value(sms, device_sms);
 }
 }  // namespace
 

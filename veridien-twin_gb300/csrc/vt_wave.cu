@@ -602,15 +602,12 @@ struct TimedLaunch {
 #endif
 template <int MODE, int VAR>
 int shade_grid() {
-  static int g = 0;
-  if (!g) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  static std::atomic<int> grid[MAX_DEVICES];
+  return per_device_value(grid, [](int dev) {
+    int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, wave_shade<MODE, VAR>, WAVE_THREADS, 0);
-    g = std::max(1, sms) * std::max(1, per) * VT_WAVE_SHADE_WAVES;
-  }
-  return g;
+    return device_sms(dev) * std::max(1, per) * VT_WAVE_SHADE_WAVES;
+  });
 }
 
 template <int VAR>

@@ -7,8 +7,7 @@
 `Calibration.forward(x)` returns the loss and keeps what `backward()` needs; `backward()` returns d loss / d x:
 the albedo and lamp entries by path replay and the transposed radiosity solve (vt_calib_backward), the intrinsics
 by the analytic KB4 Jacobian. The image term's dependence on the intrinsics (through visibility edges) is not
-differentiated: the intrinsics are pinned by the fiducials. `CalibrationFunction` wraps the pair as a
-torch.autograd.Function when torch is importable.
+differentiated: the intrinsics are pinned by the fiducials.
 """
 from __future__ import annotations
 
@@ -71,21 +70,3 @@ class Calibration:
         f = self.forward(x)
         return f, self.backward()
 
-
-try:  # the autograd-style wrapper for callers that optimise with torch
-    import torch
-
-    class CalibrationFunction(torch.autograd.Function):
-        """loss = CalibrationFunction.apply(x, calibration): x a float64 tensor of the packed parameters."""
-
-        @staticmethod
-        def forward(ctx, x, calib):
-            ctx.calib = calib
-            return torch.tensor(calib.forward(x.detach().cpu().numpy()), dtype=torch.float64)
-
-        @staticmethod
-        def backward(ctx, grad):
-            g = torch.from_numpy(ctx.calib.backward())
-            return grad * g, None
-except ImportError:  # pragma: no cover
-    CalibrationFunction = None

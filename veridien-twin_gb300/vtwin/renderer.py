@@ -690,6 +690,15 @@ def solve_radiosity_static(F, rho, E, B, tol=1e-6, max_iters=1000, check_every=8
     (objects with .data_ptr()), B receives the solution. Returns {iters, residual, status}."""
     lib = load()
     n = int(rho.shape[0])
+    # the C side cannot check sizes: every buffer is a contiguous float32 CUDA tensor big enough for n nodes (the C
+    # side itself refuses host memory and another device's memory)
+    for name, t, want in (("F", F, n * n), ("rho", rho, n), ("E", E, n), ("B", B, n)):
+        if not hasattr(t, "data_ptr") or str(t.dtype) != "torch.float32" or not t.is_contiguous():
+            raise VtError(A.VT_ERR_ARG, f"solve_radiosity_static: {name} must be a contiguous float32 device tensor")
+        if t.device.type != "cuda":
+            raise VtError(A.VT_ERR_ARG, f"solve_radiosity_static: {name} is not a CUDA tensor")
+        if t.numel() < want or (name != "F" and t.numel() != n):
+            raise VtError(A.VT_ERR_ARG, f"solve_radiosity_static: {name} holds {t.numel()} values, {want} needed")
     it = C.c_uint32(0)
     res = C.c_double(0.0)
     dp = lambda t: C.c_void_p(t.data_ptr())
