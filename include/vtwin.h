@@ -184,6 +184,25 @@ vt_status vt_set_node_state(vt_ctx* ctx, const float* state, uint32_t slot);
 vt_status vt_trace_rays(vt_ctx* ctx, const float* o4, const float* d4, uint32_t n, uint32_t mask, uint32_t any_hit,
                         uint32_t root, float* out4, float* out_v);
 
+/* gpu/wgsl/kernels.wgsl.js:494-551 lensTest / bsdfTest / capsuleTest / profileTest: one of the renderer's device
+ * functions on n caller cases, in the reference's float4 slots (TestU.la, lb, lc = lens[0..3], lens[4..7],
+ * lens[8..11]: (fx, fy, cx, cy), (k1..k4), (alpha, -, -, -)).
+ *   VT_UNIT_LENS     in 2n slots: (u, v, -, -) x n, then (x, y, z, -) x n;
+ *                    out 2n: (kb4Unproject(u, v), 0), (kb4Project(x, y, z), 0, 0) per case
+ *   VT_UNIT_BSDF     in 4n: n, l, v, (u0, u1, u2, material index of the context's scene);
+ *                    out 3n: (evalBSDF, pdfBSDF(v -> l)), sampleBSDF (l, pdf) or 0,
+ *                    (albedoSpec(material, n.v), layerNormal(n, 0.1 l, normalize(v + (0.3, 0.1, 0.2)), 2e-4, 2e-5).x);
+ *                    a material index beyond the scene's gives NaN
+ *   VT_UNIT_CAPSULE  in 4n: p, n, (a, r), b; out n: (capsuleOcc, 0, 0, 0)
+ *   VT_UNIT_PROFILE  in n: (theta, -, -, -); out n: (p(theta) of the scene's emitter, 0, 0, 0)
+ * Buffers are host or device; n <= 2^24. traceTest is vt_trace_rays. */
+enum { VT_UNIT_LENS = 0, VT_UNIT_BSDF = 1, VT_UNIT_CAPSULE = 2, VT_UNIT_PROFILE = 3 };
+typedef struct {
+  uint32_t kind, n;
+  float lens[12];
+} vt_unit_req;
+vt_status vt_unit_test(vt_ctx* ctx, const vt_unit_req* q, const float* in, float* out);
+
 /* gpu/renderer.js:1238 visible(name, pointsD, {tol, time}): occlusion from the camera centre to each point.
  * pts: n x 3 doubles (host); out: n bytes (1 visible). Traced on the device. */
 vt_status vt_visible(vt_ctx* ctx, uint32_t camera, const double* pts, uint32_t n, double tol, double time,

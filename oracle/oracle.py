@@ -221,6 +221,17 @@ class Scene:
                             C.c_uint32(root), int(fp64), _p(out), _p(dbg, C.c_uint64))
         return out, dbg
 
+    def unit_test(self, kind, tin, lens=None, fp64=False):
+        """gpu/wgsl/kernels.wgsl.js:494-551 lensTest / bsdfTest / capsuleTest / profileTest restated (kind 0..3), with
+        the reference's float4 slots; lens = (fx, fy, cx, cy, k1..k4, alpha). fp64=False: the float32 WGSL order."""
+        slots_in, slots_out = {0: (2, 2), 1: (4, 3), 2: (4, 1), 3: (1, 1)}[int(kind)]
+        tin = np.ascontiguousarray(tin, np.float32).reshape(-1, 4)
+        n = len(tin) // slots_in
+        out = np.zeros((n * slots_out, 4), np.float32)
+        lz = np.zeros(9) if lens is None else np.ascontiguousarray(lens, np.float64)
+        lib().or_unit_test(self.h, C.c_uint32(int(kind)), _p(lz), int(n), _p(tin, C.c_float), _p(out, C.c_float), int(fp64))
+        return out
+
     def render(self, req: "A.vt_render_req", y0=0, y1=None, x0=0, x1=None, fp64=True, threads=1):
         cam = self.scene["cameras"][req.camera]
         W, H = cam["size"]

@@ -157,6 +157,23 @@ static inline void unproject(const Lens& L, const double uv[2], double out[3]) {
   double s = std::sin(th) / thd;
   out[0] = xd * s; out[1] = yd * s; out[2] = std::cos(th);
 }
+// gpu/wgsl/lens.wgsl.js:32 kb4Project in precision R (the FP64 mode is gpu/lens.js:43 project)
+template <typename R> static inline void kb4_project(const Lens& L, R x, R y, R z, R uv[2]) {
+  if (sizeof(R) == 8) {
+    double X[3] = {double(x), double(y), double(z)}, o[2];
+    project(L, X, o);
+    uv[0] = R(o[0]); uv[1] = R(o[1]);
+    return;
+  }
+  R rho = std::sqrt(x * x + y * y);
+  if (rho < R(1e-30)) { uv[0] = R(L.cx); uv[1] = R(L.cy); return; }
+  R th = std::atan2(rho, z), t2 = th * th;
+  R k0 = R(L.k[0]), k1 = R(L.k[1]), k2 = R(L.k[2]), k3 = R(L.k[3]);
+  R s = th * (R(1) + t2 * (k0 + t2 * (k1 + t2 * (k2 + t2 * k3)))) / rho;
+  R xd = x * s, yd = y * s;
+  uv[0] = R(L.fx) * (xd + R(L.alpha) * yd) + R(L.cx);
+  uv[1] = R(L.fy) * yd + R(L.cy);
+}
 // gpu/wgsl/lens.wgsl.js:9-30 kb4Theta (8 fixed Newton steps) / kb4Unproject, in precision R. The FP64 mode uses
 // gpu/lens.js's unproject (20 steps, 1e-15 break).
 template <typename R> static inline V3<R> kb4_unproject(const Lens& L, R u, R v) {
@@ -1467,18 +1484,20 @@ template <typename R> struct Shader {
     }
     return clampR(v, R(0), R(1));
   }
-  // gpu/wgsl/bsdf.wgsl.js:176 layerNormal; gpu/wgsl/shade.wgsl.js:100 shadingNormal
+  // gpu/wgsl/bsdf.wgsl.js:176 layerNormal: h(s) = depth/2 cos(2 pi s / period), s = p . bd, phase taken first
+  static V3<R> layer_normal(const V3<R>& n, const V3<R>& p, const V3<R>& bd, R period, R depth) {
+    R x = dot(p, bd) / period;
+    R ph = x - std::floor(x);
+    R dh = -(depth * R(0.5)) * (R(2) * R(M_PI) / period) * std::sin(R(2) * R(M_PI) * ph);
+    V3<R> bt = bd - n * dot(bd, n);
+    return normalize(n - bt * dh);
+  }
+  // gpu/wgsl/shade.wgsl.js:100 shadingNormal
   V3<R> shading_normal(const Surf<R>& s, uint32_t opts) const {
     if (!(opts & VT_O_LAYER) || !(s.flags & VT_F_LAYER)) return s.ns;
     const float* r0 = pv(S.meshOff + 2 * s.mesh);
     const float* r1 = pv(S.meshOff + 2 * s.mesh + 1);
-    V3<R> bd = ld3<R>(r0);
-    R period = r1[1], depth = r1[2];
-    R x = dot(s.p, bd) / period;
-    R ph = x - std::floor(x);
-    R dh = -(depth * R(0.5)) * (R(2) * R(M_PI) / period) * std::sin(R(2) * R(M_PI) * ph);
-    V3<R> bt = bd - s.ns * dot(bd, s.ns);
-    V3<R> n = normalize(s.ns - bt * dh);
+    V3<R> n = layer_normal(s.ns, s.p, ld3<R>(r0), R(r1[1]), R(r1[2]));
     if (dot(n, s.ng) <= R(0)) n = s.ns;
     return n;
   }
@@ -3198,6 +3217,63 @@ void or_trace_wgsl(void* h, int n, const float* o4, const float* d4, uint32_t ma
   };
   if (fp64) run(double(0)); else run(float(0));
   if (dbgOut) for (int k = 0; k < 16; k++) dbgOut[k] = dbg.c[k];
+}
+// gpu/wgsl/kernels.wgsl.js:494-551 lensTest / bsdfTest / capsuleTest / profileTest on the CPU, with the same float4
+// input and output slots (kind 0 lens, 1 BSDF, 2 capsule, 3 profile); lens = fx, fy, cx, cy, k1..k4, alpha. fp64 = 0
+// is the float32 WGSL-order restatement, 1 the float64 one (gpu/lens.js's 20-step inverse, gpu/bsdf.js).
+void or_unit_test(void* h, uint32_t kind, const double* lens, int n, const float* in, float* out, int fp64) {
+  Scene* S = static_cast<Scene*>(h);
+  Dbg dbg;
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    Tracer<R> tr(*S, dbg);
+    Shader<R> sh(tr);
+    auto v3 = [&](int slot) { const float* p = in + 4 * size_t(slot); return V3<R>(R(p[0]), R(p[1]), R(p[2])); };
+    auto put = [&](int slot, R a, R b, R c, R d) {
+      float* o = out + 4 * size_t(slot);
+      o[0] = float(a); o[1] = float(b); o[2] = float(c); o[3] = float(d);
+    };
+    for (int i = 0; i < n; i++) {
+      if (kind == 0) {
+        Lens L{lens[0], lens[1], lens[2], lens[3], lens[8], {lens[4], lens[5], lens[6], lens[7]}};
+        if (sizeof(R) == 4) {   // the device's float lens: its parameters rounded to float32 first
+          L.fx = float(L.fx); L.fy = float(L.fy); L.cx = float(L.cx); L.cy = float(L.cy); L.alpha = float(L.alpha);
+          for (double& k : L.k) k = float(k);
+        }
+        V3<R> r = kb4_unproject<R>(L, R(in[4 * i]), R(in[4 * i + 1]));
+        R uv[2];
+        const float* X = in + 4 * size_t(n + i);
+        kb4_project<R>(L, R(X[0]), R(X[1]), R(X[2]), uv);
+        put(2 * i, r.x, r.y, r.z, R(0));
+        put(2 * i + 1, uv[0], uv[1], R(0), R(0));
+      } else if (kind == 1) {
+        const float mw = in[16 * size_t(i) + 15];
+        const uint32_t m = uint32_t(mw);
+        if (!(mw >= 0.0f) || m >= S->nMat) {
+          const R q = std::numeric_limits<R>::quiet_NaN();
+          for (int k = 0; k < 3; k++) put(3 * i + k, q, q, q, q);
+          continue;
+        }
+        V3<R> nn = v3(4 * i), l = v3(4 * i + 1), v = v3(4 * i + 2), u = v3(4 * i + 3), ls;
+        MatR<R> M = sh.load_mat(m);
+        V3<R> f = eval_bsdf(M, nn, l, v);
+        R pdf = pdf_bsdf(M, nn, v, l);
+        R sp = sample_bsdf(M, nn, v, u, ls);
+        V3<R> a = sh.albedo(m, dot(nn, v), 0);
+        V3<R> ln = Shader<R>::layer_normal(nn, l * R(0.1), normalize(v + V3<R>(R(0.3f), R(0.1f), R(0.2f))), R(2e-4f), R(2e-5f));
+        put(3 * i, f.x, f.y, f.z, pdf);
+        if (sp > R(0)) put(3 * i + 1, ls.x, ls.y, ls.z, sp); else put(3 * i + 1, R(0), R(0), R(0), R(0));
+        put(3 * i + 2, a.x, a.y, a.z, ln.x);
+      } else if (kind == 2) {
+        const float* a = in + 16 * size_t(i) + 8;
+        R o = capsule_occ<R>(v3(4 * i), v3(4 * i + 1), V3<R>(R(a[0]), R(a[1]), R(a[2])), v3(4 * i + 3), R(a[3]));
+        put(i, o, R(0), R(0), R(0));
+      } else {
+        put(i, sh.profile(R(in[4 * i])), R(0), R(0), R(0));
+      }
+    }
+  };
+  if (fp64) run(double(0)); else run(float(0));
 }
 // render rows [y0, y1) of a camera; out: w x (y1-y0) x 4 doubles. threads > 1 splits rows.
 void or_render(void* h, const vt_render_req* q, uint32_t y0, uint32_t y1, uint32_t x0, uint32_t x1, int fp64, int threads, double* out, uint64_t* dbgOut) {

@@ -496,3 +496,53 @@ def test_lite_emitter_samples_are_stratified_and_posed():
     want = (T[:3, :3] @ es0[:, :3].astype(np.float64).T).T + T[:3, 3]
     assert np.abs(es1[:, :3] - want).max() < 1e-6
     assert np.array_equal(es1[:, 3], es0[:, 3]) and np.allclose(es1[:, 7], es0[:, 7])
+
+
+def test_unit_kernel_restatements_agree_across_precisions():
+    """The restated unit kernels (gpu/wgsl/kernels.wgsl.js:494-551): the float32 WGSL-order forms against the float64
+    ones on random cases: KB4 unproject / project (8 fixed Newton steps against gpu/lens.js's 20), the capsule
+    occlusion, the emission profile at and between its knots, and the BSDF on all material kinds, where float32 is
+    within 1e-5 of float64 on nearly every case (the rest are grazing angles that float32 itself rounds away)."""
+    from vtwin import dome
+
+    sc = dome.make_dome_scene(seed=1, width=64, height=48, level=2)
+    sc["materials"].append({**dome.lambertian("coated", [0.0, 0.0, 0.0]), "metallic": 1, "coated": 1, "f0": [0.95, 0.64, 0.54],
+                            "roughness": 0.4, "ior": 1.5, "coat_ior": 1.5, "coat_roughness": 0.08, "tau": [0.9, 0.7, 0.5]})
+    sc["emitter"]["theta"] = [0.0, 0.5, 1.0]
+    sc["emitter"]["p"] = [1.0, 0.6, 0.1]
+    S = O.Scene(sc)
+    rng = np.random.default_rng(1)
+    n = 4000
+    lens = [300.0, 300.0, 319.5, 239.5, 0.05, -0.01, 0.002, -0.0003, 0.0]
+    tin = np.zeros((2 * n, 4), np.float32)
+    tin[:n, 0], tin[:n, 1] = rng.uniform(0, 640, n), rng.uniform(0, 480, n)
+    tin[n:, :3] = rng.normal(size=(n, 3))
+    tin[n:, 2] = np.abs(tin[n:, 2]) + 0.5
+    a, b = S.unit_test(0, tin, lens=lens), S.unit_test(0, tin, lens=lens, fp64=True)
+    assert np.abs(a[0::2, :3] - b[0::2, :3]).max() <= 1e-5 and np.abs(a[1::2, :2] - b[1::2, :2]).max() <= 1e-3
+    tb = np.zeros((2 * n, 4), np.float32)
+    tb[n:, :3] = b[0::2, :3]
+    back = S.unit_test(0, tb, lens=lens, fp64=True)[1::2, :2]
+    assert np.abs(back - tin[:n, :2]).max() <= 1e-3                 # project(unproject(uv)) = uv
+    pt = np.zeros((6, 4), np.float32)
+    pt[:, 0] = [0.0, 0.25, 0.5, 0.75, 1.0, 1.5]
+    assert np.allclose(S.unit_test(3, pt, fp64=True)[:, 0], [1.0, 0.8, 0.6, 0.35, 0.1, 0.0], atol=1e-6)
+    tc = np.zeros((4 * n, 4), np.float32)
+    tc[0::4, :3] = rng.uniform(-0.1, 0.1, (n, 3))
+    tc[1::4, :3] = rng.normal(size=(n, 3))
+    tc[1::4, :3] /= np.linalg.norm(tc[1::4, :3], axis=1, keepdims=True)
+    tc[2::4, :3], tc[2::4, 3], tc[3::4, :3] = [0.0, 0.0, -0.1], 0.01, [0.0, 0.0, 0.1]
+    c32, c64 = S.unit_test(2, tc)[:, 0], S.unit_test(2, tc, fp64=True)[:, 0]
+    assert np.abs(c32 - c64).max() <= 1e-5 and np.mean(c64 > 0) > 0.5
+    nm = len(sc["materials"])
+    tv = np.zeros((4 * n, 4), np.float32)
+    for k in range(3):
+        w = rng.normal(size=(n, 3))
+        tv[k::4, :3] = w / np.linalg.norm(w, axis=1, keepdims=True)
+    tv[1::4, :3] *= np.sign(np.sum(tv[1::4, :3] * tv[0::4, :3], 1))[:, None]
+    tv[2::4, :3] *= np.sign(np.sum(tv[2::4, :3] * tv[0::4, :3], 1))[:, None]
+    tv[3::4, :3] = rng.random((n, 3))
+    tv[3::4, 3] = rng.integers(0, nm, n)
+    f32, f64 = S.unit_test(1, tv)[0::3], S.unit_test(1, tv, fp64=True)[0::3]
+    rel = np.abs(f32[:, :3] - f64[:, :3]).max(1) / np.maximum(np.abs(f64[:, :3]).max(1), 1e-3)
+    assert np.mean(rel <= 1e-5) >= 0.99

@@ -128,6 +128,16 @@ __device__ __forceinline__ float3 kb4_unproject(const Kb4& L, float u, float v) 
   const float s = sn / thd;
   return f3(xd * s, yd * s, cs);
 }
+// camera-frame point -> pixel (gpu/wgsl/lens.wgsl.js:32 kb4Project)
+__device__ __forceinline__ float2 kb4_project(const Kb4& L, float3 X) {
+  const float rho = sqrtf(X.x * X.x + X.y * X.y);
+  if (rho < 1e-30f) return make_float2(L.cx, L.cy);
+  const float th = atan2f(rho, X.z);
+  const float t2 = th * th;
+  const float s = th * (1.0f + t2 * (L.k0 + t2 * (L.k1 + t2 * (L.k2 + t2 * L.k3)))) / rho;
+  const float xd = X.x * s, yd = X.y * s;
+  return make_float2(L.fx * (xd + L.alpha * yd) + L.cx, L.fy * yd + L.cy);
+}
 
 // ------------------------------------------------------------------------------------------------ BSDF
 // gpu/bsdf.js:4-18 (the WGSL copy gpu/wgsl/bsdf.wgsl.js:28-155)
@@ -155,8 +165,7 @@ __device__ __forceinline__ float fresnel(float cosi, float eta) {
   return 0.5f * (rs * rs + rp * rp);
 }
 __device__ __forceinline__ float3 schlick3(float3 f0, float c) {
-  const float t = 1.0f - clampf(c, 0.0f, 1.0f);
-  const float m = t * t * t * t * t;
+  const float m = powf(1.0f - clampf(c, 0.0f, 1.0f), 5.0f);   // gpu/wgsl/bsdf.wgsl.js:38: pow(1 - c, 5)
   return f0 + (f3(1.0f, 1.0f, 1.0f) - f0) * m;
 }
 __device__ __forceinline__ float3 fresnel_rgb(const Mat& M, float c) {
@@ -269,16 +278,19 @@ __device__ __forceinline__ float sample_bsdf(const Mat& M, float3 n, float3 v, f
   if (dot(n, l) <= 0.0f) return 0.0f;
   return pdf_bsdf(M, n, v, l);
 }
-// directional albedo tables at cosine mu: specular + diffuse parts (gpu/wgsl/bsdf.wgsl.js:158-173)
-__device__ __forceinline__ float3 albedo(const Scene& S, uint32_t m, float mu) {
+// directional albedo tables at cosine mu (gpu/wgsl/bsdf.wgsl.js:158-173): part 0 the specular lobe (albedoSpec),
+// part 1 the diffuse one (albedoDiff)
+__device__ __forceinline__ float3 albedo_part(const Scene& S, uint32_t m, float mu, uint32_t part) {
   const float x = clampf(mu * float(VT_ALBEDO_BINS) - 0.5f, 0.0f, float(VT_ALBEDO_BINS - 1));
   const uint32_t i = uint32_t(floorf(x));
   const uint32_t j = min(uint32_t(VT_ALBEDO_BINS - 1), i + 1u);
   const float f = x - float(i);
   const float4* base = S.params + S.alb_off + m * VT_ALBEDO_BINS * 2u;
-  const float3 s = mix3(xyz(__ldg(base + 2 * i)), xyz(__ldg(base + 2 * j)), f);
-  const float3 d = mix3(xyz(__ldg(base + 2 * i + 1)), xyz(__ldg(base + 2 * j + 1)), f);
-  return s + d;
+  return mix3(xyz(__ldg(base + 2 * i + part)), xyz(__ldg(base + 2 * j + part)), f);
+}
+// specular + diffuse parts
+__device__ __forceinline__ float3 albedo(const Scene& S, uint32_t m, float mu) {
+  return albedo_part(S, m, mu, 0u) + albedo_part(S, m, mu, 1u);
 }
 
 // ------------------------------------------------------------------------------------------------ instances
@@ -652,16 +664,20 @@ __device__ __forceinline__ Surf surface(const Scene& S, const Hit& h, float3 o, 
 __device__ __forceinline__ float3 offset_ray(float3 p, float3 ng, float3 dir) {
   return p + ng * (dot(ng, dir) > 0.0f ? EPS_OFF : -EPS_OFF);
 }
-// FDM layer lines (gpu/wgsl/bsdf.wgsl.js:176, gpu/wgsl/shade.wgsl.js:100)
+// FDM layer lines, h(s) = depth/2 cos(2 pi s / period) with s = p . bd: the tilted normal (gpu/wgsl/bsdf.wgsl.js:176
+// layerNormal); the phase is taken first so that the sine's argument stays small in float32
+__device__ __forceinline__ float3 layer_normal(float3 n, float3 p, float3 bd, float period, float depth) {
+  const float x = dot(p, bd) / period;
+  const float ph = x - floorf(x);
+  const float dh = -(depth * 0.5f) * (2.0f * PI_F / period) * sinf(2.0f * PI_F * ph);
+  const float3 bt = bd - n * dot(bd, n);
+  return normalize(n - bt * dh);
+}
+// gpu/wgsl/shade.wgsl.js:100 shadingNormal
 __device__ __forceinline__ float3 shading_normal(const Scene& S, const Surf& s, uint32_t opts) {
   if (!(opts & VT_O_LAYER) || !(s.flags & VT_F_LAYER)) return s.ns;
   const float4 r0 = __ldg(S.params + S.mesh_off + 2u * s.mesh), r1 = __ldg(S.params + S.mesh_off + 2u * s.mesh + 1u);
-  const float3 bd = xyz(r0);
-  const float x = dot(s.p, bd) / r1.y;
-  const float ph = x - floorf(x);
-  const float dh = -(r1.z * 0.5f) * (2.0f * PI_F / r1.y) * sinf(2.0f * PI_F * ph);
-  const float3 bt = bd - s.ns * dot(bd, s.ns);
-  float3 n = normalize(s.ns - bt * dh);
+  float3 n = layer_normal(s.ns, s.p, xyz(r0), r1.y, r1.z);
   if (dot(n, s.ng) <= 0.0f) n = s.ns;
   return n;
 }

@@ -82,6 +82,13 @@ class vt_blas_info(C.Structure):
                 ("kind", C.c_int32)]
 
 
+VT_UNIT_LENS, VT_UNIT_BSDF, VT_UNIT_CAPSULE, VT_UNIT_PROFILE = 0, 1, 2, 3
+
+
+class vt_unit_req(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("n", C.c_uint32), ("lens", C.c_float * 12)]
+
+
 class vt_render_req(C.Structure):
     _fields_ = [("camera", C.c_uint32), ("spp", C.c_uint32), ("light_samples", C.c_uint32), ("seed", C.c_uint32),
                 ("options", C.c_uint32), ("mode", C.c_uint32), ("max_depth", C.c_uint32), ("root", C.c_uint32),

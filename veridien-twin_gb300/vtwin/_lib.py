@@ -24,6 +24,7 @@ SIGNATURES = {
     "vt_set_node_state": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vt_trace_rays": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                   C.c_void_p, C.c_void_p]),
+    "vt_unit_test": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_unit_req), C.c_void_p, C.c_void_p]),
     "vt_visible": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_double, C.c_double, C.c_void_p]),
     "vt_project": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_render_camera": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_render_req), C.c_void_p]),

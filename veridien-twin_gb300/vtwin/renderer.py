@@ -576,6 +576,23 @@ class TwinRenderer:
         inst = out[:, 2].view(np.uint32).copy()
         return t, tri, inst, out[:, 3].copy(), v
 
+    def unit_test(self, kind, tin, lens=None):
+        """gpu/wgsl/kernels.wgsl.js:494-551 lensTest / bsdfTest / capsuleTest / profileTest (vt_unit_test): tin is the
+        reference's float4 input slots ((n x slots) x 4); returns the output slots. lens: (fx, fy, cx, cy, k1..k4,
+        alpha) for VT_UNIT_LENS."""
+        slots_in, slots_out = {A.VT_UNIT_LENS: (2, 2), A.VT_UNIT_BSDF: (4, 3), A.VT_UNIT_CAPSULE: (4, 1),
+                               A.VT_UNIT_PROFILE: (1, 1)}[kind]
+        tin = np.ascontiguousarray(tin, np.float32).reshape(-1, 4)
+        if len(tin) % slots_in:
+            raise VtError(A.VT_ERR_ARG, f"unit test: {len(tin)} input slots is not a multiple of {slots_in}")
+        n = len(tin) // slots_in
+        q = A.vt_unit_req(kind=int(kind), n=n)
+        if lens is not None:
+            q.lens[:9] = [float(x) for x in lens]
+        out = np.zeros((n * slots_out, 4), np.float32)
+        check(self.lib.vt_unit_test(self._ctx, C.byref(q), _p(tin), _p(out)), self._ctx)
+        return out
+
     def visible(self, name, pointsD, tol=2e-4, time=0.5):
         pts = np.ascontiguousarray(pointsD, np.float64).reshape(-1, 3)
         out = np.zeros(len(pts), np.uint8)
