@@ -380,11 +380,26 @@ typedef struct {
   uint32_t replay;                                /* 1: the backward traces every path again from its sample numbers;
                                                      0: the forward keeps each path's record (160 B) when they fit in half
                                                      the free device memory, and replays otherwise */
+  uint32_t intrinsics;                            /* 1: the backward also gives the image loss's derivative in each
+                                                     camera's KB4 intrinsics (vt_calib_intrinsics_grad); the stored form
+                                                     then keeps a derivative record per path (320 B) beside its record */
 } vt_calib_req;
 /* Image loss of the request (and the images). Keeps the state the backward replays. */
 vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* req, double* loss);
 /* Gradient of the last forward's image loss: g_albedo (n_materials x 3), g_lamp (n_lamps). */
 vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp);
+/* The last backward's derivative of the image loss in the intrinsics (fx, fy, cx, cy, k1..k4) of each camera of the
+ * forward, in the request's camera order (n_cameras x 8), when that forward set `intrinsics`. It follows every path's
+ * smooth dependence on its primary ray: the hit points, the interpolated normals, the light samples' distances,
+ * cosines, MIS weights and emission profile, the cosine-sampled continuations, the emitter hit's MIS weight, chained
+ * through the KB4 inverse (gpu/lens.js:25 distortDeriv). Where a path changes in steps (the triangle a ray hits, a
+ * shadow ray's outcome, a node's radiosity) the step is not differentiated. No counterpart in the reference. */
+vt_status vt_calib_intrinsics_grad(vt_ctx* ctx, double* g_K);
+/* For checking the intrinsics' derivative: the discrete decisions of the stored forward's paths of the camera at
+ * `slot` of the request (stored form with `intrinsics` = 1), per path in (row, column, sub-sample) order:
+ * tri_inst 4 x (triangle, instance) of each bounce (VT_MISS: none), q 4 x 4 light-sample weights of each vertex
+ * (0: occluded or no contribution). Host or device buffers. */
+vt_status vt_calib_export_paths(vt_ctx* ctx, uint32_t slot, uint32_t* tri_inst, float* q);
 /* KB4 intrinsics of a camera: fx, fy, cx, cy, k1..k4 (gpu/lens.js:8 lensParams; skew stays). */
 vt_status vt_set_camera_intrinsics(vt_ctx* ctx, uint32_t camera, const double K[8]);
 vt_status vt_get_camera_intrinsics(const vt_ctx* ctx, uint32_t camera, double K[8]);

@@ -244,8 +244,12 @@ class Scene:
         return out, dbg
 
     # ----------------------------------------------------------------------------------------- calibration
-    def calib_render(self, camera, albedo, lamp, H, tri_node, spp=4, nl=1, seed=0, depth=3, y0=0, y1=None, fp64=True, threads=1):
-        """The calibration estimator of the CUDA library restated: rows [y0, y1) of a camera's image (h, w, 3)."""
+    def calib_render(self, camera, albedo, lamp, H, tri_node, spp=4, nl=1, seed=0, depth=3, y0=0, y1=None, fp64=True, threads=1,
+                     frozen=None, K=None):
+        """The calibration estimator of the CUDA library restated: rows [y0, y1) of a camera's image (h, w, 3).
+        frozen = (tri_inst (h, w, spp, 4, 2), q (h, w, spp, 4, 4)): replay every path on the given triangles' planes
+        with the given shadow outcomes (q = 0 occluded), so the image moves smoothly with the intrinsics K (fx, fy,
+        cx, cy, k1..k4; None: the scene camera's)."""
         cam = self.scene["cameras"][camera]
         W, Hh = cam["size"]
         y1 = Hh if y1 is None else y1
@@ -254,9 +258,15 @@ class Scene:
         Hn = np.ascontiguousarray(H, np.float64).ravel()
         tn = np.ascontiguousarray(tri_node, np.uint32)
         out = np.zeros((y1 - y0, W, 3))
-        lib().or_calib_render(self.h, C.c_uint32(camera), C.c_uint32(spp), C.c_uint32(nl), C.c_uint32(seed), C.c_uint32(depth), _p(alb),
-                              _p(lam), _p(Hn), C.c_uint32(len(Hn) // 3), _p(tn, C.c_uint32), C.c_uint32(y0), C.c_uint32(y1), int(fp64),
-                              int(threads), _p(out))
+        ti = qq = None
+        if frozen is not None:
+            ti = np.ascontiguousarray(frozen[0], np.uint32)
+            qq = np.ascontiguousarray(frozen[1], np.float32)
+        Kd = None if K is None else np.ascontiguousarray(K, np.float64)
+        lib().or_calib_render_frozen(self.h, C.c_uint32(camera), C.c_uint32(spp), C.c_uint32(nl), C.c_uint32(seed), C.c_uint32(depth),
+                                     _p(alb), _p(lam), _p(Hn), C.c_uint32(len(Hn) // 3), _p(tn, C.c_uint32), C.c_uint32(y0), C.c_uint32(y1),
+                                     int(fp64), int(threads), _p(ti, C.c_uint32) if ti is not None else None,
+                                     _p(qq, C.c_float) if qq is not None else None, _p(Kd) if Kd is not None else None, _p(out))
         return out
 
     def direct_transfer(self, centres, normals, samples=16, fp64=True, threads=1):

@@ -1351,6 +1351,23 @@ template <typename R> struct Tracer {
     V3<R> q = (p0 + u * s) - (a + v * t);
     return dot(q, q) <= r * r;
   }
+  // the hit of a ray on a given triangle's plane (instance `inst` posed at `time`, MISS: static), with no range test
+  // on t, u, v: the frozen replay of a path whose hit triangles are fixed (checks of the intrinsics' derivative)
+  Hit<R> frozen_hit(uint32_t tri, uint32_t inst, const V3<R>& o, const V3<R>& d, R time) const {
+    V3<R> ol = o, dl = d;
+    if (inst != MISS) {
+      M3<R> M; V3<R> p;
+      inst_pose(inst, time, M, p);
+      ol = M.tmul(o - p); dl = M.tmul(d);
+    }
+    const float* r = T + size_t(tri) * 16;
+    V3<R> v0 = ld3<R>(r), e1 = ld3<R>(r + 4), e2 = ld3<R>(r + 8);
+    V3<R> pv = cross(dl, e2);
+    R inv = R(1) / dot(e1, pv);
+    V3<R> sv = ol - v0;
+    V3<R> qv = cross(sv, e1);
+    return Hit<R>{dot(e2, qv) * inv, dot(sv, pv) * inv, dot(dl, qv) * inv, tri, inst};
+  }
   // gpu/wgsl/trace.wgsl.js:302 traceSceneSkip
   Hit<R> trace(const V3<R>& o, const V3<R>& d, R tmin, R tmax, R time, bool anyHit, uint32_t mask, uint32_t skip) const {
     Hit<R> best{tmax, 0, 0, MISS, MISS};
@@ -1783,16 +1800,26 @@ template <typename R> static void render_pixel(Tracer<R>& tr, const Shader<R>& s
 // triangle radiance, node irradiance H (planar 3 x n).
 struct CalibIn {
   const double* albedo; const double* lamp; const double* H; uint32_t nNodes; const uint32_t* triNode; uint32_t nStatic;
+  // frozen replay (checks only): per path in (row, column, sub-sample) order, 4 x (triangle, instance) of its bounces
+  // and 4 x 4 light-sample weights (0: occluded); null for the ordinary estimator
+  const uint32_t* fzTI = nullptr; const float* fzQ = nullptr;
 };
+// fti / fq (frozen replay): this path's bounces' triangles and light-sample weights; the rays then meet those
+// triangles' planes and a light sample with weight 0 counts as occluded, so that the estimator moves smoothly with
+// the camera ray
 template <typename R> static V3<R> calib_path(Tracer<R>& tr, const Shader<R>& sh, const CalibIn& C, const V3<R>& pos, const V3<R>& d0, R tt,
-                                              uint32_t i, const PixSeeds& Sd, uint32_t nl, uint32_t depth, uint32_t skip) {
+                                              uint32_t i, const PixSeeds& Sd, uint32_t nl, uint32_t depth, uint32_t skip,
+                                              const uint32_t* fti = nullptr, const float* fq = nullptr) {
   const Scene& S = tr.S;
   V3<R> L, T(1, 1, 1), o = pos, d = d0;
   const R area = R(tr.SU[3]);
   R pbPrev = 0;
   for (uint32_t b = 1; b <= depth; b++) {
     Hit<R> h;
-    if (b == 1) {
+    if (fti) {
+      if (fti[2 * (b - 1)] == MISS) break;
+      h = tr.frozen_hit(fti[2 * (b - 1)], fti[2 * (b - 1) + 1], o, d, tt);
+    } else if (b == 1) {
       h = tr.trace(o, d, R(0), R(BIGD), tt, false, 1u, 0u);
       Hit<R> hd = tr.trace(o, d, R(0), h.t, tt, false, 2u, skip);
       if (hd.tri != MISS) h = hd;
@@ -1841,8 +1868,10 @@ template <typename R> static V3<R> calib_path(Tracer<R>& tr, const Shader<R>& sh
       if (prof <= R(0)) continue;
       R pdfW = d2 / (cosE * area), pb = cosS * R(INV_PI_D);
       R w = R(nl) * R(nl) * pdfW * pdfW / (R(nl) * R(nl) * pdfW * pdfW + pb * pb);
-      Hit<R> shd = tr.trace(Shader<R>::offset_ray(s.p, s.ng, wi), wi, R(0), dist - R(2e-5), tt, true, 3u, tr.su_u(7));
-      if (shd.tri == MISS) sum = sum + R(C.lamp[lo]) * (prof * cosS * w * R(INV_PI_D) / pdfW);
+      bool vis;
+      if (fq) vis = fq[4 * (b - 1) + j] != 0.0f;
+      else vis = tr.trace(Shader<R>::offset_ray(s.p, s.ng, wi), wi, R(0), dist - R(2e-5), tt, true, 3u, tr.su_u(7)).tri == MISS;
+      if (vis) sum = sum + R(C.lamp[lo]) * (prof * cosS * w * R(INV_PI_D) / pdfW);
     }
     V3<R> Tr = T * rho;
     L = L + Tr * (sum / R(nl));
@@ -1888,7 +1917,9 @@ template <typename R> static void calib_pixel(Tracer<R>& tr, const Shader<R>& sh
     float tt = mixf(0.0f, 1.0f, kr(i, GOLD, Sd.s[2]));
     V3<R> dc = kb4_unproject<R>(L, R(uvx), R(uvy));
     V3<R> d = normalize(rx * dc.x + ry * dc.y + rz * dc.z);
-    acc = acc + calib_path<R>(tr, sh, C, pos, d, R(tt), i, Sd, nl, depth, skip);
+    const size_t path = (size_t(y) * cam.width + x) * spp + i;
+    acc = acc + calib_path<R>(tr, sh, C, pos, d, R(tt), i, Sd, nl, depth, skip, C.fzTI ? C.fzTI + path * 8 : nullptr,
+                              C.fzQ ? C.fzQ + path * 16 : nullptr);
   }
   R sc = R(1) / R(spp);
   out[0] = double(acc.x * sc); out[1] = double(acc.y * sc); out[2] = double(acc.z * sc);
@@ -3371,14 +3402,17 @@ void or_render(void* h, const vt_render_req* q, uint32_t y0, uint32_t y1, uint32
   if (dbgOut) for (int k = 0; k < 16; k++) { dbgOut[k] = 0; for (auto& d : dbgs) dbgOut[k] += d.c[k]; }
 }
 
-void or_calib_render(void* h, uint32_t camera, uint32_t spp, uint32_t nl, uint32_t seed, uint32_t depth, const double* albedo,
-                     const double* lamp, const double* H, uint32_t nNodes, const uint32_t* triNode, uint32_t y0, uint32_t y1, int fp64,
-                     int threads, double* out) {
+// the calibration render with optional frozen path decisions (fz_ti, fz_q: see CalibIn; null for the estimator) and
+// optional intrinsics K (fx, fy, cx, cy, k1..k4; null: the scene camera's)
+void or_calib_render_frozen(void* h, uint32_t camera, uint32_t spp, uint32_t nl, uint32_t seed, uint32_t depth, const double* albedo,
+                            const double* lamp, const double* H, uint32_t nNodes, const uint32_t* triNode, uint32_t y0, uint32_t y1, int fp64,
+                            int threads, const uint32_t* fz_ti, const float* fz_q, const double* K, double* out) {
   Scene* S = static_cast<Scene*>(h);
-  const vt_camera_desc& cam = S->cams[camera];
+  vt_camera_desc cam = S->cams[camera];
+  if (K) { cam.fx = K[0]; cam.fy = K[1]; cam.cx = K[2]; cam.cy = K[3]; for (int k = 0; k < 4; k++) cam.k[k] = K[4 + k]; }
   uint32_t skip = 0;
   for (size_t i = 0; i < S->blas.size(); i++) if (S->blas[i].owner == int(camera)) skip |= 1u << i;
-  CalibIn C{albedo, lamp, H, nNodes, triNode, S->staticTris};
+  CalibIn C{albedo, lamp, H, nNodes, triNode, S->staticTris, fz_ti, fz_q};
   const uint32_t w = cam.width;
   std::atomic<uint32_t> next(y0);
   std::vector<Dbg> dbgs(std::max(1, threads));
@@ -3401,6 +3435,12 @@ void or_calib_render(void* h, uint32_t camera, uint32_t spp, uint32_t nl, uint32
     for (int t = 0; t < threads; t++) th.emplace_back(work, t);
     for (auto& x : th) x.join();
   }
+}
+
+void or_calib_render(void* h, uint32_t camera, uint32_t spp, uint32_t nl, uint32_t seed, uint32_t depth, const double* albedo,
+                     const double* lamp, const double* H, uint32_t nNodes, const uint32_t* triNode, uint32_t y0, uint32_t y1, int fp64,
+                     int threads, double* out) {
+  or_calib_render_frozen(h, camera, spp, nl, seed, depth, albedo, lamp, H, nNodes, triNode, y0, y1, fp64, threads, nullptr, nullptr, nullptr, out);
 }
 
 void or_direct_transfer(void* h, const float* C, const float* N, uint32_t n, uint32_t samples, int fp64, int threads, double* D) {

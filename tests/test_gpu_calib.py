@@ -161,6 +161,72 @@ def test_adjoint_matches_fp64_oracle_fd(rig):
         assert vec <= 1e-3
 
 
+def test_image_intrinsics_gradient_matches_frozen_fp64_fd(rig):
+    """The image loss's derivative in a camera's KB4 intrinsics (fx, fy, cx, cy, k1..k4) against FP64 central
+    differences of the FP64 oracle's estimator replayed with the GPU's own discrete decisions frozen: every path's
+    hit triangles and shadow outcomes are the GPU forward's (vt_calib_export_paths), so the oracle's image moves
+    smoothly with K and its differences measure exactly the derivative the adjoint computes (the interior term; a ray
+    crossing an edge is a step that is not differentiated). The steps are 1e-6 and 5e-7 relative (taken exactly
+    between float32 lens values, as the device holds them): the frozen estimator keeps threshold tests of its own (a
+    grazing view switching to the geometric normal, the emitter's cosine cut-off at its silhouette), and steps of
+    1e-4 or 1e-5 (0.016 or 0.0016 px for cx) cross them on a handful of the 256k paths; at 1e-6 and 5e-7 none is
+    crossed and the two agree. Then the same derivative from the replay form, and, for information, the ordinary FP64
+    differences at 1e-4, which also see the edges."""
+    r, sc, info, t_alb, t_lamp, targets = rig
+    alb, lamp = f32(np.clip(t_alb * 1.03, 0.01, 1.0)), f32(t_lamp * 0.97)
+    K_true = r.get_intrinsics(2)
+    K0 = f32(K_true * np.array([1.02, 0.985, 1.0, 1.0, 1.1, 0.9, 1.2, 0.8]) + np.array([0, 0, 2.0, -1.5, 0.004, -0.003, 0, 0]))
+    r.set_intrinsics(2, K0)
+    kw = dict(spp=4, max_depth=3)
+    try:
+        loss_g, imgs = r.calib_forward([2], alb, lamp, targets=[targets[2]], intrinsics=True, **kw)
+        r.calib_backward()
+        gK = r.calib_intrinsics_grad()[0]
+        frozen = r.calib_export_paths(0, spp=4)
+        r.calib_forward([2], alb, lamp, targets=[targets[2]], images=False, intrinsics=True, replay=True, **kw)
+        r.calib_backward()
+        gK_replay = r.calib_intrinsics_grad()[0]
+    finally:
+        r.set_intrinsics(2, K_true)
+    ex = r.calib_export(with_F=True)
+    Hn, _ = O.calib_radiosity(ex["F"], ex["D"], lamp, alb, ex["node_mat"])
+    S = O.Scene(sc)
+    S.set_poses()
+    T2 = targets[2][..., :3].astype(np.float64)
+
+    def loss64(K, fz):
+        img = S.calib_render(2, alb, lamp, Hn, ex["tri_node"], spp=4, depth=3, fp64=True, threads=16, frozen=fz, K=K)
+        return np.mean((img - T2) ** 2)
+
+    base = loss64(K0, frozen)
+
+    def central(k, rel, fz):
+        h = rel * max(abs(K0[k]), 1e-2)
+        Kp, Km = K0.copy(), K0.copy()
+        Kp[k], Km[k] = np.float32(K0[k] + h), np.float32(K0[k] - h)   # the device's float32 lens, steps taken exactly
+        return (loss64(Kp, fz) - loss64(Km, fz)) / (Kp[k] - Km[k])
+
+    FD = np.array([central(k, 1e-6, frozen) for k in range(8)])
+    FD6 = np.array([central(k, 5e-7, frozen) for k in range(8)])
+    FD_plain = np.array([central(k, 1e-4, None) for k in range(8)])
+    names = ["fx", "fy", "cx", "cy", "k1", "k2", "k3", "k4"]
+    for k in range(8):
+        print(f"\n{names[k]}: adjoint {gK[k]: .6e}  frozen FP64 FD {FD[k]: .6e} ({FD6[k]: .6e})  replay form {gK_replay[k]: .6e}  "
+              f"ordinary FD {FD_plain[k]: .6e}", end="")
+    vec = np.linalg.norm(gK - FD) / np.linalg.norm(FD)
+    steps = np.linalg.norm(FD6 - FD) / np.linalg.norm(FD)
+    worst = np.max(np.abs(gK - FD) / np.abs(FD))
+    vec_replay = np.linalg.norm(gK_replay - gK) / np.linalg.norm(gK)
+    vec_plain = np.linalg.norm(gK - FD_plain) / np.linalg.norm(FD_plain)
+    print(f"\nloss GPU {loss_g:.6e} / frozen FP64 {base:.6e}; vector relative error {vec:.2e} against the frozen FP64 "
+          f"differences (worst entry {worst:.1e}; steps 1e-6 and 5e-7 agree to {steps:.1e}), {vec_replay:.1e} between the stored and "
+          f"replay forms, {vec_plain:.2e} against the ordinary differences (edges included)")
+    assert abs(base - loss_g) <= 1e-4 * loss_g
+    assert steps <= 1e-4
+    assert vec <= 1e-3 and worst <= 1e-2
+    assert vec_replay <= 1e-4
+
+
 def test_reprojection_jacobian(rig):
     r, sc, *_ = rig
     rng = np.random.default_rng(11)

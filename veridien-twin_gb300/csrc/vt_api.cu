@@ -149,6 +149,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   cudaFree(ctx->nodes.mem);
   cudaFree(ctx->nodes.table_mem);
   cudaFree(ctx->calib.records);
+  cudaFree(ctx->calib.tan);
   for (float4* p : ctx->calib.image) cudaFree(p);
   for (float4* p : ctx->calib.target) cudaFree(p);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);

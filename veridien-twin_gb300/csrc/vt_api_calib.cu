@@ -73,7 +73,8 @@ vt_status alloc_calib(vt_ctx* ctx) {
   K.max_partials = std::max<uint32_t>(4096, 2 * ((K.n + 7) / 8) + 16);
   const size_t bytes[] = {n * n * 4, n * L * 4, n * 12, n * 12, n * 4, size_t(ctx->S.tri_count) * 4, size_t(ctx->S.tri_count) * 4,
                           kMaxMat * 12, L * 4, n * 12, n * 4, n * 12,
-                          size_t(K.max_partials) * 8, kMaxMat * 24, L * 8, n * 24, n * 8, n * 8, n * 24, vtk::jacobi_t_work(uint32_t(n)), 64};
+                          size_t(K.max_partials) * 8, kMaxMat * 24, L * 8, n * 24, n * 8, n * 8, n * 24, vtk::jacobi_t_work(uint32_t(n)), 64,
+                          ctx->S.cams.size() * 64};
   size_t total = 0;
   for (size_t b : bytes) total += (b + 255) / 256 * 256;
   cudaFree(K.mem);
@@ -91,6 +92,7 @@ vt_status alloc_calib(vt_ctx* ctx) {
   K.g_alb = reinterpret_cast<double*>(take()); K.g_lamp = reinterpret_cast<double*>(take()); K.g_H = reinterpret_cast<double*>(take());
   K.lam0 = reinterpret_cast<double*>(take()); K.lam1 = reinterpret_cast<double*>(take()); K.lam = reinterpret_cast<double*>(take());
   K.work = reinterpret_cast<double*>(take()); K.loss = reinterpret_cast<double*>(take());
+  K.g_K = reinterpret_cast<double*>(take());
   return VT_OK;
 }
 
@@ -109,6 +111,7 @@ vtk::CalibDev calib_dev(vt_ctx* ctx, uint32_t cam) {
   C.n_static_tris = K.n_static; C.n_mat = K.n_mat; C.n_lamps = K.n_lamps; C.n_nodes = K.n;
   C.target = K.target[cam]; C.image = K.image[cam]; C.inv_count = K.inv_count;
   C.partials = K.partials; C.g_albedo = K.g_alb; C.g_lamp = K.g_lamp; C.g_H = K.g_H;
+  C.g_K = K.g_K + 8 * size_t(cam);
   return C;
 }
 
@@ -229,14 +232,17 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
     rec_total += size_t(vtk::tiled_pixels(cps[c].w, cps[c].h, cps[c].tile_w, cps[c].tile_h)) * cps[c].spp;
   }
   K.stored = false;
+  K.want_k = q->intrinsics != 0;
+  K.have_k = false;
   uint32_t wave_paths = 0;
   if (!q->replay) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     const size_t rec_bytes = vtk::calib_record_bytes(uint32_t(std::min<size_t>(rec_total, 0xffffffffu)));
+    const size_t tan_bytes = K.want_k ? vtk::calib_tan_bytes(uint32_t(std::min<size_t>(rec_total, 0xffffffffu))) : 0;
     wave_paths = uint32_t(std::min<size_t>(8u << 20, rec_total));
     const size_t wave_need = vtk::wave_bytes(wave_paths, cps[0].n_light, 0);
-    if (rec_total < 0xffffffffu && rec_bytes + (ctx->wave_cap >= wave_need ? 0 : wave_need) <= fr / 2) {
+    if (rec_total < 0xffffffffu && rec_bytes + tan_bytes + (ctx->wave_cap >= wave_need ? 0 : wave_need) <= fr / 2) {
       vt_status st = VT_OK;
       if (K.rec_cap < rec_bytes) {
         VT_CK(cudaStreamSynchronize(ctx->stream));
@@ -245,6 +251,14 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
         K.rec_cap = 0;
         if (cudaMalloc(&K.records, rec_bytes) != cudaSuccess) { cudaGetLastError(); st = VT_ERR_OOM; }
         else K.rec_cap = rec_bytes;
+      }
+      if (st == VT_OK && K.tan_cap < tan_bytes) {
+        VT_CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(K.tan);
+        K.tan = nullptr;
+        K.tan_cap = 0;
+        if (cudaMalloc(&K.tan, tan_bytes) != cudaSuccess) { cudaGetLastError(); st = VT_ERR_OOM; }
+        else K.tan_cap = tan_bytes;
       }
       if (st == VT_OK && ctx->wave_cap < wave_need) {
         VT_CK(cudaStreamSynchronize(ctx->stream));
@@ -268,9 +282,10 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
     if (K.stored) {
       const vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, wave_paths, cp.n_light, 0, ctx->d_work);
       nb = vtk::calib_wave_forward(dev_scene(ctx), cp, C, wb, wave_paths, static_cast<char*>(K.records) + K.rec_off[c] * vtk::calib_record_bytes(1),
+                                   K.want_k ? static_cast<char*>(K.tan) + K.rec_off[c] * vtk::calib_tan_bytes(1) : nullptr,
                                    std::min<int>(ctx->wave_blocks, int(K.max_partials)), ctx->stream);
     } else {
-      nb = vtk::launch_calib(dev_scene(ctx), cp, C, false, blocks, ctx->stream);
+      nb = vtk::launch_calib(dev_scene(ctx), cp, C, 0, blocks, ctx->stream);
     }
     vtk::launch_sum(K.partials, nb, K.loss, ctx->stream);
     VT_CK(cudaGetLastError());
@@ -299,16 +314,19 @@ vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp) {
   VT_CK(cudaMemsetAsync(K.g_alb, 0, size_t(K.n_mat) * 24, ctx->stream));
   VT_CK(cudaMemsetAsync(K.g_lamp, 0, size_t(K.n_lamps) * 8, ctx->stream));
   VT_CK(cudaMemsetAsync(K.g_H, 0, n * 24, ctx->stream));
+  VT_CK(cudaMemsetAsync(K.g_K, 0, ctx->S.cams.size() * 64, ctx->stream));
   // every camera of the forward: from the kept records, or by tracing each path again
   for (size_t c = 0; c < K.cams.size(); c++) {
     const uint32_t cam = K.cams[c];
     const vtk::CamParams cp = calib_cam(ctx, cam, K.spp, K.nl, K.seed, K.depth);
     if (K.stored)
       vtk::calib_records_backward(cp, calib_dev(ctx, cam), static_cast<char*>(K.records) + K.rec_off[c] * vtk::calib_record_bytes(1),
+                                  K.want_k ? static_cast<char*>(K.tan) + K.rec_off[c] * vtk::calib_tan_bytes(1) : nullptr,
                                   ctx->wave_blocks * 2, ctx->stream);
     else
-      vtk::launch_calib(dev_scene(ctx), cp, calib_dev(ctx, cam), true, ctx->wave_blocks * 2, ctx->stream);
+      vtk::launch_calib(dev_scene(ctx), cp, calib_dev(ctx, cam), K.want_k ? 2 : 1, ctx->wave_blocks * 2, ctx->stream);
   }
+  K.have_k = K.want_k;
   VT_CK(cudaGetLastError());
   // transposed Jacobi: lambda = F^T (g_H + rho o lambda) per channel, from lambda = 0
   for (uint32_t c = 0; c < 3; c++) {
@@ -342,6 +360,40 @@ vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp) {
   }
   if (g_albedo) std::copy(ga.begin(), ga.end(), g_albedo);
   if (g_lamp) std::copy(gl.begin(), gl.end(), g_lamp);
+  return VT_OK;
+}
+
+vt_status vt_calib_intrinsics_grad(vt_ctx* ctx, double* g_K) {
+  if (!ctx || !g_K) return VT_ERR_ARG;
+  auto& K = ctx->calib;
+  if (!K.have_k) return fail(ctx, VT_ERR_STATE, "calib: no backward of a forward with intrinsics = 1");
+  std::vector<double> all(ctx->S.cams.size() * 8);
+  VT_CK(cudaMemcpyAsync(all.data(), K.g_K, all.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t c = 0; c < K.cams.size(); c++) std::copy(all.begin() + 8 * K.cams[c], all.begin() + 8 * K.cams[c] + 8, g_K + 8 * c);
+  return VT_OK;
+}
+
+vt_status vt_calib_export_paths(vt_ctx* ctx, uint32_t slot, uint32_t* tri_inst, float* q) {
+  if (!ctx || !tri_inst || !q) return VT_ERR_ARG;
+  auto& K = ctx->calib;
+  if (!K.have_forward || !K.stored || !K.want_k) return fail(ctx, VT_ERR_STATE, "calib: export needs a stored forward with intrinsics = 1");
+  if (slot >= K.cams.size()) return fail(ctx, VT_ERR_ARG, "calib: camera slot out of range");
+  const uint32_t cam = K.cams[slot];
+  const vtk::CamParams cp = calib_cam(ctx, cam, K.spp, K.nl, K.seed, K.depth);
+  const size_t paths = size_t(cp.w) * cp.h * cp.spp;
+  const size_t b_ti = paths * vtk::CAL_MAX_DEPTH * 8, b_q = paths * vtk::CAL_MAX_DEPTH * vtk::CAL_MAX_NL * 4;
+  vt_status s = ensure_scratch(ctx, b_ti + b_q + 512);
+  if (s != VT_OK) return s;
+  char* base = static_cast<char*>(ctx->d_scratch);
+  uint32_t* d_ti = reinterpret_cast<uint32_t*>(base);
+  float* d_q = reinterpret_cast<float*>(base + (b_ti + 255) / 256 * 256);
+  vtk::calib_export_paths(cp, static_cast<char*>(K.records) + K.rec_off[slot] * vtk::calib_record_bytes(1),
+                          static_cast<char*>(K.tan) + K.rec_off[slot] * vtk::calib_tan_bytes(1), d_ti, d_q, ctx->stream);
+  VT_CK(cudaGetLastError());
+  VT_CK(cudaMemcpyAsync(tri_inst, d_ti, b_ti, cudaMemcpyDefault, ctx->stream));
+  VT_CK(cudaMemcpyAsync(q, d_q, b_q, cudaMemcpyDefault, ctx->stream));
+  VT_CK(cudaStreamSynchronize(ctx->stream));
   return VT_OK;
 }
 

@@ -16,6 +16,7 @@
 #include <utility>
 
 #include "vt_calib.cuh"
+#include "vt_calib_tan.cuh"
 #include "vt_camera.cuh"
 #include "vt_wave.cuh"
 
@@ -51,6 +52,17 @@ struct CalPath {
   uint32_t node;         // node term at the last shading vertex (~0: none)
 };
 
+// the derivative record of a path in d0 (stored form, kept only when the intrinsics' derivative is asked for): each
+// light sample's dq (per unit emitter radiance and albedo; cleared with q when the sample is occluded), the emitter
+// hit's d a, the ray's tangents between bounces, and the triangle each bounce hit (~0: none)
+struct CalTan {
+  float dq[CAL_MAX_DEPTH][CAL_MAX_NL][3];
+  float de[3];
+  Tan3 Jo, Jd;
+  float3 dpb;
+  uint32_t tri[CAL_MAX_DEPTH], inst[CAL_MAX_DEPTH];
+};
+
 // emitter sample by the area CDF, with the index of the triangle (gpu/wgsl/shade.wgsl.js:31)
 __device__ __forceinline__ uint32_t sample_emitter_idx(const Scene& S, float3 u, float time, float3& p, float3& n, float3& axis) {
   uint32_t lo = 0, hi = S.emit_n - 1u;
@@ -71,7 +83,45 @@ __device__ __forceinline__ uint32_t sample_emitter_idx(const Scene& S, float3 u,
   return lo;
 }
 
-__device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, const CalibDev& C, uint32_t id, uint32_t i, CalPath& P) {
+__device__ __forceinline__ float3 alb(const CalibDev& C, uint32_t m) { return f3(__ldg(C.albedo + 3 * m), __ldg(C.albedo + 3 * m + 1), __ldg(C.albedo + 3 * m + 2)); }
+
+// the emitter hit's weight a = w prof (w = 1 at the first vertex, else pb^2 / (pb^2 + nl^2 pL^2) with
+// pL = t^2 / (cosE area)) and its derivative, given the tangents of the ray, of the hit distance and of the
+// previous vertex's continuation pdf pb
+__device__ __forceinline__ float3 tan_emitter_hit(const Scene& S, const Hit& h, const Surf& s, float3 d, float tt, uint32_t b, float pb, float3 dpb,
+                                                 float fnl, float area, const Tan3& Jd, const Tan3& Jx, float3 dt) {
+  Tan3 JnE;
+  const float3 nE = tan_interp_normal(S, h, s, tt, Jx, JnE);
+  const float3 axis = emitter_axis_at(S, tt);
+  const float c = clampf(dot(-d, axis), -1.0f, 1.0f);
+  const float th = acosf(c);
+  const float prof = profile(S, th), slope = profile_slope(S, th);
+  const float cosE = dot(-d, nE);
+  const float pL = h.t * h.t / (cosE * area);
+  const float A = pb * pb, B = fnl * fnl * pL * pL, AB = A + B;
+  const float w = b > 1 ? A / AB : 1.0f;
+  const float dtv[3] = {dt.x, dt.y, dt.z}, dpbv[3] = {dpb.x, dpb.y, dpb.z};
+  float out[3];
+  for (int j = 0; j < 3; j++) {
+    const float dc = -dot(axis, Jd.c[j]);
+    const float dth = (1.0f - c * c) > 0.0f ? -dc / sqrtf(1.0f - c * c) : 0.0f;
+    float dw = 0.0f;
+    if (b > 1) {
+      const float dcosE = -dot(Jd.c[j], nE) - dot(d, JnE.c[j]);
+      const float dpL = (2.0f * h.t * dtv[j] * cosE - h.t * h.t * dcosE) / (cosE * cosE * area);
+      const float dA = 2.0f * pb * dpbv[j], dB = 2.0f * fnl * fnl * pL * dpL;
+      dw = (dA * B - A * dB) / (AB * AB);
+    }
+    out[j] = dw * prof + w * slope * dth;
+  }
+  return f3(out[0], out[1], out[2]);
+}
+
+// With TAN, dL[c] (c = r, g, b) receives the derivative of the path's radiance in channel c with respect to its
+// primary direction d0; the path's values are the estimator's own either way.
+template <bool TAN>
+__device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, const CalibDev& C, uint32_t id, uint32_t i, CalPath& P,
+                                           float3* dL = nullptr) {
   P.n = 0;
   P.emit_lamp = MISS;
   P.emit_a = 0.0f;
@@ -86,10 +136,16 @@ __device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, 
   const float area = __ldg(S.su + 3);
   const uint32_t skip_sh = ldu(S.su + 7);
   float pb_prev = 0.0f;
+  Tan3 Jo, Jd;
+  float3 dpb = f3(0, 0, 0), T = f3(1, 1, 1);
+  if (TAN) { Jo = tan_zero(); Jd = tan_identity(); dL[0] = dL[1] = dL[2] = f3(0, 0, 0); }
   for (uint32_t b = 1; b <= cp.max_depth; b++) {
     const Hit h = trace_scene<false>(S, cp.root, o, d, 0.0f, BIG, tt, 3u, b == 1 ? cp.skip : 0u);
     if (h.tri == MISS) return;
     const Surf s = surface(S, h, o, d, tt);
+    Tan3 Jx;
+    float3 dt;
+    if (TAN) tan_plane_hit(Jo, Jd, d, s.ng, h.t, Jx, dt);
     if (s.flags & VT_F_EMITTER) {
       const float3 nE = emitter_normal(S, h, s, tt);
       const float cosE = dot(-d, nE);
@@ -102,6 +158,10 @@ __device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, 
         }
         P.emit_lamp = __ldg(C.emit_of_tri + h.tri);
         P.emit_a = w * prof;
+        if (TAN) {
+          const float3 de = tan_emitter_hit(S, h, s, d, tt, b, pb_prev, dpb, fnl, area, Jd, Jx, dt) * __ldg(C.lamp + P.emit_lamp);
+          dL[0] = dL[0] + de * T.x; dL[1] = dL[1] + de * T.y; dL[2] = dL[2] + de * T.z;
+        }
       }
       return;
     }
@@ -109,6 +169,9 @@ __device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, 
     V.mat = s.mat;
     P.n++;
     const float3 n = s.ns, wo = -d;
+    Tan3 Jn;
+    float3 Tr = T;
+    if (TAN) { Jn = tan_shading_normal(S, h, s, tt, Jx); Tr = mul3(T, alb(C, s.mat)); }
     const float sh0 = b == 1 ? u01(pcg(hs + 3u)) : bounce_shift(hs, b, 0);
     const float sh1 = b == 1 ? u01(pcg(hs + 4u)) : bounce_shift(hs, b, 1);
     const float sh2 = b == 1 ? u01(pcg(hs + 5u)) : bounce_shift(hs, b, 2);
@@ -127,7 +190,13 @@ __device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, 
       const float pdfW = d2 / (cosE * area), pb = cosS * INV_PI_F;
       const float w = fnl * fnl * pdfW * pdfW / (fnl * fnl * pdfW * pdfW + pb * pb);
       const Hit sh = trace_scene<true>(S, cp.root, offset_ray(s.p, s.ng, wi), wi, 0.0f, dist - 2e-5f, tt, 3u, skip_sh);
-      if (sh.tri == MISS) V.q[j] = prof * cosS * w * INV_PI_F / pdfW;
+      if (sh.tri == MISS) {
+        V.q[j] = prof * cosS * w * INV_PI_F / pdfW;
+        if (TAN) {
+          const float3 dq = tan_light(S, s.p, n, lp, ln, la, area, fnl, V.q[j], Jx, Jn) * (__ldg(C.lamp + V.lamp[j]) / fnl);
+          dL[0] = dL[0] + dq * Tr.x; dL[1] = dL[1] + dq * Tr.y; dL[2] = dL[2] + dq * Tr.z;
+        }
+      }
     }
     if (b == cp.max_depth) {
       if (h.inst == MISS && h.tri < C.n_static_tris) P.node = __ldg(C.tri_node + h.tri);
@@ -144,12 +213,17 @@ __device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, 
     const float cl = dot(n, l);
     if (cl <= 0.0f || dot(s.ng, l) <= 0.0f) return;
     pb_prev = cl * INV_PI_F;
+    if (TAN) {
+      const Tan3 Jl = tan_continue(n, Jn, r, cpz, sp, sqrtf(fmaxf(0.0f, 1.0f - u1)));
+      dpb = (tan_dot(l, Jn) + tan_dot(n, Jl)) * INV_PI_F;
+      Jo = Jx;
+      Jd = Jl;
+      T = Tr;
+    }
     o = offset_ray(s.p, s.ng, l);
     d = l;
   }
 }
-
-__device__ __forceinline__ float3 alb(const CalibDev& C, uint32_t m) { return f3(__ldg(C.albedo + 3 * m), __ldg(C.albedo + 3 * m + 1), __ldg(C.albedo + 3 * m + 2)); }
 
 // radiance of a recorded path
 __device__ __forceinline__ float3 path_value(const CalibDev& C, const CalPath& P, uint32_t nl) {
@@ -230,8 +304,9 @@ __device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, u
 // records without tracing again. Records of path (i, id) of a camera sit at rec[i n_pix + id].
 constexpr int WT = 256;
 
+template <bool TAN>
 __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const CamParams cp, const CalibDev C, WaveBufs wb, CalPath* rec,
-                                                        uint32_t b) {
+                                                        CalTan* tan, uint32_t b) {
   const uint32_t n = *wb.count_in;
   const uint32_t nl = cp.n_light;
   const float fnl = float(nl);
@@ -247,8 +322,26 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
     const float tt = o4.w, pb_prev = d4.w;
     const Hit h{hv.x, hv.y, hv.z, __float_as_uint(hv.w), wb.hinst[p]};
     bool cont = false, shadow = false;
+    Tan3 Jo, Jd, Jx;
+    float3 dpb, dt;
+    if (TAN) {
+      CalTan& G = tan[p];
+      if (b == 1) {
+        for (uint32_t a = 0; a < CAL_MAX_DEPTH; a++) {
+          G.tri[a] = MISS; G.inst[a] = MISS;
+          for (uint32_t j = 0; j < CAL_MAX_NL; j++) G.dq[a][j][0] = G.dq[a][j][1] = G.dq[a][j][2] = 0.0f;
+        }
+        G.de[0] = G.de[1] = G.de[2] = 0.0f;
+        Jo = tan_zero(); Jd = tan_identity(); dpb = f3(0, 0, 0);
+      } else {
+        Jo = G.Jo; Jd = G.Jd; dpb = G.dpb;
+      }
+      G.tri[b - 1] = h.tri;
+      G.inst[b - 1] = h.inst;
+    }
     if (h.tri != MISS) {
       const Surf s = surface(S, h, o, d, tt);
+      if (TAN) tan_plane_hit(Jo, Jd, d, s.ng, h.t, Jx, dt);
       if (s.flags & VT_F_EMITTER) {
         const float3 nE = emitter_normal(S, h, s, tt);
         const float cosE = dot(-d, nE);
@@ -261,6 +354,10 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
           }
           P.emit_lamp = __ldg(C.emit_of_tri + h.tri);
           P.emit_a = w * prof;
+          if (TAN) {
+            const float3 de = tan_emitter_hit(S, h, s, d, tt, b, pb_prev, dpb, fnl, area, Jd, Jx, dt);
+            tan[p].de[0] = de.x; tan[p].de[1] = de.y; tan[p].de[2] = de.z;
+          }
         }
       } else {
         const uint32_t vk = P.n;
@@ -268,6 +365,8 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
         V.mat = s.mat;
         P.n = vk + 1;
         const float3 nrm = s.ns, wo = -d;
+        Tan3 Jn;
+        if (TAN) Jn = tan_shading_normal(S, h, s, tt, Jx);
         const float sh0 = b == 1 ? u01(pcg(hs + 3u)) : bounce_shift(hs, b, 0);
         const float sh1 = b == 1 ? u01(pcg(hs + 4u)) : bounce_shift(hs, b, 1);
         const float sh2 = b == 1 ? u01(pcg(hs + 5u)) : bounce_shift(hs, b, 2);
@@ -288,6 +387,10 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
           const float pdfW = d2 / (cosE * area), pb = cosS * INV_PI_F;
           const float w = fnl * fnl * pdfW * pdfW / (fnl * fnl * pdfW * pdfW + pb * pb);
           V.q[j] = prof * cosS * w * INV_PI_F / pdfW;
+          if (TAN) {
+            const float3 dq = tan_light(S, s.p, nrm, lp, ln, la, area, fnl, V.q[j], Jx, Jn);
+            tan[p].dq[vk][j][0] = dq.x; tan[p].dq[vk][j][1] = dq.y; tan[p].dq[vk][j][2] = dq.z;
+          }
           const float3 so = offset_ray(s.p, s.ng, wi);
           srec[3 * j] = make_float4(so.x, so.y, so.z, dist - 2e-5f);
           srec[3 * j + 1] = make_float4(wi.x, wi.y, wi.z, 1.0f);
@@ -312,6 +415,12 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
             wb.d[p] = make_float4(l.x, l.y, l.z, cl * INV_PI_F);
             wb.meta[p] = make_uint4(meta.x, meta.y, meta.z, b + 1u);
             cont = true;
+            if (TAN) {
+              const Tan3 Jl = tan_continue(nrm, Jn, r, cpz, sp, sqrtf(fmaxf(0.0f, 1.0f - u1)));
+              tan[p].dpb = (tan_dot(l, Jn) + tan_dot(nrm, Jl)) * INV_PI_F;
+              tan[p].Jo = Jx;
+              tan[p].Jd = Jl;
+            }
           }
         }
       }
@@ -324,7 +433,8 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
 }
 
 // any hit of the pending light samples on persistent lanes; an occluded sample's contribution is cleared in the record
-__global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, const CamParams cp, WaveBufs wb, CalPath* rec) {
+template <bool TAN>
+__global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, const CamParams cp, WaveBufs wb, CalPath* rec, CalTan* tan) {
   const uint32_t n = *wb.count_sh;
   const uint32_t nl = cp.n_light;
   const uint32_t skip = ldu(S.su + 7);
@@ -360,7 +470,11 @@ __global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, cons
     bool done = r == 2;
     if (r == 1) done = !trace_phase(S, cp.root, o, d, 0.0f, tt, 3u, skip, st, st.k + 1);
     if (!done) continue;
-    if (st.best.tri != MISS) rec[p].v[__float_as_uint(srec[3 * j + 2].z)].q[j] = 0.0f;
+    if (st.best.tri != MISS) {
+      const uint32_t vk = __float_as_uint(srec[3 * j + 2].z);
+      rec[p].v[vk].q[j] = 0.0f;
+      if (TAN) tan[p].dq[vk][j][0] = tan[p].dq[vk][j][1] = tan[p].dq[vk][j][2] = 0.0f;
+    }
     j++;
     active = next_sample();
   }
@@ -368,14 +482,49 @@ __global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, cons
 
 // per pixel: the image value from the records in sub-sample order, its loss partial (forward); or the gradient of
 // every record (backward)
-__global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, const CalibDev C, const CalPath* __restrict__ rec, uint32_t n_pix,
-                                                          int backward) {
+// the derivative in d0 of a recorded path's radiance, per channel, from its derivative record
+__device__ __forceinline__ void path_tangent(const CalibDev& C, const CalPath& P, const CalTan& G, uint32_t nl, float3* dL) {
+  dL[0] = dL[1] = dL[2] = f3(0, 0, 0);
+  float3 T = f3(1, 1, 1);
+  for (uint32_t k = 0; k < P.n; k++) {
+    T = mul3(T, alb(C, P.v[k].mat));
+    for (uint32_t j = 0; j < nl; j++) {
+      if (P.v[k].q[j] == 0.0f) continue;
+      const float3 dq = f3(G.dq[k][j][0], G.dq[k][j][1], G.dq[k][j][2]) * (__ldg(C.lamp + P.v[k].lamp[j]) / float(nl));
+      dL[0] = dL[0] + dq * T.x; dL[1] = dL[1] + dq * T.y; dL[2] = dL[2] + dq * T.z;
+    }
+  }
+  if (P.emit_lamp != MISS) {
+    const float3 de = f3(G.de[0], G.de[1], G.de[2]) * __ldg(C.lamp + P.emit_lamp);
+    dL[0] = dL[0] + de * T.x; dL[1] = dL[1] + de * T.y; dL[2] = dL[2] + de * T.z;
+  }
+}
+
+// the derivative of the loss in the camera's intrinsics from one sub-sample: G = g . dL / d d0 (FP64), chained
+// through d d0 / d K at the sub-sample's image position
+__device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_t id, uint32_t i, const float3* dL, double3 g, double* sh_k) {
+  uint32_t x, y;
+  if (!pixel_xy(cp, id, x, y)) return;
+  const double G[3] = {g.x * dL[0].x + g.y * dL[1].x + g.z * dL[2].x, g.x * dL[0].y + g.y * dL[1].y + g.z * dL[2].y,
+                       g.x * dL[0].z + g.y * dL[1].z + g.z * dL[2].z};
+  if (G[0] == 0.0 && G[1] == 0.0 && G[2] == 0.0) return;
+  const uint32_t hs = hash3(x, y, cp.seed * 64u + cp.cam_index);
+  const float2 uv = subsample_uv(x, y, i, hs);
+  float J[3][8];
+  kb4_ray_jacobian(cp.lens, uv.x, uv.y, f3(cp.rx[0], cp.rx[1], cp.rx[2]), f3(cp.ry[0], cp.ry[1], cp.ry[2]), f3(cp.rz[0], cp.rz[1], cp.rz[2]), J);
+  for (int k = 0; k < 8; k++) atomicAdd(sh_k + k, G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k]);
+}
+
+__global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, const CalibDev C, const CalPath* __restrict__ rec,
+                                                          const CalTan* __restrict__ tan, uint32_t n_pix, int backward) {
   extern __shared__ double sm[];
   double* sh_alb = sm;
   double* sh_lamp = sm + 3 * C.n_mat;
   __shared__ double red[CT / 32];
+  __shared__ double sh_k[8];
   if (backward) {
     for (uint32_t k = threadIdx.x; k < 3 * C.n_mat + C.n_lamps; k += blockDim.x) sm[k] = 0.0;
+    if (threadIdx.x < 8) sh_k[threadIdx.x] = 0.0;
     __syncthreads();
   }
   double loss = 0.0;
@@ -388,7 +537,14 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
       const float4 I = C.image[px], Tg = C.target ? C.target[px] : make_float4(0.f, 0.f, 0.f, 0.f);
       const double k = 2.0 * C.inv_count * double(sc);
       const double3 g = make_double3(k * (double(I.x) - Tg.x), k * (double(I.y) - Tg.y), k * (double(I.z) - Tg.z));
-      for (uint32_t i = 0; i < cp.spp; i++) path_grad(C, rec[size_t(i) * n_pix + id], cp.n_light, g, sh_alb, sh_lamp);
+      for (uint32_t i = 0; i < cp.spp; i++) {
+        path_grad(C, rec[size_t(i) * n_pix + id], cp.n_light, g, sh_alb, sh_lamp);
+        if (backward == 2) {
+          float3 dL[3];
+          path_tangent(C, rec[size_t(i) * n_pix + id], tan[size_t(i) * n_pix + id], cp.n_light, dL);
+          add_intrinsics_grad(cp, id, i, dL, g, sh_k);
+        }
+      }
     } else {
       float3 s = f3(0, 0, 0);
       for (uint32_t i = 0; i < cp.spp; i++) s = s + path_value(C, rec[size_t(i) * n_pix + id], cp.n_light);
@@ -405,6 +561,7 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < 3 * C.n_mat; k += blockDim.x) if (sm[k] != 0.0) atomicAdd(C.g_albedo + k, sm[k]);
     for (uint32_t k = threadIdx.x; k < C.n_lamps; k += blockDim.x) if (sh_lamp[k] != 0.0) atomicAdd(C.g_lamp + k, sh_lamp[k]);
+    if (backward == 2 && threadIdx.x < 8 && sh_k[threadIdx.x] != 0.0) atomicAdd(C.g_K + threadIdx.x, sh_k[threadIdx.x]);
     return;
   }
   for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
@@ -422,8 +579,10 @@ __global__ void __launch_bounds__(CT) calib_kernel(const Scene S, const CamParam
   double* sh_alb = sm;                       // n_mat x 3
   double* sh_lamp = sm + 3 * C.n_mat;        // n_lamps
   __shared__ double red[CT / 32];
+  __shared__ double sh_k[8];
   if (backward) {
     for (uint32_t k = threadIdx.x; k < 3 * C.n_mat + C.n_lamps; k += blockDim.x) sm[k] = 0.0;
+    if (threadIdx.x < 8) sh_k[threadIdx.x] = 0.0;
     __syncthreads();
   }
   double loss = 0.0;
@@ -441,7 +600,13 @@ __global__ void __launch_bounds__(CT) calib_kernel(const Scene S, const CamParam
     float3 s = f3(0, 0, 0);
     for (uint32_t i = 0; i < cp.spp; i++) {
       CalPath P;
-      calib_path(S, cp, C, id, i, P);
+      if (backward == 2) {
+        float3 dL[3];
+        calib_path<true>(S, cp, C, id, i, P, dL);
+        add_intrinsics_grad(cp, id, i, dL, g, sh_k);
+      } else {
+        calib_path<false>(S, cp, C, id, i, P);
+      }
       if (backward) path_grad(C, P, cp.n_light, g, sh_alb, sh_lamp);
       else s = s + path_value(C, P, cp.n_light);
     }
@@ -459,6 +624,7 @@ __global__ void __launch_bounds__(CT) calib_kernel(const Scene S, const CamParam
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < 3 * C.n_mat; k += blockDim.x) if (sh_alb[k] != 0.0) atomicAdd(C.g_albedo + k, sh_alb[k]);
     for (uint32_t k = threadIdx.x; k < C.n_lamps; k += blockDim.x) if (sh_lamp[k] != 0.0) atomicAdd(C.g_lamp + k, sh_lamp[k]);
+    if (backward == 2 && threadIdx.x < 8 && sh_k[threadIdx.x] != 0.0) atomicAdd(C.g_K + threadIdx.x, sh_k[threadIdx.x]);
     return;
   }
   for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
@@ -581,11 +747,12 @@ __global__ void sum_kernel(const double* __restrict__ p, uint32_t n, double* __r
 }
 // calib_shade_kernel's grid-stride loop runs as one wave of its own occupancy (3 blocks of 256 per SM at 80
 // registers) rather than on the traversal kernels' grid, a wave and a third of it (C4 forward 200 -> 196 ms)
+template <bool TAN>
 int calib_shade_grid() {
   static std::atomic<int> grid[MAX_DEVICES];
   return per_device_value(grid, [](int dev) {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, calib_shade_kernel, WT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, calib_shade_kernel<TAN>, WT, 0);
     return device_sms(dev) * std::max(1, per);
   });
 }
@@ -593,9 +760,12 @@ int calib_shade_grid() {
 
 size_t calib_record_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalPath); }
 
-uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records, int blocks,
-                            cudaStream_t st) {
+size_t calib_tan_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalTan); }
+
+uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records, void* tangents,
+                            int blocks, cudaStream_t st) {
   CalPath* rec = static_cast<CalPath*>(records);
+  CalTan* tan = static_cast<CalTan*>(tangents);
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t per_wave = std::max(1u, std::min(cp.spp, wave_paths / std::max(1u, n_pix)));
   for (uint32_t i0 = 0; i0 < cp.spp; i0 += per_wave) {
@@ -603,6 +773,7 @@ uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev&
     cudaMemsetAsync(wb.counts, 0, 16, st);
     launch_wave_gen(cp, wb, i0, n_i, n_pix, blocks, st);
     CalPath* rb = rec + size_t(i0) * n_pix;
+    CalTan* tb = tan ? tan + size_t(i0) * n_pix : nullptr;
     for (uint32_t b = 1; b <= cp.max_depth; b++) {
       WaveBufs w = wb;
       w.q_in = (b & 1) ? wb.qa : wb.qb;
@@ -613,27 +784,54 @@ uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev&
       cudaMemsetAsync(w.count_out, 0, 4, st);
       cudaMemsetAsync(w.count_sh, 0, 4, st);
       launch_wave_extend(S, cp, w, blocks, st);
-      calib_shade_kernel<<<calib_shade_grid(), WT, 0, st>>>(S, cp, C, w, rb, b);
+      if (tb) calib_shade_kernel<true><<<calib_shade_grid<true>(), WT, 0, st>>>(S, cp, C, w, rb, tb, b);
+      else calib_shade_kernel<false><<<calib_shade_grid<false>(), WT, 0, st>>>(S, cp, C, w, rb, nullptr, b);
       cudaMemsetAsync(w.fetch, 0, 4, st);
-      calib_shadow_kernel<<<blocks, WT, 0, st>>>(S, cp, w, rb);
+      if (tb) calib_shadow_kernel<true><<<blocks, WT, 0, st>>>(S, cp, w, rb, tb);
+      else calib_shadow_kernel<false><<<blocks, WT, 0, st>>>(S, cp, w, rb, nullptr);
     }
   }
   const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
-  calib_records_kernel<<<grid, CT, 0, st>>>(cp, C, rec, n_pix, 0);
+  calib_records_kernel<<<grid, CT, 0, st>>>(cp, C, rec, tan, n_pix, 0);
   return grid;
 }
 
-void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* records, int blocks, cudaStream_t st) {
+void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* records, const void* tangents, int blocks, cudaStream_t st) {
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
-  calib_records_kernel<<<grid, CT, size_t(3 * C.n_mat + C.n_lamps) * 8, st>>>(cp, C, static_cast<const CalPath*>(records), n_pix, 1);
+  calib_records_kernel<<<grid, CT, size_t(3 * C.n_mat + C.n_lamps) * 8, st>>>(cp, C, static_cast<const CalPath*>(records),
+                                                                             static_cast<const CalTan*>(tangents), n_pix, tangents ? 2 : 1);
 }
 
-uint32_t launch_calib(const Scene& S, const CamParams& cp, const CalibDev& C, bool backward, int blocks, cudaStream_t st) {
+// per path of the camera's records, in (row, column, sub-sample) order: the triangle and instance of each bounce
+// (~0: none) and each vertex's light samples' q (0: occluded or no contribution)
+__global__ void calib_export_paths_kernel(const CamParams cp, const CalPath* __restrict__ rec, const CalTan* __restrict__ tan, uint32_t n_pix,
+                                          uint32_t* __restrict__ tri_inst, float* __restrict__ q) {
+  const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t x, y;
+  if (id >= n_pix || !pixel_xy(cp, id, x, y)) return;
+  for (uint32_t i = 0; i < cp.spp; i++) {
+    const size_t r = size_t(i) * n_pix + id, o = (size_t(y) * cp.w + x) * cp.spp + i;
+    const CalPath& P = rec[r];
+    for (uint32_t b = 0; b < CAL_MAX_DEPTH; b++) {
+      tri_inst[(o * CAL_MAX_DEPTH + b) * 2] = tan[r].tri[b];
+      tri_inst[(o * CAL_MAX_DEPTH + b) * 2 + 1] = tan[r].inst[b];
+      for (uint32_t j = 0; j < CAL_MAX_NL; j++) q[(o * CAL_MAX_DEPTH + b) * CAL_MAX_NL + j] = b < P.n && j < cp.n_light ? P.v[b].q[j] : 0.0f;
+    }
+  }
+}
+
+void calib_export_paths(const CamParams& cp, const void* records, const void* tangents, uint32_t* tri_inst, float* q, cudaStream_t st) {
+  const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
+  calib_export_paths_kernel<<<(n_pix + 127) / 128, 128, 0, st>>>(cp, static_cast<const CalPath*>(records), static_cast<const CalTan*>(tangents),
+                                                                n_pix, tri_inst, q);
+}
+
+uint32_t launch_calib(const Scene& S, const CamParams& cp, const CalibDev& C, int mode, int blocks, cudaStream_t st) {
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
-  const size_t smem = backward ? size_t(3 * C.n_mat + C.n_lamps) * 8 : 0;
-  calib_kernel<<<grid, CT, smem, st>>>(S, cp, C, n_pix, backward ? 1 : 0);
+  const size_t smem = mode ? size_t(3 * C.n_mat + C.n_lamps) * 8 : 0;
+  calib_kernel<<<grid, CT, smem, st>>>(S, cp, C, n_pix, mode);
   return grid;
 }
 

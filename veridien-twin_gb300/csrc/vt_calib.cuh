@@ -23,18 +23,27 @@ struct CalibDev {
   double* g_albedo;             // backward accumulators (FP64)
   double* g_lamp;
   double* g_H;                  // 3 x n_nodes
+  double* g_K;                  // this camera's 8 intrinsics (fx, fy, cx, cy, k1..k4): the image loss's derivative
 };
 
 // stored-path form: the wavefront forward of one camera (records of all its paths kept, path (i, id) at
 // records[i n_pix + id]), the image and per-block loss partials (returns their number); and the backward from the
 // records, without tracing
 size_t calib_record_bytes(uint32_t paths);
+// with `tangents` (calib_tan_bytes per path, NULL: none) the forward also keeps each path's derivative record in its
+// primary direction, and the backward then adds the derivative in the camera's intrinsics (C.g_K)
+size_t calib_tan_bytes(uint32_t paths);
 uint32_t calib_wave_forward(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records,
-                            int blocks, cudaStream_t st);
-void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* records, int blocks, cudaStream_t st);
+                            void* tangents, int blocks, cudaStream_t st);
+void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* records, const void* tangents, int blocks, cudaStream_t st);
+// the recorded paths' discrete decisions (for checking): per path in (row, column, sub-sample) order, CAL_MAX_DEPTH x
+// (triangle, instance) and CAL_MAX_DEPTH x CAL_MAX_NL light-sample weights q (0: occluded or no contribution)
+void calib_export_paths(const CamParams& cp, const void* records, const void* tangents, uint32_t* tri_inst, float* q, cudaStream_t st);
 // replay form, forward: image + per-block loss partials (returns the number of partials); backward: gradients of the
 // image loss, every path traced again from its sample numbers
-uint32_t launch_calib(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, bool backward, int blocks, cudaStream_t st);
+// mode 0 forward, 1 backward (albedos, emitter radiances, node light), 2 the backward and the derivative in the
+// camera's intrinsics (C.g_K)
+uint32_t launch_calib(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, int mode, int blocks, cudaStream_t st);
 // D[i][t]: irradiance at node i (centre, normal) from emitter triangle t at unit radiance, with visibility
 void launch_direct_transfer(const vtd::Scene& S, const float* centres, const float* normals, uint32_t n, uint32_t n_lamps,
                             uint32_t samples, float* D, cudaStream_t st);

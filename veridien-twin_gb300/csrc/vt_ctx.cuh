@@ -110,9 +110,14 @@ struct vt_ctx {
     uint32_t max_partials = 0;
     std::vector<float4*> image, target;   // per scene camera (device, w x h)
     std::vector<std::vector<float>> albedo_host;
-    // path records of the last forward (stored form), per camera of the request
+    // path records of the last forward (stored form), per camera of the request, and with the intrinsics' derivative
+    // asked for, each path's derivative record in its primary direction
     void* records = nullptr;
     size_t rec_cap = 0;
+    void* tan = nullptr;
+    size_t tan_cap = 0;
+    bool want_k = false, have_k = false;
+    double* g_K = nullptr;   // 8 per scene camera
     std::vector<size_t> rec_off;
     bool stored = false;
     // last forward

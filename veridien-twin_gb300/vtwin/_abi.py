@@ -139,7 +139,7 @@ class vt_calib_req(C.Structure):
     _fields_ = [("cameras", C.POINTER(C.c_uint32)), ("n_cameras", C.c_uint32), ("spp", C.c_uint32), ("light_samples", C.c_uint32),
                 ("seed", C.c_uint32), ("max_depth", C.c_uint32), ("jacobi_iters", C.c_uint32),
                 ("albedo", C.POINTER(C.c_double)), ("lamp", C.POINTER(C.c_double)), ("targets", C.POINTER(C.c_float)),
-                ("images", C.POINTER(C.c_float)), ("replay", C.c_uint32)]
+                ("images", C.POINTER(C.c_float)), ("replay", C.c_uint32), ("intrinsics", C.c_uint32)]
 
 
 class vt_solve_req(C.Structure):

@@ -53,6 +53,8 @@ SIGNATURES = {
     "vt_calib_export": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vt_calib_forward": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_calib_req), C.POINTER(C.c_double)]),
     "vt_calib_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vt_calib_intrinsics_grad": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vt_calib_export_paths": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "vt_set_camera_intrinsics": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_get_camera_intrinsics": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_reproj_loss": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_double),

@@ -5,9 +5,12 @@
               + w_reproj x reprojection loss (mean over cameras, fiducials and both coordinates, vt_reproj_loss)
 
 `Calibration.forward(x)` returns the loss and keeps what `backward()` needs; `backward()` returns d loss / d x:
-the albedo and lamp entries by path replay and the transposed radiosity solve (vt_calib_backward), the intrinsics
-by the analytic KB4 Jacobian. The image term's dependence on the intrinsics (through visibility edges) is not
-differentiated: the intrinsics are pinned by the fiducials.
+the albedo and lamp entries by path replay and the transposed radiosity solve (vt_calib_backward); the intrinsics
+by the reprojection term's analytic KB4 Jacobian and, with image_intrinsics=True, the image term's derivative along
+every path's primary ray (vt_calib_intrinsics_grad: hit points, normals, light samples' weights, continuations,
+through the KB4 inverse). The image term's steps (a ray's hit triangle, a shadow ray's outcome) are not
+differentiated, and with intrinsics far from the target's (10 %: edges tens of pixels apart) those steps carry most
+of the image loss's dependence on K, so by default the intrinsics follow the fiducials alone.
 """
 from __future__ import annotations
 
@@ -16,14 +19,16 @@ import numpy as np
 
 class Calibration:
     def __init__(self, renderer, cameras, targets, fiducials=None, uv_targets=None, w_reproj=1.0, spp=32, light_samples=1, seed=0,
-                 max_depth=3, jacobi_iters=0):
+                 max_depth=3, jacobi_iters=0, image_intrinsics=False):
         self.r = renderer
         self.cameras = [renderer._cam(c) for c in cameras]
         self.targets = [np.ascontiguousarray(t, np.float32) for t in targets]
         self.fid = None if fiducials is None else np.ascontiguousarray(fiducials, np.float64)
         self.uv_t = None if uv_targets is None else np.ascontiguousarray(uv_targets, np.float64)
         self.w = float(w_reproj)
-        self.kw = dict(spp=spp, lightSamples=light_samples, seed=seed, max_depth=max_depth, jacobi_iters=jacobi_iters)
+        self.kw = dict(spp=spp, lightSamples=light_samples, seed=seed, max_depth=max_depth, jacobi_iters=jacobi_iters,
+                       intrinsics=bool(image_intrinsics))
+        self.image_intrinsics = bool(image_intrinsics)
         info = renderer.calib_info
         self.n_mat, self.n_lamps = info["n_materials"], info["n_lamps"]
         self.n = 3 * self.n_mat + self.n_lamps + 8 * len(self.cameras)
@@ -64,7 +69,8 @@ class Calibration:
             raise RuntimeError("backward before forward")
         (gK,) = self._last
         ga, gl = self.r.calib_backward()
-        return self.pack(ga, gl, self.w * gK)
+        gi = self.r.calib_intrinsics_grad() if self.image_intrinsics else 0.0
+        return self.pack(ga, gl, gi + self.w * gK)
 
     def loss_and_grad(self, x):
         f = self.forward(x)

@@ -491,9 +491,10 @@ class TwinRenderer:
         return out
 
     def calib_forward(self, cameras, albedo, lamp, spp=32, lightSamples=1, seed=0, max_depth=3, jacobi_iters=0, targets=None,
-                      images=True, replay=False):
+                      images=True, replay=False, intrinsics=False):
         """Image loss (mean of (I - T)^2 over pixels and channels) of the calibration render; returns (loss, images)
-        with images a list of (h, w, 4) float32 arrays per camera (or None)."""
+        with images a list of (h, w, 4) float32 arrays per camera (or None). intrinsics: the backward also gives the
+        loss's derivative in each camera's KB4 intrinsics (calib_intrinsics_grad)."""
         cams = [self._cam(c) for c in cameras]
         cam_arr = np.ascontiguousarray(cams, np.uint32)
         alb = np.ascontiguousarray(albedo, np.float64).reshape(-1, 3)
@@ -508,9 +509,11 @@ class TwinRenderer:
                            light_samples=int(lightSamples), seed=int(seed), max_depth=int(max_depth), jacobi_iters=int(jacobi_iters),
                            albedo=alb.ctypes.data_as(C.POINTER(C.c_double)), lamp=lam.ctypes.data_as(C.POINTER(C.c_double)),
                            targets=tg.ctypes.data_as(C.POINTER(C.c_float)) if tg is not None else None,
-                           images=img.ctypes.data_as(C.POINTER(C.c_float)) if img is not None else None, replay=int(bool(replay)))
+                           images=img.ctypes.data_as(C.POINTER(C.c_float)) if img is not None else None, replay=int(bool(replay)),
+                           intrinsics=int(bool(intrinsics)))
         loss = C.c_double(0.0)
         check(self.lib.vt_calib_forward(self._ctx, C.byref(q), C.byref(loss)), self._ctx)
+        self._calib_cams = cams
         out = None
         if img is not None:
             out, o = [], 0
@@ -526,6 +529,23 @@ class TwinRenderer:
         gl = np.zeros(i["n_lamps"], np.float64)
         check(self.lib.vt_calib_backward(self._ctx, _p(ga), _p(gl)), self._ctx)
         return ga, gl
+
+    def calib_intrinsics_grad(self):
+        """The last calib_backward's image-loss derivative in each forward camera's (fx, fy, cx, cy, k1..k4): an
+        (n_cameras, 8) array (the forward must have asked for it with intrinsics=True)."""
+        n = len(self._calib_cams) if getattr(self, "_calib_cams", None) else 0
+        g = np.zeros((max(n, 1), 8), np.float64)
+        check(self.lib.vt_calib_intrinsics_grad(self._ctx, _p(g)), self._ctx)
+        return g[:n]
+
+    def calib_export_paths(self, slot, spp):
+        """The stored forward's discrete path decisions of the forward's camera `slot` (for checks): triangle and
+        instance per bounce (h, w, spp, 4, 2) and light-sample weights per vertex (h, w, spp, 4, 4)."""
+        w, h = self.scene["cameras"][self._calib_cams[slot]]["size"]
+        ti = np.zeros((h, w, spp, 4, 2), np.uint32)
+        q = np.zeros((h, w, spp, 4, 4), np.float32)
+        check(self.lib.vt_calib_export_paths(self._ctx, int(slot), _p(ti), _p(q)), self._ctx)
+        return ti, q
 
     def set_intrinsics(self, name, K):
         K = np.ascontiguousarray(K, np.float64)
