@@ -41,6 +41,7 @@ def lib():
                    "or_lite_display", "or_scene_load_uniform"):
             getattr(_lib, nm).restype = None
         _lib.or_fresnel_average.restype = C.c_double
+        _lib.or_fresnel_dielectric.restype = C.c_double
         _lib.or_disc_irradiance.restype = C.c_double
         _lib.or_profile.restype = C.c_double
         _lib.or_capsule_occ.restype = C.c_double
@@ -120,6 +121,11 @@ def brute_force(T, count, o, d, tmin=0.0, tmax=np.inf):
 
 def fresnel_average(eta):
     return lib().or_fresnel_average(C.c_double(eta))
+
+
+def fresnel_dielectric(cosi, eta):
+    """gpu/bsdf.js:25 fresnelDielectric (unpolarised, FP64)."""
+    return lib().or_fresnel_dielectric(C.c_double(cosi), C.c_double(eta))
 
 
 def disc_irradiance(x, n, c, m, a, L, nr=48, nphi=96):

@@ -3152,6 +3152,7 @@ void or_brute_force(const float* T, uint32_t count, int n, const float* o, const
 }
 
 double or_fresnel_average(double eta) { return fresnel_average(eta); }
+double or_fresnel_dielectric(double cosi, double eta) { return fresnel_dielectric<double>(cosi, eta); }
 double or_disc_irradiance(const double* x, const double* n, const double* c, const double* m, double a, double L, int nr, int nphi) {
   return disc_irradiance(x, n, c, m, a, L, nr, nphi);
 }

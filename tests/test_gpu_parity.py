@@ -143,11 +143,23 @@ def _render_pair(scene, poses, mode, depth, spp, nl, node_state=None, eavg=None,
 
 
 def _radiance_stats(gpu, ref):
+    """Per-pixel relative error (largest channel); over the pixels outside 1e-4 (whole sub-samples whose shadow or
+    silhouette decision flips between float32 and float64) the mean signed error and its standard error, so that a
+    bias hiding among them would show: flips that are rounding go both ways and average to zero."""
     g, f = gpu[..., :3].astype(np.float64), ref[..., :3]
     den = np.maximum(np.abs(f).max(-1), 1e-3 * max(1e-12, np.abs(f).max()))
     rel = np.abs(g - f).max(-1) / den
+    out = rel > 1e-4
+    signed = ((g - f).sum(-1) / (3.0 * den))[out]
     return {"within_1e-4": float((rel <= 1e-4).mean()), "median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
-            "mean_rel": float(abs(g.mean() / f.mean() - 1)), "alpha_same": float((gpu[..., 3] == ref[..., 3]).mean())}
+            "mean_rel": float(abs(g.mean() / f.mean() - 1)), "alpha_same": float((gpu[..., 3] == ref[..., 3]).mean()),
+            "outside": int(out.sum()), "outside_signed_mean": float(signed.mean()) if out.any() else 0.0,
+            "outside_signed_sem": float(signed.std() / np.sqrt(max(1, out.sum()))) if out.any() else 0.0}
+
+
+def _assert_unbiased(s):
+    # the flipped pixels' signed errors average to zero within 4 standard errors
+    assert abs(s["outside_signed_mean"]) <= 4.0 * s["outside_signed_sem"] + 1e-4, s
 
 
 def test_twin_radiance_matches_fp64_oracle(inst_scene, inst_poses):
@@ -163,6 +175,7 @@ def test_twin_radiance_matches_fp64_oracle(inst_scene, inst_poses):
     s = _radiance_stats(gpu, ref)
     print("\ntwin radiance vs FP64:", s)
     assert s["median"] < 1e-5 and s["within_1e-4"] > 0.97 and s["mean_rel"] < 1e-3 and s["alpha_same"] == 1.0
+    _assert_unbiased(s)
 
 
 def test_path_radiance_matches_fp64_oracle(dome_small):
@@ -170,6 +183,7 @@ def test_path_radiance_matches_fp64_oracle(dome_small):
     s = _radiance_stats(gpu, ref)
     print("\npath (depth 4) radiance vs FP64:", s)
     assert s["median"] < 1e-5 and s["within_1e-4"] > 0.9 and s["mean_rel"] < 2e-3 and s["alpha_same"] == 1.0
+    _assert_unbiased(s)
 
 
 def test_refinement_pass(inst_scene, inst_poses):
