@@ -356,8 +356,10 @@ vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* t
  * The backward differentiates every path (path-replay backpropagation: from its record kept by a wavefront forward,
  * or by tracing it again from its sample numbers when the records do not fit) and solves the transposed radiosity
  * system lambda = F^T (g_H + rho o lambda) for the nodes' share. Parameters: per-material albedo (RGB, all
- * in (0, 1]) and per-emitter-triangle radiance. KB4 intrinsics enter through vt_reproj_loss (analytic Jacobians);
- * the image term's dependence on them (through visibility edges) is not differentiated. */
+ * in (0, 1]) and per-emitter-triangle radiance. KB4 intrinsics enter through vt_reproj_loss (analytic Jacobians)
+ * and, with `intrinsics` set, through the image term: forward-mode tangents of each path's primary ray chained
+ * through the KB4 inverse (vt_calib_intrinsics_grad). The image's dependence through visibility edges (a hit or a
+ * shadow outcome that changes with the ray) is not differentiated. */
 typedef struct {
   uint32_t n_nodes;       /* radiosity nodes (<= static triangles), e.g. 4096 */
   uint32_t lamp_samples;  /* points per (node, emitter triangle) for D, e.g. 16 */
@@ -441,6 +443,7 @@ typedef struct {
   double residual;         /* final relative residual (accurate) */
   double ms;               /* device time of the solve (CUDA events) */
   double sweep_ms;         /* mean device time of one GEMM launch of a sweep (BF16/FP8: the tcgen05 kernel) */
+  double convert_ms;       /* BF16/FP8: device time of converting F (hi/lo split, FP8 rows; 0 when reused), not in ms */
 } vt_solve_req;
 vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* req);
 

@@ -925,8 +925,8 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   q->iters = sweeps; q->refinements = refinements; q->residual = resid; q->ms = ms;
   q->sweep_ms = sweeps ? gemm_ms / sweeps : 0.0;
+  q->convert_ms = conv_ms;
   ctx->tim.solve_ms = ms;
-  (void)conv_ms;
   if (herr) return fail(ctx, VT_ERR_TIMEOUT, "solve: a tensor-core pipeline wait ran out");
   return resid <= q->tol ? VT_OK : VT_ERR_NOT_CONVERGED;
 }
@@ -1008,6 +1008,7 @@ vt_status vt_radiosity_solve(vt_ctx* ctx, vt_solve_req* q) {
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   q->iters = it; q->refinements = 0; q->residual = resid; q->ms = ms;
   q->sweep_ms = sweep_n ? sweep_sum / sweep_n : 0.0;
+  q->convert_ms = 0.0;
   ctx->tim.solve_ms = ms;
   return resid <= q->tol ? VT_OK : VT_ERR_NOT_CONVERGED;
 }

@@ -146,7 +146,8 @@ class vt_solve_req(C.Structure):
     _fields_ = [("n", C.c_uint32), ("n_rhs", C.c_uint32), ("F", f32p), ("rho", f32p), ("E", f32p), ("B", f32p),
                 ("precision", C.c_uint32), ("max_iters", C.c_uint32), ("warm_start", C.c_uint32),
                 ("check_every", C.c_uint32), ("reuse_f", C.c_uint32), ("tol", C.c_double), ("iters", C.c_uint32),
-                ("refinements", C.c_uint32), ("residual", C.c_double), ("ms", C.c_double), ("sweep_ms", C.c_double)]
+                ("refinements", C.c_uint32), ("residual", C.c_double), ("ms", C.c_double), ("sweep_ms", C.c_double),
+                ("convert_ms", C.c_double)]
 
 
 class vt_bvh_result(C.Structure):

@@ -719,7 +719,7 @@ def solve_radiosity(F, rho, E, precision=A.VT_PREC_FP32, tol=1e-6, max_iters=100
     if st not in (A.VT_OK, A.VT_ERR_NOT_CONVERGED):
         check(st, ctx)
     return B, {"iters": q.iters, "refinements": q.refinements, "residual": q.residual, "ms": q.ms, "sweep_ms": q.sweep_ms,
-               "status": st}
+               "convert_ms": q.convert_ms, "status": st}
 
 
 def solve_radiosity_static(F, rho, E, B, tol=1e-6, max_iters=1000, check_every=8, stream=None):
