@@ -331,10 +331,16 @@ def run_case(spec):
         w, h, spp = (int(x) for x in a)
         r = TwinRenderer.create(dome.make_dome_scene(seed=1, width=w, height=h))
         r.set_pose_array(A.identity_poses(1))
-        for _ in range(2):
-            r.renderCamera(0, spp=spp, lightSamples=NL, seed=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
+        r.renderCamera(0, spp=spp, lightSamples=NL, seed=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
         ms = r.timings()["render_ms"]
-        print(json.dumps({"case": spec, "render_ms": ms, "msamples_per_s": w * h * spp / ms / 1e3}))
+        # the second frame with per-launch events: its launches and rays per kernel (a profiler skips the first
+        # frame's launches and captures the second's)
+        r.kernel_profile(True, True)
+        r.renderCamera(0, spp=spp, lightSamples=NL, seed=0, mode=A.VT_SHADE_PATH, max_depth=DEPTH)
+        kt = r.timings()
+        r.kernel_profile(False, False)
+        print(json.dumps({"case": spec, "render_ms": ms, "msamples_per_s": w * h * spp / ms / 1e3,
+                          **{k: v for k, v in kt.items() if k.startswith(("extend_", "shade_", "shadow_"))}}))
         r.destroy()
     elif kind == "radiosity1":
         from vtwin.renderer import form_factors, solve_radiosity
@@ -733,7 +739,7 @@ def radiosity_bench(torch, cpu_check=True):
         res = {"n": n, "rhs": R, "tol": tol, "F": {"rays_per_pair": K, "build_ms": scene_r.timings()["trace_ms"]}}
         sols = {}
         for name, prec in precs:
-            solve_radiosity(F, P["rho"], E, precision=prec, tol=tol, max_iters=400)          # warm; converts F once
+            _, first = solve_radiosity(F, P["rho"], E, precision=prec, tol=tol, max_iters=400)   # warm; converts F once
             B, info = solve_radiosity(F, P["rho"], E, precision=prec, tol=tol, max_iters=400, reuse_f=True)
             sols[name] = B
             sb = {"fp32": 4, "bf16": 2, "fp8": 1}[name]
@@ -741,8 +747,23 @@ def radiosity_bench(torch, cpu_check=True):
             res[name] = {"ms": info["ms"], "sweeps": info["iters"], "refinements": info["refinements"], "residual": info["residual"],
                          "sweep_ms": info["sweep_ms"], "sweep_gbs": alg / (info["sweep_ms"] / 1e3) / 1e9 if info["sweep_ms"] else None,
                          "status": info["status"]}
+            if name != "fp32":
+                # the conversion of F (hi/lo split, FP8 rows) is done once per matrix and reused by later solves
+                res[name]["convert_ms"] = first["convert_ms"]
+                res[name]["ms_with_conversion"] = info["ms"] + first["convert_ms"]
+        # the plain FP32 path's roof: its sweeps are 2 n^2 R flop on the CUDA cores' FMA pipes (128 lanes per SM, 2 flop
+        # per FMA at the maximum SM clock); the FP32 solve's sweeps at that rate
+        props = torch.cuda.get_device_properties(0)
+        fp32_roof = props.multi_processor_count * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        flops = 2.0 * n * n * R
+        roof_ms = res["fp32"]["sweeps"] * flops / (fp32_roof * 1e12) * 1e3
+        res["fp32"]["roof"] = {"fma_tflops": fp32_roof, "sweep_tflops": flops / (res["fp32"]["sweep_ms"] / 1e3) / 1e12,
+                               "sweep_frac": flops / (res["fp32"]["sweep_ms"] / 1e3) / 1e12 / fp32_roof,
+                               "solve_ms_at_roof": roof_ms,
+                               "note": "the FP32 solve's sweeps at the FP32 FMA roof: a lower bound of any FP32 CUDA-core solve"}
         for name in ("bf16", "fp8"):
             res[name]["speedup_vs_fp32"] = res["fp32"]["ms"] / res[name]["ms"]
+            res[name]["speedup_vs_fp32_at_roof"] = roof_ms / res[name]["ms"]
         res["roofline_bf16_sweep"] = {"bound": "hbm", "achieved": res["bf16"]["sweep_gbs"], "peak": hbm, "unit": "GB/s",
                                       "frac": (res["bf16"]["sweep_gbs"] or 0) / hbm, "kernel": "tc_gemm_kernel<BF16>"}
         if cpu_check:

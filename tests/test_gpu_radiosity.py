@@ -99,3 +99,34 @@ def test_offset_device_f_matches_aligned(system):
     E = dome.radiosity_rhs(n, P["lamps"], 1, seed=3)
     with pytest.raises(VtError):
         solve_radiosity(Fo, P["rho"], E, precision=A.VT_PREC_FP32_TMA, tol=1e-6, max_iters=50)
+
+
+@pytest.mark.parametrize("case", ["c1", "c2_shaped"])
+def test_configured_solves_match_fp64(case):
+    """The configurations' systems gated in the suite, against the oracle's FP64 Jacobi (to 1e-12): C1 (N = 4096, one
+    right-hand side, dense F with visibility through the dome, 64 rays per pair) for FP32, BF16 and FP8; and a
+    C2-shaped system (N = 8192, 64 right-hand sides: random masks over the 96 lamp nodes, intensities U[10, 100]; F with
+    4 rays per pair, as the C2 bench builds it) for FP32, BF16 and FP8, on 8 of the columns. The bar: 1e-4 relative
+    error against FP64 (the configurations' target), each column."""
+    torch = pytest.importorskip("torch")
+    from vtwin.renderer import TwinRenderer
+
+    n, R, rays = (4096, 1, 64) if case == "c1" else (8192, 64, 4)
+    precs = (A.VT_PREC_FP32, A.VT_PREC_BF16, A.VT_PREC_FP8)
+    scene_r = TwinRenderer.create(dome.make_dome_scene(seed=1, width=32, height=24, level=5), nodes=False)
+    scene_r.set_pose_array(A.identity_poses(1))
+    P = dome.dome_patches(n, seed=2)
+    F = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    scene_r.form_factors_visible(P["centres"], P["normals"], P["areas"], rays=rays, out=F)
+    E = dome.radiosity_rhs(n, P["lamps"], R, seed=5)
+    Fh = F.cpu().numpy()
+    pick = np.unique(np.linspace(0, R - 1, min(8, R)).astype(int))
+    B64, _ = O.jacobi64(Fh, P["rho"], np.ascontiguousarray(E[:, pick]), tol=1e-12, max_it=600, threads=16)
+    for prec in precs:
+        B, info = solve_radiosity(F, P["rho"], E, precision=prec, tol=1e-6 if case == "c1" else 1e-5, max_iters=400)
+        col = np.linalg.norm(B[:, pick] - B64, axis=0) / np.linalg.norm(B64, axis=0)
+        print(f"\n{case} precision {prec}: {info['iters']} sweeps, {info['refinements']} residuals, {info['ms']:.2f} ms; "
+              f"worst column {col.max():.2e} against FP64")
+        assert info["status"] == A.VT_OK
+        assert col.max() <= 1e-4
+    scene_r.destroy()
