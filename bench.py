@@ -40,6 +40,13 @@ sys.path.insert(0, os.path.join(ROOT, "veridien-twin_gb300"))
 METRIC = "path Msamples/s and radiosity solve ms at 1e-4 rel err vs FP64, plain vs mixed"
 W_, H_, SPP, DEPTH, NL = 640, 480, 16, 4, 1
 WORKLOAD = "C0 synthetic dome path tracer: 640x480 KB4 camera, 16 spp, depth 4, 1 light sample, ~12.4k tris"
+# DRAM bytes (read + write) of wave_extend per extension ray and its issue rate, measured by ncu on this workload:
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,sm__inst_executed.avg.per_cycle_active ... -k regex:wave_extend`
+# over the four launches of one frame of `bench.py --case render:640:480:16` (1339.5 MB for 19,248,063 rays)
+EXTEND_DRAM_PER_RAY = 1339544576.0 / 19248063.0
+EXTEND_IPC = 2.755
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4 wave_extend launches of one 640x480x16 frame, "
+                  "per extension ray (69.6 B), times this run's rays per launch")
 
 
 def bench_config(world):
@@ -285,9 +292,13 @@ def main():
             rays_per_launch = kt["extend_rays"] / max(kt["extend_launches"], 1)
             per_launch = cnt["bytes_per_extension_ray"] * rays_per_launch
             ach = per_launch / (launch_ms / 1e3) / 1e9
-            dram_per_ray = 17553408.0 / 307200.0     # ncu: wave_extend, bounce 1 of 320x240x4 (profiles/wave_kernels_320x240x4.md)
             line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                                "traffic": dram_per_ray * rays_per_launch, "kernel": "wave_extend",
+                                "traffic": EXTEND_DRAM_PER_RAY * rays_per_launch, "kernel": "wave_extend",
+                                "traffic_source": TRAFFIC_SOURCE,
+                                "issue_frac": EXTEND_IPC / 4.0,
+                                "issue_note": "instructions issued per cycle per SM over its 4 schedulers, time-weighted over the frame's "
+                                              "wave_extend launches (ncu, same workload): the traversal is issue- and divergence-bound, "
+                                              "the scene stays in L1/L2",
                                 "launch_ms": launch_ms, "rays_per_launch": rays_per_launch, "bytes_per_launch": per_launch,
                                 "note": "algorithmic bytes per launch = rays x (64 B per BVH node visit + 48 B per triangle test), "
                                         "counted by the oracle on extension rays of the same frame; the scene is L2-resident, so "
@@ -633,7 +644,8 @@ def lite_frame_bench(torch, device=0, level=7, frames=12, warmup=3):
 
 
 def sensor_bench(torch, device=0):
-    """The camera sensor chain (vt_sensor_frame: optics + RI, glare, expose, demosaic, WB/CCM, NR, tone, YCbCr) at 1280x720
+    """The camera sensor chain (vt_sensor_frame: optics + RI, glare, expose, demosaic, WB/CCM, NR, tone, YCbCr; three fused
+    passes, six with glare and sharpening) at 1280x720
     (the frame of the reference's quoted 0.195 ms on an RTX 4090 for its full chain) and 1920x1200, with the default
     ISP and with every stage on (glare, Hamilton-Adams, bilateral NR, S-curve, unsharp mask). Device time per frame
     (events around the chain), median of 20 frames after 3 warm-up frames."""
@@ -655,9 +667,9 @@ def sensor_bench(torch, device=0):
                 if k >= 3:
                     ms.append(r.timings()["sensor_ms"])
             res[name + "_ms"] = float(np.median(ms))
-        # algorithmic bytes of the default chain: radiance 16 B + RI 4 B in, A 16 B out / in twice, raw 4 B out / in,
-        # green plane 4 B, B 16 B out / in, 8-bit RGB 4 B and YUV 1.5 B out
-        bpp = 16 + 4 + 16 + 16 + 4 + 4 + 4 + 4 + 16 + 16 + 16 + 4 + 1.5
+        # algorithmic bytes of the default chain (three fused passes): radiance 16 B + RI 4 B in, raw 4 B out and in,
+        # the demosaiced image 16 B out and in, 8-bit RGB 4 B and YUV 1.5 B out
+        bpp = 16 + 4 + 4 + 4 + 16 + 16 + 4 + 1.5
         res["default_gbs"] = bpp * w * h / (res["default_ms"] / 1e3) / 1e9
         out[f"{w}x{h}"] = res
         r.destroy()

@@ -637,10 +637,9 @@ static vt_status sensor_impl(vt_ctx* ctx, uint32_t camera, const vt_sensor_unifo
   if (!C.isp_mem) {
     const size_t px = size_t(W) * H;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const size_t b4 = al(px * 16), bl = al(std::max<size_t>(lev, 1) * 16), b1 = al(px * 4), bo = al(px * 4),
-                 by = al(px + 2 * size_t((W + 1) / 2) * ((H + 1) / 2)), bs = 256,
-                 bp = al(size_t((W + 31) / 32) * ((H + 7) / 8) * 12 + 12);
-    if (cudaMalloc(&C.isp_mem, 2 * b4 + 2 * bl + b1 + bo + by + bs + bp) != cudaSuccess) {
+    const size_t b4 = al(px * 16), bl = al(std::max<size_t>(lev, 1) * 16), bo = al(px * 4),
+                 by = al(px + 2 * size_t((W + 1) / 2) * ((H + 1) / 2)), bs = 256;
+    if (cudaMalloc(&C.isp_mem, 2 * b4 + 2 * bl + bo + by + bs) != cudaSuccess) {
       cudaGetLastError();
       C.isp_mem = nullptr;
       return fail(ctx, VT_ERR_OOM, "sensor chain buffers");
@@ -650,11 +649,9 @@ static vt_status sensor_impl(vt_ctx* ctx, uint32_t camera, const vt_sensor_unifo
     C.isp.B = reinterpret_cast<float4*>(p); p += b4;
     C.isp.GA = reinterpret_cast<float4*>(p); p += bl;
     C.isp.GB = reinterpret_cast<float4*>(p); p += bl;
-    C.isp.gpl = reinterpret_cast<float*>(p); p += b1;
     C.isp.out = reinterpret_cast<uchar4*>(p); p += bo;
     C.isp.yuv = reinterpret_cast<uint8_t*>(p); p += by;
-    C.isp.stats = reinterpret_cast<uint32_t*>(p); p += bs;
-    C.isp.part = reinterpret_cast<uint32_t*>(p);
+    C.isp.stats = reinterpret_cast<uint32_t*>(p);
     C.isp_lev = std::max<size_t>(lev, 1);
   }
   C.isp.L = C.radiance;
@@ -663,12 +660,12 @@ static vt_status sensor_impl(vt_ctx* ctx, uint32_t camera, const vt_sensor_unifo
   vtk::SensorParams sp;
   std::memcpy(sp.w, su->words, sizeof(sp.w));
   VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  vtk::launch_isp(sp, C.isp, ctx->stream);
+  const int isp_launches = vtk::launch_isp(sp, C.isp, ctx->stream);
   VT_CK(cudaGetLastError());
   VT_CK(cudaEventRecord(ctx->ev1, ctx->stream));
   if (!sync) {
     if (stats) VT_CK(cudaMemcpyAsync(stats, C.isp.stats, 16, cudaMemcpyDeviceToHost, ctx->stream));
-    ctx->tim.launches += 8;
+    ctx->tim.launches += isp_launches;
     C.exposed = C.processed = true;
     return VT_OK;
   }
@@ -679,7 +676,7 @@ static vt_status sensor_impl(vt_ctx* ctx, uint32_t camera, const vt_sensor_unifo
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   ctx->tim.sensor_ms = ms;
-  ctx->tim.launches += 8;
+  ctx->tim.launches += isp_launches;
   C.exposed = C.processed = true;
   return VT_OK;
 }

@@ -339,9 +339,11 @@ __device__ __forceinline__ void inst_pose(const Scene& S, uint32_t i, float time
 // ------------------------------------------------------------------------------------------------ traversal
 struct Hit { float t, u, v; uint32_t tri, inst; };
 
+// sign(d) / max(|d|, 1e-20) per component: the correctly rounded reciprocal of the positive denominator with d's sign,
+// the same value as the IEEE quotient and fewer instructions
 __device__ __forceinline__ float3 safe_inv(float3 d) {
-  return f3(copysignf(1.0f, d.x) / fmaxf(fabsf(d.x), 1e-20f), copysignf(1.0f, d.y) / fmaxf(fabsf(d.y), 1e-20f),
-            copysignf(1.0f, d.z) / fmaxf(fabsf(d.z), 1e-20f));
+  return f3(copysignf(__frcp_rn(fmaxf(fabsf(d.x), 1e-20f)), d.x), copysignf(__frcp_rn(fmaxf(fabsf(d.y), 1e-20f)), d.y),
+            copysignf(__frcp_rn(fmaxf(fabsf(d.z), 1e-20f)), d.z));
 }
 // entry distance of the ray into [lo, hi] within [tmin, tmax], BIG when missed (gpu/wgsl/trace.wgsl.js:178)
 __device__ __forceinline__ float slab(float3 lo, float3 hi, float3 o, float3 inv, float tmin, float tmax) {
@@ -349,6 +351,22 @@ __device__ __forceinline__ float slab(float3 lo, float3 hi, float3 o, float3 inv
   const float a = fmaxf(fmaxf(fminf(t0.x, t1.x), fminf(t0.y, t1.y)), fmaxf(fminf(t0.z, t1.z), tmin));
   const float b = fminf(fminf(fmaxf(t0.x, t1.x), fmaxf(t0.y, t1.y)), fminf(fmaxf(t0.z, t1.z), tmax));
   return a <= b ? a : BIG;
+}
+// slab() of a node's two children at once (boxes [a0, a1] and [a2, a3]): each axis's plane distances of both boxes as
+// a pair of float32 lanes, every element rounded as slab()'s own subtraction and product (x - y is x + (-y) exactly)
+__device__ __forceinline__ void slab_pair(float4 a0, float4 a1, float4 a2, float4 a3, float3 o, float3 inv, float tmin, float tmax,
+                                          float& t0, float& t1) {
+  const float2 ox = make_float2(-o.x, -o.x), oy = make_float2(-o.y, -o.y), oz = make_float2(-o.z, -o.z);
+  const float2 ix = make_float2(inv.x, inv.x), iy = make_float2(inv.y, inv.y), iz = make_float2(inv.z, inv.z);
+  const float2 lx = __fmul2_rn(__fadd2_rn(make_float2(a0.x, a2.x), ox), ix), hx = __fmul2_rn(__fadd2_rn(make_float2(a1.x, a3.x), ox), ix);
+  const float2 ly = __fmul2_rn(__fadd2_rn(make_float2(a0.y, a2.y), oy), iy), hy = __fmul2_rn(__fadd2_rn(make_float2(a1.y, a3.y), oy), iy);
+  const float2 lz = __fmul2_rn(__fadd2_rn(make_float2(a0.z, a2.z), oz), iz), hz = __fmul2_rn(__fadd2_rn(make_float2(a1.z, a3.z), oz), iz);
+  const float e0 = fmaxf(fmaxf(fminf(lx.x, hx.x), fminf(ly.x, hy.x)), fmaxf(fminf(lz.x, hz.x), tmin));
+  const float f0 = fminf(fminf(fmaxf(lx.x, hx.x), fmaxf(ly.x, hy.x)), fminf(fmaxf(lz.x, hz.x), tmax));
+  const float e1 = fmaxf(fmaxf(fminf(lx.y, hx.y), fminf(ly.y, hy.y)), fmaxf(fminf(lz.y, hz.y), tmin));
+  const float f1 = fminf(fminf(fmaxf(lx.y, hx.y), fmaxf(ly.y, hy.y)), fminf(fmaxf(lz.y, hz.y), tmax));
+  t0 = e0 <= f0 ? e0 : BIG;
+  t1 = e1 <= f1 ? e1 : BIG;
 }
 // Moller-Trumbore on the packed record (gpu/wgsl/trace.wgsl.js:195)
 __device__ __forceinline__ bool tri_hit(const Scene& S, uint32_t k, float3 o, float3 d, float tmin, float tmax, float& t, float& u, float& v) {
@@ -475,6 +493,11 @@ struct TraceState {
   Hit best;
   uint32_t node, sp, visits;
   int k;                // current phase: -1 the static BVH, k >= 0 posed body k
+  // trace_step's node in progress: its children's entry distances (BIG once a leaf child is taken) and records (the
+  // triangle counts clamped to 16 bits: child 0's low, child 1's high), and the leaf being tested
+  float t0, t1;
+  uint32_t r0, r1, c01;
+  uint32_t lk, lend;    // triangles lk .. lend - 1 of the leaf are left (lk == lend: the next step visits st.node)
 };
 
 // set up the first phase at or after `from` that has something to traverse; false when none is left
@@ -484,15 +507,19 @@ __device__ __forceinline__ bool trace_phase(const Scene& S, uint32_t root, float
   if (k < 0) {
     if (mask & 1u) {
       st.k = -1; st.ol = o; st.dl = d; st.inv = safe_inv(d); st.node = root; st.sp = 0; st.visits = 0;
+      st.lk = st.lend = 0;
       return true;
     }
     k = 0;
   }
   const int n_inst = (mask & 2u) ? int(min(ldu(S.su + 16), uint32_t(VT_MAX_INST))) : 0;
-  const float3 winv = safe_inv(d);
+  // the world-frame inverse direction, once a body gets past its flags (a ray's last phase usually meets none)
+  float3 winv;
+  bool have_inv = false;
   for (; k < n_inst; k++) {
     const float* I = inst_rec(S, uint32_t(k));
     if ((ldu(I + 15) & 2u) || ((skip >> k) & 1u)) continue;
+    if (!have_inv) { winv = safe_inv(d); have_inv = true; }
     if (slab(ld3(I + 16), ld3(I + 20), o, winv, tmin, st.best.t) >= st.best.t) continue;
     if (!seg_near_capsule(o, d, tmin, fminf(st.best.t, 1e3f), ld3(I + 32), ld3(I + 36), __ldg(I + 35))) continue;
     Rot R;
@@ -504,6 +531,7 @@ __device__ __forceinline__ bool trace_phase(const Scene& S, uint32_t root, float
     st.node = ldu(I + 11);
     st.sp = 0;
     st.visits = 0;
+    st.lk = st.lend = 0;
     st.k = k;
     return true;
   }
@@ -576,6 +604,92 @@ __device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceStat
   t1 = t1 < st.best.t ? t1 : BIG;
   // staged records were checked for increasing child indices when the set was built
   if (!staged && ((t0 < BIG && c0 == 0u && r0 <= node) || (t1 < BIG && c1 == 0u && r1 <= node))) { atomicAdd(S.dbg + DBG_CORRUPT, 1u); return 1; }
+  const bool go0 = t0 < BIG, go1 = t1 < BIG;
+  if (go0 && go1) {
+    if (t1 < t0) { stk.set(st.sp, r0, t0); st.node = r1; }
+    else { stk.set(st.sp, r1, t1); st.node = r0; }
+    st.sp = min(st.sp + 1u, STACK - 1u);
+  } else if (go0) {
+    st.node = r0;
+  } else if (go1) {
+    st.node = r1;
+  } else {
+    while (st.sp > 0u) {
+      st.sp--;
+      const uint2 e = stk.get(st.sp);
+      if (__uint_as_float(e.y) < st.best.t) { st.node = e.x; return 0; }
+    }
+    return 1;
+  }
+  return 0;
+}
+
+// trace_visit's operations, one unit per step: a step either visits a node (the child boxes, and the first leaf child
+// to test) or tests one triangle of that leaf. The node's children stay in the state until its leaves are done; then
+// the same step takes the next node from its interior children or the stack. Per ray the sequence of operations is
+// trace_visit's (child 0's leaf in triangle order, child 1's leaf only if its box is still nearer than the best hit,
+// then the push / pop with the updated best), so are the hits; a warp's lanes no longer wait for the longest leaf loop
+// among them. 0 continue, 1 the phase is finished, 2 an any-hit query found its hit.
+// the leaf of child c, when its box is nearer than the best hit: its triangles become the ones left, and the child's
+// distance BIG (trace_visit drops a tested leaf child from the push / pop the same way, after its loop)
+__device__ __forceinline__ bool leaf_enter(const Scene& S, TraceState& st, uint32_t c) {
+  const float tc = c == 0u ? st.t0 : st.t1;
+  const uint32_t cnt = (st.c01 >> (16u * c)) & 0xffffu, ref = c == 0u ? st.r0 : st.r1;
+  if (!(tc < st.best.t && cnt > 0u)) return false;
+  if (cnt > MAX_LEAF) atomicAdd(S.dbg + DBG_LEAF, 1u);
+  st.lk = ref;
+  st.lend = ref + min(cnt, MAX_LEAF);
+  if (c == 0u) st.t0 = BIG; else st.t1 = BIG;
+  return true;
+}
+
+template <bool ANY>
+__device__ __forceinline__ int trace_step(const Scene& S, float tmin, TraceState& st, LaneStack& stk) {
+  bool more;
+  if (st.lk == st.lend) {
+    if (++st.visits > MAX_VISITS) { atomicAdd(S.dbg + DBG_VISITS, 1u); return 1; }
+    const uint32_t node = st.node;
+#if VT_TOP_NODES
+    float4 a0, a1, a2, a3;
+    if ((node & TOP_BIT) != 0u) {
+      const float4* nb = stk.top + 4u * (node & 0xffffu);
+      a0 = nb[0]; a1 = nb[1]; a2 = nb[2]; a3 = nb[3];
+    } else {
+      const float4* nb = S.nodes + 4u * node;
+      a0 = __ldg(nb); a1 = __ldg(nb + 1); a2 = __ldg(nb + 2); a3 = __ldg(nb + 3);
+    }
+#else
+    const float4* nb = S.nodes + 4u * node;
+    const float4 a0 = __ldg(nb), a1 = __ldg(nb + 1), a2 = __ldg(nb + 2), a3 = __ldg(nb + 3);
+#endif
+    slab_pair(a0, a1, a2, a3, st.ol, st.inv, tmin, st.best.t, st.t0, st.t1);
+    st.c01 = min(fu(a1.w), 0xffffu) | (min(fu(a3.w), 0xffffu) << 16);
+    st.r0 = fu(a0.w); st.r1 = fu(a2.w);
+    more = leaf_enter(S, st, 0u) || leaf_enter(S, st, 1u);
+  } else {
+    const uint32_t k = st.lk++;
+    float t, u, v;
+    if (tri_hit(S, k, st.ol, st.dl, tmin, st.best.t, t, u, v)) {
+      st.best.t = t; st.best.u = u; st.best.v = v; st.best.tri = k; st.best.inst = st.k < 0 ? MISS : uint32_t(st.k);
+      if (ANY) return 2;
+    }
+    // the leaf done: child 1's leaf next (when that was child 0's and child 1's box is still nearer)
+    more = st.lk != st.lend || leaf_enter(S, st, 1u);
+  }
+  if (more) return 0;
+  const uint32_t node = st.node;
+#if VT_TOP_NODES
+  const bool staged = (node & TOP_BIT) != 0u;
+#else
+  constexpr bool staged = false;
+#endif
+  const float t0 = st.t0 < st.best.t ? st.t0 : BIG;
+  const float t1 = st.t1 < st.best.t ? st.t1 : BIG;
+  const uint32_t r0 = st.r0, r1 = st.r1;
+  if (!staged && ((t0 < BIG && (st.c01 & 0xffffu) == 0u && r0 <= node) || (t1 < BIG && (st.c01 >> 16) == 0u && r1 <= node))) {
+    atomicAdd(S.dbg + DBG_CORRUPT, 1u);
+    return 1;
+  }
   const bool go0 = t0 < BIG, go1 = t1 < BIG;
   if (go0 && go1) {
     if (t1 < t0) { stk.set(st.sp, r0, t0); st.node = r1; }

@@ -1,14 +1,19 @@
-// The camera sensor chain after the path tracer, radiance -> raw DN -> 8-bit RGB and YCbCr (gpu/wgsl/sensor.wgsl.js):
-//   isp_optics       E = L (pi T / 4 N^2) RI, the horizontal half of the optics blur (pixel-integrated Gaussian)
-//   glare_down/blur  veiling glare on a 1/F level: box mean, then a Gaussian over whole rows and columns (zero outside)
-//   isp_expose       the vertical half of the blur, the glare mix E' = (1 - k) E + k G, the sensor model (vt_sensor.cuh)
-//   demosaic_g       green plane: bilinear, edge-aware (OpenCV EA) or Hamilton-Adams
-//   demosaic_rb      red and blue (colour differences or bilinear), black level, white-balance statistics, WB, CCM
-//   isp_nr           3x3 bilateral on linear RGB, range sigma from the modelled shot + read noise
-//   isp_output       tone curve, unsharp mask on luma, BT.601 full-range YCbCr, 4:2:0 chroma, 8-bit RGB, luma sum
-// Each stage is one pass over the frame (a 1920x1200 frame is 2.3 M pixels: every pass is HBM/L2-bound at a few
-// microseconds); the statistics are integer sums of per-block partials added by one small kernel, so they do not
-// depend on scheduling.
+// The camera sensor chain after the path tracer, radiance -> raw DN -> 8-bit RGB and YCbCr (gpu/wgsl/sensor.wgsl.js),
+// in three fused passes over the frame (plus three small ones on the glare level when veiling glare is on):
+//   glare_down/blur   veiling glare on a 1/F level: box mean, then a Gaussian over whole rows and columns (zero outside)
+//   isp_expose        E = L (pi T / 4 N^2) RI with the pixel-integrated Gaussian optics blur (the horizontal half into
+//                     shared rows with the vertical half's halo, then the vertical half), the glare mix
+//                     E' = (1 - k) E + k G and the sensor model (vt_sensor.cuh): raw DN
+//   isp_demosaic      a raw tile with a 3-pixel halo in shared memory; the green plane (bilinear, edge-aware or
+//                     Hamilton-Adams) on the tile and a 1-pixel ring; red and blue (colour differences or bilinear),
+//                     black level, white-balance statistics, WB, CCM
+//   isp_finish        3x3 bilateral noise reduction on linear RGB (range sigma from the modelled shot + read noise) and
+//                     the output stage on each 2x2 block: tone curve, BT.601 full-range YCbCr, 4:2:0 chroma, 8-bit RGB,
+//                     luma sum. With sharpening on (an unsharp mask over toned luma, radius up to 4) noise reduction
+//                     and output run as two passes (isp_nr, isp_output), since the mask reads the reduced image's
+//                     neighbours.
+// The statistics are integer sums: each block adds its partial with one atomic per word, exact in any order. The
+// exposure pass clears them.
 //
 // This translation unit is compiled without multiply-add contraction (--fmad=false) and uses the fixed-order
 // elementary functions of vt_sensor.cuh, so every value is the one the CPU restatement computes from the same
@@ -50,28 +55,21 @@ __device__ __forceinline__ void block_taps(float sg, int r, float* taps) {
   __syncthreads();
 }
 
-__global__ void isp_optics_kernel(const SensorParams P, const float4* __restrict__ L, const float* __restrict__ ri, float4* __restrict__ A) {
-  __shared__ float taps[25];
-  const Su su{P.w};
-  const int W = int(P.w[0]), H = int(P.w[1]);
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  const float sg = su.f(5);
-  const int r = gauss_taps(sg);
-  block_taps(sg, r, taps);
-  if (x >= W || y >= H) return;
-  float ax = 0.0f, ay = 0.0f, az = 0.0f, ws = 0.0f;
-  for (int k = -r; k <= r; k++) {
-    const int xx = clampi(x + k, 0, W - 1);
-    const float w = taps[k + r];
-    const float4 l = __ldg(L + size_t(y) * W + xx);
-    const float m = __ldg(ri + size_t(y) * W + xx);
-    ax = ax + w * l.x * m;
-    ay = ay + w * l.y * m;
-    az = az + w * l.z * m;
-    ws = ws + w;
+// a block's sums of v[0..n-1] added to stats[0..n-1] with one atomic each (integer: exact in any order)
+__device__ __forceinline__ void block_add(const uint32_t* v, int n, uint32_t* stats) {
+  __shared__ uint32_t sm[8][3];
+  const int t = threadIdx.y * blockDim.x + threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t a[3] = {v[0], n > 1 ? v[1] : 0u, n > 2 ? v[2] : 0u};
+  for (int k = 0; k < n; k++)
+    for (int s = 16; s > 0; s >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], s);
+  if (lane == 0)
+    for (int k = 0; k < n; k++) sm[warp][k] = a[k];
+  __syncthreads();
+  if (t < n) {
+    uint32_t s = 0;
+    for (int w = 0; w < int(blockDim.x * blockDim.y) / 32; w++) s += sm[w][t];
+    if (s) atomicAdd(stats + t, s);
   }
-  const float s = su.f(4) / ws;
-  A[size_t(y) * W + x] = make_float4(ax * s, ay * s, az * s, 1.0f);
 }
 
 __global__ void glare_down_kernel(const SensorParams P, const float4* __restrict__ L, const float* __restrict__ ri, float4* __restrict__ G) {
@@ -134,34 +132,70 @@ __device__ __forceinline__ float3 glare_at(const Su& su, const float4* __restric
                      mix(mix(a.z, b.z, fx), mix(c.z, d.z, fx), fy));
 }
 
-__global__ void isp_expose_kernel(const SensorParams P, const float4* __restrict__ A, const float4* __restrict__ G, float* __restrict__ raw) {
+// output rows per block of the exposure pass (32 x 8 threads, three rows each) and the shared rows it needs with the
+// vertical blur's halo (at most 12 taps each side)
+constexpr int EX_TY = 24;
+constexpr int EX_ROWS = EX_TY + 24;
+
+__global__ void __launch_bounds__(256) isp_expose_kernel(const SensorParams P, const float4* __restrict__ L, const float* __restrict__ ri,
+                                                         const float4* __restrict__ G, float* __restrict__ raw, uint32_t* __restrict__ stats) {
   __shared__ float taps[25];
+  __shared__ float hx[EX_ROWS][32], hy[EX_ROWS][32], hz[EX_ROWS][32];
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x = blockIdx.x * 32 + tx, y0 = blockIdx.y * EX_TY;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && ty == 0 && tx < 4) stats[tx] = 0u;
   const float sg = su.f(5);
   const int r = gauss_taps(sg);
   block_taps(sg, r, taps);
-  if (x >= W || y >= H) return;
-  float ex = 0.0f, ey = 0.0f, ez = 0.0f, ws = 0.0f;
-  for (int k = -r; k <= r; k++) {
-    const int yy = clampi(y + k, 0, H - 1);
-    const float w = taps[k + r];
-    const float4 e = A[size_t(yy) * W + x];
-    ex = ex + w * e.x;
-    ey = ey + w * e.y;
-    ez = ez + w * e.z;
-    ws = ws + w;
+  // the horizontal half on shared row j = image row clamp(y0 - r + j): the vertical half's tap k of output row y0 + i
+  // is row i + k + r, the clamped row y0 + i + k as the separable blur has it
+  const int rows = min(EX_TY, H - y0) + 2 * r;
+  if (x < W) {
+    for (int j = ty; j < rows; j += 8) {
+      const int yy = clampi(y0 - r + j, 0, H - 1);
+      float ax = 0.0f, ay = 0.0f, az = 0.0f, ws = 0.0f;
+      for (int k = -r; k <= r; k++) {
+        const int xx = clampi(x + k, 0, W - 1);
+        const float w = taps[k + r];
+        const float4 l = __ldg(L + size_t(yy) * W + xx);
+        const float m = __ldg(ri + size_t(yy) * W + xx);
+        ax = ax + w * l.x * m;
+        ay = ay + w * l.y * m;
+        az = az + w * l.z * m;
+        ws = ws + w;
+      }
+      const float s = su.f(4) / ws;
+      hx[j][tx] = ax * s;
+      hy[j][tx] = ay * s;
+      hz[j][tx] = az * s;
+    }
   }
-  ex = ex / ws; ey = ey / ws; ez = ez / ws;
-  const float k = su.f(52);
-  if (k > 0.0f) {
-    const float3 g = glare_at(su, G, x, y, W, H);
-    ex = (1.0f - k) * ex + k * g.x;
-    ey = (1.0f - k) * ey + k * g.y;
-    ez = (1.0f - k) * ez + k * g.z;
+  __syncthreads();
+  if (x >= W) return;
+  const float kg = su.f(52);
+  for (int i = ty; i < EX_TY; i += 8) {
+    const int y = y0 + i;
+    if (y >= H) break;
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f, ws = 0.0f;
+    for (int k = -r; k <= r; k++) {
+      const float w = taps[k + r];
+      const int j = i + k + r;
+      ex = ex + w * hx[j][tx];
+      ey = ey + w * hy[j][tx];
+      ez = ez + w * hz[j][tx];
+      ws = ws + w;
+    }
+    ex = ex / ws; ey = ey / ws; ez = ez / ws;
+    if (kg > 0.0f) {
+      const float3 g = glare_at(su, G, x, y, W, H);
+      ex = (1.0f - kg) * ex + kg * g.x;
+      ey = (1.0f - kg) * ey + kg * g.y;
+      ez = (1.0f - kg) * ez + kg * g.z;
+    }
+    raw[size_t(y) * W + x] = sensor_dn(P.w, ex, ey, ez, x, y, W, P.w[3]);
   }
-  raw[size_t(y) * W + x] = sensor_dn(P.w, ex, ey, ez, x, y, W, P.w[3]);
 }
 
 // raw DN mirrored at the borders (reflect by one, which keeps the CFA phase), then clamped
@@ -173,16 +207,13 @@ __device__ __forceinline__ float raw_at(const float* __restrict__ raw, int x, in
   return raw[size_t(clampi(y, 0, H - 1)) * W + clampi(x, 0, W - 1)];
 }
 
-__global__ void demosaic_g_kernel(const SensorParams P, const float* __restrict__ raw, float* __restrict__ gpl) {
-  const Su su{P.w};
-  const int W = int(P.w[0]), H = int(P.w[1]);
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
-  float g = raw_at(raw, x, y, W, H);
-  if (cfa_channel(P.w[2], uint32_t(x), uint32_t(y)) != 1u) {
-    const float gl = raw_at(raw, x - 1, y, W, H), gr = raw_at(raw, x + 1, y, W, H);
-    const float gu = raw_at(raw, x, y - 1, W, H), gd = raw_at(raw, x, y + 1, W, H);
-    const uint32_t mode = P.w[50];
+// the green value at (x, y) of the image, with rw(xx, yy) = raw_at(raw, xx, yy) for |xx - x|, |yy - y| <= 2
+template <class Raw>
+__device__ __forceinline__ float green_at(const Su& su, uint32_t code, uint32_t mode, Raw&& rw, int x, int y) {
+  float g = rw(x, y);
+  if (cfa_channel(code, uint32_t(x), uint32_t(y)) != 1u) {
+    const float gl = rw(x - 1, y), gr = rw(x + 1, y);
+    const float gu = rw(x, y - 1), gd = rw(x, y + 1);
     if (mode == 0) {
       g = 0.25f * (gl + gr + gu + gd);
     } else if (mode == 1) {
@@ -190,44 +221,44 @@ __global__ void demosaic_g_kernel(const SensorParams P, const float* __restrict_
       g = dh < dv ? 0.5f * (gl + gr) : dv < dh ? 0.5f * (gu + gd) : 0.25f * (gl + gr + gu + gd);
     } else {
       const float c = g;
-      const float lh = 2.0f * c - raw_at(raw, x - 2, y, W, H) - raw_at(raw, x + 2, y, W, H);
-      const float lv = 2.0f * c - raw_at(raw, x, y - 2, W, H) - raw_at(raw, x, y + 2, W, H);
+      const float lh = 2.0f * c - rw(x - 2, y) - rw(x + 2, y);
+      const float lv = 2.0f * c - rw(x, y - 2) - rw(x, y + 2);
       const float dh = fabsf(gl - gr) + fabsf(lh), dv = fabsf(gu - gd) + fabsf(lv);
       const float gh = 0.5f * (gl + gr) + 0.25f * lh, gv = 0.5f * (gu + gd) + 0.25f * lv;
       g = dh < dv ? gh : dv < dh ? gv : 0.5f * (gh + gv);
       g = fminf(fmaxf(g, 0.0f), su.f(24));
     }
   }
-  gpl[size_t(y) * W + x] = g;
+  return g;
 }
 
-// a block's sums of v[0..2] (256 threads) written to out[0..2]
-__device__ __forceinline__ void block_sum3(const uint32_t v[3], uint32_t* out) {
-  __shared__ uint32_t sm[8][3];
-  const int t = threadIdx.y * blockDim.x + threadIdx.x, lane = t & 31, warp = t >> 5;
-  uint32_t a[3] = {v[0], v[1], v[2]};
-  for (int k = 0; k < 3; k++)
-    for (int s = 16; s > 0; s >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], s);
-  if (lane == 0)
-    for (int k = 0; k < 3; k++) sm[warp][k] = a[k];
-  __syncthreads();
-  if (t < 3) {
-    uint32_t s = 0;
-    for (int w = 0; w < int(blockDim.x * blockDim.y) / 32; w++) s += sm[w][t];
-    out[t] = s;
-  }
-}
+// output rows per block of the demosaic pass (32 x 8 threads, two rows each)
+constexpr int DM_TY = 16;
 
-__global__ void __launch_bounds__(256) demosaic_rb_kernel(const SensorParams P, const float* __restrict__ raw, const float* __restrict__ gpl,
-                                                          float4* __restrict__ B, uint32_t* __restrict__ part) {
+__global__ void __launch_bounds__(256) isp_demosaic_kernel(const SensorParams P, const float* __restrict__ raw, float4* __restrict__ B,
+                                                           uint32_t* __restrict__ stats) {
+  // rs[j][i] = raw_at(x0 - 3 + i, y0 - 3 + j); gs[j][i] = the green plane at the image pixel clamp(x0 - 1 + i, y0 - 1 + j)
+  __shared__ float rs[DM_TY + 6][38];
+  __shared__ float gs[DM_TY + 2][34];
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * DM_TY;
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  for (int e = t; e < (DM_TY + 6) * 38; e += 256) rs[e / 38][e % 38] = raw_at(raw, x0 - 3 + e % 38, y0 - 3 + e / 38, W, H);
+  __syncthreads();
+  const uint32_t code = P.w[2], mode = P.w[50];
+  auto rw = [&](int xx, int yy) { return rs[yy - y0 + 3][xx - x0 + 3]; };
+  for (int e = t; e < (DM_TY + 2) * 34; e += 256) {
+    const int px = clampi(x0 - 1 + e % 34, 0, W - 1), py = clampi(y0 - 1 + e / 34, 0, H - 1);
+    gs[e / 34][e % 34] = green_at(su, code, mode, rw, px, py);
+  }
+  __syncthreads();
+  auto g_at = [&](int xx, int yy) { return gs[yy - y0 + 1][xx - x0 + 1]; };
   uint32_t q[3] = {0u, 0u, 0u};
-  if (x < W && y < H) {
-    const uint32_t code = P.w[2], mode = P.w[50];
+  for (int rr = 0; rr < DM_TY / 8; rr++) {
+    const int x = x0 + int(threadIdx.x), y = y0 + int(threadIdx.y) + 8 * rr;
+    if (x >= W || y >= H) continue;
     const uint32_t own = cfa_channel(code, uint32_t(x), uint32_t(y));
-    auto g_at = [&](int xx, int yy) { return gpl[size_t(clampi(yy, 0, H - 1)) * W + clampi(xx, 0, W - 1)]; };
     const float g = g_at(x, y);
     float sr = 0.0f, sb = 0.0f, cr = 0.0f, cb = 0.0f;
     for (int dy = -1; dy <= 1; dy++)
@@ -236,7 +267,7 @@ __global__ void __launch_bounds__(256) demosaic_rb_kernel(const SensorParams P, 
         const uint32_t ch = cfa_channel(code, uint32_t(xx), uint32_t(yy));
         if (ch == 1u) continue;
         if (ch == own && !(dx == 0 && dy == 0)) continue;
-        const float d = raw_at(raw, xx, yy, W, H) - g_at(xx, yy);
+        const float d = rw(xx, yy) - g_at(xx, yy);
         if (ch == 0u) { sr = sr + d; cr = cr + 1.0f; } else { sb = sb + d; cb = cb + 1.0f; }
       }
     float r = g + sr / fmaxf(cr, 1.0f), gg = g, b = g + sb / fmaxf(cb, 1.0f);
@@ -248,7 +279,7 @@ __global__ void __launch_bounds__(256) demosaic_rb_kernel(const SensorParams P, 
           const uint32_t ch = cfa_channel(code, uint32_t(xx), uint32_t(yy));
           if (ch == own && !(dx == 0 && dy == 0)) continue;
           if (ch == 1u && own == 1u && !(dx == 0 && dy == 0)) continue;
-          const float v = raw_at(raw, xx, yy, W, H);
+          const float v = rw(xx, yy);
           if (ch == 0u) { s0 = s0 + v; c0 = c0 + 1.0f; } else if (ch == 1u) { s1 = s1 + v; c1 = c1 + 1.0f; } else { s2 = s2 + v; c2 = c2 + 1.0f; }
         }
       r = s0 / fmaxf(c0, 1.0f);
@@ -258,23 +289,21 @@ __global__ void __launch_bounds__(256) demosaic_rb_kernel(const SensorParams P, 
     }
     const float black = su.f(25), full = fmaxf(su.f(24) - black, 1.0f);
     float c[3] = {(r - black) / full, (gg - black) / full, (b - black) / full};
-    for (int k = 0; k < 3; k++) q[k] = uint32_t(rintf(clamp01(c[k]) * 1023.0f));
+    for (int k = 0; k < 3; k++) q[k] += uint32_t(rintf(clamp01(c[k]) * 1023.0f));
     for (int k = 0; k < 3; k++) c[k] = c[k] * su.f(28 + k);
     float o[3];
     for (int k = 0; k < 3; k++) o[k] = su.f(32 + 4 * k) * c[0] + su.f(33 + 4 * k) * c[1] + su.f(34 + 4 * k) * c[2];
     B[size_t(y) * W + x] = make_float4(o[0], o[1], o[2], 1.0f);
   }
-  // white-balance statistics: integer sums per block into this block's partial (added up by isp_stats_kernel)
-  block_sum3(q, part + 3 * size_t(blockIdx.y * gridDim.x + blockIdx.x));
+  // white-balance statistics R, G, B
+  block_add(q, 3, stats + 1);
 }
 
-__global__ void isp_nr_kernel(const SensorParams P, const float4* __restrict__ B, float4* __restrict__ A) {
-  const Su su{P.w};
-  const int W = int(P.w[0]), H = int(P.w[1]);
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
-  const float4 c0 = B[size_t(y) * W + x];
-  if (P.w[51] == 0u || su.f(58) <= 0.0f) { A[size_t(y) * W + x] = c0; return; }
+// the noise-reduced pixel (x, y) of the image, with b(xx, yy) = the demosaiced pixel at the clamped (xx, yy)
+template <class Fetch>
+__device__ __forceinline__ float4 nr_pixel(const Su& su, const uint32_t* w, Fetch&& b, int x, int y) {
+  const float4 c0 = b(x, y);
+  if (w[51] == 0u || su.f(58) <= 0.0f) return c0;
   const float Y0 = fmaxf(c0.x * 0.2126f + c0.y * 0.7152f + c0.z * 0.0722f, 0.0f);
   const float fullE = fmaxf(su.f(24) - su.f(25), 1.0f) / fmaxf(su.f(23) * su.f(7), 1e-9f);
   const float sn = sqrtf(Y0 * fullE + su.f(20) * su.f(20)) / fullE;
@@ -282,15 +311,24 @@ __global__ void isp_nr_kernel(const SensorParams P, const float4* __restrict__ B
   float ax = 0.0f, ay = 0.0f, az = 0.0f, ws = 0.0f;
   for (int dy = -1; dy <= 1; dy++)
     for (int dx = -1; dx <= 1; dx++) {
-      const float4 c = B[size_t(clampi(y + dy, 0, H - 1)) * W + clampi(x + dx, 0, W - 1)];
+      const float4 c = b(x + dx, y + dy);
       const float dY = (c.x - c0.x) * 0.2126f + (c.y - c0.y) * 0.7152f + (c.z - c0.z) * 0.0722f;
-      const float w = vt_expf(-0.5f * float(dx * dx + dy * dy) / (ss * ss) - 0.5f * dY * dY / (rs * rs));
-      ax = ax + w * c.x;
-      ay = ay + w * c.y;
-      az = az + w * c.z;
-      ws = ws + w;
+      const float wt = vt_expf(-0.5f * float(dx * dx + dy * dy) / (ss * ss) - 0.5f * dY * dY / (rs * rs));
+      ax = ax + wt * c.x;
+      ay = ay + wt * c.y;
+      az = az + wt * c.z;
+      ws = ws + wt;
     }
-  A[size_t(y) * W + x] = make_float4(ax / ws, ay / ws, az / ws, 1.0f);
+  return make_float4(ax / ws, ay / ws, az / ws, 1.0f);
+}
+
+__global__ void isp_nr_kernel(const SensorParams P, const float4* __restrict__ B, float4* __restrict__ A) {
+  const Su su{P.w};
+  const int W = int(P.w[0]), H = int(P.w[1]);
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  auto b = [&](int xx, int yy) { return B[size_t(clampi(yy, 0, H - 1)) * W + clampi(xx, 0, W - 1)]; };
+  A[size_t(y) * W + x] = nr_pixel(su, P.w, b, x, y);
 }
 
 __device__ __forceinline__ float srgb_oetf(float v) { return v <= 0.0031308f ? 12.92f * v : 1.055f * vt_powf(v, 0.41666666666666669f) - 0.055f; }
@@ -309,90 +347,104 @@ __device__ __forceinline__ float tone_c(const Su& su, float x) {
   if (m < 1.5f) return vt_powf(c, 1.0f / fmaxf(su.f(45), 1e-3f));
   return c;
 }
-__device__ __forceinline__ float3 toned(const Su& su, const float4* __restrict__ A, int x, int y, int W, int H) {
-  const float4 c = A[size_t(clampi(y, 0, H - 1)) * W + clampi(x, 0, W - 1)];
+__device__ __forceinline__ float3 toned(const Su& su, float4 c) {
   return make_float3(tone_c(su, c.x), tone_c(su, c.y), tone_c(su, c.z));
 }
 __device__ __forceinline__ float luma601(float3 c) { return c.x * 0.299f + c.y * 0.587f + c.z * 0.114f; }
 
-// one thread per 2x2 block
-__global__ void __launch_bounds__(256) isp_output_kernel(const SensorParams P, const float4* __restrict__ A, uchar4* __restrict__ out,
-                                                         uint8_t* __restrict__ yuv, uint32_t* __restrict__ part) {
-  const Su su{P.w};
-  const int W = int(P.w[0]), H = int(P.w[1]);
-  const int gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y * blockDim.y + threadIdx.y;
+// the output stage of the 2x2 block (gx, gy): at(x, y) = the linear pixel at the clamped (x, y) (read at the block's
+// pixels, and with SHARPEN at their neighbours within the mask's radius); returns the block's luma sum
+template <bool SHARPEN, class Fetch>
+__device__ __forceinline__ uint32_t output_block(const Su& su, const uint32_t* w, Fetch&& at, int gx, int gy, int W, int H,
+                                                 uchar4* __restrict__ out, uint8_t* __restrict__ yuv) {
   const int bx = gx * 2, by = gy * 2;
   uint32_t lsum = 0;
-  if (bx < W && by < H) {
-    float Ys[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    float cb = 0.0f, cr = 0.0f, nb = 0.0f;
-    const float amt = su.f(46);
-    const int rad = clampi(int(rintf(su.f(47))), 1, 4);
-    const bool c420 = P.w[48] != 0u;
+  float Ys[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  float cb = 0.0f, cr = 0.0f, nb = 0.0f;
+  const bool c420 = w[48] != 0u;
+  for (int q = 0; q < 4; q++) {
+    const int x = bx + (q & 1), y = by + (q >> 1);
+    if (x >= W || y >= H) continue;
+    float3 c = toned(su, at(x, y));
+    if (SHARPEN) {
+      const float amt = su.f(46);
+      const int rad = clampi(int(rintf(su.f(47))), 1, 4);
+      float m = 0.0f, n = 0.0f;
+      for (int dy = -rad; dy <= rad; dy++)
+        for (int dx = -rad; dx <= rad; dx++) {
+          m = m + luma601(toned(su, at(x + dx, y + dy)));
+          n = n + 1.0f;
+        }
+      const float s = amt * (luma601(c) - m / n);
+      c = make_float3(c.x + s, c.y + s, c.z + s);
+    }
+    const float r8 = clamp01(c.x) * 255.0f, g8 = clamp01(c.y) * 255.0f, b8 = clamp01(c.z) * 255.0f;
+    Ys[q] = 0.299f * r8 + 0.587f * g8 + 0.114f * b8;
+    cb = cb + (128.0f - 0.168736f * r8 - 0.331264f * g8 + 0.5f * b8);
+    cr = cr + (128.0f + 0.5f * r8 - 0.418688f * g8 - 0.081312f * b8);
+    nb = nb + 1.0f;
+    if (!c420) {
+      const float y8 = fminf(fmaxf(rintf(Ys[q]), 0.0f), 255.0f);
+      out[size_t(y) * W + x] = make_uchar4(uint8_t(rintf(r8)), uint8_t(rintf(g8)), uint8_t(rintf(b8)), 255);
+      lsum += uint32_t(y8);
+    }
+  }
+  if (c420) {
+    const float Cb = fminf(fmaxf(rintf(cb / nb), 0.0f), 255.0f), Cr = fminf(fmaxf(rintf(cr / nb), 0.0f), 255.0f);
+    const int cw = (W + 1) / 2, chh = (H + 1) / 2;
     for (int q = 0; q < 4; q++) {
       const int x = bx + (q & 1), y = by + (q >> 1);
       if (x >= W || y >= H) continue;
-      float3 c = toned(su, A, x, y, W, H);
-      if (amt > 0.0f) {
-        float m = 0.0f, n = 0.0f;
-        for (int dy = -rad; dy <= rad; dy++)
-          for (int dx = -rad; dx <= rad; dx++) {
-            m = m + luma601(toned(su, A, x + dx, y + dy, W, H));
-            n = n + 1.0f;
-          }
-        const float s = amt * (luma601(c) - m / n);
-        c = make_float3(c.x + s, c.y + s, c.z + s);
-      }
-      const float r8 = clamp01(c.x) * 255.0f, g8 = clamp01(c.y) * 255.0f, b8 = clamp01(c.z) * 255.0f;
-      Ys[q] = 0.299f * r8 + 0.587f * g8 + 0.114f * b8;
-      cb = cb + (128.0f - 0.168736f * r8 - 0.331264f * g8 + 0.5f * b8);
-      cr = cr + (128.0f + 0.5f * r8 - 0.418688f * g8 - 0.081312f * b8);
-      nb = nb + 1.0f;
-      if (!c420) {
-        const float y8 = fminf(fmaxf(rintf(Ys[q]), 0.0f), 255.0f);
-        out[size_t(y) * W + x] = make_uchar4(uint8_t(rintf(r8)), uint8_t(rintf(g8)), uint8_t(rintf(b8)), 255);
-        lsum += uint32_t(y8);
-      }
+      const float y8 = fminf(fmaxf(rintf(Ys[q]), 0.0f), 255.0f);
+      const float r = y8 + 1.402f * (Cr - 128.0f);
+      const float g = y8 - 0.344136f * (Cb - 128.0f) - 0.714136f * (Cr - 128.0f);
+      const float b = y8 + 1.772f * (Cb - 128.0f);
+      out[size_t(y) * W + x] = make_uchar4(uint8_t(fminf(fmaxf(rintf(r), 0.0f), 255.0f)), uint8_t(fminf(fmaxf(rintf(g), 0.0f), 255.0f)),
+                                           uint8_t(fminf(fmaxf(rintf(b), 0.0f), 255.0f)), 255);
+      yuv[size_t(y) * W + x] = uint8_t(y8);
+      lsum += uint32_t(y8);
     }
-    if (c420) {
-      const float Cb = fminf(fmaxf(rintf(cb / nb), 0.0f), 255.0f), Cr = fminf(fmaxf(rintf(cr / nb), 0.0f), 255.0f);
-      const int cw = (W + 1) / 2, chh = (H + 1) / 2;
-      for (int q = 0; q < 4; q++) {
-        const int x = bx + (q & 1), y = by + (q >> 1);
-        if (x >= W || y >= H) continue;
-        const float y8 = fminf(fmaxf(rintf(Ys[q]), 0.0f), 255.0f);
-        const float r = y8 + 1.402f * (Cr - 128.0f);
-        const float g = y8 - 0.344136f * (Cb - 128.0f) - 0.714136f * (Cr - 128.0f);
-        const float b = y8 + 1.772f * (Cb - 128.0f);
-        out[size_t(y) * W + x] = make_uchar4(uint8_t(fminf(fmaxf(rintf(r), 0.0f), 255.0f)), uint8_t(fminf(fmaxf(rintf(g), 0.0f), 255.0f)),
-                                             uint8_t(fminf(fmaxf(rintf(b), 0.0f), 255.0f)), 255);
-        yuv[size_t(y) * W + x] = uint8_t(y8);
-        lsum += uint32_t(y8);
-      }
-      yuv[size_t(W) * H + size_t(gy) * cw + gx] = uint8_t(Cb);
-      yuv[size_t(W) * H + size_t(cw) * chh + size_t(gy) * cw + gx] = uint8_t(Cr);
-    }
+    yuv[size_t(W) * H + size_t(gy) * cw + gx] = uint8_t(Cb);
+    yuv[size_t(W) * H + size_t(cw) * chh + size_t(gy) * cw + gx] = uint8_t(Cr);
   }
-  const uint32_t v[3] = {lsum, 0u, 0u};
-  block_sum3(v, part + 3 * size_t(blockIdx.y * gridDim.x + blockIdx.x));
+  return lsum;
 }
 
-// stats[k] = the sum of the blocks' partials of statistic k (n blocks, 3 words each): one block, fixed order
-__global__ void __launch_bounds__(1024) isp_stats_kernel(const uint32_t* __restrict__ part, uint32_t n, int k0, int k1, uint32_t* __restrict__ stats) {
-  __shared__ uint32_t sm[32];
-  for (int k = k0; k < k1; k++) {
-    uint32_t s = 0;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += part[3 * size_t(i) + (k - k0)];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31u) == 0) sm[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t t = 0;
-      for (int w = 0; w < int(blockDim.x) / 32; w++) t += sm[w];
-      stats[k] = t;
-    }
-    __syncthreads();
+// the output stage with sharpening, on the (noise-reduced) image A: one thread per 2x2 block
+__global__ void __launch_bounds__(256) isp_output_kernel(const SensorParams P, const float4* __restrict__ A, uchar4* __restrict__ out,
+                                                         uint8_t* __restrict__ yuv, uint32_t* __restrict__ stats) {
+  const Su su{P.w};
+  const int W = int(P.w[0]), H = int(P.w[1]);
+  const int gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y * blockDim.y + threadIdx.y;
+  uint32_t lsum = 0;
+  if (gx * 2 < W && gy * 2 < H) {
+    auto at = [&](int xx, int yy) { return A[size_t(clampi(yy, 0, H - 1)) * W + clampi(xx, 0, W - 1)]; };
+    lsum = output_block<true>(su, P.w, at, gx, gy, W, H, out, yuv);
   }
+  block_add(&lsum, 1, stats);
+}
+
+// noise reduction and the output stage without sharpening: one thread per 2x2 block, the block's 64 x 16 pixels of
+// the demosaiced image with a 1-pixel ring in shared memory (bs[j][i] = B at the clamped (x0 - 1 + i, y0 - 1 + j))
+__global__ void __launch_bounds__(256) isp_finish_kernel(const SensorParams P, const float4* __restrict__ B, uchar4* __restrict__ out,
+                                                         uint8_t* __restrict__ yuv, uint32_t* __restrict__ stats) {
+  __shared__ float4 bs[18][66];
+  const Su su{P.w};
+  const int W = int(P.w[0]), H = int(P.w[1]);
+  const int x0 = blockIdx.x * 64, y0 = blockIdx.y * 16;
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  for (int e = t; e < 18 * 66; e += 256)
+    bs[e / 66][e % 66] = B[size_t(clampi(y0 - 1 + e / 66, 0, H - 1)) * W + clampi(x0 - 1 + e % 66, 0, W - 1)];
+  __syncthreads();
+  const int gx = blockIdx.x * 32 + threadIdx.x, gy = blockIdx.y * 8 + threadIdx.y;
+  uint32_t lsum = 0;
+  if (gx * 2 < W && gy * 2 < H) {
+    // the ring holds the clamped neighbours of the block's pixels, so the offsets index it directly
+    auto b = [&](int xx, int yy) { return bs[yy - y0 + 1][xx - x0 + 1]; };
+    auto at = [&](int xx, int yy) { return nr_pixel(su, P.w, b, xx, yy); };
+    lsum = output_block<false>(su, P.w, at, gx, gy, W, H, out, yuv);
+  }
+  block_add(&lsum, 1, stats);
 }
 
 static float host_float(uint32_t u) {
@@ -401,10 +453,10 @@ static float host_float(uint32_t u) {
   return f;
 }
 
-void launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
+int launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
   const uint32_t W = P.w[0], H = P.w[1];
-  const dim3 blk(32, 8), g((W + 31) / 32, (H + 7) / 8);
-  isp_optics_kernel<<<g, blk, 0, st>>>(P, b.L, b.ri, b.A);
+  const dim3 blk(32, 8);
+  int launches = 0;
   const float k = host_float(P.w[52]);
   if (k > 0.0f) {
     const int F = int(host_float(P.w[54]));
@@ -413,18 +465,21 @@ void launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
     glare_down_kernel<<<gg, blk, 0, st>>>(P, b.L, b.ri, b.GA);
     glare_blur_kernel<<<gg, blk, 0, st>>>(P, b.GA, b.GB, 0);
     glare_blur_kernel<<<gg, blk, 0, st>>>(P, b.GB, b.GA, 1);
+    launches += 3;
   }
-  isp_expose_kernel<<<g, blk, 0, st>>>(P, b.A, b.GA, b.raw);
-  demosaic_g_kernel<<<g, blk, 0, st>>>(P, b.raw, b.gpl);
-  demosaic_rb_kernel<<<g, blk, 0, st>>>(P, b.raw, b.gpl, b.B, b.part);
-  isp_stats_kernel<<<1, 1024, 0, st>>>(b.part, g.x * g.y, 1, 4, b.stats);
-  // noise reduction off: the output stage reads the demosaiced image directly (the kernel would copy it)
-  const bool nr = P.w[51] != 0u && host_float(P.w[58]) > 0.0f;
-  if (nr) isp_nr_kernel<<<g, blk, 0, st>>>(P, b.B, b.A);
+  isp_expose_kernel<<<dim3((W + 31) / 32, (H + EX_TY - 1) / EX_TY), blk, 0, st>>>(P, b.L, b.ri, b.GA, b.raw, b.stats);
+  isp_demosaic_kernel<<<dim3((W + 31) / 32, (H + DM_TY - 1) / DM_TY), blk, 0, st>>>(P, b.raw, b.B, b.stats);
+  launches += 2;
   const uint32_t cw = (W + 1) / 2, ch = (H + 1) / 2;
   const dim3 go((cw + 31) / 32, (ch + 7) / 8);
-  isp_output_kernel<<<go, blk, 0, st>>>(P, nr ? b.A : b.B, b.out, b.yuv, b.part);
-  isp_stats_kernel<<<1, 1024, 0, st>>>(b.part, go.x * go.y, 0, 1, b.stats);
+  if (host_float(P.w[46]) > 0.0f) {   // sharpening: the mask reads the reduced image's neighbours
+    const bool nr = P.w[51] != 0u && host_float(P.w[58]) > 0.0f;
+    if (nr) isp_nr_kernel<<<dim3((W + 31) / 32, (H + 7) / 8), blk, 0, st>>>(P, b.B, b.A);
+    isp_output_kernel<<<go, blk, 0, st>>>(P, nr ? b.A : b.B, b.out, b.yuv, b.stats);
+    return launches + (nr ? 2 : 1);
+  }
+  isp_finish_kernel<<<go, blk, 0, st>>>(P, b.B, b.out, b.yuv, b.stats);
+  return launches + 1;
 }
 
 // ------------------------------------------------------------------------------------- the raster pass's display

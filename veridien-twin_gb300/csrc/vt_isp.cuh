@@ -8,20 +8,18 @@ namespace vtk {
 struct IspBufs {
   const float4* L;   // radiance (w x h)
   const float* ri;   // relative illumination x vignetting (w x h)
-  float4* A;         // irradiance after the horizontal blur; later the noise-reduced image
+  float4* A;         // the noise-reduced image (with sharpening on)
   float4* B;         // demosaiced, white-balanced, colour-corrected linear RGB
   float4* GA;        // glare level (ceil(w / F) x ceil(h / F)), two buffers
   float4* GB;
   float* raw;        // raw DN (w x h)
-  float* gpl;        // green plane (w x h)
   uchar4* out;       // 8-bit RGB (alpha 255)
   uint8_t* yuv;      // Y (w x h), then Cb and Cr (ceil(w/2) x ceil(h/2) each)
   uint32_t* stats;   // luma sum, white-balance sums R, G, B
-  uint32_t* part;    // per-block partial sums (3 words per block of 32 x 8 pixels)
 };
 
-// the whole chain for one frame of the uniform's size
-void launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st);
+// the whole chain for one frame of the uniform's size; returns the number of kernels launched
+int launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st);
 
 // the raster pass's display look (vt_lite_display): du as lite_nodes/renderer.js:892 writes it, the previous frame's
 // statistics; stats receives this frame's (luma sum, count)

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_extend(con
   };
   while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
     if (!active) continue;
-    const int r = trace_visit<false>(Sl, 0.0f, st, stk);
+    const int r = trace_step<false>(Sl, 0.0f, st, stk);
     if (HC && r != 0 && VAR == WAVE_PLAIN && ci != MISS && st.k == -1) {
       wb.hcache[ci] = make_float4(st.best.t, st.best.u, st.best.v, __uint_as_float(st.best.tri));
       ci = MISS;
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(WAVE_THREADS, VT_TRACE_BLOCKS) wave_shadow(con
   };
   while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
     if (!active) continue;
-    const int r = trace_visit<true>(S, 0.0f, st, stk);
+    const int r = trace_step<true>(S, 0.0f, st, stk);
     bool done = r == 2;
     if (r == 1) done = !trace_phase(S, root, o, d, 0.0f, nee.w, 3u, skip, st, st.k + 1);
     if (!done) continue;
