@@ -886,7 +886,9 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
     refinements++;
     resid = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
     if (resid <= q->tol || sweeps >= max_it) break;
-    // correction: (I - diag(rho) F_lp) d = r by Jacobi sweeps from d = r
+    // correction: (I - diag(rho) F_lp) d = r by Jacobi sweeps from d = r, to the accuracy the next residual needs to
+    // fall under tol with a margin of 4 (an inexact correction), never finer than the low precision's floor
+    const double inner_goal = std::min(0.1, std::max(inner_tol, 0.25 * q->tol / resid));
     VT_CK(cudaMemcpyAsync(d, r, nr * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     for (uint32_t k = 0; k < inner_max && sweeps < max_it; k++) {
       if (fp8) {
@@ -909,7 +911,7 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
       float gms = 0;
       cudaEventElapsedTime(&gms, ctx->ev2, ctx->ev3);
       gemm_ms += gms;
-      if (!(h[1] > 0) || std::sqrt(h[0] / h[1]) <= inner_tol) break;
+      if (!(h[1] > 0) || std::sqrt(h[0] / h[1]) <= inner_goal) break;
     }
     vtk::tc_axpy(B, d, nr, ctx->stream);
   }

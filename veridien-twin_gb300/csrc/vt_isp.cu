@@ -132,26 +132,27 @@ __device__ __forceinline__ float3 glare_at(const Su& su, const float4* __restric
                      mix(mix(a.z, b.z, fx), mix(c.z, d.z, fx), fy));
 }
 
-// output rows per block of the exposure pass (32 x 8 threads, three rows each) and the shared rows it needs with the
-// vertical blur's halo (at most 12 taps each side)
-constexpr int EX_TY = 24;
-constexpr int EX_ROWS = EX_TY + 24;
+// the exposure pass's blocks: 32 columns x ty output rows (ty <= EX_MAX; 32 x 8 threads, a thread takes every 8th
+// row) and the shared rows they need with the vertical blur's halo (at most 12 taps each side)
+constexpr int EX_MAX = 40;
+constexpr int EX_ROWS = EX_MAX + 24;
 
 __global__ void __launch_bounds__(256) isp_expose_kernel(const SensorParams P, const float4* __restrict__ L, const float* __restrict__ ri,
-                                                         const float4* __restrict__ G, float* __restrict__ raw, uint32_t* __restrict__ stats) {
+                                                         const float4* __restrict__ G, float* __restrict__ raw, uint32_t* __restrict__ stats,
+                                                         int ty_rows) {
   __shared__ float taps[25];
   __shared__ float hx[EX_ROWS][32], hy[EX_ROWS][32], hz[EX_ROWS][32];
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int x = blockIdx.x * 32 + tx, y0 = blockIdx.y * EX_TY;
+  const int x = blockIdx.x * 32 + tx, y0 = blockIdx.y * ty_rows;
   if (blockIdx.x == 0 && blockIdx.y == 0 && ty == 0 && tx < 4) stats[tx] = 0u;
   const float sg = su.f(5);
   const int r = gauss_taps(sg);
   block_taps(sg, r, taps);
   // the horizontal half on shared row j = image row clamp(y0 - r + j): the vertical half's tap k of output row y0 + i
   // is row i + k + r, the clamped row y0 + i + k as the separable blur has it
-  const int rows = min(EX_TY, H - y0) + 2 * r;
+  const int rows = min(ty_rows, H - y0) + 2 * r;
   if (x < W) {
     for (int j = ty; j < rows; j += 8) {
       const int yy = clampi(y0 - r + j, 0, H - 1);
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(256) isp_expose_kernel(const SensorParams P, c
   __syncthreads();
   if (x >= W) return;
   const float kg = su.f(52);
-  for (int i = ty; i < EX_TY; i += 8) {
+  for (int i = ty; i < ty_rows; i += 8) {
     const int y = y0 + i;
     if (y >= H) break;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f, ws = 0.0f;
@@ -232,68 +233,151 @@ __device__ __forceinline__ float green_at(const Su& su, uint32_t code, uint32_t 
   return g;
 }
 
-// output rows per block of the demosaic pass (32 x 8 threads, two rows each)
-constexpr int DM_TY = 16;
+// the demosaic pass's tile: 64 pixels x 2 tq rows per block of 32 x 8 threads (tq <= QR_MAX quad rows), one 2x2
+// quad per thread and quad row
+constexpr int DM_TX = 64, QR_MAX = 16;
 
-__global__ void __launch_bounds__(256) isp_demosaic_kernel(const SensorParams P, const float* __restrict__ raw, float4* __restrict__ B,
-                                                           uint32_t* __restrict__ stats) {
-  // rs[j][i] = raw_at(x0 - 3 + i, y0 - 3 + j); gs[j][i] = the green plane at the image pixel clamp(x0 - 1 + i, y0 - 1 + j)
-  __shared__ float rs[DM_TY + 6][38];
-  __shared__ float gs[DM_TY + 2][34];
-  const Su su{P.w};
-  const int W = int(P.w[0]), H = int(P.w[1]);
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * DM_TY;
-  const int t = threadIdx.y * 32 + threadIdx.x;
-  for (int e = t; e < (DM_TY + 6) * 38; e += 256) rs[e / 38][e % 38] = raw_at(raw, x0 - 3 + e % 38, y0 - 3 + e / 38, W, H);
-  __syncthreads();
-  const uint32_t code = P.w[2], mode = P.w[50];
-  auto rw = [&](int xx, int yy) { return rs[yy - y0 + 3][xx - x0 + 3]; };
-  for (int e = t; e < (DM_TY + 2) * 34; e += 256) {
-    const int px = clampi(x0 - 1 + e % 34, 0, W - 1), py = clampi(y0 - 1 + e / 34, 0, H - 1);
-    gs[e / 34][e % 34] = green_at(su, code, mode, rw, px, py);
-  }
-  __syncthreads();
-  auto g_at = [&](int xx, int yy) { return gs[yy - y0 + 1][xx - x0 + 1]; };
-  uint32_t q[3] = {0u, 0u, 0u};
-  for (int rr = 0; rr < DM_TY / 8; rr++) {
-    const int x = x0 + int(threadIdx.x), y = y0 + int(threadIdx.y) + 8 * rr;
-    if (x >= W || y >= H) continue;
-    const uint32_t own = cfa_channel(code, uint32_t(x), uint32_t(y));
-    const float g = g_at(x, y);
-    float sr = 0.0f, sb = 0.0f, cr = 0.0f, cb = 0.0f;
+// the 2x2 CFA pattern words of cfa_channel: RGGB, GRBG, GBRG, BGGR
+constexpr uint32_t CFA_PATS[4] = {0x2110u, 0x1201u, 0x1021u, 0x0112u};
+__host__ __device__ constexpr uint32_t pat_channel(uint32_t pats, int x, int y) { return (pats >> (4u * (uint32_t(y & 1) * 2u + uint32_t(x & 1)))) & 0xfu; }
+
+// black level, white-balance statistics (added to q), WB and CCM of one demosaiced pixel
+__device__ __forceinline__ float4 rb_finish(const Su& su, float r, float gg, float b, uint32_t q[3]) {
+  const float black = su.f(25), full = fmaxf(su.f(24) - black, 1.0f);
+  float c[3] = {(r - black) / full, (gg - black) / full, (b - black) / full};
+  for (int k = 0; k < 3; k++) q[k] += uint32_t(rintf(clamp01(c[k]) * 1023.0f));
+  for (int k = 0; k < 3; k++) c[k] = c[k] * su.f(28 + k);
+  float o[3];
+  for (int k = 0; k < 3; k++) o[k] = su.f(32 + 4 * k) * c[0] + su.f(33 + 4 * k) * c[1] + su.f(34 + 4 * k) * c[2];
+  return make_float4(o[0], o[1], o[2], 1.0f);
+}
+
+// red and blue of image pixel (x, y) anywhere in the frame (neighbours clamped): rw / g_at give the raw and green
+// values of image pixels within one of it
+template <class Raw, class Green>
+__device__ __forceinline__ void rb_general(uint32_t code, uint32_t mode, Raw&& rw, Green&& g_at, int x, int y, int W, int H,
+                                           float& r, float& gg, float& b) {
+  const uint32_t own = cfa_channel(code, uint32_t(x), uint32_t(y));
+  const float g = g_at(x, y);
+  float sr = 0.0f, sb = 0.0f, cr = 0.0f, cb = 0.0f;
+  for (int dy = -1; dy <= 1; dy++)
+    for (int dx = -1; dx <= 1; dx++) {
+      const int xx = clampi(x + dx, 0, W - 1), yy = clampi(y + dy, 0, H - 1);
+      const uint32_t ch = cfa_channel(code, uint32_t(xx), uint32_t(yy));
+      if (ch == 1u) continue;
+      if (ch == own && !(dx == 0 && dy == 0)) continue;
+      const float d = rw(xx, yy) - g_at(xx, yy);
+      if (ch == 0u) { sr = sr + d; cr = cr + 1.0f; } else { sb = sb + d; cb = cb + 1.0f; }
+    }
+  r = g + sr / fmaxf(cr, 1.0f); gg = g; b = g + sb / fmaxf(cb, 1.0f);
+  if (mode <= 1u) {
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
     for (int dy = -1; dy <= 1; dy++)
       for (int dx = -1; dx <= 1; dx++) {
         const int xx = clampi(x + dx, 0, W - 1), yy = clampi(y + dy, 0, H - 1);
         const uint32_t ch = cfa_channel(code, uint32_t(xx), uint32_t(yy));
-        if (ch == 1u) continue;
         if (ch == own && !(dx == 0 && dy == 0)) continue;
-        const float d = rw(xx, yy) - g_at(xx, yy);
-        if (ch == 0u) { sr = sr + d; cr = cr + 1.0f; } else { sb = sb + d; cb = cb + 1.0f; }
+        if (ch == 1u && own == 1u && !(dx == 0 && dy == 0)) continue;
+        const float v = rw(xx, yy);
+        if (ch == 0u) { s0 = s0 + v; c0 = c0 + 1.0f; } else if (ch == 1u) { s1 = s1 + v; c1 = c1 + 1.0f; } else { s2 = s2 + v; c2 = c2 + 1.0f; }
       }
-    float r = g + sr / fmaxf(cr, 1.0f), gg = g, b = g + sb / fmaxf(cb, 1.0f);
-    if (mode <= 1u) {
-      float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
-      for (int dy = -1; dy <= 1; dy++)
-        for (int dx = -1; dx <= 1; dx++) {
-          const int xx = clampi(x + dx, 0, W - 1), yy = clampi(y + dy, 0, H - 1);
-          const uint32_t ch = cfa_channel(code, uint32_t(xx), uint32_t(yy));
-          if (ch == own && !(dx == 0 && dy == 0)) continue;
-          if (ch == 1u && own == 1u && !(dx == 0 && dy == 0)) continue;
-          const float v = rw(xx, yy);
-          if (ch == 0u) { s0 = s0 + v; c0 = c0 + 1.0f; } else if (ch == 1u) { s1 = s1 + v; c1 = c1 + 1.0f; } else { s2 = s2 + v; c2 = c2 + 1.0f; }
-        }
-      r = s0 / fmaxf(c0, 1.0f);
-      gg = s1 / fmaxf(c1, 1.0f);
-      b = s2 / fmaxf(c2, 1.0f);
-      if (mode == 1u) gg = g;
+    r = s0 / fmaxf(c0, 1.0f);
+    gg = s1 / fmaxf(c1, 1.0f);
+    b = s2 / fmaxf(c2, 1.0f);
+    if (mode == 1u) gg = g;
+  }
+}
+
+// rb_general for a pixel whose 3x3 neighbourhood lies inside the frame, at CFA phase (PX, PY) of pattern PATS: the
+// same taps in the same order, with every channel test and count known at compile time (counts 1, 2 or 4, so each
+// quotient is a product by 1, 1/2 or 1/4, exactly as the division gives it); rw / g_at take offsets from the pixel
+template <uint32_t PATS, int PX, int PY, class Raw, class Green>
+__device__ __forceinline__ void rb_inner(uint32_t mode, Raw&& rw, Green&& g_at, float& r, float& gg, float& b) {
+  constexpr uint32_t own = pat_channel(PATS, PX, PY);
+  const float g = g_at(0, 0);
+  float sr = 0.0f, sb = 0.0f, cr = 0.0f, cb = 0.0f;
+#pragma unroll
+  for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+      const uint32_t ch = pat_channel(PATS, PX + dx, PY + dy);
+      if (ch == 1u) continue;
+      if (ch == own && !(dx == 0 && dy == 0)) continue;
+      const float d = rw(dx, dy) - g_at(dx, dy);
+      if (ch == 0u) { sr = sr + d; cr = cr + 1.0f; } else { sb = sb + d; cb = cb + 1.0f; }
     }
-    const float black = su.f(25), full = fmaxf(su.f(24) - black, 1.0f);
-    float c[3] = {(r - black) / full, (gg - black) / full, (b - black) / full};
-    for (int k = 0; k < 3; k++) q[k] += uint32_t(rintf(clamp01(c[k]) * 1023.0f));
-    for (int k = 0; k < 3; k++) c[k] = c[k] * su.f(28 + k);
-    float o[3];
-    for (int k = 0; k < 3; k++) o[k] = su.f(32 + 4 * k) * c[0] + su.f(33 + 4 * k) * c[1] + su.f(34 + 4 * k) * c[2];
-    B[size_t(y) * W + x] = make_float4(o[0], o[1], o[2], 1.0f);
+  r = g + sr / fmaxf(cr, 1.0f); gg = g; b = g + sb / fmaxf(cb, 1.0f);
+  if (mode <= 1u) {
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+      for (int dx = -1; dx <= 1; dx++) {
+        const uint32_t ch = pat_channel(PATS, PX + dx, PY + dy);
+        if (ch == own && !(dx == 0 && dy == 0)) continue;
+        if (ch == 1u && own == 1u && !(dx == 0 && dy == 0)) continue;
+        const float v = rw(dx, dy);
+        if (ch == 0u) { s0 = s0 + v; c0 = c0 + 1.0f; } else if (ch == 1u) { s1 = s1 + v; c1 = c1 + 1.0f; } else { s2 = s2 + v; c2 = c2 + 1.0f; }
+      }
+    r = s0 / fmaxf(c0, 1.0f);
+    gg = s1 / fmaxf(c1, 1.0f);
+    b = s2 / fmaxf(c2, 1.0f);
+    if (mode == 1u) gg = g;
+  }
+}
+
+// CODE: the CFA pattern index as cfa_channel reads the uniform's code (0 RGGB, 1 GRBG, 2 GBRG, 3 and above BGGR)
+template <int CODE>
+__global__ void __launch_bounds__(256) isp_demosaic_kernel(const SensorParams P, const float* __restrict__ raw, float4* __restrict__ B,
+                                                           uint32_t* __restrict__ stats, int tq) {
+  constexpr uint32_t PATS = CFA_PATS[CODE];
+  // rs[j][i] = raw_at(x0 - 3 + i, y0 - 3 + j); gs[j][i] = the green plane at the image pixel clamp(x0 - 1 + i, y0 - 1 + j)
+  __shared__ float rs[2 * QR_MAX + 6][DM_TX + 6];
+  __shared__ float gs[2 * QR_MAX + 2][DM_TX + 2];
+  const Su su{P.w};
+  const int W = int(P.w[0]), H = int(P.w[1]);
+  const int x0 = blockIdx.x * DM_TX, y0 = blockIdx.y * 2 * tq;
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  constexpr int RW = DM_TX + 6, GW = DM_TX + 2;
+  for (int e = t; e < (2 * tq + 6) * RW; e += 256) rs[e / RW][e % RW] = raw_at(raw, x0 - 3 + e % RW, y0 - 3 + e / RW, W, H);
+  __syncthreads();
+  const uint32_t code = P.w[2], mode = P.w[50];
+  auto rw = [&](int xx, int yy) { return rs[yy - y0 + 3][xx - x0 + 3]; };
+  for (int e = t; e < (2 * tq + 2) * GW; e += 256) {
+    const int px = clampi(x0 - 1 + e % GW, 0, W - 1), py = clampi(y0 - 1 + e / GW, 0, H - 1);
+    gs[e / GW][e % GW] = green_at(su, code, mode, rw, px, py);
+  }
+  __syncthreads();
+  auto g_at = [&](int xx, int yy) { return gs[yy - y0 + 1][xx - x0 + 1]; };
+  uint32_t q[3] = {0u, 0u, 0u};
+  for (int qr = int(threadIdx.y); qr < tq; qr += 8) {
+  const int qx = x0 + 2 * int(threadIdx.x), qy = y0 + 2 * qr;
+  if (qx >= 2 && qx + 3 <= W && qy >= 2 && qy + 3 <= H) {
+    // the quad's 4 x 4 neighbourhood lies inside the frame: tile offsets of pixel (qx, qy)
+    const int ri = qx - x0 + 3, rj = qy - y0 + 3, gi = qx - x0 + 1, gj = qy - y0 + 1;
+    float r, gg, b;
+    float4* o = B + size_t(qy) * W + qx;
+#define VT_QUAD_PIXEL(PX, PY)                                                                                        \
+    {                                                                                                                \
+      auto rwq = [&](int dx, int dy) { return rs[rj + PY + dy][ri + PX + dx]; };                                     \
+      auto gq = [&](int dx, int dy) { return gs[gj + PY + dy][gi + PX + dx]; };                                      \
+      rb_inner<PATS, PX, PY>(mode, rwq, gq, r, gg, b);                                                               \
+      o[size_t(PY) * W + PX] = rb_finish(su, r, gg, b, q);                                                           \
+    }
+    VT_QUAD_PIXEL(0, 0)
+    VT_QUAD_PIXEL(1, 0)
+    VT_QUAD_PIXEL(0, 1)
+    VT_QUAD_PIXEL(1, 1)
+#undef VT_QUAD_PIXEL
+  } else {
+    for (int k = 0; k < 4; k++) {
+      const int x = qx + (k & 1), y = qy + (k >> 1);
+      if (x >= W || y >= H) continue;
+      float r, gg, b;
+      rb_general(code, mode, rw, g_at, x, y, W, H, r, gg, b);
+      B[size_t(y) * W + x] = rb_finish(su, r, gg, b, q);
+    }
+  }
   }
   // white-balance statistics R, G, B
   block_add(q, 3, stats + 1);
@@ -313,7 +397,8 @@ __device__ __forceinline__ float4 nr_pixel(const Su& su, const uint32_t* w, Fetc
     for (int dx = -1; dx <= 1; dx++) {
       const float4 c = b(x + dx, y + dy);
       const float dY = (c.x - c0.x) * 0.2126f + (c.y - c0.y) * 0.7152f + (c.z - c0.z) * 0.0722f;
-      const float wt = vt_expf(-0.5f * float(dx * dx + dy * dy) / (ss * ss) - 0.5f * dY * dY / (rs * rs));
+      // the centre tap's exponent is exactly zero for a finite pixel (the demosaiced image is finite): weight 1
+      const float wt = dx == 0 && dy == 0 ? 1.0f : vt_expf(-0.5f * float(dx * dx + dy * dy) / (ss * ss) - 0.5f * dY * dY / (rs * rs));
       ax = ax + wt * c.x;
       ay = ay + wt * c.y;
       az = az + wt * c.z;
@@ -424,25 +509,27 @@ __global__ void __launch_bounds__(256) isp_output_kernel(const SensorParams P, c
   block_add(&lsum, 1, stats);
 }
 
-// noise reduction and the output stage without sharpening: one thread per 2x2 block, the block's 64 x 16 pixels of
-// the demosaiced image with a 1-pixel ring in shared memory (bs[j][i] = B at the clamped (x0 - 1 + i, y0 - 1 + j))
+// noise reduction and the output stage without sharpening: one thread per 2x2 block, the block's 64 x 2 tq pixels
+// (tq <= QR_MAX quad rows; a thread takes every 8th quad row) of the demosaiced image with a
+// 1-pixel ring in shared memory (bs[j][i] = B at the clamped (x0 - 1 + i, y0 - 1 + j))
 __global__ void __launch_bounds__(256) isp_finish_kernel(const SensorParams P, const float4* __restrict__ B, uchar4* __restrict__ out,
-                                                         uint8_t* __restrict__ yuv, uint32_t* __restrict__ stats) {
-  __shared__ float4 bs[18][66];
+                                                         uint8_t* __restrict__ yuv, uint32_t* __restrict__ stats, int tq) {
+  __shared__ float4 bs[2 * QR_MAX + 2][66];
   const Su su{P.w};
   const int W = int(P.w[0]), H = int(P.w[1]);
-  const int x0 = blockIdx.x * 64, y0 = blockIdx.y * 16;
+  const int x0 = blockIdx.x * 64, y0 = blockIdx.y * 2 * tq;
   const int t = threadIdx.y * 32 + threadIdx.x;
-  for (int e = t; e < 18 * 66; e += 256)
+  for (int e = t; e < (2 * tq + 2) * 66; e += 256)
     bs[e / 66][e % 66] = B[size_t(clampi(y0 - 1 + e / 66, 0, H - 1)) * W + clampi(x0 - 1 + e % 66, 0, W - 1)];
   __syncthreads();
-  const int gx = blockIdx.x * 32 + threadIdx.x, gy = blockIdx.y * 8 + threadIdx.y;
+  // the ring holds the clamped neighbours of the block's pixels, so the offsets index it directly
+  auto b = [&](int xx, int yy) { return bs[yy - y0 + 1][xx - x0 + 1]; };
+  auto at = [&](int xx, int yy) { return nr_pixel(su, P.w, b, xx, yy); };
+  const int gx = blockIdx.x * 32 + threadIdx.x;
   uint32_t lsum = 0;
-  if (gx * 2 < W && gy * 2 < H) {
-    // the ring holds the clamped neighbours of the block's pixels, so the offsets index it directly
-    auto b = [&](int xx, int yy) { return bs[yy - y0 + 1][xx - x0 + 1]; };
-    auto at = [&](int xx, int yy) { return nr_pixel(su, P.w, b, xx, yy); };
-    lsum = output_block<false>(su, P.w, at, gx, gy, W, H, out, yuv);
+  for (int qr = int(threadIdx.y); qr < tq; qr += 8) {
+    const int gy = blockIdx.y * tq + qr;
+    if (gx * 2 < W && gy * 2 < H) lsum += output_block<false>(su, P.w, at, gx, gy, W, H, out, yuv);
   }
   block_add(&lsum, 1, stats);
 }
@@ -452,6 +539,11 @@ static float host_float(uint32_t u) {
   std::memcpy(&f, &u, 4);
   return f;
 }
+
+// block heights: 24 output rows for the exposure pass, 8 quad rows (16 pixel rows) for demosaic and finish. Taller
+// blocks with fewer of them (one wave on 1280x720) measured no faster: the passes lose their overlap of one block's
+// loads with another's arithmetic.
+constexpr int EX_ROWS_PER_BLOCK = 24, QR_PER_BLOCK = 8;
 
 int launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
   const uint32_t W = P.w[0], H = P.w[1];
@@ -467,18 +559,25 @@ int launch_isp(const SensorParams& P, const IspBufs& b, cudaStream_t st) {
     glare_blur_kernel<<<gg, blk, 0, st>>>(P, b.GB, b.GA, 1);
     launches += 3;
   }
-  isp_expose_kernel<<<dim3((W + 31) / 32, (H + EX_TY - 1) / EX_TY), blk, 0, st>>>(P, b.L, b.ri, b.GA, b.raw, b.stats);
-  isp_demosaic_kernel<<<dim3((W + 31) / 32, (H + DM_TY - 1) / DM_TY), blk, 0, st>>>(P, b.raw, b.B, b.stats);
+  constexpr int ex_rows = EX_ROWS_PER_BLOCK, dm_q = QR_PER_BLOCK, fn_q = QR_PER_BLOCK;
+  isp_expose_kernel<<<dim3((W + 31) / 32, (H + ex_rows - 1) / ex_rows), blk, 0, st>>>(P, b.L, b.ri, b.GA, b.raw, b.stats, ex_rows);
+  const uint32_t qrows = (H + 1) / 2;
+  const dim3 gd((W + DM_TX - 1) / DM_TX, (qrows + dm_q - 1) / dm_q);
+  const uint32_t code = P.w[2];
+  if (code == 0u) isp_demosaic_kernel<0><<<gd, blk, 0, st>>>(P, b.raw, b.B, b.stats, dm_q);
+  else if (code == 1u) isp_demosaic_kernel<1><<<gd, blk, 0, st>>>(P, b.raw, b.B, b.stats, dm_q);
+  else if (code == 2u) isp_demosaic_kernel<2><<<gd, blk, 0, st>>>(P, b.raw, b.B, b.stats, dm_q);
+  else isp_demosaic_kernel<3><<<gd, blk, 0, st>>>(P, b.raw, b.B, b.stats, dm_q);
   launches += 2;
   const uint32_t cw = (W + 1) / 2, ch = (H + 1) / 2;
-  const dim3 go((cw + 31) / 32, (ch + 7) / 8);
   if (host_float(P.w[46]) > 0.0f) {   // sharpening: the mask reads the reduced image's neighbours
+    const dim3 go((cw + 31) / 32, (ch + 7) / 8);
     const bool nr = P.w[51] != 0u && host_float(P.w[58]) > 0.0f;
     if (nr) isp_nr_kernel<<<dim3((W + 31) / 32, (H + 7) / 8), blk, 0, st>>>(P, b.B, b.A);
     isp_output_kernel<<<go, blk, 0, st>>>(P, nr ? b.A : b.B, b.out, b.yuv, b.stats);
     return launches + (nr ? 2 : 1);
   }
-  isp_finish_kernel<<<go, blk, 0, st>>>(P, b.B, b.out, b.yuv, b.stats);
+  isp_finish_kernel<<<dim3((cw + 31) / 32, (ch + fn_q - 1) / fn_q), blk, 0, st>>>(P, b.B, b.out, b.yuv, b.stats, fn_q);
   return launches + 1;
 }
 

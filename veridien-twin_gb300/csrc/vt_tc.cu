@@ -295,6 +295,21 @@ __device__ __forceinline__ void block_sum2(double a, double b, double* partials)
 
 constexpr uint32_t CB_THREADS = 256;
 
+// a block's sums of a and b into partials[2 block], [2 block + 1]: per thread and per warp in FP32, per block in FP64
+// (a sweep's stopping test needs no more, and FP64 per element would cost more than the sweep's memory traffic)
+__device__ __forceinline__ void block_sum2f(float a, float b, double* partials) {
+  __shared__ double sa[32], sb[32];
+  for (int o = 16; o > 0; o >>= 1) { a += __shfl_down_sync(0xffffffffu, a, o); b += __shfl_down_sync(0xffffffffu, b, o); }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (l == 0) { sa[w] = double(a); sb[w] = double(b); }
+  __syncthreads();
+  if (w == 0) {
+    double x = l < nw ? sa[l] : 0.0, y = l < nw ? sb[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) { x += __shfl_down_sync(0xffffffffu, x, o); y += __shfl_down_sync(0xffffffffu, y, o); }
+    if (l == 0) { partials[2 * blockIdx.x] = x; partials[2 * blockIdx.x + 1] = y; }
+  }
+}
+
 // thread per (row, column < R); splits summed in order s = 0, 1, ... (deterministic)
 __global__ void __launch_bounds__(CB_THREADS) combine_sweep_kernel(const float* __restrict__ P, uint32_t splits, uint32_t n, uint32_t R,
                                                                    const float* __restrict__ rho, const float* __restrict__ rhs,
@@ -302,7 +317,7 @@ __global__ void __launch_bounds__(CB_THREADS) combine_sweep_kernel(const float* 
                                                                    const float* __restrict__ rs, const float* __restrict__ cs,
                                                                    double* __restrict__ parts) {
   const size_t idx = size_t(blockIdx.x) * CB_THREADS + threadIdx.x;
-  double d2 = 0.0, y2 = 0.0;
+  float d2 = 0.0f, y2 = 0.0f;
   if (idx < size_t(n) * R) {
     const uint32_t i = uint32_t(idx / R), c = uint32_t(idx % R);
     float acc = 0.0f;
@@ -310,11 +325,11 @@ __global__ void __launch_bounds__(CB_THREADS) combine_sweep_kernel(const float* 
     if (rs) acc *= rs[i] * cs[c];
     const float y = fmaf(rho[i], acc, rhs[idx]);
     Y[idx] = y;
-    const double dd = double(y) - double(Xin[idx]);
+    const float dd = y - Xin[idx];
     d2 = dd * dd;
-    y2 = double(y) * double(y);
+    y2 = y * y;
   }
-  block_sum2(d2, y2, parts);
+  block_sum2f(d2, y2, parts);
 }
 
 __global__ void __launch_bounds__(CB_THREADS) combine_residual_kernel(const float* __restrict__ P, uint32_t splits, uint32_t n, uint32_t R,
