@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, cons
   };
   while (take_rays(active, exhausted, wb.fetch, n, cp.refill, start)) {
     if (!active) continue;
-    const int r = trace_visit<true>(S, 0.0f, st, stk);
+    const int r = trace_step<true>(S, 0.0f, st, stk);
     bool done = r == 2;
     if (r == 1) done = !trace_phase(S, cp.root, o, d, 0.0f, tt, 3u, skip, st, st.k + 1);
     if (!done) continue;

@@ -557,81 +557,15 @@ struct LaneStack {
   __device__ __forceinline__ uint2 get(uint32_t i) const { return i < SH_DEPTH ? sh[i * stride + lane] : deep[i - SH_DEPTH]; }
 };
 
-// one node visit of the current phase (an iteration of traverse's loop): 0 continue, 1 the phase is finished,
-// 2 an any-hit query found its hit
-template <bool ANY>
-__device__ __forceinline__ int trace_visit(const Scene& S, float tmin, TraceState& st, LaneStack& stk) {
-  if (++st.visits > MAX_VISITS) { atomicAdd(S.dbg + DBG_VISITS, 1u); return 1; }
-  const uint32_t node = st.node;
-  const uint32_t inst = st.k < 0 ? MISS : uint32_t(st.k);
-#if VT_TOP_NODES
-  const bool staged = (node & TOP_BIT) != 0u;
-  float4 a0, a1, a2, a3;
-  // a staged node from shared memory, the rest through the read-only global path
-  if (staged) {
-    const float4* nb = stk.top + 4u * (node & 0xffffu);
-    a0 = nb[0]; a1 = nb[1]; a2 = nb[2]; a3 = nb[3];
-  } else {
-    const float4* nb = S.nodes + 4u * node;
-    a0 = __ldg(nb); a1 = __ldg(nb + 1); a2 = __ldg(nb + 2); a3 = __ldg(nb + 3);
-  }
-#else
-  constexpr bool staged = false;
-  const float4* nb = S.nodes + 4u * node;
-  const float4 a0 = __ldg(nb), a1 = __ldg(nb + 1), a2 = __ldg(nb + 2), a3 = __ldg(nb + 3);
-#endif
-  float t0 = slab(xyz(a0), xyz(a1), st.ol, st.inv, tmin, st.best.t);
-  float t1 = slab(xyz(a2), xyz(a3), st.ol, st.inv, tmin, st.best.t);
-  const uint32_t c0 = fu(a1.w), c1 = fu(a3.w), r0 = fu(a0.w), r1 = fu(a2.w);
-#pragma unroll
-  for (int c = 0; c < 2; c++) {
-    const float tc = c == 0 ? t0 : t1;
-    const uint32_t cnt = c == 0 ? c0 : c1, ref = c == 0 ? r0 : r1;
-    if (tc < st.best.t && cnt > 0u) {
-      if (cnt > MAX_LEAF) atomicAdd(S.dbg + DBG_LEAF, 1u);
-      const uint32_t end = ref + min(cnt, MAX_LEAF);
-      for (uint32_t k = ref; k < end; k++) {
-        float t, u, v;
-        if (tri_hit(S, k, st.ol, st.dl, tmin, st.best.t, t, u, v)) {
-          st.best.t = t; st.best.u = u; st.best.v = v; st.best.tri = k; st.best.inst = inst;
-          if (ANY) return 2;
-        }
-      }
-      if (c == 0) t0 = BIG; else t1 = BIG;
-    }
-  }
-  t0 = t0 < st.best.t ? t0 : BIG;
-  t1 = t1 < st.best.t ? t1 : BIG;
-  // staged records were checked for increasing child indices when the set was built
-  if (!staged && ((t0 < BIG && c0 == 0u && r0 <= node) || (t1 < BIG && c1 == 0u && r1 <= node))) { atomicAdd(S.dbg + DBG_CORRUPT, 1u); return 1; }
-  const bool go0 = t0 < BIG, go1 = t1 < BIG;
-  if (go0 && go1) {
-    if (t1 < t0) { stk.set(st.sp, r0, t0); st.node = r1; }
-    else { stk.set(st.sp, r1, t1); st.node = r0; }
-    st.sp = min(st.sp + 1u, STACK - 1u);
-  } else if (go0) {
-    st.node = r0;
-  } else if (go1) {
-    st.node = r1;
-  } else {
-    while (st.sp > 0u) {
-      st.sp--;
-      const uint2 e = stk.get(st.sp);
-      if (__uint_as_float(e.y) < st.best.t) { st.node = e.x; return 0; }
-    }
-    return 1;
-  }
-  return 0;
-}
-
-// trace_visit's operations, one unit per step: a step either visits a node (the child boxes, and the first leaf child
-// to test) or tests one triangle of that leaf. The node's children stay in the state until its leaves are done; then
-// the same step takes the next node from its interior children or the stack. Per ray the sequence of operations is
-// trace_visit's (child 0's leaf in triangle order, child 1's leaf only if its box is still nearer than the best hit,
-// then the push / pop with the updated best), so are the hits; a warp's lanes no longer wait for the longest leaf loop
-// among them. 0 continue, 1 the phase is finished, 2 an any-hit query found its hit.
+// The current phase's traversal, one unit of traverse's loop per step: a step either visits a node (the child boxes,
+// and the first leaf child to test) or tests one triangle of that leaf. The node's children stay in the state until
+// its leaves are done; then the same step takes the next node from its interior children or the stack. Per ray the
+// sequence of operations is traverse's (child 0's leaf in triangle order, child 1's leaf only if its box is still
+// nearer than the best hit, then the push / pop with the updated best), so are the hits; a warp's lanes do not wait
+// for the longest leaf loop among them. The 2048-visit and 64-triangle caps and the parent-before-child check count
+// into dbg as in traverse. 0 continue, 1 the phase is finished, 2 an any-hit query found its hit.
 // the leaf of child c, when its box is nearer than the best hit: its triangles become the ones left, and the child's
-// distance BIG (trace_visit drops a tested leaf child from the push / pop the same way, after its loop)
+// distance BIG (traverse drops a tested leaf child from the push / pop the same way, after its loop)
 __device__ __forceinline__ bool leaf_enter(const Scene& S, TraceState& st, uint32_t c) {
   const float tc = c == 0u ? st.t0 : st.t1;
   const uint32_t cnt = (st.c01 >> (16u * c)) & 0xffffu, ref = c == 0u ? st.r0 : st.r1;

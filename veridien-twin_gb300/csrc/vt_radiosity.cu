@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(FV_THREADS, 4) ff_visibility_kernel(const Scen
   };
   while (take_rays(active, exhausted, head, total, REFILL, start)) {
     if (!active) continue;
-    const int r = trace_visit<true>(S, 0.0f, st, stk);
+    const int r = trace_step<true>(S, 0.0f, st, stk);
     bool done = r == 2;
     if (r == 1) done = !trace_phase(S, 0u, o, d, 0.0f, 0.5f, 3u, skip, st, st.k + 1);
     if (!done) continue;
