@@ -539,6 +539,21 @@ def calib_bench(torch, device=0):
         FD.append((cal.forward(xp) - cal.forward(xm)) / (xp[i] - xm[i]))
         G.append(g[i])
     cal.forward(x0)
+    # the two forms of the render alone (image loss, intrinsics on): paths' records kept, or traced again in chunks
+    alb0, lamp0 = x0[:n_alb].reshape(-1, 3), x0[n_alb:n_alb + info["n_lamps"]]
+    forms = {}
+    for name, rp in (("stored", False), ("replay", True), ("replay_chunks_of_4", 4)):
+        fw2, bw2 = [], []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            r.calib_forward(cams, alb0, lamp0, spp=SPP_C, max_depth=DEPTH_C, targets=targets, images=False, replay=rp, intrinsics=True)
+            b = time.perf_counter()
+            r.calib_backward()
+            c = time.perf_counter()
+            fw2.append(b - a)
+            bw2.append(c - b)
+        forms[name] = {"forward_ms": min(fw2) * 1e3, "backward_ms": min(bw2) * 1e3}
     G, FD = np.array(G), np.array(FD)
     vec = float(np.linalg.norm(G - FD) / np.linalg.norm(FD))
     worst = float(np.max(np.abs(G - FD) / np.maximum(np.abs(FD), 1e-2 * np.abs(FD).max())))
@@ -547,7 +562,10 @@ def calib_bench(torch, device=0):
             "params": 8 * 3 + info["n_lamps"] + 3 * 8, "parameter_vector": int(cal.n),
             "params_note": "8 materials x RGB + emitter triangles + 3 x 8 intrinsics; the vector also holds the unused bench and "
                            "emitter materials (zero gradient)", "setup_s": setup_s, "forward_ms": fms, "backward_ms": bms,
-            "forward_msamples_per_s": samples / (fms / 1e3) / 1e6, "loss_at_start": float(loss0),
+            "forward_msamples_per_s": samples / (fms / 1e3) / 1e6, "loss_at_start": float(loss0), "forms": forms,
+            "forms_note": "the render alone (image loss with the intrinsics' derivative): every path's record kept, or the paths "
+                          "traced again in chunks of sub-samples through the same kernels (the form used when the records do not fit): "
+                          "'replay' sizes the chunk to the free memory (here all 32 sub-samples), 'replay_chunks_of_4' takes 8 chunks",
             "grad_check": {"entries": len(ids), "h": 3e-3, "vector_rel_err": vec, "worst_entry_rel_err": worst,
                            "note": "GPU central differences of the FP32 render (FP64 loss) on albedo and lamp entries; FP64-oracle "
                                    "differences (albedos, lamps at h = 1e-4; intrinsics with the path decisions frozen) are in "

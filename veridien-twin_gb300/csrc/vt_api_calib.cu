@@ -271,6 +271,38 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
       K.stored = st == VT_OK;
     }
   }
+  if (!K.stored) {
+    // replay form: the paths traced in chunks of sub-samples, one chunk's records (and derivative records) at a time,
+    // a chunk sized to a quarter of the free memory (or to replay - 1 sub-samples when the request asks for less)
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    size_t n_pix_max = 1;
+    for (const auto& cp : cps) n_pix_max = std::max<size_t>(n_pix_max, vtk::tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h));
+    const size_t per_sub = n_pix_max * (vtk::calib_record_bytes(1) + (K.want_k ? vtk::calib_tan_bytes(1) : 0));
+    const uint32_t cap = q->replay >= 2 ? q->replay - 1 : q->spp;
+    K.chunk = uint32_t(std::max<size_t>(1, std::min<size_t>({size_t(cap), size_t(q->spp), (fr / 4) / std::max<size_t>(per_sub, 1)})));
+    const size_t chunk_paths = n_pix_max * K.chunk;
+    K.wave_paths = uint32_t(std::min<size_t>(8u << 20, chunk_paths));
+    const size_t rec_bytes = vtk::calib_record_bytes(uint32_t(chunk_paths));
+    const size_t tan_bytes = K.want_k ? vtk::calib_tan_bytes(uint32_t(chunk_paths)) : 0;
+    const size_t wave_need = vtk::wave_bytes(K.wave_paths, cps[0].n_light, 0);
+    auto grow = [&](void*& ptr, size_t& cap_bytes, size_t need) -> bool {
+      if (cap_bytes >= need) return true;
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(ptr);
+      ptr = nullptr;
+      cap_bytes = 0;
+      if (cudaMalloc(&ptr, need) != cudaSuccess) { cudaGetLastError(); return false; }
+      cap_bytes = need;
+      return true;
+    };
+    void* wave = ctx->d_wave;
+    size_t wave_cap = ctx->wave_cap;
+    const bool ok = grow(K.records, K.rec_cap, rec_bytes) && (!tan_bytes || grow(K.tan, K.tan_cap, tan_bytes)) && grow(wave, wave_cap, wave_need);
+    ctx->d_wave = wave;
+    ctx->wave_cap = wave_cap;
+    if (!ok) return fail(ctx, VT_ERR_OOM, "calib: replay buffers (one chunk of path records and the wave state)");
+  }
   double total = 0.0;
   off = 0;
   for (uint32_t c = 0; c < q->n_cameras; c++) {
@@ -285,7 +317,12 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
                                    K.want_k ? static_cast<char*>(K.tan) + K.rec_off[c] * vtk::calib_tan_bytes(1) : nullptr,
                                    std::min<int>(ctx->wave_blocks, int(K.max_partials)), ctx->stream);
     } else {
-      nb = vtk::launch_calib(dev_scene(ctx), cp, C, 0, blocks, ctx->stream);
+      const vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, K.wave_paths, cp.n_light, 0, ctx->d_work);
+      const int wblocks = std::min<int>(ctx->wave_blocks, int(K.max_partials));
+      nb = 0;
+      for (uint32_t i0 = 0; i0 < cp.spp; i0 += K.chunk)
+        nb = vtk::calib_wave_chunk(dev_scene(ctx), cp, C, wb, K.wave_paths, K.records, nullptr, i0, std::min(cp.spp, i0 + K.chunk), 0, wblocks,
+                                   ctx->stream);
     }
     vtk::launch_sum(K.partials, nb, K.loss, ctx->stream);
     VT_CK(cudaGetLastError());
@@ -323,8 +360,13 @@ vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp) {
       vtk::calib_records_backward(cp, calib_dev(ctx, cam), static_cast<char*>(K.records) + K.rec_off[c] * vtk::calib_record_bytes(1),
                                   K.want_k ? static_cast<char*>(K.tan) + K.rec_off[c] * vtk::calib_tan_bytes(1) : nullptr,
                                   ctx->wave_blocks * 2, ctx->stream);
-    else
-      vtk::launch_calib(dev_scene(ctx), cp, calib_dev(ctx, cam), K.want_k ? 2 : 1, ctx->wave_blocks * 2, ctx->stream);
+    else {
+      const vtk::WaveBufs wb = vtk::wave_carve(ctx->d_wave, K.wave_paths, cp.n_light, 0, ctx->d_work);
+      const int wblocks = std::min<int>(ctx->wave_blocks, int(K.max_partials));
+      for (uint32_t i0 = 0; i0 < cp.spp; i0 += K.chunk)
+        vtk::calib_wave_chunk(dev_scene(ctx), cp, calib_dev(ctx, cam), wb, K.wave_paths, K.records, K.want_k ? K.tan : nullptr, i0,
+                              std::min(cp.spp, i0 + K.chunk), K.want_k ? 2 : 1, wblocks, ctx->stream);
+    }
   }
   K.have_k = K.want_k;
   VT_CK(cudaGetLastError());

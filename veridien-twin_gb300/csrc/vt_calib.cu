@@ -9,10 +9,14 @@
 // carries: rho / pi x H(node), H = F B the irradiance from the other nodes. An emitter hit adds its radiance
 // (MIS-weighted after the first vertex). Nothing in the sampling depends on the parameters, so the estimator is a
 // polynomial in the albedos, linear in the emitter radiances and in H, and its derivative is exact by replay:
-// the same path is traced again from the same sample numbers, and each term's derivative is accumulated (FP64).
+// each path's record (its vertices' materials and nodes, its light samples' contributions) is differentiated term by
+// term, and the derivatives are accumulated in FP64.
 //
-// The forward and the backward run the same kernel code for the path (one kernel, a uniform `backward` flag), so
-// the replayed path is bit-identical to the one the forward rendered.
+// The paths are traced by the wavefront kernels of the path tracer (closest hit, then calib_shade, then
+// calib_shadow), which write each path's record. When the records of every path fit in memory the backward reads the
+// forward's records; otherwise the paths are traced again in chunks of sub-samples, each chunk's records
+// differentiated before the next is traced. Both forms trace the same paths with the same kernels, so the replayed
+// records are bit-identical to the forward's.
 #include <utility>
 
 #include "vt_calib.cuh"
@@ -117,114 +121,6 @@ __device__ __forceinline__ float3 tan_emitter_hit(const Scene& S, const Hit& h, 
   return f3(out[0], out[1], out[2]);
 }
 
-// With TAN, dL[c] (c = r, g, b) receives the derivative of the path's radiance in channel c with respect to its
-// primary direction d0; the path's values are the estimator's own either way.
-template <bool TAN>
-__device__ __forceinline__ void calib_path(const Scene& S, const CamParams& cp, const CalibDev& C, uint32_t id, uint32_t i, CalPath& P,
-                                           float3* dL = nullptr) {
-  P.n = 0;
-  P.emit_lamp = MISS;
-  P.emit_a = 0.0f;
-  P.node = MISS;
-  float4 o4, d4;
-  uint32_t hs;
-  if (!camera_path(cp, id, i, o4, d4, hs)) return;
-  float3 o = xyz(o4), d = xyz(d4);
-  const float tt = o4.w;
-  const uint32_t nl = cp.n_light;
-  const float fnl = float(nl);
-  const float area = __ldg(S.su + 3);
-  const uint32_t skip_sh = ldu(S.su + 7);
-  float pb_prev = 0.0f;
-  Tan3 Jo, Jd;
-  float3 dpb = f3(0, 0, 0), T = f3(1, 1, 1);
-  if (TAN) { Jo = tan_zero(); Jd = tan_identity(); dL[0] = dL[1] = dL[2] = f3(0, 0, 0); }
-  for (uint32_t b = 1; b <= cp.max_depth; b++) {
-    const Hit h = trace_scene<false>(S, cp.root, o, d, 0.0f, BIG, tt, 3u, b == 1 ? cp.skip : 0u);
-    if (h.tri == MISS) return;
-    const Surf s = surface(S, h, o, d, tt);
-    Tan3 Jx;
-    float3 dt;
-    if (TAN) tan_plane_hit(Jo, Jd, d, s.ng, h.t, Jx, dt);
-    if (s.flags & VT_F_EMITTER) {
-      const float3 nE = emitter_normal(S, h, s, tt);
-      const float cosE = dot(-d, nE);
-      if (cosE > 0.0f) {
-        const float prof = profile(S, acosf(clampf(dot(-d, emitter_axis_at(S, tt)), -1.0f, 1.0f)));
-        float w = 1.0f;
-        if (b > 1) {
-          const float pL = h.t * h.t / (cosE * area);
-          w = pb_prev * pb_prev / (pb_prev * pb_prev + fnl * fnl * pL * pL);
-        }
-        P.emit_lamp = __ldg(C.emit_of_tri + h.tri);
-        P.emit_a = w * prof;
-        if (TAN) {
-          const float3 de = tan_emitter_hit(S, h, s, d, tt, b, pb_prev, dpb, fnl, area, Jd, Jx, dt) * __ldg(C.lamp + P.emit_lamp);
-          dL[0] = dL[0] + de * T.x; dL[1] = dL[1] + de * T.y; dL[2] = dL[2] + de * T.z;
-        }
-      }
-      return;
-    }
-    CalVertex& V = P.v[P.n];
-    V.mat = s.mat;
-    P.n++;
-    const float3 n = s.ns, wo = -d;
-    Tan3 Jn;
-    float3 Tr = T;
-    if (TAN) { Jn = tan_shading_normal(S, h, s, tt, Jx); Tr = mul3(T, alb(C, s.mat)); }
-    const float sh0 = b == 1 ? u01(pcg(hs + 3u)) : bounce_shift(hs, b, 0);
-    const float sh1 = b == 1 ? u01(pcg(hs + 4u)) : bounce_shift(hs, b, 1);
-    const float sh2 = b == 1 ? u01(pcg(hs + 5u)) : bounce_shift(hs, b, 2);
-    for (uint32_t j = 0; j < nl; j++) {
-      const float3 u = f3(kr(i * nl + j, KL0, sh0), kr(i * nl + j, KL1, sh1), kr(i * nl + j, KL2, sh2));
-      float3 lp, ln, la;
-      V.lamp[j] = sample_emitter_idx(S, u, tt, lp, ln, la);
-      V.q[j] = 0.0f;
-      float3 wi = lp - s.p;
-      const float d2 = dot(wi, wi), dist = sqrtf(d2);
-      wi = wi / dist;
-      const float cosE = dot(-wi, ln), cosS = dot(n, wi);
-      if (cosE <= 0.0f || cosS <= 0.0f || dot(s.ng, wi) <= 0.0f || dot(n, wo) <= 0.0f) continue;
-      const float prof = profile(S, acosf(clampf(dot(-wi, la), -1.0f, 1.0f)));
-      if (prof <= 0.0f) continue;
-      const float pdfW = d2 / (cosE * area), pb = cosS * INV_PI_F;
-      const float w = fnl * fnl * pdfW * pdfW / (fnl * fnl * pdfW * pdfW + pb * pb);
-      const Hit sh = trace_scene<true>(S, cp.root, offset_ray(s.p, s.ng, wi), wi, 0.0f, dist - 2e-5f, tt, 3u, skip_sh);
-      if (sh.tri == MISS) {
-        V.q[j] = prof * cosS * w * INV_PI_F / pdfW;
-        if (TAN) {
-          const float3 dq = tan_light(S, s.p, n, lp, ln, la, area, fnl, V.q[j], Jx, Jn) * (__ldg(C.lamp + V.lamp[j]) / fnl);
-          dL[0] = dL[0] + dq * Tr.x; dL[1] = dL[1] + dq * Tr.y; dL[2] = dL[2] + dq * Tr.z;
-        }
-      }
-    }
-    if (b == cp.max_depth) {
-      if (h.inst == MISS && h.tri < C.n_static_tris) P.node = __ldg(C.tri_node + h.tri);
-      return;
-    }
-    if (dot(n, wo) <= 0.0f) return;
-    const float u1 = b == 1 ? kr(i, KB1, u01(pcg(hs + 7u))) : kr(i, KB1, bounce_shift(hs, b, 4));
-    const float u2 = b == 1 ? kr(i, KB2, u01(pcg(hs + 8u))) : kr(i, KB2, bounce_shift(hs, b, 5));
-    const float3 t = basis_t(n), bb = basis_b(n);
-    const float r = sqrtf(u1);
-    float sp, cpz;
-    sincosf(2.0f * PI_F * u2, &sp, &cpz);
-    const float3 l = t * (r * cpz) + bb * (r * sp) + n * sqrtf(fmaxf(0.0f, 1.0f - u1));
-    const float cl = dot(n, l);
-    if (cl <= 0.0f || dot(s.ng, l) <= 0.0f) return;
-    pb_prev = cl * INV_PI_F;
-    if (TAN) {
-      const Tan3 Jl = tan_continue(n, Jn, r, cpz, sp, sqrtf(fmaxf(0.0f, 1.0f - u1)));
-      dpb = (tan_dot(l, Jn) + tan_dot(n, Jl)) * INV_PI_F;
-      Jo = Jx;
-      Jd = Jl;
-      T = Tr;
-    }
-    o = offset_ray(s.p, s.ng, l);
-    d = l;
-  }
-}
-
 // radiance of a recorded path
 __device__ __forceinline__ float3 path_value(const CalibDev& C, const CalPath& P, uint32_t nl) {
   float3 L = f3(0, 0, 0), T = f3(1, 1, 1);
@@ -296,12 +192,12 @@ __device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, u
   }
 }
 
-// ------------------------------------------------------------------------------------ wavefront form, stored paths
-// The same estimator as calib_path, split like the path tracer: the closest-hit kernel of the wavefront, then
-// calib_shade (one vertex: the record of the vertex, its light samples' unshadowed contributions and shadow
-// segments, the cosine continuation), then calib_shadow (any hit per light sample; an occluded sample's contribution
-// is cleared in the record). Each path's record (CalPath) stays in HBM, so the backward evaluates path_grad on the
-// records without tracing again. Records of path (i, id) of a camera sit at rec[i n_pix + id].
+// ------------------------------------------------------------------------------------ the wavefront estimator
+// The estimator split like the path tracer: the closest-hit kernel of the wavefront, then calib_shade (one vertex:
+// the record of the vertex, its light samples' unshadowed contributions and shadow segments, the cosine
+// continuation), then calib_shadow (any hit per light sample; an occluded sample's contribution is cleared in the
+// record). Each path's record (CalPath) stays in HBM, so the backward evaluates path_grad on the records without
+// tracing again. Records of path (i, id) of a camera's sub-samples [i0, i1) sit at rec[(i - i0) n_pix + id].
 constexpr int WT = 256;
 
 template <bool TAN>
@@ -515,8 +411,12 @@ __device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_
   for (int k = 0; k < 8; k++) atomicAdd(sh_k + k, G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k]);
 }
 
+// per pixel over the records of sub-samples [i0, i1): backward 0 adds their values to the pixel's running sum (kept in
+// the image between chunks; the chunk that ends at spp writes the image and the loss partials), 1 / 2 accumulate the
+// gradients (2: with the intrinsics' derivative)
 __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, const CalibDev C, const CalPath* __restrict__ rec,
-                                                          const CalTan* __restrict__ tan, uint32_t n_pix, int backward) {
+                                                          const CalTan* __restrict__ tan, uint32_t n_pix, int backward, uint32_t i0,
+                                                          uint32_t i1) {
   extern __shared__ double sm[];
   double* sh_alb = sm;
   double* sh_lamp = sm + 3 * C.n_mat;
@@ -537,17 +437,24 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
       const float4 I = C.image[px], Tg = C.target ? C.target[px] : make_float4(0.f, 0.f, 0.f, 0.f);
       const double k = 2.0 * C.inv_count * double(sc);
       const double3 g = make_double3(k * (double(I.x) - Tg.x), k * (double(I.y) - Tg.y), k * (double(I.z) - Tg.z));
-      for (uint32_t i = 0; i < cp.spp; i++) {
-        path_grad(C, rec[size_t(i) * n_pix + id], cp.n_light, g, sh_alb, sh_lamp);
+      for (uint32_t i = i0; i < i1; i++) {
+        const size_t r = size_t(i - i0) * n_pix + id;
+        path_grad(C, rec[r], cp.n_light, g, sh_alb, sh_lamp);
         if (backward == 2) {
           float3 dL[3];
-          path_tangent(C, rec[size_t(i) * n_pix + id], tan[size_t(i) * n_pix + id], cp.n_light, dL);
+          path_tangent(C, rec[r], tan[r], cp.n_light, dL);
           add_intrinsics_grad(cp, id, i, dL, g, sh_k);
         }
       }
     } else {
+      // the sum over sub-samples in order, carried across chunks exactly (a float in the image)
       float3 s = f3(0, 0, 0);
-      for (uint32_t i = 0; i < cp.spp; i++) s = s + path_value(C, rec[size_t(i) * n_pix + id], cp.n_light);
+      if (i0 > 0) s = xyz(C.image[px]);
+      for (uint32_t i = i0; i < i1; i++) s = s + path_value(C, rec[size_t(i - i0) * n_pix + id], cp.n_light);
+      if (i1 < cp.spp) {
+        C.image[px] = make_float4(s.x, s.y, s.z, 0.0f);
+        continue;
+      }
       const float4 I = make_float4(s.x * sc, s.y * sc, s.z * sc, 1.0f);
       C.image[px] = I;
       if (C.target) {
@@ -560,69 +467,6 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
   if (backward) {
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < 3 * C.n_mat; k += blockDim.x) if (sm[k] != 0.0) atomicAdd(C.g_albedo + k, sm[k]);
-    for (uint32_t k = threadIdx.x; k < C.n_lamps; k += blockDim.x) if (sh_lamp[k] != 0.0) atomicAdd(C.g_lamp + k, sh_lamp[k]);
-    if (backward == 2 && threadIdx.x < 8 && sh_k[threadIdx.x] != 0.0) atomicAdd(C.g_K + threadIdx.x, sh_k[threadIdx.x]);
-    return;
-  }
-  for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loss;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < CT / 32; w++) t += red[w];
-    C.partials[blockIdx.x] = t * C.inv_count;
-  }
-}
-
-__global__ void __launch_bounds__(CT) calib_kernel(const Scene S, const CamParams cp, const CalibDev C, uint32_t n_pix, int backward) {
-  extern __shared__ double sm[];
-  double* sh_alb = sm;                       // n_mat x 3
-  double* sh_lamp = sm + 3 * C.n_mat;        // n_lamps
-  __shared__ double red[CT / 32];
-  __shared__ double sh_k[8];
-  if (backward) {
-    for (uint32_t k = threadIdx.x; k < 3 * C.n_mat + C.n_lamps; k += blockDim.x) sm[k] = 0.0;
-    if (threadIdx.x < 8) sh_k[threadIdx.x] = 0.0;
-    __syncthreads();
-  }
-  double loss = 0.0;
-  const float sc = cp.scale / float(cp.spp);
-  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n_pix; id += gridDim.x * blockDim.x) {
-    uint32_t x, y;
-    if (!pixel_xy(cp, id, x, y)) continue;
-    const size_t px = size_t(y) * cp.w + x;
-    double3 g = make_double3(0.0, 0.0, 0.0);
-    if (backward) {
-      const float4 I = C.image[px], Tg = C.target ? C.target[px] : make_float4(0.f, 0.f, 0.f, 0.f);
-      const double k = 2.0 * C.inv_count * double(sc);
-      g = make_double3(k * (double(I.x) - Tg.x), k * (double(I.y) - Tg.y), k * (double(I.z) - Tg.z));
-    }
-    float3 s = f3(0, 0, 0);
-    for (uint32_t i = 0; i < cp.spp; i++) {
-      CalPath P;
-      if (backward == 2) {
-        float3 dL[3];
-        calib_path<true>(S, cp, C, id, i, P, dL);
-        add_intrinsics_grad(cp, id, i, dL, g, sh_k);
-      } else {
-        calib_path<false>(S, cp, C, id, i, P);
-      }
-      if (backward) path_grad(C, P, cp.n_light, g, sh_alb, sh_lamp);
-      else s = s + path_value(C, P, cp.n_light);
-    }
-    if (!backward) {
-      const float4 I = make_float4(s.x * sc, s.y * sc, s.z * sc, 1.0f);
-      C.image[px] = I;
-      if (C.target) {
-        const float4 Tg = C.target[px];
-        const double dx = double(I.x) - Tg.x, dy = double(I.y) - Tg.y, dz = double(I.z) - Tg.z;
-        loss += dx * dx + dy * dy + dz * dz;
-      }
-    }
-  }
-  if (backward) {
-    __syncthreads();
-    for (uint32_t k = threadIdx.x; k < 3 * C.n_mat; k += blockDim.x) if (sh_alb[k] != 0.0) atomicAdd(C.g_albedo + k, sh_alb[k]);
     for (uint32_t k = threadIdx.x; k < C.n_lamps; k += blockDim.x) if (sh_lamp[k] != 0.0) atomicAdd(C.g_lamp + k, sh_lamp[k]);
     if (backward == 2 && threadIdx.x < 8 && sh_k[threadIdx.x] != 0.0) atomicAdd(C.g_K + threadIdx.x, sh_k[threadIdx.x]);
     return;
@@ -762,18 +606,17 @@ size_t calib_record_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalPat
 
 size_t calib_tan_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalTan); }
 
-uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records, void* tangents,
-                            int blocks, cudaStream_t st) {
-  CalPath* rec = static_cast<CalPath*>(records);
-  CalTan* tan = static_cast<CalTan*>(tangents);
+// the paths of sub-samples [i0, i1) of the camera through the wavefront, their records at rec[(i - i0) n_pix + id]
+static void calib_trace(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, CalPath* rec, CalTan* tan,
+                        uint32_t i0, uint32_t i1, int blocks, cudaStream_t st) {
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
-  const uint32_t per_wave = std::max(1u, std::min(cp.spp, wave_paths / std::max(1u, n_pix)));
-  for (uint32_t i0 = 0; i0 < cp.spp; i0 += per_wave) {
-    const uint32_t n_i = std::min(per_wave, cp.spp - i0);
+  const uint32_t per_wave = std::max(1u, std::min(i1 - i0, wave_paths / std::max(1u, n_pix)));
+  for (uint32_t w0 = i0; w0 < i1; w0 += per_wave) {
+    const uint32_t n_i = std::min(per_wave, i1 - w0);
     cudaMemsetAsync(wb.counts, 0, 16, st);
-    launch_wave_gen(cp, wb, i0, n_i, n_pix, blocks, st);
-    CalPath* rb = rec + size_t(i0) * n_pix;
-    CalTan* tb = tan ? tan + size_t(i0) * n_pix : nullptr;
+    launch_wave_gen(cp, wb, w0, n_i, n_pix, blocks, st);
+    CalPath* rb = rec + size_t(w0 - i0) * n_pix;
+    CalTan* tb = tan ? tan + size_t(w0 - i0) * n_pix : nullptr;
     for (uint32_t b = 1; b <= cp.max_depth; b++) {
       WaveBufs w = wb;
       w.q_in = (b & 1) ? wb.qa : wb.qb;
@@ -791,8 +634,22 @@ uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev&
       else calib_shadow_kernel<false><<<blocks, WT, 0, st>>>(S, cp, w, rb, nullptr);
     }
   }
+}
+
+uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records, void* tangents,
+                            int blocks, cudaStream_t st) {
+  return calib_wave_chunk(S, cp, C, wb, wave_paths, records, tangents, 0, cp.spp, 0, blocks, st);
+}
+
+uint32_t calib_wave_chunk(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records, void* tangents,
+                          uint32_t i0, uint32_t i1, int mode, int blocks, cudaStream_t st) {
+  CalPath* rec = static_cast<CalPath*>(records);
+  CalTan* tan = static_cast<CalTan*>(tangents);
+  calib_trace(S, cp, C, wb, wave_paths, rec, tan, i0, i1, blocks, st);
+  const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
-  calib_records_kernel<<<grid, CT, 0, st>>>(cp, C, rec, tan, n_pix, 0);
+  const size_t smem = mode ? size_t(3 * C.n_mat + C.n_lamps) * 8 : 0;
+  calib_records_kernel<<<grid, CT, smem, st>>>(cp, C, rec, tan, n_pix, mode, i0, i1);
   return grid;
 }
 
@@ -800,7 +657,8 @@ void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* 
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
   calib_records_kernel<<<grid, CT, size_t(3 * C.n_mat + C.n_lamps) * 8, st>>>(cp, C, static_cast<const CalPath*>(records),
-                                                                             static_cast<const CalTan*>(tangents), n_pix, tangents ? 2 : 1);
+                                                                             static_cast<const CalTan*>(tangents), n_pix, tangents ? 2 : 1,
+                                                                             0, cp.spp);
 }
 
 // per path of the camera's records, in (row, column, sub-sample) order: the triangle and instance of each bounce
@@ -825,14 +683,6 @@ void calib_export_paths(const CamParams& cp, const void* records, const void* ta
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   calib_export_paths_kernel<<<(n_pix + 127) / 128, 128, 0, st>>>(cp, static_cast<const CalPath*>(records), static_cast<const CalTan*>(tangents),
                                                                 n_pix, tri_inst, q);
-}
-
-uint32_t launch_calib(const Scene& S, const CamParams& cp, const CalibDev& C, int mode, int blocks, cudaStream_t st) {
-  const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
-  const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
-  const size_t smem = mode ? size_t(3 * C.n_mat + C.n_lamps) * 8 : 0;
-  calib_kernel<<<grid, CT, smem, st>>>(S, cp, C, n_pix, mode);
-  return grid;
 }
 
 void launch_direct_transfer(const Scene& S, const float* centres, const float* normals, uint32_t n, uint32_t n_lamps, uint32_t samples, float* D,

@@ -39,11 +39,13 @@ void calib_records_backward(const CamParams& cp, const CalibDev& C, const void* 
 // the recorded paths' discrete decisions (for checking): per path in (row, column, sub-sample) order, CAL_MAX_DEPTH x
 // (triangle, instance) and CAL_MAX_DEPTH x CAL_MAX_NL light-sample weights q (0: occluded or no contribution)
 void calib_export_paths(const CamParams& cp, const void* records, const void* tangents, uint32_t* tri_inst, float* q, cudaStream_t st);
-// replay form, forward: image + per-block loss partials (returns the number of partials); backward: gradients of the
-// image loss, every path traced again from its sample numbers
-// mode 0 forward, 1 backward (albedos, emitter radiances, node light), 2 the backward and the derivative in the
-// camera's intrinsics (C.g_K)
-uint32_t launch_calib(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, int mode, int blocks, cudaStream_t st);
+// replay form: the paths of the camera's sub-samples [i0, i1) traced into `records` (and `tangents`, NULL: none) at
+// records[(i - i0) n_pix + id], then mode 0 adds their values to the image (the chunk ending at spp writes the image
+// and the per-block loss partials, whose number it returns), 1 accumulates the gradients of the image loss
+// (albedos, emitter radiances, node light), 2 also the derivative in the camera's intrinsics (C.g_K). The image of
+// the forward's chunks is the stored form's image bit for bit.
+uint32_t calib_wave_chunk(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records,
+                          void* tangents, uint32_t i0, uint32_t i1, int mode, int blocks, cudaStream_t st);
 // D[i][t]: irradiance at node i (centre, normal) from emitter triangle t at unit radiance, with visibility
 void launch_direct_transfer(const vtd::Scene& S, const float* centres, const float* normals, uint32_t n, uint32_t n_lamps,
                             uint32_t samples, float* D, cudaStream_t st);

@@ -120,6 +120,8 @@ struct vt_ctx {
     double* g_K = nullptr;   // 8 per scene camera
     std::vector<size_t> rec_off;
     bool stored = false;
+    // replay form: sub-samples per chunk and the wave size of the tracing
+    uint32_t chunk = 0, wave_paths = 0;
     // last forward
     std::vector<uint32_t> cams;
     uint32_t spp = 0, nl = 0, seed = 0, depth = 0, iters = 0;

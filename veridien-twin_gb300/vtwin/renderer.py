@@ -494,7 +494,9 @@ class TwinRenderer:
                       images=True, replay=False, intrinsics=False):
         """Image loss (mean of (I - T)^2 over pixels and channels) of the calibration render; returns (loss, images)
         with images a list of (h, w, 4) float32 arrays per camera (or None). intrinsics: the backward also gives the
-        loss's derivative in each camera's KB4 intrinsics (calib_intrinsics_grad)."""
+        loss's derivative in each camera's KB4 intrinsics (calib_intrinsics_grad). replay: False keeps every path's
+        record when they fit; True traces the paths again in chunks of sub-samples sized to the free memory; an
+        integer c >= 1 traces them again in chunks of at most c sub-samples."""
         cams = [self._cam(c) for c in cameras]
         cam_arr = np.ascontiguousarray(cams, np.uint32)
         alb = np.ascontiguousarray(albedo, np.float64).reshape(-1, 3)
@@ -509,7 +511,7 @@ class TwinRenderer:
                            light_samples=int(lightSamples), seed=int(seed), max_depth=int(max_depth), jacobi_iters=int(jacobi_iters),
                            albedo=alb.ctypes.data_as(C.POINTER(C.c_double)), lamp=lam.ctypes.data_as(C.POINTER(C.c_double)),
                            targets=tg.ctypes.data_as(C.POINTER(C.c_float)) if tg is not None else None,
-                           images=img.ctypes.data_as(C.POINTER(C.c_float)) if img is not None else None, replay=int(bool(replay)),
+                           images=img.ctypes.data_as(C.POINTER(C.c_float)) if img is not None else None, replay=0 if replay is False else 1 if replay is True else 1 + int(replay),
                            intrinsics=int(bool(intrinsics)))
         loss = C.c_double(0.0)
         check(self.lib.vt_calib_forward(self._ctx, C.byref(q), C.byref(loss)), self._ctx)
