@@ -606,7 +606,7 @@ vt_status vt_lite_debug(vt_ctx* ctx, int what, uint32_t camera, void* dst, size_
 vt_status vt_raster(vt_ctx* ctx, const float* clip, uint32_t n_verts, const uint32_t* idx, uint32_t n_tris, uint32_t width,
                     uint32_t height, uint32_t samples, uint64_t* keys);
 
-/* ------------------------------------------------------------------ scene preparation (host, no device) */
+/* ------------------------------------------------------------------ scene preparation */
 
 /* The mesh clean-up the reference runs in JavaScript before packing (gpu/scene_gpu.js), for callers that load a
  * scene directory (scene.json + meshes/\*.bin): results are library-owned until vt_mesh_free. Positions and normals
@@ -626,6 +626,12 @@ vt_status vt_weld(const float* P, const float* N, uint32_t n_verts, const uint32
  * triangle by its pattern of split edges, until no edge is longer than h or after max_passes (24). */
 vt_status vt_subdivide(const double* P, const double* N, uint32_t n_verts, const uint32_t* I, uint32_t n_idx, double h, uint32_t max_passes,
                        vt_mesh_out* out);
+/* The same weld and subdivide on a CUDA device: identical vertices, numbering and triangles, host buffers in and out.
+ * First-met numbering becomes a sort of (key, input position) pairs whose runs lead with the first occurrence, and
+ * a scan of the leads in input order; the arithmetic is the host's, in doubles without contraction. */
+vt_status vt_weld_device(int32_t device, const float* P, const float* N, uint32_t n_verts, const uint32_t* I, uint32_t n_idx, vt_mesh_out* out);
+vt_status vt_subdivide_device(int32_t device, const double* P, const double* N, uint32_t n_verts, const uint32_t* I, uint32_t n_idx, double h,
+                              uint32_t max_passes, vt_mesh_out* out);
 /* gpu/scene_gpu.js:146 benchMesh: a grid of cells <= h over `fine` (x0, y0, x1, y1) within `extent` and four coarse
  * quads out to the extent, at height z, normal +z. */
 vt_status vt_bench_mesh(double z, const double extent[4], const double fine[4], double h, vt_mesh_out* out);

@@ -11,6 +11,8 @@
 
 #include "../../include/vtwin.h"
 
+#include "vt_scene_prep.h"
+
 namespace {
 
 struct Buf {
@@ -62,6 +64,16 @@ struct Key6Hash {
 };
 
 }  // namespace
+
+namespace vt {
+vt_status mesh_hand_out(std::vector<double>&& P, std::vector<double>&& N, std::vector<uint32_t>&& I, vt_mesh_out* out) {
+  Buf b;
+  b.P = std::move(P);
+  b.N = std::move(N);
+  b.I = std::move(I);
+  return hand_out(std::move(b), out);
+}
+}  // namespace vt
 
 extern "C" {
 

@@ -95,7 +95,7 @@ const cat = (T, parts) => { const n = parts.reduce((a, p) => a + p.length, 0); c
  * library's weld / subdivide, the reference's arithmetic), the bench, posed bodies by bodyOfPart in the body frame,
  * the mesh table, materials and the emitter from physics, the KB4 cameras. gpu/scene_gpu.js:241-330.
  */
-export function prepareDesc(scene, meshData, physics, { nodeSpacing = 0.003 } = {}) {
+export function prepareDesc(scene, meshData, physics, { nodeSpacing = 0.003, device = -1 } = {}) {
   const bodies = bodyOfPart(scene);
   const benchMat = scene.bench?.material || 'bench_white';
   const matNames = [], matIndex = {};
@@ -117,8 +117,8 @@ export function prepareDesc(scene, meshData, physics, { nodeSpacing = 0.003 } = 
     const lay = materials[matIndex[m.material]].layer;
     const flags = MESH_FLAG.STATIC | (m.build_dir && lay && lay[1] > 0 ? MESH_FLAG.LAYER : 0);
     const mid = addMesh(m.name, m.material, flags, m.build_dir);
-    const w = addon.weld(d.P, d.N, d.I);
-    const s = addon.subdivide(w.P, w.N, w.I, nodeSpacing, 24);
+    const w = addon.weld(d.P, d.N, d.I, device);
+    const s = addon.subdivide(w.P, w.N, w.I, nodeSpacing, 24, device);
     sP.push(Float32Array.from(s.P)); sN.push(Float32Array.from(s.N));
     sI.push(Uint32Array.from(s.I, (i) => i + nv)); sTM.push(new Uint32Array(s.I.length / 3).fill(mid)); sVM.push(new Uint32Array(s.P.length / 3).fill(mid));
     for (let i = 0; i < s.P.length; i += 3) {
@@ -189,7 +189,7 @@ export class TwinRenderer {
     const loaded = typeof opts.scene === 'string' ? await loadScene(opts.scene) : opts.scene;
     r.scene = loaded.scene;
     r.physics = opts.physics || {};
-    r.desc = prepareDesc(loaded.scene, loaded.meshes, r.physics, { nodeSpacing: r.opts.nodeSpacing });
+    r.desc = prepareDesc(loaded.scene, loaded.meshes, r.physics, { nodeSpacing: r.opts.nodeSpacing, device: opts.device ?? 0 });
     r.ctx = addon.create(r.desc, { leafSize: r.opts.leafSize, albedoSamples: 1024, device: opts.device ?? 0 });
     r.cameras = {};
     r.desc.cameras.forEach((c, i) => { r.cameras[c.name] = { index: i, size: [c.width, c.height], lens: c.lens, manual: null, awb: null }; });

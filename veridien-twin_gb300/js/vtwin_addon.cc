@@ -932,28 +932,35 @@ napi_value mesh_result(napi_env env, vt_mesh_out& m) {
   return o;
 }
 
-// weld(P: Float32Array, N: Float32Array, I: Uint32Array) -> {P, N, I} (gpu/scene_gpu.js:68)
+// weld(P: Float32Array, N: Float32Array, I: Uint32Array, device?) -> {P, N, I} (gpu/scene_gpu.js:68); with a CUDA
+// device ordinal the weld runs there (the same result)
 napi_value Weld(napi_env env, napi_callback_info info) {
   Args a(env, info);
   size_t bp = 0, bi = 0;
   const float* P = static_cast<const float*>(data_of(env, a.v[0], &bp));
   const float* N = static_cast<const float*>(data_of(env, a.v[1]));
   const uint32_t* I = static_cast<const uint32_t*>(data_of(env, a.v[2], &bi));
+  const int device = a.n > 3 ? int(f64v(env, a.v[3])) : -1;
   vt_mesh_out m{};
-  if (throw_status(env, vt_weld(P, N, uint32_t(bp / 12), I, uint32_t(bi / 4), &m), nullptr)) return nullptr;
+  const vt_status st = device >= 0 ? vt_weld_device(device, P, N, uint32_t(bp / 12), I, uint32_t(bi / 4), &m)
+                                   : vt_weld(P, N, uint32_t(bp / 12), I, uint32_t(bi / 4), &m);
+  if (throw_status(env, st, nullptr)) return nullptr;
   return mesh_result(env, m);
 }
 
-// subdivide(P: Float64Array, N: Float64Array, I: Uint32Array, h, maxPasses) -> {P, N, I} (gpu/scene_gpu.js:93)
+// subdivide(P: Float64Array, N: Float64Array, I: Uint32Array, h, maxPasses, device?) -> {P, N, I} (gpu/scene_gpu.js:93)
 napi_value Subdivide(napi_env env, napi_callback_info info) {
   Args a(env, info);
   size_t bp = 0, bi = 0;
   const double* P = static_cast<const double*>(data_of(env, a.v[0], &bp));
   const double* N = static_cast<const double*>(data_of(env, a.v[1]));
   const uint32_t* I = static_cast<const uint32_t*>(data_of(env, a.v[2], &bi));
+  const uint32_t passes = a.n > 4 ? u32v(env, a.v[4]) : 24;
+  const int device = a.n > 5 ? int(f64v(env, a.v[5])) : -1;
   vt_mesh_out m{};
-  if (throw_status(env, vt_subdivide(P, N, uint32_t(bp / 24), I, uint32_t(bi / 4), f64v(env, a.v[3]), a.n > 4 ? u32v(env, a.v[4]) : 24, &m), nullptr))
-    return nullptr;
+  const vt_status st = device >= 0 ? vt_subdivide_device(device, P, N, uint32_t(bp / 24), I, uint32_t(bi / 4), f64v(env, a.v[3]), passes, &m)
+                                   : vt_subdivide(P, N, uint32_t(bp / 24), I, uint32_t(bi / 4), f64v(env, a.v[3]), passes, &m);
+  if (throw_status(env, st, nullptr)) return nullptr;
   return mesh_result(env, m);
 }
 

@@ -35,6 +35,9 @@ SIGNATURES = {
     "vt_render_frame": (C.c_int32, [C.c_void_p, C.POINTER(A.vt_frame_req)]),
     "vt_weld": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(A.vt_mesh_out)]),
     "vt_subdivide": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_double, C.c_uint32, C.POINTER(A.vt_mesh_out)]),
+    "vt_weld_device": (C.c_int32, [C.c_int32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(A.vt_mesh_out)]),
+    "vt_subdivide_device": (C.c_int32, [C.c_int32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_double, C.c_uint32,
+                                        C.POINTER(A.vt_mesh_out)]),
     "vt_bench_mesh": (C.c_int32, [C.c_double, C.c_void_p, C.c_void_p, C.c_double, C.POINTER(A.vt_mesh_out)]),
     "vt_compute_normals": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
     "vt_mesh_free": (None, [C.POINTER(A.vt_mesh_out)]),

@@ -22,9 +22,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr"]
 
 
-# per-file flags: the sensor chain, the rasteriser and the BVH builder are compiled without multiply-add
+# per-file flags: the sensor chain, the rasteriser, the BVH builder and the scene preparation are compiled without multiply-add
 # contraction, so their arithmetic is the sequence of separately rounded operations that the CPU code performs
-EXTRA = {"vt_isp.cu": ["--fmad=false"], "vt_lite_raster.cu": ["--fmad=false"], "vt_bvh_gpu.cu": ["--fmad=false"],
+EXTRA = {"vt_isp.cu": ["--fmad=false"], "vt_lite_raster.cu": ["--fmad=false"], "vt_bvh_gpu.cu": ["--fmad=false"], "vt_scene_gpu.cu": ["--fmad=false"],
          # the raster pass's shading: WGSL's own f32 precision (division 2.5 ulp, inverseSqrt 2 ulp), not IEEE division
          "vt_lite.cu": ["--use_fast_math"]}
 

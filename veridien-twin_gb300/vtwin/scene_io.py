@@ -1,8 +1,9 @@
 """Loading a twin scene directory (scene.json + meshes/*.bin) into the scene dict that TwinRenderer.create takes:
 the front half of gpu/scene_gpu.js:241 prepareScene (static meshes welded and subdivided to the node spacing, the
 bench mesh, bodies by bodyOfPart, the mesh table and its flags, materials and the emitter from physics), with the
-mesh clean-up in libvtwin (vt_weld, vt_subdivide, vt_bench_mesh, vt_compute_normals: host code, no device). The
-packing, BVHs, capsules and albedo tables are vt_create's.
+mesh clean-up in libvtwin (vt_weld, vt_subdivide, vt_bench_mesh, vt_compute_normals on the host; weld and subdivide
+also on a CUDA device, vt_weld_device / vt_subdivide_device, with identical results). The packing, BVHs, capsules and
+albedo tables are vt_create's.
 """
 from __future__ import annotations
 
@@ -40,23 +41,31 @@ def _p(a):
 
 
 # ------------------------------------------------------------------------------------------- mesh clean-up
-def weld(P, N, I):
-    """gpu/scene_gpu.js:68 weld: vertices merged by position (1e-7 m) and normal (1e-4); float64 out."""
+def weld(P, N, I, device=None):
+    """gpu/scene_gpu.js:68 weld: vertices merged by position (1e-7 m) and normal (1e-4); float64 out. device: a CUDA
+    ordinal to weld on (the same result), None for the host."""
     P = np.ascontiguousarray(P, np.float32).reshape(-1, 3)
     N = np.ascontiguousarray(N, np.float32).reshape(-1, 3)
     I = np.ascontiguousarray(I, np.uint32).ravel()
     out = A.vt_mesh_out()
-    check(load().vt_weld(_p(P), _p(N), len(P), _p(I), len(I), C.byref(out)))
+    if device is None:
+        check(load().vt_weld(_p(P), _p(N), len(P), _p(I), len(I), C.byref(out)))
+    else:
+        check(load().vt_weld_device(int(device), _p(P), _p(N), len(P), _p(I), len(I), C.byref(out)))
     return _take(out)
 
 
-def subdivide(P, N, I, h, max_passes=24):
-    """gpu/scene_gpu.js:95 subdivide: conforming edge bisection until every edge is <= h."""
+def subdivide(P, N, I, h, max_passes=24, device=None):
+    """gpu/scene_gpu.js:95 subdivide: conforming edge bisection until every edge is <= h. device: a CUDA ordinal to
+    subdivide on (the same result), None for the host."""
     P = np.ascontiguousarray(P, np.float64).reshape(-1, 3)
     N = np.ascontiguousarray(N, np.float64).reshape(-1, 3)
     I = np.ascontiguousarray(I, np.uint32).ravel()
     out = A.vt_mesh_out()
-    check(load().vt_subdivide(_p(P), _p(N), len(P), _p(I), len(I), float(h), int(max_passes), C.byref(out)))
+    if device is None:
+        check(load().vt_subdivide(_p(P), _p(N), len(P), _p(I), len(I), float(h), int(max_passes), C.byref(out)))
+    else:
+        check(load().vt_subdivide_device(int(device), _p(P), _p(N), len(P), _p(I), len(I), float(h), int(max_passes), C.byref(out)))
     return _take(out)
 
 
@@ -194,8 +203,9 @@ def _emitter(physics: dict | None) -> dict:
             "axis_deg": float("nan") if ax is None else float(ax)}
 
 
-def prepare_scene(scene: dict, meshes: dict, physics: dict | None = None, node_spacing: float = 0.003) -> dict:
-    """gpu/scene_gpu.js:241 prepareScene up to the packing: the scene dict of vtwin.dome's form."""
+def prepare_scene(scene: dict, meshes: dict, physics: dict | None = None, node_spacing: float = 0.003, device: int | None = None) -> dict:
+    """gpu/scene_gpu.js:241 prepareScene up to the packing: the scene dict of vtwin.dome's form. device: a CUDA ordinal
+    to weld and subdivide on (the same scene), None for the host."""
     bodies = _body_of_part(scene)
     metas = list(scene["meshes"])
     bench_mat = (scene.get("bench") or {}).get("material") or "bench_white"
@@ -227,8 +237,8 @@ def prepare_scene(scene: dict, meshes: dict, physics: dict | None = None, node_s
         lay = mat.get("layer")
         flags = MESH_FLAG["STATIC"] | (MESH_FLAG["LAYER"] if m.get("build_dir") and lay and lay[1] > 0 else 0)
         mid = add_mesh(m["name"], m["material"], flags, m.get("build_dir"))
-        P, N, I = weld(d["P"], d["N"], d["I"])
-        P, N, I = subdivide(P, N, I, node_spacing)
+        P, N, I = weld(d["P"], d["N"], d["I"], device=device)
+        P, N, I = subdivide(P, N, I, node_spacing, device=device)
         sP.append(P); sN.append(N); sI.append(I.reshape(-1, 3) + nv)
         sTM.append(np.full(len(I) // 3, mid, np.uint32)); sVM.append(np.full(len(P), mid, np.uint32))
         nv += len(P)
@@ -299,7 +309,7 @@ def prepare_scene(scene: dict, meshes: dict, physics: dict | None = None, node_s
             "cameras": cams, "scope": scene.get("scope")}
 
 
-def load_scene(path: str, physics: dict | None = None, node_spacing: float = 0.003) -> dict:
+def load_scene(path: str, physics: dict | None = None, node_spacing: float = 0.003, device: int | None = None) -> dict:
     """A scene directory to the scene dict: load_scene_dir + prepare_scene."""
     scene, meshes = load_scene_dir(path)
-    return prepare_scene(scene, meshes, physics, node_spacing)
+    return prepare_scene(scene, meshes, physics, node_spacing, device=device)
