@@ -148,6 +148,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   cudaFree(ctx->calib.mem);
   cudaFree(ctx->nodes.mem);
   cudaFree(ctx->nodes.table_mem);
+  cudaFree(ctx->nodes.direct_mem);
   cudaFree(ctx->calib.records);
   cudaFree(ctx->calib.tan);
   for (float4* p : ctx->calib.image) cudaFree(p);

@@ -67,6 +67,7 @@ vt_status vt_nodes_build(vt_ctx* ctx, const vt_nodes_opts* opts, vt_nodes_info* 
   VT_CK(cudaStreamSynchronize(ctx->stream));
   cudaFree(N.mem);
   cudaFree(N.table_mem);
+  cudaFree(N.direct_mem);
   N = vt_ctx::Nodes{};
   if (cudaMalloc(&N.mem, b_g + b_aux + b_act + b_nbr + b_amu) != cudaSuccess) {
     cudaGetLastError();
@@ -107,6 +108,11 @@ vt_status vt_nodes_build(vt_ctx* ctx, const vt_nodes_opts* opts, vt_nodes_info* 
     if (aux[i].x <= 0.5f * float(K)) N.active_h.push_back(i);
   }
   N.n_active = uint32_t(N.active_h.size());
+  if (cudaMalloc(&N.direct_mem, vtk::node_direct_bytes(N.n_active, o.node_samples)) != cudaSuccess) {
+    cudaGetLastError();
+    N.direct_mem = nullptr;
+    return fail(ctx, VT_ERR_OOM, "nodes: direct-light buffers");
+  }
   const auto t0 = std::chrono::steady_clock::now();
   std::vector<uint32_t> nbr;
   vt::node_neighbours(ctx->S, N.active_h, o.nbr_k, double(o.smooth_radius), double(o.smooth_sigma), nbr);
@@ -154,7 +160,8 @@ vt_status vt_nodes_direct(vt_ctx* ctx, uint32_t moved) {
   if (!ctx) return VT_ERR_ARG;
   if (!ctx->nodes.built) return fail(ctx, VT_ERR_ARG, "nodes: vt_nodes_build first");
   VT_CK(cudaEventRecord(ctx->nev[0], ctx->stream));
-  vtk::launch_node_direct(dev_scene(ctx), ctx->nodes.active, ctx->nodes.n_active, ctx->nodes.o.node_samples, moved, ctx->d_nstate, ctx->stream);
+  vtk::launch_node_direct(dev_scene(ctx), ctx->nodes.active, ctx->nodes.n_active, ctx->nodes.o.node_samples, moved, ctx->d_nstate,
+                          ctx->nodes.direct_mem, ctx->wave_blocks, ctx->stream);
   VT_CK(cudaGetLastError());
   VT_CK(cudaEventRecord(ctx->nev[1], ctx->stream));
   ctx->nodes.timed_direct = true;

@@ -140,6 +140,7 @@ struct vt_ctx {
     uint2* nbr = nullptr;
     float4* amu = nullptr;
     void* table_mem = nullptr;               // transport table: row offsets, then entries
+    void* direct_mem = nullptr;              // the direct light's shadow rays and terms (node_direct_bytes)
     uint32_t* row = nullptr;
     float4* ent = nullptr;
     uint64_t nnz = 0;

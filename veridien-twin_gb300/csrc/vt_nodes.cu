@@ -12,6 +12,10 @@
 #include "vt_kernels.cuh"
 #include "vt_nodes.cuh"
 
+#ifndef VT_NODE_TRACE_BLOCKS
+#define VT_NODE_TRACE_BLOCKS 4   // blocks of 256 per SM the persistent shadow lanes are compiled for (64 registers)
+#endif
+
 namespace vtk {
 
 using namespace vtd;
@@ -110,13 +114,38 @@ __global__ void amu_kernel(const Scene S, uint32_t n_mat, uint32_t K, float4* __
 // visibility code (1 all lit samples visible, 0 none, 0.5 mixed, -1 no lit sample) and the capsule visibility V.
 // moved != 0: only nodes whose segment to the emitter passes near a moved body's bounding capsule, now or at the
 // last full update.
-__global__ void node_direct_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t NS, uint32_t moved,
-                                   float4* __restrict__ nstate) {
-  const uint32_t skip = ldu(S.su + 7);
+//
+// In three passes, so that the shadow rays run on persistent traversal lanes: node_direct_setup (one thread per
+// (node, sample): the sample, its unshadowed term and its shadow ray, queued when the sample is lit),
+// node_direct_shadow (any hit of the queued rays) and node_direct_sum (per node: the visible terms added in sample
+// order, the codes). Every value is the one-pass estimator's: the shadow answers do not depend on the order rays are
+// traced in, and each node's terms are added in sample order.
+namespace {
+constexpr uint32_t ND_LIT = 1u, ND_VIS = 2u, ND_RUN = 4u;
+
+// append `want` lanes' items to a queue with one atomic per warp; returns the slot of this lane (if want)
+__device__ __forceinline__ uint32_t node_append(uint32_t* count, bool want) {
+  const uint32_t act = __activemask();
+  const uint32_t mask = __ballot_sync(act, want);
+  if (!mask) return 0;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, uint32_t(__popc(mask)));
+  base = __shfl_sync(act, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+}  // namespace
+
+__global__ void __launch_bounds__(256) node_direct_setup(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t NS,
+                                                         uint32_t moved, NodeDirectBufs b) {
   const float area = __ldg(S.su + 3);
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_active; k += gridDim.x * blockDim.x) {
+  const size_t total = size_t(n_active) * NS;
+  for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += size_t(gridDim.x) * blockDim.x) {
+    const uint32_t k = uint32_t(t / NS), s = uint32_t(t % NS);
     const uint32_t i = active[k];
     const float3 p = node_pos(S, i), n = node_nrm(S, i);
+    bool run = true;
     if (moved) {
       Rot R;
       float3 pp;
@@ -125,80 +154,16 @@ __global__ void node_direct_kernel(const Scene S, const uint32_t* __restrict__ a
       const float rr = __ldg(S.su + 23) + 1e-3f;
       bool near = false;
       const uint32_t cnt = min(ldu(S.su + 16), uint32_t(VT_MAX_INST));
-      for (uint32_t b = 0; b < cnt && !near; b++) {
-        if (!((moved >> b) & 1u)) continue;
-        const float* I = inst_rec(S, b);
-        near = seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 32), ld3(I + 36), __ldg(I + 35) + rr) ||
-               seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 40), ld3(I + 44), __ldg(I + 43) + rr);
-      }
-      if (!near) continue;
-    }
-    const uint32_t m = node_mat(S, i);
-    const uint32_t hs = pcg(i * 2246822519u + 3u);
-    const float s0 = u01(pcg(hs)), s1 = u01(pcg(hs + 1u)), s2 = u01(pcg(hs + 2u));
-    float3 B = f3(0, 0, 0);
-    uint32_t n_lit = 0, n_vis = 0;
-    const float3 o = p + n * EPS_OFF;
-    for (uint32_t s = 0; s < NS; s++) {
-      float3 lp, ln, la;
-      sample_emitter(S, f3(kr(s, KL0, s0), kr(s, KL1, s1), kr(s, KL2, s2)), 0.5f, lp, ln, la);
-      float3 wi = lp - p;
-      const float d2 = dot(wi, wi), dist = sqrtf(d2);
-      wi = wi / dist;
-      const float cosE = dot(-wi, ln), cosN = dot(n, wi);
-      if (cosE <= 0.0f || cosN <= 0.0f) continue;
-      const float3 Le = emitted(S, ln, la, -wi);
-      if (maxc(Le) <= 0.0f) continue;
-      n_lit++;
-      if (trace_scene<true>(S, 0u, o, wi, 0.0f, dist - 2e-5f, 0.5f, 3u, skip).tri != MISS) continue;
-      n_vis++;
-      B = B + Le * (cosE * cosN * area / d2) * albedo(S, m, cosN);
-    }
-    B = B / float(NS);
-    const float vis = n_lit == 0 ? -1.0f : n_vis == n_lit ? 1.0f : n_vis == 0 ? 0.0f : 0.5f;
-    nstate[4u * i + 3u] = make_float4(B.x, B.y, B.z, vis);
-    const float4 old = nstate[4u * i];
-    nstate[4u * i] = make_float4(old.x, old.y, old.z, capsule_vis(S, p, n));
-  }
-}
-
-// The same with one thread per (node, emitter sample): G = NS threads of a warp share a node (NS divides 32), each
-// traces one shadow ray, and the node's first lane adds the group's terms in sample order as the loop above does.
-template <uint32_t G>
-__global__ void __launch_bounds__(256) node_direct_group_kernel(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t moved,
-                                                                float4* __restrict__ nstate) {
-  const uint32_t skip = ldu(S.su + 7);
-  const float area = __ldg(S.su + 3);
-  const uint32_t lane = threadIdx.x & 31u, s = lane % G, lead = lane - s;
-  const size_t total = size_t(n_active) * G;
-  const size_t stride = size_t(gridDim.x) * blockDim.x;
-  // whole warps iterate together (the shuffles below need every lane)
-  for (size_t base = size_t(blockIdx.x) * blockDim.x + (threadIdx.x - lane); base < total; base += stride) {
-    const size_t t = base + lane;
-    const bool in = t < total;
-    const uint32_t k = in ? uint32_t(t / G) : 0u;
-    const uint32_t i = in ? active[k] : 0u;
-    const float3 p = node_pos(S, i), n = node_nrm(S, i);
-    bool run = in;
-    if (in && moved) {
-      Rot R;
-      float3 pp;
-      inst_pose(S, ldu(S.su + 17), 0.5f, R, pp);
-      const float3 dE = (rmul(R, ld3(S.su + 20)) + pp) - p;
-      const float rr = __ldg(S.su + 23) + 1e-3f;
-      bool near = false;
-      const uint32_t cnt = min(ldu(S.su + 16), uint32_t(VT_MAX_INST));
-      for (uint32_t b = 0; b < cnt && !near; b++) {
-        if (!((moved >> b) & 1u)) continue;
-        const float* I = inst_rec(S, b);
+      for (uint32_t bb = 0; bb < cnt && !near; bb++) {
+        if (!((moved >> bb) & 1u)) continue;
+        const float* I = inst_rec(S, bb);
         near = seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 32), ld3(I + 36), __ldg(I + 35) + rr) ||
                seg_near_capsule(p, dE, 0.0f, 1.0f, ld3(I + 40), ld3(I + 44), __ldg(I + 43) + rr);
       }
       run = near;
     }
+    uint32_t flags = run ? ND_RUN : 0u;
     float3 c = f3(0, 0, 0);
-    uint32_t lit = 0, vis = 0;
-    const uint32_t m = run ? node_mat(S, i) : 0u;
     if (run) {
       const uint32_t hs = pcg(i * 2246822519u + 3u);
       const float s0 = u01(pcg(hs)), s1 = u01(pcg(hs + 1u)), s2 = u01(pcg(hs + 2u));
@@ -211,32 +176,71 @@ __global__ void __launch_bounds__(256) node_direct_group_kernel(const Scene S, c
       if (cosE > 0.0f && cosN > 0.0f) {
         const float3 Le = emitted(S, ln, la, -wi);
         if (maxc(Le) > 0.0f) {
-          lit = 1;
-          if (trace_scene<true>(S, 0u, p + n * EPS_OFF, wi, 0.0f, dist - 2e-5f, 0.5f, 3u, skip).tri == MISS) {
-            vis = 1;
-            c = Le * (cosE * cosN * area / d2) * albedo(S, m, cosN);
-          }
+          flags |= ND_LIT;
+          c = Le * (cosE * cosN * area / d2) * albedo(S, node_mat(S, i), cosN);
+          const float3 o = p + n * EPS_OFF;
+          b.ro[t] = make_float4(o.x, o.y, o.z, dist - 2e-5f);
+          b.rd[t] = make_float4(wi.x, wi.y, wi.z, 0.0f);
         }
       }
     }
-    // the group's lead adds the terms of samples 0, 1, ... in order
+    b.term[t] = make_float4(c.x, c.y, c.z, __uint_as_float(flags));
+    const uint32_t q = node_append(b.counts, (flags & ND_LIT) != 0u);
+    if (flags & ND_LIT) b.queue[q] = uint32_t(t);
+  }
+}
+
+// any hit of every queued shadow ray (the static BVH, then each posed body that passes its culls) on persistent
+// lanes; a visible sample gets ND_VIS
+__global__ void __launch_bounds__(256, VT_NODE_TRACE_BLOCKS) node_direct_shadow(const Scene S, NodeDirectBufs b, uint32_t refill) {
+  const uint32_t n = b.counts[0];
+  const uint32_t skip = ldu(S.su + 7);
+  __shared__ uint2 stack_sh[SH_DEPTH * 256];
+  LaneStack stk;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = 256;
+  TraceState st;
+  float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
+  uint32_t t = 0;
+  bool active = false, exhausted = false;
+  auto visible = [&]() { b.term[t].w = __uint_as_float(__float_as_uint(b.term[t].w) | ND_VIS); };
+  auto start = [&](uint32_t idx) {
+    t = b.queue[idx];
+    const float4 o4 = b.ro[t], d4 = b.rd[t];
+    o = xyz(o4); d = xyz(d4);
+    st.best = Hit{o4.w, 0.0f, 0.0f, MISS, MISS};
+    active = trace_phase(S, 0u, o, d, 0.0f, 0.5f, 3u, skip, st, -1);
+    if (!active) visible();
+  };
+  while (take_rays(active, exhausted, b.counts + 1, n, refill, start)) {
+    if (!active) continue;
+    const int r = trace_step<true>(S, 0.0f, st, stk);
+    bool done = r == 2;
+    if (r == 1) done = !trace_phase(S, 0u, o, d, 0.0f, 0.5f, 3u, skip, st, st.k + 1);
+    if (!done) continue;
+    if (st.best.tri == MISS) visible();
+    active = false;
+  }
+}
+
+__global__ void node_direct_sum(const Scene S, const uint32_t* __restrict__ active, uint32_t n_active, uint32_t NS, NodeDirectBufs b,
+                                float4* __restrict__ nstate) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_active; k += gridDim.x * blockDim.x) {
+    const size_t t0 = size_t(k) * NS;
+    if (!(__float_as_uint(b.term[t0].w) & ND_RUN)) continue;
     float3 B = f3(0, 0, 0);
     uint32_t n_lit = 0, n_vis = 0;
-    for (uint32_t q = 0; q < G; q++) {
-      const float cx = __shfl_sync(0xffffffffu, c.x, lead + q), cy = __shfl_sync(0xffffffffu, c.y, lead + q),
-                  cz = __shfl_sync(0xffffffffu, c.z, lead + q);
-      const uint32_t lq = __shfl_sync(0xffffffffu, lit, lead + q), vq = __shfl_sync(0xffffffffu, vis, lead + q);
-      if (vq) B = B + f3(cx, cy, cz);
-      n_lit += lq;
-      n_vis += vq;
+    for (uint32_t s = 0; s < NS; s++) {
+      const float4 c = b.term[t0 + s];
+      const uint32_t f = __float_as_uint(c.w);
+      n_lit += (f & ND_LIT) ? 1u : 0u;
+      if (f & ND_VIS) { n_vis++; B = B + xyz(c); }
     }
-    if (run && s == 0) {
-      B = B / float(G);
-      const float v = n_lit == 0 ? -1.0f : n_vis == n_lit ? 1.0f : n_vis == 0 ? 0.0f : 0.5f;
-      nstate[4u * i + 3u] = make_float4(B.x, B.y, B.z, v);
-      const float4 old = nstate[4u * i];
-      nstate[4u * i] = make_float4(old.x, old.y, old.z, capsule_vis(S, p, n));
-    }
+    B = B / float(NS);
+    const uint32_t i = active[k];
+    const float vis = n_lit == 0 ? -1.0f : n_vis == n_lit ? 1.0f : n_vis == 0 ? 0.0f : 0.5f;
+    nstate[4u * i + 3u] = make_float4(B.x, B.y, B.z, vis);
+    const float4 old = nstate[4u * i];
+    nstate[4u * i] = make_float4(old.x, old.y, old.z, capsule_vis(S, node_pos(S, i), node_nrm(S, i)));
   }
 }
 
@@ -398,19 +402,23 @@ void launch_amu(const Scene& S, uint32_t n_mat, uint32_t K, float4* amu, cudaStr
   amu_kernel<<<grid_for(size_t(n_mat) * K, 128), 128, 0, st>>>(S, n_mat, K, amu);
 }
 
-void launch_node_direct(const Scene& S, const uint32_t* active, uint32_t n_active, uint32_t NS, uint32_t moved, float4* nstate,
-                        cudaStream_t st) {
+size_t node_direct_bytes(uint32_t n_active, uint32_t NS) { return size_t(n_active) * NS * (3 * 16 + 4) + 256; }
+
+void launch_node_direct(const Scene& S, const uint32_t* active, uint32_t n_active, uint32_t NS, uint32_t moved, float4* nstate, void* work,
+                        int trace_blocks, cudaStream_t st) {
   if (!n_active) return;
-  const size_t t = size_t(n_active);
-  switch (NS) {   // one thread per emitter sample when the samples of a node fit a warp evenly
-    case 1: node_direct_group_kernel<1><<<grid_for(t, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
-    case 2: node_direct_group_kernel<2><<<grid_for(t * 2, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
-    case 4: node_direct_group_kernel<4><<<grid_for(t * 4, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
-    case 8: node_direct_group_kernel<8><<<grid_for(t * 8, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
-    case 16: node_direct_group_kernel<16><<<grid_for(t * 16, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
-    case 32: node_direct_group_kernel<32><<<grid_for(t * 32, 256), 256, 0, st>>>(S, active, n_active, moved, nstate); break;
-    default: node_direct_kernel<<<grid_for(t, 64), 64, 0, st>>>(S, active, n_active, NS, moved, nstate);
-  }
+  const size_t total = size_t(n_active) * NS;
+  char* w = static_cast<char*>(work);
+  NodeDirectBufs b;
+  b.counts = reinterpret_cast<uint32_t*>(w);
+  b.ro = reinterpret_cast<float4*>(w + 256);
+  b.rd = b.ro + total;
+  b.term = b.rd + total;
+  b.queue = reinterpret_cast<uint32_t*>(b.term + total);
+  cudaMemsetAsync(b.counts, 0, 8, st);
+  node_direct_setup<<<grid_for(total, 256), 256, 0, st>>>(S, active, n_active, NS, moved, b);
+  node_direct_shadow<<<trace_blocks, 256, 0, st>>>(S, b, 8u);
+  node_direct_sum<<<grid_for(n_active, 256), 256, 0, st>>>(S, active, n_active, NS, b, nstate);
 }
 
 void launch_transport_count(const uint32_t* active, uint32_t n_active, uint32_t K, const uint32_t* gtable, uint32_t* cnt, cudaStream_t st) {
