@@ -141,54 +141,57 @@ __device__ __forceinline__ float3 path_value(const CalibDev& C, const CalPath& P
 }
 
 // d loss / d parameters of one recorded path, given g = d loss / d (path radiance); FP64 into shared accumulators
-__device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, uint32_t nl, double3 g, double* sh_alb, double* sh_lamp) {
-  double Tp[CAL_MAX_DEPTH + 1][3];
-  Tp[0][0] = Tp[0][1] = Tp[0][2] = 1.0;
-  for (uint32_t k = 0; k < P.n; k++) {
-    const float3 r = alb(C, P.v[k].mat);
-    Tp[k + 1][0] = Tp[k][0] * r.x; Tp[k + 1][1] = Tp[k][1] * r.y; Tp[k + 1][2] = Tp[k][2] * r.z;
-  }
-  // a term of value val (per channel) that carries the albedos of shading vertices 0..last
-  auto add_albedo = [&](const double val[3], uint32_t last) {
-    for (uint32_t l = 0; l <= last; l++) {
-      const uint32_t m = P.v[l].mat;
-      const float3 r = alb(C, m);
-      atomicAdd(sh_alb + 3 * m, g.x * val[0] / double(r.x));
-      atomicAdd(sh_alb + 3 * m + 1, g.y * val[1] / double(r.y));
-      atomicAdd(sh_alb + 3 * m + 2, g.z * val[2] / double(r.z));
-    }
-  };
-  for (uint32_t k = 0; k < P.n; k++) {
-    double s = 0.0;
+__device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, uint32_t nl, double3 gd, double* sh_alb, double* sh_lamp) {
+  // Each term is formed in FP32 and added to the FP64 accumulators (FP64 arithmetic runs at a small fraction of
+  // this part's FP32 rate; the reductions stay FP64). A term whose albedo product ends at vertex k adds
+  // g o value / rho_l to every vertex l <= k: D[k] gathers the g-weighted values of the terms ending at k, and vertex
+  // l receives (sum_{k >= l} D[k]) / rho_l, one atomic per channel.
+  const float3 g = f3(float(gd.x), float(gd.y), float(gd.z));
+  const float fnl = float(nl);
+  float3 T = f3(1, 1, 1);
+  float3 D[CAL_MAX_DEPTH], rho[CAL_MAX_DEPTH];
+#pragma unroll
+  for (uint32_t k = 0; k < CAL_MAX_DEPTH; k++) {
+    D[k] = f3(0, 0, 0);
+    rho[k] = f3(1, 1, 1);
+    if (k >= P.n) continue;
+    rho[k] = alb(C, P.v[k].mat);
+    T = T * rho[k];
+    float s = 0.0f;
     for (uint32_t j = 0; j < nl; j++) {
       const float q = P.v[k].q[j];
       if (q == 0.0f) continue;
-      const double dl = (g.x * Tp[k + 1][0] + g.y * Tp[k + 1][1] + g.z * Tp[k + 1][2]) * double(q) / double(nl);
-      atomicAdd(sh_lamp + P.v[k].lamp[j], dl);
-      s += double(__ldg(C.lamp + P.v[k].lamp[j])) * double(q);
+      atomicAdd(sh_lamp + P.v[k].lamp[j], double(dot(g, T) * q / fnl));
+      s += __ldg(C.lamp + P.v[k].lamp[j]) * q;
     }
-    if (s != 0.0) {
-      const double val[3] = {Tp[k + 1][0] * s / nl, Tp[k + 1][1] * s / nl, Tp[k + 1][2] * s / nl};
-      add_albedo(val, k);
-    }
+    if (s != 0.0f) D[k] = D[k] + g * T * (s / fnl);
     if (k + 1 == P.n && P.node != MISS) {
-      const double hx = __ldg(C.H + P.node), hy = __ldg(C.H + C.n_nodes + P.node), hz = __ldg(C.H + 2 * C.n_nodes + P.node);
-      const double ip = 1.0 / 3.14159265358979323846;
-      atomicAdd(C.g_H + P.node, g.x * Tp[k + 1][0] * ip);
-      atomicAdd(C.g_H + C.n_nodes + P.node, g.y * Tp[k + 1][1] * ip);
-      atomicAdd(C.g_H + 2 * C.n_nodes + P.node, g.z * Tp[k + 1][2] * ip);
-      const double val[3] = {Tp[k + 1][0] * hx * ip, Tp[k + 1][1] * hy * ip, Tp[k + 1][2] * hz * ip};
-      add_albedo(val, k);
+      const float ip = 0.318309886183790672f;
+      const float3 Hn = f3(__ldg(C.H + P.node), __ldg(C.H + C.n_nodes + P.node), __ldg(C.H + 2 * C.n_nodes + P.node));
+      atomicAdd(C.g_H + P.node, double(g.x * T.x * ip));
+      atomicAdd(C.g_H + C.n_nodes + P.node, double(g.y * T.y * ip));
+      atomicAdd(C.g_H + 2 * C.n_nodes + P.node, double(g.z * T.z * ip));
+      D[k] = D[k] + g * T * Hn * ip;
     }
   }
   if (P.emit_lamp != MISS && P.emit_a != 0.0f) {
-    const double a = P.emit_a;
-    atomicAdd(sh_lamp + P.emit_lamp, (g.x * Tp[P.n][0] + g.y * Tp[P.n][1] + g.z * Tp[P.n][2]) * a);
+    atomicAdd(sh_lamp + P.emit_lamp, double(dot(g, T) * P.emit_a));
     if (P.n) {
-      const double Le = a * double(__ldg(C.lamp + P.emit_lamp));
-      const double val[3] = {Tp[P.n][0] * Le, Tp[P.n][1] * Le, Tp[P.n][2] * Le};
-      add_albedo(val, P.n - 1);
+      const float Le = P.emit_a * __ldg(C.lamp + P.emit_lamp);
+#pragma unroll
+      for (uint32_t k = 0; k < CAL_MAX_DEPTH; k++)
+        if (k + 1 == P.n) D[k] = D[k] + g * T * Le;
     }
+  }
+  float3 acc = f3(0, 0, 0);
+#pragma unroll
+  for (int k = CAL_MAX_DEPTH - 1; k >= 0; k--) {
+    if (uint32_t(k) >= P.n) continue;
+    acc = acc + D[k];
+    const uint32_t m = P.v[k].mat;
+    atomicAdd(sh_alb + 3 * m, double(acc.x / rho[k].x));
+    atomicAdd(sh_alb + 3 * m + 1, double(acc.y / rho[k].y));
+    atomicAdd(sh_alb + 3 * m + 2, double(acc.z / rho[k].z));
   }
 }
 
@@ -401,14 +404,16 @@ __device__ __forceinline__ void path_tangent(const CalibDev& C, const CalPath& P
 __device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_t id, uint32_t i, const float3* dL, double3 g, double* sh_k) {
   uint32_t x, y;
   if (!pixel_xy(cp, id, x, y)) return;
-  const double G[3] = {g.x * dL[0].x + g.y * dL[1].x + g.z * dL[2].x, g.x * dL[0].y + g.y * dL[1].y + g.z * dL[2].y,
-                       g.x * dL[0].z + g.y * dL[1].z + g.z * dL[2].z};
-  if (G[0] == 0.0 && G[1] == 0.0 && G[2] == 0.0) return;
+  // the term in FP32, its accumulation in FP64
+  const float gx = float(g.x), gy = float(g.y), gz = float(g.z);
+  const float G[3] = {gx * dL[0].x + gy * dL[1].x + gz * dL[2].x, gx * dL[0].y + gy * dL[1].y + gz * dL[2].y,
+                      gx * dL[0].z + gy * dL[1].z + gz * dL[2].z};
+  if (G[0] == 0.0f && G[1] == 0.0f && G[2] == 0.0f) return;
   const uint32_t hs = hash3(x, y, cp.seed * 64u + cp.cam_index);
   const float2 uv = subsample_uv(x, y, i, hs);
   float J[3][8];
   kb4_ray_jacobian(cp.lens, uv.x, uv.y, f3(cp.rx[0], cp.rx[1], cp.rx[2]), f3(cp.ry[0], cp.ry[1], cp.ry[2]), f3(cp.rz[0], cp.rz[1], cp.rz[2]), J);
-  for (int k = 0; k < 8; k++) atomicAdd(sh_k + k, G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k]);
+  for (int k = 0; k < 8; k++) atomicAdd(sh_k + k, double(G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k]));
 }
 
 // per pixel over the records of sub-samples [i0, i1): backward 0 adds their values to the pixel's running sum (kept in
