@@ -35,6 +35,9 @@ __device__ __forceinline__ void block_sum2(double a, double b, double* partials)
   }
 }
 
+// KEEP: F fits in half the L2 and is read with the cache's default policy, so the next sweep finds it there; a larger F
+// is streamed (evict-first), which keeps B and the vectors in L2 instead
+template <bool KEEP>
 __global__ void __launch_bounds__(MV_THREADS) jacobi_matvec_kernel(const float* __restrict__ F, const float* __restrict__ rho,
                                                                    const float* __restrict__ E, const float* __restrict__ Bin,
                                                                    float* __restrict__ Bout, uint32_t n, double* __restrict__ partials) {
@@ -52,12 +55,12 @@ __global__ void __launch_bounds__(MV_THREADS) jacobi_matvec_kernel(const float* 
       const uint32_t n4 = n >> 2;
 #pragma unroll 4
       for (uint32_t j = lane; j < n4; j += 32) {
-        const float4 f = __ldcs(F4 + j);
+        const float4 f = KEEP ? __ldg(F4 + j) : __ldcs(F4 + j);
         const float4 b = __ldg(B4 + j);
         acc = fmaf(f.x, b.x, acc); acc = fmaf(f.y, b.y, acc); acc = fmaf(f.z, b.z, acc); acc = fmaf(f.w, b.w, acc);
       }
     } else {
-      for (uint32_t j = lane; j < n; j += 32) acc = fmaf(__ldcs(Fr + j), __ldg(Bin + j), acc);
+      for (uint32_t j = lane; j < n; j += 32) acc = fmaf(KEEP ? __ldg(Fr + j) : __ldcs(Fr + j), __ldg(Bin + j), acc);
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) {
@@ -175,7 +178,14 @@ void launch_jacobi_matvec(const float* F, const float* rho, const float* E, cons
                           uint32_t* n_partials, cudaStream_t st) {
   const uint32_t blocks = (n + MV_THREADS / 32 - 1) / (MV_THREADS / 32);
   *n_partials = blocks;
-  jacobi_matvec_kernel<<<blocks, MV_THREADS, 0, st>>>(F, rho, E, Bin, Bout, n, partials);
+  static std::atomic<int> l2[MAX_DEVICES];
+  const size_t l2_bytes = size_t(per_device_value(l2, [](int dev) {
+    int b = 0;
+    if (cudaDeviceGetAttribute(&b, cudaDevAttrL2CacheSize, dev) != cudaSuccess) { cudaGetLastError(); b = 0; }
+    return b;
+  }));
+  if (size_t(n) * n * 4 <= l2_bytes / 2) jacobi_matvec_kernel<true><<<blocks, MV_THREADS, 0, st>>>(F, rho, E, Bin, Bout, n, partials);
+  else jacobi_matvec_kernel<false><<<blocks, MV_THREADS, 0, st>>>(F, rho, E, Bin, Bout, n, partials);
 }
 
 // ---------------------------------------------------------------------------------------------- FP32 GEMM sweep
