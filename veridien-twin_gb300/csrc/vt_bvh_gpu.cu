@@ -3,10 +3,11 @@
 // The host builder decides each node from its slot range alone. It computes the range's bounds, bins the
 // centroids in 16 bins per axis, takes the cheapest SAH split (traversal and intersection cost 1), and partitions
 // the slot order in place with gpu/bvh.js's swap-with-the-end loop. The nodes are then numbered in LIFO task
-// order. Here every level of the tree is one pass over its tasks. A task of at least BIG_TASK slots gets a
-// 512-thread block, a smaller one a warp. The task computes bounds, bins, SAH choice and partition, then appends
-// its two children to the next level. The host replays the LIFO numbering over the decided shapes, so the node
-// array is the host builder's.
+// order. Here every level of the tree is one pass over its tasks. A task of at least BIG_TASK slots is spread over
+// blocks of CHUNK slots (six launches per level), a smaller one gets a warp. A task computes bounds, bins, SAH
+// choice and partition, then appends its two children to the next level. Two passes per level over the decided
+// shapes (subtree sizes up, numbers down) give the LIFO numbering and write the node words, so the node array is
+// the host builder's.
 //
 // Exactness:
 // - Bounds and per-bin bounds are minima and maxima of floats, exact in any order. A node box keeps the first slot
@@ -23,6 +24,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -39,10 +42,13 @@ constexpr int BINS = 16;
 #ifndef VT_BVH_BIG
 #define VT_BVH_BIG 8192
 #endif
+#ifndef VT_BVH_CHUNK
+#define VT_BVH_CHUNK 4096
+#endif
 constexpr int BT = VT_BVH_BLOCK;   // threads of a big task's block
 constexpr int BIG_TASK = VT_BVH_BIG;   // ranges of at least this many slots are big tasks
+constexpr int CHUNK = VT_BVH_CHUNK;    // slots of a big task per block
 constexpr int WPB = 8;             // warp tasks per 256-thread block
-constexpr double KBIG = 1e30;
 constexpr int THR_MIN = 64;        // ranges above this many slots bin through float thresholds
 
 struct Task { int32_t s, e, parent, slot; };
@@ -68,7 +74,6 @@ struct GroupSh {
   float redf[BT / 32];
   uint32_t redu[BT / 32];
   int32_t dec[4];                    // axis, bin, split
-  double origin, scale;
   float thr[3][BINS - 1];            // per axis the least centroid of bins 1..15
 };
 
@@ -191,21 +196,18 @@ __device__ __forceinline__ int bin_by_threshold(const float* t, float c) {
   return b;
 }
 
-// one task: bounds, SAH choice, partition, children
+// Bounds of the slots [a, b) of the task that starts at s: node-box keys (value, then the slot's offset from s, so
+// that the first slot among equal values wins) and the plain centroid box, reduced over the group.
 template <int G>
-__device__ void run_task(const Build& B, const Task T, const Grp<G>& g) {
-  GroupSh& sh = *g.sh;
-  const int32_t s = T.s, e = T.e, cnt = e - s;
-  // bounds: node box with the first slot among equal values, centroid box plain
-  unsigned long long klo[3], khi[3];
-  float clo[3], chi[3];
+__device__ __forceinline__ void range_bounds(const Build& B, int32_t s, int32_t a, int32_t b, const Grp<G>& g, unsigned long long* klo,
+                                             unsigned long long* khi, float* clo, float* chi) {
   for (int k = 0; k < 3; k++) { klo[k] = ~0ull; khi[k] = 0ull; clo[k] = INFINITY; chi[k] = -INFINITY; }
-  for (int32_t p = s + g.lane; p < e; p += G) {
+  for (int32_t p = a + g.lane; p < b; p += G) {
     const uint32_t t = B.order[p];
-    const float4 a = B.bmin[t], z = B.bmax[t], c = B.cen[t];
+    const float4 lo = B.bmin[t], hi = B.bmax[t], c = B.cen[t];
     const uint32_t off = uint32_t(p - s);
     for (int k = 0; k < 3; k++) {
-      const float av = comp(a, k), zv = comp(z, k);
+      const float av = comp(lo, k), zv = comp(hi, k);
       const unsigned long long ka = (static_cast<unsigned long long>(ord(av == 0.0f ? 0.0f : av)) << 32) | off;
       const unsigned long long kz = (static_cast<unsigned long long>(ord(zv == 0.0f ? 0.0f : zv)) << 32) | (0xffffffffu - off);
       klo[k] = min(klo[k], ka);
@@ -218,35 +220,40 @@ __device__ void run_task(const Build& B, const Task T, const Grp<G>& g) {
     klo[k] = g.min64(klo[k]); khi[k] = g.max64(khi[k]);
     clo[k] = g.minf(clo[k]); chi[k] = g.maxf(chi[k]);
   }
-  if (g.lane == 0) {
-    float lo[3], hi[3];
-    for (int k = 0; k < 3; k++) {
-      lo[k] = comp(B.bmin[B.order[s + uint32_t(klo[k] & 0xffffffffu)]], k);
-      hi[k] = comp(B.bmax[B.order[s + (0xffffffffu - uint32_t(khi[k] & 0xffffffffu))]], k);
-    }
-    if (T.parent >= 0) {
-      Shape& P = B.shapes[T.parent];
-      for (int k = 0; k < 3; k++) { P.lo[T.slot][k] = lo[k]; P.hi[T.slot][k] = hi[k]; }
-    } else {
-      for (int k = 0; k < 3; k++) { B.root_box[k] = lo[k]; B.root_box[3 + k] = hi[k]; }
-    }
+}
+
+// the node box from the reduced keys: the values of the slots they name
+__device__ __forceinline__ void key_box(const Build& B, int32_t s, const unsigned long long* klo, const unsigned long long* khi, float* lo, float* hi) {
+  for (int k = 0; k < 3; k++) {
+    lo[k] = comp(B.bmin[B.order[s + uint32_t(klo[k] & 0xffffffffu)]], k);
+    hi[k] = comp(B.bmax[B.order[s + (0xffffffffu - uint32_t(khi[k] & 0xffffffffu))]], k);
   }
-  if (cnt <= 1) {
-    if (g.lane == 0 && T.parent < 0) *B.root_leaf = 1;
-    return;
+}
+
+__device__ __forceinline__ void write_box(const Build& B, const Task& T, const float* lo, const float* hi) {
+  if (T.parent >= 0) {
+    Shape& P = B.shapes[T.parent];
+    for (int k = 0; k < 3; k++) { P.lo[T.slot][k] = lo[k]; P.hi[T.slot][k] = hi[k]; }
+  } else {
+    for (int k = 0; k < 3; k++) { B.root_box[k] = lo[k]; B.root_box[3 + k] = hi[k]; }
   }
-  // bins per axis with a positive centroid extent
-  double origin[3], scale[3];
-  bool use[3];
+}
+
+// bins per axis with a positive centroid extent
+__device__ __forceinline__ void bin_frame(const float* clo, const float* chi, double* origin, double* scale, bool* use) {
   for (int k = 0; k < 3; k++) {
     origin[k] = double(clo[k]);
     const double extent = double(chi[k]) - origin[k];
     use[k] = extent > 0;
     scale[k] = use[k] ? BINS / extent : 0.0;
   }
-  // FP64 is a small fraction of FP32 on this part: a range of more than THR_MIN slots bins its centroids through
-  // each axis' 15 float thresholds (bin_threshold) instead of one double expression per slot and axis
-  const bool thr = cnt > THR_MIN;
+}
+
+// empty bins and, for a range of more than THR_MIN slots, each axis' 15 float thresholds (FP64 is a small fraction
+// of FP32 on this part: such a range bins its centroids through bin_threshold's floats instead of one double
+// expression per slot and axis)
+template <int G>
+__device__ __forceinline__ void bins_clear(GroupSh& sh, const Grp<G>& g, bool thr, const double* origin, const double* scale, const bool* use) {
   for (int i = g.lane; i < 3 * BINS; i += G) {
     (&sh.cnt[0][0])[i] = 0;
     for (int k = 0; k < 3; k++) { (&sh.blo[0][0][0])[3 * i + k] = 0xffffffffu; (&sh.bhi[0][0][0])[3 * i + k] = 0u; }
@@ -255,84 +262,125 @@ __device__ void run_task(const Build& B, const Task T, const Grp<G>& g) {
       sh.thr[ax][b - 1] = use[ax] ? bin_threshold(origin[ax], scale[ax], b) : INFINITY;
     }
   }
-  g.sync();
-  for (int32_t p = s + g.lane; p < e; p += G) {
+}
+
+// the slots [a, b) into the group's shared bins
+template <int G>
+__device__ __forceinline__ void bins_fill(const Build& B, GroupSh& sh, const Grp<G>& g, int32_t a, int32_t b, bool thr, const double* origin,
+                                          const double* scale, const bool* use) {
+  for (int32_t p = a + g.lane; p < b; p += G) {
     const uint32_t t = B.order[p];
-    const float4 a = B.bmin[t], z = B.bmax[t], c = B.cen[t];
+    const float4 lo = B.bmin[t], hi = B.bmax[t], c = B.cen[t];
     for (int ax = 0; ax < 3; ax++) {
       if (!use[ax]) continue;
-      const int b = thr ? bin_by_threshold(sh.thr[ax], comp(c, ax)) : bin_of(comp(c, ax), origin[ax], scale[ax]);
-      atomicAdd(&sh.cnt[ax][b], 1u);
+      const int bn = thr ? bin_by_threshold(sh.thr[ax], comp(c, ax)) : bin_of(comp(c, ax), origin[ax], scale[ax]);
+      atomicAdd(&sh.cnt[ax][bn], 1u);
       for (int k = 0; k < 3; k++) {
-        atomicMin(&sh.blo[ax][b][k], ord(comp(a, k)));
-        atomicMax(&sh.bhi[ax][b][k], ord(comp(z, k)));
+        atomicMin(&sh.blo[ax][bn][k], ord(comp(lo, k)));
+        atomicMax(&sh.bhi[ax][bn][k], ord(comp(hi, k)));
       }
     }
   }
-  g.sync();
-  // SAH choice (gpu/bvh.js:60-118) on the group's first warp: a 16-lane segment per axis holds its bins, prefix and
-  // suffix boxes come from segmented scans, and lane b prices the split after bin b. Only splits after a non-empty
-  // bin are priced: the splits that follow an empty bin cost exactly what the last split after a non-empty bin
-  // costs, and the host's strict comparison keeps the earlier one. The cheapest split wins, ties to the lower
-  // (axis, bin), which is the host's loop order.
-  if (g.lane < 32) {
-    const int l16 = g.lane & 15;
-    double plo[3], phi[3];
+}
+
+// SAH choice (gpu/bvh.js:60-118) over the bins in shared memory, on the group's first warp: a 16-lane segment per
+// axis holds its bins, prefix and suffix boxes come from segmented scans, and lane b prices the split after bin b.
+// Only splits after a non-empty bin are priced: the splits that follow an empty bin cost exactly what the last split
+// after a non-empty bin costs, and the host's strict comparison keeps the earlier one. The cheapest split wins, ties
+// to the lower (axis, bin), which is the host's loop order. Leaves sh.dec = {axis, bin, split}, split -1 for a leaf,
+// -2 for the median without partition, 0 for a partition at (axis, bin).
+__device__ void choose_split(GroupSh& sh, int lane, const float* box_lo, const float* box_hi, const bool* use, int32_t cnt, uint32_t leaf) {
+  if (lane >= 32) return;
+  const int l16 = lane & 15;
+  double plo[3], phi[3];
+  for (int k = 0; k < 3; k++) { plo[k] = double(box_lo[k]); phi[k] = double(box_hi[k]); }
+  const double parent = half_area(plo, phi);
+  double best_cost = INFINITY;
+  int best_idx = 1 << 30;
+  for (int round = 0; round < 2; round++) {
+    const int ax = round * 2 + (lane >> 4);
+    const bool live = ax < 3 && use[ax < 3 ? ax : 0];
+    const uint32_t c = live ? sh.cnt[ax][l16] : 0u;
+    float lo[3], hi[3];
     for (int k = 0; k < 3; k++) {
-      plo[k] = double(comp(B.bmin[B.order[s + uint32_t(klo[k] & 0xffffffffu)]], k));
-      phi[k] = double(comp(B.bmax[B.order[s + (0xffffffffu - uint32_t(khi[k] & 0xffffffffu))]], k));
+      lo[k] = c ? unord(sh.blo[ax < 3 ? ax : 0][l16][k]) : INFINITY;
+      hi[k] = c ? unord(sh.bhi[ax < 3 ? ax : 0][l16][k]) : -INFINITY;
     }
-    const double parent = half_area(plo, phi);
-    double best_cost = INFINITY;
-    int best_idx = 1 << 30;
-    for (int round = 0; round < 2; round++) {
-      const int ax = round * 2 + (g.lane >> 4);
-      const bool live = ax < 3 && use[ax];
-      const uint32_t c = live ? sh.cnt[ax][l16] : 0u;
-      float lo[3], hi[3];
+    // inclusive prefix (bins 0..b) and suffix (bins b..15) within the segment
+    uint32_t pc = c, sc = c;
+    float pl[3] = {lo[0], lo[1], lo[2]}, ph[3] = {hi[0], hi[1], hi[2]}, sl[3] = {lo[0], lo[1], lo[2]}, shh[3] = {hi[0], hi[1], hi[2]};
+    for (int d = 1; d < 16; d <<= 1) {
+      const uint32_t uc = __shfl_up_sync(0xffffffffu, pc, d, 16), dc = __shfl_down_sync(0xffffffffu, sc, d, 16);
+      float ul[3], uh[3], dl[3], dh[3];
       for (int k = 0; k < 3; k++) {
-        lo[k] = c ? unord(sh.blo[ax < 3 ? ax : 0][l16][k]) : INFINITY;
-        hi[k] = c ? unord(sh.bhi[ax < 3 ? ax : 0][l16][k]) : -INFINITY;
+        ul[k] = __shfl_up_sync(0xffffffffu, pl[k], d, 16); uh[k] = __shfl_up_sync(0xffffffffu, ph[k], d, 16);
+        dl[k] = __shfl_down_sync(0xffffffffu, sl[k], d, 16); dh[k] = __shfl_down_sync(0xffffffffu, shh[k], d, 16);
       }
-      // inclusive prefix (bins 0..b) and suffix (bins b..15) within the segment
-      uint32_t pc = c, sc = c;
-      float pl[3] = {lo[0], lo[1], lo[2]}, ph[3] = {hi[0], hi[1], hi[2]}, sl[3] = {lo[0], lo[1], lo[2]}, shh[3] = {hi[0], hi[1], hi[2]};
-      for (int d = 1; d < 16; d <<= 1) {
-        const uint32_t uc = __shfl_up_sync(0xffffffffu, pc, d, 16), dc = __shfl_down_sync(0xffffffffu, sc, d, 16);
-        float ul[3], uh[3], dl[3], dh[3];
-        for (int k = 0; k < 3; k++) {
-          ul[k] = __shfl_up_sync(0xffffffffu, pl[k], d, 16); uh[k] = __shfl_up_sync(0xffffffffu, ph[k], d, 16);
-          dl[k] = __shfl_down_sync(0xffffffffu, sl[k], d, 16); dh[k] = __shfl_down_sync(0xffffffffu, shh[k], d, 16);
-        }
-        if (l16 >= d) { pc += uc; for (int k = 0; k < 3; k++) { pl[k] = fminf(pl[k], ul[k]); ph[k] = fmaxf(ph[k], uh[k]); } }
-        if (l16 + d < 16) { sc += dc; for (int k = 0; k < 3; k++) { sl[k] = fminf(sl[k], dl[k]); shh[k] = fmaxf(shh[k], dh[k]); } }
-      }
-      // the suffix of bin b + 1
-      const uint32_t rc = __shfl_down_sync(0xffffffffu, sc, 1, 16);
-      float rl[3], rh[3];
-      for (int k = 0; k < 3; k++) { rl[k] = __shfl_down_sync(0xffffffffu, sl[k], 1, 16); rh[k] = __shfl_down_sync(0xffffffffu, shh[k], 1, 16); }
-      if (live && l16 < BINS - 1 && c && rc) {
-        const double la[3] = {double(pl[0]), double(pl[1]), double(pl[2])}, lb[3] = {double(ph[0]), double(ph[1]), double(ph[2])};
-        const double ra[3] = {double(rl[0]), double(rl[1]), double(rl[2])}, rb[3] = {double(rh[0]), double(rh[1]), double(rh[2])};
-        const double cost = 1.0 + 1.0 * (double(pc) * half_area(la, lb) + double(rc) * half_area(ra, rb)) / parent;
-        if (cost < best_cost) { best_cost = cost; best_idx = ax * 16 + l16; }
-      }
+      if (l16 >= d) { pc += uc; for (int k = 0; k < 3; k++) { pl[k] = fminf(pl[k], ul[k]); ph[k] = fmaxf(ph[k], uh[k]); } }
+      if (l16 + d < 16) { sc += dc; for (int k = 0; k < 3; k++) { sl[k] = fminf(sl[k], dl[k]); shh[k] = fmaxf(shh[k], dh[k]); } }
     }
-    for (int o = 16; o; o >>= 1) {
-      const double oc = __shfl_xor_sync(0xffffffffu, best_cost, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
-      if (oc < best_cost || (oc == best_cost && oi < best_idx)) { best_cost = oc; best_idx = oi; }
-    }
-    if (g.lane == 0) {
-      const int best_axis = best_idx < (1 << 30) ? best_idx >> 4 : -1, best_bin = best_axis >= 0 ? best_idx & 15 : -1;
-      // split: -1 leaf, -2 median without partition, 0 partition at (axis, bin)
-      int split = 0;
-      if (best_axis < 0) split = cnt > int32_t(B.leaf) * 4 ? -2 : -1;
-      else if (cnt <= int32_t(B.leaf) && best_cost >= double(cnt)) split = -1;
-      sh.dec[0] = best_axis; sh.dec[1] = best_bin; sh.dec[2] = split;
-      if (split == 0) { sh.origin = origin[best_axis]; sh.scale = scale[best_axis]; }
+    // the suffix of bin b + 1
+    const uint32_t rc = __shfl_down_sync(0xffffffffu, sc, 1, 16);
+    float rl[3], rh[3];
+    for (int k = 0; k < 3; k++) { rl[k] = __shfl_down_sync(0xffffffffu, sl[k], 1, 16); rh[k] = __shfl_down_sync(0xffffffffu, shh[k], 1, 16); }
+    if (live && l16 < BINS - 1 && c && rc) {
+      const double la[3] = {double(pl[0]), double(pl[1]), double(pl[2])}, lb[3] = {double(ph[0]), double(ph[1]), double(ph[2])};
+      const double ra[3] = {double(rl[0]), double(rl[1]), double(rl[2])}, rb[3] = {double(rh[0]), double(rh[1]), double(rh[2])};
+      const double cost = 1.0 + 1.0 * (double(pc) * half_area(la, lb) + double(rc) * half_area(ra, rb)) / parent;
+      if (cost < best_cost) { best_cost = cost; best_idx = ax * 16 + l16; }
     }
   }
+  for (int o = 16; o; o >>= 1) {
+    const double oc = __shfl_xor_sync(0xffffffffu, best_cost, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
+    if (oc < best_cost || (oc == best_cost && oi < best_idx)) { best_cost = oc; best_idx = oi; }
+  }
+  if (lane == 0) {
+    const int best_axis = best_idx < (1 << 30) ? best_idx >> 4 : -1, best_bin = best_axis >= 0 ? best_idx & 15 : -1;
+    int split = 0;
+    if (best_axis < 0) split = cnt > int32_t(leaf) * 4 ? -2 : -1;
+    else if (cnt <= int32_t(leaf) && best_cost >= double(cnt)) split = -1;
+    sh.dec[0] = best_axis; sh.dec[1] = best_bin; sh.dec[2] = split;
+  }
+}
+
+// an interior node over [s, e) split at m: its shape, and its two children as tasks of the next level
+__device__ void emit_node(const Build& B, const Task& T, int32_t m) {
+  const uint32_t id = atomicAdd(B.counters, 1u);
+  Shape& S = B.shapes[id];
+  S.s = T.s; S.e = T.e; S.m = m; S.child[0] = -1; S.child[1] = -1;
+  if (T.parent >= 0) B.shapes[T.parent].child[T.slot] = int32_t(id);
+  auto push = [&](const Task c) {
+    if (c.e - c.s >= BIG_TASK) B.next_big[atomicAdd(B.counters + 1, 1u)] = c;
+    else B.next_small[atomicAdd(B.counters + 2, 1u)] = c;
+  };
+  push(Task{T.s, m, int32_t(id), 0});
+  push(Task{m, T.e, int32_t(id), 1});
+}
+
+// one task on one group: bounds, SAH choice, partition, children
+template <int G>
+__device__ void run_task(const Build& B, const Task T, const Grp<G>& g) {
+  GroupSh& sh = *g.sh;
+  const int32_t s = T.s, e = T.e, cnt = e - s;
+  unsigned long long klo[3], khi[3];
+  float clo[3], chi[3], lo[3], hi[3];
+  range_bounds(B, s, s, e, g, klo, khi, clo, chi);
+  key_box(B, s, klo, khi, lo, hi);
+  if (g.lane == 0) write_box(B, T, lo, hi);
+  if (cnt <= 1) {
+    if (g.lane == 0 && T.parent < 0) *B.root_leaf = 1;
+    return;
+  }
+  double origin[3], scale[3];
+  bool use[3];
+  bin_frame(clo, chi, origin, scale, use);
+  const bool thr = cnt > THR_MIN;
+  bins_clear(sh, g, thr, origin, scale, use);
+  g.sync();
+  bins_fill(B, sh, g, s, e, thr, origin, scale, use);
+  g.sync();
+  choose_split(sh, g.lane, lo, hi, use, cnt, B.leaf);
   g.sync();
   const int split = sh.dec[2];
   int32_t m;
@@ -343,7 +391,7 @@ __device__ void run_task(const Build& B, const Task T, const Grp<G>& g) {
     m = s + (cnt >> 1);
   } else {
     const int ax = sh.dec[0], bb = sh.dec[1];
-    const double o = sh.origin, sc = sh.scale;
+    const double o = origin[ax], sc = scale[ax];
     // left of the split: bin <= bb, i.e. below the threshold of bin bb + 1
     const float cut = thr ? sh.thr[ax][bb] : 0.0f;
     auto left = [&](uint32_t t) {
@@ -396,25 +444,7 @@ __device__ void run_task(const Build& B, const Task T, const Grp<G>& g) {
     g.sync();
     m = (m0 == s || m0 == e) ? s + (cnt >> 1) : m0;
   }
-  // an interior node: its shape, and its two children as tasks of the next level
-  if (g.lane == 0) {
-    const uint32_t id = atomicAdd(B.counters, 1u);
-    Shape& S = B.shapes[id];
-    S.s = s; S.e = e; S.m = m; S.child[0] = -1; S.child[1] = -1;
-    if (T.parent >= 0) B.shapes[T.parent].child[T.slot] = int32_t(id);
-    auto push = [&](const Task c) {
-      if (c.e - c.s >= BIG_TASK) B.next_big[atomicAdd(B.counters + 1, 1u)] = c;
-      else B.next_small[atomicAdd(B.counters + 2, 1u)] = c;
-    };
-    push(Task{s, m, int32_t(id), 0});
-    push(Task{m, e, int32_t(id), 1});
-  }
-}
-
-__global__ void __launch_bounds__(BT) big_tasks(Build B, const Task* __restrict__ tasks) {
-  __shared__ GroupSh sh;
-  Grp<BT> g{int(threadIdx.x), int(threadIdx.x >> 5), &sh};
-  run_task<BT>(B, tasks[blockIdx.x], g);
+  if (g.lane == 0) emit_node(B, T, m);
 }
 
 __global__ void __launch_bounds__(32 * WPB) small_tasks(Build B, const Task* __restrict__ tasks, uint32_t n) {
@@ -423,6 +453,286 @@ __global__ void __launch_bounds__(32 * WPB) small_tasks(Build B, const Task* __r
   if (i >= n) return;   // whole warps leave: a warp task synchronises only within its warp
   Grp<32> g{int(threadIdx.x & 31), 0, &sh[w]};
   run_task<32>(B, tasks[i], g);
+}
+
+// A task of at least BIG_TASK slots is spread over blocks of CHUNK slots each, in six launches per tree level:
+// bounds (per-chunk partial keys), bins (each block reduces the partials, bins its chunk in shared memory and merges
+// into the task's bins in global memory), choice and left counts (every block of the task prices the same bins), the
+// partition's two passes, and the copy back with the node's children. The partition is the same closed form: a
+// chunk's ranks among the left slots of [m0, e) counted from the top, and among the right slots of [s, m0) counted
+// from the bottom, start after the chunks above it (all of them in [m0, e)) and below it (all in [s, m0)), so only
+// the per-chunk left counts cross blocks.
+struct BigState {
+  float lo[3], hi[3];                // node box
+  double origin[3], scale[3];
+  int32_t use[3];
+  float thr[3][BINS - 1];
+  uint32_t cnt[3][BINS];
+  uint32_t blo[3][BINS][3], bhi[3][BINS][3];
+  int32_t axis, bin, split, m0, K;
+};
+
+struct Big {
+  const Task* tasks;                 // this level's big tasks
+  const uint32_t* map;               // per block: its task
+  const int32_t* info;               // per task: first block, number of chunks
+  BigState* state;                   // per task
+  unsigned long long* pk;            // per block: klo[3], khi[3]
+  float* pc;                         // per block: clo[3], chi[3]
+  uint32_t* nleft;                   // per block: left slots of its chunk
+};
+
+struct Chunk {
+  Task T;
+  uint32_t task;
+  int32_t first, n, c, a, b;         // first block and number of chunks of the task; this chunk and its slots [a, b)
+};
+
+__device__ __forceinline__ Chunk chunk_of(const Big& G, uint32_t blk) {
+  Chunk C;
+  C.task = G.map[blk];
+  C.T = G.tasks[C.task];
+  C.first = G.info[2 * C.task];
+  C.n = G.info[2 * C.task + 1];
+  C.c = int32_t(blk) - C.first;
+  C.a = C.T.s + C.c * CHUNK;
+  C.b = min(C.T.e, C.a + CHUNK);
+  return C;
+}
+
+__global__ void __launch_bounds__(BT) big_bounds(Build B, Big G) {
+  __shared__ GroupSh sh;
+  const Grp<BT> g{int(threadIdx.x), int(threadIdx.x >> 5), &sh};
+  const Chunk C = chunk_of(G, blockIdx.x);
+  unsigned long long klo[3], khi[3];
+  float clo[3], chi[3];
+  range_bounds(B, C.T.s, C.a, C.b, g, klo, khi, clo, chi);
+  if (g.lane == 0)
+    for (int k = 0; k < 3; k++) {
+      G.pk[6ull * blockIdx.x + k] = klo[k]; G.pk[6ull * blockIdx.x + 3 + k] = khi[k];
+      G.pc[6ull * blockIdx.x + k] = clo[k]; G.pc[6ull * blockIdx.x + 3 + k] = chi[k];
+    }
+  if (C.c == 0) {
+    BigState& S = G.state[C.task];
+    for (int i = g.lane; i < 3 * BINS; i += BT) {
+      (&S.cnt[0][0])[i] = 0u;
+      for (int k = 0; k < 3; k++) { (&S.blo[0][0][0])[3 * i + k] = 0xffffffffu; (&S.bhi[0][0][0])[3 * i + k] = 0u; }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BT) big_bins(Build B, Big G) {
+  __shared__ GroupSh sh;
+  const Grp<BT> g{int(threadIdx.x), int(threadIdx.x >> 5), &sh};
+  const Chunk C = chunk_of(G, blockIdx.x);
+  BigState& S = G.state[C.task];
+  unsigned long long klo[3], khi[3];
+  float clo[3], chi[3];
+  for (int k = 0; k < 3; k++) { klo[k] = ~0ull; khi[k] = 0ull; clo[k] = INFINITY; chi[k] = -INFINITY; }
+  for (int j = g.lane; j < C.n; j += BT) {
+    const size_t q = size_t(C.first + j);
+    for (int k = 0; k < 3; k++) {
+      klo[k] = min(klo[k], G.pk[6 * q + k]); khi[k] = max(khi[k], G.pk[6 * q + 3 + k]);
+      clo[k] = fminf(clo[k], G.pc[6 * q + k]); chi[k] = fmaxf(chi[k], G.pc[6 * q + 3 + k]);
+    }
+  }
+  for (int k = 0; k < 3; k++) {
+    klo[k] = g.min64(klo[k]); khi[k] = g.max64(khi[k]);
+    clo[k] = g.minf(clo[k]); chi[k] = g.maxf(chi[k]);
+  }
+  double origin[3], scale[3];
+  bool use[3];
+  bin_frame(clo, chi, origin, scale, use);
+  bins_clear(sh, g, true, origin, scale, use);
+  if (C.c == 0 && g.lane == 0) {
+    float lo[3], hi[3];
+    key_box(B, C.T.s, klo, khi, lo, hi);
+    write_box(B, C.T, lo, hi);
+    for (int k = 0; k < 3; k++) {
+      S.lo[k] = lo[k]; S.hi[k] = hi[k];
+      S.origin[k] = origin[k]; S.scale[k] = scale[k]; S.use[k] = use[k];
+    }
+  }
+  g.sync();
+  if (C.c == 0)
+    for (int i = g.lane; i < 3 * (BINS - 1); i += BT) (&S.thr[0][0])[i] = (&sh.thr[0][0])[i];
+  bins_fill(B, sh, g, C.a, C.b, true, origin, scale, use);
+  g.sync();
+  for (int i = g.lane; i < 3 * BINS; i += BT) {
+    const uint32_t c = (&sh.cnt[0][0])[i];
+    if (!c) continue;
+    atomicAdd(&S.cnt[0][0] + i, c);
+    for (int k = 0; k < 3; k++) {
+      atomicMin(&S.blo[0][0][0] + 3 * i + k, (&sh.blo[0][0][0])[3 * i + k]);
+      atomicMax(&S.bhi[0][0][0] + 3 * i + k, (&sh.bhi[0][0][0])[3 * i + k]);
+    }
+  }
+}
+
+// left of the split at (axis, bin): the centroid below the threshold of bin + 1
+__device__ __forceinline__ bool big_left(const Build& B, int ax, float cut, uint32_t t) { return comp(B.cen[t], ax) < cut; }
+
+__global__ void __launch_bounds__(BT) big_choose(Build B, Big G) {
+  __shared__ GroupSh sh;
+  const Grp<BT> g{int(threadIdx.x), int(threadIdx.x >> 5), &sh};
+  const Chunk C = chunk_of(G, blockIdx.x);
+  BigState& S = G.state[C.task];
+  for (int i = g.lane; i < 3 * BINS; i += BT) {
+    (&sh.cnt[0][0])[i] = (&S.cnt[0][0])[i];
+    for (int k = 0; k < 3; k++) {
+      (&sh.blo[0][0][0])[3 * i + k] = (&S.blo[0][0][0])[3 * i + k];
+      (&sh.bhi[0][0][0])[3 * i + k] = (&S.bhi[0][0][0])[3 * i + k];
+    }
+  }
+  g.sync();
+  const float lo[3] = {S.lo[0], S.lo[1], S.lo[2]}, hi[3] = {S.hi[0], S.hi[1], S.hi[2]};
+  const bool use[3] = {S.use[0] != 0, S.use[1] != 0, S.use[2] != 0};
+  choose_split(sh, g.lane, lo, hi, use, C.T.e - C.T.s, B.leaf);
+  g.sync();
+  const int ax = sh.dec[0], bb = sh.dec[1], split = sh.dec[2];
+  if (C.c == 0 && g.lane == 0) { S.axis = ax; S.bin = bb; S.split = split; }
+  if (split != 0) return;
+  const float cut = S.thr[ax][bb];
+  uint32_t nl = 0;
+  for (int32_t p = C.a + g.lane; p < C.b; p += BT) nl += big_left(B, ax, cut, B.order[p]) ? 1u : 0u;
+  nl = g.sum(nl);
+  if (g.lane == 0) G.nleft[blockIdx.x] = nl;
+}
+
+// m0 of the chunk's task, the left slots in the chunks above this one and the right slots in the chunks below it
+__device__ __forceinline__ void big_offsets(const Big& G, const Chunk& C, const Grp<BT>& g, int32_t& m0, uint32_t& above, uint32_t& below) {
+  uint32_t nl = 0, ab = 0, be = 0;
+  for (int j = g.lane; j < C.n; j += BT) {
+    const uint32_t L = G.nleft[C.first + j];
+    nl += L;
+    if (j > C.c) ab += L;
+    if (j < C.c) be += uint32_t(min(C.T.e, C.T.s + (j + 1) * CHUNK) - (C.T.s + j * CHUNK)) - L;
+  }
+  m0 = C.T.s + int32_t(g.sum(nl));
+  above = g.sum(ab);
+  below = g.sum(be);
+}
+
+// pass 1: [m0, e) from the top (qpos of the left slots, right slots down one)
+__global__ void __launch_bounds__(BT) big_part_top(Build B, Big G) {
+  __shared__ GroupSh sh;
+  const Grp<BT> g{int(threadIdx.x), int(threadIdx.x >> 5), &sh};
+  const Chunk C = chunk_of(G, blockIdx.x);
+  BigState& S = G.state[C.task];
+  if (S.split != 0) return;
+  int32_t m0;
+  uint32_t above, below;
+  big_offsets(G, C, g, m0, above, below);
+  if (C.c == 0 && g.lane == 0) S.m0 = m0;
+  const int ax = S.axis;
+  const float cut = S.thr[ax][S.bin];
+  const int32_t s = C.T.s, lo = max(C.a, m0);
+  uint32_t K = above;
+  for (int32_t base = 0; base < C.b - lo; base += BT) {
+    const int32_t x = C.b - 1 - (base + g.lane);
+    const bool valid = x >= lo;
+    const uint32_t t = valid ? B.order[x] : 0u;
+    const bool L = valid && big_left(B, ax, cut, t);
+    uint32_t tot;
+    const uint32_t r = g.scan(L, tot);
+    if (L) B.qpos[s + K + r] = x;
+    else if (valid && x > m0) B.scratch[x - 1] = t;
+    K += tot;
+  }
+  if (g.lane == 0 && C.a <= m0 && m0 < C.b) S.K = int32_t(K);
+}
+
+// pass 2: [s, m0) from the bottom, and the slot at m0
+__global__ void __launch_bounds__(BT) big_part_bottom(Build B, Big G) {
+  __shared__ GroupSh sh;
+  const Grp<BT> g{int(threadIdx.x), int(threadIdx.x >> 5), &sh};
+  const Chunk C = chunk_of(G, blockIdx.x);
+  const BigState& S = G.state[C.task];
+  if (S.split != 0) return;
+  int32_t m0;
+  uint32_t above, below;
+  big_offsets(G, C, g, m0, above, below);
+  const int ax = S.axis;
+  const float cut = S.thr[ax][S.bin];
+  const int32_t s = C.T.s, e = C.T.e, hi = min(C.b, m0);
+  if (g.lane == 0 && C.a <= m0 && m0 < C.b) {
+    const uint32_t t = B.order[m0];
+    const int32_t K = S.K;
+    if (!big_left(B, ax, cut, t)) B.scratch[(K ? B.qpos[s + K - 1] : e) - 1] = t;
+  }
+  uint32_t k0 = below;
+  for (int32_t base = 0; base < hi - C.a; base += BT) {
+    const int32_t p = C.a + base + g.lane;
+    const bool valid = p < hi;
+    const uint32_t t = valid ? B.order[p] : 0u;
+    const bool R = valid && !big_left(B, ax, cut, t);
+    uint32_t tot;
+    const uint32_t r = g.scan(R, tot);
+    if (R) {
+      const uint32_t k = k0 + r + 1;
+      B.scratch[(k == 1 ? e : B.qpos[s + k - 2]) - 1] = t;
+      B.scratch[p] = B.order[B.qpos[s + k - 1]];
+    } else if (valid) {
+      B.scratch[p] = t;
+    }
+    k0 += tot;
+  }
+}
+
+// the partitioned chunk back into the slot order; the task's first block records the node and its children
+__global__ void __launch_bounds__(BT) big_finish(Build B, Big G) {
+  const Chunk C = chunk_of(G, blockIdx.x);
+  const BigState& S = G.state[C.task];
+  const int32_t s = C.T.s, e = C.T.e, cnt = e - s;
+  if (S.split == 0)
+    for (int32_t p = C.a + int32_t(threadIdx.x); p < C.b; p += BT) B.order[p] = B.scratch[p];
+  if (C.c != 0 || threadIdx.x != 0) return;
+  if (S.split == -1) {
+    if (C.T.parent < 0) *B.root_leaf = 1;
+    return;
+  }
+  const int32_t m0 = S.m0;
+  const int32_t m = (S.split == -2 || m0 == s || m0 == e) ? s + (cnt >> 1) : m0;
+  emit_node(B, C.T, m);
+}
+
+// Node numbers in the host builder's task order (pop a node, number its interior children slot 0 then slot 1, push
+// them), without the replay: a node popped at counter c numbers its children c, c + 1, and the slot-1 child's
+// subtree is processed before the slot-0 child's. So the slot-1 child is popped at c + (interior children) and the
+// slot-0 child after the slot-1 child's D interior descendants, where D sums 1 + D over a node's interior children.
+// The shapes of one tree level are one contiguous id range (the level's emits finish before the next level starts),
+// so D is one launch per level from the deepest up and the numbers one launch per level from the root down, which
+// also writes each node's 16 words.
+__global__ void number_up(const Shape* __restrict__ S, int32_t* D, uint32_t a, uint32_t b) {
+  const uint32_t i = a + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b) return;
+  int32_t d = 0;
+  for (int slot = 0; slot < 2; slot++) {
+    const int32_t c = S[i].child[slot];
+    if (c >= 0) d += 1 + D[c];
+  }
+  D[i] = d;
+}
+
+__global__ void number_down(const Shape* __restrict__ S, const int32_t* __restrict__ D, int32_t* num, int32_t* pop, uint32_t a, uint32_t b,
+                            uint32_t* words) {
+  const uint32_t i = a + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b) return;
+  const Shape X = S[i];
+  int32_t k = pop[i];
+  int32_t cn[2] = {-1, -1};
+  for (int slot = 0; slot < 2; slot++)
+    if (X.child[slot] >= 0) { cn[slot] = k++; num[X.child[slot]] = cn[slot]; }
+  if (X.child[1] >= 0) pop[X.child[1]] = k;
+  if (X.child[0] >= 0) pop[X.child[0]] = k + (X.child[1] >= 0 ? D[X.child[1]] : 0);
+  const int32_t lo[2] = {X.s, X.m}, hi[2] = {X.m, X.e};
+  uint4* w = reinterpret_cast<uint4*>(words + size_t(num[i]) * VT_NODE_WORDS);
+  for (int slot = 0; slot < 2; slot++) {
+    const uint32_t ref = X.child[slot] >= 0 ? uint32_t(cn[slot]) : uint32_t(lo[slot]);
+    const uint32_t count = X.child[slot] >= 0 ? 0u : uint32_t(hi[slot] - lo[slot]);
+    w[2 * slot] = make_uint4(__float_as_uint(X.lo[slot][0]), __float_as_uint(X.lo[slot][1]), __float_as_uint(X.lo[slot][2]), ref);
+    w[2 * slot + 1] = make_uint4(__float_as_uint(X.hi[slot][0]), __float_as_uint(X.hi[slot][1]), __float_as_uint(X.hi[slot][2]), count);
+  }
 }
 
 // per triangle: its box as the host builder takes it (std::min / std::max over the three vertices, first of equals)
@@ -448,8 +758,6 @@ __global__ void tri_boxes(const float* __restrict__ P, const uint32_t* __restric
   order[t] = t;
 }
 
-inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
-
 }  // namespace
 
 // Builds the static BVH of (P, I) on the current device. False, with out untouched, when the root itself is a
@@ -457,11 +765,27 @@ inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t n, uint32_t leaf, vt::Bvh& out, std::string& err) {
   if (n < 2) return false;
   leaf = std::max(1u, leaf);
+  // VT_BVH_TIMING=1 prints the build's phases to stderr
+  static const bool timing = [] { const char* v = std::getenv("VT_BVH_TIMING"); return v && *v && *v != '0'; }();
+  using clk = std::chrono::steady_clock;
+  const auto t_start = clk::now();
+  auto ms = [&](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
+  double ph[3] = {0, 0, 0};   // setup + upload, levels, numbering + readback
+  auto mark = [&](int i, clk::time_point& a) { ph[i] = ms(a); a = clk::now(); };
+  clk::time_point tp = t_start;
+  int n_levels = 0;
   const size_t nn = n;
   // one allocation: inputs, per-triangle records, order/scratch/qpos, shapes, two task lists x 2 levels, counters
   const size_t b_P = 3ull * n_verts * 4, b_I = 3ull * nn * 4, b_f4 = nn * 16, b_u = nn * 4, b_sh = nn * sizeof(Shape), b_t = nn * sizeof(Task);
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-  const size_t total = al(b_P) + al(b_I) + 3 * al(b_f4) + 3 * al(b_u) + al(b_sh) + 4 * al(b_t) + 256;
+  // big tasks of one level: at most n / BIG_TASK of them, in at most n / CHUNK + (tasks) chunks
+  const size_t max_big = nn / BIG_TASK + 2, max_chunks = nn / CHUNK + max_big + 2;
+  const size_t b_state = max_big * sizeof(BigState), b_pk = max_chunks * 48, b_pc = max_chunks * 24, b_nl = max_chunks * 4,
+               b_map = (max_chunks + 2 * max_big) * 4;
+  // numbering: D, number and pop counter per shape, 16 words per node
+  const size_t b_num = nn * 4, b_words = nn * VT_NODE_WORDS * 4;
+  const size_t total = al(b_P) + al(b_I) + 3 * al(b_f4) + 3 * al(b_u) + al(b_sh) + 4 * al(b_t) + al(b_state) + al(b_pk) + al(b_pc) + al(b_nl) +
+                       al(b_map) + 3 * al(b_num) + al(b_words) + 256;
   char* mem = nullptr;
   cudaStream_t st = nullptr;
   auto fail = [&](const char* what) {
@@ -487,6 +811,16 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
   B.shapes = reinterpret_cast<Shape*>(take(b_sh));
   Task* lists[2][2];
   for (auto& l : lists) { l[0] = reinterpret_cast<Task*>(take(b_t)); l[1] = reinterpret_cast<Task*>(take(b_t)); }
+  Big G;
+  G.state = reinterpret_cast<BigState*>(take(b_state));
+  G.pk = reinterpret_cast<unsigned long long*>(take(b_pk));
+  G.pc = reinterpret_cast<float*>(take(b_pc));
+  G.nleft = reinterpret_cast<uint32_t*>(take(b_nl));
+  uint32_t* dmap = reinterpret_cast<uint32_t*>(take(b_map));
+  int32_t* dD = reinterpret_cast<int32_t*>(take(b_num));
+  int32_t* dnum = reinterpret_cast<int32_t*>(take(b_num));
+  int32_t* dpop = reinterpret_cast<int32_t*>(take(b_num));
+  uint32_t* dwords = reinterpret_cast<uint32_t*>(take(b_words));
   char* tail = mem + o;
   B.counters = reinterpret_cast<uint32_t*>(tail);          // 3 words
   B.root_box = reinterpret_cast<float*>(tail + 16);        // 6 floats
@@ -496,24 +830,59 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
     return fail("upload");
   cudaMemsetAsync(tail, 0, 64, st);
   tri_boxes<<<(n + 255) / 256, 256, 0, st>>>(dP, dI, n, bmin, bmax, cen, B.order);
+  if (timing) { cudaStreamSynchronize(st); mark(0, tp); }
   const Task root{0, int32_t(n), -1, 0};
   uint32_t nb = n >= uint32_t(BIG_TASK) ? 1 : 0, ns = 1 - nb;
   if (cudaMemcpyAsync(lists[0][nb ? 0 : 1], &root, sizeof(Task), cudaMemcpyHostToDevice, st) != cudaSuccess) return fail("upload");
   int cur = 0;
   uint32_t counts[3];
+  std::vector<Task> big;              // this level's big tasks, read back after each level
+  std::vector<uint32_t> plan;         // per block its task, then per task its first block and chunk count
+  std::vector<uint32_t> level_end;    // shapes emitted up to and including each level
+  if (nb) big.push_back(root);
   for (int level = 0; nb + ns > 0; level++) {
     if (level > 4096) return fail("level cap");
     B.next_big = lists[cur ^ 1][0];
     B.next_small = lists[cur ^ 1][1];
     cudaMemsetAsync(B.counters + 1, 0, 8, st);
-    if (nb) big_tasks<<<nb, BT, 0, st>>>(B, lists[cur][0]);
+    if (nb) {
+      uint32_t blocks = 0;
+      for (const Task& t : big) blocks += uint32_t((t.e - t.s + CHUNK - 1) / CHUNK);
+      if (blocks > max_chunks || nb > max_big) return fail("chunk plan");
+      plan.assign(size_t(blocks) + 2 * nb, 0u);
+      uint32_t first = 0;
+      for (uint32_t i = 0; i < nb; i++) {
+        const uint32_t k = uint32_t((big[i].e - big[i].s + CHUNK - 1) / CHUNK);
+        for (uint32_t j = 0; j < k; j++) plan[first + j] = i;
+        plan[blocks + 2 * i] = first;
+        plan[blocks + 2 * i + 1] = k;
+        first += k;
+      }
+      if (cudaMemcpyAsync(dmap, plan.data(), plan.size() * 4, cudaMemcpyHostToDevice, st) != cudaSuccess) return fail("chunk plan");
+      G.tasks = lists[cur][0];
+      G.map = dmap;
+      G.info = reinterpret_cast<const int32_t*>(dmap + blocks);
+      big_bounds<<<blocks, BT, 0, st>>>(B, G);
+      big_bins<<<blocks, BT, 0, st>>>(B, G);
+      big_choose<<<blocks, BT, 0, st>>>(B, G);
+      big_part_top<<<blocks, BT, 0, st>>>(B, G);
+      big_part_bottom<<<blocks, BT, 0, st>>>(B, G);
+      big_finish<<<blocks, BT, 0, st>>>(B, G);
+    }
     if (ns) small_tasks<<<(ns + WPB - 1) / WPB, 32 * WPB, 0, st>>>(B, lists[cur][1], ns);
     if (cudaMemcpyAsync(counts, B.counters, 12, cudaMemcpyDeviceToHost, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
       return fail("level");
     nb = counts[1];
     ns = counts[2];
+    level_end.push_back(counts[0]);
+    big.resize(nb);
+    if (nb && (cudaMemcpyAsync(big.data(), lists[cur ^ 1][0], nb * sizeof(Task), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+               cudaStreamSynchronize(st) != cudaSuccess))
+      return fail("level");
     cur ^= 1;
+    n_levels = level + 1;
   }
+  if (timing) mark(1, tp);
   int32_t root_leaf = 0;
   float root_box[6];
   cudaMemcpyAsync(&root_leaf, B.root_leaf, 4, cudaMemcpyDeviceToHost, st);
@@ -521,43 +890,37 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail("readback");
   if (root_leaf) { cudaFree(mem); cudaStreamDestroy(st); return false; }
   const uint32_t n_shapes = counts[0];
-  std::vector<Shape> shapes(n_shapes);
+  // node numbers and words on the device; the tree's depth is the number of levels that emitted nodes
   vt::Bvh bv;
+  uint32_t depth = 0;
+  for (size_t L = 0; L < level_end.size(); L++)
+    if (level_end[L] > (L ? level_end[L - 1] : 0u)) depth = uint32_t(L) + 1;
+  for (size_t L = level_end.size(); L-- > 0;) {
+    const uint32_t a = L ? level_end[L - 1] : 0u, b = level_end[L];
+    if (b > a) number_up<<<(b - a + 255) / 256, 256, 0, st>>>(B.shapes, dD, a, b);
+  }
+  const int32_t root_init[2] = {0, 1};   // the root is node 0, popped at counter 1
+  cudaMemcpyAsync(dnum, &root_init[0], 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dpop, &root_init[1], 4, cudaMemcpyHostToDevice, st);
+  for (size_t L = 0; L < level_end.size(); L++) {
+    const uint32_t a = L ? level_end[L - 1] : 0u, b = level_end[L];
+    if (b > a) number_down<<<(b - a + 255) / 256, 256, 0, st>>>(B.shapes, dD, dnum, dpop, a, b, dwords);
+  }
+  bv.words.resize(size_t(n_shapes) * VT_NODE_WORDS);
   bv.order.resize(n);
-  cudaMemcpyAsync(shapes.data(), B.shapes, size_t(n_shapes) * sizeof(Shape), cudaMemcpyDeviceToHost, st);
+  bv.node_count = n_shapes;
+  bv.max_depth = std::max(1u, depth);
+  cudaMemcpyAsync(bv.words.data(), dwords, bv.words.size() * 4, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(bv.order.data(), B.order, b_u, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail("readback");
   cudaFree(mem);
   cudaStreamDestroy(st);
-  // node numbers in the host builder's task order: pop a node, number its interior children (slot 0 then 1), push them
-  struct Item { int32_t shape; uint32_t node, depth; };
-  std::vector<Item> stack{{0, 0, 1}};
-  bv.words.assign(VT_NODE_WORDS, 0u);
-  bv.node_count = 1;
-  bv.max_depth = 1;
-  while (!stack.empty()) {
-    const Item it = stack.back();
-    stack.pop_back();
-    bv.max_depth = std::max(bv.max_depth, it.depth);
-    const Shape& S = shapes[it.shape];
-    const int32_t lo[2] = {S.s, S.m}, hi[2] = {S.m, S.e};
-    for (int slot = 0; slot < 2; slot++) {
-      uint32_t ref, count;
-      if (S.child[slot] < 0) {
-        ref = uint32_t(lo[slot]); count = uint32_t(hi[slot] - lo[slot]);
-      } else {
-        ref = bv.node_count++;
-        bv.words.resize(bv.words.size() + VT_NODE_WORDS, 0u);
-        count = 0;
-        stack.push_back({S.child[slot], ref, it.depth + 1});
-      }
-      uint32_t* w = bv.words.data() + size_t(it.node) * VT_NODE_WORDS + slot * 8;
-      w[0] = fbits(S.lo[slot][0]); w[1] = fbits(S.lo[slot][1]); w[2] = fbits(S.lo[slot][2]); w[3] = ref;
-      w[4] = fbits(S.hi[slot][0]); w[5] = fbits(S.hi[slot][1]); w[6] = fbits(S.hi[slot][2]); w[7] = count;
-    }
-  }
+  if (timing) mark(2, tp);
   for (int k = 0; k < 3; k++) { bv.lo[k] = root_box[k]; bv.hi[k] = root_box[3 + k]; }
   out = std::move(bv);
+  if (timing)
+    std::fprintf(stderr, "gpu bvh build of %u triangles: %.2f ms (setup + upload %.2f, %d levels %.2f, numbering + readback %.2f)\n", n,
+                 ms(t_start), ph[0], n_levels, ph[1], ph[2]);
   return true;
 }
 
