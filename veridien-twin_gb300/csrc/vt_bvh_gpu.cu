@@ -4,7 +4,8 @@
 // centroids in 16 bins per axis, takes the cheapest SAH split (traversal and intersection cost 1), and partitions
 // the slot order in place with gpu/bvh.js's swap-with-the-end loop. The nodes are then numbered in LIFO task
 // order. Here every level of the tree is one pass over its tasks. A task of at least BIG_TASK slots is spread over
-// blocks of CHUNK slots (six launches per level), a smaller one gets a warp. A task computes bounds, bins, SAH
+// blocks of CHUNK slots (six launches per level); one of at least MID_TASK slots gets a block, one of more than TINY
+// slots a warp, a smaller one a thread. A task computes bounds, bins, SAH
 // choice and partition, then appends its two children to the next level. Two passes per level over the decided
 // shapes (subtree sizes up, numbers down) give the LIFO numbering and write the node words, so the node array is
 // the host builder's.
@@ -48,6 +49,12 @@ constexpr int BINS = 16;
 constexpr int BT = VT_BVH_BLOCK;   // threads of a big task's block
 constexpr int BIG_TASK = VT_BVH_BIG;   // ranges of at least this many slots are big tasks
 constexpr int CHUNK = VT_BVH_CHUNK;    // slots of a big task per block
+constexpr int TINY = 32;               // ranges of at most this many slots are decided by one thread
+#ifndef VT_BVH_MID
+#define VT_BVH_MID 1024
+#endif
+constexpr int MID_TASK = VT_BVH_MID;   // ranges of at least this many slots (and below BIG_TASK) get a block
+constexpr int MT = 256;                // threads of a mid task's block
 constexpr int WPB = 8;             // warp tasks per 256-thread block
 constexpr int THR_MIN = 64;        // ranges above this many slots bin through float thresholds
 
@@ -59,8 +66,8 @@ struct Build {
   uint32_t *order, *scratch;
   int32_t* qpos;
   Shape* shapes;
-  uint32_t* counters;                // [0] shapes, [1] next big tasks, [2] next small tasks
-  Task *next_big, *next_small;
+  uint32_t* counters;                // [0] shapes, next [1] big, [2] small, [3] tiny and [4] mid tasks
+  Task *next_big, *next_small, *next_tiny, *next_mid;
   float* root_box;                   // lo xyz, hi xyz of the whole range
   int32_t* root_leaf;
   uint32_t leaf;
@@ -352,7 +359,9 @@ __device__ void emit_node(const Build& B, const Task& T, int32_t m) {
   if (T.parent >= 0) B.shapes[T.parent].child[T.slot] = int32_t(id);
   auto push = [&](const Task c) {
     if (c.e - c.s >= BIG_TASK) B.next_big[atomicAdd(B.counters + 1, 1u)] = c;
-    else B.next_small[atomicAdd(B.counters + 2, 1u)] = c;
+    else if (c.e - c.s >= MID_TASK) B.next_mid[atomicAdd(B.counters + 4, 1u)] = c;
+    else if (c.e - c.s > TINY) B.next_small[atomicAdd(B.counters + 2, 1u)] = c;
+    else B.next_tiny[atomicAdd(B.counters + 3, 1u)] = c;
   };
   push(Task{T.s, m, int32_t(id), 0});
   push(Task{m, T.e, int32_t(id), 1});
@@ -447,12 +456,103 @@ __device__ void run_task(const Build& B, const Task T, const Grp<G>& g) {
   if (g.lane == 0) emit_node(B, T, m);
 }
 
+__global__ void __launch_bounds__(MT) mid_tasks(Build B, const Task* __restrict__ tasks) {
+  __shared__ GroupSh sh;
+  const Grp<MT> g{int(threadIdx.x), int(threadIdx.x >> 5), &sh};
+  run_task<MT>(B, tasks[blockIdx.x], g);
+}
+
 __global__ void __launch_bounds__(32 * WPB) small_tasks(Build B, const Task* __restrict__ tasks, uint32_t n) {
   __shared__ GroupSh sh[WPB];
   const uint32_t w = threadIdx.x >> 5, i = blockIdx.x * WPB + w;
   if (i >= n) return;   // whole warps leave: a warp task synchronises only within its warp
   Grp<32> g{int(threadIdx.x & 31), 0, &sh[w]};
   run_task<32>(B, tasks[i], g);
+}
+
+// A range of at most TINY slots on one thread, in the host builder's own sequential form: node box by strict
+// comparisons (the first slot among equal values), bins by the double expression, the SAH price of each split after
+// a non-empty bin from the two sides' boxes, and gpu/bvh.js's swap-with-the-end partition.
+__global__ void __launch_bounds__(128) tiny_tasks(Build B, const Task* __restrict__ tasks, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Task T = tasks[i];
+  const int32_t s = T.s, e = T.e, cnt = e - s;
+  uint32_t tt[TINY];
+  float lo[3], hi[3], clo[3], chi[3];
+  for (int j = 0; j < cnt; j++) {
+    const uint32_t t = B.order[s + j];
+    tt[j] = t;
+    const float4 a = B.bmin[t], z = B.bmax[t], c = B.cen[t];
+    for (int k = 0; k < 3; k++) {
+      if (j == 0 || comp(a, k) < lo[k]) lo[k] = comp(a, k);
+      if (j == 0 || comp(z, k) > hi[k]) hi[k] = comp(z, k);
+      clo[k] = j == 0 ? comp(c, k) : fminf(clo[k], comp(c, k));
+      chi[k] = j == 0 ? comp(c, k) : fmaxf(chi[k], comp(c, k));
+    }
+  }
+  write_box(B, T, lo, hi);
+  if (cnt <= 1) {
+    if (T.parent < 0) *B.root_leaf = 1;
+    return;
+  }
+  double origin[3], scale[3];
+  bool use[3];
+  bin_frame(clo, chi, origin, scale, use);
+  double plo[3], phi[3];
+  for (int k = 0; k < 3; k++) { plo[k] = double(lo[k]); phi[k] = double(hi[k]); }
+  const double parent = half_area(plo, phi);
+  double best_cost = INFINITY;
+  int best_axis = -1, best_bin = -1;
+  uint8_t bn[TINY];
+  for (int ax = 0; ax < 3; ax++) {
+    if (!use[ax]) continue;
+    uint32_t present = 0;
+    for (int j = 0; j < cnt; j++) {
+      bn[j] = uint8_t(bin_of(comp(B.cen[tt[j]], ax), origin[ax], scale[ax]));
+      present |= 1u << bn[j];
+    }
+    for (int v = 0; v < BINS - 1; v++) {
+      if (!(present >> v & 1u) || !(present >> (v + 1))) continue;   // an empty bin, or nothing to its right
+      float ll[3] = {INFINITY, INFINITY, INFINITY}, lh[3] = {-INFINITY, -INFINITY, -INFINITY};
+      float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
+      uint32_t nl = 0;
+      for (int j = 0; j < cnt; j++) {
+        const float4 a = B.bmin[tt[j]], z = B.bmax[tt[j]];
+        const bool L = bn[j] <= v;
+        nl += L ? 1u : 0u;
+        float* xl = L ? ll : rl;
+        float* xh = L ? lh : rh;
+        for (int k = 0; k < 3; k++) { xl[k] = fminf(xl[k], comp(a, k)); xh[k] = fmaxf(xh[k], comp(z, k)); }
+      }
+      const double la[3] = {double(ll[0]), double(ll[1]), double(ll[2])}, lb[3] = {double(lh[0]), double(lh[1]), double(lh[2])};
+      const double ra[3] = {double(rl[0]), double(rl[1]), double(rl[2])}, rb[3] = {double(rh[0]), double(rh[1]), double(rh[2])};
+      const double cost = 1.0 + 1.0 * (double(nl) * half_area(la, lb) + double(uint32_t(cnt) - nl) * half_area(ra, rb)) / parent;
+      if (cost < best_cost) { best_cost = cost; best_axis = ax; best_bin = v; }
+    }
+  }
+  int32_t m;
+  if (best_axis < 0) {
+    if (cnt <= int32_t(B.leaf) * 4) {
+      if (T.parent < 0) *B.root_leaf = 1;
+      return;
+    }
+    m = s + (cnt >> 1);
+  } else if (cnt <= int32_t(B.leaf) && best_cost >= double(cnt)) {
+    if (T.parent < 0) *B.root_leaf = 1;
+    return;
+  } else {
+    int32_t a = 0, b = cnt - 1;
+    while (a <= b) {
+      const uint32_t t = tt[a];
+      if (bin_of(comp(B.cen[t], best_axis), origin[best_axis], scale[best_axis]) <= best_bin) a++;
+      else { tt[a] = tt[b]; tt[b] = t; b--; }
+    }
+    for (int j = 0; j < cnt; j++) B.order[s + j] = tt[j];
+    const int32_t m0 = s + a;
+    m = (m0 == s || m0 == e) ? s + (cnt >> 1) : m0;
+  }
+  emit_node(B, T, m);
 }
 
 // A task of at least BIG_TASK slots is spread over blocks of CHUNK slots each, in six launches per tree level:
@@ -775,7 +875,8 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
   clk::time_point tp = t_start;
   int n_levels = 0;
   const size_t nn = n;
-  // one allocation: inputs, per-triangle records, order/scratch/qpos, shapes, two task lists x 2 levels, counters
+  // one allocation: inputs, per-triangle records, order/scratch/qpos, shapes, four task lists x 2 level parities, the
+  // big tasks' chunk state, the numbering arrays and node words, counters
   const size_t b_P = 3ull * n_verts * 4, b_I = 3ull * nn * 4, b_f4 = nn * 16, b_u = nn * 4, b_sh = nn * sizeof(Shape), b_t = nn * sizeof(Task);
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   // big tasks of one level: at most n / BIG_TASK of them, in at most n / CHUNK + (tasks) chunks
@@ -784,7 +885,7 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
                b_map = (max_chunks + 2 * max_big) * 4;
   // numbering: D, number and pop counter per shape, 16 words per node
   const size_t b_num = nn * 4, b_words = nn * VT_NODE_WORDS * 4;
-  const size_t total = al(b_P) + al(b_I) + 3 * al(b_f4) + 3 * al(b_u) + al(b_sh) + 4 * al(b_t) + al(b_state) + al(b_pk) + al(b_pc) + al(b_nl) +
+  const size_t total = al(b_P) + al(b_I) + 3 * al(b_f4) + 3 * al(b_u) + al(b_sh) + 8 * al(b_t) + al(b_state) + al(b_pk) + al(b_pc) + al(b_nl) +
                        al(b_map) + 3 * al(b_num) + al(b_words) + 256;
   char* mem = nullptr;
   cudaStream_t st = nullptr;
@@ -809,8 +910,9 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
   B.scratch = reinterpret_cast<uint32_t*>(take(b_u));
   B.qpos = reinterpret_cast<int32_t*>(take(b_u));
   B.shapes = reinterpret_cast<Shape*>(take(b_sh));
-  Task* lists[2][2];
-  for (auto& l : lists) { l[0] = reinterpret_cast<Task*>(take(b_t)); l[1] = reinterpret_cast<Task*>(take(b_t)); }
+  Task* lists[2][4];   // per level parity: big, small, tiny and mid tasks
+  for (auto& l : lists)
+    for (auto& x : l) x = reinterpret_cast<Task*>(take(b_t));
   Big G;
   G.state = reinterpret_cast<BigState*>(take(b_state));
   G.pk = reinterpret_cast<unsigned long long*>(take(b_pk));
@@ -822,29 +924,32 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
   int32_t* dpop = reinterpret_cast<int32_t*>(take(b_num));
   uint32_t* dwords = reinterpret_cast<uint32_t*>(take(b_words));
   char* tail = mem + o;
-  B.counters = reinterpret_cast<uint32_t*>(tail);          // 3 words
-  B.root_box = reinterpret_cast<float*>(tail + 16);        // 6 floats
-  B.root_leaf = reinterpret_cast<int32_t*>(tail + 48);
+  B.counters = reinterpret_cast<uint32_t*>(tail);          // 5 words
+  B.root_box = reinterpret_cast<float*>(tail + 32);        // 6 floats
+  B.root_leaf = reinterpret_cast<int32_t*>(tail + 64);
   B.leaf = leaf;
   if (cudaMemcpyAsync(dP, P, b_P, cudaMemcpyHostToDevice, st) != cudaSuccess || cudaMemcpyAsync(dI, I, b_I, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail("upload");
-  cudaMemsetAsync(tail, 0, 64, st);
+  cudaMemsetAsync(tail, 0, 128, st);
   tri_boxes<<<(n + 255) / 256, 256, 0, st>>>(dP, dI, n, bmin, bmax, cen, B.order);
   if (timing) { cudaStreamSynchronize(st); mark(0, tp); }
   const Task root{0, int32_t(n), -1, 0};
-  uint32_t nb = n >= uint32_t(BIG_TASK) ? 1 : 0, ns = 1 - nb;
-  if (cudaMemcpyAsync(lists[0][nb ? 0 : 1], &root, sizeof(Task), cudaMemcpyHostToDevice, st) != cudaSuccess) return fail("upload");
+  uint32_t nb = n >= uint32_t(BIG_TASK) ? 1 : 0, nm = !nb && n >= uint32_t(MID_TASK) ? 1 : 0, nt = n <= uint32_t(TINY) ? 1 : 0,
+           ns = 1 - nb - nm - nt;
+  if (cudaMemcpyAsync(lists[0][nb ? 0 : nm ? 3 : nt ? 2 : 1], &root, sizeof(Task), cudaMemcpyHostToDevice, st) != cudaSuccess) return fail("upload");
   int cur = 0;
-  uint32_t counts[3];
+  uint32_t counts[5];
   std::vector<Task> big;              // this level's big tasks, read back after each level
   std::vector<uint32_t> plan;         // per block its task, then per task its first block and chunk count
   std::vector<uint32_t> level_end;    // shapes emitted up to and including each level
   if (nb) big.push_back(root);
-  for (int level = 0; nb + ns > 0; level++) {
+  for (int level = 0; nb + nm + ns + nt > 0; level++) {
     if (level > 4096) return fail("level cap");
     B.next_big = lists[cur ^ 1][0];
     B.next_small = lists[cur ^ 1][1];
-    cudaMemsetAsync(B.counters + 1, 0, 8, st);
+    B.next_tiny = lists[cur ^ 1][2];
+    B.next_mid = lists[cur ^ 1][3];
+    cudaMemsetAsync(B.counters + 1, 0, 16, st);
     if (nb) {
       uint32_t blocks = 0;
       for (const Task& t : big) blocks += uint32_t((t.e - t.s + CHUNK - 1) / CHUNK);
@@ -869,11 +974,15 @@ bool gpu_sah_build(const float* P, uint32_t n_verts, const uint32_t* I, uint32_t
       big_part_bottom<<<blocks, BT, 0, st>>>(B, G);
       big_finish<<<blocks, BT, 0, st>>>(B, G);
     }
+    if (nm) mid_tasks<<<nm, MT, 0, st>>>(B, lists[cur][3]);
     if (ns) small_tasks<<<(ns + WPB - 1) / WPB, 32 * WPB, 0, st>>>(B, lists[cur][1], ns);
-    if (cudaMemcpyAsync(counts, B.counters, 12, cudaMemcpyDeviceToHost, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+    if (nt) tiny_tasks<<<(nt + 127) / 128, 128, 0, st>>>(B, lists[cur][2], nt);
+    if (cudaMemcpyAsync(counts, B.counters, 20, cudaMemcpyDeviceToHost, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
       return fail("level");
     nb = counts[1];
     ns = counts[2];
+    nt = counts[3];
+    nm = counts[4];
     level_end.push_back(counts[0]);
     big.resize(nb);
     if (nb && (cudaMemcpyAsync(big.data(), lists[cur ^ 1][0], nb * sizeof(Task), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
