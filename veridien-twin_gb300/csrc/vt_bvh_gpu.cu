@@ -473,6 +473,15 @@ __global__ void __launch_bounds__(32 * WPB) small_tasks(Build B, const Task* __r
 // A range of at most TINY slots on one thread, in the host builder's own sequential form: node box by strict
 // comparisons (the first slot among equal values), bins by the double expression, the SAH price of each split after
 // a non-empty bin from the two sides' boxes, and gpu/bvh.js's swap-with-the-end partition.
+//
+// FP64 issues at a small fraction of FP32 on this part, so a lane visits only its own splits (the set bits of its
+// bins), and splits are compared on the undivided sum X = n_l A_l + n_r A_r. The host's cost 1 + X / parent does
+// not decrease with X, and it keeps the first split of least cost. Two sums more than tol = (parent + X) 2^-49
+// apart (eight units in the last place of the cost) give different costs, so only splits within tol of the best
+// sum get the exact cost and the host's strict comparison; a degenerate or non-finite parent area takes the exact
+// cost of every split.
+__device__ __forceinline__ double sah_cost(double X, double parent) { return 1.0 + 1.0 * X / parent; }
+
 __global__ void __launch_bounds__(128) tiny_tasks(Build B, const Task* __restrict__ tasks, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -502,7 +511,8 @@ __global__ void __launch_bounds__(128) tiny_tasks(Build B, const Task* __restric
   double plo[3], phi[3];
   for (int k = 0; k < 3; k++) { plo[k] = double(lo[k]); phi[k] = double(hi[k]); }
   const double parent = half_area(plo, phi);
-  double best_cost = INFINITY;
+  const bool exact = !(parent > 0.0 && parent < INFINITY);
+  double best_x = 0.0, best_cost = INFINITY;   // best_cost NaN: not yet computed for best_x
   int best_axis = -1, best_bin = -1;
   uint8_t bn[TINY];
   for (int ax = 0; ax < 3; ax++) {
@@ -512,8 +522,9 @@ __global__ void __launch_bounds__(128) tiny_tasks(Build B, const Task* __restric
       bn[j] = uint8_t(bin_of(comp(B.cen[tt[j]], ax), origin[ax], scale[ax]));
       present |= 1u << bn[j];
     }
-    for (int v = 0; v < BINS - 1; v++) {
-      if (!(present >> v & 1u) || !(present >> (v + 1))) continue;   // an empty bin, or nothing to its right
+    // the splits after a non-empty bin with something to their right, in increasing bin order
+    for (uint32_t cand = present & ((1u << (31 - __clz(present))) - 1u); cand; cand &= cand - 1u) {
+      const int v = __ffs(cand) - 1;
       float ll[3] = {INFINITY, INFINITY, INFINITY}, lh[3] = {-INFINITY, -INFINITY, -INFINITY};
       float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
       uint32_t nl = 0;
@@ -527,10 +538,31 @@ __global__ void __launch_bounds__(128) tiny_tasks(Build B, const Task* __restric
       }
       const double la[3] = {double(ll[0]), double(ll[1]), double(ll[2])}, lb[3] = {double(lh[0]), double(lh[1]), double(lh[2])};
       const double ra[3] = {double(rl[0]), double(rl[1]), double(rl[2])}, rb[3] = {double(rh[0]), double(rh[1]), double(rh[2])};
-      const double cost = 1.0 + 1.0 * (double(nl) * half_area(la, lb) + double(uint32_t(cnt) - nl) * half_area(ra, rb)) / parent;
-      if (cost < best_cost) { best_cost = cost; best_axis = ax; best_bin = v; }
+      const double X = double(nl) * half_area(la, lb) + double(uint32_t(cnt) - nl) * half_area(ra, rb);
+      bool take;
+      if (exact || best_axis < 0) {
+        const double c = sah_cost(X, parent);
+        if (best_axis >= 0 && best_cost != best_cost) best_cost = sah_cost(best_x, parent);
+        take = c < best_cost;
+        if (take) best_cost = c;
+      } else {
+        const double tol = (parent + best_x) * 0x1p-49;
+        if (X < best_x - tol) {
+          take = true;
+          best_cost = NAN;
+        } else if (X > best_x + tol) {
+          take = false;
+        } else {
+          if (best_cost != best_cost) best_cost = sah_cost(best_x, parent);
+          const double c = sah_cost(X, parent);
+          take = c < best_cost;
+          if (take) best_cost = c;
+        }
+      }
+      if (take) { best_x = X; best_axis = ax; best_bin = v; }
     }
   }
+  if (best_axis >= 0 && best_cost != best_cost) best_cost = sah_cost(best_x, parent);
   int32_t m;
   if (best_axis < 0) {
     if (cnt <= int32_t(B.leaf) * 4) {
