@@ -74,6 +74,33 @@ def test_chain_bit_exact(rendered, k):
     assert 5 < rgba[..., :3].mean() < 250     # not saturated or black: the comparison means something
 
 
+@pytest.mark.parametrize("k", [0, 1, 3])
+def test_chain_bit_exact_1280x720(k):
+    """The frame size the sensor chain is measured at (1280 x 720): every fused tile of the expose, demosaic, noise
+    reduction and output passes, the image's ragged right and bottom tiles and the block statistics, bit for bit."""
+    sc = dome.make_dome_scene(seed=2, width=1280, height=720, level=4, with_instruments=2)
+    r = TwinRenderer.create(sc)
+    try:
+        T = dome.instrument_poses(n_poses=1, n_tools=2, seed=5)[0]
+        r.set_pose_array(np.concatenate([A.identity_poses(1), T]))
+        r.renderCamera(0, spp=1, lightSamples=1, seed=2, mode=A.VT_SHADE_PATH, max_depth=2)
+        L = r.readback(0, "linear")
+        out = r.sensor(0, seed=9, frame=3, exposure_s=2e-3, gain=1.5, params=VARIANTS[k])
+        raw_w, rgba_w, yuv_w, st_w = O.isp_chain(out["uniform"], L, r.relative_illumination(0))
+        raw, rgba = r.readback(0, "raw"), r.readback(0, "rgba8")
+        assert raw.shape == (720, 1280)
+        assert np.array_equal(raw, raw_w), (np.abs(raw - raw_w).max(), (raw != raw_w).sum())
+        assert np.array_equal(rgba, rgba_w), ((rgba != rgba_w).sum(),)
+        assert np.array_equal(out["stats"], st_w)
+        if int(out["uniform"][48]):
+            yuv = r.readback(0, "yuv420")
+            for plane in ("y", "cb", "cr"):
+                assert np.array_equal(yuv[plane], yuv_w[plane]), plane
+        assert 5 < rgba[..., :3].mean() < 250
+    finally:
+        r.destroy()
+
+
 def test_auto_exposure_converges(rendered):
     """AE (gpu/sensor.js:128) moves the exposure toward the target mean luma 0.45 frame by frame; AWB gains stay
     finite and positive."""
