@@ -564,8 +564,10 @@ def calib_bench(torch, device=0):
                            "emitter materials (zero gradient)", "setup_s": setup_s, "forward_ms": fms, "backward_ms": bms,
             "forward_msamples_per_s": samples / (fms / 1e3) / 1e6, "loss_at_start": float(loss0), "forms": forms,
             "forms_note": "the render alone (image loss with the intrinsics' derivative): every path's record kept, or the paths "
-                          "traced again in chunks of sub-samples through the same kernels (the form used when the records do not fit): "
-                          "'replay' sizes the chunk to the free memory (here all 32 sub-samples), 'replay_chunks_of_4' takes 8 chunks",
+                          "traced in chunks of sub-samples through the same kernels (the form used when the records do not fit), "
+                          "keeping only each path's hit triangles and shadow outcomes (24 B), from which the backward shades the "
+                          "paths again without tracing: 'replay' sizes the chunk to the free memory (here all 32 sub-samples), "
+                          "'replay_chunks_of_4' takes 8 chunks",
             "grad_check": {"entries": len(ids), "h": 3e-3, "vector_rel_err": vec, "worst_entry_rel_err": worst,
                            "note": "GPU central differences of the FP32 render (FP64 loss) on albedo and lamp entries; FP64-oracle "
                                    "differences (albedos, lamps at h = 1e-4; intrinsics with the path decisions frozen) are in "

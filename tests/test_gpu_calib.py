@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from vtwin import _abi as A
 from vtwin import dome
 from vtwin.renderer import TwinRenderer
 
@@ -325,12 +326,15 @@ def test_calibration_function_with_torch(rig):
     assert float(loss.detach()) < 0.05 * first
 
 
-@pytest.mark.parametrize("replay", [True, 1, 3])
-def test_stored_and_replayed_paths_agree(rig, replay):
+@pytest.mark.parametrize("replay,retrace", [(True, False), (1, False), (3, False), (True, True), (3, True)])
+def test_stored_and_replayed_paths_agree(rig, replay, retrace, monkeypatch):
     """The forward that keeps every path's record and the replay form, which traces the paths again in chunks of
     sub-samples (all 4 at once, 4 chunks of 1, chunks of 3 and 1) through the same wavefront kernels: the images and
     the loss are identical bit for bit (the per-pixel sums carry across chunks in sub-sample order), the gradients
-    agree to the order of their FP64 accumulation."""
+    agree to the order of their FP64 accumulation. The replay backward re-shades from the forward's recorded hits
+    and shadow outcomes, or (retrace, VT_CALIB_RETRACE=1) traces every path again."""
+    if retrace:
+        monkeypatch.setenv("VT_CALIB_RETRACE", "1")
     r, sc, info, t_alb, t_lamp, targets = rig
     alb = f32(np.clip(t_alb * 1.05, 0.01, 1.0))
     lamp = f32(t_lamp * 0.95)
@@ -345,3 +349,56 @@ def test_stored_and_replayed_paths_agree(rig, replay):
     assert l_s == l_r
     np.testing.assert_allclose(ga_s, ga_r, rtol=1e-9, atol=1e-12 * np.abs(ga_r).max())
     np.testing.assert_allclose(gl_s, gl_r, rtol=1e-9, atol=1e-12 * np.abs(gl_r).max())
+
+
+def test_replayed_decisions_with_posed_bodies(monkeypatch):
+    """The replay backward's recorded decisions on a scene with posed instrument bodies: an extension ray that met a
+    body meets the recorded triangle again in the body's frame at the path's time.
+    - Without the intrinsics' term, the stored form, the replay form from recorded decisions and the replay form
+      tracing again give identical images and losses, and albedo and lamp gradients that agree to the order of
+      their FP64 accumulation.
+    - With it, the stored forward shades with the derivative-record kernel and the replay forward with the plain
+      one, whose rays can differ in their last bits. The three forms' gradients, intrinsics included, then agree to
+      1e-6."""
+    sc = dome.make_dome_scene(seed=4, width=96, height=64, level=3, with_instruments=2)
+    sc["cameras"] = dome.batched_cameras(seed=3, n=2, width=96, height=64)
+    for cam in sc["cameras"]:
+        cam["fx"] = cam["fy"] = 300.0 * cam["size"][0] / 640.0
+    r = TwinRenderer.create(sc)
+    try:
+        T = dome.instrument_poses(n_poses=1, n_tools=2, seed=2)[0]
+        r.set_pose_array(np.concatenate([A.identity_poses(1), T]))
+        info = r.calib_setup(n_nodes=128, lamp_samples=4)
+        alb = np.clip(np.array([m["rho"] for m in sc["materials"]], np.float64), 0.05, 1.0)
+        lamp = np.full(info["n_lamps"], 50.0)
+        kw = dict(spp=3, max_depth=3)
+        _, tg = r.calib_forward([0, 1], alb, lamp, **kw)
+
+        def run(intrinsics):
+            out = {}
+            for name, rp, rt in (("stored", False, "0"), ("decisions", True, "0"), ("retrace", 2, "1")):
+                monkeypatch.setenv("VT_CALIB_RETRACE", rt)
+                l, im = r.calib_forward([0, 1], f32(alb * 0.9), f32(lamp), targets=tg, replay=rp, intrinsics=intrinsics, **kw)
+                ga, gl = r.calib_backward()
+                out[name] = (l, im, ga, gl, r.calib_intrinsics_grad() if intrinsics else None)
+            return out
+
+        out = run(False)
+        l_s, im_s, ga_s, gl_s, _ = out["stored"]
+        assert np.abs(ga_s).max() > 0
+        for name in ("decisions", "retrace"):
+            l, im, ga, gl, _ = out[name]
+            assert l == l_s and all(np.array_equal(a, b) for a, b in zip(im, im_s)), name
+            np.testing.assert_allclose(ga, ga_s, rtol=1e-9, atol=1e-12 * np.abs(ga_s).max())
+            np.testing.assert_allclose(gl, gl_s, rtol=1e-9, atol=1e-12 * np.abs(gl_s).max())
+        out = run(True)
+        ref = out["stored"]
+        assert np.abs(ref[4]).max() > 0
+        for name in ("decisions", "retrace"):
+            errs = [np.linalg.norm(out[name][k] - ref[k]) / np.linalg.norm(ref[k]) for k in (2, 3, 4)]
+            print(f"\nposed bodies, {name} vs stored with the intrinsics' term: albedo {errs[0]:.1e}, lamps {errs[1]:.1e}, "
+                  f"intrinsics {errs[2]:.1e}")
+            assert max(errs) < 1e-6, (name, errs)
+    finally:
+        monkeypatch.delenv("VT_CALIB_RETRACE", raising=False)
+        r.destroy()

@@ -151,6 +151,7 @@ vt_status vt_destroy(vt_ctx* ctx) {
   cudaFree(ctx->nodes.direct_mem);
   cudaFree(ctx->calib.records);
   cudaFree(ctx->calib.tan);
+  cudaFree(ctx->calib.dec);
   for (float4* p : ctx->calib.image) cudaFree(p);
   for (float4* p : ctx->calib.target) cudaFree(p);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);

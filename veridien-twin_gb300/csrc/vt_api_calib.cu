@@ -2,6 +2,7 @@
 // radiosity nodes from the static triangles, the node form factors F and emitter transfer D, the forward render and
 // loss, the path-replay backward with the transposed-Jacobi adjoint, and the analytic KB4 reprojection Jacobian.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -232,6 +233,7 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
     rec_total += size_t(vtk::tiled_pixels(cps[c].w, cps[c].h, cps[c].tile_w, cps[c].tile_h)) * cps[c].spp;
   }
   K.stored = false;
+  K.use_dec = false;
   K.want_k = q->intrinsics != 0;
   K.have_k = false;
   uint32_t wave_paths = 0;
@@ -302,6 +304,15 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
     ctx->d_wave = wave;
     ctx->wave_cap = wave_cap;
     if (!ok) return fail(ctx, VT_ERR_OOM, "calib: replay buffers (one chunk of path records and the wave state)");
+    // the paths' decisions (24 B each) when they fit in a quarter of what is left; otherwise the backward traces
+    // again. VT_CALIB_RETRACE=1 makes it trace again regardless.
+    const char* rt = std::getenv("VT_CALIB_RETRACE");
+    const size_t dec_bytes = vtk::calib_dec_bytes(uint32_t(std::min<size_t>(rec_total, 0xffffffffu)));
+    K.use_dec = false;
+    if (!(rt && *rt && *rt != '0') && rec_total < 0xffffffffu) {
+      cudaMemGetInfo(&fr, &tot);
+      K.use_dec = (K.dec_cap >= dec_bytes || dec_bytes <= fr / 4) && grow(K.dec, K.dec_cap, dec_bytes);
+    }
   }
   double total = 0.0;
   off = 0;
@@ -322,7 +333,8 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
       nb = 0;
       for (uint32_t i0 = 0; i0 < cp.spp; i0 += K.chunk)
         nb = vtk::calib_wave_chunk(dev_scene(ctx), cp, C, wb, K.wave_paths, K.records, nullptr, i0, std::min(cp.spp, i0 + K.chunk), 0, wblocks,
-                                   ctx->stream);
+                                   ctx->stream, K.use_dec ? static_cast<char*>(K.dec) + K.rec_off[c] * vtk::calib_dec_bytes(1) : nullptr,
+                                   K.use_dec ? 1 : 0);
     }
     vtk::launch_sum(K.partials, nb, K.loss, ctx->stream);
     VT_CK(cudaGetLastError());
@@ -365,7 +377,8 @@ vt_status vt_calib_backward(vt_ctx* ctx, double* g_albedo, double* g_lamp) {
       const int wblocks = std::min<int>(ctx->wave_blocks, int(K.max_partials));
       for (uint32_t i0 = 0; i0 < cp.spp; i0 += K.chunk)
         vtk::calib_wave_chunk(dev_scene(ctx), cp, calib_dev(ctx, cam), wb, K.wave_paths, K.records, K.want_k ? K.tan : nullptr, i0,
-                              std::min(cp.spp, i0 + K.chunk), K.want_k ? 2 : 1, wblocks, ctx->stream);
+                              std::min(cp.spp, i0 + K.chunk), K.want_k ? 2 : 1, wblocks, ctx->stream,
+                              K.use_dec ? static_cast<char*>(K.dec) + K.rec_off[c] * vtk::calib_dec_bytes(1) : nullptr, K.use_dec ? 2 : 0);
     }
   }
   K.have_k = K.want_k;

@@ -67,6 +67,16 @@ struct CalTan {
   uint32_t tri[CAL_MAX_DEPTH], inst[CAL_MAX_DEPTH];
 };
 
+// a path's discrete decisions (replay form): per bounce the triangle and instance its extension ray met (~0 and 0xff:
+// none), and one bit per vertex and light sample, set when that sample's shadow ray was occluded
+struct CalDec {
+  uint32_t tri[CAL_MAX_DEPTH];
+  uint8_t inst[CAL_MAX_DEPTH];
+  uint32_t occ;
+};
+static_assert(CAL_MAX_DEPTH * CAL_MAX_NL <= 32, "one occlusion bit per vertex and light sample");
+static_assert(VT_MAX_INST < 0xff, "instances fit a byte");
+
 // emitter sample by the area CDF, with the index of the triangle (gpu/wgsl/shade.wgsl.js:31)
 __device__ __forceinline__ uint32_t sample_emitter_idx(const Scene& S, float3 u, float time, float3& p, float3& n, float3& axis) {
   uint32_t lo = 0, hi = S.emit_n - 1u;
@@ -205,7 +215,7 @@ constexpr int WT = 256;
 
 template <bool TAN>
 __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const CamParams cp, const CalibDev C, WaveBufs wb, CalPath* rec,
-                                                        CalTan* tan, uint32_t b) {
+                                                        CalTan* tan, uint32_t b, CalDec* dec, int dmode) {
   const uint32_t n = *wb.count_in;
   const uint32_t nl = cp.n_light;
   const float fnl = float(nl);
@@ -220,6 +230,13 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
     const float3 o = xyz(o4), d = xyz(d4);
     const float tt = o4.w, pb_prev = d4.w;
     const Hit h{hv.x, hv.y, hv.z, __float_as_uint(hv.w), wb.hinst[p]};
+    if (dmode == 1) {
+      CalDec& D = dec[p];
+      if (b == 1) D.occ = 0u;
+      D.tri[b - 1] = h.tri;
+      D.inst[b - 1] = h.inst == MISS ? uint8_t(0xff) : uint8_t(h.inst);
+    }
+    const uint32_t occ = dmode == 2 ? dec[p].occ : 0u;
     bool cont = false, shadow = false;
     Tan3 Jo, Jd, Jx;
     float3 dpb, dt;
@@ -290,6 +307,14 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
             const float3 dq = tan_light(S, s.p, nrm, lp, ln, la, area, fnl, V.q[j], Jx, Jn);
             tan[p].dq[vk][j][0] = dq.x; tan[p].dq[vk][j][1] = dq.y; tan[p].dq[vk][j][2] = dq.z;
           }
+          if (dmode == 2) {
+            // the recorded shadow ray's outcome: an occluded sample is cleared as calib_shadow_kernel clears it
+            if ((occ >> (vk * CAL_MAX_NL + j)) & 1u) {
+              V.q[j] = 0.0f;
+              if (TAN) tan[p].dq[vk][j][0] = tan[p].dq[vk][j][1] = tan[p].dq[vk][j][2] = 0.0f;
+            }
+            continue;
+          }
           const float3 so = offset_ray(s.p, s.ng, wi);
           srec[3 * j] = make_float4(so.x, so.y, so.z, dist - 2e-5f);
           srec[3 * j + 1] = make_float4(wi.x, wi.y, wi.z, 1.0f);
@@ -333,7 +358,7 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
 
 // any hit of the pending light samples on persistent lanes; an occluded sample's contribution is cleared in the record
 template <bool TAN>
-__global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, const CamParams cp, WaveBufs wb, CalPath* rec, CalTan* tan) {
+__global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, const CamParams cp, WaveBufs wb, CalPath* rec, CalTan* tan, CalDec* dec) {
   const uint32_t n = *wb.count_sh;
   const uint32_t nl = cp.n_light;
   const uint32_t skip = ldu(S.su + 7);
@@ -373,6 +398,7 @@ __global__ void __launch_bounds__(WT, 4) calib_shadow_kernel(const Scene S, cons
       const uint32_t vk = __float_as_uint(srec[3 * j + 2].z);
       rec[p].v[vk].q[j] = 0.0f;
       if (TAN) tan[p].dq[vk][j][0] = tan[p].dq[vk][j][1] = tan[p].dq[vk][j][2] = 0.0f;
+      if (dec) dec[p].occ |= 1u << (vk * CAL_MAX_NL + j);
     }
     j++;
     active = next_sample();
@@ -612,8 +638,53 @@ size_t calib_record_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalPat
 size_t calib_tan_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalTan); }
 
 // the paths of sub-samples [i0, i1) of the camera through the wavefront, their records at rec[(i - i0) n_pix + id]
+// tri_hit's arithmetic without its range checks: for a hit tri_hit accepted, the same t, u, v; a recorded hit is met
+// again even when the ray moved by rounding (the derivative-record kernel's ray can differ from the plain kernel's
+// in its last bits)
+__device__ __forceinline__ void tri_uvt(const Scene& S, uint32_t k, float3 o, float3 d, float& t, float& u, float& v) {
+  const float4* r = S.tris + 4u * k;
+  const float3 v0 = xyz(__ldg(r)), e1 = xyz(__ldg(r + 1)), e2 = xyz(__ldg(r + 2));
+  const float3 p = cross(d, e2);
+  const float det = dot(e1, p);
+  const float inv = 1.0f / det;
+  const float3 s = o - v0;
+  u = dot(s, p) * inv;
+  const float3 q = cross(s, e1);
+  v = dot(d, q) * inv;
+  t = dot(e2, q) * inv;
+}
+
+// the extension rays of a replayed bounce meet the triangles the traced bounce recorded: the traversal's frame (the
+// world, or the instance's pose at the path's time) and its triangle arithmetic, so t, u, v are the traced hit's
+__global__ void __launch_bounds__(256) calib_rehit_kernel(const Scene S, WaveBufs wb, const CalDec* __restrict__ dec, uint32_t b) {
+  const uint32_t n = *wb.count_in;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = wb.q_in[k];
+    const uint32_t tri = dec[p].tri[b - 1], inst = dec[p].inst[b - 1];
+    float4 hit = make_float4(BIG, 0.0f, 0.0f, __uint_as_float(MISS));
+    uint32_t hinst = MISS;
+    if (tri != MISS) {
+      const float4 o4 = wb.o[p], d4 = wb.d[p];
+      float3 o = xyz(o4), d = xyz(d4);
+      if (inst != 0xffu) {
+        Rot R;
+        float3 pp;
+        inst_pose(S, inst, o4.w, R, pp);
+        o = rtmul(R, o - pp);
+        d = rtmul(R, d);
+        hinst = inst;
+      }
+      float t, u, v;
+      tri_uvt(S, tri, o, d, t, u, v);
+      hit = make_float4(t, u, v, __uint_as_float(tri));
+    }
+    wb.hit[p] = hit;
+    wb.hinst[p] = hinst;
+  }
+}
+
 static void calib_trace(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, CalPath* rec, CalTan* tan,
-                        uint32_t i0, uint32_t i1, int blocks, cudaStream_t st) {
+                        uint32_t i0, uint32_t i1, int blocks, cudaStream_t st, CalDec* dec, int dmode) {
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t per_wave = std::max(1u, std::min(i1 - i0, wave_paths / std::max(1u, n_pix)));
   for (uint32_t w0 = i0; w0 < i1; w0 += per_wave) {
@@ -622,6 +693,8 @@ static void calib_trace(const Scene& S, const CamParams& cp, const CalibDev& C, 
     launch_wave_gen(cp, wb, w0, n_i, n_pix, blocks, st);
     CalPath* rb = rec + size_t(w0 - i0) * n_pix;
     CalTan* tb = tan ? tan + size_t(w0 - i0) * n_pix : nullptr;
+    CalDec* db = dec && dmode ? dec + size_t(w0) * n_pix : nullptr;
+    const int dm = db ? dmode : 0;
     for (uint32_t b = 1; b <= cp.max_depth; b++) {
       WaveBufs w = wb;
       w.q_in = (b & 1) ? wb.qa : wb.qb;
@@ -631,12 +704,14 @@ static void calib_trace(const Scene& S, const CamParams& cp, const CalibDev& C, 
       w.count_sh = wb.counts + 2;
       cudaMemsetAsync(w.count_out, 0, 4, st);
       cudaMemsetAsync(w.count_sh, 0, 4, st);
-      launch_wave_extend(S, cp, w, blocks, st);
-      if (tb) calib_shade_kernel<true><<<calib_shade_grid<true>(), WT, 0, st>>>(S, cp, C, w, rb, tb, b);
-      else calib_shade_kernel<false><<<calib_shade_grid<false>(), WT, 0, st>>>(S, cp, C, w, rb, nullptr, b);
+      if (dm == 2) calib_rehit_kernel<<<std::max(1, blocks), 256, 0, st>>>(S, w, db, b);
+      else launch_wave_extend(S, cp, w, blocks, st);
+      if (tb) calib_shade_kernel<true><<<calib_shade_grid<true>(), WT, 0, st>>>(S, cp, C, w, rb, tb, b, db, dm);
+      else calib_shade_kernel<false><<<calib_shade_grid<false>(), WT, 0, st>>>(S, cp, C, w, rb, nullptr, b, db, dm);
+      if (dm == 2) continue;   // the recorded shadow outcomes were applied by the shading
       cudaMemsetAsync(w.fetch, 0, 4, st);
-      if (tb) calib_shadow_kernel<true><<<blocks, WT, 0, st>>>(S, cp, w, rb, tb);
-      else calib_shadow_kernel<false><<<blocks, WT, 0, st>>>(S, cp, w, rb, nullptr);
+      if (tb) calib_shadow_kernel<true><<<blocks, WT, 0, st>>>(S, cp, w, rb, tb, db);
+      else calib_shadow_kernel<false><<<blocks, WT, 0, st>>>(S, cp, w, rb, nullptr, db);
     }
   }
 }
@@ -646,11 +721,13 @@ uint32_t calib_wave_forward(const Scene& S, const CamParams& cp, const CalibDev&
   return calib_wave_chunk(S, cp, C, wb, wave_paths, records, tangents, 0, cp.spp, 0, blocks, st);
 }
 
+size_t calib_dec_bytes(uint32_t paths) { return size_t(paths) * sizeof(CalDec); }
+
 uint32_t calib_wave_chunk(const Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records, void* tangents,
-                          uint32_t i0, uint32_t i1, int mode, int blocks, cudaStream_t st) {
+                          uint32_t i0, uint32_t i1, int mode, int blocks, cudaStream_t st, void* decisions, int dec_mode) {
   CalPath* rec = static_cast<CalPath*>(records);
   CalTan* tan = static_cast<CalTan*>(tangents);
-  calib_trace(S, cp, C, wb, wave_paths, rec, tan, i0, i1, blocks, st);
+  calib_trace(S, cp, C, wb, wave_paths, rec, tan, i0, i1, blocks, st, static_cast<CalDec*>(decisions), dec_mode);
   const uint32_t n_pix = tiled_pixels(cp.w, cp.h, cp.tile_w, cp.tile_h);
   const uint32_t grid = std::max(1u, std::min(uint32_t(blocks), (n_pix + CT - 1) / CT));
   const size_t smem = mode ? size_t(3 * C.n_mat + C.n_lamps) * 8 : 0;

@@ -44,8 +44,16 @@ void calib_export_paths(const CamParams& cp, const void* records, const void* ta
 // and the per-block loss partials, whose number it returns), 1 accumulates the gradients of the image loss
 // (albedos, emitter radiances, node light), 2 also the derivative in the camera's intrinsics (C.g_K). The image of
 // the forward's chunks is the stored form's image bit for bit.
+//
+// `decisions` (calib_dec_bytes per path of the camera, at decisions[i n_pix + id]; NULL: none) keeps each path's
+// discrete decisions: per bounce the triangle and instance the extension ray met, per vertex and light sample
+// whether the shadow ray was occluded. dec_mode 1 records them while tracing; dec_mode 2 replays them: the extension
+// rays meet the recorded triangles (one intersection each, the traversal's own arithmetic) and the occluded samples
+// are cleared without shadow rays, so the records are the traced ones bit for bit.
 uint32_t calib_wave_chunk(const vtd::Scene& S, const CamParams& cp, const CalibDev& C, WaveBufs wb, uint32_t wave_paths, void* records,
-                          void* tangents, uint32_t i0, uint32_t i1, int mode, int blocks, cudaStream_t st);
+                          void* tangents, uint32_t i0, uint32_t i1, int mode, int blocks, cudaStream_t st, void* decisions = nullptr,
+                          int dec_mode = 0);
+size_t calib_dec_bytes(uint32_t paths);
 // D[i][t]: irradiance at node i (centre, normal) from emitter triangle t at unit radiance, with visibility
 void launch_direct_transfer(const vtd::Scene& S, const float* centres, const float* normals, uint32_t n, uint32_t n_lamps,
                             uint32_t samples, float* D, cudaStream_t st);

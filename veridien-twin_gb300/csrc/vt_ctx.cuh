@@ -120,8 +120,12 @@ struct vt_ctx {
     double* g_K = nullptr;   // 8 per scene camera
     std::vector<size_t> rec_off;
     bool stored = false;
-    // replay form: sub-samples per chunk and the wave size of the tracing
+    // replay form: sub-samples per chunk and the wave size of the tracing; every path's discrete decisions (per
+    // camera at rec_off), kept by the forward when they fit so that the backward re-shades without tracing
     uint32_t chunk = 0, wave_paths = 0;
+    void* dec = nullptr;
+    size_t dec_cap = 0;
+    bool use_dec = false;
     // last forward
     std::vector<uint32_t> cams;
     uint32_t spp = 0, nl = 0, seed = 0, depth = 0, iters = 0;
