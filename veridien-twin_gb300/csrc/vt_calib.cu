@@ -232,7 +232,12 @@ __global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const Ca
     const Hit h{hv.x, hv.y, hv.z, __float_as_uint(hv.w), wb.hinst[p]};
     if (dmode == 1) {
       CalDec& D = dec[p];
-      if (b == 1) D.occ = 0u;
+      // every bounce of the path starts as none: a replay whose path continues where the recorded one stopped (its
+      // rays can differ from the recorded ones in the last bits) meets nothing there, never a stale triangle
+      if (b == 1) {
+        D.occ = 0u;
+        for (uint32_t a = 0; a < CAL_MAX_DEPTH; a++) { D.tri[a] = MISS; D.inst[a] = uint8_t(0xff); }
+      }
       D.tri[b - 1] = h.tri;
       D.inst[b - 1] = h.inst == MISS ? uint8_t(0xff) : uint8_t(h.inst);
     }
