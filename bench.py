@@ -16,7 +16,7 @@ bounded sample of the same frame; the reference itself is JavaScript + WebGPU an
   python bench.py --case radiosity:N:PREC:SWEEPS   one 64-RHS radiosity solve capped at SWEEPS sweeps (fp32|bf16|fp8)
   python bench.py --case radiosity1:N:PREC:SWEEPS  the same with one right-hand side (fp32|fp32tma|bf16|fp8)
   python bench.py --case batch:W:H:SPP:POSES       one 3-camera pose batch (6 instruments, depth 6, sensor on)
-  python bench.py --case calib:W:H:SPP             one calibration forward + backward (3 cameras, depth 3, 4096 nodes)
+  python bench.py --case calib:W:H:SPP[:replay]    one calibration forward + backward (3 cameras, depth 3, 4096 nodes)
   python bench.py --case nodes                     the scene node radiosity on the level-5 and level-8 domes
   python bench.py --case sensor                    the camera sensor chain at 1280x720 and 1920x1200
   python bench.py --case twin[:LEVEL]              the reference's twin frame (3 x 1280x720, presets live / balanced / judge)
@@ -399,7 +399,8 @@ def run_case(spec):
     elif kind == "calib":
         from vtwin.renderer import TwinRenderer
 
-        w, h, spp = (int(x) for x in a)
+        w, h, spp = (int(x) for x in a[:3])
+        replay = len(a) > 3 and a[3] == "replay"
         sc = dome.make_dome_scene(seed=1, width=w, height=h, level=5)
         sc["cameras"] = dome.batched_cameras(seed=3, n=3, width=w, height=h)
         r = TwinRenderer.create(sc)
@@ -408,7 +409,7 @@ def run_case(spec):
         lamp = np.full(info["n_lamps"], 50.0)
         _, tg = r.calib_forward([0, 1, 2], alb, lamp, spp=spp, max_depth=3)
         t0 = time.perf_counter()
-        loss, _ = r.calib_forward([0, 1, 2], alb * 0.9, lamp, targets=tg, images=False, spp=spp, max_depth=3, intrinsics=True)
+        loss, _ = r.calib_forward([0, 1, 2], alb * 0.9, lamp, targets=tg, images=False, spp=spp, max_depth=3, intrinsics=True, replay=replay)
         t1 = time.perf_counter()
         r.calib_backward()
         t2 = time.perf_counter()
