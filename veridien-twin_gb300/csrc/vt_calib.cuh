@@ -66,7 +66,8 @@ size_t jacobi_t_work(uint32_t n);
 // y = a o b (n floats)
 void launch_mul(const float* a, const float* b, float* y, uint32_t n, cudaStream_t st);
 // the calibration model's node radiosity for one channel: B = rho o (DL + F B) by `iters` Jacobi sweeps from
-// B = rho o DL, in FP64 (F in FP32), then H = F B rounded to FP32; B0, B1: n doubles of work
+// B = rho o DL, at FP64 accuracy (F in FP32; float-pair products and sums), then H = F B rounded to FP32; B0, B1:
+// n doubles of work
 void launch_radiosity64(const float* F, const float* rho, const float* DL, uint32_t n, uint32_t iters, double* B0, double* B1, float* H,
                         cudaStream_t st);
 // sum of n doubles (deterministic order) into out
