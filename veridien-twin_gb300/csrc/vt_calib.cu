@@ -151,12 +151,18 @@ __device__ __forceinline__ float3 path_value(const CalibDev& C, const CalPath& P
 }
 
 // d loss / d parameters of one recorded path, given g = d loss / d (path radiance); FP64 into shared accumulators
-__device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, uint32_t nl, double3 gd, double* sh_alb, double* sh_lamp) {
+// a path's albedo gradient: per vertex its material and g-weighted value (on: the vertex exists)
+struct AlbGrad {
+  uint32_t mat[CAL_MAX_DEPTH];
+  float3 val[CAL_MAX_DEPTH];
+  bool on[CAL_MAX_DEPTH];
+};
+
+__device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, uint32_t nl, float3 g, double* sh_lamp, AlbGrad& ag) {
   // Each term is formed in FP32 and added to the FP64 accumulators (FP64 arithmetic runs at a small fraction of
   // this part's FP32 rate; the reductions stay FP64). A term whose albedo product ends at vertex k adds
   // g o value / rho_l to every vertex l <= k: D[k] gathers the g-weighted values of the terms ending at k, and vertex
-  // l receives (sum_{k >= l} D[k]) / rho_l, one atomic per channel.
-  const float3 g = f3(float(gd.x), float(gd.y), float(gd.z));
+  // l receives (sum_{k >= l} D[k]) / rho_l, which the caller sums over the warp per material.
   const float fnl = float(nl);
   float3 T = f3(1, 1, 1);
   float3 D[CAL_MAX_DEPTH], rho[CAL_MAX_DEPTH];
@@ -196,12 +202,37 @@ __device__ __forceinline__ void path_grad(const CalibDev& C, const CalPath& P, u
   float3 acc = f3(0, 0, 0);
 #pragma unroll
   for (int k = CAL_MAX_DEPTH - 1; k >= 0; k--) {
-    if (uint32_t(k) >= P.n) continue;
+    ag.on[k] = uint32_t(k) < P.n;
+    if (!ag.on[k]) continue;
     acc = acc + D[k];
-    const uint32_t m = P.v[k].mat;
-    atomicAdd(sh_alb + 3 * m, double(acc.x / rho[k].x));
-    atomicAdd(sh_alb + 3 * m + 1, double(acc.y / rho[k].y));
-    atomicAdd(sh_alb + 3 * m + 2, double(acc.z / rho[k].z));
+    ag.mat[k] = P.v[k].mat;
+    ag.val[k] = f3(acc.x / rho[k].x, acc.y / rho[k].y, acc.z / rho[k].z);
+  }
+}
+
+// Adds each lane's value (on: it has one) to sh[3 key + c]: the lanes with the same key are summed over the warp in
+// FP32 (a fixed butterfly, so the sum depends only on the warp's lanes), then one FP64 shared atomic per key and
+// channel. Called by all 32 lanes of the warp.
+__device__ __forceinline__ void warp_key_add3(double* sh, uint32_t key, float3 v, bool on) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t pending = __ballot_sync(0xffffffffu, on);
+  while (pending) {
+    const uint32_t leader = __ffs(pending) - 1;
+    const uint32_t k0 = __shfl_sync(0xffffffffu, key, leader);
+    const bool in = on && key == k0;
+    pending &= ~__ballot_sync(0xffffffffu, in);
+    float a = in ? v.x : 0.0f, b = in ? v.y : 0.0f, c = in ? v.z : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if (lane == leader) {
+      atomicAdd(sh + 3 * k0, double(a));
+      atomicAdd(sh + 3 * k0 + 1, double(b));
+      atomicAdd(sh + 3 * k0 + 2, double(c));
+    }
+    if (in) on = false;
   }
 }
 
@@ -432,7 +463,7 @@ __device__ __forceinline__ void path_tangent(const CalibDev& C, const CalPath& P
 
 // the derivative of the loss in the camera's intrinsics from one sub-sample: G = g . dL / d d0 (FP64), chained
 // through d d0 / d K at the sub-sample's image position
-__device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_t id, uint32_t i, const float3* dL, double3 g, double* sh_k) {
+__device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_t id, uint32_t i, const float3* dL, double3 g, double* kacc) {
   uint32_t x, y;
   if (!pixel_xy(cp, id, x, y)) return;
   // the term in FP32, its accumulation in FP64
@@ -444,7 +475,8 @@ __device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_
   const float2 uv = subsample_uv(x, y, i, hs);
   float J[3][8];
   kb4_ray_jacobian(cp.lens, uv.x, uv.y, f3(cp.rx[0], cp.rx[1], cp.rx[2]), f3(cp.ry[0], cp.ry[1], cp.ry[2]), f3(cp.rz[0], cp.rz[1], cp.rz[2]), J);
-  for (int k = 0; k < 8; k++) atomicAdd(sh_k + k, double(G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k]));
+#pragma unroll
+  for (int k = 0; k < 8; k++) kacc[k] += double(G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k]);
 }
 
 // per pixel over the records of sub-samples [i0, i1): backward 0 adds their values to the pixel's running sum (kept in
@@ -464,25 +496,41 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
     __syncthreads();
   }
   double loss = 0.0;
+  // the thread's intrinsics terms, summed in registers (one warp sum and 8 shared atomics per warp at the end: all
+  // lanes add to the same 8 words, where per-path atomics would contend)
+  double kacc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   const float sc = cp.scale / float(cp.spp);
-  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n_pix; id += gridDim.x * blockDim.x) {
-    uint32_t x, y;
-    if (!pixel_xy(cp, id, x, y)) continue;
+  // the block's threads take pixels base + threadIdx.x together, so that a warp's lanes stay together for the
+  // per-material warp sums of the backward
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n_pix; base += gridDim.x * blockDim.x) {
+    const uint32_t id = base + threadIdx.x;
+    uint32_t x = 0, y = 0;
+    const bool valid = id < n_pix && pixel_xy(cp, id, x, y);
     const size_t px = size_t(y) * cp.w + x;
     if (backward) {
-      const float4 I = C.image[px], Tg = C.target ? C.target[px] : make_float4(0.f, 0.f, 0.f, 0.f);
-      const double k = 2.0 * C.inv_count * double(sc);
-      const double3 g = make_double3(k * (double(I.x) - Tg.x), k * (double(I.y) - Tg.y), k * (double(I.z) - Tg.z));
+      double3 g = make_double3(0.0, 0.0, 0.0);
+      if (valid) {
+        const float4 I = C.image[px], Tg = C.target ? C.target[px] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const double k = 2.0 * C.inv_count * double(sc);
+        g = make_double3(k * (double(I.x) - Tg.x), k * (double(I.y) - Tg.y), k * (double(I.z) - Tg.z));
+      }
+      const float3 gf = f3(float(g.x), float(g.y), float(g.z));
       for (uint32_t i = i0; i < i1; i++) {
         const size_t r = size_t(i - i0) * n_pix + id;
-        path_grad(C, rec[r], cp.n_light, g, sh_alb, sh_lamp);
-        if (backward == 2) {
+        AlbGrad ag;
+#pragma unroll
+        for (uint32_t k = 0; k < CAL_MAX_DEPTH; k++) { ag.on[k] = false; ag.mat[k] = 0u; ag.val[k] = f3(0, 0, 0); }
+        if (valid) path_grad(C, rec[r], cp.n_light, gf, sh_lamp, ag);
+#pragma unroll
+        for (uint32_t k = 0; k < CAL_MAX_DEPTH; k++) warp_key_add3(sh_alb, ag.mat[k], ag.val[k], ag.on[k]);
+        if (backward == 2 && valid) {
           float3 dL[3];
           path_tangent(C, rec[r], tan[r], cp.n_light, dL);
-          add_intrinsics_grad(cp, id, i, dL, g, sh_k);
+          add_intrinsics_grad(cp, id, i, dL, g, kacc);
         }
       }
     } else {
+      if (!valid) continue;
       // the sum over sub-samples in order, carried across chunks exactly (a float in the image)
       float3 s = f3(0, 0, 0);
       if (i0 > 0) s = xyz(C.image[px]);
@@ -501,6 +549,14 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
     }
   }
   if (backward) {
+    if (backward == 2) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        double v = kacc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31u) == 0u && v != 0.0) atomicAdd(sh_k + k, v);
+      }
+    }
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < 3 * C.n_mat; k += blockDim.x) if (sm[k] != 0.0) atomicAdd(C.g_albedo + k, sm[k]);
     for (uint32_t k = threadIdx.x; k < C.n_lamps; k += blockDim.x) if (sh_lamp[k] != 0.0) atomicAdd(C.g_lamp + k, sh_lamp[k]);
