@@ -245,7 +245,7 @@ __device__ __forceinline__ void warp_key_add3(double* sh, uint32_t key, float3 v
 constexpr int WT = 256;
 
 template <bool TAN>
-__global__ void __launch_bounds__(WT) calib_shade_kernel(const Scene S, const CamParams cp, const CalibDev C, WaveBufs wb, CalPath* rec,
+__global__ void __launch_bounds__(WT, 3) calib_shade_kernel(const Scene S, const CamParams cp, const CalibDev C, WaveBufs wb, CalPath* rec,
                                                         CalTan* tan, uint32_t b, CalDec* dec, int dmode) {
   const uint32_t n = *wb.count_in;
   const uint32_t nl = cp.n_light;
