@@ -354,8 +354,10 @@ vt_status vt_batch_autotune(vt_ctx* ctx, const vt_batch_req* req, vt_tune_row* t
  *   loss         mean over pixels and channels of (I - T)^2 against per-camera target images (FP64 reduction).
  *
  * The backward differentiates every path (path-replay backpropagation: from its record kept by a wavefront forward,
- * or, when the records do not fit, by tracing the paths again in chunks of sub-samples through the same wavefront
- * kernels) and solves the transposed radiosity
+ * or, when the records do not fit, by shading the paths again in chunks of sub-samples through the same wavefront
+ * kernels, from each path's hit triangles and shadow outcomes kept by the forward, 24 B per path; with the
+ * environment variable VT_CALIB_RETRACE=1, or when those do not fit either, by tracing them again) and solves the
+ * transposed radiosity
  * system lambda = F^T (g_H + rho o lambda) for the nodes' share. Parameters: per-material albedo (RGB, all
  * in (0, 1]) and per-emitter-triangle radiance. KB4 intrinsics enter through vt_reproj_loss (analytic Jacobians)
  * and, with `intrinsics` set, through the image term: forward-mode tangents of each path's primary ray chained
@@ -382,10 +384,11 @@ typedef struct {
   float* images;                                  /* optional out: the rendered images, same layout (host or device) */
   uint32_t replay;                                /* 0: the forward keeps each path's record (160 B) when they fit in half
                                                      the free device memory, and replays otherwise; 1: replay: the paths
-                                                     are traced again, forward and backward, in chunks of sub-samples whose
-                                                     records fit a quarter of the free memory, each chunk's records
-                                                     differentiated before the next is traced (the same kernels and images
-                                                     as the stored form); 1 + c: replay in chunks of at most c sub-samples */
+                                                     are traced in chunks of sub-samples whose records fit a quarter of
+                                                     the free memory (the same kernels and images as the stored form),
+                                                     keeping their hits and shadow outcomes; the backward shades each
+                                                     chunk again from those and differentiates it before the next;
+                                                     1 + c: replay in chunks of at most c sub-samples */
   uint32_t intrinsics;                            /* 1: the backward also gives the image loss's derivative in each
                                                      camera's KB4 intrinsics (vt_calib_intrinsics_grad); the stored form
                                                      then keeps a derivative record per path (320 B) beside its record */

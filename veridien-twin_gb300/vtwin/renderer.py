@@ -495,8 +495,9 @@ class TwinRenderer:
         """Image loss (mean of (I - T)^2 over pixels and channels) of the calibration render; returns (loss, images)
         with images a list of (h, w, 4) float32 arrays per camera (or None). intrinsics: the backward also gives the
         loss's derivative in each camera's KB4 intrinsics (calib_intrinsics_grad). replay: False keeps every path's
-        record when they fit; True traces the paths again in chunks of sub-samples sized to the free memory; an
-        integer c >= 1 traces them again in chunks of at most c sub-samples."""
+        record when they fit; True traces the paths in chunks of sub-samples sized to the free memory, keeping only
+        their hits and shadow outcomes, from which the backward shades each chunk again; an integer c >= 1 does the
+        same in chunks of at most c sub-samples."""
         cams = [self._cam(c) for c in cameras]
         cam_arr = np.ascontiguousarray(cams, np.uint32)
         alb = np.ascontiguousarray(albedo, np.float64).reshape(-1, 3)
