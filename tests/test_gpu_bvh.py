@@ -47,6 +47,18 @@ def test_device_build_matches_oracle_on_random_and_degenerate_meshes():
         _same(build_bvh(P, I, 4, device=0), O.bvh_build(P, I, 4))
 
 
+@pytest.mark.parametrize("leaf", [600, 2500])
+def test_device_build_large_leaves(leaf):
+    """A leaf size large enough that ranges handled by whole blocks (1024-8191 slots) and by chunks (8192 slots and
+    more) end as leaves, or split at the median when no split is priced."""
+    st = dome.make_dome_scene(seed=1, width=32, height=24, level=6)["static"]
+    _same(build_bvh(st["P"], st["I"], leaf, device=0), O.bvh_build(st["P"], st["I"], leaf))
+    rng = np.random.default_rng(12)
+    P = rng.normal(size=(3 * 40000, 3)).astype(np.float32)
+    I = np.arange(3 * 40000, dtype=np.uint32).reshape(-1, 3)
+    _same(build_bvh(P, I, leaf, device=0), O.bvh_build(P, I, leaf))
+
+
 def test_device_build_coincident_centroids_and_signed_zeros():
     rng = np.random.default_rng(3)
     P = np.repeat(rng.normal(size=(40, 3)).astype(np.float32), 3, axis=0)
