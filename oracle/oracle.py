@@ -80,11 +80,15 @@ def bvh_build(pos, idx, leaf=4):
     idx = np.ascontiguousarray(idx, np.uint32).ravel()
     n = len(idx) // 3
     cap = max(4, -(-n // max(1, leaf)) * 2) * 4 + 16
-    nodes = np.zeros(cap * 16, np.uint32)
-    order = np.zeros(max(1, n), np.uint32)
-    info = np.zeros(7)
-    cnt = lib().or_bvh_build(_p(pos, C.c_float), _p(idx, C.c_uint32), C.c_uint32(n), leaf, _p(nodes, C.c_uint32), cap,
-                             _p(order, C.c_uint32), _p(info))
+    while True:
+        nodes = np.zeros(cap * 16, np.uint32)
+        order = np.zeros(max(1, n), np.uint32)
+        info = np.zeros(7)
+        cnt = lib().or_bvh_build(_p(pos, C.c_float), _p(idx, C.c_uint32), C.c_uint32(n), leaf, _p(nodes, C.c_uint32), cap,
+                                 _p(order, C.c_uint32), _p(info))
+        if cnt >= 0 or -cnt <= cap:
+            break
+        cap = -cnt   # the node count the build needs (many leaves smaller than `leaf`)
     assert cnt > 0, cnt
     return {"nodes": nodes[: cnt * 16].copy(), "node_count": cnt, "order": order[:n].copy(), "max_depth": int(info[0]),
             "bmin": info[1:4].copy(), "bmax": info[4:7].copy()}

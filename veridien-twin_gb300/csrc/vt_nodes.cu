@@ -39,15 +39,10 @@ __device__ __forceinline__ uint32_t node_mat(const Scene& S, uint32_t i) {
   return fu(__ldg(S.params + S.mesh_off + 2u * fu(__ldg(S.verts + 2u * i).w)).w);
 }
 
-// the node a gather ray lands on: the hit triangle's vertex of largest barycentric, if the ray meets its front
-__device__ __forceinline__ uint32_t gather_hit(const Scene& S, uint32_t i, uint32_t j, uint32_t K, uint32_t* tri_out, float3* bb_out) {
-  const float3 p = node_pos(S, i), n = node_nrm(S, i);
-  const float3 dir = gather_dir(i, j, K, n);
-  const Hit h = trace_scene<false>(S, 0u, p + n * EPS_OFF, dir, 0.0f, BIG, 0.5f, 1u, 0u);
-  *tri_out = h.tri;
+// the node that hit h lands on: the hit triangle's vertex of largest barycentric, if the ray meets its front
+__device__ __forceinline__ uint32_t landing_node(const Scene& S, const Hit& h, float3 dir) {
   if (h.tri == MISS) return MISS;
   const float3 bb = f3(1.0f - h.u - h.v, h.u, h.v);
-  *bb_out = bb;
   const float4* r = S.tris + 4u * h.tri;
   const uint32_t v0 = fu(__ldg(r).w), v1 = fu(__ldg(r + 1).w), v2 = fu(__ldg(r + 2).w);
   const float3 nv = xyz(__ldg(S.verts + 2u * v0 + 1u)) * bb.x + xyz(__ldg(S.verts + 2u * v1 + 1u)) * bb.y + xyz(__ldg(S.verts + 2u * v2 + 1u)) * bb.z;
@@ -56,12 +51,35 @@ __device__ __forceinline__ uint32_t gather_hit(const Scene& S, uint32_t i, uint3
   return bb.y >= bb.z ? v1 : v2;
 }
 
-__global__ void gather_build_kernel(const Scene S, uint32_t n_nodes, uint32_t K, uint32_t* __restrict__ gtable) {
-  const size_t total = size_t(n_nodes) * K;
-  for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < total; r += size_t(gridDim.x) * blockDim.x) {
-    uint32_t tri;
-    float3 bb;
-    gtable[r] = gather_hit(S, uint32_t(r / K), uint32_t(r % K), K, &tri, &bb);
+// The gather table's rays (node i, ray j at r = i K + j) on persistent closest-hit lanes (trace_step: one node visit
+// or triangle test per lane step, the same per-ray sequence as trace_scene's static descent, so the same hits); a
+// lane takes the next ray when its own finishes. `head` counts the rays taken.
+__global__ void __launch_bounds__(256, VT_NODE_TRACE_BLOCKS) gather_build_kernel(const Scene S, uint32_t K, uint64_t r0, uint32_t total,
+                                                                                 uint32_t* __restrict__ gtable, uint32_t* head) {
+  __shared__ uint2 stack_sh[SH_DEPTH * 256];
+  LaneStack stk;
+  stk.sh = stack_sh; stk.lane = threadIdx.x; stk.stride = 256;
+  TraceState st;
+  float3 o = f3(0, 0, 0), d = f3(0, 0, 1);
+  uint64_t r = 0;
+  bool active = false, exhausted = false;
+  auto finish = [&]() {
+    gtable[r] = landing_node(S, st.best, d);
+    active = false;
+  };
+  auto start = [&](uint32_t idx) {
+    r = r0 + idx;
+    const uint32_t i = uint32_t(r / K), j = uint32_t(r % K);
+    const float3 p = node_pos(S, i), n = node_nrm(S, i);
+    d = gather_dir(i, j, K, n);
+    o = p + n * EPS_OFF;
+    st.best = Hit{BIG, 0.0f, 0.0f, MISS, MISS};
+    active = trace_phase(S, 0u, o, d, 0.0f, 0.5f, 1u, 0u, st, -1);
+    if (!active) { active = true; finish(); }
+  };
+  while (take_rays(active, exhausted, head, total, 8u, start)) {
+    if (!active) continue;
+    if (trace_step<false>(S, 0.0f, st, stk) != 0) finish();
   }
 }
 
@@ -393,7 +411,19 @@ static int grid_for(size_t work, int threads) {
 
 void launch_gather_build(const Scene& S, uint32_t n_nodes, uint32_t K, uint32_t* gtable, float4* aux, cudaStream_t st) {
   const size_t rays = size_t(n_nodes) * K;
-  gather_build_kernel<<<grid_for(rays, 128), 128, 0, st>>>(S, n_nodes, K, gtable);
+  static std::atomic<int> grid[MAX_DEVICES];
+  const int g = per_device_value(grid, [](int dev) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gather_build_kernel, 256, 0);
+    return device_sms(dev) * std::max(1, per);
+  });
+  // aux's first word counts the rays taken (aux is written by gather_count_kernel afterwards); at most 2^31 rays per
+  // launch
+  uint32_t* head = reinterpret_cast<uint32_t*>(aux);
+  for (size_t r0 = 0; r0 < rays; r0 += size_t(1) << 31) {
+    cudaMemsetAsync(head, 0, 4, st);
+    gather_build_kernel<<<g, 256, 0, st>>>(S, K, r0, uint32_t(std::min(rays - r0, size_t(1) << 31)), gtable, head);
+  }
   gather_count_kernel<<<grid_for(n_nodes, 128), 128, 0, st>>>(n_nodes, K, gtable, aux);
   gather_remap_kernel<<<grid_for(rays, 128), 128, 0, st>>>(S, n_nodes, K, gtable, aux);
 }
