@@ -47,6 +47,17 @@ def test_device_build_matches_oracle_on_random_and_degenerate_meshes():
         _same(build_bvh(P, I, 4, device=0), O.bvh_build(P, I, 4))
 
 
+def test_device_build_at_task_size_boundaries():
+    """Meshes whose root and top ranges sit at the builder's boundaries: one thread (32 slots or fewer), one warp,
+    one block (1024-8191), 4096-slot chunks (8192 and more, one of them partial)."""
+    rng = np.random.default_rng(21)
+    for n in (32, 33, 1023, 1024, 4096, 4097, 8191, 8192, 8193, 12289, 16385):
+        P = rng.normal(size=(3 * n, 3)).astype(np.float32)
+        I = np.arange(3 * n, dtype=np.uint32).reshape(-1, 3)
+        for leaf in (1, 4):
+            _same(build_bvh(P, I, leaf, device=0), O.bvh_build(P, I, leaf))
+
+
 @pytest.mark.parametrize("leaf", [600, 2500])
 def test_device_build_large_leaves(leaf):
     """A leaf size large enough that ranges handled by whole blocks (1024-8191 slots) and by chunks (8192 slots and
