@@ -892,6 +892,11 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
     // fall under tol with a margin of 4 (an inexact correction), never finer than the low precision's floor
     const double inner_goal = std::min(0.1, std::max(inner_tol, 0.25 * q->tol / resid));
     VT_CK(cudaMemcpyAsync(d, r, nr * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    // The sweeps' relative change falls geometrically. Each host check costs a stream synchronisation, about as
+    // much as a sweep at small n, so after two checked sweeps the observed rate predicts how many more reach the
+    // goal; they run back to back and one check follows (then one per sweep, should the prediction fall short).
+    uint32_t batch = 1, in_batch = 0, k_prev = 0;
+    double c_prev = -1.0;
     for (uint32_t k = 0; k < inner_max && sweeps < max_it; k++) {
       if (fp8) {
         vtk::tc_pack_b(vtk::TC_FP8, d, n, R, nullptr, nullptr, Bq, cs, cm, ctx->stream);
@@ -909,11 +914,21 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
       ctx->tim.launches += 3;
       std::swap(d, d2);
       sweeps++;
+      if (++in_batch < batch && k + 1 < inner_max && sweeps < max_it) continue;
       if ((s = read_norms(h)) != VT_OK) return s;
       float gms = 0;
       cudaEventElapsedTime(&gms, ctx->ev2, ctx->ev3);
-      gemm_ms += gms;
-      if (!(h[1] > 0) || std::sqrt(h[0] / h[1]) <= inner_goal) break;
+      gemm_ms += gms * float(in_batch);
+      const double c = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+      if (!(h[1] > 0) || c <= inner_goal) break;
+      batch = 1;
+      if (c_prev > 0.0 && c < c_prev) {
+        const double rate = std::pow(c / c_prev, 1.0 / double(k + 1 - k_prev));
+        if (rate > 0.0 && rate < 0.95) batch = uint32_t(std::min(8.0, std::max(1.0, std::ceil(std::log(inner_goal / c) / std::log(rate)))));
+      }
+      c_prev = c;
+      k_prev = k + 1;
+      in_batch = 0;
     }
     vtk::tc_axpy(B, d, nr, ctx->stream);
   }
