@@ -639,24 +639,34 @@ __device__ __forceinline__ void df_mac(float f, float2 x, float& sh, float& sl) 
   sl = __fsub_rn(lo, __fsub_rn(sh, t));
 }
 
-constexpr uint32_t JT_SPLITS = 16, JT_COLS = 256;
+// 64 row splits, so that a sweep has blocks enough to fill the SMs several times; a thread sums its column's rows in
+// two interleaved float pairs (two independent dependency chains), which meet in FP64
+constexpr uint32_t JT_SPLITS = 64, JT_COLS = 256;
 // partial[split][j] = sum over rows i of the split of F[i][j] (g_i + rho_i lam_i)
 __global__ void __launch_bounds__(JT_COLS) jacobi_t_kernel(const float* __restrict__ F, const double* __restrict__ g, const float* __restrict__ rho,
                                                           const double* __restrict__ lam, uint32_t n, double* __restrict__ part) {
   __shared__ float2 w[JT_COLS];
   const uint32_t j = blockIdx.x * JT_COLS + threadIdx.x;
   const uint32_t rows = (n + JT_SPLITS - 1) / JT_SPLITS, i0 = blockIdx.y * rows, i1 = min(n, i0 + rows);
-  float sh = 0.0f, sl = 0.0f;
+  float sh0 = 0.0f, sl0 = 0.0f, sh1 = 0.0f, sl1 = 0.0f;
   for (uint32_t ib = i0; ib < i1; ib += JT_COLS) {
     const uint32_t ii = ib + threadIdx.x;
     w[threadIdx.x] = ii < i1 ? df_split(g[ii] + double(rho[ii]) * lam[ii]) : make_float2(0.0f, 0.0f);
     __syncthreads();
     const uint32_t m = min(JT_COLS, i1 - ib);
-    if (j < n)
-      for (uint32_t k = 0; k < m; k++) df_mac(F[size_t(ib + k) * n + j], w[k], sh, sl);
+    if (j < n) {
+      const float* Fc = F + size_t(ib) * n + j;
+      uint32_t k = 0;
+      for (; k + 1 < m; k += 2) {
+        const float f0 = Fc[size_t(k) * n], f1 = Fc[size_t(k + 1) * n];
+        df_mac(f0, w[k], sh0, sl0);
+        df_mac(f1, w[k + 1], sh1, sl1);
+      }
+      if (k < m) df_mac(Fc[size_t(k) * n], w[k], sh0, sl0);
+    }
     __syncthreads();
   }
-  if (j < n) part[size_t(blockIdx.y) * n + j] = double(sh) + double(sl);
+  if (j < n) part[size_t(blockIdx.y) * n + j] = (double(sh0) + double(sl0)) + (double(sh1) + double(sl1));
 }
 __global__ void jacobi_t_combine(const double* __restrict__ part, uint32_t n, double* __restrict__ out) {
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -674,21 +684,22 @@ __global__ void __launch_bounds__(256) radiosity64_kernel(const float* __restric
   const uint32_t row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
   if (row >= n) return;
   const float* Fr = F + size_t(row) * n;
-  float sh = 0.0f, sl = 0.0f;
+  // four float pairs, one per component of a float4 (four independent dependency chains), meeting in FP64
+  float sh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, sl[4] = {0.0f, 0.0f, 0.0f, 0.0f};
   if ((n & 3u) == 0u && (reinterpret_cast<uintptr_t>(F) & 15u) == 0u) {
     const float4* F4 = reinterpret_cast<const float4*>(Fr);
     const float4* B4 = reinterpret_cast<const float4*>(Bin);   // two pairs per float4
     for (uint32_t j = lane; j < (n >> 2); j += 32) {
       const float4 f = __ldg(F4 + j), b01 = __ldg(B4 + 2 * j), b23 = __ldg(B4 + 2 * j + 1);
-      df_mac(f.x, make_float2(b01.x, b01.y), sh, sl);
-      df_mac(f.y, make_float2(b01.z, b01.w), sh, sl);
-      df_mac(f.z, make_float2(b23.x, b23.y), sh, sl);
-      df_mac(f.w, make_float2(b23.z, b23.w), sh, sl);
+      df_mac(f.x, make_float2(b01.x, b01.y), sh[0], sl[0]);
+      df_mac(f.y, make_float2(b01.z, b01.w), sh[1], sl[1]);
+      df_mac(f.z, make_float2(b23.x, b23.y), sh[2], sl[2]);
+      df_mac(f.w, make_float2(b23.z, b23.w), sh[3], sl[3]);
     }
   } else {
-    for (uint32_t j = lane; j < n; j += 32) df_mac(__ldg(Fr + j), Bin[j], sh, sl);
+    for (uint32_t j = lane; j < n; j += 32) df_mac(__ldg(Fr + j), Bin[j], sh[j & 3u], sl[j & 3u]);
   }
-  double a = double(sh) + double(sl);
+  double a = ((double(sh[0]) + double(sl[0])) + (double(sh[1]) + double(sl[1]))) + ((double(sh[2]) + double(sl[2])) + (double(sh[3]) + double(sl[3])));
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if (lane) return;
   if (H) H[row] = float(a);
