@@ -877,6 +877,7 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
     return VT_OK;
   };
   VT_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  double last_rate = 0.0;   // the sweeps' rate of change in the previous correction (the same matrix)
   for (;;) {
     // accurate residual of the current iterate
     vtk::tc_pack_b(vtk::TC_BF16X3, B, n, R, Bhi, Blo, nullptr, nullptr, nullptr, ctx->stream);
@@ -893,8 +894,9 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
     const double inner_goal = std::min(0.1, std::max(inner_tol, 0.25 * q->tol / resid));
     VT_CK(cudaMemcpyAsync(d, r, nr * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     // The sweeps' relative change falls geometrically. Each host check costs a stream synchronisation, about as
-    // much as a sweep at small n, so after two checked sweeps the observed rate predicts how many more reach the
-    // goal; they run back to back and one check follows (then one per sweep, should the prediction fall short).
+    // much as a sweep at small n, so the observed rate (from two checked sweeps, or the previous correction's)
+    // predicts how many more sweeps reach the goal; they run back to back and one check follows (then one per
+    // sweep, should the prediction fall short).
     uint32_t batch = 1, in_batch = 0, k_prev = 0;
     double c_prev = -1.0;
     for (uint32_t k = 0; k < inner_max && sweeps < max_it; k++) {
@@ -922,10 +924,11 @@ static vt_status tc_solve(vt_ctx* ctx, vt_solve_req* q) {
       const double c = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
       if (!(h[1] > 0) || c <= inner_goal) break;
       batch = 1;
-      if (c_prev > 0.0 && c < c_prev) {
-        const double rate = std::pow(c / c_prev, 1.0 / double(k + 1 - k_prev));
-        if (rate > 0.0 && rate < 0.95) batch = uint32_t(std::min(8.0, std::max(1.0, std::ceil(std::log(inner_goal / c) / std::log(rate)))));
-      }
+      double rate = 0.0;
+      if (c_prev > 0.0 && c < c_prev) rate = std::pow(c / c_prev, 1.0 / double(k + 1 - k_prev));
+      else if (c_prev < 0.0) rate = last_rate;   // a later correction's first check: the previous correction's rate
+      if (c_prev > 0.0 && rate > 0.0) last_rate = rate;
+      if (rate > 0.0 && rate < 0.95) batch = uint32_t(std::min(8.0, std::max(1.0, std::ceil(std::log(inner_goal / c) / std::log(rate)))));
       c_prev = c;
       k_prev = k + 1;
       in_batch = 0;
