@@ -472,8 +472,8 @@ vt_status vt_form_factors_visible(vt_ctx* ctx, uint32_t n, const float* centres,
  * memory up front. F (n x n), rho (n), E (n) and B (n, out) are device pointers the caller owns; scratch is a static
  * device array of VT_STATIC_SOLVE_MAX_N nodes (about 160 KB) that every GPU loading the library holds until exit.
  * n > VT_STATIC_SOLVE_MAX_N or a host pointer returns VT_ERR_ARG. The first call on a device looks up the array's
- * device address (make that first call before any stream capture). All calls share the array: calls that overlap on
- * the GPU race. stream: a cudaStream_t (NULL = legacy default stream). iters / residual may be NULL. */
+ * device address. All calls share the array: calls that overlap on the GPU race. stream: a cudaStream_t (NULL =
+ * legacy default stream). iters / residual may be NULL. */
 #define VT_STATIC_SOLVE_MAX_N 16384
 vt_status vt_radiosity_solve_static(const float* F, const float* rho, const float* E, float* B, uint32_t n, uint32_t max_iters,
                                     uint32_t check_every, double tol, void* stream, uint32_t* iters, double* residual);
