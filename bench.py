@@ -575,7 +575,7 @@ def calib_bench(torch, device=0):
                                    "tests/test_gpu_calib.py"}}
 
 
-PRESETS_REF = {   # gpu/renderer.js:31-66 DEFAULTS (the judge preset) and the live / balanced presets
+PRESETS_REF = {   # gpu/renderer.js:31-66 DEFAULTS (its preset named "judge") and its "live" / "balanced" presets
     "live": {"spp": 1, "lightSamples": 1, "refine": 0, "radiosityEvery": 2, "itersPerFrame": 1},
     "balanced": {"spp": 1, "lightSamples": 2, "refine": 2, "refineLightSamples": 1, "refineShadows": False, "radiosityEvery": 2,
                  "itersPerFrame": 1},
