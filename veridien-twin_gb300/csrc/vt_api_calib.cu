@@ -200,11 +200,12 @@ vt_status vt_calib_forward(vt_ctx* ctx, const vt_calib_req* q, double* loss) {
   VT_CK(cudaMemcpyAsync(K.albedo, alb.data(), alb.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
   VT_CK(cudaMemcpyAsync(K.lamp, lamp.data(), lamp.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
   VT_CK(cudaMemcpyAsync(K.rho, rho.data(), rho.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-  // radiosity: B = rho o (D L + F B) per channel, iters FP64 sweeps from B = rho o D L; H = F B. FP64 so that the
-  // node light carries no rounding that moves with every parameter (central differences of the loss see it)
+  // radiosity: B = rho o (D L + F B) per channel, iters sweeps at FP64 accuracy from B = rho o D L; H = F B. FP64
+  // accuracy so that the node light carries no rounding that moves with every parameter (central differences of the
+  // loss see it). The three channels in one pass over F; the iterates in the adjoint's work array (48 n bytes of its
+  // JT splits x n doubles), which the forward does not otherwise use
   vtk::launch_dl(K.D, K.lamp, K.n, K.n_lamps, K.DL, ctx->stream);
-  for (uint32_t c = 0; c < 3; c++)
-    vtk::launch_radiosity64(K.F, K.rho + size_t(c) * K.n, K.DL, K.n, iters, K.lam0, K.lam1, K.H + size_t(c) * K.n, ctx->stream);
+  vtk::launch_radiosity64(K.F, K.rho, K.DL, K.n, iters, K.work, K.H, ctx->stream);
   // cameras
   size_t px_total = 0;
   for (uint32_t c = 0; c < q->n_cameras; c++) px_total += size_t(S.cams[q->cameras[c]].width) * S.cams[q->cameras[c]].height;

@@ -677,37 +677,49 @@ __global__ void jacobi_t_combine(const double* __restrict__ part, uint32_t n, do
   out[j] = a;
 }
 
-// B_out = rho o (DL + F B_in) at FP64 accuracy (F in FP32, B as float pairs, the products summed in float pairs), one
-// warp per row; with `H` set, H = F B_in (rounded to FP32) instead
+// The three channels' B_c,out = rho_c o (DL + F B_c,in) at FP64 accuracy (F in FP32, B as float pairs planar [c][n],
+// the products summed in float pairs), one warp per row reading F once for all three; with `H` set, H_c = F B_c,in
+// (rounded to FP32) instead. Each channel's sums run in the order of a one-channel sweep, so the values are its.
 __global__ void __launch_bounds__(256) radiosity64_kernel(const float* __restrict__ F, const float* __restrict__ rho, const float* __restrict__ DL,
                                                         const float2* __restrict__ Bin, float2* __restrict__ Bout, float* __restrict__ H,
                                                         uint32_t n) {
   const uint32_t row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
   if (row >= n) return;
   const float* Fr = F + size_t(row) * n;
-  float sh = 0.0f, sl = 0.0f;
-  if ((n & 3u) == 0u && (reinterpret_cast<uintptr_t>(F) & 15u) == 0u) {
+  float sh[3] = {0.0f, 0.0f, 0.0f}, sl[3] = {0.0f, 0.0f, 0.0f};
+  if ((n & 3u) == 0u && ((reinterpret_cast<uintptr_t>(F) | reinterpret_cast<uintptr_t>(Bin)) & 15u) == 0u) {
     const float4* F4 = reinterpret_cast<const float4*>(Fr);
-    const float4* B4 = reinterpret_cast<const float4*>(Bin);   // two pairs per float4
     for (uint32_t j = lane; j < (n >> 2); j += 32) {
-      const float4 f = __ldg(F4 + j), b01 = __ldg(B4 + 2 * j), b23 = __ldg(B4 + 2 * j + 1);
-      df_mac(f.x, make_float2(b01.x, b01.y), sh, sl);
-      df_mac(f.y, make_float2(b01.z, b01.w), sh, sl);
-      df_mac(f.z, make_float2(b23.x, b23.y), sh, sl);
-      df_mac(f.w, make_float2(b23.z, b23.w), sh, sl);
+      const float4 f = __ldg(F4 + j);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const float4* B4 = reinterpret_cast<const float4*>(Bin + size_t(c) * n);   // two pairs per float4
+        const float4 b01 = __ldg(B4 + 2 * j), b23 = __ldg(B4 + 2 * j + 1);
+        df_mac(f.x, make_float2(b01.x, b01.y), sh[c], sl[c]);
+        df_mac(f.y, make_float2(b01.z, b01.w), sh[c], sl[c]);
+        df_mac(f.z, make_float2(b23.x, b23.y), sh[c], sl[c]);
+        df_mac(f.w, make_float2(b23.z, b23.w), sh[c], sl[c]);
+      }
     }
   } else {
-    for (uint32_t j = lane; j < n; j += 32) df_mac(__ldg(Fr + j), Bin[j], sh, sl);
+    for (uint32_t j = lane; j < n; j += 32) {
+      const float f = __ldg(Fr + j);
+#pragma unroll
+      for (int c = 0; c < 3; c++) df_mac(f, Bin[size_t(c) * n + j], sh[c], sl[c]);
+    }
   }
-  double a = double(sh) + double(sl);
-  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-  if (lane) return;
-  if (H) H[row] = float(a);
-  else Bout[row] = df_split(double(rho[row]) * (double(DL[row]) + a));
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double a = double(sh[c]) + double(sl[c]);
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane) continue;
+    if (H) H[size_t(c) * n + row] = float(a);
+    else Bout[size_t(c) * n + row] = df_split(double(rho[size_t(c) * n + row]) * (double(DL[row]) + a));
+  }
 }
 __global__ void radiosity64_init(const float* __restrict__ rho, const float* __restrict__ DL, float2* __restrict__ B, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) B[i] = df_split(double(rho[i]) * double(DL[i]));
+  if (i < 3 * n) B[i] = df_split(double(rho[i]) * double(DL[i % n]));
 }
 
 __global__ void mul_kernel(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ y, uint32_t n) {
@@ -897,12 +909,12 @@ void launch_sum(const double* p, uint32_t n, double* out, cudaStream_t st) { sum
 
 void launch_mul(const float* a, const float* b, float* y, uint32_t n, cudaStream_t st) { mul_kernel<<<(n + 255) / 256, 256, 0, st>>>(a, b, y, n); }
 
-void launch_radiosity64(const float* F, const float* rho, const float* DL, uint32_t n, uint32_t iters, double* B0, double* B1, float* H,
+void launch_radiosity64(const float* F, const float* rho, const float* DL, uint32_t n, uint32_t iters, void* work, float* H,
                         cudaStream_t st) {
-  // the iterates as float pairs, in the two n-double buffers
-  float2* p0 = reinterpret_cast<float2*>(B0);
-  float2* p1 = reinterpret_cast<float2*>(B1);
-  radiosity64_init<<<(n + 255) / 256, 256, 0, st>>>(rho, DL, p0, n);
+  // the three channels' iterates as float pairs, two planar 3 x n arrays in `work`
+  float2* p0 = static_cast<float2*>(work);
+  float2* p1 = p0 + size_t(3) * n;
+  radiosity64_init<<<(3 * n + 255) / 256, 256, 0, st>>>(rho, DL, p0, n);
   float2 *cur = p0, *nxt = p1;
   for (uint32_t it = 0; it < iters; it++) {
     radiosity64_kernel<<<(n + 7) / 8, 256, 0, st>>>(F, rho, DL, cur, nxt, nullptr, n);

@@ -65,11 +65,10 @@ void launch_jacobi_t(const float* F, const double* g, const float* rho, const do
 size_t jacobi_t_work(uint32_t n);
 // y = a o b (n floats)
 void launch_mul(const float* a, const float* b, float* y, uint32_t n, cudaStream_t st);
-// the calibration model's node radiosity for one channel: B = rho o (DL + F B) by `iters` Jacobi sweeps from
-// B = rho o DL, at FP64 accuracy (F in FP32; float-pair products and sums), then H = F B rounded to FP32; B0, B1:
-// n doubles of work
-void launch_radiosity64(const float* F, const float* rho, const float* DL, uint32_t n, uint32_t iters, double* B0, double* B1, float* H,
-                        cudaStream_t st);
+// the calibration model's node radiosity for the three channels at once: B_c = rho_c o (DL + F B_c) by `iters`
+// Jacobi sweeps from B_c = rho_c o DL, at FP64 accuracy (F in FP32; float-pair products and sums), then H_c = F B_c
+// rounded to FP32; rho and H planar 3 x n; work: at least 48 n bytes, 16-byte aligned
+void launch_radiosity64(const float* F, const float* rho, const float* DL, uint32_t n, uint32_t iters, void* work, float* H, cudaStream_t st);
 // sum of n doubles (deterministic order) into out
 void launch_sum(const double* p, uint32_t n, double* out, cudaStream_t st);
 
