@@ -463,7 +463,7 @@ __device__ __forceinline__ void path_tangent(const CalibDev& C, const CalPath& P
 
 // the derivative of the loss in the camera's intrinsics from one sub-sample: G = g . dL / d d0 (FP64), chained
 // through d d0 / d K at the sub-sample's image position
-__device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_t id, uint32_t i, const float3* dL, double3 g, double* kacc) {
+__device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_t id, uint32_t i, const float3* dL, double3 g, float* kacc) {
   uint32_t x, y;
   if (!pixel_xy(cp, id, x, y)) return;
   // the term in FP32, its accumulation in FP64
@@ -476,7 +476,7 @@ __device__ __forceinline__ void add_intrinsics_grad(const CamParams& cp, uint32_
   float J[3][8];
   kb4_ray_jacobian(cp.lens, uv.x, uv.y, f3(cp.rx[0], cp.rx[1], cp.rx[2]), f3(cp.ry[0], cp.ry[1], cp.ry[2]), f3(cp.rz[0], cp.rz[1], cp.rz[2]), J);
 #pragma unroll
-  for (int k = 0; k < 8; k++) kacc[k] += double(G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k]);
+  for (int k = 0; k < 8; k++) kacc[k] += G[0] * J[0][k] + G[1] * J[1][k] + G[2] * J[2][k];
 }
 
 // per pixel over the records of sub-samples [i0, i1): backward 0 adds their values to the pixel's running sum (kept in
@@ -496,9 +496,10 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
     __syncthreads();
   }
   double loss = 0.0;
-  // the thread's intrinsics terms, summed in registers (one warp sum and 8 shared atomics per warp at the end: all
-  // lanes add to the same 8 words, where per-path atomics would contend)
-  double kacc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  // the thread's intrinsics terms (one pixel's sub-samples of the launch) summed in FP32 registers, then one FP64 warp
+  // sum and 8 shared atomics per warp at the end: all lanes add to the same 8 words, where per-path atomics would
+  // contend, and FP64 issues at a small fraction of FP32 on this part
+  float kacc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
   const float sc = cp.scale / float(cp.spp);
   // the block's threads take pixels base + threadIdx.x together, so that a warp's lanes stay together for the
   // per-material warp sums of the backward
@@ -552,7 +553,7 @@ __global__ void __launch_bounds__(CT) calib_records_kernel(const CamParams cp, c
     if (backward == 2) {
 #pragma unroll
       for (int k = 0; k < 8; k++) {
-        double v = kacc[k];
+        double v = double(kacc[k]);
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if ((threadIdx.x & 31u) == 0u && v != 0.0) atomicAdd(sh_k + k, v);
       }
